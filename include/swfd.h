@@ -1,0 +1,180 @@
+/*
+ * swfd.h -- C ABI of the GB300-native sweeping positivity-preserving
+ * FD-WENO Euler time step.
+ *
+ * The reference (dcgriffi/Sweeping_FD_WENO) has no library interface: each
+ * example is one Fortran PROGRAM whose internal procedures are called by host
+ * association.  Every entry point below replaces one of those procedures (or
+ * a group of them) and names it, as path:line inside the reference project.
+ * A Fortran host binds them with iso_c_binding.
+ *
+ * Conventions
+ *  - Every call returns swfd_status: 0 on success, a negative value on error.
+ *    Nothing in the library calls exit(); the reference's `stop` paths map to
+ *    status codes and the host decides whether to stop.
+ *  - State arrays crossing the ABI use the reference's own layout
+ *    u(ncomp, -2:nx+3, -2:ny+3), Fortran column-major (component fastest,
+ *    then x index, then y index), double precision, ghost layers included.
+ *    1D problems use u(3, -2:nx+3).
+ *  - The handle owns all device memory.  Host arrays are only borrowed for the
+ *    duration of the call that receives them.
+ *  - One handle per host thread.  Each handle owns one CUDA stream.
+ */
+#ifndef SWFD_H
+#define SWFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWFD_ABI_VERSION 1
+
+typedef int32_t swfd_status;
+enum {
+  SWFD_OK = 0,
+  SWFD_ERR_INVALID = -1,        /* bad argument or configuration */
+  SWFD_ERR_CUDA = -2,           /* a CUDA runtime call failed */
+  SWFD_ERR_SWEEP_NOCONV = -3,   /* sweep hit swp_num without P,rho > eps
+                                   (ex4_sedov_2d/main.f90:1747-1752 `stop`) */
+  SWFD_ERR_PUBAR_NONPOS = -4,   /* P(u_bar) <= 0 before the pressure sweep
+                                   (ex4_sedov_2d/main.f90:1447-1454 `stop`) */
+  SWFD_ERR_NONFINITE = -5,      /* alpha or dt is not finite */
+  SWFD_ERR_OOM = -6,            /* device allocation refused */
+  SWFD_ERR_TIMEOUT = -7,        /* a bounded device-side wait expired */
+  SWFD_ERR_UNSUPPORTED = -8,    /* option recognised but not implemented */
+  SWFD_ERR_MAX_STEPS = -9       /* run_to stopped at its step limit */
+};
+
+/* Problem = one reference example, with all of its per-example switches
+ * (operation order, epsilons, comparison operators, boundary conditions). */
+enum {
+  SWFD_PROBLEM_SEDOV_1D = 2,   /* ex2_sedov_1d/main.f90 */
+  SWFD_PROBLEM_VORTEX_2D = 3,  /* ex3_vortex_accuracy_2d/main.f90 */
+  SWFD_PROBLEM_SEDOV_2D = 4,   /* ex4_sedov_2d/main.f90 on one 1x1 block */
+  SWFD_PROBLEM_JET_2D = 5      /* ex5_mach2000_jet/main.f90 */
+};
+
+/* How the reference's double-kind literals (1d-6, 13d0/12d0, 0.75d0, ...)
+ * are evaluated.  The reference Makefiles build with -fdefault-real-8 only,
+ * under which gfortran promotes those literals (and the subexpressions that
+ * contain them) to REAL(16).  SWFD_LITERALS_DOUBLE evaluates everything in
+ * binary64 (the -fdefault-double-8 build). */
+enum { SWFD_LITERALS_DOUBLE = 0, SWFD_LITERALS_QUAD = 1 };
+
+/* Arithmetic of the WENO flux and the RK update.  Pressure recovery, the
+ * positivity test, the sweeps and the conservation sums are always FP64. */
+enum { SWFD_PRECISION_FP64 = 0, SWFD_PRECISION_FP32_BULK = 1 };
+
+/* u_bar of the pressure sweep: the reference's sequential weighted sum
+ * (ex3_vortex_accuracy_2d/main.f90:913-920), or a deterministic tree sum. */
+enum { SWFD_UBAR_SEQUENTIAL = 0, SWFD_UBAR_TREE = 1 };
+
+typedef struct swfd_config {
+  int32_t abi_version;   /* must be SWFD_ABI_VERSION */
+  int32_t problem;       /* SWFD_PROBLEM_* */
+  int32_t nx, ny;        /* interior cells; ny is ignored in 1D */
+  int32_t use_limiter;   /* 2 = sweeping (reference default), 0 = none;
+                            1 (Zhang-Shu flux limiter) -> SWFD_ERR_UNSUPPORTED */
+  int32_t swp_num;       /* max forward/backward sweep pairs per RK stage */
+  int32_t literals;      /* SWFD_LITERALS_* */
+  int32_t precision;     /* SWFD_PRECISION_* */
+  int32_t ubar_mode;     /* SWFD_UBAR_* */
+  int32_t device;        /* CUDA device ordinal */
+  double cfl;            /* CFL number of the problem's dt rule */
+  double time_terminal;  /* final time T */
+  double gamma;          /* ratio of specific heats */
+  double e_background;   /* point-energy problems: background total energy */
+  double e_blast;        /* point-energy problems: blast energy numerator
+                            (1D: E = e_blast/dx, 2D: E = e_blast/(dx*dy)) */
+  int32_t reserved[8];   /* zero */
+} swfd_config;
+
+/* Sweep statistics exactly as the reference counts them
+ * (ex3_vortex_accuracy_2d/main.f90:815-840; counters :14, :24-31). */
+typedef struct swfd_sweep_stats {
+  int64_t sweep_count;      /* sweep_lim invocations */
+  int64_t total_sweep;      /* sum of sweep_track(1:sweep_count) */
+  int64_t max_sweep;        /* maxval(sweep_track(1:sweep_count)) */
+  int64_t total_neg;        /* negative-pair nodal adjustments */
+  int64_t max_neg;
+  int64_t total_pos;        /* positive-neighbour nodal adjustments */
+  int64_t max_pos;
+  int64_t den_count;        /* density sweeps performed */
+  int64_t pre_count;        /* forward/backward sweep pairs performed */
+  int64_t sweep_fail_count; /* sweeps that hit swp_num ("SWEEP FAIL") */
+} swfd_sweep_stats;
+
+typedef struct swfd_handle swfd_handle;
+
+/* Fill cfg with the reference example's compile-time PARAMETERs
+ * (ex2_sedov_1d/main.f90:4-7, ex3_vortex_accuracy_2d/main.f90:5-7,
+ *  ex4_sedov_2d/main.f90:15-20,50, ex5_mach2000_jet/main.f90:4-6). */
+swfd_status swfd_config_default(swfd_config* cfg, int32_t problem);
+
+/* Allocate device state for one problem instance.  Replaces the module-level
+ * arrays of each PROGRAM (ex3_vortex_accuracy_2d/main.f90:8-37) and
+ * sweeping_order (:1211-1270). */
+swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out);
+swfd_status swfd_destroy(swfd_handle* h);
+
+/* Initial data + bc: initdata (ex3_vortex_accuracy_2d/main.f90:671-697,
+ * ex2_sedov_1d/main.f90:405-428, ex4_sedov_2d/main.f90:1121-1189,
+ * ex5_mach2000_jet/main.f90:744-768).  Sets time to 0, clears statistics. */
+swfd_status swfd_init_problem(swfd_handle* h);
+
+/* Copy a host state u(ncomp,-2:nx+3,-2:ny+3) in / out. */
+swfd_status swfd_upload_state(swfd_handle* h, const double* u);
+swfd_status swfd_download_state(swfd_handle* h, double* u);
+
+/* wenofd + scheme (ex3_vortex_accuracy_2d/main.f90:115-547): alpha of the
+ * current state, then RHS(ncomp,-2:nx+3,-2:ny+3) (zero in the ghosts). */
+swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs);
+
+/* One SSP-RK3 step: rk (ex3_vortex_accuracy_2d/main.f90:564-632) followed by
+ * `time = time + dt` (:53).  dt_out may be NULL. */
+swfd_status swfd_step(swfd_handle* h, double* dt_out);
+
+/* The time loop DO WHILE (time <= time_terminal - 1d-10)
+ * (ex3_vortex_accuracy_2d/main.f90:51-56), bounded by max_steps (<= 0: none).
+ * nsteps_out may be NULL. */
+swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out);
+
+/* sweep_lim on the current state, as called after an RK stage whose
+ * checkpositivity flagged a cell (ex3_vortex_accuracy_2d/main.f90:888-1137). */
+swfd_status swfd_sweep(swfd_handle* h);
+
+/* checkpositivity (ex3_vortex_accuracy_2d/main.f90:634-651): *postag = 1 if
+ * an interior cell fails the problem's positivity test. */
+swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag);
+
+/* findalpha (ex3_vortex_accuracy_2d/main.f90:549-562) of the current state. */
+swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax);
+
+swfd_status swfd_get_time(swfd_handle* h, double* t);
+swfd_status swfd_set_time(swfd_handle* h, double t);
+
+/* Statistics printed by output (ex3_vortex_accuracy_2d/main.f90:815-840). */
+swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s);
+/* Per-sweep tracks sweep_track/neg_track/pos_track(1:sweep_count); any of
+ * the output pointers may be NULL; writes min(cap, sweep_count) entries. */
+swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg,
+                                  int32_t* pos, int64_t cap, int64_t* count);
+
+/* The scalar WENO5 reconstructions of MODULE weno5, weno_left/weno_right
+ * (ex3_vortex_accuracy_2d/weno5.f90:86-146), evaluated on the GPU for n
+ * stencils average(-2:2) stored contiguously (5 doubles each). */
+swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
+                             int32_t literals, int32_t device, double* uleft,
+                             double* uright);
+
+/* Last error message of the handle (or of the process when h is NULL). */
+swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len);
+const char* swfd_status_string(swfd_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWFD_H */

@@ -1,0 +1,1207 @@
+/*
+ * swfd_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, single-threaded restatement of the reference's sweeping
+ * FD-WENO Euler time step (dcgriffi/Sweeping_FD_WENO, Fortran).  It is the
+ * parity oracle for the CUDA library and the timed CPU baseline.  Only the
+ * tests, __graft_entry__.smoke() and bench.py (CPU-baseline leg) may load
+ * it; the product never calls, links or falls back to it.
+ *
+ * Parity pinning: the reference ships no tests and no golden outputs, and no
+ * Fortran compiler exists in this container, so the reference cannot be run
+ * here.  The restatement is pinned by known-answer properties of the
+ * reference's own algorithm (5th-order vortex convergence,
+ * ex3_vortex_accuracy_2d/main.f90:725-777; exact conservation of the sweeps;
+ * positivity after a converged sweep; WENO5 reproduction of quadratics),
+ * checked in tests/test_oracle.py.
+ *
+ * Faithfulness rules followed throughout:
+ *  - operation order is the Fortran left-to-right order of each statement;
+ *    x**2 is x*x; no reassociation, no reciprocal-multiply for a division;
+ *    compiled with -ffp-contract=off so no FMA is formed;
+ *  - gfortran -fdefault-real-8 (the reference Makefiles, e.g.
+ *    ex3_vortex_accuracy_2d/Makefile:15) promotes double-kind literals
+ *    (1d-6, 13d0/12d0, 0.75d0, 1d-15 ...) to REAL(16); every subexpression
+ *    that contains one is evaluated in _Float128 when cfg.literals ==
+ *    SWFD_LITERALS_QUAD and rounded to double once on assignment, exactly as
+ *    a mixed REAL(8)/REAL(16) Fortran expression is;
+ *  - MIN/MAX are fmin/fmax.
+ *
+ * Memory layout: u(ncomp, -2:nx+3, -2:ny+3) in Fortran column-major order,
+ * the layout of the reference arrays (ex3_vortex_accuracy_2d/main.f90:8).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/swfd.h"
+
+typedef _Float128 Q;
+
+#define MAXC 4
+
+typedef struct oracle {
+  swfd_config cfg;
+  int ndim, nc, nx, ny, LI, LJ;
+  int quad;
+  double gamma, gamma1, eps, eps2, weno_eps, dx, dy;
+  Q weno_eps_q;
+  /* per-example switches (the variant matrix of the reference) */
+  int problem;
+  double *u, *u0, *rhs, *fp, *fn, *gp, *gn, *fpf, *fnf, *gpf, *gnf;
+  double *x, *y;
+  double *wk_w, *wk_vx, *wk_vy, *wk_h; /* per-line Roe prep, 0:max(nx,ny)+2 */
+  double *rho_t;                        /* sweep scratch */
+  int *sI_i, *sI_j, *sII_i, *sII_j;     /* snake orderings, 1-based cells */
+  double weight;                        /* all weights are equal */
+  double alphamax, dt, time;
+  int postag;
+  /* statistics (ex3_vortex_accuracy_2d/main.f90:14,24-31) */
+  int64_t sweep_count, den_count, pre_count, fail_count;
+  int64_t t_pos_count, t_neg_count;
+  int32_t *sweep_track, *neg_track, *pos_track;
+  int64_t track_cap;
+  int status;
+} oracle;
+
+/* ------------------------------------------------------------------ */
+/* indexing                                                            */
+/* ------------------------------------------------------------------ */
+static inline size_t IX(const oracle* o, int c, int i, int j) {
+  return (size_t)c + (size_t)o->nc * ((size_t)(i + 2) + (size_t)o->LI * (size_t)(j + 2));
+}
+#define U(a, c, i, j) ((a)[IX(o, (c), (i), (j))])
+
+static inline double sq(double a) { return a * a; }
+static inline Q sqq(Q a) { return a * a; }
+
+/* ------------------------------------------------------------------ */
+/* WENO5 (ex3_vortex_accuracy_2d/weno5.f90:3-15, 86-146)               */
+/* ------------------------------------------------------------------ */
+/* c(-1:2,0:2), reshaped column-major from weno5.f90:3-15 */
+static const double WC[4][3] = {
+    /* c(-1,:) */ {1.83333333333333333333333333333333, -1.16666666666666666666666666666667,
+                   0.333333333333333333333333333333333},
+    /* c( 0,:) */ {0.333333333333333333333333333333333, 0.833333333333333333333333333333333,
+                   -0.166666666666666666666666666666667},
+    /* c( 1,:) */ {-0.166666666666666666666666666666667, 0.833333333333333333333333333333333,
+                   0.333333333333333333333333333333333},
+    /* c( 2,:) */ {0.333333333333333333333333333333333, -1.16666666666666666666666666666667,
+                   1.83333333333333333333333333333333}};
+#define CW(r, i) WC[(r) + 1][(i)]
+
+/* smoothness indicators beta(1:3), weno5.f90:100-102 (a[0..4] = average(-2..2)) */
+static void weno_beta(int quad, const double* a, double* b) {
+  const double am2 = a[0], am1 = a[1], a0 = a[2], ap1 = a[3], ap2 = a[4];
+  if (quad) {
+    const Q c1312 = (Q)13 / (Q)12, two = 2, three = 3, four = 4, qrt = 0.25;
+    Q s, t;
+    s = (Q)a0 - two * (Q)ap1 + (Q)ap2;
+    t = three * (Q)a0 - four * (Q)ap1 + (Q)ap2;
+    b[0] = (double)(c1312 * sqq(s) + qrt * sqq(t));
+    s = (Q)am1 - two * (Q)a0 + (Q)ap1;
+    /* (average(-1)-average(1))**2 has only REAL(8) operands */
+    b[1] = (double)(c1312 * sqq(s) + qrt * (Q)sq(am1 - ap1));
+    s = (Q)am2 - two * (Q)am1 + (Q)a0;
+    t = (Q)am2 - four * (Q)am1 + three * (Q)a0;
+    b[2] = (double)(c1312 * sqq(s) + qrt * sqq(t));
+  } else {
+    const double c1312 = 13.0 / 12.0;
+    b[0] = c1312 * sq(a0 - 2.0 * ap1 + ap2) + 0.25 * sq(3.0 * a0 - 4.0 * ap1 + ap2);
+    b[1] = c1312 * sq(am1 - 2.0 * a0 + ap1) + 0.25 * sq(am1 - ap1);
+    b[2] = c1312 * sq(am2 - 2.0 * am1 + a0) + 0.25 * sq(am2 - 4.0 * am1 + 3.0 * a0);
+  }
+}
+
+/* alpha = lin/(eps+beta)**2, weno5.f90:104-106,138-140 */
+static double weno_alpha(const oracle* o, double lin, double beta) {
+  if (o->quad) {
+    Q s = o->weno_eps_q + (Q)beta;
+    return (double)((Q)lin / (s * s));
+  }
+  double s = o->weno_eps + beta;
+  return lin / (s * s);
+}
+
+/* weno_left (weno5.f90:86-113) */
+double oracle_weno_left_impl(const oracle* o, const double* a) {
+  double up[3], beta[3], al[3], ww[3];
+  for (int k = 1; k <= 3; ++k) {
+    int is = k - 3;
+    double s = 0.0;
+    for (int i = 0; i <= 2; ++i) s = s + CW(-is - 1, i) * a[is + i + 2];
+    up[k - 1] = s;
+  }
+  weno_beta(o->quad, a, beta);
+  al[0] = weno_alpha(o, 0.1, beta[0]);
+  al[1] = weno_alpha(o, 0.6, beta[1]);
+  al[2] = weno_alpha(o, 0.3, beta[2]);
+  ww[0] = al[0] / (al[0] + al[1] + al[2]);
+  ww[1] = al[1] / (al[0] + al[1] + al[2]);
+  ww[2] = al[2] / (al[0] + al[1] + al[2]);
+  return ww[0] * up[2] + ww[1] * up[1] + ww[2] * up[0];
+}
+
+/* weno_right (weno5.f90:120-146) */
+double oracle_weno_right_impl(const oracle* o, const double* a) {
+  double um[3], beta[3], al[3], ww[3];
+  for (int k = 1; k <= 3; ++k) {
+    int is = k - 3;
+    double s = 0.0;
+    for (int i = 0; i <= 2; ++i) s = s + CW(-is, i) * a[is + i + 2];
+    um[k - 1] = s;
+  }
+  weno_beta(o->quad, a, beta);
+  al[0] = weno_alpha(o, 0.3, beta[0]);
+  al[1] = weno_alpha(o, 0.6, beta[1]);
+  al[2] = weno_alpha(o, 0.1, beta[2]);
+  ww[0] = al[0] / (al[0] + al[1] + al[2]);
+  ww[1] = al[1] / (al[0] + al[1] + al[2]);
+  ww[2] = al[2] / (al[0] + al[1] + al[2]);
+  return ww[0] * um[2] + ww[1] * um[1] + ww[2] * um[0];
+}
+
+/* ------------------------------------------------------------------ */
+/* literal-sensitive comparisons and RK combinations                    */
+/* ------------------------------------------------------------------ */
+/* rho < 1d-8 with a double-kind literal (ex3_vortex_accuracy_2d/main.f90:75) */
+static int lt_lit_1em8(const oracle* o, double rho) {
+  if (o->quad) return (Q)rho < (Q)1e-8f128;
+  return rho < 1e-8;
+}
+static int gt_lit_1em8(const oracle* o, double rho) {
+  if (o->quad) return (Q)rho > (Q)1e-8f128;
+  return rho > 1e-8;
+}
+static int le_lit_1em8(const oracle* o, double rho) {
+  if (o->quad) return (Q)rho <= (Q)1e-8f128;
+  return rho <= 1e-8;
+}
+/* u = 0.75d0*u0 + 0.25d0*(u + dt*RHS)  (ex3_vortex_accuracy_2d/main.f90:604) */
+static inline double rk2(const oracle* o, double u0, double v) {
+  if (o->quad) return (double)((Q)0.75 * (Q)u0 + (Q)0.25 * (Q)v);
+  return 0.75 * u0 + 0.25 * v;
+}
+/* u = (u0 + 2d0*(u + dt*RHS))/3d0  (ex3_vortex_accuracy_2d/main.f90:621) */
+static inline double rk3(const oracle* o, double u0, double v) {
+  if (o->quad) return (double)(((Q)u0 + (Q)2 * (Q)v) / (Q)3);
+  return (u0 + 2.0 * v) / 3.0;
+}
+
+/* ------------------------------------------------------------------ */
+/* 2D: fluxes (ex3_vortex_accuracy_2d/main.f90:61-113,                  */
+/*             ex4_sedov_2d/main.f90:125-177)                           */
+/* ------------------------------------------------------------------ */
+static void fflux2d(const oracle* o, const double* a, double* f, int gdir) {
+  double rho = a[0], mx = a[1], my = a[2], e = a[3];
+  double vx = mx / rho, vy = my / rho;
+  int guard = (o->problem == SWFD_PROBLEM_SEDOV_2D) ? (rho < o->eps2) : lt_lit_1em8(o, rho);
+  if (guard) vx = 0.0;
+  if (guard) vy = 0.0;
+  double pres = o->gamma1 * (e - 0.5 * rho * (vx * vx) - 0.5 * rho * (vy * vy));
+  if (!gdir) {
+    f[0] = mx;
+    f[1] = rho * (vx * vx) + pres;
+    f[2] = rho * vx * vy;
+    f[3] = (e + pres) * vx;
+  } else {
+    f[0] = my;
+    f[1] = rho * vx * vy;
+    f[2] = rho * (vy * vy) + pres;
+    f[3] = (e + pres) * vy;
+  }
+}
+
+/* findalpha (ex3_vortex_accuracy_2d/main.f90:549-562;
+ *            eps2-guarded form ex5_mach2000_jet/main.f90:553-589,
+ *            ex4_sedov_2d/main.f90:652-683) */
+static void findalpha2d(oracle* o) {
+  double am = 0.0;
+  for (int i = -2; i <= o->nx + 3; ++i)
+    for (int j = -2; j <= o->ny + 3; ++j) {
+      double u1 = U(o->u, 0, i, j), u2 = U(o->u, 1, i, j), u3 = U(o->u, 2, i, j),
+             u4 = U(o->u, 3, i, j);
+      double den = u1;
+      if (o->problem == SWFD_PROBLEM_VORTEX_2D) {
+        double pres = o->gamma1 * (u4 - u2 * u2 / u1 / 2.0 - u3 * u3 / u1 / 2.0);
+        double sound = sqrt(o->gamma * pres / den);
+        am = fmax(fmax(am, fabs(u2 / u1) + sound), fabs(u3 / u1) + sound);
+      } else {
+        double vx, vy;
+        if (den >= o->eps2) {
+          vx = u2 / den;
+          vy = u3 / den;
+        } else {
+          vx = 0.0;
+          vy = 0.0;
+        }
+        double pres = o->gamma1 * (u4 - 0.5 * den * (vx * vx) - 0.5 * den * (vy * vy));
+        double sound = sqrt(o->gamma * pres / den);
+        double a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+        am = fmax(am, a);
+      }
+    }
+  o->alphamax = am;
+}
+
+/* Roe average + eigenvectors + characteristic WENO for one interface of one
+ * line (x pass ex3_vortex_accuracy_2d/main.f90:148-229, y pass :349-431;
+ * ex4 regularisers ex4_sedov_2d/main.f90:234,240,455). s[m][c] holds the
+ * split fluxes of stencil cells m = 0..4 (offsets -2..2).  ydir swaps the
+ * roles of the two momentum components. */
+static void interface2d(const oracle* o, int ydir, double wl, double wr, double vxl, double vxr,
+                        double vyl, double vyr, double hl, double hr, const double sp[5][4],
+                        const double sn[5][4], double* outp, double* outn) {
+  double evr[4][4], evl[4][4], cu_p[4][5], cu_n[4][5], ur[4], ul[4];
+  const double g1 = o->gamma1;
+  double t0, t1, t2, t3;
+  if (o->problem == SWFD_PROBLEM_SEDOV_2D && o->quad)
+    t0 = (double)((Q)wl / ((Q)(wl + wr) + (Q)1e-15f128));
+  else
+    t0 = wl / (wl + wr + 1.e-15);
+  t1 = 1. - t0;
+  double vxm = t0 * vxl + t1 * vxr;
+  double vym = t0 * vyl + t1 * vyr;
+  double hm = t0 * hl + t1 * hr;
+  double qm = 0.5 * (vxm * vxm + vym * vym);
+  double cm;
+  if (o->problem == SWFD_PROBLEM_SEDOV_2D && o->quad)
+    cm = (double)((Q)sqrt(fabs(g1 * (hm - qm))) + (Q)1e-15f128);
+  else if (o->problem == SWFD_PROBLEM_SEDOV_2D)
+    cm = sqrt(fabs(g1 * (hm - qm))) + 1e-15;
+  else
+    cm = sqrt(fabs(g1 * (hm - qm))) + 1.e-15;
+  double vn = ydir ? vym : vxm; /* velocity normal to the interface */
+  double vt = ydir ? vxm : vym; /* tangential velocity */
+  t0 = vn * cm;
+  /* evr rows: 1 = density, 2 = x-momentum, 3 = y-momentum, 4 = energy */
+  evr[0][0] = 1.0; evr[0][1] = 0.0; evr[0][2] = 1.0; evr[0][3] = 1.0;
+  if (!ydir) {
+    evr[1][0] = vxm - cm; evr[1][1] = 0.0; evr[1][2] = vxm; evr[1][3] = vxm + cm;
+    evr[2][0] = vym;      evr[2][1] = 1.0; evr[2][2] = vym; evr[2][3] = vym;
+  } else {
+    evr[1][0] = vxm;      evr[1][1] = 1.0; evr[1][2] = vxm; evr[1][3] = vxm;
+    evr[2][0] = vym - cm; evr[2][1] = 0.0; evr[2][2] = vym; evr[2][3] = vym + cm;
+  }
+  evr[3][0] = hm - t0; evr[3][1] = vt; evr[3][2] = qm; evr[3][3] = hm + t0;
+  double rcm = 1. / cm;
+  double b1 = g1 * rcm * rcm;
+  double b2 = qm * b1;
+  t0 = vn * rcm;
+  t1 = b1 * vn;
+  t2 = 0.5 * b1;
+  t3 = b1 * vt;
+  if (!ydir) {
+    evl[0][0] = 0.5 * (b2 + t0); evl[0][1] = -0.5 * (t1 + rcm); evl[0][2] = -0.5 * t3; evl[0][3] = t2;
+    evl[1][0] = -vym;            evl[1][1] = 0.0;               evl[1][2] = 1.0;        evl[1][3] = 0.0;
+    evl[2][0] = 1. - b2;         evl[2][1] = t1;                evl[2][2] = t3;         evl[2][3] = -b1;
+    evl[3][0] = 0.5 * (b2 - t0); evl[3][1] = -0.5 * (t1 - rcm); evl[3][2] = -0.5 * t3; evl[3][3] = t2;
+  } else {
+    evl[0][0] = 0.5 * (b2 + t0); evl[0][1] = -0.5 * t3; evl[0][2] = -0.5 * (t1 + rcm); evl[0][3] = t2;
+    evl[1][0] = -vxm;            evl[1][1] = 1.0;       evl[1][2] = 0.0;               evl[1][3] = 0.0;
+    evl[2][0] = 1. - b2;         evl[2][1] = t3;        evl[2][2] = t1;                evl[2][3] = -b1;
+    evl[3][0] = 0.5 * (b2 - t0); evl[3][1] = -0.5 * t3; evl[3][2] = -0.5 * (t1 - rcm); evl[3][3] = t2;
+  }
+  for (int ig = 0; ig < 5; ++ig)
+    for (int k = 0; k < 4; ++k) {
+      cu_p[k][ig] = evl[k][0] * sp[ig][0] + evl[k][1] * sp[ig][1] + evl[k][2] * sp[ig][2] +
+                    evl[k][3] * sp[ig][3];
+      cu_n[k][ig] = evl[k][0] * sn[ig][0] + evl[k][1] * sn[ig][1] + evl[k][2] * sn[ig][2] +
+                    evl[k][3] * sn[ig][3];
+    }
+  for (int kk = 0; kk < 4; ++kk) {
+    ur[kk] = oracle_weno_right_impl(o, cu_p[kk]);
+    ul[kk] = oracle_weno_left_impl(o, cu_n[kk]);
+  }
+  for (int k = 0; k < 4; ++k) {
+    outp[k] = evr[k][0] * ur[0] + evr[k][1] * ur[1] + evr[k][2] * ur[2] + evr[k][3] * ur[3];
+    outn[k] = evr[k][0] * ul[0] + evr[k][1] * ul[1] + evr[k][2] * ul[2] + evr[k][3] * ul[3];
+  }
+}
+
+/* cell preparation of one line (x pass ex3_vortex_accuracy_2d/main.f90:134-147,
+ * y pass :335-348; ex4 y pass uses 1./(den+1d-15), ex4_sedov_2d/main.f90:426) */
+static void prep_cell(const oracle* o, int ydir, const double* a, double* w, double* vx,
+                      double* vy, double* h) {
+  double den = a[0], xmt = a[1], ymt = a[2], eng = a[3];
+  double t0;
+  if (ydir && o->problem == SWFD_PROBLEM_SEDOV_2D) {
+    if (o->quad)
+      t0 = (double)((Q)1 / ((Q)den + (Q)1e-15f128));
+    else
+      t0 = 1. / (den + 1e-15);
+  } else {
+    t0 = 1. / den;
+  }
+  double vex = xmt * t0, vey = ymt * t0;
+  double pre = o->gamma1 * (eng - 0.5 * (xmt * vex + ymt * vey));
+  *w = sqrt(fabs(den));
+  *vx = vex;
+  *vy = vey;
+  *h = (pre + eng) * t0;
+}
+
+/* wenofd (ex3_vortex_accuracy_2d/main.f90:115-534; ex4_sedov_2d/main.f90:179-637) */
+static void wenofd2d(oracle* o) {
+  const int nx = o->nx, ny = o->ny;
+  findalpha2d(o);
+  const double am = o->alphamax;
+  for (int i = -2; i <= nx + 3; ++i)
+    for (int j = -2; j <= ny + 3; ++j) {
+      double a[4], f[4], g[4];
+      for (int c = 0; c < 4; ++c) a[c] = U(o->u, c, i, j);
+      fflux2d(o, a, f, 0);
+      fflux2d(o, a, g, 1);
+      for (int c = 0; c < 4; ++c) {
+        U(o->fp, c, i, j) = 0.5 * (a[c] + f[c] / am);
+        U(o->fn, c, i, j) = 0.5 * (a[c] - f[c] / am);
+        U(o->gp, c, i, j) = 0.5 * (a[c] + g[c] / am);
+        U(o->gn, c, i, j) = 0.5 * (a[c] - g[c] / am);
+      }
+    }
+  const int premul = (o->problem == SWFD_PROBLEM_SEDOV_2D);
+  /* x pass */
+  for (int j = 0; j <= ny + 1; ++j) {
+    for (int i = 0; i <= nx + 2; ++i) {
+      double a[4];
+      for (int c = 0; c < 4; ++c) a[c] = U(o->u, c, i, j);
+      prep_cell(o, 0, a, &o->wk_w[i], &o->wk_vx[i], &o->wk_vy[i], &o->wk_h[i]);
+    }
+    for (int i = 0; i <= nx + 1; ++i) {
+      double sp[5][4], sn[5][4], op[4], on[4];
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 4; ++c) {
+          sp[ig][c] = U(o->fp, c, i + ig - 2, j);
+          sn[ig][c] = U(o->fn, c, i + ig - 2, j);
+        }
+      interface2d(o, 0, o->wk_w[i], o->wk_w[i + 1], o->wk_vx[i], o->wk_vx[i + 1], o->wk_vy[i],
+                  o->wk_vy[i + 1], o->wk_h[i], o->wk_h[i + 1], (const double(*)[4])sp,
+                  (const double(*)[4])sn, op, on);
+      for (int c = 0; c < 4; ++c) {
+        U(o->fpf, c, i, j) = premul ? am * op[c] : op[c];
+        U(o->fnf, c, i, j) = premul ? am * on[c] : on[c];
+      }
+    }
+  }
+  /* y pass */
+  for (int i = 0; i <= nx + 1; ++i) {
+    for (int j = 0; j <= ny + 2; ++j) {
+      double a[4];
+      for (int c = 0; c < 4; ++c) a[c] = U(o->u, c, i, j);
+      prep_cell(o, 1, a, &o->wk_w[j], &o->wk_vx[j], &o->wk_vy[j], &o->wk_h[j]);
+    }
+    for (int j = 0; j <= ny + 1; ++j) {
+      double sp[5][4], sn[5][4], op[4], on[4];
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 4; ++c) {
+          sp[ig][c] = U(o->gp, c, i, j + ig - 2);
+          sn[ig][c] = U(o->gn, c, i, j + ig - 2);
+        }
+      interface2d(o, 1, o->wk_w[j], o->wk_w[j + 1], o->wk_vx[j], o->wk_vx[j + 1], o->wk_vy[j],
+                  o->wk_vy[j + 1], o->wk_h[j], o->wk_h[j + 1], (const double(*)[4])sp,
+                  (const double(*)[4])sn, op, on);
+      for (int c = 0; c < 4; ++c) {
+        U(o->gpf, c, i, j) = premul ? am * op[c] : op[c];
+        U(o->gnf, c, i, j) = premul ? am * on[c] : on[c];
+      }
+    }
+  }
+}
+
+/* scheme (ex3_vortex_accuracy_2d/main.f90:536-547; ex4_sedov_2d/main.f90:639-650) */
+static void scheme2d(oracle* o) {
+  const size_t n = (size_t)o->nc * o->LI * o->LJ;
+  memset(o->rhs, 0, n * sizeof(double));
+  const double am = o->alphamax, dx = o->dx, dy = o->dy;
+  const int premul = (o->problem == SWFD_PROBLEM_SEDOV_2D);
+  for (int i = 1; i <= o->nx; ++i)
+    for (int j = 1; j <= o->ny; ++j)
+      for (int c = 0; c < 4; ++c) {
+        double A = (U(o->fpf, c, i, j) - U(o->fnf, c, i + 1, j)) -
+                   (U(o->fpf, c, i - 1, j) - U(o->fnf, c, i, j));
+        double B = (U(o->gpf, c, i, j) - U(o->gnf, c, i, j + 1)) -
+                   (U(o->gpf, c, i, j - 1) - U(o->gnf, c, i, j));
+        if (premul)
+          U(o->rhs, c, i, j) = -A / dx - B / dy;
+        else
+          U(o->rhs, c, i, j) = -(am * A) / dx - (am * B) / dy;
+      }
+}
+
+/* checkpositivity (ex3_vortex_accuracy_2d/main.f90:634-651; `<` in
+ * ex4_sedov_2d/main.f90:779-801 and ex5_mach2000_jet/main.f90:667-684) */
+static int checkpositivity2d(const oracle* o) {
+  const int strict = (o->problem == SWFD_PROBLEM_SEDOV_2D || o->problem == SWFD_PROBLEM_JET_2D);
+  int postag = 0;
+  for (int i = 1; i <= o->nx; ++i)
+    for (int j = 1; j <= o->ny; ++j) {
+      double u1 = U(o->u, 0, i, j), u2 = U(o->u, 1, i, j), u3 = U(o->u, 2, i, j),
+             u4 = U(o->u, 3, i, j);
+      double pe = u4 - u3 * u3 / u1 / 2. - u2 * u2 / u1 / 2.;
+      if (strict) {
+        if (u1 < o->eps) postag = 1;
+        if (pe < o->eps) postag = 1;
+      } else {
+        if (u1 <= o->eps) postag = 1;
+        if (pe <= o->eps) postag = 1;
+      }
+    }
+  return postag;
+}
+
+/* bc (ex3_vortex_accuracy_2d/main.f90:653-669 periodic;
+ *     ex4_sedov_2d/main.f90:922-994 reflect x=0,y=0 + outflow;
+ *     ex5_mach2000_jet/main.f90:686-742 jet inflow + reflect y=0 + outflow) */
+static void bc2d(oracle* o) {
+  const int nx = o->nx, ny = o->ny;
+  double* u = o->u;
+  if (o->problem == SWFD_PROBLEM_VORTEX_2D) {
+    for (int j = -2; j <= ny + 3; ++j)
+      for (int i = 1; i <= 3; ++i)
+        for (int c = 0; c < 4; ++c) {
+          U(u, c, 1 - i, j) = U(u, c, nx + 1 - i, j);
+          U(u, c, nx + i, j) = U(u, c, i, j);
+        }
+    for (int j = 1; j <= 3; ++j)
+      for (int i = -2; i <= nx + 3; ++i)
+        for (int c = 0; c < 4; ++c) {
+          U(u, c, i, 1 - j) = U(u, c, i, ny + 1 - j);
+          U(u, c, i, ny + j) = U(u, c, i, j);
+        }
+  } else if (o->problem == SWFD_PROBLEM_SEDOV_2D) {
+    for (int j = -2; j <= ny + 3; ++j)
+      for (int i = 1; i <= 3; ++i) {
+        U(u, 0, 1 - i, j) = U(u, 0, i, j);
+        U(u, 1, 1 - i, j) = -U(u, 1, i, j);
+        U(u, 2, 1 - i, j) = U(u, 2, i, j);
+        U(u, 3, 1 - i, j) = U(u, 3, i, j);
+      }
+    for (int j = 1; j <= 3; ++j)
+      for (int i = -2; i <= nx + 3; ++i) {
+        U(u, 0, i, 1 - j) = U(u, 0, i, j);
+        U(u, 1, i, 1 - j) = U(u, 1, i, j);
+        U(u, 2, i, 1 - j) = -U(u, 2, i, j);
+        U(u, 3, i, 1 - j) = U(u, 3, i, j);
+      }
+    /* x(nx+1) > xm and y(ny+1) > ym always hold on the single block */
+    for (int ig = 1; ig <= 3; ++ig)
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int c = 0; c < 4; ++c) U(u, c, nx + ig, j) = U(u, c, nx, j);
+    for (int ig = 1; ig <= 3; ++ig)
+      for (int i = -2; i <= nx + 3; ++i)
+        for (int c = 0; c < 4; ++c) U(u, c, i, ny + ig) = U(u, c, i, ny);
+  } else if (o->problem == SWFD_PROBLEM_JET_2D) {
+    const double ujet = 800.;
+    for (int j = -2; j <= ny + 3; ++j) {
+      if (o->y[j + 2] <= 0.05) {
+        for (int i = 1; i <= 3; ++i) {
+          U(u, 0, 1 - i, j) = 5.;
+          U(u, 1, 1 - i, j) = 5. * ujet;
+          U(u, 2, 1 - i, j) = 0.;
+          U(u, 3, 1 - i, j) =
+              0.4127 / o->gamma1 + 0.5 * (U(u, 1, 1 - i, j) * U(u, 1, 1 - i, j)) / U(u, 0, 1 - i, j);
+        }
+      } else {
+        for (int i = 1; i <= 3; ++i) {
+          U(u, 0, 1 - i, j) = 0.5;
+          U(u, 1, 1 - i, j) = 0.;
+          U(u, 2, 1 - i, j) = 0.;
+          U(u, 3, 1 - i, j) = 0.4127 / o->gamma1;
+        }
+      }
+    }
+    for (int j = 1; j <= 3; ++j)
+      for (int i = -2; i <= nx + 3; ++i) {
+        for (int c = 0; c < 4; ++c) U(u, c, i, 1 - j) = U(u, c, i, j);
+        U(u, 2, i, 1 - j) = -U(u, 2, i, j);
+      }
+    for (int ig = 1; ig <= 3; ++ig)
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int c = 0; c < 4; ++c) U(u, c, nx + ig, j) = U(u, c, nx, j);
+    for (int ig = 1; ig <= 3; ++ig)
+      for (int i = -2; i <= nx + 3; ++i)
+        for (int c = 0; c < 4; ++c) U(u, c, i, ny + ig) = U(u, c, i, ny);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* 2D sweeping post-process                                             */
+/* ------------------------------------------------------------------ */
+/* sweeping_order (ex3_vortex_accuracy_2d/main.f90:1211-1270) */
+static void sweeping_order(oracle* o) {
+  const int nx = o->nx, ny = o->ny;
+  int k = 0;
+  for (int j = 1; j <= ny; ++j) {
+    if (j % 2 == 1)
+      for (int i = 1; i <= nx; ++i) { o->sI_i[k] = i; o->sI_j[k] = j; ++k; }
+    else
+      for (int i = nx; i >= 1; --i) { o->sI_i[k] = i; o->sI_j[k] = j; ++k; }
+  }
+  k = 0;
+  for (int i = 1; i <= nx; ++i) {
+    if (i % 2 == 1)
+      for (int j = 1; j <= ny; ++j) { o->sII_i[k] = i; o->sII_j[k] = j; ++k; }
+    else
+      for (int j = ny; j >= 1; --j) { o->sII_i[k] = i; o->sII_j[k] = j; ++k; }
+  }
+}
+
+static inline double pres2d_sweep(double g1, const double* v) {
+  return g1 * (v[3] - 0.5 * (v[1] * v[1] + v[2] * v[2]) / (v[0]));
+}
+
+/* nod_lim (ex3_vortex_accuracy_2d/main.f90:846-884) */
+static void nod_lim2d(oracle* o, const double* v1, const double* v2, const double* vb,
+                      double* out) {
+  const double g1 = o->gamma1, eps = o->eps;
+  double p1 = g1 * (v1[3] - 0.5 * (v1[1] * v1[1] + v1[2] * v1[2]) / v1[0]);
+  double p2 = g1 * (v2[3] - 0.5 * (v2[1] * v2[1] + v2[2] * v2[2]) / v2[0]);
+  double t;
+  if (p2 > eps) {
+    t = (p1 - eps) / (p1 - p2);
+    o->t_pos_count++;
+  } else {
+    double pb = g1 * (vb[3] - 0.5 * (vb[1] * vb[1] + vb[2] * vb[2]) / vb[0]);
+    double t_1 = (p1 - eps) / (p1 - pb);
+    double d12 = sqrt(sq(v2[3] - v1[3]) + sq(v2[2] - v1[2]) + sq(v2[1] - v1[1]) + sq(v2[0] - v1[0]));
+    double d1b = sqrt(sq(vb[3] - v1[3]) + sq(vb[2] - v1[2]) + sq(vb[1] - v1[1]) + sq(vb[0] - v1[0]));
+    t = fmin(t_1 * d1b / d12, 0.25);
+    o->t_neg_count++;
+  }
+  for (int c = 0; c < 4; ++c) out[c] = (1 - t) * v1[c] + t * v2[c];
+}
+
+static void track_push(oracle* o) {
+  if (o->sweep_count > o->track_cap) {
+    int64_t cap = o->track_cap ? 2 * o->track_cap : 1024;
+    o->sweep_track = realloc(o->sweep_track, cap * sizeof(int32_t));
+    o->neg_track = realloc(o->neg_track, cap * sizeof(int32_t));
+    o->pos_track = realloc(o->pos_track, cap * sizeof(int32_t));
+    for (int64_t k = o->track_cap; k < cap; ++k)
+      o->sweep_track[k] = o->neg_track[k] = o->pos_track[k] = 0;
+    o->track_cap = cap;
+  }
+}
+
+/* scalar_sweep (ex3_vortex_accuracy_2d/main.f90:1140-1209) */
+static void scalar_sweep2d(oracle* o) {
+  const int nx = o->nx, ny = o->ny, N = nx * ny;
+  double rho_min = 1e20;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) rho_min = fmin(U(o->u, 0, i, j), rho_min);
+  const double delta = 1e-12;
+  if (rho_min < delta) {
+    double* rt = o->rho_t; /* rho_t(i,j), i fastest */
+#define RT(i, j) rt[(size_t)((i)-1) + (size_t)nx * (size_t)((j)-1)]
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) RT(i, j) = U(o->u, 0, i, j);
+    const double w = o->weight;
+    for (int k = 0; k < N - 1; ++k) {
+      double v_i = RT(o->sI_i[k], o->sI_j[k]);
+      double v_ip1 = RT(o->sI_i[k + 1], o->sI_j[k + 1]);
+      if (v_i < delta) {
+        RT(o->sI_i[k + 1], o->sI_j[k + 1]) = v_ip1 + (w / w) * (v_i - delta);
+        RT(o->sI_i[k], o->sI_j[k]) = delta;
+      }
+    }
+    for (int k = N - 1; k >= 1; --k) {
+      double v_i = RT(o->sI_i[k], o->sI_j[k]);
+      double v_im1 = RT(o->sI_i[k - 1], o->sI_j[k - 1]);
+      if (v_i < delta) {
+        RT(o->sI_i[k - 1], o->sI_j[k - 1]) = v_im1 + (w / w) * (v_i - delta);
+        RT(o->sI_i[k], o->sI_j[k]) = delta;
+      }
+    }
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) U(o->u, 0, i, j) = RT(i, j);
+#undef RT
+    o->den_count++;
+  }
+}
+
+/* one forward or backward pass along an ordering
+ * (ex3_vortex_accuracy_2d/main.f90:939-1016 ordering I, :1023-1104 ordering II) */
+static void pressure_pass2d(oracle* o, const int* oi, const int* oj, int N, int forward,
+                            const double* ubar) {
+  const double g1 = o->gamma1, eps = o->eps, w = o->weight;
+  int k0 = forward ? 0 : N - 1, k1 = forward ? N - 1 : 0, dk = forward ? 1 : -1;
+  for (int k = k0; k != k1; k += dk) {
+    double vi[4], vp[4], vit[4], d[4];
+    for (int c = 0; c < 4; ++c) vi[c] = U(o->u, c, oi[k], oj[k]);
+    double pres_v_i = pres2d_sweep(g1, vi);
+    if (pres_v_i <= eps || vi[0] <= eps) {
+      for (int c = 0; c < 4; ++c) vp[c] = U(o->u, c, oi[k + dk], oj[k + dk]);
+      nod_lim2d(o, vi, vp, ubar, vit);
+      for (int c = 0; c < 4; ++c) d[c] = vi[c] - vit[c];
+      for (int c = 0; c < 4; ++c) {
+        U(o->u, c, oi[k], oj[k]) = vit[c];
+        U(o->u, c, oi[k + dk], oj[k + dk]) = vp[c] + (w / w) * (d[c]);
+      }
+    }
+  }
+}
+
+/* sweep_lim (ex3_vortex_accuracy_2d/main.f90:888-1137; P(u_bar) check and
+ * stop-on-failure of ex4_sedov_2d/main.f90:1447-1454,1747-1752; `>=` exit
+ * test of ex5_mach2000_jet/main.f90:1162) */
+static int sweep_lim2d(oracle* o) {
+  const int nx = o->nx, ny = o->ny, N = nx * ny;
+  scalar_sweep2d(o);
+  double ra = 0.0, m1a = 0.0, m2a = 0.0, ea = 0.0;
+  const double w = o->weight;
+  if (o->cfg.ubar_mode == SWFD_UBAR_TREE) {
+    /* not used by the oracle: the oracle is always sequential */
+  }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      ra = ra + w * U(o->u, 0, i, j);
+      m1a = m1a + w * U(o->u, 1, i, j);
+      m2a = m2a + w * U(o->u, 2, i, j);
+      ea = ea + w * U(o->u, 3, i, j);
+    }
+  double ubar[4] = {ra, m1a, m2a, ea};
+  if (o->problem == SWFD_PROBLEM_SEDOV_2D) {
+    if (o->gamma1 * (ubar[3] - 0.5 * (ubar[1] * ubar[1] + ubar[2] * ubar[2]) / ubar[0]) <= 0.)
+      return SWFD_ERR_PUBAR_NONPOS;
+  }
+  o->sweep_count++;
+  track_push(o);
+  o->t_pos_count = 0;
+  o->t_neg_count = 0;
+  const int ge = (o->problem == SWFD_PROBLEM_JET_2D);
+  for (int q = 1; q <= o->cfg.swp_num; ++q) {
+    const int* oi = (q % 2 == 1) ? o->sI_i : o->sII_i;
+    const int* oj = (q % 2 == 1) ? o->sI_j : o->sII_j;
+    pressure_pass2d(o, oi, oj, N, 1, ubar);
+    pressure_pass2d(o, oi, oj, N, 0, ubar);
+    double rho_min = 1e20, p_min = 1e20;
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double v[4];
+        for (int c = 0; c < 4; ++c) v[c] = U(o->u, c, i, j);
+        p_min = fmin(o->gamma1 * (v[3] - 0.5 * (v[1] * v[1] + v[2] * v[2]) / v[0]), p_min);
+        rho_min = fmin(v[0], rho_min);
+      }
+    o->pre_count++;
+    int ok = ge ? (p_min >= o->eps && rho_min >= o->eps) : (p_min > o->eps && rho_min > o->eps);
+    if (ok) {
+      o->sweep_track[o->sweep_count - 1] = q;
+      o->neg_track[o->sweep_count - 1] = (int32_t)o->t_neg_count;
+      o->pos_track[o->sweep_count - 1] = (int32_t)o->t_pos_count;
+      break;
+    }
+    if (q == o->cfg.swp_num) {
+      o->fail_count++;
+      if (o->problem == SWFD_PROBLEM_SEDOV_2D) return SWFD_ERR_SWEEP_NOCONV;
+    }
+  }
+  return SWFD_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* 1D (ex2_sedov_1d/main.f90, built with -fdefault-real-8)              */
+/* ------------------------------------------------------------------ */
+#define U1(a, c, i) ((a)[(size_t)(c) + 3 * (size_t)((i) + 2)])
+
+/* fflux (ex2_sedov_1d/main.f90:57-73) */
+static void fflux1d(const oracle* o, double rho, double mx, double e, double* f) {
+  double vx = 0.0; /* the reference leaves vx undefined only for NaN rho */
+  if (gt_lit_1em8(o, rho)) vx = mx / rho;
+  if (le_lit_1em8(o, rho)) vx = 0.;
+  double pres = o->gamma1 * (e - 0.5 * rho * (vx * vx));
+  f[0] = mx;
+  f[1] = rho * (vx * vx) + pres;
+  f[2] = (e + pres) * vx;
+}
+
+/* findalpha (ex2_sedov_1d/main.f90:273-285) */
+static void findalpha1d(oracle* o) {
+  double am = 0.0;
+  for (int i = -2; i <= o->nx + 3; ++i) {
+    double den = U1(o->u, 0, i);
+    double pres = o->gamma1 * (U1(o->u, 2, i) - U1(o->u, 1, i) * U1(o->u, 1, i) / U1(o->u, 0, i) / 2.);
+    double sound = sqrt(o->gamma * pres / den);
+    am = fmax(am, fabs(U1(o->u, 1, i) / U1(o->u, 0, i)) + sound);
+  }
+  o->alphamax = am;
+}
+
+/* wenofd (ex2_sedov_1d/main.f90:75-250): eigenvectors at cell m */
+static void wenofd1d(oracle* o) {
+  const int n = o->nx;
+  findalpha1d(o);
+  const double am = o->alphamax, g1 = o->gamma1;
+  for (int i = -2; i <= n + 3; ++i) {
+    double f[3];
+    fflux1d(o, U1(o->u, 0, i), U1(o->u, 1, i), U1(o->u, 2, i), f);
+    for (int c = 0; c < 3; ++c) {
+      U1(o->fp, c, i) = 0.5 * (U1(o->u, c, i) + f[c] / am);
+      U1(o->fn, c, i) = 0.5 * (U1(o->u, c, i) - f[c] / am);
+    }
+  }
+  for (int m = 0; m <= n + 1; ++m) {
+    double evr[3][3], evl[3][3], cu_p[3][5], cu_n[3][5], ur[3], ul[3];
+    double u1 = U1(o->u, 0, m), u2 = U1(o->u, 1, m), u3 = U1(o->u, 2, m);
+    double vxm = u2 / u1;
+    double hm = (g1 * (u3 - 0.5 * (u2 * u2) / u1) + u3) / u1;
+    double qm = 0.5 * vxm * vxm;
+    double cm = sqrt(g1 * (hm - qm));
+    double t0 = vxm * cm;
+    evr[0][0] = 1.0; evr[0][1] = 1.0; evr[0][2] = 1.0;
+    evr[1][0] = vxm - cm; evr[1][1] = vxm; evr[1][2] = vxm + cm;
+    evr[2][0] = hm - t0; evr[2][1] = qm; evr[2][2] = hm + t0;
+    double rcm = 1. / cm;
+    double b1 = g1 * rcm * rcm;
+    double b2 = qm * b1;
+    t0 = vxm * rcm;
+    double t1 = b1 * vxm;
+    double t2 = 0.5 * b1;
+    evl[0][0] = 0.5 * (b2 + t0); evl[0][1] = -0.5 * (t1 + rcm); evl[0][2] = t2;
+    evl[1][0] = 1. - b2;         evl[1][1] = t1;                evl[1][2] = -b1;
+    evl[2][0] = 0.5 * (b2 - t0); evl[2][1] = -0.5 * (t1 - rcm); evl[2][2] = t2;
+    for (int jj = 0; jj < 5; ++jj)
+      for (int k = 0; k < 3; ++k) {
+        int mm = m + jj - 2;
+        cu_p[k][jj] = evl[k][0] * U1(o->fp, 0, mm) + evl[k][1] * U1(o->fp, 1, mm) +
+                      evl[k][2] * U1(o->fp, 2, mm);
+        cu_n[k][jj] = evl[k][0] * U1(o->fn, 0, mm) + evl[k][1] * U1(o->fn, 1, mm) +
+                      evl[k][2] * U1(o->fn, 2, mm);
+      }
+    for (int kk = 0; kk < 3; ++kk) {
+      ur[kk] = oracle_weno_right_impl(o, cu_p[kk]);
+      ul[kk] = oracle_weno_left_impl(o, cu_n[kk]);
+    }
+    for (int k = 0; k < 3; ++k) {
+      U1(o->fpf, k, m) = evr[k][0] * ur[0] + evr[k][1] * ur[1] + evr[k][2] * ur[2];
+      U1(o->fnf, k, m) = evr[k][0] * ul[0] + evr[k][1] * ul[1] + evr[k][2] * ul[2];
+    }
+  }
+}
+
+/* scheme (ex2_sedov_1d/main.f90:252-271) */
+static void scheme1d(oracle* o) {
+  const int n = o->nx;
+  memset(o->rhs, 0, (size_t)3 * o->LI * sizeof(double));
+  double* flus = o->gp; /* scratch: flus(:, 1:n+1) */
+  for (int i = 1; i <= n + 1; ++i)
+    for (int c = 0; c < 3; ++c)
+      U1(flus, c, i) = o->alphamax * (U1(o->fpf, c, i - 1) - U1(o->fnf, c, i));
+  for (int i = 1; i <= n; ++i)
+    for (int c = 0; c < 3; ++c) U1(o->rhs, c, i) = -(U1(flus, c, i + 1) - U1(flus, c, i)) / o->dx;
+}
+
+/* checkpositivity (ex2_sedov_1d/main.f90:376-392) */
+static int checkpositivity1d(const oracle* o) {
+  int postag = 0;
+  for (int m = 1; m <= o->nx; ++m) {
+    if (U1(o->u, 0, m) <= o->eps) postag = 1;
+    if (U1(o->u, 2, m) - U1(o->u, 1, m) * U1(o->u, 1, m) / U1(o->u, 0, m) / 2. <= o->eps) postag = 1;
+  }
+  return postag;
+}
+
+/* nod_lim (ex2_sedov_1d/main.f90:517-560) */
+static void nod_lim1d(oracle* o, const double* v1, const double* v2, const double* vb,
+                      double* out) {
+  const double g1 = o->gamma1, eps = o->eps;
+  double p1 = g1 * (v1[2] - 0.5 * (v1[1] * v1[1] / v1[0]));
+  double p2 = g1 * (v2[2] - 0.5 * (v2[1] * v2[1] / v2[0]));
+  double t;
+  if (p2 > eps) {
+    t = (p1 - eps) / (p1 - p2);
+    o->t_pos_count++;
+  } else {
+    double pb = g1 * (vb[2] - 0.5 * (vb[1] * vb[1] / vb[0]));
+    double t_1 = (p1 - eps) / (p1 - pb);
+    double d12 = sqrt(sq(v2[2] - v1[2]) + sq(v2[1] - v1[1]) + sq(v2[0] - v1[0]));
+    double d1b = sqrt(sq(vb[2] - v1[2]) + sq(vb[1] - v1[1]) + sq(vb[0] - v1[0]));
+    t = fmin(t_1 * d1b / d12, 0.25);
+    o->t_neg_count++;
+  }
+  for (int c = 0; c < 3; ++c) out[c] = (1 - t) * v1[c] + t * v2[c];
+}
+
+/* scalar_sweep (ex2_sedov_1d/main.f90:729-790): always, over -2..n+3 */
+static void scalar_sweep1d(oracle* o) {
+  const int n = o->nx;
+  const double delta = 1e-13, w = o->weight;
+  double* rt = o->rho_t; /* rho_t(-2:n+3) */
+  for (int j = -2; j <= n + 3; ++j) rt[j + 2] = U1(o->u, 0, j);
+  for (int j = -2; j <= n + 2; ++j) {
+    double v_j = rt[j + 2], v_jp1 = rt[j + 3];
+    if (v_j < delta) {
+      rt[j + 3] = v_jp1 + (w / w) * (v_j - delta);
+      rt[j + 2] = delta;
+    }
+  }
+  for (int j = n + 3; j >= -1; --j) {
+    double v_j = rt[j + 2], v_jm1 = rt[j + 1];
+    if (v_j < delta) {
+      rt[j + 1] = v_jm1 + (w / w) * (v_j - delta);
+      rt[j + 2] = delta;
+    }
+  }
+  for (int j = -2; j <= n + 3; ++j) U1(o->u, 0, j) = rt[j + 2];
+  o->den_count++;
+}
+
+/* sweep_lim (ex2_sedov_1d/main.f90:564-726) */
+static int sweep_lim1d(oracle* o) {
+  const int n = o->nx;
+  const double g1 = o->gamma1, eps = o->eps, w = o->weight;
+  scalar_sweep1d(o);
+  double ra = 0.0, ma = 0.0, ea = 0.0; /* dot_product(., weights), in index order */
+  for (int i = -2; i <= n + 3; ++i) ra = ra + U1(o->u, 0, i) * w;
+  for (int i = -2; i <= n + 3; ++i) ma = ma + U1(o->u, 1, i) * w;
+  for (int i = -2; i <= n + 3; ++i) ea = ea + U1(o->u, 2, i) * w;
+  double ubar[3] = {ra, ma, ea};
+  o->sweep_count++;
+  track_push(o);
+  o->t_pos_count = 0;
+  o->t_neg_count = 0;
+  for (int q = 1; q <= o->cfg.swp_num; ++q) {
+    for (int j = -2; j <= n + 2; ++j) {
+      double vj[3], vp[3], vjt[3];
+      for (int c = 0; c < 3; ++c) vj[c] = U1(o->u, c, j);
+      double pres_v_j = g1 * (vj[2] - 0.5 * (vj[1] * vj[1]) / vj[0]);
+      if (pres_v_j <= eps || vj[0] <= eps) {
+        for (int c = 0; c < 3; ++c) vp[c] = U1(o->u, c, j + 1);
+        nod_lim1d(o, vj, vp, ubar, vjt);
+        for (int c = 0; c < 3; ++c) {
+          double d = vj[c] - vjt[c];
+          U1(o->u, c, j) = vjt[c];
+          U1(o->u, c, j + 1) = vp[c] + (w / w) * (d);
+        }
+      }
+    }
+    for (int j = n + 3; j >= -1; --j) {
+      double vj[3], vp[3], vjt[3];
+      for (int c = 0; c < 3; ++c) vj[c] = U1(o->u, c, j);
+      double pres_v_j = g1 * (vj[2] - 0.5 * (vj[1] * vj[1]) / vj[0]);
+      if (pres_v_j <= eps || vj[0] <= eps) {
+        for (int c = 0; c < 3; ++c) vp[c] = U1(o->u, c, j - 1);
+        nod_lim1d(o, vj, vp, ubar, vjt);
+        for (int c = 0; c < 3; ++c) {
+          double d = vj[c] - vjt[c];
+          U1(o->u, c, j) = vjt[c];
+          U1(o->u, c, j - 1) = vp[c] + (w / w) * (d);
+        }
+      }
+    }
+    double rho_min = 1e20, p_min = 1e20;
+    for (int i = -2; i <= n + 3; ++i) {
+      double u1 = U1(o->u, 0, i), u2 = U1(o->u, 1, i), u3 = U1(o->u, 2, i);
+      p_min = fmin(g1 * (u3 - 0.5 * (u2 * u2) / u1), p_min);
+      rho_min = fmin(u1, rho_min);
+    }
+    o->pre_count++;
+    if (p_min > eps && rho_min > eps) {
+      o->sweep_track[o->sweep_count - 1] = q;
+      o->neg_track[o->sweep_count - 1] = (int32_t)o->t_neg_count;
+      o->pos_track[o->sweep_count - 1] = (int32_t)o->t_pos_count;
+      break;
+    }
+    if (q == o->cfg.swp_num) o->fail_count++; /* ex2 records nothing */
+  }
+  return SWFD_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* stage / step / loop                                                 */
+/* ------------------------------------------------------------------ */
+static void wenofd_any(oracle* o) {
+  if (o->ndim == 1) wenofd1d(o); else wenofd2d(o);
+}
+static void scheme_any(oracle* o) {
+  if (o->ndim == 1) scheme1d(o); else scheme2d(o);
+}
+static int check_any(oracle* o) { return o->ndim == 1 ? checkpositivity1d(o) : checkpositivity2d(o); }
+static int sweep_any(oracle* o) { return o->ndim == 1 ? sweep_lim1d(o) : sweep_lim2d(o); }
+static void bc_any(oracle* o) {
+  if (o->ndim == 2) bc2d(o); /* ex2's bc is empty (ex2_sedov_1d/main.f90:394-403) */
+}
+
+static size_t state_len(const oracle* o) { return (size_t)o->nc * o->LI * o->LJ; }
+
+/* dt rule of the problem, evaluated right after the stage-1 wenofd
+ * (ex2_sedov_1d/main.f90:293; ex3_vortex_accuracy_2d/main.f90:570-572;
+ *  ex4_sedov_2d/main.f90:696-700; ex5_mach2000_jet/main.f90:597-605) */
+static void compute_dt(oracle* o) {
+  const double cfl = o->cfg.cfl, am = o->alphamax;
+  switch (o->problem) {
+    case SWFD_PROBLEM_SEDOV_1D: o->dt = o->dx * cfl / am; break;
+    case SWFD_PROBLEM_VORTEX_2D: o->dt = pow(o->dx, 5. / 3.) * cfl / am; break;
+    default: {
+      double dtx = o->dx * cfl / am, dty = o->dy * cfl / am;
+      double dtc = fmin(dtx, dty);
+      o->dt = fmin(dtc, o->cfg.time_terminal - o->time);
+    }
+  }
+}
+
+/* rk / rk3 (ex3_vortex_accuracy_2d/main.f90:564-632; ex2_sedov_1d/main.f90:287-328) */
+int oracle_step(oracle* o) {
+  const size_t n = state_len(o);
+  double* u = o->u;
+  int st;
+  for (int stage = 1; stage <= 3; ++stage) {
+    wenofd_any(o);
+    if (stage == 1) {
+      compute_dt(o);
+      memcpy(o->u0, u, n * sizeof(double));
+    }
+    scheme_any(o);
+    const double dt = o->dt;
+    for (size_t k = 0; k < n; ++k) {
+      double v = u[k] + dt * o->rhs[k];
+      if (stage == 1) u[k] = v;
+      else if (stage == 2) u[k] = rk2(o, o->u0[k], v);
+      else u[k] = rk3(o, o->u0[k], v);
+    }
+    o->postag = check_any(o);
+    if (o->cfg.use_limiter == 2 && o->postag == 1) {
+      st = sweep_any(o);
+      o->postag = 0;
+      if (st != SWFD_OK) return o->status = st;
+    }
+    bc_any(o);
+  }
+  o->time = o->time + o->dt;
+  return SWFD_OK;
+}
+
+/* time <= time_terminal - 1d-10 (ex3_vortex_accuracy_2d/main.f90:51) */
+int oracle_time_loop_continue(const oracle* o) {
+  if (o->quad) return (Q)o->time <= (Q)o->cfg.time_terminal - (Q)1e-10f128;
+  return o->time <= o->cfg.time_terminal - 1e-10;
+}
+
+int64_t oracle_run(oracle* o, int64_t max_steps) {
+  int64_t k = 0;
+  while (oracle_time_loop_continue(o)) {
+    if (max_steps > 0 && k >= max_steps) break;
+    int st = oracle_step(o);
+    ++k;
+    if (st != SWFD_OK) return -1;
+  }
+  return k;
+}
+
+/* ------------------------------------------------------------------ */
+/* initial data (host side of each example)                             */
+/* ------------------------------------------------------------------ */
+/* exact (ex3_vortex_accuracy_2d/main.f90:699-718) */
+static void vortex_exact(const oracle* o, double x, double y, double t, double* e) {
+  const double pi = 3.14159265358979323846264338327950, g1 = o->gamma1, gamma = o->gamma;
+  double r = sqrt(sq(x - 5. - t) + sq(y - 5. - t));
+  double mag = 10.0828;
+  e[0] = pow(1 - g1 * (mag * mag) / 8. / gamma / (pi * pi) * exp(1. - r * r), 1. / g1);
+  e[1] = e[0] * (1. - mag / 2. / pi * exp((1. - r * r) / 2.) * (y - 5.));
+  e[2] = e[0] * (1. + mag / 2. / pi * exp((1. - r * r) / 2.) * (x - 5.));
+  e[3] = pow(e[0], gamma) / g1 + 0.5 * (e[1] * e[1]) / e[0] + 0.5 * (e[2] * e[2]) / e[0];
+}
+
+void oracle_init(oracle* o) {
+  const int nx = o->nx, ny = o->ny;
+  memset(o->u, 0, state_len(o) * sizeof(double));
+  o->time = 0.0;
+  o->sweep_count = o->den_count = o->pre_count = o->fail_count = 0;
+  o->status = 0;
+  switch (o->problem) {
+    case SWFD_PROBLEM_SEDOV_1D: { /* ex2_sedov_1d/main.f90:405-428 */
+      double xleft = -2., xright = 2.;
+      o->dx = (xright - xleft) / nx;
+      for (int i = -2; i <= nx + 3; ++i) o->x[i + 2] = xleft + i * o->dx - o->dx / 2.;
+      for (int i = -2; i <= nx + 3; ++i) {
+        U1(o->u, 0, i) = 1.;
+        U1(o->u, 1, i) = 0.;
+        U1(o->u, 2, i) = o->cfg.e_background;
+      }
+      U1(o->u, 2, nx / 2 + 1) = o->cfg.e_blast / o->dx;
+      break;
+    }
+    case SWFD_PROBLEM_VORTEX_2D: { /* ex3_vortex_accuracy_2d/main.f90:671-697 */
+      double xleft = 0., xright = 10., yleft = 0., yright = 10.;
+      o->dx = (xright - xleft) / nx;
+      o->dy = (yright - yleft) / ny;
+      for (int i = -2; i <= nx + 3; ++i) o->x[i + 2] = xleft + i * o->dx - o->dx / 2.;
+      for (int i = -2; i <= ny + 3; ++i) o->y[i + 2] = yleft + i * o->dy - o->dy / 2.;
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          double e[4];
+          vortex_exact(o, o->x[i + 2], o->y[j + 2], 0., e);
+          for (int c = 0; c < 4; ++c) U(o->u, c, i, j) = e[c];
+        }
+      bc2d(o);
+      break;
+    }
+    case SWFD_PROBLEM_SEDOV_2D: { /* ex4_sedov_2d/main.f90:1121-1189, one block */
+      const double xm = 1.3, ym = 1.3;
+      double xleft = xm / 1 * 0, xright = xm / 1 * (0 + 1);
+      double yleft = ym / 1 * 0, yright = ym / 1 * (0 + 1);
+      o->dx = (xright - xleft) / nx;
+      o->dy = (yright - yleft) / ny;
+      for (int i = -2; i <= nx + 3; ++i) o->x[i + 2] = xleft + i * o->dx - o->dx / 2.;
+      for (int i = -2; i <= ny + 3; ++i) o->y[i + 2] = yleft + i * o->dy - o->dy / 2.;
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(o->u, 0, i, j) = 1;
+          U(o->u, 3, i, j) = o->cfg.e_background;
+        }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double gx = xleft + o->dx * (i - 0.5), gy = yleft + o->dy * (j - 0.5);
+          if (fabs(gx - 0.0) <= o->dx / 2.0 && fabs(gy - 0.0) <= o->dy / 2.0)
+            U(o->u, 3, i, j) = o->cfg.e_blast / (o->dx * o->dy);
+        }
+      bc2d(o);
+      break;
+    }
+    case SWFD_PROBLEM_JET_2D: { /* ex5_mach2000_jet/main.f90:744-768 */
+      double xleft = 0., xright = 1., yleft = 0., yright = 0.25;
+      o->dx = (xright - xleft) / nx;
+      o->dy = (yright - yleft) / ny;
+      for (int i = -2; i <= nx + 3; ++i) o->x[i + 2] = xleft + i * o->dx - o->dx / 2.;
+      for (int i = -2; i <= ny + 3; ++i) o->y[i + 2] = yleft + i * o->dy - o->dy / 2.;
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(o->u, 0, i, j) = 0.5;
+          U(o->u, 3, i, j) = 0.4127 / o->gamma1;
+        }
+      bc2d(o);
+      break;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* lifetime + accessors (ctypes surface of the oracle)                  */
+/* ------------------------------------------------------------------ */
+oracle* oracle_create(const swfd_config* cfg) {
+  oracle* o = calloc(1, sizeof(oracle));
+  o->cfg = *cfg;
+  o->problem = cfg->problem;
+  o->quad = cfg->literals == SWFD_LITERALS_QUAD;
+  o->ndim = (cfg->problem == SWFD_PROBLEM_SEDOV_1D) ? 1 : 2;
+  o->nc = o->ndim == 1 ? 3 : 4;
+  o->nx = cfg->nx;
+  o->ny = o->ndim == 1 ? 1 : cfg->ny;
+  o->LI = o->nx + 6;
+  o->LJ = o->ndim == 1 ? 1 : o->ny + 6;
+  o->gamma = cfg->gamma;
+  o->gamma1 = cfg->gamma - 1.;
+  o->eps = 1e-13;
+  o->eps2 = 1e-8;
+  o->weno_eps = 1e-6;
+  o->weno_eps_q = 1e-6f128;
+  const size_t n = state_len(o);
+  double** arrs[] = {&o->u, &o->u0, &o->rhs, &o->fp, &o->fn, &o->gp,
+                     &o->gn, &o->fpf, &o->fnf, &o->gpf, &o->gnf};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) *arrs[k] = calloc(n, sizeof(double));
+  o->x = calloc(o->nx + 6, sizeof(double));
+  o->y = calloc(o->ny + 6, sizeof(double));
+  int mx = (o->nx > o->ny ? o->nx : o->ny) + 3;
+  o->wk_w = calloc(mx, sizeof(double));
+  o->wk_vx = calloc(mx, sizeof(double));
+  o->wk_vy = calloc(mx, sizeof(double));
+  o->wk_h = calloc(mx, sizeof(double));
+  if (o->ndim == 2) {
+    size_t N = (size_t)o->nx * o->ny;
+    o->rho_t = calloc(N, sizeof(double));
+    o->sI_i = calloc(N, sizeof(int));
+    o->sI_j = calloc(N, sizeof(int));
+    o->sII_i = calloc(N, sizeof(int));
+    o->sII_j = calloc(N, sizeof(int));
+    sweeping_order(o);
+    /* weights(i,j) = 1./(nSteps_x*nSteps_y) (ex3_vortex_accuracy_2d/main.f90:44) */
+    o->weight = 1. / ((double)o->nx * (double)o->ny);
+  } else {
+    o->rho_t = calloc(o->nx + 6, sizeof(double));
+    /* weights(i) = 1/(nSteps + 6) (ex2_sedov_1d/main.f90:31) */
+    o->weight = 1 / ((double)o->nx + 6);
+  }
+  return o;
+}
+
+void oracle_destroy(oracle* o) {
+  if (!o) return;
+  double* arrs[] = {o->u, o->u0, o->rhs, o->fp, o->fn, o->gp, o->gn, o->fpf, o->fnf, o->gpf, o->gnf,
+                    o->x, o->y, o->wk_w, o->wk_vx, o->wk_vy, o->wk_h, o->rho_t};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) free(arrs[k]);
+  free(o->sI_i); free(o->sI_j); free(o->sII_i); free(o->sII_j);
+  free(o->sweep_track); free(o->neg_track); free(o->pos_track);
+  free(o);
+}
+
+int64_t oracle_state_len(const oracle* o) { return (int64_t)state_len(o); }
+void oracle_get_state(const oracle* o, double* out) { memcpy(out, o->u, state_len(o) * sizeof(double)); }
+void oracle_set_state(oracle* o, const double* in) { memcpy(o->u, in, state_len(o) * sizeof(double)); }
+double oracle_get_time(const oracle* o) { return o->time; }
+void oracle_set_time(oracle* o, double t) { o->time = t; }
+double oracle_get_dt(const oracle* o) { return o->dt; }
+double oracle_get_alphamax(const oracle* o) { return o->alphamax; }
+double oracle_get_dx(const oracle* o) { return o->dx; }
+double oracle_get_dy(const oracle* o) { return o->dy; }
+int oracle_get_status(const oracle* o) { return o->status; }
+
+/* findalpha of the current state */
+double oracle_find_alpha(oracle* o) {
+  if (o->ndim == 1) findalpha1d(o); else findalpha2d(o);
+  return o->alphamax;
+}
+
+/* wenofd + scheme of the current state; rhs in the state layout */
+void oracle_flux_divergence(oracle* o, double* rhs) {
+  wenofd_any(o);
+  scheme_any(o);
+  memcpy(rhs, o->rhs, state_len(o) * sizeof(double));
+}
+
+int oracle_check_positivity(oracle* o) { return check_any(o); }
+
+/* sweep_lim on the current state */
+int oracle_sweep(oracle* o) { return sweep_any(o); }
+
+/* bc on the current state */
+void oracle_bc(oracle* o) { bc_any(o); }
+
+/* stats: out[0..9] in swfd_sweep_stats order */
+void oracle_get_stats(const oracle* o, int64_t* out) {
+  int64_t tot = 0, mx = 0, tn = 0, mn = 0, tp = 0, mp = 0;
+  for (int64_t k = 0; k < o->sweep_count; ++k) {
+    tot += o->sweep_track[k];
+    if (k == 0 || o->sweep_track[k] > mx) mx = o->sweep_track[k];
+    tn += o->neg_track[k];
+    if (k == 0 || o->neg_track[k] > mn) mn = o->neg_track[k];
+    tp += o->pos_track[k];
+    if (k == 0 || o->pos_track[k] > mp) mp = o->pos_track[k];
+  }
+  out[0] = o->sweep_count; out[1] = tot; out[2] = mx; out[3] = tn; out[4] = mn;
+  out[5] = tp; out[6] = mp; out[7] = o->den_count; out[8] = o->pre_count; out[9] = o->fail_count;
+}
+
+int64_t oracle_get_tracks(const oracle* o, int32_t* sweep, int32_t* neg, int32_t* pos, int64_t cap) {
+  int64_t n = o->sweep_count < cap ? o->sweep_count : cap;
+  for (int64_t k = 0; k < n; ++k) {
+    if (sweep) sweep[k] = o->sweep_track[k];
+    if (neg) neg[k] = o->neg_track[k];
+    if (pos) pos[k] = o->pos_track[k];
+  }
+  return o->sweep_count;
+}
+
+/* scalar WENO entry points (weno5.f90:86-146) */
+void oracle_weno5(const double* stencils, int64_t n, double weno_eps, int literals, double* uleft,
+                  double* uright) {
+  oracle o;
+  memset(&o, 0, sizeof(o));
+  o.quad = literals == SWFD_LITERALS_QUAD;
+  o.weno_eps = weno_eps;
+  o.weno_eps_q = (weno_eps == 1e-12) ? 1e-12f128 : 1e-6f128;
+  for (int64_t k = 0; k < n; ++k) {
+    if (uleft) uleft[k] = oracle_weno_left_impl(&o, stencils + 5 * k);
+    if (uright) uright[k] = oracle_weno_right_impl(&o, stencils + 5 * k);
+  }
+}

@@ -1,0 +1,157 @@
+"""ctypes view of the C ABI declared in include/swfd.h.
+
+The shared library is loaded from the package's own ``_lib`` directory.  There
+is no fallback: if the library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libswfd.so"
+ABI_VERSION = 1
+
+# status codes
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_SWEEP_NOCONV = -3
+ERR_PUBAR_NONPOS = -4
+ERR_NONFINITE = -5
+ERR_OOM = -6
+ERR_TIMEOUT = -7
+ERR_UNSUPPORTED = -8
+ERR_MAX_STEPS = -9
+
+# problems (one per reference example)
+SEDOV_1D = 2   # ex2_sedov_1d
+VORTEX_2D = 3  # ex3_vortex_accuracy_2d
+SEDOV_2D = 4   # ex4_sedov_2d
+JET_2D = 5     # ex5_mach2000_jet
+
+LITERALS_DOUBLE = 0
+LITERALS_QUAD = 1
+PRECISION_FP64 = 0
+PRECISION_FP32_BULK = 1
+UBAR_SEQUENTIAL = 0
+UBAR_TREE = 1
+
+
+class SwfdConfig(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32),
+        ("problem", C.c_int32),
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("use_limiter", C.c_int32),
+        ("swp_num", C.c_int32),
+        ("literals", C.c_int32),
+        ("precision", C.c_int32),
+        ("ubar_mode", C.c_int32),
+        ("device", C.c_int32),
+        ("cfl", C.c_double),
+        ("time_terminal", C.c_double),
+        ("gamma", C.c_double),
+        ("e_background", C.c_double),
+        ("e_blast", C.c_double),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class SwfdSweepStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "sweep_count", "total_sweep", "max_sweep", "total_neg", "max_neg", "total_pos",
+        "max_pos", "den_count", "pre_count", "sweep_fail_count")]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+STATS_FIELDS = [f for f, _ in SwfdSweepStats._fields_]
+
+# name -> (restype, argtypes) for every entry point of include/swfd.h
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+_SIGS = {
+    "swfd_config_default": (C.c_int32, [C.POINTER(SwfdConfig), C.c_int32]),
+    "swfd_create": (C.c_int32, [C.POINTER(SwfdConfig), C.POINTER(_P)]),
+    "swfd_destroy": (C.c_int32, [_P]),
+    "swfd_init_problem": (C.c_int32, [_P]),
+    "swfd_upload_state": (C.c_int32, [_P, _DP]),
+    "swfd_download_state": (C.c_int32, [_P, _DP]),
+    "swfd_flux_divergence": (C.c_int32, [_P, _DP]),
+    "swfd_step": (C.c_int32, [_P, _DP]),
+    "swfd_run": (C.c_int32, [_P, C.c_int64, C.POINTER(C.c_int64)]),
+    "swfd_sweep": (C.c_int32, [_P]),
+    "swfd_check_positivity": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "swfd_find_alpha": (C.c_int32, [_P, _DP]),
+    "swfd_get_time": (C.c_int32, [_P, _DP]),
+    "swfd_set_time": (C.c_int32, [_P, C.c_double]),
+    "swfd_get_sweep_stats": (C.c_int32, [_P, C.POINTER(SwfdSweepStats)]),
+    "swfd_get_sweep_tracks": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32), C.c_int64,
+                                          C.POINTER(C.c_int64)]),
+    "swfd_weno5_batch": (C.c_int32, [_DP, C.c_int64, C.c_double, C.c_int32, C.c_int32, _DP, _DP]),
+    "swfd_last_error": (C.c_int32, [_P, C.c_char_p, C.c_size_t]),
+    "swfd_status_string": (C.c_char_p, [C.c_int32]),
+}
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load libswfd.so (once) and attach the prototypes.  Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def exported_names() -> list[str]:
+    return list(_SIGS)
+
+
+class SwfdError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"swfd status {status}: {msg}")
+        self.status = status
+
+
+def last_error(handle=None) -> str:
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    lib.swfd_last_error(handle, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int, handle=None) -> int:
+    if status != OK:
+        raise SwfdError(status, last_error(handle) or load().swfd_status_string(status).decode())
+    return status
+
+
+def config_default(problem: int) -> SwfdConfig:
+    cfg = SwfdConfig()
+    check(load().swfd_config_default(C.byref(cfg), problem))
+    return cfg
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_DP)

@@ -1,0 +1,645 @@
+// swfd_api.cu -- the C ABI: handle lifetime, problem set-up, the SSP-RK3
+// step/stage orchestration, the sweep driver and the statistics.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "swfd_internal.h"
+
+using namespace swfd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+swfd_status fail(swfd_handle* h, swfd_status st, const std::string& msg) {
+  if (h) h->last_error = msg;
+  g_last_error = msg;
+  return st;
+}
+
+#define CU(h, call)                                                                 \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail((h), e_ == cudaErrorMemoryAllocation ? SWFD_ERR_OOM : SWFD_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+#define ST(call)                          \
+  do {                                    \
+    swfd_status s_ = (call);              \
+    if (s_ != SWFD_OK) return s_;         \
+  } while (0)
+
+int64_t host_len(const Params& p) { return (int64_t)p.g.nc * p.g.LI * p.g.LJ; }
+
+// Derive the per-example switches (the reference's variant matrix) and the
+// grid spacing exactly as each initdata computes it.
+swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
+  Geom& g = p.g;
+  p.problem = c.problem;
+  p.literals = c.literals;
+  p.gamma = c.gamma;
+  p.gamma1 = c.gamma - 1.;
+  p.eps = 1e-13;
+  p.eps2 = 1e-8;
+  p.weno_eps = 1e-6;
+  p.time_terminal = c.time_terminal;
+  if (c.nx < 8) {
+    err = "nx must be >= 8";
+    return SWFD_ERR_INVALID;
+  }
+  switch (c.problem) {
+    case SWFD_PROBLEM_SEDOV_1D: {
+      g.ndim = 1;
+      g.nc = 3;
+      g.nx = c.nx;
+      g.ny = 1;
+      g.LI = c.nx + 6;
+      g.LJ = 1;
+      double xleft = -2., xright = 2.;  // ex2_sedov_1d/main.f90:408-410
+      p.dx = (xright - xleft) / c.nx;
+      p.dy = 0;
+      p.dt_rule = 1;
+      p.dt_num_x = p.dx * c.cfl;  // dt = dx*cfl/alphamax (:293)
+      break;
+    }
+    case SWFD_PROBLEM_VORTEX_2D:
+    case SWFD_PROBLEM_SEDOV_2D:
+    case SWFD_PROBLEM_JET_2D: {
+      if (c.ny < 8) {
+        err = "ny must be >= 8";
+        return SWFD_ERR_INVALID;
+      }
+      g.ndim = 2;
+      g.nc = 4;
+      g.nx = c.nx;
+      g.ny = c.ny;
+      g.LI = c.nx + 6;
+      g.LJ = c.ny + 6;
+      if (c.problem == SWFD_PROBLEM_VORTEX_2D) {
+        p.dx = (10. - 0.) / c.nx;  // ex3_vortex_accuracy_2d/main.f90:675-681
+        p.dy = (10. - 0.) / c.ny;
+        p.dt_rule = 3;
+        p.dt_num_x = pow(p.dx, 5. / 3.) * c.cfl;  // :572
+      } else if (c.problem == SWFD_PROBLEM_SEDOV_2D) {
+        const double xm = 1.3, ym = 1.3;  // ex4_sedov_2d/main.f90:20,1154-1161 (one block)
+        double xleft = xm / 1 * 0, xright = xm / 1 * (0 + 1);
+        double yleft = ym / 1 * 0, yright = ym / 1 * (0 + 1);
+        p.dx = (xright - xleft) / c.nx;
+        p.dy = (yright - yleft) / c.ny;
+        p.dt_rule = 4;
+        p.alpha_guarded = 1;
+        p.flux_guard_eps2 = 1;
+        p.roe_reg_ex4 = 1;
+        p.alpha_premul = 1;
+        p.pos_strict = 1;
+      } else {
+        p.dx = (1. - 0.) / c.nx;  // ex5_mach2000_jet/main.f90:748-754
+        p.dy = (0.25 - 0.) / c.ny;
+        p.dt_rule = 4;
+        p.alpha_guarded = 1;
+        p.pos_strict = 1;
+        p.exit_ge = 1;
+        // inflow rows: y(j) = yleft + j*dy - dy/2 <= 0.05 (:703)
+        p.jet_jmax = -3;
+        for (int j = -2; j <= c.ny + 3; ++j)
+          if (0. + j * p.dy - p.dy / 2. <= 0.05) p.jet_jmax = j;
+        const double ujet = 800.;
+        p.jet_in[0] = 5.;
+        p.jet_in[1] = 5. * ujet;
+        p.jet_in[2] = 0.;
+        p.jet_in[3] = 0.4127 / p.gamma1 + 0.5 * (p.jet_in[1] * p.jet_in[1]) / p.jet_in[0];
+        p.jet_amb[0] = 0.5;
+        p.jet_amb[1] = 0.;
+        p.jet_amb[2] = 0.;
+        p.jet_amb[3] = 0.4127 / p.gamma1;
+      }
+      if (p.dt_rule == 4) {
+        p.dt_num_x = p.dx * c.cfl;
+        p.dt_num_y = p.dy * c.cfl;
+      }
+      break;
+    }
+    default:
+      err = "unknown problem";
+      return SWFD_ERR_INVALID;
+  }
+  g.pitch = ((g.LI + 31) / 32) * 32;
+  g.plane = (int64_t)g.pitch * g.LJ;
+  return SWFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// initial data on the host (same libm as the reference's gfortran runtime)
+// ---------------------------------------------------------------------------
+inline double sqd(double a) { return a * a; }
+
+// exact (ex3_vortex_accuracy_2d/main.f90:699-718)
+void vortex_exact(double g1, double gamma, double x, double y, double t, double* e) {
+  const double pi = 3.14159265358979323846264338327950;
+  double r = sqrt(sqd(x - 5. - t) + sqd(y - 5. - t));
+  double mag = 10.0828;
+  e[0] = pow(1 - g1 * (mag * mag) / 8. / gamma / (pi * pi) * exp(1. - r * r), 1. / g1);
+  e[1] = e[0] * (1. - mag / 2. / pi * exp((1. - r * r) / 2.) * (y - 5.));
+  e[2] = e[0] * (1. + mag / 2. / pi * exp((1. - r * r) / 2.) * (x - 5.));
+  e[3] = pow(e[0], gamma) / g1 + 0.5 * (e[1] * e[1]) / e[0] + 0.5 * (e[2] * e[2]) / e[0];
+}
+
+// Fortran-layout initial state, ghosts included (bc is applied on the device)
+void init_host(const swfd_handle* h, double* u) {
+  const Params& p = h->p;
+  const Geom& g = p.g;
+  const int nx = g.nx, ny = g.ny, nc = g.nc, LI = g.LI;
+  auto U = [&](int c, int i, int j) -> double& {
+    return u[(size_t)c + (size_t)nc * ((size_t)(i + 2) + (size_t)LI * (size_t)(j + 2))];
+  };
+  std::fill(u, u + host_len(p), 0.0);
+  switch (p.problem) {
+    case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:405-428
+      for (int i = -2; i <= nx + 3; ++i) {
+        U(0, i, -2) = 1.;
+        U(1, i, -2) = 0.;
+        U(2, i, -2) = h->cfg.e_background;
+      }
+      U(2, nx / 2 + 1, -2) = h->cfg.e_blast / p.dx;
+      break;
+    case SWFD_PROBLEM_VORTEX_2D:  // ex3_vortex_accuracy_2d/main.f90:683-694
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          double x = 0. + i * p.dx - p.dx / 2., y = 0. + j * p.dy - p.dy / 2., e[4];
+          vortex_exact(p.gamma1, p.gamma, x, y, 0., e);
+          for (int c = 0; c < 4; ++c) U(c, i, j) = e[c];
+        }
+      break;
+    case SWFD_PROBLEM_SEDOV_2D:  // ex4_sedov_2d/main.f90:1170-1186
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(0, i, j) = 1;
+          U(3, i, j) = h->cfg.e_background;
+        }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double gx = 0. + p.dx * (i - 0.5), gy = 0. + p.dy * (j - 0.5);
+          if (fabs(gx - 0.0) <= p.dx / 2.0 && fabs(gy - 0.0) <= p.dy / 2.0)
+            U(3, i, j) = h->cfg.e_blast / (p.dx * p.dy);
+        }
+      break;
+    case SWFD_PROBLEM_JET_2D:  // ex5_mach2000_jet/main.f90:763-765
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(0, i, j) = 0.5;
+          U(3, i, j) = 0.4127 / p.gamma1;
+        }
+      break;
+  }
+}
+
+double* cur_state(swfd_handle* h) { return h->st[h->cur]; }
+
+swfd_status sync_scalars(swfd_handle* h) {
+  CU(h, cudaMemcpyAsync(h->hsc, h->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status check_device_error(swfd_handle* h) {
+  ST(sync_scalars(h));
+  if (h->hsc->error) {
+    int e = h->hsc->error;
+    h->hsc->error = 0;
+    CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
+    return fail(h, SWFD_ERR_NONFINITE,
+                std::string("non-finite ") + ((e & 1) ? "alphamax" : "dt") + " on the device");
+  }
+  return SWFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sweep_lim (ex3_vortex_accuracy_2d/main.f90:888-1137; 1D ex2_sedov_1d/main.f90:564-726;
+// ex4 P(u_bar) check :1447-1454 and stop :1747-1752; ex5 `>=` exit :1162)
+// ---------------------------------------------------------------------------
+swfd_status sweep_lim(swfd_handle* h, double* u) {
+  const Params& p = h->p;
+  cudaStream_t s = h->stream;
+  // density sweep
+  if (p.g.ndim == 1) {
+    CU(h, launch_density_sweep(p, u, s));
+    h->den_count++;
+  } else {
+    CU(h, launch_rho_min(p, u, h->dsc, s));
+    ST(sync_scalars(h));
+    unsigned long long k = h->hsc->rho_min_key;
+    unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    double rho_min;
+    memcpy(&rho_min, &b, sizeof(double));
+    if (rho_min < 1e-12) {
+      CU(h, launch_density_sweep(p, u, s));
+      h->den_count++;
+    }
+  }
+  CU(h, launch_ubar(p, u, h->dsc, s));
+  if (p.problem == SWFD_PROBLEM_SEDOV_2D) {
+    ST(sync_scalars(h));
+    const double* ub = h->hsc->ubar;
+    if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.)
+      return fail(h, SWFD_ERR_PUBAR_NONPOS, "P(u_bar) <= 0");
+  }
+  h->sweep_count++;
+  h->sweep_track.push_back(0);
+  h->neg_track.push_back(0);
+  h->pos_track.push_back(0);
+  CU(h, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
+  for (int q = 1; q <= h->cfg.swp_num; ++q) {
+    int ord = (q % 2 == 1) ? 1 : 2;
+    CU(h, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
+    CU(h, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
+    CU(h, launch_exit_count(p, u, h->dsc, s));
+    ST(sync_scalars(h));
+    h->pre_count++;
+    if (h->hsc->bad_count == 0) {
+      h->sweep_track.back() = q;
+      h->neg_track.back() = (int32_t)h->hsc->t_neg;
+      h->pos_track.back() = (int32_t)h->hsc->t_pos;
+      break;
+    }
+    if (q == h->cfg.swp_num) {
+      h->fail_count++;
+      if (p.problem == SWFD_PROBLEM_SEDOV_2D)
+        return fail(h, SWFD_ERR_SWEEP_NOCONV, "SWEEP FAIL: swp_num reached");
+    }
+  }
+  return SWFD_OK;
+}
+
+// one RK stage: findalpha, [dt], LF split, WENO fluxes, RHS + RK combination +
+// checkpositivity, [sweep], bc
+swfd_status stage(swfd_handle* h, int k, double* in, double* u0, double* out) {
+  const Params& p = h->p;
+  cudaStream_t s = h->stream;
+  CU(h, launch_alpha(p, in, h->dsc, s));
+  if (k == 1) CU(h, launch_dt(p, h->dsc, s));
+  CU(h, launch_prep(p, in, h->dsc, h->split, h->roe, s));
+  CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
+  CU(h, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
+  if (h->cfg.use_limiter == 2) {
+    ST(sync_scalars(h));
+    if (h->hsc->postag) ST(sweep_lim(h, out));
+  }
+  CU(h, launch_bc(p, out, s));
+  return SWFD_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* swfd_status_string(swfd_status s) {
+  switch (s) {
+    case SWFD_OK: return "ok";
+    case SWFD_ERR_INVALID: return "invalid argument";
+    case SWFD_ERR_CUDA: return "CUDA error";
+    case SWFD_ERR_SWEEP_NOCONV: return "sweep did not converge within swp_num";
+    case SWFD_ERR_PUBAR_NONPOS: return "P(u_bar) <= 0";
+    case SWFD_ERR_NONFINITE: return "non-finite alpha or dt";
+    case SWFD_ERR_OOM: return "device allocation failed";
+    case SWFD_ERR_TIMEOUT: return "device-side wait timed out";
+    case SWFD_ERR_UNSUPPORTED: return "unsupported option";
+    case SWFD_ERR_MAX_STEPS: return "step limit reached";
+    default: return "unknown status";
+  }
+}
+
+swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
+  if (!cfg) return fail(nullptr, SWFD_ERR_INVALID, "cfg is NULL");
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->abi_version = SWFD_ABI_VERSION;
+  cfg->problem = problem;
+  cfg->use_limiter = 2;
+  cfg->swp_num = 20000;
+  cfg->literals = SWFD_LITERALS_DOUBLE;
+  cfg->precision = SWFD_PRECISION_FP64;
+  cfg->ubar_mode = SWFD_UBAR_SEQUENTIAL;
+  cfg->device = 0;
+  cfg->gamma = 1.4;
+  switch (problem) {
+    case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:4-7,423-425
+      cfg->nx = 800;
+      cfg->ny = 1;
+      cfg->swp_num = 50;
+      cfg->cfl = 1.2;
+      cfg->time_terminal = 0.001;
+      cfg->e_background = 1e-9 / (1.4 - 1.);
+      cfg->e_blast = 3200000.0;
+      break;
+    case SWFD_PROBLEM_VORTEX_2D:  // ex3_vortex_accuracy_2d/main.f90:5-7,570
+      cfg->nx = cfg->ny = 180;
+      cfg->cfl = 0.5;
+      cfg->time_terminal = 0.01;
+      break;
+    case SWFD_PROBLEM_SEDOV_2D:  // ex4_sedov_2d/main.f90:18-20,687,1172,1182
+      cfg->nx = cfg->ny = 640;
+      cfg->cfl = 0.5;
+      cfg->time_terminal = 1;
+      cfg->e_background = 1e-12;
+      cfg->e_blast = 0.244816;
+      break;
+    case SWFD_PROBLEM_JET_2D:  // ex5_mach2000_jet/main.f90:4-6,597
+      cfg->nx = 800;
+      cfg->ny = 200;
+      cfg->cfl = 1. / 4.;
+      cfg->time_terminal = 0.001;
+      cfg->gamma = 5. / 3.;
+      break;
+    default:
+      return fail(nullptr, SWFD_ERR_INVALID, "unknown problem");
+  }
+  return SWFD_OK;
+}
+
+swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
+  if (!cfg || !out) return fail(nullptr, SWFD_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (cfg->abi_version != SWFD_ABI_VERSION)
+    return fail(nullptr, SWFD_ERR_INVALID, "abi_version mismatch");
+  if (cfg->literals != SWFD_LITERALS_DOUBLE)
+    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
+  if (cfg->precision != SWFD_PRECISION_FP64)
+    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "precision: only SWFD_PRECISION_FP64 is built");
+  if (cfg->use_limiter != 0 && cfg->use_limiter != 2)
+    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "use_limiter must be 0 or 2");
+  if (cfg->ubar_mode != SWFD_UBAR_SEQUENTIAL)
+    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "ubar_mode: only sequential is built");
+  if (cfg->swp_num < 1) return fail(nullptr, SWFD_ERR_INVALID, "swp_num must be >= 1");
+  if (!(cfg->gamma > 1.0)) return fail(nullptr, SWFD_ERR_INVALID, "gamma must be > 1");
+  swfd_handle* h = new swfd_handle();
+  h->cfg = *cfg;
+  std::string err;
+  swfd_status st = make_params(*cfg, h->p, err);
+  if (st != SWFD_OK) {
+    delete h;
+    return fail(nullptr, st, err);
+  }
+  h->device = cfg->device;
+  const Geom& g = h->p.g;
+  auto cleanup_fail = [&](cudaError_t e) {
+    std::string m = std::string("swfd_create: ") + cudaGetErrorString(e);
+    swfd_destroy(h);
+    return fail(nullptr, e == cudaErrorMemoryAllocation ? SWFD_ERR_OOM : SWFD_ERR_CUDA, m);
+  };
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return cleanup_fail(e);
+  const size_t pb = (size_t)g.plane * sizeof(double);
+  for (int k = 0; k < 3; ++k)
+    if ((e = cudaMalloc(&h->st[k], g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->split, 4 * g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->roe, 8 * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->flux, 4 * g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->rhs_tmp, g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->dsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMallocHost(&h->hsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
+  const size_t hb = (size_t)host_len(h->p) * sizeof(double);
+  if ((e = cudaMalloc(&h->d_stage, hb)) != cudaSuccess) return cleanup_fail(e);
+  for (int k = 0; k < 3; ++k)
+    if ((e = cudaMemsetAsync(h->st[k], 0, g.nc * pb, h->stream)) != cudaSuccess)
+      return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->split, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->roe, 0, 8 * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->flux, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->dsc, 0, sizeof(DevScalars), h->stream)) != cudaSuccess)
+    return cleanup_fail(e);
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cleanup_fail(e);
+  *out = h;
+  return SWFD_OK;
+}
+
+swfd_status swfd_destroy(swfd_handle* h) {
+  if (!h) return SWFD_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int k = 0; k < 3; ++k) cudaFree(h->st[k]);
+  cudaFree(h->split);
+  cudaFree(h->roe);
+  cudaFree(h->flux);
+  cudaFree(h->rhs_tmp);
+  cudaFree(h->dsc);
+  cudaFree(h->d_stage);
+  if (h->hsc) cudaFreeHost(h->hsc);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SWFD_OK;
+}
+
+swfd_status swfd_upload_state(swfd_handle* h, const double* u) {
+  if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  const size_t hb = (size_t)host_len(h->p) * sizeof(double);
+  CU(h, cudaMemcpyAsync(h->d_stage, u, hb, cudaMemcpyHostToDevice, h->stream));
+  CU(h, launch_fortran_to_soa(h->p, h->d_stage, cur_state(h), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status swfd_download_state(swfd_handle* h, double* u) {
+  if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  const size_t hb = (size_t)host_len(h->p) * sizeof(double);
+  CU(h, launch_soa_to_fortran(h->p, cur_state(h), h->d_stage, h->stream));
+  CU(h, cudaMemcpyAsync(u, h->d_stage, hb, cudaMemcpyDeviceToHost, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status swfd_init_problem(swfd_handle* h) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  std::vector<double> u((size_t)host_len(h->p));
+  init_host(h, u.data());
+  ST(swfd_upload_state(h, u.data()));
+  CU(h, launch_bc(h->p, cur_state(h), h->stream));
+  h->time = 0;
+  h->sweep_count = h->den_count = h->pre_count = h->fail_count = 0;
+  h->sweep_track.clear();
+  h->neg_track.clear();
+  h->pos_track.clear();
+  CU(h, cudaMemsetAsync(h->dsc, 0, sizeof(DevScalars), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status swfd_get_time(swfd_handle* h, double* t) {
+  if (!h || !t) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  *t = h->time;
+  return SWFD_OK;
+}
+
+swfd_status swfd_set_time(swfd_handle* h, double t) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  CU(h, cudaSetDevice(h->device));
+  h->time = t;
+  CU(h, cudaMemcpyAsync(&h->dsc->time, &h->time, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status swfd_step(swfd_handle* h, double* dt_out) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  CU(h, cudaSetDevice(h->device));
+  double* X = h->st[h->cur];
+  double* Y = h->st[(h->cur + 1) % 3];
+  double* Z = h->st[(h->cur + 2) % 3];
+  ST(stage(h, 1, X, X, Y));
+  ST(stage(h, 2, Y, X, Z));
+  ST(stage(h, 3, Z, X, X));
+  CU(h, launch_time_advance(h->dsc, h->stream));
+  ST(check_device_error(h));
+  h->time = h->hsc->time;
+  if (dt_out) *dt_out = h->hsc->dt;
+  return SWFD_OK;
+}
+
+swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  int64_t k = 0;
+  // DO WHILE (time <= time_terminal - 1d-10)  (ex3_vortex_accuracy_2d/main.f90:51)
+  while (h->time <= h->cfg.time_terminal - 1e-10) {
+    if (max_steps > 0 && k >= max_steps) {
+      if (nsteps_out) *nsteps_out = k;
+      return SWFD_ERR_MAX_STEPS;
+    }
+    swfd_status st = swfd_step(h, nullptr);
+    if (st != SWFD_OK) {
+      if (nsteps_out) *nsteps_out = k;
+      return st;
+    }
+    ++k;
+  }
+  if (nsteps_out) *nsteps_out = k;
+  return SWFD_OK;
+}
+
+swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
+  if (!h || !rhs) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  const Params& p = h->p;
+  double* u = cur_state(h);
+  CU(h, launch_alpha(p, u, h->dsc, h->stream));
+  CU(h, launch_prep(p, u, h->dsc, h->split, h->roe, h->stream));
+  CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? u : h->roe, h->dsc, h->flux, h->stream));
+  CU(h, launch_rhs(p, h->flux, h->dsc, h->rhs_tmp, h->stream));
+  const size_t hb = (size_t)host_len(p) * sizeof(double);
+  CU(h, launch_soa_to_fortran(p, h->rhs_tmp, h->d_stage, h->stream));
+  CU(h, cudaMemcpyAsync(rhs, h->d_stage, hb, cudaMemcpyDeviceToHost, h->stream));
+  ST(check_device_error(h));
+  return SWFD_OK;
+}
+
+swfd_status swfd_sweep(swfd_handle* h) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  CU(h, cudaSetDevice(h->device));
+  ST(sweep_lim(h, cur_state(h)));
+  CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
+  if (!h || !postag) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  CU(h, launch_positivity(h->p, cur_state(h), h->dsc, h->stream));
+  ST(sync_scalars(h));
+  *postag = h->hsc->postag;
+  return SWFD_OK;
+}
+
+swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax) {
+  if (!h || !alphamax) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  CU(h, launch_alpha(h->p, cur_state(h), h->dsc, h->stream));
+  ST(sync_scalars(h));
+  *alphamax = h->hsc->alphamax;
+  return SWFD_OK;
+}
+
+swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
+  if (!h || !s) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  memset(s, 0, sizeof(*s));
+  s->sweep_count = h->sweep_count;
+  for (size_t k = 0; k < h->sweep_track.size(); ++k) {
+    s->total_sweep += h->sweep_track[k];
+    s->total_neg += h->neg_track[k];
+    s->total_pos += h->pos_track[k];
+    if (k == 0 || h->sweep_track[k] > s->max_sweep) s->max_sweep = h->sweep_track[k];
+    if (k == 0 || h->neg_track[k] > s->max_neg) s->max_neg = h->neg_track[k];
+    if (k == 0 || h->pos_track[k] > s->max_pos) s->max_pos = h->pos_track[k];
+  }
+  s->den_count = h->den_count;
+  s->pre_count = h->pre_count;
+  s->sweep_fail_count = h->fail_count;
+  return SWFD_OK;
+}
+
+swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos,
+                                  int64_t cap, int64_t* count) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  int64_t n = (int64_t)h->sweep_track.size();
+  int64_t m = std::min<int64_t>(n, std::max<int64_t>(cap, 0));
+  for (int64_t k = 0; k < m; ++k) {
+    if (sweep) sweep[k] = h->sweep_track[k];
+    if (neg) neg[k] = h->neg_track[k];
+    if (pos) pos[k] = h->pos_track[k];
+  }
+  if (count) *count = n;
+  return SWFD_OK;
+}
+
+swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps, int32_t literals,
+                             int32_t device, double* uleft, double* uright) {
+  if (n < 0 || (n > 0 && !stencils)) return fail(nullptr, SWFD_ERR_INVALID, "bad arguments");
+  if (literals != SWFD_LITERALS_DOUBLE)
+    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
+  if (n == 0) return SWFD_OK;
+  CU(nullptr, cudaSetDevice(device));
+  double *ds = nullptr, *dl = nullptr, *dr = nullptr;
+  cudaStream_t s = nullptr;
+  auto done = [&](swfd_status st) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(ds);
+    cudaFree(dl);
+    cudaFree(dr);
+    if (s) cudaStreamDestroy(s);
+    return st;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&ds, 5 * n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&dl, n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&dr, n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMemcpyAsync(ds, stencils, 5 * n * sizeof(double), cudaMemcpyHostToDevice, s)) !=
+          cudaSuccess ||
+      (e = launch_weno_batch(ds, n, weno_eps, dl, dr, s)) != cudaSuccess ||
+      (uleft && (e = cudaMemcpyAsync(uleft, dl, n * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
+                    cudaSuccess) ||
+      (uright && (e = cudaMemcpyAsync(uright, dr, n * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
+                     cudaSuccess) ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return done(fail(nullptr, SWFD_ERR_CUDA, std::string("swfd_weno5_batch: ") + cudaGetErrorString(e)));
+  return done(SWFD_OK);
+}
+
+swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len) {
+  if (!buf || len == 0) return SWFD_ERR_INVALID;
+  const std::string& m = h ? h->last_error : g_last_error;
+  snprintf(buf, len, "%s", m.c_str());
+  return SWFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// swfd_internal.h -- shared declarations of the CUDA library (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/swfd.h"
+
+namespace swfd {
+
+// Device layout: structure-of-arrays planes.  Plane c holds component c of
+// every cell (i, j), i in [-2, nx+3], j in [-2, ny+3], at offset
+// (i + 2) + pitch * (j + 2).  pitch is nx + 6 rounded up to 32 doubles so
+// that every row starts on a 256-byte boundary.  1D problems use one row.
+struct Geom {
+  int ndim = 2;
+  int nc = 4;      // conserved components
+  int nx = 0, ny = 1;
+  int LI = 0, LJ = 0;  // nx + 6, ny + 6 (1 in 1D)
+  int pitch = 0;
+  int64_t plane = 0;   // doubles per plane
+  __host__ __device__ int64_t at(int i, int j) const {
+    return (int64_t)(i + 2) + (int64_t)pitch * (int64_t)(j + 2);
+  }
+};
+
+// Per-problem switches of the reference's variant matrix, resolved on the
+// host once and passed to every kernel by value.
+struct Params {
+  Geom g;
+  int problem = 0;
+  int literals = 0;
+  int pos_strict = 0;    // checkpositivity uses `<` (ex4, ex5)
+  int exit_ge = 0;       // sweep exit test uses `>=` (ex5)
+  int alpha_guarded = 0; // findalpha with the eps2 velocity guard (ex4, ex5)
+  int flux_guard_eps2 = 0;  // fflux guard `rho < eps2` (ex4) instead of 1d-8
+  int roe_reg_ex4 = 0;   // 1d-15 Roe regularisers and y-pass 1/(den+1d-15)
+  int alpha_premul = 0;  // fluxes scaled by alpha inside wenofd (ex4)
+  int dt_rule = 0;       // 1: dx*cfl/a; 3: dx**(5/3)*cfl/a; 4: min(dx,dy)*cfl/a clamped
+  double gamma = 1.4, gamma1 = 0.4, eps = 1e-13, eps2 = 1e-8, weno_eps = 1e-6;
+  double dx = 0, dy = 0;
+  double dt_num_x = 0;   // dx*cfl   (or dx**(5/3)*cfl for dt_rule 3)
+  double dt_num_y = 0;   // dy*cfl
+  double time_terminal = 0;
+  // jet inflow (ex5_mach2000_jet/main.f90:702-719)
+  int jet_jmax = 0;      // y(j) <= 0.05  <=>  j <= jet_jmax
+  double jet_in[4] = {0, 0, 0, 0};
+  double jet_amb[4] = {0, 0, 0, 0};
+};
+
+// Device scalars of one handle, in one small allocation.
+struct DevScalars {
+  double alphamax;
+  double dt;
+  double time;
+  double ubar[4];
+  double pmin;           // unused by the flag-count exit test, kept for stats
+  unsigned long long alpha_bits;
+  unsigned long long rho_min_key;
+  int postag;
+  int bad_count;         // cells failing the sweep exit test
+  int error;
+  int pad;
+  long long t_pos, t_neg;
+};
+
+}  // namespace swfd
+
+struct swfd_handle {
+  swfd_config cfg;
+  swfd::Params p;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // state buffers (3 rotating states of nc planes each)
+  double* st[3] = {nullptr, nullptr, nullptr};
+  int cur = 0;  // index of the current state buffer
+  // scratch planes
+  double* split = nullptr;  // fp, fn (x) and gp, gn (y): 4*nc planes
+  double* roe = nullptr;    // w, vx, vy, h for x (4 planes) and y (4 planes)
+  double* flux = nullptr;   // fp_flux, fn_flux, gp_flux, gn_flux: 4*nc planes
+  double* rhs_tmp = nullptr;  // nc planes (flux_divergence output)
+  double* sweep_tmp = nullptr;  // nc planes (host I/O staging)
+  swfd::DevScalars* dsc = nullptr;   // device scalars
+  swfd::DevScalars* hsc = nullptr;   // pinned host mirror
+  // host-side run state
+  double time = 0;
+  int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;
+  std::vector<int32_t> sweep_track, neg_track, pos_track;
+  std::string last_error;
+  // host staging for layout conversion
+  double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
+  double* d_stage = nullptr;  // device, nc * LI * LJ doubles
+};
+
+namespace swfd {
+
+// kernels.cu
+cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
+cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, double* split,
+                        double* roe, cudaStream_t s);
+cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
+                        const DevScalars* dsc, double* flux, cudaStream_t s);
+cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
+                      const double* flux, const DevScalars* dsc, double* out, cudaStream_t s);
+cudaError_t launch_rhs(const Params& p, const double* flux, const DevScalars* dsc, double* rhs,
+                       cudaStream_t s);
+cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
+                              cudaStream_t s);
+
+// sweep.cu
+cudaError_t launch_rho_min(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_density_sweep(const Params& p, double* u, cudaStream_t s);
+cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int forward,
+                                 DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+
+}  // namespace swfd

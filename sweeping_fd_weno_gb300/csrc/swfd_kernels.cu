@@ -1,0 +1,615 @@
+// swfd_kernels.cu -- boundary conditions, CFL reduction, LF splitting, the
+// characteristic WENO5 interface fluxes and the fused RHS + SSP-RK3 update.
+#include "swfd_device.cuh"
+
+namespace swfd {
+
+#define SWFD_BLOCK 256
+
+__device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
+
+// ---------------------------------------------------------------------------
+// bc: every ghost cell gets its final value directly, resolved through the
+// order in which the reference applies its loops (the order defines the
+// corner ghosts).
+// ---------------------------------------------------------------------------
+__global__ void k_bc2d(Params p, double* __restrict__ u) {
+  const Geom& g = p.g;
+  const int nx = g.nx, ny = g.ny;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  if (t >= ncell) return;
+  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  bool gi = (i < 1 || i > nx), gj = (j < 1 || j > ny);
+  if (!gi && !gj) return;
+  double v[4];
+  int si = i, sj = j;
+  double sgn[4] = {1., 1., 1., 1.};
+  bool fixed = false;
+  if (p.problem == SWFD_PROBLEM_VORTEX_2D) {
+    // ex3_vortex_accuracy_2d/main.f90:653-669: x wrap for all rows, then y
+    // wrap for all columns -> fully periodic
+    si = i < 1 ? i + nx : (i > nx ? i - nx : i);
+    sj = j < 1 ? j + ny : (j > ny ? j - ny : j);
+  } else {
+    // ex4_sedov_2d/main.f90:922-994, ex5_mach2000_jet/main.f90:702-738:
+    // left (reflect / inflow) for all rows, bottom reflect for all columns,
+    // right outflow for all rows, top outflow for all columns.
+    const bool jet = (p.problem == SWFD_PROBLEM_JET_2D);
+    int ii = i, jj = j;
+    if (jj > ny) jj = ny;             // top outflow copies row ny
+    if (ii > nx) ii = nx;             // right outflow copies column nx
+    if (jj < 1) {                     // bottom reflect of row 1-j
+      jj = 1 - jj;
+      sgn[2] = -1.;
+    }
+    if (ii < 1) {
+      if (jet) {
+        // inflow state of row jj, then (if jj came from the bottom) mirrored
+        const double* s = (jj <= p.jet_jmax) ? p.jet_in : p.jet_amb;
+        for (int c = 0; c < 4; ++c) v[c] = s[c];
+        fixed = true;
+      } else {
+        ii = 1 - ii;                  // left reflect
+        sgn[1] = -1.;
+      }
+    }
+    si = ii;
+    sj = jj;
+  }
+  if (!fixed)
+    for (int c = 0; c < 4; ++c) v[c] = u[c * g.plane + g.at(si, sj)];
+  const int64_t o = g.at(i, j);
+  for (int c = 0; c < 4; ++c) u[c * g.plane + o] = (sgn[c] < 0.) ? -v[c] : v[c];
+}
+
+cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s) {
+  if (p.g.ndim == 1) return cudaSuccess;  // ex2_sedov_1d/main.f90:394-403 is empty
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  k_bc2d<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// findalpha: max over all cells including ghosts
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_max(double v) {
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
+__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  double a = 0.0;
+  if (t < ncell) {
+    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    int64_t o = g.at(i, j);
+    const double g1 = p.gamma1, gamma = p.gamma;
+    if (g.ndim == 1) {
+      // ex2_sedov_1d/main.f90:278-283
+      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o);
+      double pres = g1 * (u3 - u2 * u2 / u1 / 2.);
+      double sound = sqrt(gamma * pres / u1);
+      a = fabs(u2 / u1) + sound;
+    } else {
+      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
+             u4 = ld(u + 3 * g.plane + o);
+      if (!p.alpha_guarded) {
+        // ex3_vortex_accuracy_2d/main.f90:556-559
+        double pres = g1 * (u4 - u2 * u2 / u1 / 2. - u3 * u3 / u1 / 2.);
+        double sound = sqrt(gamma * pres / u1);
+        a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+      } else {
+        // ex5_mach2000_jet/main.f90:571-584
+        double vx = 0., vy = 0.;
+        if (u1 >= p.eps2) {
+          vx = u2 / u1;
+          vy = u3 / u1;
+        }
+        double pres = g1 * (u4 - 0.5 * u1 * (vx * vx) - 0.5 * u1 * (vy * vy));
+        double sound = sqrt(gamma * pres / u1);
+        a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+      }
+    }
+    a = fmax(0.0, a);
+  }
+  a = block_max(a);
+  if (threadIdx.x == 0) atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+}
+
+__global__ void k_alpha_final(DevScalars* dsc) {
+  dsc->alphamax = __longlong_as_double((long long)dsc->alpha_bits);
+  if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
+}
+
+cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(&dsc->alpha_bits, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  k_alpha<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc);
+  k_alpha_final<<<1, 1, 0, s>>>(dsc);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// dt rule, after the stage-1 findalpha
+// (ex2_sedov_1d/main.f90:293; ex3_vortex_accuracy_2d/main.f90:572;
+//  ex4_sedov_2d/main.f90:696-700; ex5_mach2000_jet/main.f90:601-605)
+// ---------------------------------------------------------------------------
+__global__ void k_dt(Params p, DevScalars* dsc) {
+  const double am = dsc->alphamax;
+  double dt;
+  if (p.dt_rule == 4) {
+    double dtx = p.dt_num_x / am, dty = p.dt_num_y / am;
+    double dtc = fmin(dtx, dty);
+    dt = fmin(dtc, p.time_terminal - dsc->time);
+  } else {
+    dt = p.dt_num_x / am;
+  }
+  dsc->dt = dt;
+  if (!isfinite(dt)) dsc->error |= 2;
+}
+
+cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s) {
+  k_dt<<<1, 1, 0, s>>>(p, dsc);
+  return cudaGetLastError();
+}
+
+__global__ void k_time_advance(DevScalars* dsc) { dsc->time = dsc->time + dsc->dt; }
+
+cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s) {
+  k_time_advance<<<1, 1, 0, s>>>(dsc);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Lax-Friedrichs splitting + Roe preparation, one thread per cell
+// (ex3_vortex_accuracy_2d/main.f90:61-131,134-147,335-348)
+// split planes: [0,nc) fp, [nc,2nc) fn, [2nc,3nc) gp, [3nc,4nc) gn
+// roe planes:   0 w, 1 vx, 2 vy, 3 h (x pass); 4..7 the y pass (ex4 only)
+// ---------------------------------------------------------------------------
+__global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalars* dsc,
+                         double* __restrict__ split, double* __restrict__ roe) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  if (t >= ncell) return;
+  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  const int64_t o = g.at(i, j), P = g.plane;
+  const double am = dsc->alphamax, g1 = p.gamma1;
+  double rho = ld(u + o), mx = ld(u + P + o), my = ld(u + 2 * P + o), e = ld(u + 3 * P + o);
+  // fflux / gflux
+  double vx = mx / rho, vy = my / rho;
+  bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
+  if (guard) {
+    vx = 0.;
+    vy = 0.;
+  }
+  double pres = g1 * (e - 0.5 * rho * (vx * vx) - 0.5 * rho * (vy * vy));
+  double fxy = rho * vx * vy;
+  double f1 = rho * (vx * vx) + pres, f3 = (e + pres) * vx;
+  double g2 = rho * (vy * vy) + pres, g3 = (e + pres) * vy;
+  // fp = 0.5*(u + f/alpha), fn = 0.5*(u - f/alpha); f/alpha shared by both
+  double q;
+  q = mx / am;  split[0 * P + o] = 0.5 * (rho + q); split[4 * P + o] = 0.5 * (rho - q);
+  q = f1 / am;  split[1 * P + o] = 0.5 * (mx + q);  split[5 * P + o] = 0.5 * (mx - q);
+  double qxy = fxy / am;
+  split[2 * P + o] = 0.5 * (my + qxy); split[6 * P + o] = 0.5 * (my - qxy);
+  q = f3 / am;  split[3 * P + o] = 0.5 * (e + q);   split[7 * P + o] = 0.5 * (e - q);
+  q = my / am;  split[8 * P + o] = 0.5 * (rho + q); split[12 * P + o] = 0.5 * (rho - q);
+  split[9 * P + o] = 0.5 * (mx + qxy); split[13 * P + o] = 0.5 * (mx - qxy);
+  q = g2 / am;  split[10 * P + o] = 0.5 * (my + q); split[14 * P + o] = 0.5 * (my - q);
+  q = g3 / am;  split[11 * P + o] = 0.5 * (e + q);  split[15 * P + o] = 0.5 * (e - q);
+  // Roe preparation (x pass; the y pass is the same except in ex4)
+  double t0 = 1. / rho;
+  double vex = mx * t0, vey = my * t0;
+  double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+  double w = sqrt(fabs(rho));
+  roe[0 * P + o] = w;
+  roe[1 * P + o] = vex;
+  roe[2 * P + o] = vey;
+  roe[3 * P + o] = (pre + e) * t0;
+  if (p.roe_reg_ex4) {
+    // ex4_sedov_2d/main.f90:426
+    t0 = 1. / (rho + 1e-15);
+    vex = mx * t0;
+    vey = my * t0;
+    pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+    roe[4 * P + o] = w;
+    roe[5 * P + o] = vex;
+    roe[6 * P + o] = vey;
+    roe[7 * P + o] = (pre + e) * t0;
+  }
+}
+
+__global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalars* dsc,
+                         double* __restrict__ split) {
+  const Geom& g = p.g;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.LI) return;
+  const int64_t o = t, P = g.plane;
+  const double am = dsc->alphamax, g1 = p.gamma1;
+  double rho = ld(u + o), mx = ld(u + P + o), e = ld(u + 2 * P + o);
+  // fflux (ex2_sedov_1d/main.f90:57-73)
+  double vx = 0.;
+  if (rho > 1e-8) vx = mx / rho;
+  if (rho <= 1e-8) vx = 0.;
+  double pres = g1 * (e - 0.5 * rho * (vx * vx));
+  double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
+  double a[3] = {rho, mx, e};
+  for (int c = 0; c < 3; ++c) {
+    double q = f[c] / am;
+    split[c * P + o] = 0.5 * (a[c] + q);
+    split[(3 + c) * P + o] = 0.5 * (a[c] - q);
+  }
+}
+
+cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, double* split,
+                        double* roe, cudaStream_t s) {
+  if (p.g.ndim == 1) {
+    k_prep1d<<<(p.g.LI + SWFD_BLOCK - 1) / SWFD_BLOCK, SWFD_BLOCK, 0, s>>>(p, u, dsc, split);
+  } else {
+    int64_t n = (int64_t)p.g.LI * p.g.LJ;
+    k_prep2d<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc, split,
+                                                                                 roe);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// characteristic WENO5 flux of one interface (x: i+1/2 of row j; y: j+1/2 of
+// column i).  sp/sn point at stencil cell -2, component 0 of the positive /
+// negative split flux; components are P apart, stencil cells `step` apart.
+// ---------------------------------------------------------------------------
+template <int YDIR>
+__device__ __forceinline__ void interface_flux(const Eigen2D& E, const double* __restrict__ sp,
+                                               const double* __restrict__ sn, int64_t P,
+                                               int64_t step, double weps, double outp[4],
+                                               double outn[4]) {
+  double ur[4], ul[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double cp[5], cn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double* a = sp + m * step;
+      const double* b = sn + m * step;
+      double a0 = ld(a), a1 = ld(a + P), a2 = ld(a + 2 * P), a3 = ld(a + 3 * P);
+      double b0 = ld(b), b1 = ld(b + P), b2 = ld(b + 2 * P), b3 = ld(b + 3 * P);
+      if (k == 0) {
+        cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, b0, b1, b2, b3);
+      } else if (k == 1) {
+        cp[m] = proj_row2<YDIR>(E.vt, a0, a1, a2);
+        cn[m] = proj_row2<YDIR>(E.vt, b0, b1, b2);
+      } else if (k == 2) {
+        cp[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, b0, b1, b2, b3);
+      } else {
+        cp[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, b0, b1, b2, b3);
+      }
+    }
+    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
+    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+  }
+  // evr . ur (main.f90:226-229): row 1 [1,0,1,1]; normal-momentum row
+  // [vn-c, 0, vn, vn+c]; tangential row [vt, 1, vt, vt]; energy row
+  // [H-vn c, vt, q, H+vn c]
+  const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
+  outp[0] = ur[0] + ur[2] + ur[3];
+  outn[0] = ul[0] + ul[2] + ul[3];
+  outp[n] = E.e_nm * ur[0] + E.vn * ur[2] + E.e_np * ur[3];
+  outn[n] = E.e_nm * ul[0] + E.vn * ul[2] + E.e_np * ul[3];
+  outp[tt] = E.vt * ur[0] + ur[1] + E.vt * ur[2] + E.vt * ur[3];
+  outn[tt] = E.vt * ul[0] + ul[1] + E.vt * ul[2] + E.vt * ul[3];
+  outp[3] = E.e_hm * ur[0] + E.vt * ur[1] + E.qm * ur[2] + E.e_hp * ur[3];
+  outn[3] = E.e_hm * ul[0] + E.vt * ul[1] + E.qm * ul[2] + E.e_hp * ul[3];
+}
+
+// x pass: interfaces i = 0..nx+1 of rows j = 1..ny (the rows the RHS uses)
+__global__ void __launch_bounds__(128) k_flux_x(Params p, const double* __restrict__ split,
+                                                const double* __restrict__ roe,
+                                                const DevScalars* dsc, double* __restrict__ flux) {
+  const Geom& g = p.g;
+  int li = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx+1
+  int j = blockIdx.y + 1;
+  if (li > g.nx + 1) return;
+  const int i = li;
+  const int64_t P = g.plane, o = g.at(i, j);
+  Eigen2D E;
+  roe_eigen2d(p.gamma1, 0, ld(roe + o), ld(roe + o + 1), ld(roe + P + o), ld(roe + P + o + 1),
+              ld(roe + 2 * P + o), ld(roe + 2 * P + o + 1), ld(roe + 3 * P + o),
+              ld(roe + 3 * P + o + 1), E);
+  double op[4], on[4];
+  interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, p.weno_eps, op, on);
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    flux[c * P + o] = p.alpha_premul ? am * op[c] : op[c];
+    flux[(4 + c) * P + o] = p.alpha_premul ? am * on[c] : on[c];
+  }
+}
+
+// y pass: interfaces j = 0..ny+1 of columns i = 1..nx
+__global__ void __launch_bounds__(128) k_flux_y(Params p, const double* __restrict__ split,
+                                                const double* __restrict__ roe,
+                                                const DevScalars* dsc, double* __restrict__ flux) {
+  const Geom& g = p.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  // 1..nx
+  int j = blockIdx.y;                                 // 0..ny+1
+  if (i > g.nx) return;
+  const int64_t P = g.plane, o = g.at(i, j), pit = g.pitch;
+  const double* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+  Eigen2D E;
+  roe_eigen2d(p.gamma1, 1, ld(r + o), ld(r + o + pit), ld(r + P + o), ld(r + P + o + pit),
+              ld(r + 2 * P + o), ld(r + 2 * P + o + pit), ld(r + 3 * P + o),
+              ld(r + 3 * P + o + pit), E);
+  double op[4], on[4];
+  interface_flux<1>(E, split + 8 * P + o - 2 * pit, split + 12 * P + o - 2 * pit, P, pit,
+                    p.weno_eps, op, on);
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    flux[(8 + c) * P + o] = p.alpha_premul ? am * op[c] : op[c];
+    flux[(12 + c) * P + o] = p.alpha_premul ? am * on[c] : on[c];
+  }
+}
+
+// 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157)
+__global__ void k_flux1d(Params p, const double* __restrict__ u, const double* __restrict__ split,
+                         double* __restrict__ flux) {
+  const Geom& g = p.g;
+  int m = blockIdx.x * blockDim.x + threadIdx.x;  // 0..n+1
+  if (m > g.nx + 1) return;
+  const int64_t P = g.plane, o = g.at(m, -2);
+  const double g1 = p.gamma1;
+  double u1 = ld(u + o), u2 = ld(u + P + o), u3 = ld(u + 2 * P + o);
+  double vxm = u2 / u1;
+  double hm = (g1 * (u3 - 0.5 * (u2 * u2) / u1) + u3) / u1;
+  double qm = 0.5 * vxm * vxm;
+  double cm = sqrt(g1 * (hm - qm));
+  double t0 = vxm * cm;
+  double r10 = vxm - cm, r12 = vxm + cm, r20 = hm - t0, r22 = hm + t0;
+  double rcm = 1. / cm;
+  double b1 = g1 * rcm * rcm;
+  double b2 = qm * b1;
+  t0 = vxm * rcm;
+  double t1 = b1 * vxm;
+  double t2 = 0.5 * b1;
+  double L[3][3] = {{0.5 * (b2 + t0), -0.5 * (t1 + rcm), t2},
+                    {1. - b2, t1, -b1},
+                    {0.5 * (b2 - t0), -0.5 * (t1 - rcm), t2}};
+  double ur[3], ul[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double cp[5], cn[5];
+#pragma unroll
+    for (int jj = 0; jj < 5; ++jj) {
+      const int64_t s = o + jj - 2;
+      cp[jj] = L[k][0] * ld(split + s) + L[k][1] * ld(split + P + s) + L[k][2] * ld(split + 2 * P + s);
+      cn[jj] = L[k][0] * ld(split + 3 * P + s) + L[k][1] * ld(split + 4 * P + s) +
+               L[k][2] * ld(split + 5 * P + s);
+    }
+    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], p.weno_eps);
+    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], p.weno_eps);
+  }
+  flux[o] = ur[0] + ur[1] + ur[2];
+  flux[P + o] = r10 * ur[0] + vxm * ur[1] + r12 * ur[2];
+  flux[2 * P + o] = r20 * ur[0] + qm * ur[1] + r22 * ur[2];
+  flux[3 * P + o] = ul[0] + ul[1] + ul[2];
+  flux[4 * P + o] = r10 * ul[0] + vxm * ul[1] + r12 * ul[2];
+  flux[5 * P + o] = r20 * ul[0] + qm * ul[1] + r22 * ul[2];
+}
+
+cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
+                        const DevScalars* dsc, double* flux, cudaStream_t s) {
+  const Geom& g = p.g;
+  if (g.ndim == 1) {
+    // the 1D eigenvectors come from the state, which the caller passes as roe
+    k_flux1d<<<(g.nx + 2 + 127) / 128, 128, 0, s>>>(p, roe, split, flux);
+    return cudaGetLastError();
+  }
+  dim3 bx(128), gx((g.nx + 2 + 127) / 128, g.ny);
+  k_flux_x<<<gx, bx, 0, s>>>(p, split, roe, dsc, flux);
+  dim3 gy((g.nx + 127) / 128, g.ny + 2);
+  k_flux_y<<<gy, bx, 0, s>>>(p, split, roe, dsc, flux);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// scheme + RK stage combination + checkpositivity, one thread per cell.
+// Whole-array update as in the reference (RHS = 0 in the ghosts):
+//   stage 1  u = u + dt*RHS                          (main.f90:587)
+//   stage 2  u = 0.75*u0 + 0.25*(u + dt*RHS)         (main.f90:604)
+//   stage 3  u = (u0 + 2*(u + dt*RHS))/3             (main.f90:621)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rhs2d(const Params& p, const double* __restrict__ flux, int c,
+                                        int64_t o, double am) {
+  const int64_t P = p.g.plane, pit = p.g.pitch;
+  const double* fpf = flux + c * P;
+  const double* fnf = flux + (4 + c) * P;
+  const double* gpf = flux + (8 + c) * P;
+  const double* gnf = flux + (12 + c) * P;
+  double A = (ld(fpf + o) - ld(fnf + o + 1)) - (ld(fpf + o - 1) - ld(fnf + o));
+  double B = (ld(gpf + o) - ld(gnf + o + pit)) - (ld(gpf + o - pit) - ld(gnf + o));
+  if (p.alpha_premul) return -A / p.dx - B / p.dy;  // ex4_sedov_2d/main.f90:644-645
+  return -(am * A) / p.dx - (am * B) / p.dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
+}
+
+__device__ __forceinline__ double rhs1d(const Params& p, const double* __restrict__ flux, int c,
+                                        int64_t o, double am) {
+  // flus(i) = alphamax*(hp_flux(i-1) - hn_flux(i)); RHS = -(flus(i+1)-flus(i))/dx
+  const int64_t P = p.g.plane;
+  const double* hp = flux + c * P;
+  const double* hn = flux + (3 + c) * P;
+  double fl_i = am * (ld(hp + o - 1) - ld(hn + o));
+  double fl_ip1 = am * (ld(hp + o) - ld(hn + o + 1));
+  return -(fl_ip1 - fl_i) / p.dx;
+}
+
+__device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
+
+// u0 may alias out (stage 3 writes the step-start buffer); each element of
+// u0 is read only by the thread that then writes it.
+__global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
+                     const double* __restrict__ flux, DevScalars* dsc, double* out) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  int bad = 0;
+  if (t < ncell) {
+    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    const int64_t o = g.at(i, j), P = g.plane;
+    bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
+    const double dt = dsc->dt, am = dsc->alphamax;
+    double nv[4];
+    for (int c = 0; c < g.nc; ++c) {
+      double r = 0.0;
+      if (interior) r = (g.ndim == 1) ? rhs1d(p, flux, c, o, am) : rhs2d(p, flux, c, o, am);
+      double v = ld(u + c * P + o) + dt * r;
+      if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
+      else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+      nv[c] = v;
+      out[c * P + o] = v;
+    }
+    if (interior) {
+      // checkpositivity (ex3_vortex_accuracy_2d/main.f90:640-647,
+      // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
+      double pe;
+      if (g.ndim == 1) pe = nv[2] - nv[1] * nv[1] / nv[0] / 2.;
+      else pe = nv[3] - nv[2] * nv[2] / nv[0] / 2. - nv[1] * nv[1] / nv[0] / 2.;
+      if (p.pos_strict) bad = (nv[0] < p.eps) || (pe < p.eps);
+      else bad = (nv[0] <= p.eps) || (pe <= p.eps);
+    }
+  }
+  if (block_or(bad) && threadIdx.x == 0) atomicOr(&dsc->postag, 1);
+}
+
+cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
+                      const double* flux, const DevScalars* dsc, double* out, cudaStream_t s) {
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  cudaError_t e = cudaMemsetAsync((void*)&dsc->postag, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_rk<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(
+      p, stage, u, u0, flux, const_cast<DevScalars*>(dsc), out);
+  return cudaGetLastError();
+}
+
+__global__ void k_rhs(Params p, const double* __restrict__ flux, const DevScalars* dsc,
+                      double* __restrict__ rhs) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  if (t >= ncell) return;
+  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  const int64_t o = g.at(i, j), P = g.plane;
+  bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
+  for (int c = 0; c < g.nc; ++c) {
+    double r = 0.0;
+    if (interior)
+      r = (g.ndim == 1) ? rhs1d(p, flux, c, o, dsc->alphamax) : rhs2d(p, flux, c, o, dsc->alphamax);
+    rhs[c * P + o] = r;
+  }
+}
+
+cudaError_t launch_rhs(const Params& p, const double* flux, const DevScalars* dsc, double* rhs,
+                       cudaStream_t s) {
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  k_rhs<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, flux, dsc, rhs);
+  return cudaGetLastError();
+}
+
+__global__ void k_positivity(Params p, const double* __restrict__ u, DevScalars* dsc) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  int bad = 0;
+  if (t < ncell) {
+    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    const int64_t o = g.at(i, j), P = g.plane;
+    bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
+    if (interior) {
+      double pe, r = ld(u + o);
+      if (g.ndim == 1) {
+        double m = ld(u + P + o);
+        pe = ld(u + 2 * P + o) - m * m / r / 2.;
+      } else {
+        double mx = ld(u + P + o), my = ld(u + 2 * P + o);
+        pe = ld(u + 3 * P + o) - my * my / r / 2. - mx * mx / r / 2.;
+      }
+      if (p.pos_strict) bad = (r < p.eps) || (pe < p.eps);
+      else bad = (r <= p.eps) || (pe <= p.eps);
+    }
+  }
+  if (block_or(bad) && threadIdx.x == 0) atomicOr(&dsc->postag, 1);
+}
+
+cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  cudaError_t e = cudaMemsetAsync(&dsc->postag, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_positivity<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// layout conversion between u(nc,-2:nx+3,-2:ny+3) and the SoA planes
+// ---------------------------------------------------------------------------
+__global__ void k_f2s(Params p, const double* __restrict__ src, double* __restrict__ dst) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  if (t >= ncell) return;
+  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  for (int c = 0; c < g.nc; ++c) dst[c * g.plane + g.at(i, j)] = src[t * g.nc + c];
+}
+__global__ void k_s2f(Params p, const double* __restrict__ src, double* __restrict__ dst) {
+  const Geom& g = p.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ncell = (int64_t)g.LI * g.LJ;
+  if (t >= ncell) return;
+  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  for (int c = 0; c < g.nc; ++c) dst[t * g.nc + c] = src[c * g.plane + g.at(i, j)];
+}
+cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* dst, cudaStream_t s) {
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  k_f2s<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* dst, cudaStream_t s) {
+  int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  k_s2f<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, src, dst);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// batch of scalar WENO5 reconstructions (the MODULE weno5 entry points)
+// ---------------------------------------------------------------------------
+__global__ void k_weno_batch(const double* __restrict__ st, int64_t n, double eps,
+                             double* __restrict__ ul, double* __restrict__ ur) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double* a = st + 5 * k;
+  if (ul) ul[k] = weno_left(a[0], a[1], a[2], a[3], a[4], eps);
+  if (ur) ur[k] = weno_right(a[0], a[1], a[2], a[3], a[4], eps);
+}
+cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_weno_batch<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(st, n, eps, ul,
+                                                                                  ur);
+  return cudaGetLastError();
+}
+
+}  // namespace swfd

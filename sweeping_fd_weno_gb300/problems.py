@@ -1,0 +1,64 @@
+"""Problem configurations: the reference examples' compile-time PARAMETERs and
+the benchmark workloads built on them.
+
+``reference_defaults`` restates the PARAMETER blocks of each example's
+main.f90; ``workload`` returns the named benchmark configurations (grid sizes,
+CFL, swp_num, final time) on synthetic initial data generated by the same
+initdata formulas.
+"""
+from __future__ import annotations
+
+from . import abi
+
+
+def reference_defaults(problem: int) -> dict:
+    """PARAMETERs of the reference example behind ``problem``."""
+    base = dict(abi_version=abi.ABI_VERSION, problem=problem, use_limiter=2, swp_num=20000,
+                literals=abi.LITERALS_DOUBLE, precision=abi.PRECISION_FP64,
+                ubar_mode=abi.UBAR_SEQUENTIAL, device=0, gamma=1.4, e_background=0.0,
+                e_blast=0.0, ny=1)
+    if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425
+        base.update(nx=800, ny=1, swp_num=50, cfl=1.2, time_terminal=0.001,
+                    e_background=1e-9 / (1.4 - 1.0), e_blast=3200000.0)
+    elif problem == abi.VORTEX_2D:   # ex3_vortex_accuracy_2d/main.f90:5-7,570
+        base.update(nx=180, ny=180, cfl=0.5, time_terminal=0.01)
+    elif problem == abi.SEDOV_2D:    # ex4_sedov_2d/main.f90:18-20,687,1172,1182
+        base.update(nx=640, ny=640, cfl=0.5, time_terminal=1.0, e_background=1e-12,
+                    e_blast=0.244816)
+    elif problem == abi.JET_2D:      # ex5_mach2000_jet/main.f90:4-6,597
+        base.update(nx=800, ny=200, cfl=1.0 / 4.0, time_terminal=0.001, gamma=5.0 / 3.0)
+    else:
+        raise ValueError(f"unknown problem {problem}")
+    return base
+
+
+def make_config(problem: int, **overrides) -> abi.SwfdConfig:
+    d = reference_defaults(problem)
+    unknown = set(overrides) - set(d) - {"reserved"}
+    if unknown:
+        raise KeyError(f"unknown config fields {sorted(unknown)}")
+    d.update(overrides)
+    cfg = abi.SwfdConfig()
+    for k, v in d.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+# Benchmark workloads (sizes and parameters of the named configurations).
+def workload(name: str, **overrides) -> abi.SwfdConfig:
+    if name == "sedov1d_fp64":
+        # 1D point energy: n=800 on [-2,2], E=1e-12 background, E=3.2e6/dx centre,
+        # CFL 0.6, swp_num=2, T=0.001
+        return make_config(abi.SEDOV_1D, cfl=0.6, swp_num=2, e_background=1e-12,
+                           **overrides)
+    if name.startswith("vortex"):
+        # near-vacuum isentropic vortex on [0,10]^2, T=0.01; name 'vortex<n>'
+        n = int(name[len("vortex"):] or 180)
+        return make_config(abi.VORTEX_2D, nx=n, ny=n, **overrides)
+    if name == "jet":
+        # Mach-2000-type jet, 800x200 half domain with the y=0 symmetry plane, T=0.001
+        return make_config(abi.JET_2D, **overrides)
+    if name.startswith("sedov2d"):
+        n = int(name[len("sedov2d"):] or 640)
+        return make_config(abi.SEDOV_2D, nx=n, ny=n, **overrides)
+    raise KeyError(name)

@@ -1,0 +1,214 @@
+"""Host-side mirror of the reference PROGRAMs over the C ABI.
+
+``Solver`` owns one ``swfd_handle``: it replaces the module-level state of an
+example's main.f90 and exposes the same procedures (initdata, rk, the time
+loop, findalpha, checkpositivity, sweep_lim) plus the output stage (the .dat
+files and the sweep statistics block printed by ``output``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .problems import make_config
+
+
+class Solver:
+    """One problem instance resident on one GPU."""
+
+    def __init__(self, cfg: abi.SwfdConfig | int, **overrides):
+        if isinstance(cfg, int):
+            cfg = make_config(cfg, **overrides)
+        elif overrides:
+            raise TypeError("overrides only apply when a problem id is given")
+        self.cfg = cfg
+        self.lib = abi.load()
+        h = C.c_void_p()
+        abi.check(self.lib.swfd_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.ndim = 1 if cfg.problem == abi.SEDOV_1D else 2
+        self.nc = 3 if self.ndim == 1 else 4
+        self.nx = cfg.nx
+        self.ny = 1 if self.ndim == 1 else cfg.ny
+        self.shape = (1, self.nx + 6, 3) if self.ndim == 1 else (self.ny + 6, self.nx + 6, 4)
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.swfd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, st):
+        return abi.check(st, self.h)
+
+    # -- state --------------------------------------------------------------
+    def init_problem(self):
+        self._chk(self.lib.swfd_init_problem(self.h))
+
+    def state(self) -> np.ndarray:
+        """u(nc,-2:nx+3,-2:ny+3) as a C array [j+2, i+2, c]."""
+        out = np.empty(self.shape, dtype=np.float64)
+        self._chk(self.lib.swfd_download_state(self.h, abi.dptr(out)))
+        return out
+
+    def set_state(self, u: np.ndarray):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(self.shape)
+        self._chk(self.lib.swfd_upload_state(self.h, abi.dptr(u)))
+
+    @property
+    def time(self) -> float:
+        t = C.c_double()
+        self._chk(self.lib.swfd_get_time(self.h, C.byref(t)))
+        return t.value
+
+    @time.setter
+    def time(self, t: float):
+        self._chk(self.lib.swfd_set_time(self.h, float(t)))
+
+    # -- procedures ---------------------------------------------------------
+    def step(self) -> float:
+        dt = C.c_double()
+        self._chk(self.lib.swfd_step(self.h, C.byref(dt)))
+        return dt.value
+
+    def run(self, max_steps: int = 0) -> int:
+        n = C.c_int64()
+        st = self.lib.swfd_run(self.h, int(max_steps), C.byref(n))
+        if st not in (abi.OK, abi.ERR_MAX_STEPS):
+            self._chk(st)
+        return n.value
+
+    def flux_divergence(self) -> np.ndarray:
+        out = np.empty(self.shape, dtype=np.float64)
+        self._chk(self.lib.swfd_flux_divergence(self.h, abi.dptr(out)))
+        return out
+
+    def sweep(self):
+        self._chk(self.lib.swfd_sweep(self.h))
+
+    def check_positivity(self) -> int:
+        v = C.c_int32()
+        self._chk(self.lib.swfd_check_positivity(self.h, C.byref(v)))
+        return v.value
+
+    def find_alpha(self) -> float:
+        v = C.c_double()
+        self._chk(self.lib.swfd_find_alpha(self.h, C.byref(v)))
+        return v.value
+
+    def stats(self) -> dict:
+        s = abi.SwfdSweepStats()
+        self._chk(self.lib.swfd_get_sweep_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def tracks(self):
+        n = C.c_int64()
+        self._chk(self.lib.swfd_get_sweep_tracks(self.h, None, None, None, 0, C.byref(n)))
+        k = n.value
+        a = np.zeros(k, np.int32), np.zeros(k, np.int32), np.zeros(k, np.int32)
+        ip = C.POINTER(C.c_int32)
+        self._chk(self.lib.swfd_get_sweep_tracks(
+            self.h, a[0].ctypes.data_as(ip), a[1].ctypes.data_as(ip), a[2].ctypes.data_as(ip), k,
+            C.byref(n)))
+        return a
+
+    # -- output (ex3_vortex_accuracy_2d/main.f90:720-841) ----------------------
+    def stats_text(self) -> str:
+        """The statistics block printed by ``output`` (list-directed style)."""
+        s = self.stats()
+        n = max(s["sweep_count"], 1)
+        lines = []
+
+        def line(label, v):
+            if isinstance(v, float):
+                lines.append(f" {label} {_fortran_real(v)}")
+            else:
+                lines.append(f" {label} {v:11d}")
+
+        line("total sweep = ", s["total_sweep"])
+        line("avg sweep = ", s["total_sweep"] / n if s["sweep_count"] else float("nan"))
+        line("max sweep = ", s["max_sweep"])
+        line("total negative pairs = ", s["total_neg"])
+        line("avg negative pairs = ", s["total_neg"] / n if s["sweep_count"] else float("nan"))
+        line("max negative pairs = ", s["max_neg"])
+        line("total positive neighbors = ", s["total_pos"])
+        line("avg positive neighbors = ", s["total_pos"] / n if s["sweep_count"] else float("nan"))
+        line("max positive neighbors = ", s["max_pos"])
+        lines.append(f" # of limiter {s['den_count']:11d} {s['pre_count']:11d}")
+        return "\n".join(lines) + "\n"
+
+    def write_dat(self, out_dir: str | Path = "."):
+        """den.dat / pre.dat (+ m1.dat, m2.dat in 2D) of the interior cells."""
+        out = Path(out_dir)
+        out.mkdir(parents=True, exist_ok=True)
+        u = self.state()
+        g1 = self.cfg.gamma - 1.0
+        if self.ndim == 1:
+            x = -2.0 + np.arange(1, self.nx + 1) * (4.0 / self.nx) - (4.0 / self.nx) / 2.0
+            r = u[0, 3:self.nx + 3, :]
+            pre = g1 * (r[:, 2] - 0.5 * r[:, 1] ** 2 / r[:, 0])
+            _write_cols(out / "den.dat", [x, r[:, 0]])
+            _write_cols(out / "pre.dat", [x, pre])
+            _write_cols(out / "vel.dat", [x, r[:, 1] / r[:, 0]])
+            return
+        dx = self._dx()
+        dy = self._dy()
+        rows = u[3:self.ny + 3, 3:self.nx + 3, :]
+        jj, ii = np.meshgrid(np.arange(1, self.ny + 1), np.arange(1, self.nx + 1), indexing="ij")
+        x = dx * (ii - 0.5)
+        y = dy * (jj - 0.5)
+        rho, m1, m2, e = (rows[..., c] for c in range(4))
+        pre = g1 * (e - 0.5 * m1 ** 2 / rho - 0.5 * m2 ** 2 / rho)
+        _write_cols(out / "den.dat", [x.ravel(), y.ravel(), rho.ravel()])
+        _write_cols(out / "pre.dat", [x.ravel(), y.ravel(), pre.ravel()])
+        _write_cols(out / "m1.dat", [x.ravel(), y.ravel(), m1.ravel()])
+        _write_cols(out / "m2.dat", [x.ravel(), y.ravel(), m2.ravel()])
+
+    def _dx(self):
+        p = self.cfg.problem
+        if p == abi.VORTEX_2D:
+            return 10.0 / self.nx
+        if p == abi.SEDOV_2D:
+            return 1.3 / self.nx
+        return 1.0 / self.nx
+
+    def _dy(self):
+        p = self.cfg.problem
+        if p == abi.VORTEX_2D:
+            return 10.0 / self.ny
+        if p == abi.SEDOV_2D:
+            return 1.3 / self.ny
+        return 0.25 / self.ny
+
+
+def _fortran_real(v: float) -> str:
+    """gfortran list-directed REAL(8): 0.1 <= |v| < 1e16 as F, else E with 3-digit exponent."""
+    if v != v:
+        return "             NaN"
+    a = abs(v)
+    if a != 0.0 and (a < 0.1 or a >= 1e16):
+        m, e = f"{v:.16E}".split("E")
+        return f"{m}E{int(e):+04d}"
+    digits = 17 - (len(str(int(a))) if a >= 1 else 0)
+    return f"{v:.{max(digits, 1)}f}"
+
+
+def _write_cols(path: Path, cols):
+    with open(path, "w") as f:
+        for row in zip(*cols):
+            f.write("".join(f"  {_fortran_real(float(v))}" for v in row) + "\n")
