@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the sweeping FD-WENO Euler step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one SSP-RK3 time step (three RK stages, each with its CFL reduction,
+characteristic WENO5 fluxes, RK update, positivity test, sweep when flagged and
+boundary conditions) of the 360x360 near-vacuum isentropic vortex in plain
+FP64, on state resident in HBM.  The metric is cell-updates/s per RK stage:
+interior cells x stages / time.  One JSON line is printed by rank 0.
+
+Under torchrun (N > 1) every rank advances its own replica (the path does not
+shard within one grid); the value is the sum of all ranks' work over the
+slowest rank's time.
+
+--impl reference times the reference's algorithm on the host CPU instead: the
+CPU restatement of the reference in its quad-literal mode (the arithmetic of
+the reference's -fdefault-real-8 build), one RK3 step of the vortex per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s per RK stage, FP32-batched vs plain FP64; p50/p99 solve latency"
+UNIT = "cell-updates/s"
+# compulsory HBM traffic of one fused 2D FP64 RK stage, bytes per cell
+# (read u_k and u0, write u_k+1: 85.3 B averaged over the three stages)
+STAGE_BYTES_PER_CELL = (64 + 96 + 96) / 3.0
+# algorithmic FP64 work of one interface flux (Roe eigenvectors, 40 projections,
+# 8 WENO5 reconstructions, back projection), counted from the kernel source:
+# 800 adds/multiplies + 50 divisions + 1 square root
+FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[4:8]) if v == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(nx: int, budget_s: float = 10.0) -> dict:
+    """The CPU oracle on the host, one thread, on a bounded sample of the workload."""
+    import oracle
+    from sweeping_fd_weno_gb300 import problems
+    oracle.build()
+    o = oracle.Oracle(problems.workload(f"vortex{nx}"))
+    o.init_problem()
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        o.step()
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s or steps >= 200:
+            break
+    el = time.perf_counter() - t0
+    v = nx * nx * 3 * steps / el
+    # the reference's own build promotes its double literals to REAL(16):
+    # one RK3 step of a 120x120 vortex in that arithmetic
+    q = oracle.Oracle(problems.workload("vortex120", literals=1))
+    q.init_problem()
+    t1 = time.perf_counter()
+    q.step()
+    qel = time.perf_counter() - t1
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} SSP-RK3 steps of the {nx}x{nx} vortex, double literals "
+                      f"(the arithmetic of the GPU path), single thread, {el:.1f} s",
+            "quad_literal_value": 120 * 120 * 3 / qel,
+            "quad_literal_sample": f"1 SSP-RK3 step of a 120x120 vortex with REAL(16) literals "
+                                   f"(the reference's -fdefault-real-8 build), {qel:.1f} s"}
+
+
+def run_reference(args, rank):
+    """The reference's algorithm on the host CPU (its quad-literal build arithmetic)."""
+    if rank != 0:
+        return 0
+    import oracle
+    from sweeping_fd_weno_gb300 import problems
+    oracle.build()
+    n = args.reference_nx
+    cfg = problems.workload(f"vortex{n}", literals=1)
+    o = oracle.Oracle(cfg)
+    o.init_problem()
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    el = time.perf_counter() - t0
+    v = n * n * 3 * args.steps / el
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex",
+        "config": {"workload": "vortex360_fp64", "sample_nx": n, "ny": n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} SSP-RK3 steps of a {n}x{n} vortex, REAL(16) "
+                                   "literals as the reference's -fdefault-real-8 build; the "
+                                   "reference itself is serial Fortran and no Fortran compiler "
+                                   "exists here"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="vortex360")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--reference-nx", type=int, default=180)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import numpy as np
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, abi, problems
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    cfg = problems.workload(args.workload, device=local)
+    solver = Solver(cfg)
+    solver.init_problem()
+    cells = solver.nx * solver.ny
+    ext = torch.cuda.ExternalStream(solver.stream_ptr(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        solver.step()
+
+    solver.reset_profile()
+    solver.set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()  # evict L2 (129 MB) between timed steps
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+        solver.step()
+        e1.record(ext)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    prof = solver.profile()
+    solver.set_profiling(False)
+    t_max = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    total_ms = float(t_max.item())
+    updates = cells * 3 * args.steps * world
+    value = updates / (total_ms * 1e-3)
+
+    # end to end through the public API with host buffers: upload the step's
+    # input from pinned memory, step, read the result back
+    host = torch.empty(int(np.prod(solver.shape)), dtype=torch.float64).pin_memory()
+    hu = host.numpy().reshape(solver.shape)
+    solver.state(out=hu)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        solver.set_state(hu)
+        solver.step()
+        solver.state(out=hu)
+    e2e_s = time.perf_counter() - t0
+    t_e2e = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(t_e2e, op=dist.ReduceOp.MAX)
+    e2e_s = float(t_e2e.item())
+    state_bytes = int(np.prod(solver.shape)) * 8
+    e2e = {"value": cells * 3 * args.e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
+           "steps": args.e2e_steps}
+
+    # dominant kernel: the WENO flux kernels (one launch per direction per stage)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    import ctypes as C
+    fp64 = C.c_double(0.0)
+    abi.load().swfd_probe_fp64_peak(local, C.byref(fp64))
+    flux_ms_per_launch = prof["flux_ms"] / max(prof["flux_launches"], 1)
+    # per launch (one direction of one stage): read the split fluxes (8 doubles)
+    # and Roe averages (4 doubles) of every cell once, write 8 doubles per interface
+    launch_bytes = cells * (12 + 8) * 8.0
+    achieved = launch_bytes / (flux_ms_per_launch * 1e-3) / 1e9
+    launch_flops = cells * FLUX_FLOPS_PER_INTERFACE
+    fp64_achieved = launch_flops / (flux_ms_per_launch * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak, "traffic": None,
+        "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+        "kernel": "k_flux_x / k_flux_y (characteristic WENO5 interface fluxes)",
+        "launch_ms": flux_ms_per_launch,
+        "compute_bound": "fp64",
+        "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64.value,
+                 "frac": fp64_achieved / fp64.value if fp64.value else None,
+                 "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains)",
+                 "flops_per_interface": FLUX_FLOPS_PER_INTERFACE},
+        "stage_hbm": {"achieved": STAGE_BYTES_PER_CELL * value / 1e9, "peak": hbm_peak,
+                      "frac": STAGE_BYTES_PER_CELL * value / 1e9 / hbm_peak,
+                      "bytes_per_cell_stage": STAGE_BYTES_PER_CELL},
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex (no dataset)",
+        "config": {"workload": f"{args.workload}_fp64", "nx": solver.nx, "ny": solver.ny,
+                   "stages_per_step": 3, "precision": "plain FP64 (double literals)",
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": prof["kernel_launches"],
+        "roofline": roofline,
+        "sweep": {"invocations": prof["sweep_invocations"], "ms": prof["sweep_ms"]},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line))
+    solver.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

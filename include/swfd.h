@@ -170,6 +170,28 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
                              int32_t literals, int32_t device, double* uleft,
                              double* uright);
 
+/* Instrumentation (no counterpart in the reference, which only prints a
+ * wall-clock "CPU Time", ex4_sedov_2d/main.f90:111,118-119). */
+typedef struct swfd_profile {
+  int64_t kernel_launches;  /* kernels this handle launched since the reset */
+  int64_t stages;           /* RK stages executed */
+  int64_t flux_launches;    /* WENO flux kernel launches timed with events */
+  double flux_ms;           /* summed event time of those launches */
+  int64_t sweep_invocations;
+  double sweep_ms;          /* summed event time of sweep_lim work */
+} swfd_profile;
+
+/* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
+swfd_status swfd_get_stream(swfd_handle* h, void** stream);
+/* on != 0: bracket the flux kernels and the sweep with CUDA events. */
+swfd_status swfd_set_profiling(swfd_handle* h, int32_t on);
+swfd_status swfd_get_profile(swfd_handle* h, swfd_profile* prof);
+swfd_status swfd_reset_profile(swfd_handle* h);
+
+/* Measured FP64 FMA throughput of the device in GFLOP/s (2 flops per FMA):
+ * the denominator of the FP64-pipe roofline of the FP64 path. */
+swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops);
+
 /* Last error message of the handle (or of the process when h is NULL). */
 swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len);
 const char* swfd_status_string(swfd_status s);

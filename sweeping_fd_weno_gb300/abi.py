@@ -74,6 +74,15 @@ class SwfdSweepStats(C.Structure):
 
 STATS_FIELDS = [f for f, _ in SwfdSweepStats._fields_]
 
+
+class SwfdProfile(C.Structure):
+    _fields_ = [("kernel_launches", C.c_int64), ("stages", C.c_int64),
+                ("flux_launches", C.c_int64), ("flux_ms", C.c_double),
+                ("sweep_invocations", C.c_int64), ("sweep_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
 # name -> (restype, argtypes) for every entry point of include/swfd.h
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
@@ -97,6 +106,11 @@ _SIGS = {
                                           C.POINTER(C.c_int32), C.c_int64,
                                           C.POINTER(C.c_int64)]),
     "swfd_weno5_batch": (C.c_int32, [_DP, C.c_int64, C.c_double, C.c_int32, C.c_int32, _DP, _DP]),
+    "swfd_get_stream": (C.c_int32, [_P, C.POINTER(_P)]),
+    "swfd_set_profiling": (C.c_int32, [_P, C.c_int32]),
+    "swfd_get_profile": (C.c_int32, [_P, C.POINTER(SwfdProfile)]),
+    "swfd_reset_profile": (C.c_int32, [_P]),
+    "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
     "swfd_last_error": (C.c_int32, [_P, C.c_char_p, C.c_size_t]),
     "swfd_status_string": (C.c_char_p, [C.c_int32]),
 }

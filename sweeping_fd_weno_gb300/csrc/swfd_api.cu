@@ -30,6 +30,13 @@ swfd_status fail(swfd_handle* h, swfd_status st, const std::string& msg) {
                   std::string(#call) + ": " + cudaGetErrorString(e_));              \
   } while (0)
 
+// launch `call`, which issues n kernels of this library, and count them
+#define LAUNCH(h, n, call)            \
+  do {                                \
+    CU((h), (call));                  \
+    (h)->prof.kernel_launches += (n); \
+  } while (0)
+
 #define ST(call)                          \
   do {                                    \
     swfd_status s_ = (call);              \
@@ -229,21 +236,21 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
   cudaStream_t s = h->stream;
   // density sweep
   if (p.g.ndim == 1) {
-    CU(h, launch_density_sweep(p, u, s));
+    LAUNCH(h, 1, launch_density_sweep(p, u, s));
     h->den_count++;
   } else {
-    CU(h, launch_rho_min(p, u, h->dsc, s));
+    LAUNCH(h, 1, launch_rho_min(p, u, h->dsc, s));
     ST(sync_scalars(h));
     unsigned long long k = h->hsc->rho_min_key;
     unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
     double rho_min;
     memcpy(&rho_min, &b, sizeof(double));
     if (rho_min < 1e-12) {
-      CU(h, launch_density_sweep(p, u, s));
+      LAUNCH(h, 1, launch_density_sweep(p, u, s));
       h->den_count++;
     }
   }
-  CU(h, launch_ubar(p, u, h->dsc, s));
+  LAUNCH(h, 1, launch_ubar(p, u, h->dsc, s));
   if (p.problem == SWFD_PROBLEM_SEDOV_2D) {
     ST(sync_scalars(h));
     const double* ub = h->hsc->ubar;
@@ -257,9 +264,9 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
   CU(h, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
   for (int q = 1; q <= h->cfg.swp_num; ++q) {
     int ord = (q % 2 == 1) ? 1 : 2;
-    CU(h, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
-    CU(h, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
-    CU(h, launch_exit_count(p, u, h->dsc, s));
+    LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
+    LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
+    LAUNCH(h, 1, launch_exit_count(p, u, h->dsc, s));
     ST(sync_scalars(h));
     h->pre_count++;
     if (h->hsc->bad_count == 0) {
@@ -282,16 +289,38 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
 swfd_status stage(swfd_handle* h, int k, double* in, double* u0, double* out) {
   const Params& p = h->p;
   cudaStream_t s = h->stream;
-  CU(h, launch_alpha(p, in, h->dsc, s));
-  if (k == 1) CU(h, launch_dt(p, h->dsc, s));
-  CU(h, launch_prep(p, in, h->dsc, h->split, h->roe, s));
-  CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
-  CU(h, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
+  LAUNCH(h, 2, launch_alpha(p, in, h->dsc, s));
+  if (k == 1) LAUNCH(h, 1, launch_dt(p, h->dsc, s));
+  LAUNCH(h, 1, launch_prep(p, in, h->dsc, h->split, h->roe, s));
+  if (h->prof_on) CU(h, cudaEventRecord(h->ev[0], s));
+  LAUNCH(h, p.g.ndim == 2 ? 2 : 1,
+         launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
+  if (h->prof_on) CU(h, cudaEventRecord(h->ev[1], s));
+  LAUNCH(h, 1, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
+  h->prof.stages++;
+  if (h->prof_on) {
+    float ms = 0.f;
+    CU(h, cudaEventSynchronize(h->ev[1]));
+    CU(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    h->prof.flux_ms += ms;
+    h->prof.flux_launches += p.g.ndim == 2 ? 2 : 1;
+  }
   if (h->cfg.use_limiter == 2) {
     ST(sync_scalars(h));
-    if (h->hsc->postag) ST(sweep_lim(h, out));
+    if (h->hsc->postag) {
+      if (h->prof_on) CU(h, cudaEventRecord(h->ev[2], s));
+      ST(sweep_lim(h, out));
+      if (h->prof_on) {
+        float ms = 0.f;
+        CU(h, cudaEventRecord(h->ev[3], s));
+        CU(h, cudaEventSynchronize(h->ev[3]));
+        CU(h, cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
+        h->prof.sweep_ms += ms;
+        h->prof.sweep_invocations++;
+      }
+    }
   }
-  CU(h, launch_bc(p, out, s));
+  LAUNCH(h, p.g.ndim == 2 ? 1 : 0, launch_bc(p, out, s));
   return SWFD_OK;
 }
 
@@ -410,6 +439,8 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if ((e = cudaMallocHost(&h->hsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   if ((e = cudaMalloc(&h->d_stage, hb)) != cudaSuccess) return cleanup_fail(e);
+  for (int k = 0; k < 4; ++k)
+    if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
   for (int k = 0; k < 3; ++k)
     if ((e = cudaMemsetAsync(h->st[k], 0, g.nc * pb, h->stream)) != cudaSuccess)
       return cleanup_fail(e);
@@ -435,6 +466,8 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
   if (h->hsc) cudaFreeHost(h->hsc);
+  for (int k = 0; k < 4; ++k)
+    if (h->ev[k]) cudaEventDestroy(h->ev[k]);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SWFD_OK;
@@ -500,7 +533,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   ST(stage(h, 1, X, X, Y));
   ST(stage(h, 2, Y, X, Z));
   ST(stage(h, 3, Z, X, X));
-  CU(h, launch_time_advance(h->dsc, h->stream));
+  LAUNCH(h, 1, launch_time_advance(h->dsc, h->stream));
   ST(check_device_error(h));
   h->time = h->hsc->time;
   if (dt_out) *dt_out = h->hsc->dt;
@@ -633,6 +666,30 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return done(fail(nullptr, SWFD_ERR_CUDA, std::string("swfd_weno5_batch: ") + cudaGetErrorString(e)));
   return done(SWFD_OK);
+}
+
+swfd_status swfd_get_stream(swfd_handle* h, void** stream) {
+  if (!h || !stream) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  *stream = (void*)h->stream;
+  return SWFD_OK;
+}
+
+swfd_status swfd_set_profiling(swfd_handle* h, int32_t on) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  h->prof_on = on ? 1 : 0;
+  return SWFD_OK;
+}
+
+swfd_status swfd_get_profile(swfd_handle* h, swfd_profile* prof) {
+  if (!h || !prof) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  *prof = h->prof;
+  return SWFD_OK;
+}
+
+swfd_status swfd_reset_profile(swfd_handle* h) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  h->prof = swfd_profile{};
+  return SWFD_OK;
 }
 
 swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len) {

@@ -90,6 +90,10 @@ struct swfd_handle {
   int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;
   std::vector<int32_t> sweep_track, neg_track, pos_track;
   std::string last_error;
+  // instrumentation
+  int prof_on = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  swfd_profile prof = {};
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles

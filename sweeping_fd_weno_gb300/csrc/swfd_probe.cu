@@ -1,0 +1,46 @@
+// swfd_probe.cu -- FP64 pipe throughput probe.  The FP64 path of this library
+// is bounded by the FP64 pipe, whose peak is not a published constant of
+// this part; this kernel measures it (independent DFMA chains, 8 per thread).
+#include "swfd_internal.h"
+
+namespace {
+
+__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-3, x2 = x0 + 2e-3, x3 = x0 + 3e-3;
+  double x4 = x0 + 4e-3, x5 = x0 + 5e-3, x6 = x0 + 6e-3, x7 = x0 + 7e-3;
+  for (int k = 0; k < iters; ++k) {
+    x0 = __fma_rn(x0, a, b); x1 = __fma_rn(x1, a, b); x2 = __fma_rn(x2, a, b);
+    x3 = __fma_rn(x3, a, b); x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b);
+    x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
+  }
+  double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+extern "C" swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops) {
+  if (!gflops) return SWFD_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return SWFD_ERR_CUDA;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  double* out = nullptr;
+  if (cudaMalloc(&out, 1 << 20) != cudaSuccess) return SWFD_ERR_OOM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  k_dfma_probe<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);  // warm-up
+  cudaEventRecord(e0);
+  k_dfma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess || ms <= 0.f) return SWFD_ERR_CUDA;
+  *gflops = 2.0 * 8.0 * (double)iters * threads * blocks / (ms * 1e-3) / 1e9;
+  return SWFD_OK;
+}

@@ -60,9 +60,11 @@ class Solver:
     def init_problem(self):
         self._chk(self.lib.swfd_init_problem(self.h))
 
-    def state(self) -> np.ndarray:
-        """u(nc,-2:nx+3,-2:ny+3) as a C array [j+2, i+2, c]."""
-        out = np.empty(self.shape, dtype=np.float64)
+    def state(self, out: np.ndarray | None = None) -> np.ndarray:
+        """u(nc,-2:nx+3,-2:ny+3) as a C array [j+2, i+2, c] (into ``out`` if given)."""
+        if out is None:
+            out = np.empty(self.shape, dtype=np.float64)
+        assert out.shape == self.shape and out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
         self._chk(self.lib.swfd_download_state(self.h, abi.dptr(out)))
         return out
 
@@ -126,6 +128,23 @@ class Solver:
             self.h, a[0].ctypes.data_as(ip), a[1].ctypes.data_as(ip), a[2].ctypes.data_as(ip), k,
             C.byref(n)))
         return a
+
+    # -- instrumentation ----------------------------------------------------
+    def stream_ptr(self) -> int:
+        v = C.c_void_p()
+        self._chk(self.lib.swfd_get_stream(self.h, C.byref(v)))
+        return v.value or 0
+
+    def set_profiling(self, on: bool = True):
+        self._chk(self.lib.swfd_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self) -> dict:
+        pr = abi.SwfdProfile()
+        self._chk(self.lib.swfd_get_profile(self.h, C.byref(pr)))
+        return pr.as_dict()
+
+    def reset_profile(self):
+        self._chk(self.lib.swfd_reset_profile(self.h))
 
     # -- output (ex3_vortex_accuracy_2d/main.f90:720-841) ----------------------
     def stats_text(self) -> str:

@@ -1,0 +1,60 @@
+"""CPU checks of the C ABI: the library loads, exports every entry point that
+include/swfd.h declares, and validates configurations before touching CUDA."""
+import ctypes as C
+import re
+
+import pytest
+
+from sweeping_fd_weno_gb300 import abi, problems
+
+HEADER = abi.LIB_PATH.parents[2] / "include" / "swfd.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:swfd_status|const char\*)\s+(swfd_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(swfd):
+    lib = abi.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(abi.exported_names()) == names
+
+
+@pytest.mark.parametrize("problem", [abi.SEDOV_1D, abi.VORTEX_2D, abi.SEDOV_2D, abi.JET_2D])
+def test_config_default_matches_reference_parameters(swfd, problem):
+    c = abi.config_default(problem).as_dict()
+    ref = problems.reference_defaults(problem)
+    for k, v in ref.items():
+        assert c[k] == v, (k, c[k], v)
+
+
+def test_create_rejects_bad_configs_without_cuda(swfd):
+    lib = abi.load()
+    h = C.c_void_p()
+    cfg = problems.make_config(abi.VORTEX_2D, abi_version=99)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.VORTEX_2D, nx=4)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.VORTEX_2D, use_limiter=1)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
+    cfg = problems.make_config(abi.VORTEX_2D, swp_num=0)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    assert "swp_num" in abi.last_error()
+    assert lib.swfd_config_default(C.byref(cfg), 42) == abi.ERR_INVALID
+
+
+def test_status_strings(swfd):
+    lib = abi.load()
+    for st in range(0, -10, -1):
+        assert lib.swfd_status_string(st)
+    assert lib.swfd_status_string(abi.ERR_SWEEP_NOCONV) == b"sweep did not converge within swp_num"
+
+
+def test_null_handle_is_rejected(swfd):
+    lib = abi.load()
+    assert lib.swfd_step(None, None) == abi.ERR_INVALID
+    assert lib.swfd_destroy(None) == abi.OK

@@ -1,0 +1,143 @@
+"""Known-answer checks of the CPU oracle (runs without a GPU).
+
+The reference ships no tests and no outputs, so the oracle is checked against
+properties of the reference's own algorithm: WENO5 reproduces quadratics
+(weno5.f90:86-146), the vortex converges at fifth order (the Table-1
+methodology of ex3_vortex_accuracy_2d/main.f90:725-777), the sweeps conserve
+the weighted sums and leave every cell with P, rho > eps, and the quad-literal
+build agrees with the double build to 1e-12.  It is also pinned to the
+committed golden fixtures (tests/golden, made by tests/golden/make_golden.py).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from sweeping_fd_weno_gb300 import abi, problems
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def cell_avg_quadratic(c, k):
+    # average of c0 + c1 x + c2 x^2 over [k-1/2, k+1/2]
+    return c[0] + c[1] * k + c[2] * (k * k + 1.0 / 12.0)
+
+
+@pytest.mark.parametrize("lit", [0, 1])
+def test_weno5_reproduces_quadratics(oracle_mod, lit):
+    rng = np.random.default_rng(3)
+    cs = rng.standard_normal((200, 3))
+    st = np.array([[cell_avg_quadratic(c, k) for k in range(-2, 3)] for c in cs])
+    ul, ur = oracle_mod.weno5(st, 1e-6, lit)
+    p = lambda c, x: c[0] + c[1] * x + c[2] * x * x
+    assert np.allclose(ur, [p(c, 0.5) for c in cs], rtol=0, atol=1e-12)
+    assert np.allclose(ul, [p(c, -0.5) for c in cs], rtol=0, atol=1e-12)
+
+
+def test_weno5_linear_data_uses_linear_weights(oracle_mod):
+    # a(k) = k gives beta = (1,1,1): uright = 0.3*um3 + 0.6*um2 + 0.1*um1 = 1/2
+    ul, ur = oracle_mod.weno5(np.arange(-2.0, 3.0)[None, :], 1e-6, 0)
+    assert ur[0] == pytest.approx(0.5, abs=1e-15) and ul[0] == pytest.approx(-0.5, abs=1e-15)
+
+
+def _exact_rho(x, y, t, g=1.4):
+    g1, mag = g - 1.0, 10.0828
+    r = np.sqrt((x - 5. - t) ** 2 + (y - 5. - t) ** 2)
+    return (1 - g1 * mag ** 2 / 8. / g / np.pi ** 2 * np.exp(1. - r ** 2)) ** (1. / g1)
+
+
+def test_vortex_fifth_order(oracle_mod):
+    errs = []
+    for n in (45, 90, 180):
+        o = oracle_mod.Oracle(problems.workload(f"vortex{n}"))
+        o.init_problem()
+        o.run()
+        dx = 10.0 / n
+        xs = np.arange(1, n + 1) * dx - dx / 2
+        X, Y = np.meshgrid(xs, xs, indexing="xy")
+        errs.append(np.abs(_exact_rho(X, Y, o.time) - o.state()[3:n + 3, 3:n + 3, 0]).mean())
+    order = np.log2(errs[1] / errs[2])
+    assert order > 4.5, errs
+
+
+def _poisoned_vortex(oracle_mod, n=45, seed=5, lit=0):
+    o = oracle_mod.Oracle(problems.make_config(abi.VORTEX_2D, nx=n, ny=n, literals=lit))
+    o.init_problem()
+    u = o.state()
+    rng = np.random.default_rng(seed)
+    for _ in range(30):
+        j, i = 3 + rng.integers(0, n), 3 + rng.integers(0, n)
+        v = u[j, i]
+        v[3] = 0.5 * (v[1] ** 2 + v[2] ** 2) / v[0] * (1 - rng.uniform(0, 1e-3))
+    o.set_state(u)
+    return o, u
+
+
+def test_pressure_sweep_conserves_and_restores_positivity(oracle_mod):
+    o, u0 = _poisoned_vortex(oracle_mod)
+    assert o.check_positivity() == 1
+    assert o.sweep() == 0
+    u1 = o.state()
+    n = 45
+    s0 = u0[3:n + 3, 3:n + 3].sum(axis=(0, 1))
+    s1 = u1[3:n + 3, 3:n + 3].sum(axis=(0, 1))
+    assert np.allclose(s0, s1, rtol=1e-13, atol=1e-13)
+    r = u1[3:n + 3, 3:n + 3]
+    p = 0.4 * (r[..., 3] - 0.5 * (r[..., 1] ** 2 + r[..., 2] ** 2) / r[..., 0])
+    assert (p > 1e-13).all() and (r[..., 0] > 1e-13).all()
+    s = o.stats()
+    assert s["sweep_count"] == 1 and s["total_sweep"] >= 1 and s["total_pos"] + s["total_neg"] >= 30
+
+
+def test_density_sweep_1d_conserves_mass(oracle_mod):
+    cfg = problems.workload("sedov1d_fp64", nx=100)
+    o = oracle_mod.Oracle(cfg)
+    o.init_problem()
+    u = o.state()
+    u[0, 40:45, 0] = [1e-15, -2e-14, 5e-16, 0.2, 1e-14]
+    u[0, 38:47, 2] = np.linspace(2e-12, 9e-12, 9)
+    o.set_state(u)
+    o.sweep()
+    v = o.state()
+    # both sweeps only move mass and energy between neighbours (equal weights)
+    assert np.isfinite(v).all()
+    assert np.isclose(u[0, :, 0].sum(), v[0, :, 0].sum(), rtol=1e-14)
+    assert np.isclose(u[0, :, 2].sum(), v[0, :, 2].sum(), rtol=1e-14)
+    assert o.stats()["den_count"] == 1
+
+
+def test_quad_literals_agree_with_double_to_1e12(oracle_mod):
+    us, stats = [], []
+    for lit in (0, 1):
+        o = oracle_mod.Oracle(problems.workload("vortex45", literals=lit))
+        o.init_problem()
+        o.run()
+        us.append(o.state())
+        stats.append(o.stats())
+    rel = np.abs(us[0] - us[1]) / np.maximum(np.abs(us[1]), 1e-300)
+    assert rel.max() < 1e-12
+    assert stats[0] == stats[1]
+
+
+def test_time_loop_condition_modes(oracle_mod):
+    o = oracle_mod.Oracle(problems.workload("vortex45"))
+    o.time = 0.01 - 1e-10
+    assert o.loop_continues()
+    o.time = 0.01 - 0.5e-10
+    assert not o.loop_continues()
+
+
+GOLDEN_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_matches_golden_fixture(oracle_mod, name):
+    from tests.golden.make_golden import run_case
+    ref = np.load(GOLDEN / f"{name}.npz")
+    out = run_case(oracle_mod, name)
+    for k in ref.files:
+        assert np.array_equal(ref[k], out[k]), k
+
+
+def test_golden_fixtures_exist():
+    assert len(GOLDEN_CASES) >= 4
