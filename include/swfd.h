@@ -72,6 +72,12 @@ enum { SWFD_PRECISION_FP64 = 0, SWFD_PRECISION_FP32_BULK = 1 };
  * (ex3_vortex_accuracy_2d/main.f90:913-920), or a deterministic tree sum. */
 enum { SWFD_UBAR_SEQUENTIAL = 0, SWFD_UBAR_TREE = 1 };
 
+/* How a sweep pass walks its ordering.  Both give the reference's values and
+ * counts: PARALLEL runs the independent chains of nodal adjustments
+ * concurrently and follows only chains that reach the next flagged cell in
+ * sequence; SEQUENTIAL walks every cell in one GPU thread. */
+enum { SWFD_SWEEP_PARALLEL = 0, SWFD_SWEEP_SEQUENTIAL = 1 };
+
 typedef struct swfd_config {
   int32_t abi_version;   /* must be SWFD_ABI_VERSION */
   int32_t problem;       /* SWFD_PROBLEM_* */
@@ -89,7 +95,8 @@ typedef struct swfd_config {
   double e_background;   /* point-energy problems: background total energy */
   double e_blast;        /* point-energy problems: blast energy numerator
                             (1D: E = e_blast/dx, 2D: E = e_blast/(dx*dy)) */
-  int32_t reserved[8];   /* zero */
+  int32_t sweep_mode;    /* SWFD_SWEEP_PARALLEL (default) or SWFD_SWEEP_SEQUENTIAL */
+  int32_t reserved[7];   /* zero */
 } swfd_config;
 
 /* Sweep statistics exactly as the reference counts them

@@ -37,6 +37,8 @@ PRECISION_FP64 = 0
 PRECISION_FP32_BULK = 1
 UBAR_SEQUENTIAL = 0
 UBAR_TREE = 1
+SWEEP_PARALLEL = 0
+SWEEP_SEQUENTIAL = 1
 
 
 class SwfdConfig(C.Structure):
@@ -56,7 +58,8 @@ class SwfdConfig(C.Structure):
         ("gamma", C.c_double),
         ("e_background", C.c_double),
         ("e_blast", C.c_double),
-        ("reserved", C.c_int32 * 8),
+        ("sweep_mode", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
     def as_dict(self) -> dict:

@@ -235,8 +235,19 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
   const Params& p = h->p;
   cudaStream_t s = h->stream;
   // density sweep
+  const bool seq = h->cfg.sweep_mode == SWFD_SWEEP_SEQUENTIAL;
+  auto density = [&]() -> swfd_status {
+    if (seq) {
+      LAUNCH(h, 1, launch_density_sweep(p, u, s));
+    } else {
+      int n = 0;
+      CU(h, launch_density_sweep_par(p, u, h->sweep_scratch, s, &n));
+      h->prof.kernel_launches += n;
+    }
+    return SWFD_OK;
+  };
   if (p.g.ndim == 1) {
-    LAUNCH(h, 1, launch_density_sweep(p, u, s));
+    ST(density());
     h->den_count++;
   } else {
     LAUNCH(h, 1, launch_rho_min(p, u, h->dsc, s));
@@ -246,7 +257,7 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
     double rho_min;
     memcpy(&rho_min, &b, sizeof(double));
     if (rho_min < 1e-12) {
-      LAUNCH(h, 1, launch_density_sweep(p, u, s));
+      ST(density());
       h->den_count++;
     }
   }
@@ -264,8 +275,15 @@ swfd_status sweep_lim(swfd_handle* h, double* u) {
   CU(h, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
   for (int q = 1; q <= h->cfg.swp_num; ++q) {
     int ord = (q % 2 == 1) ? 1 : 2;
-    LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
-    LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
+    if (seq) {
+      LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
+      LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
+    } else {
+      int n = 0;
+      CU(h, launch_pressure_pass_par(p, u, ord, 1, h->sweep_scratch, h->dsc, s, &n));
+      CU(h, launch_pressure_pass_par(p, u, ord, 0, h->sweep_scratch, h->dsc, s, &n));
+      h->prof.kernel_launches += n;
+    }
     LAUNCH(h, 1, launch_exit_count(p, u, h->dsc, s));
     ST(sync_scalars(h));
     h->pre_count++;
@@ -408,6 +426,8 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if (cfg->ubar_mode != SWFD_UBAR_SEQUENTIAL)
     return fail(nullptr, SWFD_ERR_UNSUPPORTED, "ubar_mode: only sequential is built");
   if (cfg->swp_num < 1) return fail(nullptr, SWFD_ERR_INVALID, "swp_num must be >= 1");
+  if (cfg->sweep_mode != SWFD_SWEEP_PARALLEL && cfg->sweep_mode != SWFD_SWEEP_SEQUENTIAL)
+    return fail(nullptr, SWFD_ERR_INVALID, "unknown sweep_mode");
   if (!(cfg->gamma > 1.0)) return fail(nullptr, SWFD_ERR_INVALID, "gamma must be > 1");
   swfd_handle* h = new swfd_handle();
   h->cfg = *cfg;
@@ -439,6 +459,8 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if ((e = cudaMallocHost(&h->hsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   if ((e = cudaMalloc(&h->d_stage, hb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->sweep_scratch, sweep_scratch_bytes(h->p))) != cudaSuccess)
+    return cleanup_fail(e);
   for (int k = 0; k < 4; ++k)
     if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
   for (int k = 0; k < 3; ++k)
@@ -465,6 +487,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->rhs_tmp);
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
+  cudaFree(h->sweep_scratch);
   if (h->hsc) cudaFreeHost(h->hsc);
   for (int k = 0; k < 4; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);

@@ -82,7 +82,7 @@ struct swfd_handle {
   double* roe = nullptr;    // w, vx, vy, h for x (4 planes) and y (4 planes)
   double* flux = nullptr;   // fp_flux, fn_flux, gp_flux, gn_flux: 4*nc planes
   double* rhs_tmp = nullptr;  // nc planes (flux_divergence output)
-  double* sweep_tmp = nullptr;  // nc planes (host I/O staging)
+  void* sweep_scratch = nullptr;  // flag bits, flagged list, chain results
   swfd::DevScalars* dsc = nullptr;   // device scalars
   swfd::DevScalars* hsc = nullptr;   // pinned host mirror
   // host-side run state
@@ -127,5 +127,10 @@ cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaS
 cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int forward,
                                  DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+size_t sweep_scratch_bytes(const Params& p);
+cudaError_t launch_pressure_pass_par(const Params& p, double* u, int ordering, int forward,
+                                     void* scratch, DevScalars* dsc, cudaStream_t s, int* nlaunch);
+cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, cudaStream_t s,
+                                     int* nlaunch);
 
 }  // namespace swfd

@@ -15,7 +15,8 @@ def reference_defaults(problem: int) -> dict:
     """PARAMETERs of the reference example behind ``problem``."""
     base = dict(abi_version=abi.ABI_VERSION, problem=problem, use_limiter=2, swp_num=20000,
                 literals=abi.LITERALS_DOUBLE, precision=abi.PRECISION_FP64,
-                ubar_mode=abi.UBAR_SEQUENTIAL, device=0, gamma=1.4, e_background=0.0,
+                ubar_mode=abi.UBAR_SEQUENTIAL, sweep_mode=abi.SWEEP_PARALLEL, device=0, gamma=1.4,
+                e_background=0.0,
                 e_blast=0.0, ny=1)
     if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425
         base.update(nx=800, ny=1, swp_num=50, cfl=1.2, time_terminal=0.001,

@@ -74,9 +74,10 @@ def test_flux_divergence_matches(swfd, oracle_mod, case):
     assert_same(g.flux_divergence(), o.flux_divergence(), "wenofd + scheme")
 
 
+@pytest.mark.parametrize("sweep_mode", [abi.SWEEP_PARALLEL, abi.SWEEP_SEQUENTIAL])
 @pytest.mark.parametrize("case", list(CASES))
-def test_three_steps_match(swfd, oracle_mod, case):
-    g, o = make_pair(oracle_mod, case)
+def test_three_steps_match(swfd, oracle_mod, case, sweep_mode):
+    g, o = make_pair(oracle_mod, case, sweep_mode=sweep_mode)
     for k in range(3):
         dt_g = g.step()
         dt_o = o.step()
@@ -145,3 +146,64 @@ def test_sweep_on_poisoned_state_matches(swfd, oracle_mod, case):
     assert g.stats() == o.stats()
     s = g.stats()
     assert s["sweep_count"] == 1 and s["pre_count"] >= 1
+
+
+def _dense_poison(u, rng, frac=0.5, block=(12, 12), ndim=2):
+    u = u.copy()
+    if ndim == 2:
+        ny, nx = u.shape[0] - 6, u.shape[1] - 6
+        j0 = 3 + rng.integers(0, ny - block[0])
+        i0 = 3 + rng.integers(0, nx - block[1])
+        cells = [(j, i) for j in range(j0, j0 + block[0]) for i in range(i0, i0 + block[1])
+                 if rng.uniform() < frac]
+    else:
+        n = u.shape[1] - 6
+        i0 = 3 + rng.integers(0, n - 40)
+        cells = [(0, i) for i in range(i0, i0 + 40) if rng.uniform() < frac]
+    return _poison(u, ndim, cells, rng)
+
+
+@pytest.mark.parametrize("case", ["vortex64x48", "jet_96x24", "sedov1d_200", "sedov2d_40"])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_parallel_sweep_equals_sequential_and_oracle_on_dense_damage(swfd, oracle_mod, case, seed):
+    g, o = make_pair(oracle_mod, case)
+    gs, _ = make_pair(oracle_mod, case, sweep_mode=abi.SWEEP_SEQUENTIAL)
+    rng = np.random.default_rng(seed)
+    u = o.state()
+    ndim = 1 if u.shape[0] == 1 else 2
+    u = _dense_poison(u, rng, frac=0.6, ndim=ndim)
+    for s in (g, gs):
+        s.set_state(u)
+    o.set_state(u)
+    st_o = o.sweep()
+    g.sweep()
+    gs.sweep()
+    assert st_o == 0
+    assert_same(gs.state(), o.state(), "sequential GPU sweep")
+    assert_same(g.state(), o.state(), "parallel GPU sweep")
+    assert g.stats() == gs.stats() == o.stats()
+
+
+def test_parallel_sweep_many_chains_256(swfd, oracle_mod):
+    """A ring of damaged cells on a 256^2 grid: hundreds of independent chains."""
+    cfg = dict(problem=abi.VORTEX_2D, nx=256, ny=256)
+    g = Solver(problems.make_config(**cfg))
+    gs = Solver(problems.make_config(**cfg, sweep_mode=abi.SWEEP_SEQUENTIAL))
+    o = oracle_mod.Oracle(problems.make_config(**cfg))
+    for s in (g, gs, o):
+        s.init_problem()
+    u = o.state()
+    rng = np.random.default_rng(9)
+    jj, ii = np.meshgrid(np.arange(256), np.arange(256), indexing="ij")
+    r = np.hypot(jj - 128, ii - 128)
+    cells = [(3 + j, 3 + i) for j, i in zip(*np.nonzero((np.abs(r - 60) < 1.5)))
+             if rng.uniform() < 0.7]
+    u = _poison(u, 2, cells, rng)
+    for s in (g, gs, o):
+        s.set_state(u)
+    o.sweep()
+    g.sweep()
+    gs.sweep()
+    assert_same(g.state(), o.state(), "parallel sweep 256^2")
+    assert_same(gs.state(), o.state(), "sequential sweep 256^2")
+    assert g.stats() == o.stats() == gs.stats()
