@@ -166,8 +166,10 @@ def _dense_poison(u, rng, frac=0.5, block=(12, 12), ndim=2):
 @pytest.mark.parametrize("case", ["vortex64x48", "jet_96x24", "sedov1d_200", "sedov2d_40"])
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_parallel_sweep_equals_sequential_and_oracle_on_dense_damage(swfd, oracle_mod, case, seed):
-    g, o = make_pair(oracle_mod, case)
-    gs, _ = make_pair(oracle_mod, case, sweep_mode=abi.SWEEP_SEQUENTIAL)
+    # swp_num 40: a sweep that does not converge must fail identically
+    # (SWEEP FAIL stops ex4; ex2, ex3, ex5 go on)
+    g, o = make_pair(oracle_mod, case, swp_num=40)
+    gs, _ = make_pair(oracle_mod, case, swp_num=40, sweep_mode=abi.SWEEP_SEQUENTIAL)
     rng = np.random.default_rng(seed)
     u = o.state()
     ndim = 1 if u.shape[0] == 1 else 2
@@ -176,9 +178,16 @@ def test_parallel_sweep_equals_sequential_and_oracle_on_dense_damage(swfd, oracl
         s.set_state(u)
     o.set_state(u)
     st_o = o.sweep()
-    g.sweep()
-    gs.sweep()
-    assert st_o == 0
+
+    def status(solver):
+        try:
+            solver.sweep()
+            return 0
+        except abi.SwfdError as e:
+            return e.status
+
+    assert status(g) == st_o
+    assert status(gs) == st_o
     assert_same(gs.state(), o.state(), "sequential GPU sweep")
     assert_same(g.state(), o.state(), "parallel GPU sweep")
     assert g.stats() == gs.stats() == o.stats()
