@@ -195,6 +195,28 @@ swfd_status swfd_set_profiling(swfd_handle* h, int32_t on);
 swfd_status swfd_get_profile(swfd_handle* h, swfd_profile* prof);
 swfd_status swfd_reset_profile(swfd_handle* h);
 
+/* swfd_flux_divergence without any allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc, such as code
+ * running under an allocator that owns all device memory (a framework's
+ * caching allocator or a memory pool that forbids other allocations),
+ * real-time loops where an allocation may block, or callers that only hold
+ * device pointers they were handed.
+ *
+ * u and rhs are DEVICE arrays in the layout u(ncomp,-2:nx+3,-2:ny+3) of the
+ * current ABI (rhs is zero in the ghosts); the work is queued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream) and the call returns
+ * without waiting.  cfg selects the problem and device as for swfd_create.
+ * Every intermediate lives in one file-scope device array of 8 MiB that each
+ * GPU loading the library holds until the process exits; grids that do not
+ * fit (beyond about 130 x 130 cells in 2D, 27000 cells in 1D) are rejected
+ * with SWFD_ERR_INVALID and a message in swfd_last_error(NULL, ...).
+ * All calls share that array and it keeps the last call's contents: calls
+ * whose work overlaps on the GPU race and corrupt each other, so order them
+ * on one stream.  The first call on a device looks up the array's address
+ * with that device current; make it before any stream capture. */
+swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const double* u, double* rhs,
+                                        void* stream);
+
 /* Measured FP64 FMA throughput of the device in GFLOP/s (2 flops per FMA):
  * the denominator of the FP64-pipe roofline of the FP64 path. */
 swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops);

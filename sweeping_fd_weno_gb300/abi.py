@@ -114,6 +114,7 @@ _SIGS = {
     "swfd_get_profile": (C.c_int32, [_P, C.POINTER(SwfdProfile)]),
     "swfd_reset_profile": (C.c_int32, [_P]),
     "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
+    "swfd_flux_divergence_static": (C.c_int32, [C.POINTER(SwfdConfig), _P, _P, _P]),
     "swfd_last_error": (C.c_int32, [_P, C.c_char_p, C.c_size_t]),
     "swfd_status_string": (C.c_char_p, [C.c_int32]),
 }

@@ -12,41 +12,33 @@
 
 using namespace swfd;
 
-namespace {
-
-thread_local std::string g_last_error;
-
-swfd_status fail(swfd_handle* h, swfd_status st, const std::string& msg) {
-  if (h) h->last_error = msg;
-  g_last_error = msg;
-  return st;
-}
-
-#define CU(h, call)                                                                 \
-  do {                                                                              \
-    cudaError_t e_ = (call);                                                        \
-    if (e_ != cudaSuccess)                                                          \
-      return fail((h), e_ == cudaErrorMemoryAllocation ? SWFD_ERR_OOM : SWFD_ERR_CUDA, \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
-  } while (0)
-
-// launch `call`, which issues n kernels of this library, and count them
-#define LAUNCH(h, n, call)            \
-  do {                                \
-    CU((h), (call));                  \
-    (h)->prof.kernel_launches += (n); \
-  } while (0)
-
-#define ST(call)                          \
-  do {                                    \
-    swfd_status s_ = (call);              \
-    if (s_ != SWFD_OK) return s_;         \
-  } while (0)
-
-int64_t host_len(const Params& p) { return (int64_t)p.g.nc * p.g.LI * p.g.LJ; }
+namespace swfd {
 
 // Derive the per-example switches (the reference's variant matrix) and the
 // grid spacing exactly as each initdata computes it.
+// Options this build implements; everything else is rejected before any
+// CUDA call.
+swfd_status check_config(const swfd_config& c, std::string& err) {
+  auto bad = [&](swfd_status st, const char* m) {
+    err = m;
+    return st;
+  };
+  if (c.abi_version != SWFD_ABI_VERSION) return bad(SWFD_ERR_INVALID, "abi_version mismatch");
+  if (c.literals != SWFD_LITERALS_DOUBLE)
+    return bad(SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
+  if (c.precision != SWFD_PRECISION_FP64)
+    return bad(SWFD_ERR_UNSUPPORTED, "precision: only SWFD_PRECISION_FP64 is built");
+  if (c.use_limiter != 0 && c.use_limiter != 2)
+    return bad(SWFD_ERR_UNSUPPORTED, "use_limiter must be 0 or 2");
+  if (c.ubar_mode != SWFD_UBAR_SEQUENTIAL)
+    return bad(SWFD_ERR_UNSUPPORTED, "ubar_mode: only sequential is built");
+  if (c.swp_num < 1) return bad(SWFD_ERR_INVALID, "swp_num must be >= 1");
+  if (c.sweep_mode != SWFD_SWEEP_PARALLEL && c.sweep_mode != SWFD_SWEEP_SEQUENTIAL)
+    return bad(SWFD_ERR_INVALID, "unknown sweep_mode");
+  if (!(c.gamma > 1.0)) return bad(SWFD_ERR_INVALID, "gamma must be > 1");
+  return SWFD_OK;
+}
+
 swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   Geom& g = p.g;
   p.problem = c.problem;
@@ -141,6 +133,45 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   g.plane = (int64_t)g.pitch * g.LJ;
   return SWFD_OK;
 }
+
+}  // namespace swfd
+
+namespace {
+thread_local std::string g_last_error;
+}  // namespace
+
+void swfd::set_last_error(const std::string& m) { g_last_error = m; }
+
+namespace {
+
+swfd_status fail(swfd_handle* h, swfd_status st, const std::string& msg) {
+  if (h) h->last_error = msg;
+  g_last_error = msg;
+  return st;
+}
+
+#define CU(h, call)                                                                 \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail((h), e_ == cudaErrorMemoryAllocation ? SWFD_ERR_OOM : SWFD_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+// launch `call`, which issues n kernels of this library, and count them
+#define LAUNCH(h, n, call)            \
+  do {                                \
+    CU((h), (call));                  \
+    (h)->prof.kernel_launches += (n); \
+  } while (0)
+
+#define ST(call)                          \
+  do {                                    \
+    swfd_status s_ = (call);              \
+    if (s_ != SWFD_OK) return s_;         \
+  } while (0)
+
+int64_t host_len(const Params& p) { return (int64_t)p.g.nc * p.g.LI * p.g.LJ; }
 
 // ---------------------------------------------------------------------------
 // initial data on the host (same libm as the reference's gfortran runtime)
@@ -415,24 +446,12 @@ swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
 swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if (!cfg || !out) return fail(nullptr, SWFD_ERR_INVALID, "NULL argument");
   *out = nullptr;
-  if (cfg->abi_version != SWFD_ABI_VERSION)
-    return fail(nullptr, SWFD_ERR_INVALID, "abi_version mismatch");
-  if (cfg->literals != SWFD_LITERALS_DOUBLE)
-    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
-  if (cfg->precision != SWFD_PRECISION_FP64)
-    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "precision: only SWFD_PRECISION_FP64 is built");
-  if (cfg->use_limiter != 0 && cfg->use_limiter != 2)
-    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "use_limiter must be 0 or 2");
-  if (cfg->ubar_mode != SWFD_UBAR_SEQUENTIAL)
-    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "ubar_mode: only sequential is built");
-  if (cfg->swp_num < 1) return fail(nullptr, SWFD_ERR_INVALID, "swp_num must be >= 1");
-  if (cfg->sweep_mode != SWFD_SWEEP_PARALLEL && cfg->sweep_mode != SWFD_SWEEP_SEQUENTIAL)
-    return fail(nullptr, SWFD_ERR_INVALID, "unknown sweep_mode");
-  if (!(cfg->gamma > 1.0)) return fail(nullptr, SWFD_ERR_INVALID, "gamma must be > 1");
+  std::string err;
+  swfd_status st = check_config(*cfg, err);
+  if (st != SWFD_OK) return fail(nullptr, st, err);
   swfd_handle* h = new swfd_handle();
   h->cfg = *cfg;
-  std::string err;
-  swfd_status st = make_params(*cfg, h->p, err);
+  st = make_params(*cfg, h->p, err);
   if (st != SWFD_OK) {
     delete h;
     return fail(nullptr, st, err);

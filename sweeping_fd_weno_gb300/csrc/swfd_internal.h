@@ -101,6 +101,11 @@ struct swfd_handle {
 
 namespace swfd {
 
+// api.cu
+swfd_status check_config(const swfd_config& c, std::string& err);
+swfd_status make_params(const swfd_config& c, Params& p, std::string& err);
+void set_last_error(const std::string& m);  // the process-wide message of swfd_last_error
+
 // kernels.cu
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
