@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "swfd_control.h"
 #include "swfd_internal.h"
 
 using namespace swfd;
@@ -243,133 +244,289 @@ double* cur_state(swfd_handle* h) { return h->st[h->cur]; }
 swfd_status sync_scalars(swfd_handle* h) {
   CU(h, cudaMemcpyAsync(h->hsc, h->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
+  h->time = h->hsc->time;
   return SWFD_OK;
 }
 
+// report (and clear) the error bits the device set during the last launch
 swfd_status check_device_error(swfd_handle* h) {
   ST(sync_scalars(h));
-  if (h->hsc->error) {
-    int e = h->hsc->error;
-    h->hsc->error = 0;
-    CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
-    return fail(h, SWFD_ERR_NONFINITE,
-                std::string("non-finite ") + ((e & 1) ? "alphamax" : "dt") + " on the device");
-  }
+  int e = h->hsc->error;
+  if (!e) return SWFD_OK;
+  CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  h->hsc->error = 0;
+  if (e & ERR_BIT_PUBAR) return fail(h, SWFD_ERR_PUBAR_NONPOS, "P(u_bar) <= 0");
+  if (e & ERR_BIT_NOCONV) return fail(h, SWFD_ERR_SWEEP_NOCONV, "SWEEP FAIL: swp_num reached");
+  return fail(h, SWFD_ERR_NONFINITE,
+              std::string("non-finite ") + ((e & ERR_BIT_ALPHA) ? "alphamax" : "dt") + " on the device");
+}
+
+// the device track arrays must hold sweep_count + extra entries
+swfd_status ensure_tracks(swfd_handle* h, int64_t extra) {
+  ST(sync_scalars(h));
+  int64_t need = h->hsc->sweep_count + extra;
+  if (need <= h->track_cap) return SWFD_OK;
+  int64_t cap = std::max<int64_t>(need, 2 * h->track_cap + 1024);
+  int* nt = nullptr;
+  CU(h, cudaMalloc(&nt, 3 * cap * sizeof(int)));
+  CU(h, cudaMemsetAsync(nt, 0, 3 * cap * sizeof(int), h->stream));
+  if (h->d_tracks)
+    for (int k = 0; k < 3; ++k)
+      CU(h, cudaMemcpyAsync(nt + k * cap, h->d_tracks + k * h->track_cap,
+                            h->track_cap * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+  CU(h, cudaMemcpyAsync(&h->dsc->tracks, &nt, sizeof(int*), cudaMemcpyHostToDevice, h->stream));
+  long long c = cap;
+  CU(h, cudaMemcpyAsync(&h->dsc->track_cap, &c, sizeof(long long), cudaMemcpyHostToDevice,
+                        h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  cudaFree(h->d_tracks);
+  h->d_tracks = nt;
+  h->track_cap = cap;
   return SWFD_OK;
 }
 
 // ---------------------------------------------------------------------------
+// Graph construction.  Work is recorded by stream capture; a conditional node
+// is spliced into the capture (cudaStreamGetCaptureInfo + cudaGraphAddNode +
+// cudaStreamUpdateCaptureDependencies) and its body is captured on the
+// stream of the next nesting depth.  The control kernels of swfd_control.cu
+// set the conditions on the device.
+// ---------------------------------------------------------------------------
+struct Builder {
+  swfd_handle* h;
+  cudaGraph_t root = nullptr;
+  int depth = 0;
+  int* count = nullptr;  // kernels emitted into the current section
+  cudaError_t err = cudaSuccess;
+  bool ok(cudaError_t e) {
+    if (e != cudaSuccess && err == cudaSuccess) err = e;
+    return err == cudaSuccess;
+  }
+  void k(int n) {
+    if (count) *count += n;
+  }
+  template <class F>
+  void cond(cudaStream_t s, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hnd,
+            F body) {
+    if (err != cudaSuccess) return;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (!ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd))) return;
+    // cudaGraphNodeParams has no default constructor (its union holds
+    // members with constructors): build it in zeroed raw storage
+    alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+    memset(raw, 0, sizeof(raw));
+    cudaGraphNodeParams* np = reinterpret_cast<cudaGraphNodeParams*>(raw);
+    np->type = cudaGraphNodeTypeConditional;
+    np->conditional.handle = hnd;
+    np->conditional.type = type;
+    np->conditional.size = 1;
+    cudaGraphNode_t node;
+    if (!ok(cudaGraphAddNode(&node, g, deps, nullptr, nd, np))) return;
+    if (!ok(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                                cudaStreamSetCaptureDependencies)))
+      return;
+    cudaGraph_t bg = np->conditional.phGraph_out[0];
+    cudaStream_t sb = h->cap[++depth];
+    if (ok(cudaStreamBeginCaptureToGraph(sb, bg, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeRelaxed))) {
+      body(sb);
+      cudaGraph_t tmp;
+      ok(cudaStreamEndCapture(sb, &tmp));
+    }
+    --depth;
+  }
+  cudaGraphConditionalHandle handle() {
+    cudaGraphConditionalHandle hnd = 0;
+    ok(cudaGraphConditionalHandleCreate(&hnd, root, 0, 0));
+    return hnd;
+  }
+};
+
+#define B_OK(b, call) \
+  do {                \
+    (b).ok(call);     \
+  } while (0)
+
 // sweep_lim (ex3_vortex_accuracy_2d/main.f90:888-1137; 1D ex2_sedov_1d/main.f90:564-726;
 // ex4 P(u_bar) check :1447-1454 and stop :1747-1752; ex5 `>=` exit :1162)
-// ---------------------------------------------------------------------------
-swfd_status sweep_lim(swfd_handle* h, double* u) {
+void emit_sweep(Builder& b, cudaStream_t s, double* u) {
+  swfd_handle* h = b.h;
   const Params& p = h->p;
-  cudaStream_t s = h->stream;
-  // density sweep
   const bool seq = h->cfg.sweep_mode == SWFD_SWEEP_SEQUENTIAL;
-  auto density = [&]() -> swfd_status {
+  int* saved = b.count;
+  h->k_density = 0;
+  h->k_q = 0;
+  auto density = [&](cudaStream_t sd) {
+    b.count = &h->k_density;
     if (seq) {
-      LAUNCH(h, 1, launch_density_sweep(p, u, s));
+      B_OK(b, launch_density_sweep(p, u, sd));
+      b.k(1);
     } else {
       int n = 0;
-      CU(h, launch_density_sweep_par(p, u, h->sweep_scratch, s, &n));
-      h->prof.kernel_launches += n;
+      B_OK(b, launch_density_sweep_par(p, u, h->sweep_scratch, sd, &n));
+      b.k(n);
     }
-    return SWFD_OK;
+    if (p.g.ndim == 1) {
+      B_OK(b, launch_count_density(h->dsc, sd));
+      b.k(1);
+    }
+    b.count = saved;
   };
   if (p.g.ndim == 1) {
-    ST(density());
-    h->den_count++;
+    density(s);
   } else {
-    LAUNCH(h, 1, launch_rho_min(p, u, h->dsc, s));
-    ST(sync_scalars(h));
-    unsigned long long k = h->hsc->rho_min_key;
-    unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-    double rho_min;
-    memcpy(&rho_min, &b, sizeof(double));
-    if (rho_min < 1e-12) {
-      ST(density());
-      h->den_count++;
-    }
+    B_OK(b, launch_rho_min(p, u, h->dsc, s));
+    cudaGraphConditionalHandle hd = b.handle();
+    B_OK(b, launch_cond_density(hd, h->dsc, s));
+    b.k(2);
+    b.cond(s, cudaGraphCondTypeIf, hd, density);
   }
-  LAUNCH(h, 1, launch_ubar(p, u, h->dsc, s));
-  if (p.problem == SWFD_PROBLEM_SEDOV_2D) {
-    ST(sync_scalars(h));
-    const double* ub = h->hsc->ubar;
-    if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.)
-      return fail(h, SWFD_ERR_PUBAR_NONPOS, "P(u_bar) <= 0");
-  }
-  h->sweep_count++;
-  h->sweep_track.push_back(0);
-  h->neg_track.push_back(0);
-  h->pos_track.push_back(0);
-  CU(h, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
-  for (int q = 1; q <= h->cfg.swp_num; ++q) {
-    int ord = (q % 2 == 1) ? 1 : 2;
+  B_OK(b, launch_ubar(p, u, h->dsc, s));
+  cudaGraphConditionalHandle hw = b.handle();
+  B_OK(b, launch_sweep_begin(hw, p, h->dsc, p.problem == SWFD_PROBLEM_SEDOV_2D, h->cfg.swp_num, s));
+  B_OK(b, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
+  b.k(2);
+  b.cond(s, cudaGraphCondTypeWhile, hw, [&](cudaStream_t sq) {
+    b.count = &h->k_q;
+    B_OK(b, launch_q_begin(p, h->dsc, sq));
+    b.k(1);
     if (seq) {
-      LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 1, h->dsc, s));
-      LAUNCH(h, 1, launch_pressure_pass(p, u, ord, 0, h->dsc, s));
+      B_OK(b, launch_pressure_pass(p, u, -1, 1, h->dsc, sq));
+      B_OK(b, launch_pressure_pass(p, u, -1, 0, h->dsc, sq));
+      b.k(2);
     } else {
       int n = 0;
-      CU(h, launch_pressure_pass_par(p, u, ord, 1, h->sweep_scratch, h->dsc, s, &n));
-      CU(h, launch_pressure_pass_par(p, u, ord, 0, h->sweep_scratch, h->dsc, s, &n));
-      h->prof.kernel_launches += n;
+      B_OK(b, launch_pressure_pass_par(p, u, -1, 1, h->sweep_scratch, h->dsc, sq, &n));
+      B_OK(b, launch_pressure_pass_par(p, u, -1, 0, h->sweep_scratch, h->dsc, sq, &n));
+      b.k(n);
     }
-    LAUNCH(h, 1, launch_exit_count(p, u, h->dsc, s));
-    ST(sync_scalars(h));
-    h->pre_count++;
-    if (h->hsc->bad_count == 0) {
-      h->sweep_track.back() = q;
-      h->neg_track.back() = (int32_t)h->hsc->t_neg;
-      h->pos_track.back() = (int32_t)h->hsc->t_pos;
-      break;
-    }
-    if (q == h->cfg.swp_num) {
-      h->fail_count++;
-      if (p.problem == SWFD_PROBLEM_SEDOV_2D)
-        return fail(h, SWFD_ERR_SWEEP_NOCONV, "SWEEP FAIL: swp_num reached");
-    }
-  }
-  return SWFD_OK;
+    B_OK(b, launch_exit_count(p, u, h->dsc, sq));
+    B_OK(b, launch_q_end(hw, h->dsc, h->cfg.swp_num, p.problem == SWFD_PROBLEM_SEDOV_2D, sq));
+    b.k(2);
+    b.count = saved;
+  });
 }
 
 // one RK stage: findalpha, [dt], LF split, WENO fluxes, RHS + RK combination +
-// checkpositivity, [sweep], bc
-swfd_status stage(swfd_handle* h, int k, double* in, double* u0, double* out) {
+// checkpositivity, [sweep], bc  (ex3_vortex_accuracy_2d/main.f90:564-632)
+void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, double* out,
+                bool events) {
+  swfd_handle* h = b.h;
   const Params& p = h->p;
-  cudaStream_t s = h->stream;
-  LAUNCH(h, 2, launch_alpha(p, in, h->dsc, s));
-  if (k == 1) LAUNCH(h, 1, launch_dt(p, h->dsc, s));
-  LAUNCH(h, 1, launch_prep(p, in, h->dsc, h->split, h->roe, s));
-  if (h->prof_on) CU(h, cudaEventRecord(h->ev[0], s));
-  LAUNCH(h, p.g.ndim == 2 ? 2 : 1,
-         launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
-  if (h->prof_on) CU(h, cudaEventRecord(h->ev[1], s));
-  LAUNCH(h, 1, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
-  h->prof.stages++;
-  if (h->prof_on) {
-    float ms = 0.f;
-    CU(h, cudaEventSynchronize(h->ev[1]));
-    CU(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
-    h->prof.flux_ms += ms;
-    h->prof.flux_launches += p.g.ndim == 2 ? 2 : 1;
+  B_OK(b, launch_alpha(p, in, h->dsc, s));
+  b.k(2);
+  if (k == 1) {
+    B_OK(b, launch_dt(p, h->dsc, s));
+    b.k(1);
   }
+  B_OK(b, launch_prep(p, in, h->dsc, h->split, h->roe, s));
+  b.k(1);
+  if (events) B_OK(b, cudaEventRecord(h->ev[2 * (k - 1)], s));
+  B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
+  b.k(p.g.ndim == 2 ? 2 : 1);
+  if (events) B_OK(b, cudaEventRecord(h->ev[2 * (k - 1) + 1], s));
+  B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
+  b.k(1);
   if (h->cfg.use_limiter == 2) {
-    ST(sync_scalars(h));
-    if (h->hsc->postag) {
-      if (h->prof_on) CU(h, cudaEventRecord(h->ev[2], s));
-      ST(sweep_lim(h, out));
-      if (h->prof_on) {
-        float ms = 0.f;
-        CU(h, cudaEventRecord(h->ev[3], s));
-        CU(h, cudaEventSynchronize(h->ev[3]));
-        CU(h, cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
-        h->prof.sweep_ms += ms;
-        h->prof.sweep_invocations++;
-      }
-    }
+    cudaGraphConditionalHandle hs = b.handle();
+    B_OK(b, launch_cond_postag(hs, h->dsc, s));
+    b.k(1);
+    int* saved = b.count;
+    h->k_sweep_fixed = 0;  // every stage emits the same sweep: count it once
+    b.count = &h->k_sweep_fixed;
+    b.cond(s, cudaGraphCondTypeIf, hs, [&](cudaStream_t sw) { emit_sweep(b, sw, out); });
+    b.count = saved;
   }
-  LAUNCH(h, p.g.ndim == 2 ? 1 : 0, launch_bc(p, out, s));
+  if (p.g.ndim == 2) {
+    B_OK(b, launch_bc(p, out, s));
+    b.k(1);
+  }
+}
+
+void emit_step(Builder& b, cudaStream_t s, bool events) {
+  swfd_handle* h = b.h;
+  double* X = h->st[h->cur];
+  double* Y = h->st[(h->cur + 1) % 3];
+  double* Z = h->st[(h->cur + 2) % 3];
+  int* saved = b.count;
+  h->k_stage = 0;
+  b.count = &h->k_stage;  // the three stages, sweeps counted apart
+  emit_stage(b, s, 1, X, X, Y, events);
+  emit_stage(b, s, 2, Y, X, Z, events);
+  emit_stage(b, s, 3, Z, X, X, events);
+  b.count = saved;
+}
+
+enum { GRAPH_STEP = 0, GRAPH_SOLVE = 1, GRAPH_SWEEP = 2 };
+
+swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
+  if (*out) return SWFD_OK;
+  Builder b;
+  b.h = h;
+  cudaStream_t s = h->cap[0];
+  CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  cudaStreamCaptureStatus cs;
+  b.ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &b.root, nullptr, nullptr, nullptr));
+  if (kind == GRAPH_STEP) {
+    emit_step(b, s, true);
+    B_OK(b, launch_time_advance(h->dsc, s));
+  } else if (kind == GRAPH_SOLVE) {
+    const double T = h->cfg.time_terminal;
+    B_OK(b, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), s));
+    cudaGraphConditionalHandle hr = b.handle();
+    B_OK(b, launch_run_cond(hr, h->dsc, T, s));
+    b.cond(s, cudaGraphCondTypeWhile, hr, [&](cudaStream_t sb) {
+      emit_step(b, sb, false);
+      B_OK(b, launch_time_advance_cond(hr, h->dsc, T, sb));
+    });
+  } else {
+    h->k_sweep_fixed = 0;
+    b.count = &h->k_sweep_fixed;
+    emit_sweep(b, s, h->st[h->cur]);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s, &g);
+  if (b.err != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(h, SWFD_ERR_CUDA,
+                std::string("graph capture: ") +
+                    cudaGetErrorString(b.err != cudaSuccess ? b.err : e2));
+  }
+  cudaError_t e3 = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e3 != cudaSuccess)
+    return fail(h, SWFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+  return SWFD_OK;
+}
+
+// kernels run by a launch, from the counters' increments (a step: its three
+// stages and the time advance; a sweep: its fixed part, the density sweep if
+// it ran, and one body per iteration q)
+void account(swfd_handle* h, const DevScalars& before, const DevScalars& after, int64_t steps,
+             int64_t extra) {
+  int64_t sweeps = after.sweep_count - before.sweep_count;
+  int64_t dens = after.den_count - before.den_count;
+  int64_t qs = after.pre_count - before.pre_count;
+  h->prof.kernel_launches += steps * (h->k_stage + 1) + sweeps * h->k_sweep_fixed +
+                             dens * h->k_density + qs * h->k_q + extra;
+  h->prof.stages += 3 * steps;
+  h->prof.sweep_invocations += sweeps;
+}
+
+// write the host-held parts of the device scalars (tracks) after a reset
+swfd_status reset_scalars(swfd_handle* h) {
+  memset(h->hsc, 0, sizeof(DevScalars));
+  h->hsc->tracks = h->d_tracks;
+  h->hsc->track_cap = h->track_cap;
+  CU(h, cudaMemcpyAsync(h->dsc, h->hsc, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream));
+  if (h->d_tracks)
+    CU(h, cudaMemsetAsync(h->d_tracks, 0, 3 * h->track_cap * sizeof(int), h->stream));
+  CU(h, cudaStreamSynchronize(h->stream));
+  h->time = 0;
   return SWFD_OK;
 }
 
@@ -480,17 +637,26 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if ((e = cudaMalloc(&h->d_stage, hb)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMalloc(&h->sweep_scratch, sweep_scratch_bytes(h->p))) != cudaSuccess)
     return cleanup_fail(e);
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < 8; ++k)
     if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
+  for (int k = 0; k < 4; ++k)
+    if ((e = cudaStreamCreateWithFlags(&h->cap[k], cudaStreamNonBlocking)) != cudaSuccess)
+      return cleanup_fail(e);
+  h->track_cap = 1024;
+  if ((e = cudaMalloc(&h->d_tracks, 3 * h->track_cap * sizeof(int))) != cudaSuccess)
+    return cleanup_fail(e);
   for (int k = 0; k < 3; ++k)
     if ((e = cudaMemsetAsync(h->st[k], 0, g.nc * pb, h->stream)) != cudaSuccess)
       return cleanup_fail(e);
   if ((e = cudaMemsetAsync(h->split, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMemsetAsync(h->roe, 0, 8 * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMemsetAsync(h->flux, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
-  if ((e = cudaMemsetAsync(h->dsc, 0, sizeof(DevScalars), h->stream)) != cudaSuccess)
-    return cleanup_fail(e);
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if (reset_scalars(h) != SWFD_OK) {
+    std::string m = h->last_error;
+    swfd_destroy(h);
+    return fail(nullptr, SWFD_ERR_CUDA, m);
+  }
   *out = h;
   return SWFD_OK;
 }
@@ -508,8 +674,14 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);
   if (h->hsc) cudaFreeHost(h->hsc);
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < 8; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_solve) cudaGraphExecDestroy(h->g_solve);
+  if (h->g_sweep) cudaGraphExecDestroy(h->g_sweep);
+  for (int k = 0; k < 4; ++k)
+    if (h->cap[k]) cudaStreamDestroy(h->cap[k]);
+  cudaFree(h->d_tracks);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SWFD_OK;
@@ -540,14 +712,8 @@ swfd_status swfd_init_problem(swfd_handle* h) {
   std::vector<double> u((size_t)host_len(h->p));
   init_host(h, u.data());
   ST(swfd_upload_state(h, u.data()));
-  CU(h, launch_bc(h->p, cur_state(h), h->stream));
-  h->time = 0;
-  h->sweep_count = h->den_count = h->pre_count = h->fail_count = 0;
-  h->sweep_track.clear();
-  h->neg_track.clear();
-  h->pos_track.clear();
-  CU(h, cudaMemsetAsync(h->dsc, 0, sizeof(DevScalars), h->stream));
-  CU(h, cudaStreamSynchronize(h->stream));
+  LAUNCH(h, h->p.g.ndim == 2 ? 1 : 0, launch_bc(h->p, cur_state(h), h->stream));
+  ST(reset_scalars(h));
   return SWFD_OK;
 }
 
@@ -569,37 +735,53 @@ swfd_status swfd_set_time(swfd_handle* h, double t) {
 swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   CU(h, cudaSetDevice(h->device));
-  double* X = h->st[h->cur];
-  double* Y = h->st[(h->cur + 1) % 3];
-  double* Z = h->st[(h->cur + 2) % 3];
-  ST(stage(h, 1, X, X, Y));
-  ST(stage(h, 2, Y, X, Z));
-  ST(stage(h, 3, Z, X, X));
-  LAUNCH(h, 1, launch_time_advance(h->dsc, h->stream));
-  ST(check_device_error(h));
-  h->time = h->hsc->time;
+  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  ST(ensure_tracks(h, 3));
+  DevScalars before = *h->hsc;
+  CU(h, cudaGraphLaunch(h->g_step, h->stream));
+  swfd_status st = check_device_error(h);
+  account(h, before, *h->hsc, 1, 0);
+  if (h->prof_on) {
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      CU(h, cudaEventElapsedTime(&ms, h->ev[2 * k], h->ev[2 * k + 1]));
+      h->prof.flux_ms += ms;
+      h->prof.flux_launches += h->p.g.ndim == 2 ? 2 : 1;
+    }
+  }
   if (dt_out) *dt_out = h->hsc->dt;
-  return SWFD_OK;
+  return st;
 }
 
 swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
-  int64_t k = 0;
-  // DO WHILE (time <= time_terminal - 1d-10)  (ex3_vortex_accuracy_2d/main.f90:51)
+  CU(h, cudaSetDevice(h->device));
+  ST(build_graph(h, GRAPH_SOLVE, &h->g_solve));
+  int64_t done = 0;
+  const int64_t chunk = 4096;  // steps per graph launch (bounds the track growth)
+  swfd_status st = SWFD_OK;
+  // DO WHILE (time <= time_terminal - 1d-10)  (ex3_vortex_accuracy_2d/main.f90:51),
+  // evaluated on the device after every step
   while (h->time <= h->cfg.time_terminal - 1e-10) {
-    if (max_steps > 0 && k >= max_steps) {
-      if (nsteps_out) *nsteps_out = k;
-      return SWFD_ERR_MAX_STEPS;
+    if (max_steps > 0 && done >= max_steps) {
+      st = SWFD_ERR_MAX_STEPS;
+      break;
     }
-    swfd_status st = swfd_step(h, nullptr);
-    if (st != SWFD_OK) {
-      if (nsteps_out) *nsteps_out = k;
-      return st;
-    }
-    ++k;
+    long long lim = (long long)(max_steps > 0 ? std::min<int64_t>(chunk, max_steps - done) : chunk);
+    ST(ensure_tracks(h, 3 * lim));
+    DevScalars before = *h->hsc;
+    CU(h, cudaMemcpyAsync(&h->dsc->steps_limit, &lim, sizeof(long long), cudaMemcpyHostToDevice,
+                          h->stream));
+    CU(h, cudaGraphLaunch(h->g_solve, h->stream));
+    st = check_device_error(h);
+    int64_t steps = h->hsc->steps;
+    account(h, before, *h->hsc, steps, 2);
+    done += steps;
+    if (st != SWFD_OK) break;
+    if (steps < lim) break;  // the time test ended the loop
   }
-  if (nsteps_out) *nsteps_out = k;
-  return SWFD_OK;
+  if (nsteps_out) *nsteps_out = done;
+  return st;
 }
 
 swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
@@ -621,9 +803,13 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
 swfd_status swfd_sweep(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   CU(h, cudaSetDevice(h->device));
-  ST(sweep_lim(h, cur_state(h)));
-  CU(h, cudaStreamSynchronize(h->stream));
-  return SWFD_OK;
+  ST(build_graph(h, GRAPH_SWEEP, &h->g_sweep));
+  ST(ensure_tracks(h, 1));
+  DevScalars before = *h->hsc;
+  CU(h, cudaGraphLaunch(h->g_sweep, h->stream));
+  swfd_status st = check_device_error(h);
+  account(h, before, *h->hsc, 0, 0);
+  return st;
 }
 
 swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
@@ -644,33 +830,53 @@ swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax) {
   return SWFD_OK;
 }
 
+namespace {
+swfd_status fetch_tracks(swfd_handle* h, std::vector<int32_t>& tr, int64_t& n) {
+  ST(sync_scalars(h));
+  n = std::min<int64_t>(h->hsc->sweep_count, h->track_cap);
+  tr.assign(3 * (size_t)n, 0);
+  for (int k = 0; k < 3 && n > 0; ++k)
+    CU(h, cudaMemcpy(tr.data() + k * n, h->d_tracks + k * h->track_cap, n * sizeof(int32_t),
+                     cudaMemcpyDeviceToHost));
+  return SWFD_OK;
+}
+}  // namespace
+
 swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
   if (!h || !s) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  std::vector<int32_t> tr;
+  int64_t n = 0;
+  ST(fetch_tracks(h, tr, n));
   memset(s, 0, sizeof(*s));
-  s->sweep_count = h->sweep_count;
-  for (size_t k = 0; k < h->sweep_track.size(); ++k) {
-    s->total_sweep += h->sweep_track[k];
-    s->total_neg += h->neg_track[k];
-    s->total_pos += h->pos_track[k];
-    if (k == 0 || h->sweep_track[k] > s->max_sweep) s->max_sweep = h->sweep_track[k];
-    if (k == 0 || h->neg_track[k] > s->max_neg) s->max_neg = h->neg_track[k];
-    if (k == 0 || h->pos_track[k] > s->max_pos) s->max_pos = h->pos_track[k];
+  s->sweep_count = h->hsc->sweep_count;
+  for (int64_t k = 0; k < n; ++k) {
+    int32_t sw = tr[k], ng = tr[n + k], ps = tr[2 * n + k];
+    s->total_sweep += sw;
+    s->total_neg += ng;
+    s->total_pos += ps;
+    if (k == 0 || sw > s->max_sweep) s->max_sweep = sw;
+    if (k == 0 || ng > s->max_neg) s->max_neg = ng;
+    if (k == 0 || ps > s->max_pos) s->max_pos = ps;
   }
-  s->den_count = h->den_count;
-  s->pre_count = h->pre_count;
-  s->sweep_fail_count = h->fail_count;
+  s->den_count = h->hsc->den_count;
+  s->pre_count = h->hsc->pre_count;
+  s->sweep_fail_count = h->hsc->fail_count;
   return SWFD_OK;
 }
 
 swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos,
                                   int64_t cap, int64_t* count) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
-  int64_t n = (int64_t)h->sweep_track.size();
+  CU(h, cudaSetDevice(h->device));
+  std::vector<int32_t> tr;
+  int64_t n = 0;
+  ST(fetch_tracks(h, tr, n));
   int64_t m = std::min<int64_t>(n, std::max<int64_t>(cap, 0));
   for (int64_t k = 0; k < m; ++k) {
-    if (sweep) sweep[k] = h->sweep_track[k];
-    if (neg) neg[k] = h->neg_track[k];
-    if (pos) pos[k] = h->pos_track[k];
+    if (sweep) sweep[k] = tr[k];
+    if (neg) neg[k] = tr[n + k];
+    if (pos) pos[k] = tr[2 * n + k];
   }
   if (count) *count = n;
   return SWFD_OK;

@@ -1,0 +1,133 @@
+// swfd_control.cu -- single-thread kernels that take the decisions the
+// reference takes on the host between its loops, so that a step (and a whole
+// solve) runs as one CUDA graph: they update the statistics counters and set
+// the values of the graph's conditional nodes (IF / WHILE).
+#include "swfd_control.h"
+
+namespace swfd {
+
+__device__ __forceinline__ double decode_key(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+// IF postag == 1 (ex3_vortex_accuracy_2d/main.f90:590-595)
+__global__ void k_cond_postag(cudaGraphConditionalHandle h, const DevScalars* d) {
+  cudaGraphSetConditional(h, d->postag ? 1u : 0u);
+}
+
+// IF rho_min < 1d-12 (ex3_vortex_accuracy_2d/main.f90:1155-1156); den_count (:1187)
+__global__ void k_cond_density(cudaGraphConditionalHandle h, DevScalars* d) {
+  bool go = decode_key(d->rho_min_key) < 1e-12;
+  if (go) d->den_count++;
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// 1D: the density sweep always runs (ex2_sedov_1d/main.f90:774)
+__global__ void k_count_density(DevScalars* d) { d->den_count++; }
+
+// sweep_lim set-up after u_bar (ex3_vortex_accuracy_2d/main.f90:928-930;
+// ex4's P(u_bar) <= 0 stop, ex4_sedov_2d/main.f90:1447-1454)
+__global__ void k_sweep_begin(cudaGraphConditionalHandle h, Params p, DevScalars* d,
+                              int check_pubar, int swp_num) {
+  if (check_pubar) {
+    const double* ub = d->ubar;
+    if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.) {
+      d->error |= ERR_BIT_PUBAR;
+      cudaGraphSetConditional(h, 0u);
+      return;
+    }
+  }
+  long long k = d->sweep_count++;
+  if (k < d->track_cap) {
+    d->tracks[k] = 0;
+    d->tracks[d->track_cap + k] = 0;
+    d->tracks[2 * d->track_cap + k] = 0;
+  }
+  d->t_pos = 0;
+  d->t_neg = 0;
+  d->q = 0;
+  cudaGraphSetConditional(h, swp_num >= 1 ? 1u : 0u);
+}
+
+// start of sweep iteration q: odd q ordering I, even q ordering II (:933)
+__global__ void k_q_begin(Params p, DevScalars* d) {
+  int q = ++d->q;
+  d->ordering = p.g.ndim == 1 ? 0 : ((q & 1) ? 1 : 2);
+}
+
+// end of sweep iteration q: pre_count, exit test and tracks (:1116-1129)
+__global__ void k_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num, int stop_on_fail) {
+  d->pre_count++;
+  if (d->bad_count == 0) {
+    long long k = d->sweep_count - 1;
+    if (k >= 0 && k < d->track_cap) {
+      d->tracks[k] = d->q;
+      d->tracks[d->track_cap + k] = (int)d->t_neg;
+      d->tracks[2 * d->track_cap + k] = (int)d->t_pos;
+    }
+    cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  if (d->q >= swp_num) {
+    d->fail_count++;
+    if (stop_on_fail) d->error |= ERR_BIT_NOCONV;
+    cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  cudaGraphSetConditional(h, 1u);
+}
+
+// DO WHILE (time <= time_terminal - 1d-10) (ex3_vortex_accuracy_2d/main.f90:51),
+// bounded by the launch's step limit and stopped by an error
+__global__ void k_run_cond(cudaGraphConditionalHandle h, const DevScalars* d, double t_end) {
+  bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// time = time + dt (:53), then the loop test
+__global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end) {
+  d->time = d->time + d->dt;
+  d->steps++;
+  bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, const DevScalars* d, cudaStream_t s) {
+  k_cond_postag<<<1, 1, 0, s>>>(h, d);
+  return cudaGetLastError();
+}
+cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s) {
+  k_cond_density<<<1, 1, 0, s>>>(h, d);
+  return cudaGetLastError();
+}
+cudaError_t launch_count_density(DevScalars* d, cudaStream_t s) {
+  k_count_density<<<1, 1, 0, s>>>(d);
+  return cudaGetLastError();
+}
+cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, DevScalars* d,
+                               int check_pubar, int swp_num, cudaStream_t s) {
+  k_sweep_begin<<<1, 1, 0, s>>>(h, p, d, check_pubar, swp_num);
+  return cudaGetLastError();
+}
+cudaError_t launch_q_begin(const Params& p, DevScalars* d, cudaStream_t s) {
+  k_q_begin<<<1, 1, 0, s>>>(p, d);
+  return cudaGetLastError();
+}
+cudaError_t launch_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num, int stop_on_fail,
+                         cudaStream_t s) {
+  k_q_end<<<1, 1, 0, s>>>(h, d, swp_num, stop_on_fail);
+  return cudaGetLastError();
+}
+cudaError_t launch_run_cond(cudaGraphConditionalHandle h, const DevScalars* d, double t_end,
+                            cudaStream_t s) {
+  k_run_cond<<<1, 1, 0, s>>>(h, d, t_end);
+  return cudaGetLastError();
+}
+cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
+                                     cudaStream_t s) {
+  k_time_advance_cond<<<1, 1, 0, s>>>(h, d, t_end);
+  return cudaGetLastError();
+}
+
+}  // namespace swfd

@@ -51,20 +51,35 @@ struct Params {
   double jet_amb[4] = {0, 0, 0, 0};
 };
 
-// Device scalars of one handle, in one small allocation.
+// Device scalars of one handle, in one small allocation.  The sweep
+// statistics and the per-sweep tracks live here so that a whole step (and a
+// whole solve) runs on the device without host round trips.
+enum : int {
+  ERR_BIT_ALPHA = 1,     // alphamax not finite or not positive
+  ERR_BIT_DT = 2,        // dt not finite
+  ERR_BIT_PUBAR = 4,     // P(u_bar) <= 0 (ex4 stop)
+  ERR_BIT_NOCONV = 8     // sweep reached swp_num (ex4 stop)
+};
+
 struct DevScalars {
   double alphamax;
   double dt;
   double time;
   double ubar[4];
-  double pmin;           // unused by the flag-count exit test, kept for stats
   unsigned long long alpha_bits;
   unsigned long long rho_min_key;
   int postag;
   int bad_count;         // cells failing the sweep exit test
-  int error;
-  int pad;
+  int error;             // ERR_BIT_*
+  int q;                 // current sweep iteration (1-based)
+  int ordering;          // ordering of the current pass (0: 1D, 1: I, 2: II)
+  int pad0;
   long long t_pos, t_neg;
+  long long sweep_count, den_count, pre_count, fail_count;
+  long long steps;        // steps taken by the current solve launch
+  long long steps_limit;  // bound of the current solve launch
+  int* tracks;            // sweep_track, neg_track, pos_track: 3 x track_cap
+  long long track_cap;
 };
 
 }  // namespace swfd
@@ -87,13 +102,19 @@ struct swfd_handle {
   swfd::DevScalars* hsc = nullptr;   // pinned host mirror
   // host-side run state
   double time = 0;
-  int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;
-  std::vector<int32_t> sweep_track, neg_track, pos_track;
   std::string last_error;
   // instrumentation
   int prof_on = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[8] = {};
   swfd_profile prof = {};
+  // CUDA graphs, built on first use: one SSP-RK3 step (with flux events),
+  // a solve (WHILE time <= T - 1d-10 over the step), and sweep_lim alone
+  cudaGraphExec_t g_step = nullptr, g_solve = nullptr, g_sweep = nullptr;
+  cudaStream_t cap[4] = {};  // capture streams, one per conditional nesting depth
+  int* d_tracks = nullptr;   // device sweep tracks (3 x track_cap)
+  int64_t track_cap = 0;
+  // kernels per graph section, for launch accounting
+  int k_stage = 0, k_sweep_fixed = 0, k_density = 0, k_q = 0, k_step = 0;
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles
@@ -129,6 +150,7 @@ cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* u
 cudaError_t launch_rho_min(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_density_sweep(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+// ordering < 0: the pass reads its ordering from dsc->ordering
 cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int forward,
                                  DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);

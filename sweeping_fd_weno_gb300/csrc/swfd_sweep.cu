@@ -190,6 +190,7 @@ cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaS
 __global__ void k_pressure_pass_seq(Params p, double* __restrict__ u, int ordering, int forward,
                                     DevScalars* dsc) {
   const Geom& g = p.g;
+  if (ordering < 0) ordering = dsc->ordering;
   const int64_t N = npos(g), P = g.plane;
   const double g1 = p.gamma1, eps = p.eps;
   double ub[4];
@@ -373,8 +374,9 @@ __device__ int64_t run_chain(const Params& p, double* u, int ordering, int forwa
 
 template <int KIND>
 __global__ void k_flag_bits(Params p, const double* __restrict__ u, int ordering, int forward,
-                            SweepScratch sc) {
+                            SweepScratch sc, const DevScalars* dsc) {
   const Geom& g = p.g;
+  if (ordering < 0) ordering = dsc->ordering;
   const int64_t N = npos(g);
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool b = false;
@@ -422,6 +424,7 @@ __global__ void __launch_bounds__(1024) k_compact(int64_t N, SweepScratch sc) {
 template <int KIND>
 __global__ void k_chain_dry(Params p, double* u, int ordering, int forward, SweepScratch sc,
                             const DevScalars* dsc) {
+  if (ordering < 0) ordering = dsc->ordering;
   const int64_t N = npos(p.g);
   const int m = sc.counters[0];
   double ub[4] = {0, 0, 0, 0};
@@ -445,6 +448,7 @@ template <int KIND>
 __global__ void k_chain_walk(Params p, double* u, int ordering, int forward, SweepScratch sc,
                              DevScalars* dsc) {
   if (sc.counters[1] == 0) return;  // no chain reaches the next flagged cell
+  if (ordering < 0) ordering = dsc->ordering;
   const int64_t N = npos(p.g);
   const int m = sc.counters[0];
   const int lane = threadIdx.x;
@@ -484,6 +488,7 @@ __global__ void k_chain_walk(Params p, double* u, int ordering, int forward, Swe
 template <int KIND>
 __global__ void k_chain_write(Params p, double* u, int ordering, int forward, SweepScratch sc,
                               DevScalars* dsc) {
+  if (ordering < 0) ordering = dsc->ordering;
   const int64_t N = npos(p.g);
   const int m = sc.counters[0];
   const bool all_roots = sc.counters[1] == 0;
@@ -533,7 +538,7 @@ static cudaError_t pass_parallel(const Params& p, double* u, int ordering, int f
   const int64_t N = npos(p.g);
   SweepScratch sc = carve(scratch, p);
   const int ord = p.g.ndim == 1 ? 0 : ordering;
-  k_flag_bits<KIND><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(p, u, ord, forward, sc);
+  k_flag_bits<KIND><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(p, u, ord, forward, sc, dsc);
   k_compact<<<1, 1024, 0, s>>>(N, sc);
   const int grid = 4 * 152;
   k_chain_dry<KIND><<<grid, 128, 0, s>>>(p, u, ord, forward, sc, dsc);
