@@ -425,10 +425,13 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
   }
   B_OK(b, launch_prep(p, in, h->dsc, h->split, h->roe, s));
   b.k(1);
-  if (events) B_OK(b, cudaEventRecord(h->ev[2 * (k - 1)], s));
+  // external event-record nodes (a plain record on a capturing stream would
+  // only be a capture dependency)
+  if (events) B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
   B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
   b.k(p.g.ndim == 2 ? 2 : 1);
-  if (events) B_OK(b, cudaEventRecord(h->ev[2 * (k - 1) + 1], s));
+  if (events)
+    B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s, cudaEventRecordExternal));
   B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
   b.k(1);
   if (h->cfg.use_limiter == 2) {
