@@ -260,7 +260,7 @@ def main():
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
            "steps": args.e2e_steps}
 
-    # dominant kernel: the WENO flux kernels (one launch per direction per stage)
+    # dominant kernel: the WENO flux kernel (one launch per stage, both directions)
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -272,17 +272,18 @@ def main():
     fp64 = C.c_double(0.0)
     abi.load().swfd_probe_fp64_peak(local, C.byref(fp64))
     flux_ms_per_launch = prof["flux_ms"] / max(prof["flux_launches"], 1)
-    # per launch (one direction of one stage): read the split fluxes (8 doubles)
-    # and Roe averages (4 doubles) of every cell once, write 8 doubles per interface
-    launch_bytes = cells * (12 + 8) * 8.0
+    # per launch (both directions of one stage): read the split fluxes (8
+    # doubles) and Roe averages (4 doubles) of every cell once per direction,
+    # write 8 doubles per interface
+    launch_bytes = 2 * cells * (12 + 8) * 8.0
     achieved = launch_bytes / (flux_ms_per_launch * 1e-3) / 1e9
-    launch_flops = cells * FLUX_FLOPS_PER_INTERFACE
+    launch_flops = 2 * cells * FLUX_FLOPS_PER_INTERFACE
     fp64_achieved = launch_flops / (flux_ms_per_launch * 1e-3) / 1e9
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "traffic": None,
         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-        "kernel": "k_flux_x / k_flux_y (characteristic WENO5 interface fluxes)",
+        "kernel": "k_flux_xy (characteristic WENO5 interface fluxes, both directions)",
         "launch_ms": flux_ms_per_launch,
         "compute_bound": "fp64",
         "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64.value,

@@ -428,8 +428,8 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
   // external event-record nodes (a plain record on a capturing stream would
   // only be a capture dependency)
   if (events) B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
-  B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, s));
-  b.k(p.g.ndim == 2 ? 2 : 1);
+  B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, &h->dsc->flux_work, s));
+  b.k(1);
   if (events)
     B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s, cudaEventRecordExternal));
   B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
@@ -749,7 +749,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
       float ms = 0.f;
       CU(h, cudaEventElapsedTime(&ms, h->ev[2 * k], h->ev[2 * k + 1]));
       h->prof.flux_ms += ms;
-      h->prof.flux_launches += h->p.g.ndim == 2 ? 2 : 1;
+      h->prof.flux_launches += 1;
     }
   }
   if (dt_out) *dt_out = h->hsc->dt;
@@ -794,7 +794,7 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
   double* u = cur_state(h);
   CU(h, launch_alpha(p, u, h->dsc, h->stream));
   CU(h, launch_prep(p, u, h->dsc, h->split, h->roe, h->stream));
-  CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? u : h->roe, h->dsc, h->flux, h->stream));
+  CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? u : h->roe, h->dsc, h->flux, &h->dsc->flux_work, h->stream));
   CU(h, launch_rhs(p, h->flux, h->dsc, h->rhs_tmp, h->stream));
   const size_t hb = (size_t)host_len(p) * sizeof(double);
   CU(h, launch_soa_to_fortran(p, h->rhs_tmp, h->d_stage, h->stream));

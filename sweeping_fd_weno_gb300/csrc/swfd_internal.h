@@ -73,7 +73,7 @@ struct DevScalars {
   int error;             // ERR_BIT_*
   int q;                 // current sweep iteration (1-based)
   int ordering;          // ordering of the current pass (0: 1D, 1: I, 2: II)
-  int pad0;
+  int flux_work;         // chunk counter of the persistent flux kernel
   long long t_pos, t_neg;
   long long sweep_count, den_count, pre_count, fail_count;
   long long steps;        // steps taken by the current solve launch
@@ -132,8 +132,9 @@ cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, double* split,
                         double* roe, cudaStream_t s);
+// work: one device int of scratch (the chunk counter of the 2D kernel)
 cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
-                        const DevScalars* dsc, double* flux, cudaStream_t s);
+                        const DevScalars* dsc, double* flux, int* work, cudaStream_t s);
 cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
                       const double* flux, const DevScalars* dsc, double* out, cudaStream_t s);

@@ -412,18 +412,90 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const double* _
   flux[5 * P + o] = r20 * ul[0] + qm * ul[1] + r22 * ul[2];
 }
 
+// Both directions in one persistent launch: a grid of exactly the resident
+// blocks, whose warps take chunks of 32 consecutive interfaces (x interfaces
+// of rows 1..ny first, then y interfaces of rows 0..ny+1) from a counter, so
+// the FP64 pipes stay busy to the last chunk instead of idling through the
+// tail of a partial last wave.
+#define SWFD_FLUX_BLOCK 128
+#define SWFD_FLUX_MINB 3
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB)
+    k_flux_xy(Params p, const double* __restrict__ split, const double* __restrict__ roe,
+              const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
+  const Geom& g = p.g;
+  const int64_t P = g.plane, pit = g.pitch;
+  const int lx = g.nx + 2;                       // x interfaces per row (0..nx+1)
+  const int64_t nx_int = (int64_t)lx * g.ny;     // rows 1..ny
+  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);  // columns 1..nx, rows 0..ny+1
+  const int64_t chunks_x = (nx_int + 31) / 32;
+  const int64_t chunks = chunks_x + (ny_int + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) break;
+    double op[4], on[4];
+    if (c < chunks_x) {
+      int64_t t = (int64_t)c * 32 + lane;
+      if (t >= nx_int) continue;
+      const int i = (int)(t % lx), j = (int)(t / lx) + 1;
+      const int64_t o = g.at(i, j);
+      Eigen2D E;
+      roe_eigen2d(p.gamma1, 0, ld(roe + o), ld(roe + o + 1), ld(roe + P + o), ld(roe + P + o + 1),
+                  ld(roe + 2 * P + o), ld(roe + 2 * P + o + 1), ld(roe + 3 * P + o),
+                  ld(roe + 3 * P + o + 1), E);
+      interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, p.weno_eps, op, on);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        flux[k * P + o] = p.alpha_premul ? am * op[k] : op[k];
+        flux[(4 + k) * P + o] = p.alpha_premul ? am * on[k] : on[k];
+      }
+    } else {
+      int64_t t = (int64_t)(c - chunks_x) * 32 + lane;
+      if (t >= ny_int) continue;
+      const int i = (int)(t % g.nx) + 1, j = (int)(t / g.nx);
+      const int64_t o = g.at(i, j);
+      const double* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+      Eigen2D E;
+      roe_eigen2d(p.gamma1, 1, ld(r + o), ld(r + o + pit), ld(r + P + o), ld(r + P + o + pit),
+                  ld(r + 2 * P + o), ld(r + 2 * P + o + pit), ld(r + 3 * P + o),
+                  ld(r + 3 * P + o + pit), E);
+      interface_flux<1>(E, split + 8 * P + o - 2 * pit, split + 12 * P + o - 2 * pit, P, pit,
+                        p.weno_eps, op, on);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        flux[(8 + k) * P + o] = p.alpha_premul ? am * op[k] : op[k];
+        flux[(12 + k) * P + o] = p.alpha_premul ? am * on[k] : on[k];
+      }
+    }
+  }
+}
+
+static int flux_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy, SWFD_FLUX_BLOCK, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  return grid;
+}
+
 cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
-                        const DevScalars* dsc, double* flux, cudaStream_t s) {
+                        const DevScalars* dsc, double* flux, int* work, cudaStream_t s) {
   const Geom& g = p.g;
   if (g.ndim == 1) {
     // the 1D eigenvectors come from the state, which the caller passes as roe
     k_flux1d<<<(g.nx + 2 + 127) / 128, 128, 0, s>>>(p, roe, split, flux);
     return cudaGetLastError();
   }
-  dim3 bx(128), gx((g.nx + 2 + 127) / 128, g.ny);
-  k_flux_x<<<gx, bx, 0, s>>>(p, split, roe, dsc, flux);
-  dim3 gy((g.nx + 127) / 128, g.ny + 2);
-  k_flux_y<<<gy, bx, 0, s>>>(p, split, roe, dsc, flux);
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_flux_xy<<<flux_grid(), SWFD_FLUX_BLOCK, 0, s>>>(p, split, roe, dsc, flux, work);
   return cudaGetLastError();
 }
 

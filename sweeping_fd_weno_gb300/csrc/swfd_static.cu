@@ -120,7 +120,7 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
   if ((e = launch_fortran_to_soa(q, u, usoa, s)) != cudaSuccess ||
       (e = launch_alpha(q, usoa, dsc, s)) != cudaSuccess ||
       (e = launch_prep(q, usoa, dsc, split, roe, s)) != cudaSuccess ||
-      (e = launch_flux(q, split, g.ndim == 1 ? usoa : roe, dsc, flux, s)) != cudaSuccess ||
+      (e = launch_flux(q, split, g.ndim == 1 ? usoa : roe, dsc, flux, &dsc->flux_work, s)) != cudaSuccess ||
       (e = launch_rhs(q, flux, dsc, rsoa, s)) != cudaSuccess ||
       (e = launch_soa_to_fortran(q, rsoa, rhs, s)) != cudaSuccess)
     return done(SWFD_ERR_CUDA, "kernel launch", e);
