@@ -178,6 +178,7 @@ def main():
     ap.add_argument("--reference-nx", type=int, default=180)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -294,6 +295,45 @@ def main():
                       "frac": STAGE_BYTES_PER_CELL * value / 1e9 / hbm_peak,
                       "bytes_per_cell_stage": STAGE_BYTES_PER_CELL},
     }
+    # the FP32-bulk precision form on the same workload, from the same state:
+    # timed the same way, with its relative L1 density error against FP64
+    fp32 = None
+    if not args.no_fp32:
+        u_start = np.empty(solver.shape)
+        s64 = Solver(problems.workload(args.workload, device=local))
+        s32 = Solver(problems.workload(args.workload, device=local,
+                                       precision=abi.PRECISION_FP32_BULK))
+        s64.init_problem()
+        s32.init_problem()
+        ext32 = torch.cuda.ExternalStream(s32.stream_ptr(), device=torch.device("cuda", local))
+        for _ in range(args.warmup):
+            s32.step()
+        s32.set_state(s64.state(out=u_start))
+        s32.time = s64.time
+        torch.cuda.synchronize()
+        ev32 = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(ext32):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(ext32)
+            s32.step()
+            b.record(ext32)
+            ev32.append((a, b))
+        torch.cuda.synchronize()
+        ms32 = sum(a.elapsed_time(b) for a, b in ev32)
+        for _ in range(args.steps):
+            s64.step()
+        r64, r32 = s64.state()[3:-3, 3:-3, 0], s32.state()[3:-3, 3:-3, 0]
+        fp32 = {"value": cells * 3 * args.steps * world / (ms32 * 1e-3),
+                "ms_per_step": ms32 / args.steps,
+                "speedup_vs_fp64": (ms_fp64 := total_ms) / ms32 if ms32 else None,
+                "rel_l1_density_err_vs_fp64": float(np.abs(r32 - r64).sum() / np.abs(r64).sum()),
+                "arithmetic": "FP32 LF splitting, WENO5 fluxes and flux differences; FP64 pressure "
+                              "recovery, RK accumulation, positivity, CFL reduction and sweeps"}
+        s32.close()
+        s64.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -308,6 +348,7 @@ def main():
         "gpu_launches": prof["kernel_launches"],
         "roofline": roofline,
         "sweep": {"invocations": prof["sweep_invocations"], "ms": prof["sweep_ms"]},
+        "fp32_bulk": fp32,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)

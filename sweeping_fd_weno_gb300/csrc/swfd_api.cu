@@ -27,8 +27,8 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
   if (c.abi_version != SWFD_ABI_VERSION) return bad(SWFD_ERR_INVALID, "abi_version mismatch");
   if (c.literals != SWFD_LITERALS_DOUBLE)
     return bad(SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
-  if (c.precision != SWFD_PRECISION_FP64)
-    return bad(SWFD_ERR_UNSUPPORTED, "precision: only SWFD_PRECISION_FP64 is built");
+  if (c.precision != SWFD_PRECISION_FP64 && c.precision != SWFD_PRECISION_FP32_BULK)
+    return bad(SWFD_ERR_INVALID, "unknown precision");
   if (c.use_limiter != 0 && c.use_limiter != 2)
     return bad(SWFD_ERR_UNSUPPORTED, "use_limiter must be 0 or 2");
   if (c.ubar_mode != SWFD_UBAR_SEQUENTIAL)
@@ -44,6 +44,7 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   Geom& g = p.g;
   p.problem = c.problem;
   p.literals = c.literals;
+  p.precision = c.precision;
   p.gamma = c.gamma;
   p.gamma1 = c.gamma - 1.;
   p.eps = 1e-13;

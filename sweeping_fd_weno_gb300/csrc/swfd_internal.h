@@ -33,6 +33,7 @@ struct Params {
   Geom g;
   int problem = 0;
   int literals = 0;
+  int precision = 0;     // SWFD_PRECISION_*
   int pos_strict = 0;    // checkpositivity uses `<` (ex4, ex5)
   int exit_ge = 0;       // sweep exit test uses `>=` (ex5)
   int alpha_guarded = 0; // findalpha with the eps2 velocity guard (ex4, ex5)
@@ -130,15 +131,16 @@ void set_last_error(const std::string& m);  // the process-wide message of swfd_
 // kernels.cu
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
-cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, double* split,
-                        double* roe, cudaStream_t s);
+// split, roe and flux planes hold doubles (FP64) or floats (FP32 bulk)
+cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
+                        void* roe, cudaStream_t s);
 // work: one device int of scratch (the chunk counter of the 2D kernel)
-cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
-                        const DevScalars* dsc, double* flux, int* work, cudaStream_t s);
+cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
+                        const DevScalars* dsc, void* flux, int* work, cudaStream_t s);
 cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
-                      const double* flux, const DevScalars* dsc, double* out, cudaStream_t s);
-cudaError_t launch_rhs(const Params& p, const double* flux, const DevScalars* dsc, double* rhs,
+                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s);
+cudaError_t launch_rhs(const Params& p, const void* flux, const DevScalars* dsc, double* rhs,
                        cudaStream_t s);
 cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s);

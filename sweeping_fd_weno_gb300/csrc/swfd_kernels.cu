@@ -177,16 +177,29 @@ cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s) {
 // (ex3_vortex_accuracy_2d/main.f90:61-131,134-147,335-348)
 // split planes: [0,nc) fp, [nc,2nc) fn, [2nc,3nc) gp, [3nc,4nc) gn
 // roe planes:   0 w, 1 vx, 2 vy, 3 h (x pass); 4..7 the y pass (ex4 only)
+// Pressure recovery from the conserved variables is FP64 in both precisions;
+// the split fluxes and Roe averages are stored and formed in T.
 // ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T ldt(const T* p) { return __ldg(p); }
+
+template <class T>
+__device__ __forceinline__ T sqrt_abs(double v);
+template <>
+__device__ __forceinline__ double sqrt_abs<double>(double v) { return sqrt(fabs(v)); }
+template <>
+__device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf((float)v)); }
+
+template <class T>
 __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalars* dsc,
-                         double* __restrict__ split, double* __restrict__ roe) {
+                         T* __restrict__ split, T* __restrict__ roe) {
   const Geom& g = p.g;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
   int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
   const int64_t o = g.at(i, j), P = g.plane;
-  const double am = dsc->alphamax, g1 = p.gamma1;
+  const double g1 = p.gamma1;
   double rho = ld(u + o), mx = ld(u + P + o), my = ld(u + 2 * P + o), e = ld(u + 3 * P + o);
   // fflux / gflux
   double vx = mx / rho, vy = my / rho;
@@ -200,25 +213,27 @@ __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalar
   double f1 = rho * (vx * vx) + pres, f3 = (e + pres) * vx;
   double g2 = rho * (vy * vy) + pres, g3 = (e + pres) * vy;
   // fp = 0.5*(u + f/alpha), fn = 0.5*(u - f/alpha); f/alpha shared by both
-  double q;
-  q = mx / am;  split[0 * P + o] = 0.5 * (rho + q); split[4 * P + o] = 0.5 * (rho - q);
-  q = f1 / am;  split[1 * P + o] = 0.5 * (mx + q);  split[5 * P + o] = 0.5 * (mx - q);
-  double qxy = fxy / am;
-  split[2 * P + o] = 0.5 * (my + qxy); split[6 * P + o] = 0.5 * (my - qxy);
-  q = f3 / am;  split[3 * P + o] = 0.5 * (e + q);   split[7 * P + o] = 0.5 * (e - q);
-  q = my / am;  split[8 * P + o] = 0.5 * (rho + q); split[12 * P + o] = 0.5 * (rho - q);
-  split[9 * P + o] = 0.5 * (mx + qxy); split[13 * P + o] = 0.5 * (mx - qxy);
-  q = g2 / am;  split[10 * P + o] = 0.5 * (my + q); split[14 * P + o] = 0.5 * (my - q);
-  q = g3 / am;  split[11 * P + o] = 0.5 * (e + q);  split[15 * P + o] = 0.5 * (e - q);
+  const T am = T(dsc->alphamax), h = T(0.5);
+  const T tr = T(rho), tmx = T(mx), tmy = T(my), te = T(e);
+  T q;
+  q = T(mx) / am;  split[0 * P + o] = h * (tr + q);   split[4 * P + o] = h * (tr - q);
+  q = T(f1) / am;  split[1 * P + o] = h * (tmx + q);  split[5 * P + o] = h * (tmx - q);
+  T qxy = T(fxy) / am;
+  split[2 * P + o] = h * (tmy + qxy); split[6 * P + o] = h * (tmy - qxy);
+  q = T(f3) / am;  split[3 * P + o] = h * (te + q);   split[7 * P + o] = h * (te - q);
+  q = T(my) / am;  split[8 * P + o] = h * (tr + q);   split[12 * P + o] = h * (tr - q);
+  split[9 * P + o] = h * (tmx + qxy); split[13 * P + o] = h * (tmx - qxy);
+  q = T(g2) / am;  split[10 * P + o] = h * (tmy + q); split[14 * P + o] = h * (tmy - q);
+  q = T(g3) / am;  split[11 * P + o] = h * (te + q);  split[15 * P + o] = h * (te - q);
   // Roe preparation (x pass; the y pass is the same except in ex4)
   double t0 = 1. / rho;
   double vex = mx * t0, vey = my * t0;
   double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
-  double w = sqrt(fabs(rho));
+  T w = sqrt_abs<T>(rho);
   roe[0 * P + o] = w;
-  roe[1 * P + o] = vex;
-  roe[2 * P + o] = vey;
-  roe[3 * P + o] = (pre + e) * t0;
+  roe[1 * P + o] = T(vex);
+  roe[2 * P + o] = T(vey);
+  roe[3 * P + o] = T((pre + e) * t0);
   if (p.roe_reg_ex4) {
     // ex4_sedov_2d/main.f90:426
     t0 = 1. / (rho + 1e-15);
@@ -226,19 +241,20 @@ __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalar
     vey = my * t0;
     pre = g1 * (e - 0.5 * (mx * vex + my * vey));
     roe[4 * P + o] = w;
-    roe[5 * P + o] = vex;
-    roe[6 * P + o] = vey;
-    roe[7 * P + o] = (pre + e) * t0;
+    roe[5 * P + o] = T(vex);
+    roe[6 * P + o] = T(vey);
+    roe[7 * P + o] = T((pre + e) * t0);
   }
 }
 
+template <class T>
 __global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalars* dsc,
-                         double* __restrict__ split) {
+                         T* __restrict__ split) {
   const Geom& g = p.g;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.LI) return;
   const int64_t o = t, P = g.plane;
-  const double am = dsc->alphamax, g1 = p.gamma1;
+  const double g1 = p.gamma1;
   double rho = ld(u + o), mx = ld(u + P + o), e = ld(u + 2 * P + o);
   // fflux (ex2_sedov_1d/main.f90:57-73)
   double vx = 0.;
@@ -247,21 +263,26 @@ __global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalar
   double pres = g1 * (e - 0.5 * rho * (vx * vx));
   double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
   double a[3] = {rho, mx, e};
+  const T am = T(dsc->alphamax);
   for (int c = 0; c < 3; ++c) {
-    double q = f[c] / am;
-    split[c * P + o] = 0.5 * (a[c] + q);
-    split[(3 + c) * P + o] = 0.5 * (a[c] - q);
+    T q = T(f[c]) / am;
+    split[c * P + o] = T(0.5) * (T(a[c]) + q);
+    split[(3 + c) * P + o] = T(0.5) * (T(a[c]) - q);
   }
 }
 
-cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, double* split,
-                        double* roe, cudaStream_t s) {
+cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
+                        void* roe, cudaStream_t s) {
+  const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (p.g.ndim == 1) {
-    k_prep1d<<<(p.g.LI + SWFD_BLOCK - 1) / SWFD_BLOCK, SWFD_BLOCK, 0, s>>>(p, u, dsc, split);
+    const int gb = (p.g.LI + SWFD_BLOCK - 1) / SWFD_BLOCK;
+    if (f32) k_prep1d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split);
+    else k_prep1d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split);
   } else {
     int64_t n = (int64_t)p.g.LI * p.g.LJ;
-    k_prep2d<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc, split,
-                                                                                 roe);
+    const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
+    if (f32) k_prep2d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split, (float*)roe);
+    else k_prep2d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split, (double*)roe);
   }
   return cudaGetLastError();
 }
@@ -271,21 +292,20 @@ cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc,
 // column i).  sp/sn point at stencil cell -2, component 0 of the positive /
 // negative split flux; components are P apart, stencil cells `step` apart.
 // ---------------------------------------------------------------------------
-template <int YDIR>
-__device__ __forceinline__ void interface_flux(const Eigen2D& E, const double* __restrict__ sp,
-                                               const double* __restrict__ sn, int64_t P,
-                                               int64_t step, double weps, double outp[4],
-                                               double outn[4]) {
-  double ur[4], ul[4];
+template <int YDIR, class T>
+__device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __restrict__ sp,
+                                               const T* __restrict__ sn, int64_t P, int64_t step,
+                                               T weps, T outp[4], T outn[4]) {
+  T ur[4], ul[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    double cp[5], cn[5];
+    T cp[5], cn[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const double* a = sp + m * step;
-      const double* b = sn + m * step;
-      double a0 = ld(a), a1 = ld(a + P), a2 = ld(a + 2 * P), a3 = ld(a + 3 * P);
-      double b0 = ld(b), b1 = ld(b + P), b2 = ld(b + 2 * P), b3 = ld(b + 3 * P);
+      const T* a = sp + m * step;
+      const T* b = sn + m * step;
+      T a0 = ldt(a), a1 = ldt(a + P), a2 = ldt(a + 2 * P), a3 = ldt(a + 3 * P);
+      T b0 = ldt(b), b1 = ldt(b + P), b2 = ldt(b + 2 * P), b3 = ldt(b + 3 * P);
       if (k == 0) {
         cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, a0, a1, a2, a3);
         cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, b0, b1, b2, b3);
@@ -317,92 +337,48 @@ __device__ __forceinline__ void interface_flux(const Eigen2D& E, const double* _
   outn[3] = E.e_hm * ul[0] + E.vt * ul[1] + E.qm * ul[2] + E.e_hp * ul[3];
 }
 
-// x pass: interfaces i = 0..nx+1 of rows j = 1..ny (the rows the RHS uses)
-__global__ void __launch_bounds__(128) k_flux_x(Params p, const double* __restrict__ split,
-                                                const double* __restrict__ roe,
-                                                const DevScalars* dsc, double* __restrict__ flux) {
-  const Geom& g = p.g;
-  int li = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx+1
-  int j = blockIdx.y + 1;
-  if (li > g.nx + 1) return;
-  const int i = li;
-  const int64_t P = g.plane, o = g.at(i, j);
-  Eigen2D E;
-  roe_eigen2d(p.gamma1, 0, ld(roe + o), ld(roe + o + 1), ld(roe + P + o), ld(roe + P + o + 1),
-              ld(roe + 2 * P + o), ld(roe + 2 * P + o + 1), ld(roe + 3 * P + o),
-              ld(roe + 3 * P + o + 1), E);
-  double op[4], on[4];
-  interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, p.weno_eps, op, on);
-  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    flux[c * P + o] = p.alpha_premul ? am * op[c] : op[c];
-    flux[(4 + c) * P + o] = p.alpha_premul ? am * on[c] : on[c];
-  }
-}
-
-// y pass: interfaces j = 0..ny+1 of columns i = 1..nx
-__global__ void __launch_bounds__(128) k_flux_y(Params p, const double* __restrict__ split,
-                                                const double* __restrict__ roe,
-                                                const DevScalars* dsc, double* __restrict__ flux) {
-  const Geom& g = p.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  // 1..nx
-  int j = blockIdx.y;                                 // 0..ny+1
-  if (i > g.nx) return;
-  const int64_t P = g.plane, o = g.at(i, j), pit = g.pitch;
-  const double* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
-  Eigen2D E;
-  roe_eigen2d(p.gamma1, 1, ld(r + o), ld(r + o + pit), ld(r + P + o), ld(r + P + o + pit),
-              ld(r + 2 * P + o), ld(r + 2 * P + o + pit), ld(r + 3 * P + o),
-              ld(r + 3 * P + o + pit), E);
-  double op[4], on[4];
-  interface_flux<1>(E, split + 8 * P + o - 2 * pit, split + 12 * P + o - 2 * pit, P, pit,
-                    p.weno_eps, op, on);
-  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    flux[(8 + c) * P + o] = p.alpha_premul ? am * op[c] : op[c];
-    flux[(12 + c) * P + o] = p.alpha_premul ? am * on[c] : on[c];
-  }
-}
-
-// 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157)
-__global__ void k_flux1d(Params p, const double* __restrict__ u, const double* __restrict__ split,
-                         double* __restrict__ flux) {
+// 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157); vxm and hm come
+// from the FP64 state (pressure recovery), the rest is in T
+template <class T>
+__global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
+                         T* __restrict__ flux) {
   const Geom& g = p.g;
   int m = blockIdx.x * blockDim.x + threadIdx.x;  // 0..n+1
   if (m > g.nx + 1) return;
   const int64_t P = g.plane, o = g.at(m, -2);
-  const double g1 = p.gamma1;
+  const double g1d = p.gamma1;
   double u1 = ld(u + o), u2 = ld(u + P + o), u3 = ld(u + 2 * P + o);
-  double vxm = u2 / u1;
-  double hm = (g1 * (u3 - 0.5 * (u2 * u2) / u1) + u3) / u1;
-  double qm = 0.5 * vxm * vxm;
-  double cm = sqrt(g1 * (hm - qm));
-  double t0 = vxm * cm;
-  double r10 = vxm - cm, r12 = vxm + cm, r20 = hm - t0, r22 = hm + t0;
-  double rcm = 1. / cm;
-  double b1 = g1 * rcm * rcm;
-  double b2 = qm * b1;
+  double vxd = u2 / u1;
+  double hmd = (g1d * (u3 - 0.5 * (u2 * u2) / u1) + u3) / u1;
+  const T g1 = T(g1d), vxm = T(vxd), hm = T(hmd);
+  T qm = T(0.5) * vxm * vxm;
+  T cm = sqrt(g1 * (hm - qm));
+  T t0 = vxm * cm;
+  T r10 = vxm - cm, r12 = vxm + cm, r20 = hm - t0, r22 = hm + t0;
+  T rcm = T(1.) / cm;
+  T b1 = g1 * rcm * rcm;
+  T b2 = qm * b1;
   t0 = vxm * rcm;
-  double t1 = b1 * vxm;
-  double t2 = 0.5 * b1;
-  double L[3][3] = {{0.5 * (b2 + t0), -0.5 * (t1 + rcm), t2},
-                    {1. - b2, t1, -b1},
-                    {0.5 * (b2 - t0), -0.5 * (t1 - rcm), t2}};
-  double ur[3], ul[3];
+  T t1 = b1 * vxm;
+  T t2 = T(0.5) * b1;
+  T L[3][3] = {{T(0.5) * (b2 + t0), -T(0.5) * (t1 + rcm), t2},
+               {T(1.) - b2, t1, -b1},
+               {T(0.5) * (b2 - t0), -T(0.5) * (t1 - rcm), t2}};
+  T ur[3], ul[3];
+  const T weps = T(p.weno_eps);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    double cp[5], cn[5];
+    T cp[5], cn[5];
 #pragma unroll
     for (int jj = 0; jj < 5; ++jj) {
       const int64_t s = o + jj - 2;
-      cp[jj] = L[k][0] * ld(split + s) + L[k][1] * ld(split + P + s) + L[k][2] * ld(split + 2 * P + s);
-      cn[jj] = L[k][0] * ld(split + 3 * P + s) + L[k][1] * ld(split + 4 * P + s) +
-               L[k][2] * ld(split + 5 * P + s);
+      cp[jj] = L[k][0] * ldt(split + s) + L[k][1] * ldt(split + P + s) +
+               L[k][2] * ldt(split + 2 * P + s);
+      cn[jj] = L[k][0] * ldt(split + 3 * P + s) + L[k][1] * ldt(split + 4 * P + s) +
+               L[k][2] * ldt(split + 5 * P + s);
     }
-    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], p.weno_eps);
-    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], p.weno_eps);
+    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
+    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
   }
   flux[o] = ur[0] + ur[1] + ur[2];
   flux[P + o] = r10 * ur[0] + vxm * ur[1] + r12 * ur[2];
@@ -415,13 +391,16 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const double* _
 // Both directions in one persistent launch: a grid of exactly the resident
 // blocks, whose warps take chunks of 32 consecutive interfaces (x interfaces
 // of rows 1..ny first, then y interfaces of rows 0..ny+1) from a counter, so
-// the FP64 pipes stay busy to the last chunk instead of idling through the
-// tail of a partial last wave.
+// the pipes stay busy to the last chunk instead of idling through the tail of
+// a partial last wave.
 #define SWFD_FLUX_BLOCK 128
-#define SWFD_FLUX_MINB 3
-__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB)
-    k_flux_xy(Params p, const double* __restrict__ split, const double* __restrict__ roe,
-              const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
+// resident blocks per SM: the FP64 pipe saturates with 3 (168 registers);
+// the FP32 pipe needs more warps in flight
+#define SWFD_FLUX_MINB(T) (sizeof(T) == 8 ? 3 : 4)
+template <class T>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
+    k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
+              const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
   const Geom& g = p.g;
   const int64_t P = g.plane, pit = g.pitch;
   const int lx = g.nx + 2;                       // x interfaces per row (0..nx+1)
@@ -430,23 +409,24 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB)
   const int64_t chunks_x = (nx_int + 31) / 32;
   const int64_t chunks = chunks_x + (ny_int + 31) / 32;
   const int lane = threadIdx.x & 31;
-  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+  const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
+  const T g1 = T(p.gamma1), weps = T(p.weno_eps);
   for (;;) {
     int c = 0;
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
-    double op[4], on[4];
+    T op[4], on[4];
     if (c < chunks_x) {
       int64_t t = (int64_t)c * 32 + lane;
       if (t >= nx_int) continue;
       const int i = (int)(t % lx), j = (int)(t / lx) + 1;
       const int64_t o = g.at(i, j);
-      Eigen2D E;
-      roe_eigen2d(p.gamma1, 0, ld(roe + o), ld(roe + o + 1), ld(roe + P + o), ld(roe + P + o + 1),
-                  ld(roe + 2 * P + o), ld(roe + 2 * P + o + 1), ld(roe + 3 * P + o),
-                  ld(roe + 3 * P + o + 1), E);
-      interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, p.weno_eps, op, on);
+      Eigen2D<T> E;
+      roe_eigen2d<T>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
+                     ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
+                     ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
+      interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, weps, op, on);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         flux[k * P + o] = p.alpha_premul ? am * op[k] : op[k];
@@ -457,13 +437,13 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB)
       if (t >= ny_int) continue;
       const int i = (int)(t % g.nx) + 1, j = (int)(t / g.nx);
       const int64_t o = g.at(i, j);
-      const double* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
-      Eigen2D E;
-      roe_eigen2d(p.gamma1, 1, ld(r + o), ld(r + o + pit), ld(r + P + o), ld(r + P + o + pit),
-                  ld(r + 2 * P + o), ld(r + 2 * P + o + pit), ld(r + 3 * P + o),
-                  ld(r + 3 * P + o + pit), E);
+      const T* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+      Eigen2D<T> E;
+      roe_eigen2d<T>(g1, 1, ldt(r + o), ldt(r + o + pit), ldt(r + P + o), ldt(r + P + o + pit),
+                     ldt(r + 2 * P + o), ldt(r + 2 * P + o + pit), ldt(r + 3 * P + o),
+                     ldt(r + 3 * P + o + pit), E);
       interface_flux<1>(E, split + 8 * P + o - 2 * pit, split + 12 * P + o - 2 * pit, P, pit,
-                        p.weno_eps, op, on);
+                        weps, op, on);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         flux[(8 + k) * P + o] = p.alpha_premul ? am * op[k] : op[k];
@@ -473,29 +453,41 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB)
   }
 }
 
+template <class T>
 static int flux_grid() {
   static int grid = 0;
   if (!grid) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy, SWFD_FLUX_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T>, SWFD_FLUX_BLOCK, 0);
     grid = sms * (per > 0 ? per : 1);
   }
   return grid;
 }
 
-cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
-                        const DevScalars* dsc, double* flux, int* work, cudaStream_t s) {
+cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
+                        const DevScalars* dsc, void* flux, int* work, cudaStream_t s) {
   const Geom& g = p.g;
+  const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (g.ndim == 1) {
     // the 1D eigenvectors come from the state, which the caller passes as roe
-    k_flux1d<<<(g.nx + 2 + 127) / 128, 128, 0, s>>>(p, roe, split, flux);
+    const int gb = (g.nx + 2 + 127) / 128;
+    if (f32)
+      k_flux1d<float><<<gb, 128, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
+    else
+      k_flux1d<double><<<gb, 128, 0, s>>>(p, (const double*)roe, (const double*)split,
+                                           (double*)flux);
     return cudaGetLastError();
   }
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_flux_xy<<<flux_grid(), SWFD_FLUX_BLOCK, 0, s>>>(p, split, roe, dsc, flux, work);
+  if (f32)
+    k_flux_xy<float><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
+        p, (const float*)split, (const float*)roe, dsc, (float*)flux, work);
+  else
+    k_flux_xy<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
+        p, (const double*)split, (const double*)roe, dsc, (double*)flux, work);
   return cudaGetLastError();
 }
 
@@ -505,37 +497,44 @@ cudaError_t launch_flux(const Params& p, const double* split, const double* roe,
 //   stage 1  u = u + dt*RHS                          (main.f90:587)
 //   stage 2  u = 0.75*u0 + 0.25*(u + dt*RHS)         (main.f90:604)
 //   stage 3  u = (u0 + 2*(u + dt*RHS))/3             (main.f90:621)
+// The flux difference is formed in T; the RK combination accumulates into the
+// FP64 state in both precisions.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rhs2d(const Params& p, const double* __restrict__ flux, int c,
-                                        int64_t o, double am) {
+template <class T>
+__device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, int c, int64_t o,
+                                   double amd) {
   const int64_t P = p.g.plane, pit = p.g.pitch;
-  const double* fpf = flux + c * P;
-  const double* fnf = flux + (4 + c) * P;
-  const double* gpf = flux + (8 + c) * P;
-  const double* gnf = flux + (12 + c) * P;
-  double A = (ld(fpf + o) - ld(fnf + o + 1)) - (ld(fpf + o - 1) - ld(fnf + o));
-  double B = (ld(gpf + o) - ld(gnf + o + pit)) - (ld(gpf + o - pit) - ld(gnf + o));
-  if (p.alpha_premul) return -A / p.dx - B / p.dy;  // ex4_sedov_2d/main.f90:644-645
-  return -(am * A) / p.dx - (am * B) / p.dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
+  const T* fpf = flux + c * P;
+  const T* fnf = flux + (4 + c) * P;
+  const T* gpf = flux + (8 + c) * P;
+  const T* gnf = flux + (12 + c) * P;
+  T A = (ldt(fpf + o) - ldt(fnf + o + 1)) - (ldt(fpf + o - 1) - ldt(fnf + o));
+  T B = (ldt(gpf + o) - ldt(gnf + o + pit)) - (ldt(gpf + o - pit) - ldt(gnf + o));
+  const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
+  if (p.alpha_premul) return -A / dx - B / dy;  // ex4_sedov_2d/main.f90:644-645
+  return -(am * A) / dx - (am * B) / dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
 }
 
-__device__ __forceinline__ double rhs1d(const Params& p, const double* __restrict__ flux, int c,
-                                        int64_t o, double am) {
+template <class T>
+__device__ __forceinline__ T rhs1d(const Params& p, const T* __restrict__ flux, int c, int64_t o,
+                                   double amd) {
   // flus(i) = alphamax*(hp_flux(i-1) - hn_flux(i)); RHS = -(flus(i+1)-flus(i))/dx
   const int64_t P = p.g.plane;
-  const double* hp = flux + c * P;
-  const double* hn = flux + (3 + c) * P;
-  double fl_i = am * (ld(hp + o - 1) - ld(hn + o));
-  double fl_ip1 = am * (ld(hp + o) - ld(hn + o + 1));
-  return -(fl_ip1 - fl_i) / p.dx;
+  const T* hp = flux + c * P;
+  const T* hn = flux + (3 + c) * P;
+  const T am = T(amd);
+  T fl_i = am * (ldt(hp + o - 1) - ldt(hn + o));
+  T fl_ip1 = am * (ldt(hp + o) - ldt(hn + o + 1));
+  return -(fl_ip1 - fl_i) / T(p.dx);
 }
 
 __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
 
 // u0 may alias out (stage 3 writes the step-start buffer); each element of
 // u0 is read only by the thread that then writes it.
+template <class T>
 __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
-                     const double* __restrict__ flux, DevScalars* dsc, double* out) {
+                     const T* __restrict__ flux, DevScalars* dsc, double* out) {
   const Geom& g = p.g;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
@@ -548,7 +547,8 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
     double nv[4];
     for (int c = 0; c < g.nc; ++c) {
       double r = 0.0;
-      if (interior) r = (g.ndim == 1) ? rhs1d(p, flux, c, o, am) : rhs2d(p, flux, c, o, am);
+      if (interior)
+        r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am) : rhs2d<T>(p, flux, c, o, am));
       double v = ld(u + c * P + o) + dt * r;
       if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
       else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
@@ -569,16 +569,22 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
 }
 
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
-                      const double* flux, const DevScalars* dsc, double* out, cudaStream_t s) {
+                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
   cudaError_t e = cudaMemsetAsync((void*)&dsc->postag, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_rk<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(
-      p, stage, u, u0, flux, const_cast<DevScalars*>(dsc), out);
+  const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
+  if (p.precision == SWFD_PRECISION_FP32_BULK)
+    k_rk<float><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const float*)flux,
+                                          const_cast<DevScalars*>(dsc), out);
+  else
+    k_rk<double><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const double*)flux,
+                                           const_cast<DevScalars*>(dsc), out);
   return cudaGetLastError();
 }
 
-__global__ void k_rhs(Params p, const double* __restrict__ flux, const DevScalars* dsc,
+template <class T>
+__global__ void k_rhs(Params p, const T* __restrict__ flux, const DevScalars* dsc,
                       double* __restrict__ rhs) {
   const Geom& g = p.g;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,15 +596,20 @@ __global__ void k_rhs(Params p, const double* __restrict__ flux, const DevScalar
   for (int c = 0; c < g.nc; ++c) {
     double r = 0.0;
     if (interior)
-      r = (g.ndim == 1) ? rhs1d(p, flux, c, o, dsc->alphamax) : rhs2d(p, flux, c, o, dsc->alphamax);
+      r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, dsc->alphamax)
+                                 : rhs2d<T>(p, flux, c, o, dsc->alphamax));
     rhs[c * P + o] = r;
   }
 }
 
-cudaError_t launch_rhs(const Params& p, const double* flux, const DevScalars* dsc, double* rhs,
+cudaError_t launch_rhs(const Params& p, const void* flux, const DevScalars* dsc, double* rhs,
                        cudaStream_t s) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
-  k_rhs<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, flux, dsc, rhs);
+  const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
+  if (p.precision == SWFD_PRECISION_FP32_BULK)
+    k_rhs<float><<<gb, SWFD_BLOCK, 0, s>>>(p, (const float*)flux, dsc, rhs);
+  else
+    k_rhs<double><<<gb, SWFD_BLOCK, 0, s>>>(p, (const double*)flux, dsc, rhs);
   return cudaGetLastError();
 }
 
@@ -673,8 +684,8 @@ __global__ void k_weno_batch(const double* __restrict__ st, int64_t n, double ep
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const double* a = st + 5 * k;
-  if (ul) ul[k] = weno_left(a[0], a[1], a[2], a[3], a[4], eps);
-  if (ur) ur[k] = weno_right(a[0], a[1], a[2], a[3], a[4], eps);
+  if (ul) ul[k] = weno_left<double>(a[0], a[1], a[2], a[3], a[4], eps);
+  if (ur) ur[k] = weno_right<double>(a[0], a[1], a[2], a[3], a[4], eps);
 }
 cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
                               cudaStream_t s) {
