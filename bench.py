@@ -328,7 +328,7 @@ def main():
         r64, r32 = s64.state()[3:-3, 3:-3, 0], s32.state()[3:-3, 3:-3, 0]
         fp32 = {"value": cells * 3 * args.steps * world / (ms32 * 1e-3),
                 "ms_per_step": ms32 / args.steps,
-                "speedup_vs_fp64": (ms_fp64 := total_ms) / ms32 if ms32 else None,
+                "speedup_vs_fp64": total_ms / ms32 if ms32 else None,
                 "rel_l1_density_err_vs_fp64": float(np.abs(r32 - r64).sum() / np.abs(r64).sum()),
                 "arithmetic": "FP32 LF splitting, WENO5 fluxes and flux differences; FP64 pressure "
                               "recovery, RK accumulation, positivity, CFL reduction and sweeps"}
