@@ -177,6 +177,46 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
                              int32_t literals, int32_t device, double* uleft,
                              double* uright);
 
+/* ---------------------------------------------------------------------------
+ * Batched engine and serving.  No counterpart in the reference, which runs one
+ * problem per program (the MPI examples spread one grid over 32 ranks).  Many
+ * independent 2D instances stay resident on one GPU and advance together: each
+ * stage is one launch per kernel over all instances and a run is one CUDA
+ * graph.  Instances are admitted and retired between runs (continuous
+ * batching); each keeps its own alpha, dt, time, sweeps and statistics and
+ * stops at its own time_terminal.
+ * ------------------------------------------------------------------------- */
+typedef struct swfd_batch swfd_batch;
+typedef struct swfd_batch_config {
+  int32_t max_slots;     /* instances resident at once */
+  int32_t max_nx, max_ny;/* largest grid a slot accepts */
+  int32_t precision;     /* SWFD_PRECISION_*, one precision for the whole batch */
+  int32_t ubar_mode;     /* SWFD_UBAR_* */
+  int32_t device;
+  int64_t pool_bytes;    /* HBM budget for instance state; 0 = 80% of free memory */
+  int32_t reserved[8];
+} swfd_batch_config;
+
+swfd_status swfd_batch_config_default(swfd_batch_config* cfg);
+swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out);
+swfd_status swfd_batch_destroy(swfd_batch* b);
+/* Admit one instance: initdata of cfg->problem (the batch's precision is
+ * used).  SWFD_ERR_OOM when no slot or not enough of the HBM budget is free. */
+swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t request_id);
+/* Advance every running instance by up to max_steps SSP-RK3 steps; an
+ * instance stops at its own T (DO WHILE time <= T - 1d-10) or on an error. */
+swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out);
+/* Instances that finished since the last poll, with their status. */
+swfd_status swfd_batch_poll(swfd_batch* b, int64_t* ids, int32_t* status, int32_t cap,
+                            int32_t* n_out);
+/* State u(4,-2:nx+3,-2:ny+3) and time of an admitted instance. */
+swfd_status swfd_batch_download(swfd_batch* b, int64_t request_id, double* u, double* time_out);
+swfd_status swfd_batch_stats(swfd_batch* b, int64_t request_id, swfd_sweep_stats* s);
+/* Free the instance's slot and memory. */
+swfd_status swfd_batch_release(swfd_batch* b, int64_t request_id);
+swfd_status swfd_batch_info(swfd_batch* b, int32_t* running, int32_t* free_slots,
+                            int64_t* free_bytes);
+
 /* Instrumentation (no counterpart in the reference, which only prints a
  * wall-clock "CPU Time", ex4_sedov_2d/main.f90:111,118-119). */
 typedef struct swfd_profile {

@@ -86,6 +86,12 @@ class SwfdProfile(C.Structure):
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
 
+class SwfdBatchConfig(C.Structure):
+    _fields_ = [("max_slots", C.c_int32), ("max_nx", C.c_int32), ("max_ny", C.c_int32),
+                ("precision", C.c_int32), ("ubar_mode", C.c_int32), ("device", C.c_int32),
+                ("pool_bytes", C.c_int64), ("reserved", C.c_int32 * 8)]
+
+
 # name -> (restype, argtypes) for every entry point of include/swfd.h
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
@@ -115,6 +121,18 @@ _SIGS = {
     "swfd_reset_profile": (C.c_int32, [_P]),
     "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
     "swfd_flux_divergence_static": (C.c_int32, [C.POINTER(SwfdConfig), _P, _P, _P]),
+    "swfd_batch_config_default": (C.c_int32, [C.POINTER(SwfdBatchConfig)]),
+    "swfd_batch_create": (C.c_int32, [C.POINTER(SwfdBatchConfig), C.POINTER(_P)]),
+    "swfd_batch_destroy": (C.c_int32, [_P]),
+    "swfd_batch_admit": (C.c_int32, [_P, C.POINTER(SwfdConfig), C.c_int64]),
+    "swfd_batch_run": (C.c_int32, [_P, C.c_int64, C.POINTER(C.c_int64)]),
+    "swfd_batch_poll": (C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32,
+                                    C.POINTER(C.c_int32)]),
+    "swfd_batch_download": (C.c_int32, [_P, C.c_int64, _DP, _DP]),
+    "swfd_batch_stats": (C.c_int32, [_P, C.c_int64, C.POINTER(SwfdSweepStats)]),
+    "swfd_batch_release": (C.c_int32, [_P, C.c_int64]),
+    "swfd_batch_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int64)]),
     "swfd_last_error": (C.c_int32, [_P, C.c_char_p, C.c_size_t]),
     "swfd_status_string": (C.c_char_p, [C.c_int32]),
 }

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "swfd_control.h"
+#include "swfd_graph.h"
 #include "swfd_internal.h"
 
 using namespace swfd;
@@ -136,6 +137,70 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   return SWFD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// initial data on the host (same libm as the reference's gfortran runtime)
+// ---------------------------------------------------------------------------
+inline double sqd(double a) { return a * a; }
+
+// exact (ex3_vortex_accuracy_2d/main.f90:699-718)
+void vortex_exact(double g1, double gamma, double x, double y, double t, double* e) {
+  const double pi = 3.14159265358979323846264338327950;
+  double r = sqrt(sqd(x - 5. - t) + sqd(y - 5. - t));
+  double mag = 10.0828;
+  e[0] = pow(1 - g1 * (mag * mag) / 8. / gamma / (pi * pi) * exp(1. - r * r), 1. / g1);
+  e[1] = e[0] * (1. - mag / 2. / pi * exp((1. - r * r) / 2.) * (y - 5.));
+  e[2] = e[0] * (1. + mag / 2. / pi * exp((1. - r * r) / 2.) * (x - 5.));
+  e[3] = pow(e[0], gamma) / g1 + 0.5 * (e[1] * e[1]) / e[0] + 0.5 * (e[2] * e[2]) / e[0];
+}
+
+// Fortran-layout initial state, ghosts included (bc is applied on the device)
+void init_host_state(const Params& p, const swfd_config& cfg, double* u) {
+  const Geom& g = p.g;
+  const int nx = g.nx, ny = g.ny, nc = g.nc, LI = g.LI;
+  auto U = [&](int c, int i, int j) -> double& {
+    return u[(size_t)c + (size_t)nc * ((size_t)(i + 2) + (size_t)LI * (size_t)(j + 2))];
+  };
+  std::fill(u, u + (size_t)g.nc * g.LI * g.LJ, 0.0);
+  switch (p.problem) {
+    case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:405-428
+      for (int i = -2; i <= nx + 3; ++i) {
+        U(0, i, -2) = 1.;
+        U(1, i, -2) = 0.;
+        U(2, i, -2) = cfg.e_background;
+      }
+      U(2, nx / 2 + 1, -2) = cfg.e_blast / p.dx;
+      break;
+    case SWFD_PROBLEM_VORTEX_2D:  // ex3_vortex_accuracy_2d/main.f90:683-694
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          double x = 0. + i * p.dx - p.dx / 2., y = 0. + j * p.dy - p.dy / 2., e[4];
+          vortex_exact(p.gamma1, p.gamma, x, y, 0., e);
+          for (int c = 0; c < 4; ++c) U(c, i, j) = e[c];
+        }
+      break;
+    case SWFD_PROBLEM_SEDOV_2D:  // ex4_sedov_2d/main.f90:1170-1186
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(0, i, j) = 1;
+          U(3, i, j) = cfg.e_background;
+        }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double gx = 0. + p.dx * (i - 0.5), gy = 0. + p.dy * (j - 0.5);
+          if (fabs(gx - 0.0) <= p.dx / 2.0 && fabs(gy - 0.0) <= p.dy / 2.0)
+            U(3, i, j) = cfg.e_blast / (p.dx * p.dy);
+        }
+      break;
+    case SWFD_PROBLEM_JET_2D:  // ex5_mach2000_jet/main.f90:763-765
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          U(0, i, j) = 0.5;
+          U(3, i, j) = 0.4127 / p.gamma1;
+        }
+      break;
+  }
+}
+
 }  // namespace swfd
 
 namespace {
@@ -178,67 +243,9 @@ int64_t host_len(const Params& p) { return (int64_t)p.g.nc * p.g.LI * p.g.LJ; }
 // ---------------------------------------------------------------------------
 // initial data on the host (same libm as the reference's gfortran runtime)
 // ---------------------------------------------------------------------------
-inline double sqd(double a) { return a * a; }
 
-// exact (ex3_vortex_accuracy_2d/main.f90:699-718)
-void vortex_exact(double g1, double gamma, double x, double y, double t, double* e) {
-  const double pi = 3.14159265358979323846264338327950;
-  double r = sqrt(sqd(x - 5. - t) + sqd(y - 5. - t));
-  double mag = 10.0828;
-  e[0] = pow(1 - g1 * (mag * mag) / 8. / gamma / (pi * pi) * exp(1. - r * r), 1. / g1);
-  e[1] = e[0] * (1. - mag / 2. / pi * exp((1. - r * r) / 2.) * (y - 5.));
-  e[2] = e[0] * (1. + mag / 2. / pi * exp((1. - r * r) / 2.) * (x - 5.));
-  e[3] = pow(e[0], gamma) / g1 + 0.5 * (e[1] * e[1]) / e[0] + 0.5 * (e[2] * e[2]) / e[0];
-}
-
-// Fortran-layout initial state, ghosts included (bc is applied on the device)
-void init_host(const swfd_handle* h, double* u) {
-  const Params& p = h->p;
-  const Geom& g = p.g;
-  const int nx = g.nx, ny = g.ny, nc = g.nc, LI = g.LI;
-  auto U = [&](int c, int i, int j) -> double& {
-    return u[(size_t)c + (size_t)nc * ((size_t)(i + 2) + (size_t)LI * (size_t)(j + 2))];
-  };
-  std::fill(u, u + host_len(p), 0.0);
-  switch (p.problem) {
-    case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:405-428
-      for (int i = -2; i <= nx + 3; ++i) {
-        U(0, i, -2) = 1.;
-        U(1, i, -2) = 0.;
-        U(2, i, -2) = h->cfg.e_background;
-      }
-      U(2, nx / 2 + 1, -2) = h->cfg.e_blast / p.dx;
-      break;
-    case SWFD_PROBLEM_VORTEX_2D:  // ex3_vortex_accuracy_2d/main.f90:683-694
-      for (int j = -2; j <= ny + 3; ++j)
-        for (int i = -2; i <= nx + 3; ++i) {
-          double x = 0. + i * p.dx - p.dx / 2., y = 0. + j * p.dy - p.dy / 2., e[4];
-          vortex_exact(p.gamma1, p.gamma, x, y, 0., e);
-          for (int c = 0; c < 4; ++c) U(c, i, j) = e[c];
-        }
-      break;
-    case SWFD_PROBLEM_SEDOV_2D:  // ex4_sedov_2d/main.f90:1170-1186
-      for (int j = -2; j <= ny + 3; ++j)
-        for (int i = -2; i <= nx + 3; ++i) {
-          U(0, i, j) = 1;
-          U(3, i, j) = h->cfg.e_background;
-        }
-      for (int j = 1; j <= ny; ++j)
-        for (int i = 1; i <= nx; ++i) {
-          double gx = 0. + p.dx * (i - 0.5), gy = 0. + p.dy * (j - 0.5);
-          if (fabs(gx - 0.0) <= p.dx / 2.0 && fabs(gy - 0.0) <= p.dy / 2.0)
-            U(3, i, j) = h->cfg.e_blast / (p.dx * p.dy);
-        }
-      break;
-    case SWFD_PROBLEM_JET_2D:  // ex5_mach2000_jet/main.f90:763-765
-      for (int j = -2; j <= ny + 3; ++j)
-        for (int i = -2; i <= nx + 3; ++i) {
-          U(0, i, j) = 0.5;
-          U(3, i, j) = 0.4127 / p.gamma1;
-        }
-      break;
-  }
-}
+// Fortran-layout initial state of the handle's problem
+void init_host(const swfd_handle* h, double* u) { swfd::init_host_state(h->p, h->cfg, u); }
 
 double* cur_state(swfd_handle* h) { return h->st[h->cur]; }
 
@@ -286,71 +293,6 @@ swfd_status ensure_tracks(swfd_handle* h, int64_t extra) {
   h->track_cap = cap;
   return SWFD_OK;
 }
-
-// ---------------------------------------------------------------------------
-// Graph construction.  Work is recorded by stream capture; a conditional node
-// is spliced into the capture (cudaStreamGetCaptureInfo + cudaGraphAddNode +
-// cudaStreamUpdateCaptureDependencies) and its body is captured on the
-// stream of the next nesting depth.  The control kernels of swfd_control.cu
-// set the conditions on the device.
-// ---------------------------------------------------------------------------
-struct Builder {
-  swfd_handle* h;
-  cudaGraph_t root = nullptr;
-  int depth = 0;
-  int* count = nullptr;  // kernels emitted into the current section
-  cudaError_t err = cudaSuccess;
-  bool ok(cudaError_t e) {
-    if (e != cudaSuccess && err == cudaSuccess) err = e;
-    return err == cudaSuccess;
-  }
-  void k(int n) {
-    if (count) *count += n;
-  }
-  template <class F>
-  void cond(cudaStream_t s, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hnd,
-            F body) {
-    if (err != cudaSuccess) return;
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t g = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t nd = 0;
-    if (!ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd))) return;
-    // cudaGraphNodeParams has no default constructor (its union holds
-    // members with constructors): build it in zeroed raw storage
-    alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
-    memset(raw, 0, sizeof(raw));
-    cudaGraphNodeParams* np = reinterpret_cast<cudaGraphNodeParams*>(raw);
-    np->type = cudaGraphNodeTypeConditional;
-    np->conditional.handle = hnd;
-    np->conditional.type = type;
-    np->conditional.size = 1;
-    cudaGraphNode_t node;
-    if (!ok(cudaGraphAddNode(&node, g, deps, nullptr, nd, np))) return;
-    if (!ok(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
-                                                cudaStreamSetCaptureDependencies)))
-      return;
-    cudaGraph_t bg = np->conditional.phGraph_out[0];
-    cudaStream_t sb = h->cap[++depth];
-    if (ok(cudaStreamBeginCaptureToGraph(sb, bg, nullptr, nullptr, 0,
-                                         cudaStreamCaptureModeRelaxed))) {
-      body(sb);
-      cudaGraph_t tmp;
-      ok(cudaStreamEndCapture(sb, &tmp));
-    }
-    --depth;
-  }
-  cudaGraphConditionalHandle handle() {
-    cudaGraphConditionalHandle hnd = 0;
-    ok(cudaGraphConditionalHandleCreate(&hnd, root, 0, 0));
-    return hnd;
-  }
-};
-
-#define B_OK(b, call) \
-  do {                \
-    (b).ok(call);     \
-  } while (0)
 
 // sweep_lim (ex3_vortex_accuracy_2d/main.f90:888-1137; 1D ex2_sedov_1d/main.f90:564-726;
 // ex4 P(u_bar) check :1447-1454 and stop :1747-1752; ex5 `>=` exit :1162)
@@ -471,6 +413,7 @@ swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
   if (*out) return SWFD_OK;
   Builder b;
   b.h = h;
+  b.cap = h->cap;
   cudaStream_t s = h->cap[0];
   CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   cudaStreamCaptureStatus cs;

@@ -81,6 +81,51 @@ struct DevScalars {
   long long steps_limit;  // bound of the current solve launch
   int* tracks;            // sweep_track, neg_track, pos_track: 3 x track_cap
   long long track_cap;
+  // batched engine only
+  int sweeping;           // this instance is inside its sweep q loop
+  int dens_active;        // this instance runs the density sweep of this stage
+  double t_end;           // time_terminal of the instance
+};
+
+// One instance of the batched engine, as the batched kernels see it.
+struct BatchSlot {
+  Params p;
+  double* st[3];          // X (step start / u0), Y, Z
+  void* split;
+  void* roe;
+  void* flux;
+  void* sweep_scratch;
+  DevScalars* dsc;
+  long long ncell;        // LI * LJ
+  long long chunk_begin;  // first flux chunk of this slot in the batch's chunk space
+  long long chunks_x;     // x-direction flux chunks
+  long long chunks;       // all flux chunks
+  int active;             // 1 while the instance is being advanced
+  int use_limiter;
+  int swp_num;
+  int stop_on_fail;       // ex4: a sweep that reaches swp_num stops the instance
+};
+
+// Device scalars of the batch.
+struct BatchCtl {
+  int any_postag;         // some active slot flagged a cell this stage
+  int n_sweeping;         // slots still inside their sweep q loop
+  int flux_work;          // chunk counter of the persistent flux kernel
+  int n_active;           // slots still being advanced
+  long long total_chunks;
+  long long steps;        // steps taken by the current launch
+  long long steps_limit;
+};
+
+// What a batched launch needs (host side).
+struct BatchLaunch {
+  BatchSlot* tab;           // device slot table
+  BatchCtl* ctl;            // device batch scalars
+  const long long* prefix;  // device flux-chunk prefix (n_slots + 1)
+  int n_slots;
+  long long max_cell;       // largest slot (LI*LJ)
+  int fp32;
+  int ubar_tree;
 };
 
 }  // namespace swfd
@@ -127,6 +172,8 @@ namespace swfd {
 swfd_status check_config(const swfd_config& c, std::string& err);
 swfd_status make_params(const swfd_config& c, Params& p, std::string& err);
 void set_last_error(const std::string& m);  // the process-wide message of swfd_last_error
+// initdata of the problem (ghosts included) in the layout u(nc,-2:nx+3,-2:ny+3)
+void init_host_state(const Params& p, const swfd_config& cfg, double* u);
 
 // kernels.cu
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
@@ -148,6 +195,19 @@ cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* ds
 cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
                               cudaStream_t s);
+
+cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
+                               cudaGraphConditionalHandle h_sweep, cudaStream_t s);
+cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s);
+cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
+cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,
+                                  cudaStream_t s);
+
+cudaError_t launch_batch_sweep_head(const BatchLaunch& b, int out, cudaStream_t s);
+cudaError_t launch_batch_sweep_iter(const BatchLaunch& b, int out, cudaGraphConditionalHandle h,
+                                    cudaStream_t s);
+cudaError_t launch_batch_sweep_cond(const BatchLaunch& b, cudaGraphConditionalHandle h,
+                                    cudaStream_t s);
 
 // sweep.cu
 cudaError_t launch_rho_min(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);

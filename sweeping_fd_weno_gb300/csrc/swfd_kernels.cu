@@ -13,10 +13,9 @@ __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
 // order in which the reference applies its loops (the order defines the
 // corner ghosts).
 // ---------------------------------------------------------------------------
-__global__ void k_bc2d(Params p, double* __restrict__ u) {
+__device__ __forceinline__ void bc2d_cell(const Params& p, double* __restrict__ u, int64_t t) {
   const Geom& g = p.g;
   const int nx = g.nx, ny = g.ny;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
   int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
@@ -63,6 +62,10 @@ __global__ void k_bc2d(Params p, double* __restrict__ u) {
   for (int c = 0; c < 4; ++c) u[c * g.plane + o] = (sgn[c] < 0.) ? -v[c] : v[c];
 }
 
+__global__ void k_bc2d(Params p, double* __restrict__ u) {
+  bc2d_cell(p, u, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s) {
   if (p.g.ndim == 1) return cudaSuccess;  // ex2_sedov_1d/main.f90:394-403 is empty
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
@@ -86,9 +89,9 @@ __device__ __forceinline__ double block_max(double v) {
   return v;
 }
 
-__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
+__device__ __forceinline__ double alpha_cell(const Params& p, const double* __restrict__ u,
+                                             int64_t t) {
   const Geom& g = p.g;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   double a = 0.0;
   if (t < ncell) {
@@ -123,14 +126,20 @@ __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc)
     }
     a = fmax(0.0, a);
   }
+  return a;
+}
+
+__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
+  double a = alpha_cell(p, u, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   a = block_max(a);
   if (threadIdx.x == 0) atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
 }
 
-__global__ void k_alpha_final(DevScalars* dsc) {
+__device__ __forceinline__ void alpha_final_body(DevScalars* dsc) {
   dsc->alphamax = __longlong_as_double((long long)dsc->alpha_bits);
   if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
 }
+__global__ void k_alpha_final(DevScalars* dsc) { alpha_final_body(dsc); }
 
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(&dsc->alpha_bits, 0, sizeof(unsigned long long), s);
@@ -146,7 +155,7 @@ cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cuda
 // (ex2_sedov_1d/main.f90:293; ex3_vortex_accuracy_2d/main.f90:572;
 //  ex4_sedov_2d/main.f90:696-700; ex5_mach2000_jet/main.f90:601-605)
 // ---------------------------------------------------------------------------
-__global__ void k_dt(Params p, DevScalars* dsc) {
+__device__ __forceinline__ void dt_body(const Params& p, DevScalars* dsc) {
   const double am = dsc->alphamax;
   double dt;
   if (p.dt_rule == 4) {
@@ -159,6 +168,7 @@ __global__ void k_dt(Params p, DevScalars* dsc) {
   dsc->dt = dt;
   if (!isfinite(dt)) dsc->error |= 2;
 }
+__global__ void k_dt(Params p, DevScalars* dsc) { dt_body(p, dsc); }
 
 cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s) {
   k_dt<<<1, 1, 0, s>>>(p, dsc);
@@ -191,10 +201,10 @@ template <>
 __device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf((float)v)); }
 
 template <class T>
-__global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalars* dsc,
-                         T* __restrict__ split, T* __restrict__ roe) {
+__device__ __forceinline__ void prep2d_cell(const Params& p, const double* __restrict__ u,
+                                            double amd, T* __restrict__ split, T* __restrict__ roe,
+                                            int64_t t) {
   const Geom& g = p.g;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
   int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
@@ -213,7 +223,7 @@ __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalar
   double f1 = rho * (vx * vx) + pres, f3 = (e + pres) * vx;
   double g2 = rho * (vy * vy) + pres, g3 = (e + pres) * vy;
   // fp = 0.5*(u + f/alpha), fn = 0.5*(u - f/alpha); f/alpha shared by both
-  const T am = T(dsc->alphamax), h = T(0.5);
+  const T am = T(amd), h = T(0.5);
   const T tr = T(rho), tmx = T(mx), tmy = T(my), te = T(e);
   T q;
   q = T(mx) / am;  split[0 * P + o] = h * (tr + q);   split[4 * P + o] = h * (tr - q);
@@ -245,6 +255,12 @@ __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalar
     roe[6 * P + o] = T(vey);
     roe[7 * P + o] = T((pre + e) * t0);
   }
+}
+
+template <class T>
+__global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalars* dsc,
+                         T* __restrict__ split, T* __restrict__ roe) {
+  prep2d_cell<T>(p, u, dsc->alphamax, split, roe, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <class T>
@@ -397,29 +413,22 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
 // resident blocks per SM: the FP64 pipe saturates with 3 (168 registers);
 // the FP32 pipe needs more warps in flight
 #define SWFD_FLUX_MINB(T) (sizeof(T) == 8 ? 3 : 4)
+// the 32 interfaces of chunk c (x chunks first, then y chunks)
 template <class T>
-__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
-    k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
-              const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
+__device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict__ split,
+                                           const T* __restrict__ roe, T am, T* __restrict__ flux,
+                                           int64_t c, int64_t chunks_x, int lane) {
   const Geom& g = p.g;
   const int64_t P = g.plane, pit = g.pitch;
-  const int lx = g.nx + 2;                       // x interfaces per row (0..nx+1)
-  const int64_t nx_int = (int64_t)lx * g.ny;     // rows 1..ny
-  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);  // columns 1..nx, rows 0..ny+1
-  const int64_t chunks_x = (nx_int + 31) / 32;
-  const int64_t chunks = chunks_x + (ny_int + 31) / 32;
-  const int lane = threadIdx.x & 31;
-  const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
+  const int lx = g.nx + 2;
+  const int64_t nx_int = (int64_t)lx * g.ny;
+  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);
   const T g1 = T(p.gamma1), weps = T(p.weno_eps);
-  for (;;) {
-    int c = 0;
-    if (lane == 0) c = atomicAdd(work, 1);
-    c = __shfl_sync(0xffffffffu, c, 0);
-    if (c >= chunks) break;
+  {
     T op[4], on[4];
     if (c < chunks_x) {
       int64_t t = (int64_t)c * 32 + lane;
-      if (t >= nx_int) continue;
+      if (t >= nx_int) return;
       const int i = (int)(t % lx), j = (int)(t / lx) + 1;
       const int64_t o = g.at(i, j);
       Eigen2D<T> E;
@@ -434,7 +443,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
       }
     } else {
       int64_t t = (int64_t)(c - chunks_x) * 32 + lane;
-      if (t >= ny_int) continue;
+      if (t >= ny_int) return;
       const int i = (int)(t % g.nx) + 1, j = (int)(t / g.nx);
       const int64_t o = g.at(i, j);
       const T* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
@@ -450,6 +459,27 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
         flux[(12 + k) * P + o] = p.alpha_premul ? am * on[k] : on[k];
       }
     }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
+    k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
+              const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
+  const Geom& g = p.g;
+  const int lx = g.nx + 2;                       // x interfaces per row (0..nx+1)
+  const int64_t nx_int = (int64_t)lx * g.ny;     // rows 1..ny
+  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);  // columns 1..nx, rows 0..ny+1
+  const int64_t chunks_x = (nx_int + 31) / 32;
+  const int64_t chunks = chunks_x + (ny_int + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) break;
+    flux_chunk<T>(p, split, roe, am, flux, c, chunks_x, lane);
   }
 }
 
@@ -533,17 +563,16 @@ __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
 // u0 may alias out (stage 3 writes the step-start buffer); each element of
 // u0 is read only by the thread that then writes it.
 template <class T>
-__global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
-                     const T* __restrict__ flux, DevScalars* dsc, double* out) {
+__device__ __forceinline__ int rk_cell(const Params& p, int stage, const double* __restrict__ u,
+                                       const double* u0, const T* __restrict__ flux, double dt,
+                                       double am, double* out, int64_t t) {
   const Geom& g = p.g;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   int bad = 0;
   if (t < ncell) {
     int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
     const int64_t o = g.at(i, j), P = g.plane;
     bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
-    const double dt = dsc->dt, am = dsc->alphamax;
     double nv[4];
     for (int c = 0; c < g.nc; ++c) {
       double r = 0.0;
@@ -565,6 +594,14 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
       else bad = (nv[0] <= p.eps) || (pe <= p.eps);
     }
   }
+  return bad;
+}
+
+template <class T>
+__global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
+                     const T* __restrict__ flux, DevScalars* dsc, double* out) {
+  int bad = rk_cell<T>(p, stage, u, u0, flux, dsc->dt, dsc->alphamax, out,
+                       (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   if (block_or(bad) && threadIdx.x == 0) atomicOr(&dsc->postag, 1);
 }
 
@@ -692,6 +729,175 @@ cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* u
   if (n <= 0) return cudaSuccess;
   k_weno_batch<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(st, n, eps, ul,
                                                                                   ur);
+  return cudaGetLastError();
+}
+
+}  // namespace swfd
+
+// ===========================================================================
+// Batched stage kernels.  blockIdx.y indexes the slot table (grid.x strides
+// over the slot's cells); slots that are not active are skipped.  The per
+// cell arithmetic is the single-instance code above.
+// ===========================================================================
+namespace swfd {
+
+__global__ void kb_stage_reset(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    ctl->any_postag = 0;
+    ctl->flux_work = 0;
+  }
+  if (s >= n || !tab[s].active) return;
+  tab[s].dsc->alpha_bits = 0;
+  tab[s].dsc->postag = 0;
+}
+
+__global__ void kb_alpha(const BatchSlot* __restrict__ tab, int in) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active) return;
+  double a = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
+       t += (int64_t)gridDim.x * blockDim.x)
+    a = fmax(a, alpha_cell(sl.p, sl.st[in], t));
+  a = block_max(a);
+  if (threadIdx.x == 0)
+    atomicMax(&sl.dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+}
+
+__global__ void kb_alpha_final(const BatchSlot* __restrict__ tab, int n, int stage) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !tab[s].active) return;
+  alpha_final_body(tab[s].dsc);
+  if (stage == 1) dt_body(tab[s].p, tab[s].dsc);
+}
+
+template <class T>
+__global__ void kb_prep(const BatchSlot* __restrict__ tab, int in) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active) return;
+  const double am = sl.dsc->alphamax;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
+       t += (int64_t)gridDim.x * blockDim.x)
+    prep2d_cell<T>(sl.p, sl.st[in], am, (T*)sl.split, (T*)sl.roe, t);
+}
+
+// all slots' interfaces in one persistent launch; chunk c belongs to the slot
+// whose [prefix[s], prefix[s+1]) holds it
+template <class T>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
+    kb_flux(const BatchSlot* __restrict__ tab, const long long* __restrict__ prefix, int n,
+            BatchCtl* ctl) {
+  const int lane = threadIdx.x & 31;
+  const long long total = ctl->total_chunks;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(&ctl->flux_work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= total) break;
+    int lo = 0, hi = n - 1;  // last slot with prefix[s] <= c
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= c) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchSlot& sl = tab[lo];
+    if (!sl.active) continue;
+    const T am = sl.p.alpha_premul ? T(sl.dsc->alphamax) : T(1.0);
+    flux_chunk<T>(sl.p, (const T*)sl.split, (const T*)sl.roe, am, (T*)sl.flux, c - prefix[lo],
+                  sl.chunks_x, lane);
+  }
+}
+
+template <class T>
+__global__ void kb_rk(const BatchSlot* __restrict__ tab, BatchCtl* ctl, int stage, int in,
+                      int out) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active) return;
+  DevScalars* d = sl.dsc;
+  const double dt = d->dt, am = d->alphamax;
+  int bad = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
+       t += (int64_t)gridDim.x * blockDim.x)
+    bad |= rk_cell<T>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux, dt, am, sl.st[out], t);
+  if (block_or(bad) && threadIdx.x == 0) {
+    atomicOr(&d->postag, 1);
+    if (sl.use_limiter == 2) atomicOr(&ctl->any_postag, 1);
+  }
+}
+
+__global__ void kb_bc(const BatchSlot* __restrict__ tab, int out) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active) return;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
+       t += (int64_t)gridDim.x * blockDim.x)
+    bc2d_cell(sl.p, sl.st[out], t);
+}
+
+// time = time + dt; an instance that reaches its T (or hits an error) stops
+__global__ void kb_time_advance(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !tab[s].active) return;
+  DevScalars* d = tab[s].dsc;
+  d->time = d->time + d->dt;
+  d->steps++;
+  if (!(d->time <= d->t_end - 1e-10) || d->error) {
+    tab[s].active = 0;
+    atomicSub(&ctl->n_active, 1);
+  }
+}
+
+__global__ void kb_cond_any_postag(cudaGraphConditionalHandle h, const BatchCtl* ctl) {
+  cudaGraphSetConditional(h, ctl->any_postag ? 1u : 0u);
+}
+
+__global__ void kb_run_cond(cudaGraphConditionalHandle h, BatchCtl* ctl, int advance) {
+  if (advance) ctl->steps++;
+  cudaGraphSetConditional(h, (ctl->n_active > 0 && ctl->steps < ctl->steps_limit) ? 1u : 0u);
+}
+
+static int batch_grid_x(int n_slots, long long max_cell) {
+  long long want = (4096 + n_slots - 1) / n_slots;
+  long long cap = (max_cell + SWFD_BLOCK - 1) / SWFD_BLOCK;
+  long long x = want < 64 ? 64 : want;
+  if (x > cap) x = cap;
+  return (int)(x < 1 ? 1 : x);
+}
+
+cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
+                               cudaGraphConditionalHandle h_sweep, cudaStream_t s) {
+  const int n = b.n_slots;
+  const int gs = (n + 127) / 128;
+  const dim3 grid(batch_grid_x(n, b.max_cell), n);
+  kb_stage_reset<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
+  kb_alpha<<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+  kb_alpha_final<<<gs, 128, 0, s>>>(b.tab, n, stage);
+  if (b.fp32) {
+    kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+    kb_flux<float><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
+    kb_rk<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
+  } else {
+    kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+    kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
+    kb_rk<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
+  }
+  if (h_sweep) kb_cond_any_postag<<<1, 1, 0, s>>>(h_sweep, b.ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s) {
+  const dim3 grid(batch_grid_x(b.n_slots, b.max_cell), b.n_slots);
+  kb_bc<<<grid, SWFD_BLOCK, 0, s>>>(b.tab, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s) {
+  kb_time_advance<<<(b.n_slots + 127) / 128, 128, 0, s>>>(b.tab, b.ctl, b.n_slots);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,
+                                  cudaStream_t s) {
+  kb_run_cond<<<1, 1, 0, s>>>(h, b.ctl, advance);
   return cudaGetLastError();
 }
 

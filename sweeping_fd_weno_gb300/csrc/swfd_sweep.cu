@@ -6,84 +6,13 @@
 // dependency.  Positions map to cells arithmetically (snake orderings I and
 // II of ex3_vortex_accuracy_2d/main.f90:1211-1270, or the index order of the
 // 1D sweep).
-#include "swfd_device.cuh"
+#include "swfd_sweep.cuh"
 
 namespace swfd {
-
-// position -> cell offset; ordering 1 = I (column by column), 2 = II (row by
-// row), 0 = 1D index order over -2..n+3
-__device__ __forceinline__ int64_t pos_cell(const Geom& g, int ordering, int64_t pos) {
-  if (ordering == 0) return pos;  // 1D: position p is cell p-2, offset p
-  int i, j;
-  if (ordering == 1) {
-    j = (int)(pos / g.nx) + 1;
-    int t = (int)(pos % g.nx);
-    i = (j & 1) ? t + 1 : g.nx - t;
-  } else {
-    i = (int)(pos / g.ny) + 1;
-    int t = (int)(pos % g.ny);
-    j = (i & 1) ? t + 1 : g.ny - t;
-  }
-  return g.at(i, j);
-}
-
-__host__ __device__ __forceinline__ int64_t npos(const Geom& g) {
-  return g.ndim == 1 ? (int64_t)g.LI : (int64_t)g.nx * g.ny;
-}
-
-// pressure as the sweep computes it
-// (2D ex3_vortex_accuracy_2d/main.f90:946, 1D ex2_sedov_1d/main.f90:603)
-__device__ __forceinline__ double sweep_pres(const Geom& g, double g1, const double* v) {
-  if (g.ndim == 1) return g1 * (v[2] - 0.5 * (v[1] * v[1]) / v[0]);
-  return g1 * (v[3] - 0.5 * (v[1] * v[1] + v[2] * v[2]) / (v[0]));
-}
-
-// nod_lim (ex3_vortex_accuracy_2d/main.f90:846-884; 1D ex2_sedov_1d/main.f90:517-560)
-__device__ void nod_lim(const Geom& g, double g1, double eps, const double* v1, const double* v2,
-                        const double* vb, double* out, long long& npos_, long long& nneg) {
-  double t;
-  if (g.ndim == 1) {
-    double p1 = g1 * (v1[2] - 0.5 * (v1[1] * v1[1] / v1[0]));
-    double p2 = g1 * (v2[2] - 0.5 * (v2[1] * v2[1] / v2[0]));
-    if (p2 > eps) {
-      t = (p1 - eps) / (p1 - p2);
-      ++npos_;
-    } else {
-      double pb = g1 * (vb[2] - 0.5 * (vb[1] * vb[1] / vb[0]));
-      double t_1 = (p1 - eps) / (p1 - pb);
-      double d12 = sqrt(dsq(v2[2] - v1[2]) + dsq(v2[1] - v1[1]) + dsq(v2[0] - v1[0]));
-      double d1b = sqrt(dsq(vb[2] - v1[2]) + dsq(vb[1] - v1[1]) + dsq(vb[0] - v1[0]));
-      t = fmin(t_1 * d1b / d12, 0.25);
-      ++nneg;
-    }
-  } else {
-    double p1 = g1 * (v1[3] - 0.5 * (v1[1] * v1[1] + v1[2] * v1[2]) / v1[0]);
-    double p2 = g1 * (v2[3] - 0.5 * (v2[1] * v2[1] + v2[2] * v2[2]) / v2[0]);
-    if (p2 > eps) {
-      t = (p1 - eps) / (p1 - p2);
-      ++npos_;
-    } else {
-      double pb = g1 * (vb[3] - 0.5 * (vb[1] * vb[1] + vb[2] * vb[2]) / vb[0]);
-      double t_1 = (p1 - eps) / (p1 - pb);
-      double d12 = sqrt(dsq(v2[3] - v1[3]) + dsq(v2[2] - v1[2]) + dsq(v2[1] - v1[1]) +
-                        dsq(v2[0] - v1[0]));
-      double d1b = sqrt(dsq(vb[3] - v1[3]) + dsq(vb[2] - v1[2]) + dsq(vb[1] - v1[1]) +
-                        dsq(vb[0] - v1[0]));
-      t = fmin(t_1 * d1b / d12, 0.25);
-      ++nneg;
-    }
-  }
-  for (int c = 0; c < g.nc; ++c) out[c] = (1 - t) * v1[c] + t * v2[c];
-}
 
 // ---------------------------------------------------------------------------
 // rho_min over the sweep domain (2D interior), ex3_vortex_accuracy_2d/main.f90:1148-1153
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long order_key(double v) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-
 __global__ void k_rho_min(Params p, const double* __restrict__ u, DevScalars* dsc) {
   const Geom& g = p.g;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -283,95 +212,6 @@ cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc,
 // MERGE chains run to their end with writes), write (TERM roots in parallel).
 // ===========================================================================
 
-struct SweepScratch {
-  uint32_t* bits;    // W = ceil((N-1)/32) words
-  int* F;            // flagged positions, sorted
-  int* dry_end;      // end position of the dry run
-  uint8_t* dry_merge;  // 1: the dry run reached F[k+1]
-  uint8_t* root;     // 1: F[k] starts a true TERM chain
-  int* counters;     // [0] m, [1] has_merge
-};
-
-// kind 0: pressure pass (nodal adjustment); kind 1: density pass
-template <int KIND>
-struct Chain {
-  double s[4];
-  __device__ __forceinline__ void load(const Params& p, const double* u, int64_t c) {
-    if (KIND == 1) s[0] = u[c];
-    else
-      for (int k = 0; k < p.g.nc; ++k) s[k] = u[k * p.g.plane + c];
-  }
-  __device__ __forceinline__ void store(const Params& p, double* u, int64_t c) const {
-    if (KIND == 1) u[c] = s[0];
-    else
-      for (int k = 0; k < p.g.nc; ++k) u[k * p.g.plane + c] = s[k];
-  }
-  __device__ __forceinline__ bool bad(const Params& p) const {
-    if (KIND == 1) return s[0] < (p.g.ndim == 1 ? 1e-13 : 1e-12);
-    double pr = sweep_pres(p.g, p.gamma1, s);
-    return pr <= p.eps || s[0] <= p.eps;
-  }
-  // one step: this (cell q) acts on nx (cell q+1); afterwards this holds the
-  // final value of cell q and nx the modified value of cell q+1
-  __device__ __forceinline__ void step(const Params& p, Chain& nx, const double* ub,
-                                       long long& npos_, long long& nneg) {
-    if (KIND == 1) {
-      const double delta = p.g.ndim == 1 ? 1e-13 : 1e-12;
-      nx.s[0] = nx.s[0] + 1.0 * (s[0] - delta);
-      s[0] = delta;
-    } else {
-      double vit[4];
-      nod_lim(p.g, p.gamma1, p.eps, s, nx.s, ub, vit, npos_, nneg);
-      for (int c = 0; c < p.g.nc; ++c) {
-        double d = s[c] - vit[c];
-        s[c] = vit[c];
-        nx.s[c] = nx.s[c] + 1.0 * (d);
-      }
-    }
-  }
-};
-
-__device__ __forceinline__ int64_t walk_cell(const Geom& g, int ordering, int forward, int64_t N,
-                                              int64_t q) {
-  return pos_cell(g, ordering, forward ? q : N - 1 - q);
-}
-
-// Run the chain that starts at q0 (bad on arrival).  stop >= 0 bounds the run:
-// reaching position `stop` returns with *merged = 1.  Returns the last
-// position the chain modified.
-template <int KIND, bool WRITE>
-__device__ int64_t run_chain(const Params& p, double* u, int ordering, int forward, int64_t N,
-                             int64_t q0, int64_t stop, const double* ub, int* merged,
-                             long long& npos_, long long& nneg) {
-  const Geom& g = p.g;
-  Chain<KIND> cur, nxt;
-  int64_t cq = walk_cell(g, ordering, forward, N, q0);
-  cur.load(p, u, cq);
-  int64_t q = q0;
-  *merged = 0;
-  for (;;) {
-    if (q >= N - 1) {  // the last position takes no step
-      if (WRITE) cur.store(p, u, cq);
-      return q;
-    }
-    int64_t cn = walk_cell(g, ordering, forward, N, q + 1);
-    nxt.load(p, u, cn);
-    cur.step(p, nxt, ub, npos_, nneg);
-    if (WRITE) cur.store(p, u, cq);
-    ++q;
-    cq = cn;
-    cur = nxt;
-    if (stop >= 0 && q == stop) {
-      *merged = 1;
-      return q;
-    }
-    if (!cur.bad(p)) {
-      if (WRITE) cur.store(p, u, cq);
-      return q;
-    }
-  }
-}
-
 template <int KIND>
 __global__ void k_flag_bits(Params p, const double* __restrict__ u, int ordering, int forward,
                             SweepScratch sc, const DevScalars* dsc) {
@@ -507,30 +347,7 @@ __global__ void k_chain_write(Params p, double* u, int ordering, int forward, Sw
   }
 }
 
-size_t sweep_scratch_bytes(const Params& p) {
-  const int64_t N = npos(p.g);
-  const int64_t W = (N + 31) / 32 + 1;
-  return W * 4 + N * 4 * 2 + N * 2 + 64 + 256;
-}
-
-static SweepScratch carve(void* base, const Params& p) {
-  const int64_t N = npos(p.g);
-  const int64_t W = (N + 31) / 32 + 1;
-  char* c = (char*)base;
-  SweepScratch s;
-  s.counters = (int*)c;
-  c += 64;
-  s.bits = (uint32_t*)c;
-  c += W * 4;
-  s.F = (int*)c;
-  c += N * 4;
-  s.dry_end = (int*)c;
-  c += N * 4;
-  s.dry_merge = (uint8_t*)c;
-  c += N;
-  s.root = (uint8_t*)c;
-  return s;
-}
+size_t sweep_scratch_bytes(const Params& p) { return sweep_scratch_bytes_impl(p); }
 
 template <int KIND>
 static cudaError_t pass_parallel(const Params& p, double* u, int ordering, int forward,
@@ -558,6 +375,394 @@ cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, 
   cudaError_t e = pass_parallel<1>(p, u, 1, 1, scratch, nullptr, s, nlaunch);
   if (e != cudaSuccess) return e;
   return pass_parallel<1>(p, u, 1, 0, scratch, nullptr, s, nlaunch);
+}
+
+}  // namespace swfd
+
+// ===========================================================================
+// Batched sweep kernels: blockIdx.y indexes the slot table; a slot takes part
+// while its `sweeping` flag (pressure passes) or `dens_active` flag (density
+// passes) is set.  Each slot's passes are exactly the single-instance ones,
+// on its stage output buffer st[out].
+// ===========================================================================
+namespace swfd {
+
+__device__ __forceinline__ bool slot_in(const BatchSlot& sl, int kind) {
+  if (!sl.active) return false;
+  return kind == 1 ? sl.dsc->dens_active != 0 : sl.dsc->sweeping != 0;
+}
+
+// per slot: does this stage sweep?  (use_limiter == 2 and postag)
+__global__ void kb_sweep_start(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) ctl->n_sweeping = 0;
+  if (s >= n || !tab[s].active) return;
+  DevScalars* d = tab[s].dsc;
+  d->sweeping = (tab[s].use_limiter == 2 && d->postag) ? 1 : 0;
+  d->dens_active = 0;
+  d->rho_min_key = ~0ull;
+}
+
+// rho_min over the interior (ex3_vortex_accuracy_2d/main.f90:1148-1153)
+__global__ void kb_rho_min(const BatchSlot* __restrict__ tab, int out) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, 0)) return;
+  const Geom& g = sl.p.g;
+  const double* u = sl.st[out];
+  const int64_t n = (int64_t)g.nx * g.ny;
+  double v = 1e20;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    v = fmin(u[g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1)], v);
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) atomicMin(&sl.dsc->rho_min_key, order_key(v));
+}
+
+__device__ __forceinline__ double decode_key_b(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+// IF rho_min < 1d-12 (:1156); den_count (:1187)
+__global__ void kb_density_decide(const BatchSlot* __restrict__ tab, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !slot_in(tab[s], 0)) return;
+  DevScalars* d = tab[s].dsc;
+  d->dens_active = decode_key_b(d->rho_min_key) < 1e-12 ? 1 : 0;
+  if (d->dens_active) d->den_count++;
+}
+
+// ordering: 1 (density, ordering I) or -1 (pressure, the slot's dsc->ordering)
+template <int KIND>
+__global__ void kb_flag(const BatchSlot* __restrict__ tab, int out, int ordering, int forward) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, KIND)) return;
+  const Params& p = sl.p;
+  const Geom& g = p.g;
+  const int ord = ordering >= 0 ? ordering : sl.dsc->ordering;
+  const double* u = sl.st[out];
+  SweepScratch sc = carve(sl.sweep_scratch, p);
+  const int64_t N = npos(g);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;  // a multiple of 32
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < N - 1; base += stride) {
+    int64_t q = base + threadIdx.x;
+    bool b = false;
+    if (q < N - 1) {
+      Chain<KIND> c;
+      c.load(p, u, walk_cell(g, ord, forward, N, q));
+      b = c.bad(p);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, b);
+    if ((threadIdx.x & 31) == 0 && q < N - 1) sc.bits[q >> 5] = m;
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(1024) kb_compact(const BatchSlot* __restrict__ tab) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, KIND)) return;
+  __shared__ int part[1024];
+  SweepScratch sc = carve(sl.sweep_scratch, sl.p);
+  const int64_t N = npos(sl.p.g);
+  const int64_t W = (N - 1 + 31) / 32;
+  const int T = blockDim.x, t = threadIdx.x;
+  const int64_t chunk = (W + T - 1) / T;
+  const int64_t w0 = t * chunk, w1 = min(W, w0 + chunk);
+  int cnt = 0;
+  for (int64_t w = w0; w < w1; ++w) cnt += __popc(sc.bits[w]);
+  part[t] = cnt;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {
+    int v = (t >= off) ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int pos = part[t] - cnt;
+  for (int64_t w = w0; w < w1; ++w) {
+    uint32_t b = sc.bits[w];
+    while (b) {
+      int i = __ffs(b) - 1;
+      b &= b - 1;
+      sc.F[pos++] = (int)(w * 32 + i);
+    }
+  }
+  if (t == T - 1) {
+    sc.counters[0] = part[T - 1];
+    sc.counters[1] = 0;
+  }
+}
+
+template <int KIND>
+__global__ void kb_dry(const BatchSlot* __restrict__ tab, int out, int ordering, int forward) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, KIND)) return;
+  const Params& p = sl.p;
+  const int ord = ordering >= 0 ? ordering : sl.dsc->ordering;
+  double* u = sl.st[out];
+  SweepScratch sc = carve(sl.sweep_scratch, p);
+  const int64_t N = npos(p.g);
+  const int m = sc.counters[0];
+  double ub[4] = {0, 0, 0, 0};
+  if (KIND == 0)
+    for (int c = 0; c < 4; ++c) ub[c] = sl.dsc->ubar[c];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    long long a = 0, b = 0;
+    int merged = 0;
+    int64_t stop = (k + 1 < m) ? sc.F[k + 1] : -1;
+    int64_t e = run_chain<KIND, false>(p, u, ord, forward, N, sc.F[k], stop, ub, &merged, a, b);
+    sc.dry_end[k] = (int)e;
+    sc.dry_merge[k] = (uint8_t)merged;
+    sc.root[k] = 0;
+    if (merged) atomicOr(&sc.counters[1], 1);
+  }
+}
+
+template <int KIND>
+__global__ void kb_walk(const BatchSlot* __restrict__ tab, int out, int ordering, int forward) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, KIND)) return;
+  const Params& p = sl.p;
+  SweepScratch sc = carve(sl.sweep_scratch, p);
+  if (sc.counters[1] == 0) return;
+  const int ord = ordering >= 0 ? ordering : sl.dsc->ordering;
+  double* u = sl.st[out];
+  const int64_t N = npos(p.g);
+  const int m = sc.counters[0];
+  const int lane = threadIdx.x;
+  double ub[4] = {0, 0, 0, 0};
+  if (KIND == 0)
+    for (int c = 0; c < 4; ++c) ub[c] = sl.dsc->ubar[c];
+  long long npos_ = 0, nneg = 0;
+  int64_t covered = -1;
+  int base = 0;
+  while (base < m) {
+    int k = base + lane;
+    bool valid = k < m;
+    int64_t f = valid ? sc.F[k] : INT64_MAX;
+    bool mg = valid && sc.dry_merge[k];
+    bool live = valid && f > covered;
+    unsigned mm = __ballot_sync(0xffffffffu, live && mg);
+    int first = mm ? __ffs(mm) - 1 : 32;
+    if (live && !mg && lane < first) sc.root[k] = 1;
+    if (first == 32) {
+      base += 32;
+      continue;
+    }
+    int64_t e = 0;
+    if (lane == first) {
+      int merged;
+      e = run_chain<KIND, true>(p, u, ord, forward, N, f, -1, ub, &merged, npos_, nneg);
+    }
+    covered = __shfl_sync(0xffffffffu, e, first);
+    base += first + 1;
+  }
+  if (KIND == 0 && (npos_ | nneg)) {
+    atomicAdd((unsigned long long*)&sl.dsc->t_pos, (unsigned long long)npos_);
+    atomicAdd((unsigned long long*)&sl.dsc->t_neg, (unsigned long long)nneg);
+  }
+}
+
+template <int KIND>
+__global__ void kb_write(const BatchSlot* __restrict__ tab, int out, int ordering, int forward) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, KIND)) return;
+  const Params& p = sl.p;
+  const int ord = ordering >= 0 ? ordering : sl.dsc->ordering;
+  double* u = sl.st[out];
+  SweepScratch sc = carve(sl.sweep_scratch, p);
+  const int64_t N = npos(p.g);
+  const int m = sc.counters[0];
+  const bool all_roots = sc.counters[1] == 0;
+  double ub[4] = {0, 0, 0, 0};
+  if (KIND == 0)
+    for (int c = 0; c < 4; ++c) ub[c] = sl.dsc->ubar[c];
+  long long npos_ = 0, nneg = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    if (!(all_roots || sc.root[k])) continue;
+    int merged;
+    run_chain<KIND, true>(p, u, ord, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg);
+  }
+  if (KIND == 0 && (npos_ | nneg)) {
+    atomicAdd((unsigned long long*)&sl.dsc->t_pos, (unsigned long long)npos_);
+    atomicAdd((unsigned long long*)&sl.dsc->t_neg, (unsigned long long)nneg);
+  }
+}
+
+// u_bar: the reference's sequential sums (one thread per component), or a
+// deterministic block tree sum (ubar_tree)
+__global__ void kb_ubar(const BatchSlot* __restrict__ tab, int out, int tree) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, 0)) return;
+  const Geom& g = sl.p.g;
+  const double* u = sl.st[out];
+  const double w = 1. / ((double)g.nx * (double)g.ny);
+  if (!tree) {
+    const int c = threadIdx.x;
+    if (c >= g.nc) return;
+    const double* pl = u + c * g.plane;
+    double s = 0.0;
+    for (int j = 1; j <= g.ny; ++j) {
+      const double* row = pl + g.at(0, j);
+      for (int i = 1; i <= g.nx; ++i) s = s + w * row[i];
+    }
+    sl.dsc->ubar[c] = s;
+    return;
+  }
+  __shared__ double red[4][256];
+  double acc[4] = {0, 0, 0, 0};
+  const int64_t n = (int64_t)g.nx * g.ny;
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
+    const int64_t o = g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1);
+    for (int c = 0; c < 4; ++c) acc[c] = acc[c] + w * u[c * g.plane + o];
+  }
+  for (int c = 0; c < 4; ++c) red[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 4; ++c) sl.dsc->ubar[c] = red[c][0];
+}
+
+// sweep_lim set-up (:928-930; ex4's P(u_bar) stop :1447-1454)
+__global__ void kb_sweep_begin(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !slot_in(tab[s], 0)) return;
+  DevScalars* d = tab[s].dsc;
+  const Params& p = tab[s].p;
+  if (p.problem == SWFD_PROBLEM_SEDOV_2D) {
+    const double* ub = d->ubar;
+    if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.) {
+      d->error |= ERR_BIT_PUBAR;
+      d->sweeping = 0;
+      return;
+    }
+  }
+  long long k = d->sweep_count++;
+  if (k < d->track_cap) {
+    d->tracks[k] = 0;
+    d->tracks[d->track_cap + k] = 0;
+    d->tracks[2 * d->track_cap + k] = 0;
+  }
+  d->t_pos = 0;
+  d->t_neg = 0;
+  d->q = 0;
+  atomicAdd(&ctl->n_sweeping, 1);
+}
+
+__global__ void kb_q_begin(const BatchSlot* __restrict__ tab, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !slot_in(tab[s], 0)) return;
+  DevScalars* d = tab[s].dsc;
+  int q = ++d->q;
+  d->ordering = (q & 1) ? 1 : 2;
+  d->bad_count = 0;
+}
+
+// exit test cells (:1106-1119; `>=` in ex5)
+__global__ void kb_exit_count(const BatchSlot* __restrict__ tab, int out) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!slot_in(sl, 0)) return;
+  const Params& p = sl.p;
+  const Geom& g = p.g;
+  const double* u = sl.st[out];
+  const int64_t n = (int64_t)g.nx * g.ny;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t = base + threadIdx.x;
+    int bad = 0;
+    if (t < n) {
+      const int64_t o = g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1);
+      double v[4];
+      for (int c = 0; c < 4; ++c) v[c] = u[c * g.plane + o];
+      double pr = sweep_pres(g, p.gamma1, v);
+      if (p.exit_ge) bad = (pr < p.eps) || (v[0] < p.eps);
+      else bad = (pr <= p.eps) || (v[0] <= p.eps);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(&sl.dsc->bad_count, __popc(m));
+  }
+}
+
+// end of iteration q: pre_count, exit test, tracks (:1116-1129)
+__global__ void kb_q_end(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !slot_in(tab[s], 0)) return;
+  DevScalars* d = tab[s].dsc;
+  d->pre_count++;
+  bool stop = false;
+  if (d->bad_count == 0) {
+    long long k = d->sweep_count - 1;
+    if (k >= 0 && k < d->track_cap) {
+      d->tracks[k] = d->q;
+      d->tracks[d->track_cap + k] = (int)d->t_neg;
+      d->tracks[2 * d->track_cap + k] = (int)d->t_pos;
+    }
+    stop = true;
+  } else if (d->q >= tab[s].swp_num) {
+    d->fail_count++;
+    if (tab[s].stop_on_fail) d->error |= ERR_BIT_NOCONV;
+    stop = true;
+  }
+  if (stop) {
+    d->sweeping = 0;
+    atomicSub(&ctl->n_sweeping, 1);
+  }
+}
+
+__global__ void kb_q_cond(cudaGraphConditionalHandle h, const BatchCtl* ctl) {
+  cudaGraphSetConditional(h, ctl->n_sweeping > 0 ? 1u : 0u);
+}
+
+static int bgx(const BatchLaunch& b) {
+  long long want = (4096 + b.n_slots - 1) / b.n_slots;
+  long long cap = (b.max_cell + 255) / 256;
+  long long x = want < 64 ? 64 : want;
+  if (x > cap) x = cap;
+  return (int)(x < 1 ? 1 : x);
+}
+
+template <int KIND>
+static void batch_pass(const BatchLaunch& b, int out, int ordering, int forward, cudaStream_t s) {
+  const int n = b.n_slots;
+  kb_flag<KIND><<<dim3(bgx(b), n), 256, 0, s>>>(b.tab, out, ordering, forward);
+  kb_compact<KIND><<<dim3(1, n), 1024, 0, s>>>(b.tab);
+  kb_dry<KIND><<<dim3(4, n), 128, 0, s>>>(b.tab, out, ordering, forward);
+  kb_walk<KIND><<<dim3(1, n), 32, 0, s>>>(b.tab, out, ordering, forward);
+  kb_write<KIND><<<dim3(4, n), 128, 0, s>>>(b.tab, out, ordering, forward);
+}
+
+cudaError_t launch_batch_sweep_head(const BatchLaunch& b, int out, cudaStream_t s) {
+  const int n = b.n_slots, gs = (n + 127) / 128;
+  kb_sweep_start<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
+  kb_rho_min<<<dim3(bgx(b), n), 256, 0, s>>>(b.tab, out);
+  kb_density_decide<<<gs, 128, 0, s>>>(b.tab, n);
+  batch_pass<1>(b, out, 1, 1, s);
+  batch_pass<1>(b, out, 1, 0, s);
+  kb_ubar<<<dim3(1, n), b.ubar_tree ? 256 : 32, 0, s>>>(b.tab, out, b.ubar_tree);
+  kb_sweep_begin<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sweep_iter(const BatchLaunch& b, int out, cudaGraphConditionalHandle h,
+                                    cudaStream_t s) {
+  const int n = b.n_slots, gs = (n + 127) / 128;
+  kb_q_begin<<<gs, 128, 0, s>>>(b.tab, n);
+  batch_pass<0>(b, out, -1, 1, s);
+  batch_pass<0>(b, out, -1, 0, s);
+  kb_exit_count<<<dim3(bgx(b), n), 256, 0, s>>>(b.tab, out);
+  kb_q_end<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
+  kb_q_cond<<<1, 1, 0, s>>>(h, b.ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sweep_cond(const BatchLaunch& b, cudaGraphConditionalHandle h,
+                                    cudaStream_t s) {
+  kb_q_cond<<<1, 1, 0, s>>>(h, b.ctl);
+  return cudaGetLastError();
 }
 
 }  // namespace swfd
