@@ -103,7 +103,7 @@ def test_admission_respects_the_hbm_budget(swfd):
     with Batch(max_slots=8, max_nx=256, max_ny=256, precision=abi.PRECISION_FP32_BULK,
                pool_bytes=60 << 20) as b:
         big = dict(problem=abi.SEDOV_2D, nx=256, ny=256)
-        assert b.admit(cfg_of(big), 1)       # ~40 MB
-        assert not b.admit(cfg_of(big), 2)   # over the 60 MB budget: waits
+        assert b.admit(cfg_of(big), 1)       # ~20 MB of state and FP32 planes
+        assert not b.admit(cfg_of(big), 2)   # over the 30 MB budget: waits
         b.release(1)
         assert b.admit(cfg_of(big), 2)
