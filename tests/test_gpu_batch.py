@@ -101,7 +101,7 @@ def test_instances_stop_at_their_own_time_and_are_polled(swfd):
 
 def test_admission_respects_the_hbm_budget(swfd):
     with Batch(max_slots=8, max_nx=256, max_ny=256, precision=abi.PRECISION_FP32_BULK,
-               pool_bytes=60 << 20) as b:
+               pool_bytes=30 << 20) as b:
         big = dict(problem=abi.SEDOV_2D, nx=256, ny=256)
         assert b.admit(cfg_of(big), 1)       # ~20 MB of state and FP32 planes
         assert not b.admit(cfg_of(big), 2)   # over the 30 MB budget: waits
