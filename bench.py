@@ -132,6 +132,181 @@ def cpu_baseline(nx: int, budget_s: float = 10.0) -> dict:
                                    f"(the reference's -fdefault-real-8 build), {qel:.1f} s"}
 
 
+# --- batched point-energy instances and the serving stream -------------------
+
+BATCH_SEED = 20261203
+SERVE_SEED = 20261204
+
+
+def point_energy_sizes(n_inst: int, seed: int = BATCH_SEED):
+    """Side lengths of the batched point-energy instances: uniform on 128..640."""
+    import numpy as np
+    return [int(n) for n in np.random.default_rng(seed).integers(128, 641, size=n_inst)]
+
+
+def _oracle_steps(args):
+    """One CPU oracle instance (a worker of the host-core baseline)."""
+    n, steps = args
+    import oracle
+    from sweeping_fd_weno_gb300 import abi, problems
+    o = oracle.Oracle(problems.make_config(abi.SEDOV_2D, nx=n, ny=n))
+    o.init_problem()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step()
+    return n * n * 3 * steps, time.perf_counter() - t0
+
+
+def cpu_batched_baseline(sizes, steps: int = 1) -> dict:
+    """The CPU oracle, one instance per host core, on the first instances of
+    the batched workload (a process pool started with spawn)."""
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    sample = sizes[:cores]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        out = pool.map(_oracle_steps, [(n, steps) for n in sample])
+    wall = time.perf_counter() - t0
+    upd = sum(u for u, _ in out)
+    busy = max(t for _, t in out)
+    return {"value": upd / busy, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(sample)} of the point-energy instances ({min(sample)}^2..."
+                      f"{max(sample)}^2), {steps} SSP-RK3 step(s) each, one instance per core, "
+                      f"FP64 double literals; value = updates / slowest instance's time "
+                      f"({busy:.1f} s; pool wall {wall:.1f} s)"}
+
+
+def bench_batched(args, local, flush):
+    """256 point-energy instances (seeded sizes 128^2..640^2 on [0,1.3]^2) in the
+    batched engine with the FP32-bulk precision, against the plain FP64 path one
+    instance at a time on a seeded sample of the same instances."""
+    import numpy as np
+    import torch
+    from sweeping_fd_weno_gb300 import Batch, Solver, abi, problems
+    sizes = point_energy_sizes(args.batch_instances)
+    dev = torch.device("cuda", local)
+    cfg_of = lambda n, **kw: problems.make_config(abi.SEDOV_2D, nx=n, ny=n, device=local, **kw)
+    b = Batch(max_slots=len(sizes), max_nx=640, max_ny=640,
+              precision=abi.PRECISION_FP32_BULK, ubar_mode=abi.UBAR_TREE, device=local)
+    t_adm = time.perf_counter()
+    for k, n in enumerate(sizes):
+        if not b.admit(cfg_of(n), k):
+            raise RuntimeError(f"instance {k} ({n}^2) not admitted")
+    t_adm = time.perf_counter() - t_adm
+    ext = torch.cuda.ExternalStream(b.stream_ptr(), device=dev)
+    b.run(args.warmup)
+    before = [b.progress(k)[1] for k in range(len(sizes))]
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    b.run(args.batch_steps)
+    e1.record(ext)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    done = [b.progress(k)[1] - before[k] for k in range(len(sizes))]
+    upd = sum(n * n * 3 * d for n, d in zip(sizes, done))
+    value = upd / (ms * 1e-3)
+    # accuracy: the smallest instances against the FP64 path after the same steps
+    check = sorted(range(len(sizes)), key=lambda k: sizes[k])[:3]
+    errs = []
+    for k in check:
+        u32, _ = b.download(k)
+        s = Solver(cfg_of(sizes[k]))
+        s.init_problem()
+        for _ in range(args.warmup + args.batch_steps):
+            s.step()
+        u64 = s.state()
+        s.close()
+        r32, r64 = u32[3:-3, 3:-3, 0], u64[3:-3, 3:-3, 0]
+        errs.append(float(np.abs(r32 - r64).sum() / np.abs(r64).sum()))
+    b.close()
+    # the plain FP64 path (and the FP32 path unbatched), one instance at a time
+    rng = np.random.default_rng(BATCH_SEED + 1)
+    sample = [sizes[k] for k in rng.choice(len(sizes), size=args.plain_sample, replace=False)]
+    plain = {}
+    for name, prec in (("fp64", abi.PRECISION_FP64), ("fp32_bulk_single", abi.PRECISION_FP32_BULK)):
+        tot_ms, tot_upd = 0.0, 0
+        for n in sample:
+            s = Solver(cfg_of(n, precision=prec))
+            s.init_problem()
+            se = torch.cuda.ExternalStream(s.stream_ptr(), device=dev)
+            for _ in range(args.warmup):   # the same steps as the batch's timed ones
+                s.step()
+            torch.cuda.synchronize()
+            for _ in range(args.plain_steps):
+                with torch.cuda.stream(se):
+                    flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True)
+                    z = torch.cuda.Event(enable_timing=True)
+                    a.record(se)
+                s.step()
+                z.record(se)
+                torch.cuda.synchronize()
+                tot_ms += a.elapsed_time(z)
+            tot_upd += n * n * 3 * args.plain_steps
+            s.close()
+        plain[name] = {"value": tot_upd / (tot_ms * 1e-3), "instances": len(sample),
+                       "steps_each": args.plain_steps}
+    return {
+        "workload": f"{len(sizes)} point-energy instances, sides uniform 128..640 "
+                    f"(numpy default_rng({BATCH_SEED})), [0,1.3]^2, corner E=0.244816/(dx*dy), "
+                    "E=1e-12 background, CFL 0.5",
+        "precision": "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, positivity, sweeps)",
+        "cells": int(sum(n * n for n in sizes)),
+        "value": value, "unit": UNIT, "ms": ms, "steps": args.batch_steps,
+        "graph_launches": 1, "admission_s": t_adm,
+        "l2": "not flushed: the batch's resident state (GBs) is far above L2",
+        "plain_fp64_one_at_a_time": plain["fp64"],
+        "fp32_bulk_one_at_a_time": plain["fp32_bulk_single"],
+        "speedup_vs_plain_fp64": value / plain["fp64"]["value"],
+        "rel_l1_density_err_vs_fp64": {f"{sizes[k]}^2": e for k, e in zip(check, errs)},
+    }
+
+
+def serving_draw(precision, device):
+    """Requests of the serving mix: the vortex (45^2..360^2, T=0.01) or a
+    point-energy instance (128^2..640^2, shortened to T=0.02)."""
+    from sweeping_fd_weno_gb300 import abi, problems
+
+    def draw(rng):
+        if rng.integers(0, 2) == 0:
+            n = int(rng.choice([45, 90, 180, 360]))
+            return problems.make_config(abi.VORTEX_2D, nx=n, ny=n, precision=precision,
+                                        device=device)
+        n = int(rng.integers(128, 641))
+        return problems.make_config(abi.SEDOV_2D, nx=n, ny=n, time_terminal=0.02,
+                                    precision=precision, device=device)
+    return draw
+
+
+def bench_serving(args, local):
+    """Poisson arrivals (mean 50 req/s) served by continuous batching (FP32 bulk)
+    and, for comparison, one at a time by the plain FP64 path."""
+    from sweeping_fd_weno_gb300 import Batch, abi
+    from sweeping_fd_weno_gb300.serving import (poisson_arrivals, serve_batched,
+                                                serve_one_at_a_time)
+    arr = poisson_arrivals(args.serve_rate, args.serve_requests, SERVE_SEED,
+                           serving_draw(abi.PRECISION_FP32_BULK, local))
+    with Batch(max_slots=args.serve_slots, max_nx=640, max_ny=640,
+               precision=abi.PRECISION_FP32_BULK, ubar_mode=abi.UBAR_TREE, device=local) as b:
+        rb = serve_batched(arr, b, step_chunk=args.serve_chunk)
+    # the same stream (same seed: same arrivals and requests) in plain FP64
+    plain = poisson_arrivals(args.serve_rate, args.serve_requests, SERVE_SEED,
+                             serving_draw(abi.PRECISION_FP64, local))
+    rp = serve_one_at_a_time(plain)
+    sb, sp = rb.summary(), rp.summary()
+    return {
+        "workload": f"{len(arr)} requests, Poisson arrivals mean {args.serve_rate:g}/s "
+                    f"(numpy default_rng({SERVE_SEED})): vortex 45^2..360^2 to T=0.01 or "
+                    "point energy 128^2..640^2 to T=0.02",
+        "batched_fp32_bulk": sb, "plain_fp64_one_at_a_time": sp,
+        "throughput_ratio": (sb["value"] / sp["value"]) if sp["value"] else None,
+        "slots": args.serve_slots, "step_chunk": args.serve_chunk,
+    }
+
+
 def run_reference(args, rank):
     """The reference's algorithm on the host CPU (its quad-literal build arithmetic)."""
     if rank != 0:
@@ -179,6 +354,16 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--plain-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--serve-chunk", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -350,6 +535,13 @@ def main():
         "sweep": {"invocations": prof["sweep_invocations"], "ms": prof["sweep_ms"]},
         "fp32_bulk": fp32,
     }
+    if not args.no_batched:
+        line["batched"] = bench_batched(args, local, flush)
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            line["batched"]["cpu_baseline"] = cpu_batched_baseline(
+                point_energy_sizes(args.batch_instances))
+    if not args.no_serving:
+        line["serving"] = bench_serving(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
     if rank == 0:

@@ -177,6 +177,13 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
                              int32_t literals, int32_t device, double* uleft,
                              double* uright);
 
+/* The u_bar summation of sweep_lim (ex3_vortex_accuracy_2d/main.f90:913-920)
+ * over a flat array: s = 0; DO m = 1, n: s = s + w*x(m), rounded step by step
+ * in that order, evaluated on the GPU by the kernel the sweep uses
+ * (a unit-test entry point; n < 2^31). */
+swfd_status swfd_sequential_sum(const double* x, int64_t n, double w, int32_t device,
+                                double* out);
+
 /* ---------------------------------------------------------------------------
  * Batched engine and serving.  No counterpart in the reference, which runs one
  * problem per program (the MPI examples spread one grid over 32 ranks).  Many
@@ -216,6 +223,12 @@ swfd_status swfd_batch_stats(swfd_batch* b, int64_t request_id, swfd_sweep_stats
 swfd_status swfd_batch_release(swfd_batch* b, int64_t request_id);
 swfd_status swfd_batch_info(swfd_batch* b, int32_t* running, int32_t* free_slots,
                             int64_t* free_bytes);
+/* Progress of one request: simulated time and SSP-RK3 steps taken so far
+ * (from the last run; no device synchronisation beyond that). */
+swfd_status swfd_batch_progress(swfd_batch* b, int64_t request_id, double* time_out,
+                                int64_t* steps_out);
+/* The CUDA stream (cudaStream_t) the batch's graph runs on. */
+swfd_status swfd_batch_get_stream(swfd_batch* b, void** stream);
 
 /* Instrumentation (no counterpart in the reference, which only prints a
  * wall-clock "CPU Time", ex4_sedov_2d/main.f90:111,118-119). */

@@ -133,6 +133,11 @@ _SIGS = {
     "swfd_batch_release": (C.c_int32, [_P, C.c_int64]),
     "swfd_batch_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int64)]),
+    "swfd_batch_get_stream": (C.c_int32, [_P, C.POINTER(_P)]),
+    "swfd_sequential_sum": (C.c_int32, [_DP, C.c_int64, C.c_double, C.c_int32,
+                                        C.POINTER(C.c_double)]),
+    "swfd_batch_progress": (C.c_int32, [_P, C.c_int64, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int64)]),
     "swfd_last_error": (C.c_int32, [_P, C.c_char_p, C.c_size_t]),
     "swfd_status_string": (C.c_char_p, [C.c_int32]),
 }

@@ -79,6 +79,17 @@ class Batch:
         abi.check(self.lib.swfd_batch_release(self.h, int(request_id)))
         self.shapes.pop(int(request_id), None)
 
+    def progress(self, request_id: int):
+        """(simulated time, steps taken) of a request as of the last run."""
+        t, n = C.c_double(), C.c_int64()
+        abi.check(self.lib.swfd_batch_progress(self.h, int(request_id), C.byref(t), C.byref(n)))
+        return t.value, n.value
+
+    def stream_ptr(self) -> int:
+        v = C.c_void_p()
+        abi.check(self.lib.swfd_batch_get_stream(self.h, C.byref(v)))
+        return v.value or 0
+
     def info(self):
         r, f, b = C.c_int32(), C.c_int32(), C.c_int64()
         abi.check(self.lib.swfd_batch_info(self.h, C.byref(r), C.byref(f), C.byref(b)))

@@ -863,6 +863,34 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
   return done(SWFD_OK);
 }
 
+swfd_status swfd_sequential_sum(const double* x, int64_t n, double w, int32_t device,
+                                double* out) {
+  if (n < 0 || n > INT32_MAX || (n > 0 && !x) || !out)
+    return fail(nullptr, SWFD_ERR_INVALID, "bad arguments");
+  CU(nullptr, cudaSetDevice(device));
+  double *dx = nullptr, *ds = nullptr;
+  cudaStream_t s = nullptr;
+  auto done = [&](swfd_status st) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(dx);
+    cudaFree(ds);
+    if (s) cudaStreamDestroy(s);
+    return st;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&dx, (n > 0 ? n : 1) * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&ds, sizeof(double))) != cudaSuccess ||
+      (n > 0 && (e = cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s)) !=
+                    cudaSuccess) ||
+      (e = launch_seq_sum(dx, (int)n, w, ds, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(out, ds, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return done(
+        fail(nullptr, SWFD_ERR_CUDA, std::string("swfd_sequential_sum: ") + cudaGetErrorString(e)));
+  return done(SWFD_OK);
+}
+
 swfd_status swfd_get_stream(swfd_handle* h, void** stream) {
   if (!h || !stream) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   *stream = (void*)h->stream;

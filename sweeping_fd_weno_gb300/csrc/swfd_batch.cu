@@ -50,6 +50,8 @@ struct swfd_batch {
   BatchCtl* h_ctl = nullptr;
   long long* d_prefix = nullptr;
   std::vector<long long> prefix;
+  DevScalars* d_dsc = nullptr;  // one DevScalars per slot, contiguous: one read-back per run
+  DevScalars* h_dsc = nullptr;  // pinned mirror
   cudaGraphExec_t g_run = nullptr;
   double* d_stage = nullptr;
   size_t stage_bytes = 0;
@@ -87,8 +89,7 @@ size_t bulk_plane_bytes(const Params& p, int fp32) {
 size_t slot_bytes(const Params& p, int fp32) {
   const size_t pb = plane_bytes(p), tb = bulk_plane_bytes(p, fp32);
   const int nc = p.g.nc;
-  return 3 * nc * pb + (4 * nc + 8) * tb + a256(4 * nc * tb) + a256(sweep_scratch_bytes(p)) +
-         a256(sizeof(DevScalars));
+  return 3 * nc * pb + (4 * nc + 8) * tb + a256(4 * nc * tb) + a256(sweep_scratch_bytes(p));
 }
 
 BatchLaunch launch_desc(swfd_batch* b) {
@@ -246,6 +247,8 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   if ((e = cudaMallocHost(&b->h_ctl, sizeof(BatchCtl))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_prefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess) return bad(e);
+  if ((e = cudaMalloc(&b->d_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
+  if ((e = cudaMallocHost(&b->h_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
   if ((e = cudaMemcpyAsync(b->d_tab, b->tab.data(), n * sizeof(BatchSlot), cudaMemcpyHostToDevice,
                            b->stream)) != cudaSuccess)
     return bad(e);
@@ -278,7 +281,9 @@ swfd_status swfd_batch_destroy(swfd_batch* b) {
   cudaFree(b->d_ctl);
   cudaFree(b->d_prefix);
   cudaFree(b->d_stage);
+  cudaFree(b->d_dsc);
   if (b->h_ctl) cudaFreeHost(b->h_ctl);
+  if (b->h_dsc) cudaFreeHost(b->h_dsc);
   for (int k = 0; k < 4; ++k)
     if (b->cap[k]) cudaStreamDestroy(b->cap[k]);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -339,7 +344,7 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   cptr += a256(4 * nc * tb);
   bs.sweep_scratch = cptr;
   cptr += a256(sweep_scratch_bytes(p));
-  sh.dsc = (DevScalars*)cptr;
+  sh.dsc = b->d_dsc + k;
   bs.dsc = sh.dsc;
   // planes are pb apart for the FP64 state; the bulk planes use the same
   // element pitch (plane) in their own type
@@ -411,11 +416,13 @@ swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out)
   BCU(b, cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, b->stream));
   BCU(b, cudaMemcpyAsync(b->tab.data(), b->d_tab, n * sizeof(BatchSlot), cudaMemcpyDeviceToHost,
                          b->stream));
+  BCU(b, cudaMemcpyAsync(b->h_dsc, b->d_dsc, n * sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                         b->stream));
   BCU(b, cudaStreamSynchronize(b->stream));
   for (int k = 0; k < n; ++k) {
     SlotHost& sh = b->slots[k];
     if (sh.state != 1) continue;
-    BCU(b, cudaMemcpy(&sh.last, sh.dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
+    sh.last = b->h_dsc[k];
     if (!b->tab[k].active) {
       sh.state = 2;
       sh.status = status_of(sh.last.error);
@@ -513,6 +520,24 @@ swfd_status swfd_batch_info(swfd_batch* b, int32_t* running, int32_t* free_slots
   if (running) *running = r;
   if (free_slots) *free_slots = f;
   if (free_bytes) *free_bytes = b->pool_bytes - b->used_bytes;
+  return SWFD_OK;
+}
+
+swfd_status swfd_batch_progress(swfd_batch* b, int64_t request_id, double* time_out,
+                                int64_t* steps_out) {
+  if (!b) return bfail(b, SWFD_ERR_INVALID, "NULL handle");
+  std::lock_guard<std::mutex> lk(b->mu);
+  int k = find_slot(b, request_id);
+  if (k < 0) return bfail(b, SWFD_ERR_INVALID, "unknown request id");
+  const SlotHost& sh = b->slots[k];
+  if (time_out) *time_out = sh.last.time;
+  if (steps_out) *steps_out = sh.last.steps;
+  return SWFD_OK;
+}
+
+swfd_status swfd_batch_get_stream(swfd_batch* b, void** stream) {
+  if (!b || !stream) return bfail(b, SWFD_ERR_INVALID, "NULL argument");
+  *stream = (void*)b->stream;
   return SWFD_OK;
 }
 

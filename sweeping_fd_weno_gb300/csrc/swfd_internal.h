@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 #include <string>
@@ -213,6 +214,7 @@ cudaError_t launch_batch_sweep_cond(const BatchLaunch& b, cudaGraphConditionalHa
 cudaError_t launch_rho_min(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_density_sweep(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+cudaError_t launch_seq_sum(const double* x, int n, double w, double* out, cudaStream_t s);
 // ordering < 0: the pass reads its ordering from dsc->ordering
 cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int forward,
                                  DevScalars* dsc, cudaStream_t s);

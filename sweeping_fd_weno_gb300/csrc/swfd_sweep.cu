@@ -87,27 +87,203 @@ cudaError_t launch_density_sweep(const Params& p, double* u, cudaStream_t s) {
 //  1D dot_product over -2..n+3, ex2_sedov_1d/main.f90:581-583).
 // One lane per component keeps the exact summation order.
 // ---------------------------------------------------------------------------
-__global__ void k_ubar_seq(Params p, const double* __restrict__ u, DevScalars* dsc) {
-  const Geom& g = p.g;
-  int c = threadIdx.x;
-  if (c >= g.nc) return;
-  const double* pl = u + c * g.plane;
+// The sum is a chain of dependent FP64 additions in the reference's order,
+// and a dependent FP64 addition on GB300 takes about 66 cycles.  The chain is
+// evaluated exactly without it: while the exact value s + p of a step stays
+// inside the binade [2^E, 2^(E+1)) of the running sum s = M * u (u = 2^(E-52),
+// M an integer in [2^52, 2^53]), the rounded result is (M + rne(p / u)) * u,
+// with rne the round-to-nearest of an integer-plus-fraction, so a run of such
+// steps is an integer prefix sum (done by the whole block in parallel).  The
+// first step of a window that leaves the binade, is a rounding tie (whose
+// result depends on the parity of the running sum), or meets a zero,
+// subnormal or non-finite value is done as one hardware addition, and the
+// integer path resumes after it.  Every step therefore rounds exactly as the
+// sequential loop does.
+constexpr int SUM_THREADS = 256;
+constexpr int SUM_PER_THREAD = 8;
+constexpr int SUM_WINDOW = SUM_THREADS * SUM_PER_THREAD;
+
+// p / u = ip + rem / 2^d relative to the binade with biased exponent eb of a
+// running sum of sign neg_s (mirrored to a positive sum): floor (fl) and
+// rounded value (r) in units of u; bad = 1 for a tie, an exponent above the
+// binade's or a non-finite p
+__device__ __forceinline__ void sum_classify(double p, int neg_s, int eb, long long& fl,
+                                             long long& r, int& bad) {
+  const unsigned long long pb = (unsigned long long)__double_as_longlong(p);
+  const int ps = (int)(pb >> 63) ^ neg_s;
+  int pe = (int)((pb >> 52) & 0x7ff);
+  unsigned long long mp = pb & 0xfffffffffffffull;
+  fl = 0;
+  r = 0;
+  bad = 0;
+  if (pe == 0x7ff) {
+    bad = 1;
+    return;
+  }
+  if (pe) mp |= 1ull << 52;
+  else pe = 1;
+  if (mp == 0) return;  // +-0
+  const int d = eb - pe;
+  if (d < 0) {  // |p / u| >= 2^53: the sum leaves the binade
+    bad = 1;
+    return;
+  }
+  unsigned long long ip, rem, half;
+  if (d == 0) {
+    ip = mp;
+    rem = 0;
+    half = 1;
+  } else if (d < 64) {
+    ip = mp >> d;
+    rem = mp & ((1ull << d) - 1);
+    half = 1ull << (d - 1);
+    if (rem == half) {
+      bad = 1;
+      return;
+    }
+  } else {  // 0 < |p / u| < 2^-10
+    ip = 0;
+    rem = 1;
+    half = 2;
+  }
+  const long long up = rem > half ? 1 : 0;
+  if (!ps) {
+    fl = (long long)ip;
+    r = (long long)ip + up;
+  } else {
+    fl = -(long long)ip - (rem != 0 ? 1 : 0);
+    r = -((long long)ip + up);
+  }
+}
+
+// s = 0; for m = 0..n-1: s = s + term(m)  (term(m) the FP64 product of the
+// reference), evaluated by one block of SUM_THREADS threads; every thread
+// returns s
+template <class Term>
+__device__ double seq_sum_block(int n, Term term) {
+  __shared__ unsigned long long warp_tot[SUM_THREADS / 32];
+  __shared__ int first_bad;
+  __shared__ double s_sh;
+  __shared__ int pos_sh;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   double s = 0.0;
+  int pos = 0;
+  while (pos < n) {
+    const unsigned long long sb = (unsigned long long)__double_as_longlong(s);
+    const int eb = (int)((sb >> 52) & 0x7ff);
+    if (eb == 0 || eb == 0x7ff) {  // zero, subnormal or non-finite sum: one hardware step
+      s = s + term(pos);
+      ++pos;
+      continue;
+    }
+    const int neg_s = (int)(sb >> 63);
+    const long long M = (long long)((sb & 0xfffffffffffffull) | (1ull << 52));
+    const int base = pos + tid * SUM_PER_THREAD;
+    long long fl[SUM_PER_THREAD], r[SUM_PER_THREAD];
+    int bad[SUM_PER_THREAD];
+    unsigned long long tsum = 0;
+#pragma unroll
+    for (int e = 0; e < SUM_PER_THREAD; ++e) {
+      const int m = base + e;
+      if (m < n) {
+        sum_classify(term(m), neg_s, eb, fl[e], r[e], bad[e]);
+      } else {
+        fl[e] = r[e] = 0;
+        bad[e] = 2;  // past the end
+      }
+      tsum += (unsigned long long)r[e];
+    }
+    // block-exclusive prefix of the per-thread sums (wrapping arithmetic: the
+    // values up to the first bad element are exact)
+    unsigned long long incl = tsum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long v = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += v;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    if (tid == 0) first_bad = INT_MAX;
+    __syncthreads();
+    unsigned long long R = incl - tsum;
+    for (int k = 0; k < wid; ++k) R += warp_tot[k];
+    int myfirst = INT_MAX;
+#pragma unroll
+    for (int e = 0; e < SUM_PER_THREAD; ++e) {
+      if (myfirst != INT_MAX) break;
+      const long long a = M + (long long)R + fl[e];
+      if (bad[e] || a < (1ll << 52) || a > (1ll << 53) - 1) {
+        myfirst = base + e;
+      } else {
+        R += (unsigned long long)r[e];
+      }
+    }
+    if (myfirst != INT_MAX) atomicMin(&first_bad, myfirst);
+    __syncthreads();
+    const int q = first_bad;
+    const bool writer = (q == INT_MAX) ? (tid == SUM_THREADS - 1) : (myfirst == q);
+    if (writer) {
+      // the sum after the integer run, M + R in units of u (in [2^52, 2^53])
+      const unsigned long long val = (unsigned long long)(M + (long long)R);
+      unsigned long long bits = (val == (1ull << 53))
+                                    ? ((unsigned long long)(eb + 1) << 52)
+                                    : (((unsigned long long)eb << 52) | (val - (1ull << 52)));
+      bits |= (unsigned long long)neg_s << 63;
+      double sn = __longlong_as_double((long long)bits);
+      int np;
+      if (q == INT_MAX) {
+        np = pos + SUM_WINDOW;
+      } else if (q < n) {
+        sn = sn + term(q);  // the step the integer path does not take
+        np = q + 1;
+      } else {
+        np = n;
+      }
+      s_sh = sn;
+      pos_sh = np;
+    }
+    __syncthreads();
+    s = s_sh;
+    pos = pos_sh;
+    __syncthreads();
+  }
+  return s;
+}
+
+// u_bar of one component (blockIdx.x): 2D weights 1/(nx*ny) over the interior
+// in j-outer/i-inner order, 1D 1/(n+6) over -2..n+3
+__device__ void ubar_component(const Geom& g, const double* __restrict__ u, int c, double* out) {
+  const double* pl = u + c * g.plane;
+  double s;
   if (g.ndim == 1) {
     const double w = 1 / ((double)g.nx + 6);
-    for (int i = -2; i <= g.nx + 3; ++i) s = s + pl[g.at(i, -2)] * w;
+    s = seq_sum_block(g.nx + 6, [&](int m) { return pl[m] * w; });
   } else {
     const double w = 1. / ((double)g.nx * (double)g.ny);
-    for (int j = 1; j <= g.ny; ++j) {
-      const double* row = pl + g.at(0, j);
-      for (int i = 1; i <= g.nx; ++i) s = s + w * row[i];
-    }
+    const int nx = g.nx;
+    s = seq_sum_block(g.nx * g.ny, [&](int m) { return w * pl[g.at(m % nx + 1, m / nx + 1)]; });
   }
-  dsc->ubar[c] = s;
+  if (threadIdx.x == 0) out[c] = s;
+}
+
+__global__ void __launch_bounds__(SUM_THREADS) k_ubar_seq(Params p, const double* __restrict__ u,
+                                                          DevScalars* dsc) {
+  if ((int)blockIdx.x < p.g.nc) ubar_component(p.g, u, blockIdx.x, dsc->ubar);
+}
+
+// the same summation over a flat array (test entry point)
+__global__ void __launch_bounds__(SUM_THREADS) k_seq_sum(const double* __restrict__ x, int n,
+                                                         double w, double* out) {
+  const double s = seq_sum_block(n, [&](int m) { return w * x[m]; });
+  if (threadIdx.x == 0) *out = s;
+}
+
+cudaError_t launch_seq_sum(const double* x, int n, double w, double* out, cudaStream_t s) {
+  k_seq_sum<<<1, SUM_THREADS, 0, s>>>(x, n, w, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
-  k_ubar_seq<<<1, 32, 0, s>>>(p, u, dsc);
+  k_ubar_seq<<<p.g.nc, SUM_THREADS, 0, s>>>(p, u, dsc);
   return cudaGetLastError();
 }
 
@@ -598,17 +774,10 @@ __global__ void kb_ubar(const BatchSlot* __restrict__ tab, int out, int tree) {
   const double* u = sl.st[out];
   const double w = 1. / ((double)g.nx * (double)g.ny);
   if (!tree) {
-    const int c = threadIdx.x;
-    if (c >= g.nc) return;
-    const double* pl = u + c * g.plane;
-    double s = 0.0;
-    for (int j = 1; j <= g.ny; ++j) {
-      const double* row = pl + g.at(0, j);
-      for (int i = 1; i <= g.nx; ++i) s = s + w * row[i];
-    }
-    sl.dsc->ubar[c] = s;
+    if ((int)blockIdx.x < g.nc) ubar_component(g, u, blockIdx.x, sl.dsc->ubar);
     return;
   }
+  if (blockIdx.x != 0) return;
   __shared__ double red[4][256];
   double acc[4] = {0, 0, 0, 0};
   const int64_t n = (int64_t)g.nx * g.ny;
@@ -742,7 +911,7 @@ cudaError_t launch_batch_sweep_head(const BatchLaunch& b, int out, cudaStream_t 
   kb_density_decide<<<gs, 128, 0, s>>>(b.tab, n);
   batch_pass<1>(b, out, 1, 1, s);
   batch_pass<1>(b, out, 1, 0, s);
-  kb_ubar<<<dim3(1, n), b.ubar_tree ? 256 : 32, 0, s>>>(b.tab, out, b.ubar_tree);
+  kb_ubar<<<dim3(4, n), SUM_THREADS, 0, s>>>(b.tab, out, b.ubar_tree);
   kb_sweep_begin<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
   return cudaGetLastError();
 }
