@@ -37,10 +37,16 @@ UNIT = "cell-updates/s"
 # compulsory HBM traffic of one fused 2D FP64 RK stage, bytes per cell
 # (read u_k and u0, write u_k+1: 85.3 B averaged over the three stages)
 STAGE_BYTES_PER_CELL = (64 + 96 + 96) / 3.0
-# algorithmic FP64 work of one interface flux (Roe eigenvectors, 40 projections,
-# 8 WENO5 reconstructions, back projection), counted from the kernel source:
-# 800 adds/multiplies + 50 divisions + 1 square root
+# FP64 work of one interface flux (Roe eigenvectors, 40 projections, 8 WENO5
+# reconstructions, back projection): 800 adds/multiplies + 50 divisions + 1
+# square root in the source; executed, 1197 FP64 pipe instructions (379 DADD,
+# 465 DMUL, 353 DFMA -- the DFMAs are the correctly rounded divisions and the
+# square root), counted by ncu on k_flux_xy<double>
 FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
+FLUX_FP64_INST_PER_INTERFACE = 1197
+# DRAM bytes of one k_flux_xy<double> launch per interior cell, from an ncu
+# capture of the 1024x1024 vortex (313.6 MB per launch, inputs above L2)
+FLUX_DRAM_BYTES_PER_CELL = 313.6e6 / (1024 * 1024)
 
 
 def env_int(k, d):
@@ -463,18 +469,25 @@ def main():
     # write 8 doubles per interface
     launch_bytes = 2 * cells * (12 + 8) * 8.0
     achieved = launch_bytes / (flux_ms_per_launch * 1e-3) / 1e9
-    launch_flops = 2 * cells * FLUX_FLOPS_PER_INTERFACE
-    fp64_achieved = launch_flops / (flux_ms_per_launch * 1e-3) / 1e9
+    launch_inst = 2 * cells * FLUX_FP64_INST_PER_INTERFACE
+    fp64_inst_rate = launch_inst / (flux_ms_per_launch * 1e-3) / 1e9
+    fp64_peak_inst = fp64.value / 2.0  # the probe counts a DFMA as 2 flops
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": achieved / hbm_peak, "traffic": None,
+        "frac": achieved / hbm_peak,
+        "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_flux_xy<double> "
+                          "on the 1024x1024 vortex (313.6 MB), scaled per cell to this grid",
         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
         "kernel": "k_flux_xy (characteristic WENO5 interface fluxes, both directions)",
         "launch_ms": flux_ms_per_launch,
         "compute_bound": "fp64",
-        "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64.value,
-                 "frac": fp64_achieved / fp64.value if fp64.value else None,
-                 "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains)",
+        "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,
+                 "frac": fp64_inst_rate / fp64_peak_inst if fp64_peak_inst else None,
+                 "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains; 2 flops each)",
+                 "inst_per_interface": FLUX_FP64_INST_PER_INTERFACE,
+                 "achieved_gflops_source_count": 2 * cells * FLUX_FLOPS_PER_INTERFACE
+                 / (flux_ms_per_launch * 1e-3) / 1e9,
                  "flops_per_interface": FLUX_FLOPS_PER_INTERFACE},
         "stage_hbm": {"achieved": STAGE_BYTES_PER_CELL * value / 1e9, "peak": hbm_peak,
                       "frac": STAGE_BYTES_PER_CELL * value / 1e9 / hbm_peak,

@@ -2,6 +2,7 @@
 // step/stage orchestration, the sweep driver and the statistics.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -370,11 +371,15 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
   b.k(1);
   // external event-record nodes (a plain record on a capturing stream would
   // only be a capture dependency)
-  if (events) B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
+  if (events)
+    B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1)], s)
+                    : cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
   B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux, &h->dsc->flux_work, s));
   b.k(1);
   if (events)
-    B_OK(b, cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s, cudaEventRecordExternal));
+    B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1) + 1], s)
+                    : cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s,
+                                               cudaEventRecordExternal));
   B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
   b.k(1);
   if (h->cfg.use_limiter == 2) {
@@ -409,8 +414,33 @@ void emit_step(Builder& b, cudaStream_t s, bool events) {
 
 enum { GRAPH_STEP = 0, GRAPH_SOLVE = 1, GRAPH_SWEEP = 2 };
 
+// the work of one graph kind, emitted into a capture or launched eagerly
+void emit_kind(Builder& b, cudaStream_t s, int kind) {
+  swfd_handle* h = b.h;
+  if (kind == GRAPH_STEP) {
+    emit_step(b, s, true);
+    B_OK(b, launch_time_advance(h->dsc, s));
+    b.k(1);
+  } else if (kind == GRAPH_SOLVE) {
+    const double T = h->cfg.time_terminal;
+    B_OK(b, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), s));
+    cudaGraphConditionalHandle hr = b.handle();
+    B_OK(b, launch_run_cond(hr, h->dsc, T, s));
+    b.k(1);
+    b.cond(s, cudaGraphCondTypeWhile, hr, [&](cudaStream_t sb) {
+      emit_step(b, sb, false);
+      B_OK(b, launch_time_advance_cond(hr, h->dsc, T, sb));
+      b.k(1);
+    });
+  } else {
+    h->k_sweep_fixed = 0;
+    b.count = &h->k_sweep_fixed;
+    emit_sweep(b, s, h->st[h->cur]);
+  }
+}
+
 swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
-  if (*out) return SWFD_OK;
+  if (*out || h->eager) return SWFD_OK;
   Builder b;
   b.h = h;
   b.cap = h->cap;
@@ -418,23 +448,7 @@ swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
   CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   cudaStreamCaptureStatus cs;
   b.ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &b.root, nullptr, nullptr, nullptr));
-  if (kind == GRAPH_STEP) {
-    emit_step(b, s, true);
-    B_OK(b, launch_time_advance(h->dsc, s));
-  } else if (kind == GRAPH_SOLVE) {
-    const double T = h->cfg.time_terminal;
-    B_OK(b, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), s));
-    cudaGraphConditionalHandle hr = b.handle();
-    B_OK(b, launch_run_cond(hr, h->dsc, T, s));
-    b.cond(s, cudaGraphCondTypeWhile, hr, [&](cudaStream_t sb) {
-      emit_step(b, sb, false);
-      B_OK(b, launch_time_advance_cond(hr, h->dsc, T, sb));
-    });
-  } else {
-    h->k_sweep_fixed = 0;
-    b.count = &h->k_sweep_fixed;
-    emit_sweep(b, s, h->st[h->cur]);
-  }
+  emit_kind(b, s, kind);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(s, &g);
   if (b.err != cudaSuccess || e2 != cudaSuccess) {
@@ -450,6 +464,23 @@ swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
   return SWFD_OK;
 }
 
+// run one graph kind: launch its graph, or (eager mode) its kernels directly
+swfd_status launch_kind(swfd_handle* h, int kind, cudaGraphExec_t g) {
+  if (!h->eager) {
+    CU(h, cudaGraphLaunch(g, h->stream));
+    return SWFD_OK;
+  }
+  Builder b;
+  b.h = h;
+  b.eager = true;
+  b.cond_word = &h->dsc->cond;
+  b.launched = &h->eager_launches;
+  emit_kind(b, h->stream, kind);
+  if (b.err != cudaSuccess)
+    return fail(h, SWFD_ERR_CUDA, std::string("eager launch: ") + cudaGetErrorString(b.err));
+  return SWFD_OK;
+}
+
 // kernels run by a launch, from the counters' increments (a step: its three
 // stages and the time advance; a sweep: its fixed part, the density sweep if
 // it ran, and one body per iteration q)
@@ -458,8 +489,13 @@ void account(swfd_handle* h, const DevScalars& before, const DevScalars& after, 
   int64_t sweeps = after.sweep_count - before.sweep_count;
   int64_t dens = after.den_count - before.den_count;
   int64_t qs = after.pre_count - before.pre_count;
-  h->prof.kernel_launches += steps * (h->k_stage + 1) + sweeps * h->k_sweep_fixed +
-                             dens * h->k_density + qs * h->k_q + extra;
+  if (h->eager) {  // counted as launched
+    h->prof.kernel_launches += h->eager_launches;
+    h->eager_launches = 0;
+  } else {
+    h->prof.kernel_launches += steps * (h->k_stage + 1) + sweeps * h->k_sweep_fixed +
+                               dens * h->k_density + qs * h->k_q + extra;
+  }
   h->prof.stages += 3 * steps;
   h->prof.sweep_invocations += sweeps;
 }
@@ -561,6 +597,10 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     return fail(nullptr, st, err);
   }
   h->device = cfg->device;
+  {  // SWFD_LAUNCH=eager: plain stream launches instead of graphs (for profilers)
+    const char* lm = getenv("SWFD_LAUNCH");
+    h->eager = lm && strcmp(lm, "eager") == 0;
+  }
   const Geom& g = h->p.g;
   auto cleanup_fail = [&](cudaError_t e) {
     std::string m = std::string("swfd_create: ") + cudaGetErrorString(e);
@@ -685,7 +725,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   ST(build_graph(h, GRAPH_STEP, &h->g_step));
   ST(ensure_tracks(h, 3));
   DevScalars before = *h->hsc;
-  CU(h, cudaGraphLaunch(h->g_step, h->stream));
+  ST(launch_kind(h, GRAPH_STEP, h->g_step));
   swfd_status st = check_device_error(h);
   account(h, before, *h->hsc, 1, 0);
   if (h->prof_on) {
@@ -719,7 +759,7 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
     DevScalars before = *h->hsc;
     CU(h, cudaMemcpyAsync(&h->dsc->steps_limit, &lim, sizeof(long long), cudaMemcpyHostToDevice,
                           h->stream));
-    CU(h, cudaGraphLaunch(h->g_solve, h->stream));
+    ST(launch_kind(h, GRAPH_SOLVE, h->g_solve));
     st = check_device_error(h);
     int64_t steps = h->hsc->steps;
     account(h, before, *h->hsc, steps, 2);
@@ -753,7 +793,7 @@ swfd_status swfd_sweep(swfd_handle* h) {
   ST(build_graph(h, GRAPH_SWEEP, &h->g_sweep));
   ST(ensure_tracks(h, 1));
   DevScalars before = *h->hsc;
-  CU(h, cudaGraphLaunch(h->g_sweep, h->stream));
+  ST(launch_kind(h, GRAPH_SWEEP, h->g_sweep));
   swfd_status st = check_device_error(h);
   account(h, before, *h->hsc, 0, 0);
   return st;

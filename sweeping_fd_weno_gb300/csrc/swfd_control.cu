@@ -12,15 +12,15 @@ __device__ __forceinline__ double decode_key(unsigned long long k) {
 }
 
 // IF postag == 1 (ex3_vortex_accuracy_2d/main.f90:590-595)
-__global__ void k_cond_postag(cudaGraphConditionalHandle h, const DevScalars* d) {
-  cudaGraphSetConditional(h, d->postag ? 1u : 0u);
+__global__ void k_cond_postag(cudaGraphConditionalHandle h, DevScalars* d) {
+  set_cond(h, &d->cond, d->postag ? 1u : 0u);
 }
 
 // IF rho_min < 1d-12 (ex3_vortex_accuracy_2d/main.f90:1155-1156); den_count (:1187)
 __global__ void k_cond_density(cudaGraphConditionalHandle h, DevScalars* d) {
   bool go = decode_key(d->rho_min_key) < 1e-12;
   if (go) d->den_count++;
-  cudaGraphSetConditional(h, go ? 1u : 0u);
+  set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
 // 1D: the density sweep always runs (ex2_sedov_1d/main.f90:774)
@@ -34,7 +34,7 @@ __global__ void k_sweep_begin(cudaGraphConditionalHandle h, Params p, DevScalars
     const double* ub = d->ubar;
     if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.) {
       d->error |= ERR_BIT_PUBAR;
-      cudaGraphSetConditional(h, 0u);
+      set_cond(h, &d->cond, 0u);
       return;
     }
   }
@@ -47,7 +47,7 @@ __global__ void k_sweep_begin(cudaGraphConditionalHandle h, Params p, DevScalars
   d->t_pos = 0;
   d->t_neg = 0;
   d->q = 0;
-  cudaGraphSetConditional(h, swp_num >= 1 ? 1u : 0u);
+  set_cond(h, &d->cond, swp_num >= 1 ? 1u : 0u);
 }
 
 // start of sweep iteration q: odd q ordering I, even q ordering II (:933)
@@ -66,23 +66,23 @@ __global__ void k_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num
       d->tracks[d->track_cap + k] = (int)d->t_neg;
       d->tracks[2 * d->track_cap + k] = (int)d->t_pos;
     }
-    cudaGraphSetConditional(h, 0u);
+    set_cond(h, &d->cond, 0u);
     return;
   }
   if (d->q >= swp_num) {
     d->fail_count++;
     if (stop_on_fail) d->error |= ERR_BIT_NOCONV;
-    cudaGraphSetConditional(h, 0u);
+    set_cond(h, &d->cond, 0u);
     return;
   }
-  cudaGraphSetConditional(h, 1u);
+  set_cond(h, &d->cond, 1u);
 }
 
 // DO WHILE (time <= time_terminal - 1d-10) (ex3_vortex_accuracy_2d/main.f90:51),
 // bounded by the launch's step limit and stopped by an error
-__global__ void k_run_cond(cudaGraphConditionalHandle h, const DevScalars* d, double t_end) {
+__global__ void k_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end) {
   bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
-  cudaGraphSetConditional(h, go ? 1u : 0u);
+  set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
 // time = time + dt (:53), then the loop test
@@ -90,10 +90,10 @@ __global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d,
   d->time = d->time + d->dt;
   d->steps++;
   bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
-  cudaGraphSetConditional(h, go ? 1u : 0u);
+  set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
-cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, const DevScalars* d, cudaStream_t s) {
+cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s) {
   k_cond_postag<<<1, 1, 0, s>>>(h, d);
   return cudaGetLastError();
 }
@@ -119,7 +119,7 @@ cudaError_t launch_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_nu
   k_q_end<<<1, 1, 0, s>>>(h, d, swp_num, stop_on_fail);
   return cudaGetLastError();
 }
-cudaError_t launch_run_cond(cudaGraphConditionalHandle h, const DevScalars* d, double t_end,
+cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
                             cudaStream_t s) {
   k_run_cond<<<1, 1, 0, s>>>(h, d, t_end);
   return cudaGetLastError();

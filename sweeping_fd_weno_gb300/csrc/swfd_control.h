@@ -5,7 +5,7 @@
 
 namespace swfd {
 
-cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, const DevScalars* d, cudaStream_t s);
+cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s);
 cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s);
 cudaError_t launch_count_density(DevScalars* d, cudaStream_t s);
 cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, DevScalars* d,
@@ -13,7 +13,7 @@ cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, De
 cudaError_t launch_q_begin(const Params& p, DevScalars* d, cudaStream_t s);
 cudaError_t launch_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num, int stop_on_fail,
                          cudaStream_t s);
-cudaError_t launch_run_cond(cudaGraphConditionalHandle h, const DevScalars* d, double t_end,
+cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
                             cudaStream_t s);
 cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
                                      cudaStream_t s);

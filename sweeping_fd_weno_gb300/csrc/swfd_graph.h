@@ -13,6 +13,11 @@ namespace swfd {
 // cudaStreamUpdateCaptureDependencies) and its body is captured on the
 // stream of the next nesting depth.  The control kernels of swfd_control.cu
 // set the conditions on the device.
+//
+// In eager mode the same emitters launch directly on the stream: handles are
+// 0, the control kernels write each decision to a condition word, and cond()
+// reads it back (after a stream synchronisation) to run a body once (IF) or
+// while it stays set (WHILE).
 // ---------------------------------------------------------------------------
 struct Builder {
   swfd_handle* h = nullptr;
@@ -21,17 +26,35 @@ struct Builder {
   int depth = 0;
   int* count = nullptr;  // kernels emitted into the current section
   cudaError_t err = cudaSuccess;
+  bool eager = false;
+  const int* cond_word = nullptr;  // eager: device word the control kernels write
+  long long* launched = nullptr;   // eager: kernels launched
   bool ok(cudaError_t e) {
     if (e != cudaSuccess && err == cudaSuccess) err = e;
     return err == cudaSuccess;
   }
   void k(int n) {
     if (count) *count += n;
+    if (launched) *launched += n;
+  }
+  bool read_cond(cudaStream_t s) {
+    int v = 0;
+    if (!ok(cudaStreamSynchronize(s))) return false;
+    if (!ok(cudaMemcpy(&v, cond_word, sizeof(int), cudaMemcpyDeviceToHost))) return false;
+    return v != 0;
   }
   template <class F>
   void cond(cudaStream_t s, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle hnd,
             F body) {
     if (err != cudaSuccess) return;
+    if (eager) {
+      if (type == cudaGraphCondTypeIf) {
+        if (read_cond(s)) body(s);
+      } else {
+        while (err == cudaSuccess && read_cond(s)) body(s);
+      }
+      return;
+    }
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -63,7 +86,10 @@ struct Builder {
   }
   cudaGraphConditionalHandle handle() {
     cudaGraphConditionalHandle hnd = 0;
+    if (eager) return 0;
     ok(cudaGraphConditionalHandleCreate(&hnd, root, 0, 0));
+    // handle 0 selects the eager path in the control kernels
+    if (err == cudaSuccess && hnd == 0) err = cudaErrorUnknown;
     return hnd;
   }
 };

@@ -86,7 +86,15 @@ struct DevScalars {
   int sweeping;           // this instance is inside its sweep q loop
   int dens_active;        // this instance runs the density sweep of this stage
   double t_end;           // time_terminal of the instance
+  int cond;               // eager launch mode: value of the last conditional decision
 };
+
+// The value of a conditional node: set on the graph's handle, or written to
+// a condition word when the section runs as plain launches (handle 0).
+__device__ __forceinline__ void set_cond(cudaGraphConditionalHandle h, int* word, unsigned v) {
+  if (h) cudaGraphSetConditional(h, v);
+  else *word = (int)v;
+}
 
 // One instance of the batched engine, as the batched kernels see it.
 struct BatchSlot {
@@ -116,6 +124,7 @@ struct BatchCtl {
   long long total_chunks;
   long long steps;        // steps taken by the current launch
   long long steps_limit;
+  int cond;               // eager launch mode: value of the last conditional decision
 };
 
 // What a batched launch needs (host side).
@@ -162,6 +171,11 @@ struct swfd_handle {
   int64_t track_cap = 0;
   // kernels per graph section, for launch accounting
   int k_stage = 0, k_sweep_fixed = 0, k_density = 0, k_q = 0, k_step = 0;
+  // eager launch mode (SWFD_LAUNCH=eager): the graph sections run as plain
+  // stream launches and the conditions are read back on the host; for
+  // profilers that do not look inside graphs with conditional nodes
+  int eager = 0;
+  long long eager_launches = 0;
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles

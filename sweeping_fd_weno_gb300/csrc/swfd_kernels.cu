@@ -846,13 +846,13 @@ __global__ void kb_time_advance(BatchSlot* __restrict__ tab, BatchCtl* ctl, int 
   }
 }
 
-__global__ void kb_cond_any_postag(cudaGraphConditionalHandle h, const BatchCtl* ctl) {
-  cudaGraphSetConditional(h, ctl->any_postag ? 1u : 0u);
+__global__ void kb_cond_any_postag(cudaGraphConditionalHandle h, BatchCtl* ctl) {
+  set_cond(h, &ctl->cond, ctl->any_postag ? 1u : 0u);
 }
 
 __global__ void kb_run_cond(cudaGraphConditionalHandle h, BatchCtl* ctl, int advance) {
   if (advance) ctl->steps++;
-  cudaGraphSetConditional(h, (ctl->n_active > 0 && ctl->steps < ctl->steps_limit) ? 1u : 0u);
+  set_cond(h, &ctl->cond, (ctl->n_active > 0 && ctl->steps < ctl->steps_limit) ? 1u : 0u);
 }
 
 static int batch_grid_x(int n_slots, long long max_cell) {

@@ -882,8 +882,8 @@ __global__ void kb_q_end(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
   }
 }
 
-__global__ void kb_q_cond(cudaGraphConditionalHandle h, const BatchCtl* ctl) {
-  cudaGraphSetConditional(h, ctl->n_sweeping > 0 ? 1u : 0u);
+__global__ void kb_q_cond(cudaGraphConditionalHandle h, BatchCtl* ctl) {
+  set_cond(h, &ctl->cond, ctl->n_sweeping > 0 ? 1u : 0u);
 }
 
 static int bgx(const BatchLaunch& b) {
