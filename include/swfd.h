@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define SWFD_ABI_VERSION 1
+#define SWFD_ABI_VERSION 2
 
 typedef int32_t swfd_status;
 enum {
@@ -45,7 +45,10 @@ enum {
   SWFD_ERR_OOM = -6,            /* device allocation refused */
   SWFD_ERR_TIMEOUT = -7,        /* a bounded device-side wait expired */
   SWFD_ERR_UNSUPPORTED = -8,    /* option recognised but not implemented */
-  SWFD_ERR_MAX_STEPS = -9       /* run_to stopped at its step limit */
+  SWFD_ERR_MAX_STEPS = -9,      /* run_to stopped at its step limit */
+  SWFD_ERR_SWEEP_CHECK = -10    /* a nodal adjustment raised the pair's total
+                                   pressure (ex6_shock_diffraction/main.f90:1413-1423,
+                                   1472-1482 `stop`) */
 };
 
 /* Problem = one reference example, with all of its per-example switches
@@ -54,7 +57,13 @@ enum {
   SWFD_PROBLEM_SEDOV_1D = 2,   /* ex2_sedov_1d/main.f90 */
   SWFD_PROBLEM_VORTEX_2D = 3,  /* ex3_vortex_accuracy_2d/main.f90 */
   SWFD_PROBLEM_SEDOV_2D = 4,   /* ex4_sedov_2d/main.f90 on one 1x1 block */
-  SWFD_PROBLEM_JET_2D = 5      /* ex5_mach2000_jet/main.f90 */
+  SWFD_PROBLEM_JET_2D = 5,     /* ex5_mach2000_jet/main.f90 */
+  SWFD_PROBLEM_SHOCK_DIFFRACTION = 6  /* ex6_shock_diffraction/main.f90: the
+                                   reference's cut_x x cut_y MPI decomposition is
+                                   part of its arithmetic (per-rank-row and
+                                   per-rank-column Lax-Friedrichs alpha, fluxes at
+                                   rank boundaries computed by both ranks) and is
+                                   reproduced on one grid */
 };
 
 /* How the reference's double-kind literals (1d-6, 13d0/12d0, 0.75d0, ...)
@@ -96,7 +105,11 @@ typedef struct swfd_config {
   double e_blast;        /* point-energy problems: blast energy numerator
                             (1D: E = e_blast/dx, 2D: E = e_blast/(dx*dy)) */
   int32_t sweep_mode;    /* SWFD_SWEEP_PARALLEL (default) or SWFD_SWEEP_SEQUENTIAL */
-  int32_t reserved[7];   /* zero */
+  int32_t total;         /* shock diffraction: the reference's `total` (step width in
+                            cells; the step top is row 6*total); 0 otherwise */
+  int32_t cut_x, cut_y;  /* shock diffraction: the reference's rank grid (4 x 8);
+                            nx = cut_x*(13*total/cut_x), ny = cut_y*(11*total/cut_y) */
+  int32_t reserved[4];   /* zero */
 } swfd_config;
 
 /* Sweep statistics exactly as the reference counts them

@@ -64,6 +64,15 @@ typedef struct oracle {
   int32_t *sweep_track, *neg_track, *pos_track;
   int64_t track_cap;
   int status;
+  /* ex6 (shock diffraction): the reference's cut_x x cut_y MPI ranks, each a
+   * local grid nxl x nyl with its own ghost layers (`rk`), the per-cell alpha
+   * of each rank, and the inflow state */
+  int ex4like; /* ex4 and ex6: eps2 flux guard, 1d-15 Roe regularisers */
+  int total, cut_x, cut_y, nxl, nyl, px, py;
+  struct oracle** rk;
+  double* alpha;
+  double dle, ule, ple;
+  int ranks_stale; /* the global state was set from outside: rebuild the ranks */
 } oracle;
 
 /* ------------------------------------------------------------------ */
@@ -197,7 +206,7 @@ static inline double rk3(const oracle* o, double u0, double v) {
 static void fflux2d(const oracle* o, const double* a, double* f, int gdir) {
   double rho = a[0], mx = a[1], my = a[2], e = a[3];
   double vx = mx / rho, vy = my / rho;
-  int guard = (o->problem == SWFD_PROBLEM_SEDOV_2D) ? (rho < o->eps2) : lt_lit_1em8(o, rho);
+  int guard = o->ex4like ? (rho < o->eps2) : lt_lit_1em8(o, rho);
   if (guard) vx = 0.0;
   if (guard) vy = 0.0;
   double pres = o->gamma1 * (e - 0.5 * rho * (vx * vx) - 0.5 * rho * (vy * vy));
@@ -257,7 +266,7 @@ static void interface2d(const oracle* o, int ydir, double wl, double wr, double 
   double evr[4][4], evl[4][4], cu_p[4][5], cu_n[4][5], ur[4], ul[4];
   const double g1 = o->gamma1;
   double t0, t1, t2, t3;
-  if (o->problem == SWFD_PROBLEM_SEDOV_2D && o->quad)
+  if (o->ex4like && o->quad)
     t0 = (double)((Q)wl / ((Q)(wl + wr) + (Q)1e-15f128));
   else
     t0 = wl / (wl + wr + 1.e-15);
@@ -267,9 +276,9 @@ static void interface2d(const oracle* o, int ydir, double wl, double wr, double 
   double hm = t0 * hl + t1 * hr;
   double qm = 0.5 * (vxm * vxm + vym * vym);
   double cm;
-  if (o->problem == SWFD_PROBLEM_SEDOV_2D && o->quad)
+  if (o->ex4like && o->quad)
     cm = (double)((Q)sqrt(fabs(g1 * (hm - qm))) + (Q)1e-15f128);
-  else if (o->problem == SWFD_PROBLEM_SEDOV_2D)
+  else if (o->ex4like)
     cm = sqrt(fabs(g1 * (hm - qm))) + 1e-15;
   else
     cm = sqrt(fabs(g1 * (hm - qm))) + 1.e-15;
@@ -327,7 +336,7 @@ static void prep_cell(const oracle* o, int ydir, const double* a, double* w, dou
                       double* vy, double* h) {
   double den = a[0], xmt = a[1], ymt = a[2], eng = a[3];
   double t0;
-  if (ydir && o->problem == SWFD_PROBLEM_SEDOV_2D) {
+  if (ydir && o->ex4like) {
     if (o->quad)
       t0 = (double)((Q)1 / ((Q)den + (Q)1e-15f128));
     else
@@ -415,7 +424,7 @@ static void scheme2d(oracle* o) {
   const size_t n = (size_t)o->nc * o->LI * o->LJ;
   memset(o->rhs, 0, n * sizeof(double));
   const double am = o->alphamax, dx = o->dx, dy = o->dy;
-  const int premul = (o->problem == SWFD_PROBLEM_SEDOV_2D);
+  const int premul = o->ex4like;
   for (int i = 1; i <= o->nx; ++i)
     for (int j = 1; j <= o->ny; ++j)
       for (int c = 0; c < 4; ++c) {
@@ -623,12 +632,12 @@ static void scalar_sweep2d(oracle* o) {
 
 /* one forward or backward pass along an ordering
  * (ex3_vortex_accuracy_2d/main.f90:939-1016 ordering I, :1023-1104 ordering II) */
-static void pressure_pass2d(oracle* o, const int* oi, const int* oj, int N, int forward,
-                            const double* ubar) {
+static int pressure_pass2d(oracle* o, const int* oi, const int* oj, int N, int forward,
+                           const double* ubar, int check) {
   const double g1 = o->gamma1, eps = o->eps, w = o->weight;
   int k0 = forward ? 0 : N - 1, k1 = forward ? N - 1 : 0, dk = forward ? 1 : -1;
   for (int k = k0; k != k1; k += dk) {
-    double vi[4], vp[4], vit[4], d[4];
+    double vi[4], vp[4], vit[4], d[4], vpt[4];
     for (int c = 0; c < 4; ++c) vi[c] = U(o->u, c, oi[k], oj[k]);
     double pres_v_i = pres2d_sweep(g1, vi);
     if (pres_v_i <= eps || vi[0] <= eps) {
@@ -636,11 +645,21 @@ static void pressure_pass2d(oracle* o, const int* oi, const int* oj, int N, int 
       nod_lim2d(o, vi, vp, ubar, vit);
       for (int c = 0; c < 4; ++c) d[c] = vi[c] - vit[c];
       for (int c = 0; c < 4; ++c) {
+        vpt[c] = vp[c] + (w / w) * (d[c]);
         U(o->u, c, oi[k], oj[k]) = vit[c];
-        U(o->u, c, oi[k + dk], oj[k + dk]) = vp[c] + (w / w) * (d[c]);
+        U(o->u, c, oi[k + dk], oj[k + dk]) = vpt[c];
+      }
+      /* ex6: total pressure must not increase (ex6_shock_diffraction/main.f90:1413-1423,
+       * active in the ordering-I passes) */
+      if (check) {
+        double pres_v_p = pres2d_sweep(g1, vp);
+        double pres_v_i_t = pres2d_sweep(g1, vit);
+        double pres_v_p_t = pres2d_sweep(g1, vpt);
+        if (pres_v_i + pres_v_p > pres_v_i_t + pres_v_p_t + eps) return SWFD_ERR_SWEEP_CHECK;
       }
     }
   }
+  return SWFD_OK;
 }
 
 /* sweep_lim (ex3_vortex_accuracy_2d/main.f90:888-1137; P(u_bar) check and
@@ -662,7 +681,7 @@ static int sweep_lim2d(oracle* o) {
       ea = ea + w * U(o->u, 3, i, j);
     }
   double ubar[4] = {ra, m1a, m2a, ea};
-  if (o->problem == SWFD_PROBLEM_SEDOV_2D) {
+  if (o->ex4like) {
     if (o->gamma1 * (ubar[3] - 0.5 * (ubar[1] * ubar[1] + ubar[2] * ubar[2]) / ubar[0]) <= 0.)
       return SWFD_ERR_PUBAR_NONPOS;
   }
@@ -674,8 +693,10 @@ static int sweep_lim2d(oracle* o) {
   for (int q = 1; q <= o->cfg.swp_num; ++q) {
     const int* oi = (q % 2 == 1) ? o->sI_i : o->sII_i;
     const int* oj = (q % 2 == 1) ? o->sI_j : o->sII_j;
-    pressure_pass2d(o, oi, oj, N, 1, ubar);
-    pressure_pass2d(o, oi, oj, N, 0, ubar);
+    const int check = o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION && (q % 2 == 1);
+    int st = pressure_pass2d(o, oi, oj, N, 1, ubar, check);
+    if (st == SWFD_OK) st = pressure_pass2d(o, oi, oj, N, 0, ubar, check);
+    if (st != SWFD_OK) return st;
     double rho_min = 1e20, p_min = 1e20;
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
@@ -694,7 +715,7 @@ static int sweep_lim2d(oracle* o) {
     }
     if (q == o->cfg.swp_num) {
       o->fail_count++;
-      if (o->problem == SWFD_PROBLEM_SEDOV_2D) return SWFD_ERR_SWEEP_NOCONV;
+      if (o->ex4like) return SWFD_ERR_SWEEP_NOCONV;
     }
   }
   return SWFD_OK;
@@ -941,8 +962,423 @@ static void compute_dt(oracle* o) {
   }
 }
 
+
+/* ------------------------------------------------------------------ */
+/* ex6: Mach 5.09 shock diffraction (ex6_shock_diffraction/main.f90).  */
+/* The reference runs on cut_x x cut_y MPI ranks and its arithmetic    */
+/* depends on that layout, so the oracle keeps one local grid per rank  */
+/* (u(4,-2:nxl+3,-2:nyl+3) with its own ghost layers), exchanges ghosts */
+/* as exchange_x/exchange_y do, gathers the interior for the sweep and  */
+/* scatters it back.  o->u is the assembled global view.               */
+/* ------------------------------------------------------------------ */
+static oracle* ex6_rank_create(const oracle* g, int px, int py) {
+  oracle* r = calloc(1, sizeof(oracle));
+  r->cfg = g->cfg;
+  r->problem = g->problem;
+  r->quad = g->quad;
+  r->ndim = 2;
+  r->nc = 4;
+  r->nx = g->nxl;
+  r->ny = g->nyl;
+  r->LI = r->nx + 6;
+  r->LJ = r->ny + 6;
+  r->gamma = g->gamma;
+  r->gamma1 = g->gamma1;
+  r->eps = g->eps;
+  r->eps2 = g->eps2;
+  r->weno_eps = g->weno_eps;
+  r->weno_eps_q = g->weno_eps_q;
+  r->ex4like = 1;
+  r->px = px;
+  r->py = py;
+  r->total = g->total;
+  r->dx = g->dx;
+  r->dy = g->dy;
+  const size_t n = state_len(r);
+  double** arrs[] = {&r->u, &r->u0, &r->rhs, &r->fp, &r->fn, &r->gp,
+                     &r->gn, &r->fpf, &r->fnf, &r->gpf, &r->gnf};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) *arrs[k] = calloc(n, sizeof(double));
+  r->alpha = calloc((size_t)r->LI * r->LJ, sizeof(double));
+  int mx = (r->nx > r->ny ? r->nx : r->ny) + 3;
+  r->wk_w = calloc(mx, sizeof(double));
+  r->wk_vx = calloc(mx, sizeof(double));
+  r->wk_vy = calloc(mx, sizeof(double));
+  r->wk_h = calloc(mx, sizeof(double));
+  return r;
+}
+
+static void ex6_rank_destroy(oracle* r) {
+  double* arrs[] = {r->u, r->u0, r->rhs, r->fp, r->fn, r->gp, r->gn, r->fpf, r->fnf, r->gpf, r->gnf,
+                    r->alpha, r->wk_w, r->wk_vx, r->wk_vy, r->wk_h};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) free(arrs[k]);
+  free(r);
+}
+
+#define UR(r, a, c, i, j) ((a)[IX((r), (c), (i), (j))])
+#define ALPHA(r, i, j) ((r)->alpha[(size_t)((i) + 2) + (size_t)(r)->LI * (size_t)((j) + 2)])
+
+/* the rank owning global cell (I, J); ghost cells belong to the edge ranks */
+static int ex6_owner_x(const oracle* o, int I) {
+  int px = I <= 0 ? 0 : (I - 1) / o->nxl;
+  return px >= o->cut_x ? o->cut_x - 1 : px;
+}
+static int ex6_owner_y(const oracle* o, int J) {
+  int py = J <= 0 ? 0 : (J - 1) / o->nyl;
+  return py >= o->cut_y ? o->cut_y - 1 : py;
+}
+
+/* global view <- ranks: interior from the owners, ghosts from the edge ranks */
+static void ex6_assemble(oracle* o) {
+  for (int J = -2; J <= o->ny + 3; ++J)
+    for (int I = -2; I <= o->nx + 3; ++I) {
+      int px = ex6_owner_x(o, I), py = ex6_owner_y(o, J);
+      const oracle* r = o->rk[px + o->cut_x * py];
+      int i = I - px * o->nxl, j = J - py * o->nyl;
+      for (int c = 0; c < 4; ++c) o->u[IX(o, c, I, J)] = r->u[IX(r, c, i, j)];
+    }
+}
+
+/* ranks <- global view, every local cell including ghosts */
+static void ex6_distribute(oracle* o) {
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    for (int j = -2; j <= r->ny + 3; ++j)
+      for (int i = -2; i <= r->nx + 3; ++i) {
+        int I = r->px * o->nxl + i, J = r->py * o->nyl + j;
+        for (int c = 0; c < 4; ++c) r->u[IX(r, c, i, j)] = o->u[IX(o, c, I, J)];
+      }
+  }
+  o->ranks_stale = 0;
+}
+
+/* findalpha of one rank (ex6_shock_diffraction/main.f90:662-691): per-cell
+ * alpha over the local cells including ghosts; returns the local max */
+static double ex6_findalpha(oracle* r) {
+  double am = 0.;
+  for (int i = -2; i <= r->nx + 3; ++i)
+    for (int j = -2; j <= r->ny + 3; ++j) {
+      double u1 = UR(r, r->u, 0, i, j), u2 = UR(r, r->u, 1, i, j), u3 = UR(r, r->u, 2, i, j),
+             u4 = UR(r, r->u, 3, i, j);
+      double den = u1, vx, vy;
+      if (den >= r->eps2) {
+        vx = u2 / den;
+        vy = u3 / den;
+      } else {
+        vx = 0.;
+        vy = 0.;
+      }
+      double pres = r->gamma1 * (u4 - 0.5 * den * (vx * vx) - 0.5 * den * (vy * vy));
+      double sound = sqrt(r->gamma * pres / den);
+      double a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+      ALPHA(r, i, j) = a;
+      am = fmax(am, a);
+    }
+  return am;
+}
+
+/* wenofd of one rank (ex6_shock_diffraction/main.f90:170-647): wall mirror
+ * at column total for global rows <= 6*total (:191-201), per-row alpha over
+ * the rank's local row (:218-224), fluxes scaled by it (:411-412); wall
+ * mirror at row 6*total over columns 1..total (:416-430); per-column alpha
+ * (:450-456) and scaling (:641-642) in the y pass */
+static void ex6_wenofd(oracle* r) {
+  const int nx = r->nx, ny = r->ny, total = r->total;
+  for (int j = 0; j <= ny + 1; ++j) {
+    if (r->px == 0 && r->py * ny + j <= total * 6)
+      for (int i = 0; i <= 2; ++i) {
+        for (int c = 0; c < 4; ++c) UR(r, r->u, c, total - i, j) = UR(r, r->u, c, total + 1 + i, j);
+        UR(r, r->u, 1, total - i, j) = -UR(r, r->u, 1, total + 1 + i, j);
+      }
+    for (int i = 0; i <= nx + 2; ++i) {
+      double a[4];
+      for (int c = 0; c < 4; ++c) a[c] = UR(r, r->u, c, i, j);
+      prep_cell(r, 0, a, &r->wk_w[i], &r->wk_vx[i], &r->wk_vy[i], &r->wk_h[i]);
+    }
+    double al = 0.;
+    for (int i = -2; i <= nx + 3; ++i) al = fmax(al, ALPHA(r, i, j));
+    for (int i = -2; i <= nx + 3; ++i) {
+      double a[4], f[4];
+      for (int c = 0; c < 4; ++c) a[c] = UR(r, r->u, c, i, j);
+      fflux2d(r, a, f, 0);
+      for (int c = 0; c < 4; ++c) {
+        UR(r, r->fp, c, i, j) = 0.5 * (a[c] + f[c] / al);
+        UR(r, r->fn, c, i, j) = 0.5 * (a[c] - f[c] / al);
+      }
+    }
+    for (int i = 0; i <= nx + 1; ++i) {
+      double sp[5][4], sn[5][4], op[4], on[4];
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 4; ++c) {
+          sp[ig][c] = UR(r, r->fp, c, i + ig - 2, j);
+          sn[ig][c] = UR(r, r->fn, c, i + ig - 2, j);
+        }
+      interface2d(r, 0, r->wk_w[i], r->wk_w[i + 1], r->wk_vx[i], r->wk_vx[i + 1], r->wk_vy[i],
+                  r->wk_vy[i + 1], r->wk_h[i], r->wk_h[i + 1], (const double(*)[4])sp,
+                  (const double(*)[4])sn, op, on);
+      for (int c = 0; c < 4; ++c) {
+        UR(r, r->fpf, c, i, j) = al * op[c];
+        UR(r, r->fnf, c, i, j) = al * on[c];
+      }
+    }
+  }
+  if (r->px == 0)
+    for (int j = -2; j <= ny + 3; ++j)
+      if (r->py * ny + j == total * 6)
+        for (int i = 0; i <= 2; ++i)
+          for (int k = 1; k <= total; ++k) {
+            for (int c = 0; c < 4; ++c) UR(r, r->u, c, k, j - i) = UR(r, r->u, c, k, j + 1 + i);
+            UR(r, r->u, 2, k, j - i) = -UR(r, r->u, 2, k, j + 1 + i);
+          }
+  for (int i = 0; i <= nx + 1; ++i) {
+    for (int j = 0; j <= ny + 2; ++j) {
+      double a[4];
+      for (int c = 0; c < 4; ++c) a[c] = UR(r, r->u, c, i, j);
+      prep_cell(r, 1, a, &r->wk_w[j], &r->wk_vx[j], &r->wk_vy[j], &r->wk_h[j]);
+    }
+    double al = 0.;
+    for (int j = -2; j <= ny + 3; ++j) al = fmax(al, ALPHA(r, i, j));
+    for (int j = -2; j <= ny + 3; ++j) {
+      double a[4], g[4];
+      for (int c = 0; c < 4; ++c) a[c] = UR(r, r->u, c, i, j);
+      fflux2d(r, a, g, 1);
+      for (int c = 0; c < 4; ++c) {
+        UR(r, r->gp, c, i, j) = 0.5 * (a[c] + g[c] / al);
+        UR(r, r->gn, c, i, j) = 0.5 * (a[c] - g[c] / al);
+      }
+    }
+    for (int j = 0; j <= ny + 1; ++j) {
+      double sp[5][4], sn[5][4], op[4], on[4];
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 4; ++c) {
+          sp[ig][c] = UR(r, r->gp, c, i, j + ig - 2);
+          sn[ig][c] = UR(r, r->gn, c, i, j + ig - 2);
+        }
+      interface2d(r, 1, r->wk_w[j], r->wk_w[j + 1], r->wk_vx[j], r->wk_vx[j + 1], r->wk_vy[j],
+                  r->wk_vy[j + 1], r->wk_h[j], r->wk_h[j + 1], (const double(*)[4])sp,
+                  (const double(*)[4])sn, op, on);
+      for (int c = 0; c < 4; ++c) {
+        UR(r, r->gpf, c, i, j) = al * op[c];
+        UR(r, r->gnf, c, i, j) = al * on[c];
+      }
+    }
+  }
+}
+
+/* exchange_x (:946-1006): ghost columns from the x neighbours (periodic) */
+static void ex6_exchange_x(oracle* o) {
+  const int n = o->cut_x * o->cut_y;
+  double** snap = malloc(n * sizeof(double*));
+  for (int k = 0; k < n; ++k) {
+    snap[k] = malloc(state_len(o->rk[k]) * sizeof(double));
+    memcpy(snap[k], o->rk[k]->u, state_len(o->rk[k]) * sizeof(double));
+  }
+  for (int k = 0; k < n; ++k) {
+    oracle* r = o->rk[k];
+    int left = (r->px + o->cut_x - 1) % o->cut_x + o->cut_x * r->py;
+    int right = (r->px + 1) % o->cut_x + o->cut_x * r->py;
+    const oracle* rl = o->rk[left];
+    const oracle* rr = o->rk[right];
+    for (int j = -2; j <= r->ny + 3; ++j)
+      for (int m = 1; m <= 3; ++m)
+        for (int c = 0; c < 4; ++c) {
+          r->u[IX(r, c, r->nx + m, j)] = snap[right][IX(rr, c, m, j)];
+          r->u[IX(r, c, 1 - m, j)] = snap[left][IX(rl, c, rl->nx + 1 - m, j)];
+        }
+  }
+  for (int k = 0; k < n; ++k) free(snap[k]);
+  free(snap);
+}
+
+/* exchange_y (:1008-1067): ghost rows from the y neighbours (periodic) */
+static void ex6_exchange_y(oracle* o) {
+  const int n = o->cut_x * o->cut_y;
+  double** snap = malloc(n * sizeof(double*));
+  for (int k = 0; k < n; ++k) {
+    snap[k] = malloc(state_len(o->rk[k]) * sizeof(double));
+    memcpy(snap[k], o->rk[k]->u, state_len(o->rk[k]) * sizeof(double));
+  }
+  for (int k = 0; k < n; ++k) {
+    oracle* r = o->rk[k];
+    int down = r->px + o->cut_x * ((r->py + o->cut_y - 1) % o->cut_y);
+    int up = r->px + o->cut_x * ((r->py + 1) % o->cut_y);
+    const oracle* rd = o->rk[down];
+    const oracle* ru = o->rk[up];
+    for (int m = 1; m <= 3; ++m)
+      for (int i = -2; i <= r->nx + 3; ++i)
+        for (int c = 0; c < 4; ++c) {
+          r->u[IX(r, c, i, r->ny + m)] = snap[up][IX(ru, c, i, m)];
+          r->u[IX(r, c, i, 1 - m)] = snap[down][IX(rd, c, i, rd->ny + 1 - m)];
+        }
+  }
+  for (int k = 0; k < n; ++k) free(snap[k]);
+  free(snap);
+}
+
+/* bc (:797-944): exchanges twice, then fixed bottom, fixed right, copied
+ * top, inflow left and the quiescent column i = 1 (the loop index after
+ * `do i = -2, 0`) below row 6*total */
+static void ex6_bc(oracle* o) {
+  ex6_exchange_x(o);
+  ex6_exchange_y(o);
+  ex6_exchange_x(o);
+  ex6_exchange_y(o);
+  const double g = o->gamma, g1 = o->gamma1;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    const int nx = r->nx, ny = r->ny;
+    if (r->py == 0)
+      for (int jj = -2; jj <= 0; ++jj)
+        for (int i = -2; i <= nx + 3; ++i) {
+          UR(r, r->u, 0, i, jj) = g;
+          UR(r, r->u, 1, i, jj) = 0.;
+          UR(r, r->u, 2, i, jj) = 0.;
+          UR(r, r->u, 3, i, jj) = 1. / g1;
+        }
+    if (r->px == o->cut_x - 1)
+      for (int ii = 1; ii <= 3; ++ii)
+        for (int j = -2; j <= ny + 3; ++j) {
+          UR(r, r->u, 0, nx + ii, j) = g;
+          UR(r, r->u, 1, nx + ii, j) = 0.;
+          UR(r, r->u, 2, nx + ii, j) = 0.;
+          UR(r, r->u, 3, nx + ii, j) = 1. / g1;
+        }
+    if (r->py == o->cut_y - 1)
+      for (int ii = 1; ii <= 3; ++ii)
+        for (int i = -2; i <= nx + 3; ++i)
+          for (int c = 0; c < 4; ++c) UR(r, r->u, c, i, ny + ii) = UR(r, r->u, c, i, ny);
+    if (r->px == 0) {
+      for (int ii = -2; ii <= 0; ++ii)
+        for (int j = -2; j <= ny + 3; ++j) {
+          UR(r, r->u, 0, ii, j) = o->dle;
+          UR(r, r->u, 1, ii, j) = o->ule * o->dle;
+          UR(r, r->u, 2, ii, j) = 0.;
+          UR(r, r->u, 3, ii, j) = o->ple / g1 + 0.5 * o->dle * (o->ule * o->ule);
+        }
+      const int i = 1; /* the DO variable after `do i = -2, 0` */
+      for (int j = -2; j <= ny + 3; ++j)
+        if (i + r->px * nx < o->total && j + r->py * ny < 6 * o->total) {
+          UR(r, r->u, 0, i, j) = 1.;
+          UR(r, r->u, 1, i, j) = 0.;
+          UR(r, r->u, 2, i, j) = 0.;
+          UR(r, r->u, 3, i, j) = 1. / g1;
+        }
+    }
+  }
+}
+
+/* checkpositivity over every rank's interior (`<=`, :773-795) */
+static int ex6_checkpositivity(oracle* o) {
+  int postag = 0;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) postag |= checkpositivity2d(o->rk[k]);
+  return postag;
+}
+
+/* gather_to_root / scatter_from_root: the global interior <-> the ranks */
+static void ex6_gather(oracle* o) {
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    const oracle* r = o->rk[k];
+    for (int j = 1; j <= r->ny; ++j)
+      for (int i = 1; i <= r->nx; ++i)
+        for (int c = 0; c < 4; ++c)
+          o->u[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)] = r->u[IX(r, c, i, j)];
+  }
+}
+static void ex6_scatter(oracle* o) {
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    for (int j = 1; j <= r->ny; ++j)
+      for (int i = 1; i <= r->nx; ++i)
+        for (int c = 0; c < 4; ++c)
+          r->u[IX(r, c, i, j)] = o->u[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)];
+  }
+}
+
+/* wenofd + scheme on every rank; returns the global alphamax */
+static double ex6_flux_divergence(oracle* o) {
+  double am = 0.;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) am = fmax(am, ex6_findalpha(o->rk[k]));
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    ex6_wenofd(o->rk[k]);
+    scheme2d(o->rk[k]);
+  }
+  return am;
+}
+
+/* rk (:693-771) */
+static int ex6_step(oracle* o) {
+  if (o->ranks_stale) ex6_distribute(o);
+  const int n = o->cut_x * o->cut_y;
+  for (int stage = 1; stage <= 3; ++stage) {
+    double am = ex6_flux_divergence(o);
+    o->alphamax = am;
+    if (stage == 1) {
+      compute_dt(o);
+      for (int k = 0; k < n; ++k)
+        memcpy(o->rk[k]->u0, o->rk[k]->u, state_len(o->rk[k]) * sizeof(double));
+    }
+    const double dt = o->dt;
+    for (int k = 0; k < n; ++k) {
+      oracle* r = o->rk[k];
+      const size_t len = state_len(r);
+      for (size_t m = 0; m < len; ++m) {
+        double v = r->u[m] + dt * r->rhs[m];
+        if (stage == 1) r->u[m] = v;
+        else if (stage == 2) r->u[m] = rk2(o, r->u0[m], v);
+        else r->u[m] = rk3(o, r->u0[m], v);
+      }
+    }
+    o->postag = ex6_checkpositivity(o);
+    ex6_gather(o);
+    if (o->cfg.use_limiter == 2 && o->postag == 1) {
+      int st = sweep_lim2d(o);
+      o->postag = 0;
+      if (st != SWFD_OK) {
+        ex6_assemble(o);
+        return o->status = st;
+      }
+    }
+    ex6_scatter(o);
+    ex6_bc(o);
+  }
+  o->time = o->time + o->dt;
+  ex6_assemble(o);
+  return SWFD_OK;
+}
+
+/* initdata (:1069-1150): post-shock state for i <= total/2 above row 6*total
+ * on the ranks of column 0, pre-shock state elsewhere, ghosts included */
+static void ex6_init(oracle* o) {
+  const double g = o->gamma, g1 = o->gamma1;
+  const double xm1 = 5.09, ss = xm1;
+  const double dri = g, pri = 1.;
+  const double ach2 = ((0.0 - ss) * (0.0 - ss)) / g / pri * dri;
+  o->ple = pri * (g * ach2 / (g + 1.) * 2. - (g - 1.) / (g + 1.));
+  o->dle = dri * (g + 1.) / 2. * ach2 / ((g - 1.) / 2. * ach2 + 1.);
+  o->ule = (0.0 - ss) / o->dle * dri + ss;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    for (int j = -2; j <= r->ny + 3; ++j)
+      for (int i = -2; i <= r->nx + 3; ++i) {
+        if (r->px == 0 && i <= o->total / 2 && r->py * r->ny + j >= o->total * 6) {
+          UR(r, r->u, 0, i, j) = o->dle;
+          UR(r, r->u, 1, i, j) = o->ule * o->dle;
+          UR(r, r->u, 2, i, j) = 0.;
+          UR(r, r->u, 3, i, j) = o->ple / g1 + 0.5 * o->dle * (o->ule * o->ule);
+        } else {
+          UR(r, r->u, 0, i, j) = dri;
+          UR(r, r->u, 1, i, j) = 0.;
+          UR(r, r->u, 2, i, j) = 0.;
+          UR(r, r->u, 3, i, j) = pri / g1;
+        }
+      }
+  }
+  o->ranks_stale = 0;
+  ex6_assemble(o);
+}
+
 /* rk / rk3 (ex3_vortex_accuracy_2d/main.f90:564-632; ex2_sedov_1d/main.f90:287-328) */
 int oracle_step(oracle* o) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) return ex6_step(o);
   const size_t n = state_len(o);
   double* u = o->u;
   int st;
@@ -1059,6 +1495,9 @@ void oracle_init(oracle* o) {
       bc2d(o);
       break;
     }
+    case SWFD_PROBLEM_SHOCK_DIFFRACTION:
+      ex6_init(o);
+      break;
     case SWFD_PROBLEM_JET_2D: { /* ex5_mach2000_jet/main.f90:744-768 */
       double xleft = 0., xright = 1., yleft = 0., yright = 0.25;
       o->dx = (xright - xleft) / nx;
@@ -1096,6 +1535,17 @@ oracle* oracle_create(const swfd_config* cfg) {
   o->eps2 = 1e-8;
   o->weno_eps = 1e-6;
   o->weno_eps_q = 1e-6f128;
+  o->ex4like = (cfg->problem == SWFD_PROBLEM_SEDOV_2D || cfg->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION);
+  if (cfg->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    /* alpha(k)=lin(k)/(1d-12+beta(k))**2 (ex6_shock_diffraction/weno5.f90:104-106,138-140) */
+    o->weno_eps = 1e-12;
+    o->weno_eps_q = 1e-12f128;
+    o->total = cfg->total;
+    o->cut_x = cfg->cut_x;
+    o->cut_y = cfg->cut_y;
+    o->nxl = cfg->nx / cfg->cut_x;
+    o->nyl = cfg->ny / cfg->cut_y;
+  }
   const size_t n = state_len(o);
   double** arrs[] = {&o->u, &o->u0, &o->rhs, &o->fp, &o->fn, &o->gp,
                      &o->gn, &o->fpf, &o->fnf, &o->gpf, &o->gnf};
@@ -1117,6 +1567,20 @@ oracle* oracle_create(const swfd_config* cfg) {
     sweeping_order(o);
     /* weights(i,j) = 1./(nSteps_x*nSteps_y) (ex3_vortex_accuracy_2d/main.f90:44) */
     o->weight = 1. / ((double)o->nx * (double)o->ny);
+    if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+      /* xlen = xright - xleft, dx = xlen/nx per rank (:1097-1104); rank (0,0)'s
+       * for the time step, every rank's own for its flux differences */
+      o->dx = (13. / o->cut_x * (0 + 1) - 13. / o->cut_x * 0) / o->nxl;
+      o->dy = (11. / o->cut_y * (0 + 1) - 11. / o->cut_y * 0) / o->nyl;
+      o->rk = calloc((size_t)o->cut_x * o->cut_y, sizeof(oracle*));
+      for (int py = 0; py < o->cut_y; ++py)
+        for (int px = 0; px < o->cut_x; ++px) {
+          oracle* r = ex6_rank_create(o, px, py);
+          r->dx = (13. / o->cut_x * (px + 1) - 13. / o->cut_x * px) / o->nxl;
+          r->dy = (11. / o->cut_y * (py + 1) - 11. / o->cut_y * py) / o->nyl;
+          o->rk[px + o->cut_x * py] = r;
+        }
+    }
   } else {
     o->rho_t = calloc(o->nx + 6, sizeof(double));
     /* weights(i) = 1/(nSteps + 6) (ex2_sedov_1d/main.f90:31) */
@@ -1132,12 +1596,19 @@ void oracle_destroy(oracle* o) {
   for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) free(arrs[k]);
   free(o->sI_i); free(o->sI_j); free(o->sII_i); free(o->sII_j);
   free(o->sweep_track); free(o->neg_track); free(o->pos_track);
+  if (o->rk) {
+    for (int k = 0; k < o->cut_x * o->cut_y; ++k) ex6_rank_destroy(o->rk[k]);
+    free(o->rk);
+  }
   free(o);
 }
 
 int64_t oracle_state_len(const oracle* o) { return (int64_t)state_len(o); }
 void oracle_get_state(const oracle* o, double* out) { memcpy(out, o->u, state_len(o) * sizeof(double)); }
-void oracle_set_state(oracle* o, const double* in) { memcpy(o->u, in, state_len(o) * sizeof(double)); }
+void oracle_set_state(oracle* o, const double* in) {
+  memcpy(o->u, in, state_len(o) * sizeof(double));
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) o->ranks_stale = 1;
+}
 double oracle_get_time(const oracle* o) { return o->time; }
 void oracle_set_time(oracle* o, double t) { o->time = t; }
 double oracle_get_dt(const oracle* o) { return o->dt; }
@@ -1148,24 +1619,67 @@ int oracle_get_status(const oracle* o) { return o->status; }
 
 /* findalpha of the current state */
 double oracle_find_alpha(oracle* o) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->ranks_stale) ex6_distribute(o);
+    double am = 0.;
+    for (int k = 0; k < o->cut_x * o->cut_y; ++k) am = fmax(am, ex6_findalpha(o->rk[k]));
+    return o->alphamax = am;
+  }
   if (o->ndim == 1) findalpha1d(o); else findalpha2d(o);
   return o->alphamax;
 }
 
 /* wenofd + scheme of the current state; rhs in the state layout */
 void oracle_flux_divergence(oracle* o, double* rhs) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->ranks_stale) ex6_distribute(o);
+    o->alphamax = ex6_flux_divergence(o);
+    memset(rhs, 0, state_len(o) * sizeof(double));
+    for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+      const oracle* r = o->rk[k];
+      for (int j = 1; j <= r->ny; ++j)
+        for (int i = 1; i <= r->nx; ++i)
+          for (int c = 0; c < 4; ++c)
+            rhs[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)] = r->rhs[IX(r, c, i, j)];
+    }
+    ex6_assemble(o); /* the wall mirrors change the state, as in the reference */
+    return;
+  }
   wenofd_any(o);
   scheme_any(o);
   memcpy(rhs, o->rhs, state_len(o) * sizeof(double));
 }
 
-int oracle_check_positivity(oracle* o) { return check_any(o); }
+int oracle_check_positivity(oracle* o) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->ranks_stale) ex6_distribute(o);
+    return ex6_checkpositivity(o);
+  }
+  return check_any(o);
+}
 
 /* sweep_lim on the current state */
-int oracle_sweep(oracle* o) { return sweep_any(o); }
+int oracle_sweep(oracle* o) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->ranks_stale) ex6_distribute(o);
+    ex6_gather(o);
+    int st = sweep_lim2d(o);
+    ex6_scatter(o);
+    return st;
+  }
+  return sweep_any(o);
+}
 
 /* bc on the current state */
-void oracle_bc(oracle* o) { bc_any(o); }
+void oracle_bc(oracle* o) {
+  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->ranks_stale) ex6_distribute(o);
+    ex6_bc(o);
+    ex6_assemble(o);
+    return;
+  }
+  bc_any(o);
+}
 
 /* stats: out[0..9] in swfd_sweep_stats order */
 void oracle_get_stats(const oracle* o, int64_t* out) {

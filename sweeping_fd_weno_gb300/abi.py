@@ -11,7 +11,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libswfd.so"
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # status codes
 OK = 0
@@ -24,12 +24,14 @@ ERR_OOM = -6
 ERR_TIMEOUT = -7
 ERR_UNSUPPORTED = -8
 ERR_MAX_STEPS = -9
+ERR_SWEEP_CHECK = -10
 
 # problems (one per reference example)
 SEDOV_1D = 2   # ex2_sedov_1d
 VORTEX_2D = 3  # ex3_vortex_accuracy_2d
 SEDOV_2D = 4   # ex4_sedov_2d
 JET_2D = 5     # ex5_mach2000_jet
+SHOCK_DIFFRACTION = 6  # ex6_shock_diffraction
 
 LITERALS_DOUBLE = 0
 LITERALS_QUAD = 1
@@ -59,7 +61,10 @@ class SwfdConfig(C.Structure):
         ("e_background", C.c_double),
         ("e_blast", C.c_double),
         ("sweep_mode", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("total", C.c_int32),
+        ("cut_x", C.c_int32),
+        ("cut_y", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
     def as_dict(self) -> dict:

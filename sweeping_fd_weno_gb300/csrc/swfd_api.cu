@@ -39,6 +39,24 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
   if (c.sweep_mode != SWFD_SWEEP_PARALLEL && c.sweep_mode != SWFD_SWEEP_SEQUENTIAL)
     return bad(SWFD_ERR_INVALID, "unknown sweep_mode");
   if (!(c.gamma > 1.0)) return bad(SWFD_ERR_INVALID, "gamma must be > 1");
+  if (c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    // ex6_shock_diffraction/main.f90:16-18: nx = 13*total/cut_x per rank,
+    // ny = 11*total/cut_y per rank
+    auto pow2 = [](int v) { return v >= 1 && (v & (v - 1)) == 0; };
+    if (!pow2(c.cut_x) || !pow2(c.cut_y))
+      return bad(SWFD_ERR_UNSUPPORTED, "cut_x and cut_y must be powers of two (exact rank widths)");
+    if (c.total < 4) return bad(SWFD_ERR_INVALID, "total must be >= 4");
+    const int nxl = 13 * c.total / c.cut_x, nyl = 11 * c.total / c.cut_y;
+    if (c.nx != c.cut_x * nxl || c.ny != c.cut_y * nyl)
+      return bad(SWFD_ERR_INVALID, "nx, ny must be cut_x*(13*total/cut_x), cut_y*(11*total/cut_y)");
+    // the walls must lie inside single ranks, away from their ghost layers,
+    // so that every rank that touches them sees the same cells
+    // (the y mirror's rows 6*total-2..6*total must also stay out of the rank
+    // below's ghost rows: local row >= 6)
+    const int j0 = 6 * c.total - (6 * c.total - 1) / nyl * nyl;
+    if (c.total > nxl - 6 || j0 < 6 || j0 > nyl - 3 || 6 * c.total >= c.ny)
+      return bad(SWFD_ERR_UNSUPPORTED, "step walls too close to a rank boundary for this rank grid");
+  }
   return SWFD_OK;
 }
 
@@ -74,7 +92,8 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
     }
     case SWFD_PROBLEM_VORTEX_2D:
     case SWFD_PROBLEM_SEDOV_2D:
-    case SWFD_PROBLEM_JET_2D: {
+    case SWFD_PROBLEM_JET_2D:
+    case SWFD_PROBLEM_SHOCK_DIFFRACTION: {
       if (c.ny < 8) {
         err = "ny must be >= 8";
         return SWFD_ERR_INVALID;
@@ -102,6 +121,34 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
         p.roe_reg_ex4 = 1;
         p.alpha_premul = 1;
         p.pos_strict = 1;
+      } else if (c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+        p.cut_x = c.cut_x;
+        p.cut_y = c.cut_y;
+        p.nxl = c.nx / c.cut_x;
+        p.nyl = c.ny / c.cut_y;
+        p.total = c.total;
+        // xlen = 13./cut_x*(px+1) - 13./cut_x*px, dx = xlen/nx (:1097-1104);
+        // the same for every rank when cut_x, cut_y are powers of two
+        p.dx = (13. / c.cut_x * (0 + 1) - 13. / c.cut_x * 0) / p.nxl;
+        p.dy = (11. / c.cut_y * (0 + 1) - 11. / c.cut_y * 0) / p.nyl;
+        p.dt_rule = 4;
+        p.alpha_guarded = 1;
+        p.flux_guard_eps2 = 1;
+        p.roe_reg_ex4 = 1;
+        p.alpha_premul = 1;
+        p.seg_alpha = 1;
+        p.sweep_check = 1;
+        p.weno_eps = 1e-12;  // ex6_shock_diffraction/weno5.f90:104-106,138-140
+        // Mach 5.09 post-shock state (:1113-1129)
+        const double gm = c.gamma, xm1 = 5.09, ss = xm1, dri = gm, pri = 1.;
+        const double ach2 = ((0.0 - ss) * (0.0 - ss)) / gm / pri * dri;
+        const double ple = pri * (gm * ach2 / (gm + 1.) * 2. - (gm - 1.) / (gm + 1.));
+        const double dle = dri * (gm + 1.) / 2. * ach2 / ((gm - 1.) / 2. * ach2 + 1.);
+        const double ule = (0.0 - ss) / dle * dri + ss;
+        p.inflow[0] = dle;
+        p.inflow[1] = ule * dle;
+        p.inflow[2] = 0.;
+        p.inflow[3] = ple / p.gamma1 + 0.5 * dle * (ule * ule);
       } else {
         p.dx = (1. - 0.) / c.nx;  // ex5_mach2000_jet/main.f90:748-754
         p.dy = (0.25 - 0.) / c.ny;
@@ -135,6 +182,21 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   }
   g.pitch = ((g.LI + 31) / 32) * 32;
   g.plane = (int64_t)g.pitch * g.LJ;
+  p.stop_sweep = c.problem == SWFD_PROBLEM_SEDOV_2D || c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
+  if (!p.seg_alpha) {
+    p.cut_x = p.cut_y = 1;
+    p.nxl = g.nx;
+    p.nyl = g.ny;
+  }
+  // split / flux planes: one copy per rank segment (6 more columns per x
+  // segment, 6 more rows per y segment)
+  p.sg = g;
+  if (g.ndim == 2) {
+    p.sg.LI = g.LI + 6 * (p.cut_x - 1);
+    p.sg.LJ = g.LJ + 6 * (p.cut_y - 1);
+    p.sg.pitch = ((p.sg.LI + 31) / 32) * 32;
+    p.sg.plane = (int64_t)p.sg.pitch * p.sg.LJ;
+  }
   return SWFD_OK;
 }
 
@@ -197,6 +259,16 @@ void init_host_state(const Params& p, const swfd_config& cfg, double* u) {
         for (int i = -2; i <= nx + 3; ++i) {
           U(0, i, j) = 0.5;
           U(3, i, j) = 0.4127 / p.gamma1;
+        }
+      break;
+    case SWFD_PROBLEM_SHOCK_DIFFRACTION:  // ex6_shock_diffraction/main.f90:1132-1148
+      // post-shock state for i <= total/2 at or above row 6*total (on the
+      // ranks of column 0), pre-shock state elsewhere; ghosts included, no bc
+      for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          const bool post = i <= p.total / 2 && j >= p.total * 6;
+          for (int c = 0; c < 4; ++c)
+            U(c, i, j) = post ? p.inflow[c] : (c == 0 ? p.gamma : (c == 3 ? 1. / p.gamma1 : 0.));
         }
       break;
   }
@@ -265,6 +337,9 @@ swfd_status check_device_error(swfd_handle* h) {
   CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   h->hsc->error = 0;
+  if (e & ERR_BIT_CHECK)
+    return fail(h, SWFD_ERR_SWEEP_CHECK,
+                "Sweep check failed: total pressure increased after adjustment");
   if (e & ERR_BIT_PUBAR) return fail(h, SWFD_ERR_PUBAR_NONPOS, "P(u_bar) <= 0");
   if (e & ERR_BIT_NOCONV) return fail(h, SWFD_ERR_SWEEP_NOCONV, "SWEEP FAIL: swp_num reached");
   return fail(h, SWFD_ERR_NONFINITE,
@@ -331,7 +406,7 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
   }
   B_OK(b, launch_ubar(p, u, h->dsc, s));
   cudaGraphConditionalHandle hw = b.handle();
-  B_OK(b, launch_sweep_begin(hw, p, h->dsc, p.problem == SWFD_PROBLEM_SEDOV_2D, h->cfg.swp_num, s));
+  B_OK(b, launch_sweep_begin(hw, p, h->dsc, p.stop_sweep, h->cfg.swp_num, s));
   B_OK(b, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
   b.k(2);
   b.cond(s, cudaGraphCondTypeWhile, hw, [&](cudaStream_t sq) {
@@ -349,7 +424,7 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
       b.k(n);
     }
     B_OK(b, launch_exit_count(p, u, h->dsc, sq));
-    B_OK(b, launch_q_end(hw, h->dsc, h->cfg.swp_num, p.problem == SWFD_PROBLEM_SEDOV_2D, sq));
+    B_OK(b, launch_q_end(hw, h->dsc, h->cfg.swp_num, p.stop_sweep, sq));
     b.k(2);
     b.count = saved;
   });
@@ -367,8 +442,11 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
     B_OK(b, launch_dt(p, h->dsc, s));
     b.k(1);
   }
-  B_OK(b, launch_prep(p, in, h->dsc, h->split, h->roe, s));
-  b.k(1);
+  {
+    int nk = 0;
+    B_OK(b, launch_split(p, in, h->dsc, h->split, h->roe, s, &nk));
+    b.k(nk);
+  }
   // external event-record nodes (a plain record on a capturing stream would
   // only be a capture dependency)
   if (events)
@@ -532,6 +610,7 @@ const char* swfd_status_string(swfd_status s) {
     case SWFD_ERR_TIMEOUT: return "device-side wait timed out";
     case SWFD_ERR_UNSUPPORTED: return "unsupported option";
     case SWFD_ERR_MAX_STEPS: return "step limit reached";
+    case SWFD_ERR_SWEEP_CHECK: return "sweep check failed: total pressure increased";
     default: return "unknown status";
   }
 }
@@ -577,6 +656,15 @@ swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
       cfg->time_terminal = 0.001;
       cfg->gamma = 5. / 3.;
       break;
+    case SWFD_PROBLEM_SHOCK_DIFFRACTION:  // ex6_shock_diffraction/main.f90:16-20,695
+      cfg->total = 80;
+      cfg->cut_x = 4;
+      cfg->cut_y = 8;
+      cfg->nx = 4 * (13 * 80 / 4);
+      cfg->ny = 8 * (11 * 80 / 8);
+      cfg->cfl = 0.9;
+      cfg->time_terminal = 2.3;
+      break;
     default:
       return fail(nullptr, SWFD_ERR_INVALID, "unknown problem");
   }
@@ -614,9 +702,20 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   const size_t pb = (size_t)g.plane * sizeof(double);
   for (int k = 0; k < 3; ++k)
     if ((e = cudaMalloc(&h->st[k], g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
-  if ((e = cudaMalloc(&h->split, 4 * g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  // split and flux planes: one copy per rank segment (sg; sg == g except ex6)
+  const size_t sb = (size_t)h->p.sg.plane * sizeof(double);
+  if ((e = cudaMalloc(&h->split, 4 * g.nc * sb)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMalloc(&h->roe, 8 * pb)) != cudaSuccess) return cleanup_fail(e);
-  if ((e = cudaMalloc(&h->flux, 4 * g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMalloc(&h->flux, 4 * g.nc * sb)) != cudaSuccess) return cleanup_fail(e);
+  if (h->p.seg_alpha) {  // per-cell alpha, alpha per rank row and per rank column
+    const size_t n = (size_t)g.plane + (size_t)g.LJ * h->p.cut_x + (size_t)g.LI * h->p.cut_y +
+                     (size_t)12 * (6 * h->p.total + 2);
+    if ((e = cudaMalloc(&h->seg_buf, n * sizeof(double))) != cudaSuccess) return cleanup_fail(e);
+    h->p.alpha_plane = h->seg_buf;
+    h->p.seg_ax = h->seg_buf + g.plane;
+    h->p.seg_ay = h->p.seg_ax + (size_t)g.LJ * h->p.cut_x;
+    h->p.wall_save = h->p.seg_ay + (size_t)g.LI * h->p.cut_y;
+  }
   if ((e = cudaMalloc(&h->rhs_tmp, g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMalloc(&h->dsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMallocHost(&h->hsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
@@ -635,9 +734,9 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   for (int k = 0; k < 3; ++k)
     if ((e = cudaMemsetAsync(h->st[k], 0, g.nc * pb, h->stream)) != cudaSuccess)
       return cleanup_fail(e);
-  if ((e = cudaMemsetAsync(h->split, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->split, 0, 4 * g.nc * sb, h->stream)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMemsetAsync(h->roe, 0, 8 * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
-  if ((e = cudaMemsetAsync(h->flux, 0, 4 * g.nc * pb, h->stream)) != cudaSuccess) return cleanup_fail(e);
+  if ((e = cudaMemsetAsync(h->flux, 0, 4 * g.nc * sb, h->stream)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cleanup_fail(e);
   if (reset_scalars(h) != SWFD_OK) {
     std::string m = h->last_error;
@@ -656,6 +755,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->split);
   cudaFree(h->roe);
   cudaFree(h->flux);
+  cudaFree(h->seg_buf);
   cudaFree(h->rhs_tmp);
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
@@ -699,7 +799,10 @@ swfd_status swfd_init_problem(swfd_handle* h) {
   std::vector<double> u((size_t)host_len(h->p));
   init_host(h, u.data());
   ST(swfd_upload_state(h, u.data()));
-  LAUNCH(h, h->p.g.ndim == 2 ? 1 : 0, launch_bc(h->p, cur_state(h), h->stream));
+  // the reference applies bc after initdata except ex6, whose time loop starts
+  // from initdata directly (ex6_shock_diffraction/main.f90:97-103)
+  if (h->p.g.ndim == 2 && h->p.problem != SWFD_PROBLEM_SHOCK_DIFFRACTION)
+    LAUNCH(h, 1, launch_bc(h->p, cur_state(h), h->stream));
   ST(reset_scalars(h));
   return SWFD_OK;
 }
@@ -777,7 +880,8 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
   const Params& p = h->p;
   double* u = cur_state(h);
   CU(h, launch_alpha(p, u, h->dsc, h->stream));
-  CU(h, launch_prep(p, u, h->dsc, h->split, h->roe, h->stream));
+  int nk = 0;
+  CU(h, launch_split(p, u, h->dsc, h->split, h->roe, h->stream, &nk));
   CU(h, launch_flux(p, h->split, p.g.ndim == 1 ? u : h->roe, h->dsc, h->flux, &h->dsc->flux_work, h->stream));
   CU(h, launch_rhs(p, h->flux, h->dsc, h->rhs_tmp, h->stream));
   const size_t hb = (size_t)host_len(p) * sizeof(double);

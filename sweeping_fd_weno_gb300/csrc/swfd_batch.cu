@@ -77,19 +77,24 @@ swfd_status bfail(swfd_batch* b, swfd_status st, const std::string& m) {
                    std::string(#call) + ": " + cudaGetErrorString(e_));                    \
   } while (0)
 
-size_t plane_bytes(const Params& p) { return a256((size_t)p.g.plane * sizeof(double)); }
+// plane strides of a slot, in elements, rounded so that every plane starts
+// on a 256-byte boundary: the state and Roe planes (g) and the split and
+// flux planes (sg: one copy per rank segment for ex6, else sg == g)
+size_t state_plane_elems(const Params& p) { return a256((size_t)p.g.plane * sizeof(double)) / 8; }
+size_t seg_plane_elems(const Params& p) { return a256((size_t)p.sg.plane * sizeof(double)) / 8; }
 
-// bytes of one bulk plane (split fluxes, Roe averages, interface fluxes):
-// the kernels index every plane with the FP64 state's element stride
-size_t bulk_plane_bytes(const Params& p, int fp32) {
-  return (plane_bytes(p) / sizeof(double)) * (fp32 ? sizeof(float) : sizeof(double));
+size_t seg_alpha_elems(const Params& p) {
+  return p.seg_alpha ? state_plane_elems(p) + (size_t)p.g.LJ * p.cut_x + (size_t)p.g.LI * p.cut_y +
+                           (size_t)12 * (6 * p.total + 2)
+                     : 0;
 }
 
 // device footprint of one instance
 size_t slot_bytes(const Params& p, int fp32) {
-  const size_t pb = plane_bytes(p), tb = bulk_plane_bytes(p, fp32);
+  const size_t pe = state_plane_elems(p), se = seg_plane_elems(p), ts = fp32 ? 4 : 8;
   const int nc = p.g.nc;
-  return 3 * nc * pb + (4 * nc + 8) * tb + a256(4 * nc * tb) + a256(sweep_scratch_bytes(p));
+  return 3 * nc * pe * 8 + a256(4 * nc * se * ts) + a256(8 * pe * ts) + a256(4 * nc * se * ts) +
+         a256(sweep_scratch_bytes(p)) + a256(seg_alpha_elems(p) * 8);
 }
 
 BatchLaunch launch_desc(swfd_batch* b) {
@@ -101,6 +106,7 @@ BatchLaunch launch_desc(swfd_batch* b) {
   L.max_cell = b->max_cell;
   L.fp32 = b->cfg.precision == SWFD_PRECISION_FP32_BULK;
   L.ubar_tree = b->cfg.ubar_mode == SWFD_UBAR_TREE;
+  L.segmented = 1;
   return L;
 }
 
@@ -191,6 +197,7 @@ swfd_status ensure_slot_tracks(swfd_batch* b, int k, int64_t extra) {
 }
 
 swfd_status status_of(int err_bits) {
+  if (err_bits & ERR_BIT_CHECK) return SWFD_ERR_SWEEP_CHECK;
   if (err_bits & ERR_BIT_PUBAR) return SWFD_ERR_PUBAR_NONPOS;
   if (err_bits & ERR_BIT_NOCONV) return SWFD_ERR_SWEEP_NOCONV;
   if (err_bits) return SWFD_ERR_NONFINITE;
@@ -328,36 +335,39 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   BCU(b, cudaMalloc(&sh.tracks, 3 * sh.track_cap * sizeof(int)));
   BCU(b, cudaMemsetAsync(sh.tracks, 0, 3 * sh.track_cap * sizeof(int), b->stream));
   // carve the slot's buffers
-  const size_t pb = plane_bytes(p), tb = bulk_plane_bytes(p, fp32);
+  const size_t pe = state_plane_elems(p), se = seg_plane_elems(p), ts = fp32 ? 4 : 8;
   const int nc = p.g.nc;
   char* cptr = (char*)sh.mem;
   BatchSlot bs{};
   for (int s = 0; s < 3; ++s) {
     bs.st[s] = (double*)cptr;
-    cptr += nc * pb;
+    cptr += nc * pe * 8;
   }
   bs.split = cptr;
-  cptr += 4 * nc * tb;
+  cptr += a256(4 * nc * se * ts);
   bs.roe = cptr;
-  cptr += 8 * tb;
+  cptr += a256(8 * pe * ts);
   bs.flux = cptr;
-  cptr += a256(4 * nc * tb);
+  cptr += a256(4 * nc * se * ts);
   bs.sweep_scratch = cptr;
   cptr += a256(sweep_scratch_bytes(p));
   sh.dsc = b->d_dsc + k;
   bs.dsc = sh.dsc;
-  // planes are pb apart for the FP64 state; the bulk planes use the same
-  // element pitch (plane) in their own type
   bs.p = p;
-  bs.p.g.plane = (int64_t)(pb / sizeof(double));
+  bs.p.g.plane = (int64_t)pe;
+  bs.p.sg.plane = (int64_t)se;
+  if (p.seg_alpha) {
+    bs.p.alpha_plane = (double*)cptr;
+    bs.p.seg_ax = bs.p.alpha_plane + pe;
+    bs.p.seg_ay = bs.p.seg_ax + (size_t)p.g.LJ * p.cut_x;
+    bs.p.wall_save = bs.p.seg_ay + (size_t)p.g.LI * p.cut_y;
+  }
   bs.ncell = (long long)p.g.LI * p.g.LJ;
-  const int64_t nx_int = (int64_t)(p.g.nx + 2) * p.g.ny;
-  const int64_t ny_int = (int64_t)p.g.nx * (p.g.ny + 2);
-  bs.chunks_x = (nx_int + 31) / 32;
-  bs.chunks = bs.chunks_x + (ny_int + 31) / 32;
+  bs.chunks_x = (flux_faces_x(p) + 31) / 32;
+  bs.chunks = bs.chunks_x + (flux_faces_y(p) + 31) / 32;
   bs.use_limiter = c.use_limiter;
   bs.swp_num = c.swp_num;
-  bs.stop_on_fail = c.problem == SWFD_PROBLEM_SEDOV_2D;
+  bs.stop_on_fail = p.stop_sweep;
   bs.active = 0;  // set once the state is in place
   // initial data
   std::vector<double> u((size_t)nc * p.g.LI * p.g.LJ);
@@ -365,7 +375,8 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   BCU(b, cudaMemcpyAsync(b->d_stage, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice,
                          b->stream));
   BCU(b, launch_fortran_to_soa(bs.p, b->d_stage, bs.st[0], b->stream));
-  BCU(b, launch_bc(bs.p, bs.st[0], b->stream));
+  if (p.problem != SWFD_PROBLEM_SHOCK_DIFFRACTION)  // ex6 starts from initdata
+    BCU(b, launch_bc(bs.p, bs.st[0], b->stream));
   DevScalars d{};
   d.tracks = sh.tracks;
   d.track_cap = sh.track_cap;

@@ -59,6 +59,10 @@ __global__ void k_q_begin(Params p, DevScalars* d) {
 // end of sweep iteration q: pre_count, exit test and tracks (:1116-1129)
 __global__ void k_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num, int stop_on_fail) {
   d->pre_count++;
+  if (d->error & ERR_BIT_CHECK) {  // ex6 stopped inside the passes
+    set_cond(h, &d->cond, 0u);
+    return;
+  }
   if (d->bad_count == 0) {
     long long k = d->sweep_count - 1;
     if (k >= 0 && k < d->track_cap) {

@@ -51,7 +51,56 @@ struct Params {
   int jet_jmax = 0;      // y(j) <= 0.05  <=>  j <= jet_jmax
   double jet_in[4] = {0, 0, 0, 0};
   double jet_amb[4] = {0, 0, 0, 0};
+  int stop_sweep = 0;    // P(u_bar) <= 0 and swp_num exhaustion stop the run (ex4, ex6)
+  // Shock diffraction (ex6_shock_diffraction/main.f90).  The reference's
+  // rank grid cut_x x cut_y (ranks of nxl x nyl cells) is part of its
+  // arithmetic: the x pass of row j uses the max alpha over the cells of
+  // its rank's local row (ghosts included), the y pass likewise per local
+  // column, and a flux at a rank boundary is computed by both ranks, each
+  // with its own alpha.  The split and flux planes therefore hold one copy
+  // per rank segment: x-direction copies shifted by 6 columns per segment,
+  // y-direction copies by 6 rows (geometry sg; sg == g when cut_x = cut_y = 1).
+  int seg_alpha = 0;     // LF alpha per rank row / column instead of alphamax
+  int cut_x = 1, cut_y = 1, nxl = 0, nyl = 0;
+  int total = 0;         // step width in cells; the step top is row 6*total
+  int sweep_check = 0;   // pressure-increase check in ordering-I passes
+  double inflow[4] = {0, 0, 0, 0};  // left inflow state (post-shock)
+  Geom sg;               // geometry of the split and flux planes
+  double* alpha_plane = nullptr;    // per-cell alpha (g geometry)
+  double* seg_ax = nullptr;         // alpha of (row j, x segment s): [(j+2)*cut_x + s]
+  double* seg_ay = nullptr;         // alpha of (column i, y segment t): [(i+2)*cut_y + t]
+  // ex6: the x wall mirror runs over each rank's local rows 0..nyl+1 only, so
+  // a rank's outer ghost rows (local -2, -1, nyl+2, nyl+3) keep the
+  // pre-mirror values of the wall columns, and its y pass reads those.  The
+  // mirror saves them here: [((j * 3) + k) * 4 + c], column total - k, row j.
+  double* wall_save = nullptr;
 };
+
+// ex6: does y segment t see cell (i, j) as it was before the x wall mirror?
+__host__ __device__ __forceinline__ bool seg_sees_premirror(const Params& p, int i, int j, int t) {
+  if (i < p.total - 2 || i > p.total || j < 0 || j > 6 * p.total || j > p.g.ny + 1) return false;
+  const int l = j - t * p.nyl;
+  return l == -2 || l == -1 || l == p.nyl + 2 || l == p.nyl + 3;
+}
+
+// offsets of the segment copies in the split / flux planes
+__host__ __device__ __forceinline__ int64_t seg_x_off(const Params& p, int i, int j, int s) {
+  return (int64_t)(i + 2 + 6 * s) + (int64_t)p.sg.pitch * (int64_t)(j + 2);
+}
+__host__ __device__ __forceinline__ int64_t seg_y_off(const Params& p, int i, int j, int t) {
+  return (int64_t)(i + 2) + (int64_t)p.sg.pitch * (int64_t)(j + 2 + 6 * t);
+}
+
+// interfaces of one stage: x faces of rows 1..ny, per rank segment its
+// local faces 0..nxl+1 (without segments: 0..nx+1); y faces of columns
+// 1..nx, per segment its local faces 0..nyl+1
+__host__ __device__ __forceinline__ int64_t flux_faces_x(const Params& p) {
+  return (int64_t)p.cut_x * (p.nxl + 2) * p.g.ny;
+}
+__host__ __device__ __forceinline__ int64_t flux_faces_y(const Params& p) {
+  return (int64_t)p.g.nx * p.cut_y * (p.nyl + 2);
+}
+
 
 // Device scalars of one handle, in one small allocation.  The sweep
 // statistics and the per-sweep tracks live here so that a whole step (and a
@@ -60,7 +109,8 @@ enum : int {
   ERR_BIT_ALPHA = 1,     // alphamax not finite or not positive
   ERR_BIT_DT = 2,        // dt not finite
   ERR_BIT_PUBAR = 4,     // P(u_bar) <= 0 (ex4 stop)
-  ERR_BIT_NOCONV = 8     // sweep reached swp_num (ex4 stop)
+  ERR_BIT_NOCONV = 8,    // sweep reached swp_num (ex4 stop)
+  ERR_BIT_CHECK = 16     // nodal adjustment raised the total pressure (ex6 stop)
 };
 
 struct DevScalars {
@@ -136,6 +186,7 @@ struct BatchLaunch {
   long long max_cell;       // largest slot (LI*LJ)
   int fp32;
   int ubar_tree;
+  int segmented;            // slots may hold rank-segmented problems (ex6)
 };
 
 }  // namespace swfd
@@ -152,6 +203,7 @@ struct swfd_handle {
   double* split = nullptr;  // fp, fn (x) and gp, gn (y): 4*nc planes
   double* roe = nullptr;    // w, vx, vy, h for x (4 planes) and y (4 planes)
   double* flux = nullptr;   // fp_flux, fn_flux, gp_flux, gn_flux: 4*nc planes
+  double* seg_buf = nullptr;  // ex6: per-cell alpha and alpha per rank row / column
   double* rhs_tmp = nullptr;  // nc planes (flux_divergence output)
   void* sweep_scratch = nullptr;  // flag bits, flagged list, chain results
   swfd::DevScalars* dsc = nullptr;   // device scalars
@@ -195,7 +247,9 @@ cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 // split, roe and flux planes hold doubles (FP64) or floats (FP32 bulk)
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
-                        void* roe, cudaStream_t s);
+                        void* roe, cudaStream_t s, int which = 3);
+cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void* split, void* roe,
+                         cudaStream_t s, int* nk);
 // work: one device int of scratch (the chunk counter of the 2D kernel)
 cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
                         const DevScalars* dsc, void* flux, int* work, cudaStream_t s);

@@ -20,6 +20,29 @@ __device__ __forceinline__ void bc2d_cell(const Params& p, double* __restrict__ 
   if (t >= ncell) return;
   int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
   bool gi = (i < 1 || i > nx), gj = (j < 1 || j > ny);
+  if (p.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    // ex6_shock_diffraction/main.f90:895-940 in its order: fixed bottom rows,
+    // fixed right columns, top rows copied from row ny, inflow left columns,
+    // then the quiescent column i = 1 (the DO variable after `do i = -2, 0`)
+    // below row 6*total.  The rank exchanges before them only fill ghosts
+    // that these overwrite, or interior cells of the single grid.
+    const double gm = p.gamma, g1 = p.gamma1;
+    double w[4] = {gm, 0., 0., 1. / g1};
+    if (i == 1 && j < 6 * p.total) {
+      w[0] = 1.;
+    } else if (i <= 0) {
+      for (int c = 0; c < 4; ++c) w[c] = p.inflow[c];
+    } else if (i > nx || j <= 0) {
+      // fixed state
+    } else if (j > ny) {
+      for (int c = 0; c < 4; ++c) w[c] = u[c * g.plane + g.at(i, ny)];
+    } else {
+      return;
+    }
+    const int64_t o = g.at(i, j);
+    for (int c = 0; c < 4; ++c) u[c * g.plane + o] = w[c];
+    return;
+  }
   if (!gi && !gj) return;
   double v[4];
   int si = i, sj = j;
@@ -129,8 +152,17 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
   return a;
 }
 
+// ex6 keeps every cell's alpha for the per-rank-row and per-rank-column maxima
+__device__ __forceinline__ void alpha_store(const Params& p, int64_t t, double a) {
+  const Geom& g = p.g;
+  if (!p.alpha_plane || t >= (int64_t)g.LI * g.LJ) return;
+  p.alpha_plane[g.at((int)(t % g.LI) - 2, (int)(t / g.LI) - 2)] = a;
+}
+
 __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
-  double a = alpha_cell(p, u, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double a = alpha_cell(p, u, t);
+  alpha_store(p, t, a);
   a = block_max(a);
   if (threadIdx.x == 0) atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
 }
@@ -148,6 +180,74 @@ cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cuda
   k_alpha<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc);
   k_alpha_final<<<1, 1, 0, s>>>(dsc);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// ex6: the Lax-Friedrichs alpha of each rank row (x pass) and rank column
+// (y pass): the max of the per-cell alpha over the rank's local cells,
+// ghosts included, starting from 0 (ex6_shock_diffraction/main.f90:218-221,
+// 450-453).  One thread per (row, x segment) and per (column, y segment).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void seg_alpha_item(const Params& p, int64_t t) {
+  const Geom& g = p.g;
+  const int64_t nrow = (int64_t)g.LJ * p.cut_x;
+  if (t < nrow) {
+    const int j = (int)(t / p.cut_x) - 2, sx = (int)(t % p.cut_x);
+    const int i0 = sx * p.nxl - 2, i1 = sx * p.nxl + p.nxl + 3;
+    double a = 0.;
+    for (int i = i0; i <= i1; ++i) a = fmax(a, p.alpha_plane[g.at(i, j)]);
+    p.seg_ax[t] = a;
+    return;
+  }
+  t -= nrow;
+  if (t >= (int64_t)g.LI * p.cut_y) return;
+  const int i = (int)(t / p.cut_y) - 2, sy = (int)(t % p.cut_y);
+  const int j0 = sy * p.nyl - 2, j1 = sy * p.nyl + p.nyl + 3;
+  double a = 0.;
+  for (int j = j0; j <= j1; ++j) a = fmax(a, p.alpha_plane[g.at(i, j)]);
+  p.seg_ay[t] = a;
+}
+
+__global__ void k_seg_alpha(Params p) {
+  seg_alpha_item(p, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__host__ __device__ __forceinline__ int64_t seg_alpha_items(const Params& p) {
+  return (int64_t)p.g.LJ * p.cut_x + (int64_t)p.g.LI * p.cut_y;
+}
+
+// ex6 wall mirrors.  x: columns total, total-1, total-2 of rows 0..6*total
+// take columns total+1..total+3 with m_x negated (:191-201); y: rows
+// 6*total, -1, -2 of columns 1..total take rows 6*total+1..+3 with m_y
+// negated (:416-430).  Targets and sources never overlap.
+__device__ __forceinline__ void wall_x_item(const Params& p, double* __restrict__ u, int t) {
+  const Geom& g = p.g;
+  const int rows = min(6 * p.total, g.ny + 1) + 1;  // rows 0..min(6*total, ny+1)
+  if (t >= rows * 3) return;
+  const int j = t / 3, k = t % 3;
+  const int64_t dst = g.at(p.total - k, j), src = g.at(p.total + 1 + k, j);
+  for (int c = 0; c < 4; ++c) {
+    p.wall_save[(int64_t)t * 4 + c] = u[c * g.plane + dst];
+    const double v = u[c * g.plane + src];
+    u[c * g.plane + dst] = (c == 1) ? -v : v;
+  }
+}
+__device__ __forceinline__ void wall_y_item(const Params& p, double* __restrict__ u, int t) {
+  const Geom& g = p.g;
+  if (t >= p.total * 3) return;
+  const int i = t % p.total + 1, k = t / p.total;
+  const int r = 6 * p.total;
+  const int64_t dst = g.at(i, r - k), src = g.at(i, r + 1 + k);
+  for (int c = 0; c < 4; ++c) {
+    const double v = u[c * g.plane + src];
+    u[c * g.plane + dst] = (c == 2) ? -v : v;
+  }
+}
+__global__ void k_wall_x(Params p, double* __restrict__ u) {
+  wall_x_item(p, u, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_wall_y(Params p, double* __restrict__ u) {
+  wall_y_item(p, u, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -200,10 +300,14 @@ __device__ __forceinline__ double sqrt_abs<double>(double v) { return sqrt(fabs(
 template <>
 __device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf((float)v)); }
 
+// which: 1 = x pass (fp, fn and the x Roe planes), 2 = y pass (gp, gn and,
+// with the ex4 regularisers, the y Roe planes), 3 = both.  With rank
+// segments (ex6) a cell near a rank boundary is split once per segment whose
+// local range holds it, with that segment's alpha.
 template <class T>
 __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __restrict__ u,
                                             double amd, T* __restrict__ split, T* __restrict__ roe,
-                                            int64_t t) {
+                                            int64_t t, int which = 3) {
   const Geom& g = p.g;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
@@ -223,34 +327,84 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   double f1 = rho * (vx * vx) + pres, f3 = (e + pres) * vx;
   double g2 = rho * (vy * vy) + pres, g3 = (e + pres) * vy;
   // fp = 0.5*(u + f/alpha), fn = 0.5*(u - f/alpha); f/alpha shared by both
-  const T am = T(amd), h = T(0.5);
+  const T h = T(0.5);
   const T tr = T(rho), tmx = T(mx), tmy = T(my), te = T(e);
-  T q;
-  q = T(mx) / am;  split[0 * P + o] = h * (tr + q);   split[4 * P + o] = h * (tr - q);
-  q = T(f1) / am;  split[1 * P + o] = h * (tmx + q);  split[5 * P + o] = h * (tmx - q);
-  T qxy = T(fxy) / am;
-  split[2 * P + o] = h * (tmy + qxy); split[6 * P + o] = h * (tmy - qxy);
-  q = T(f3) / am;  split[3 * P + o] = h * (te + q);   split[7 * P + o] = h * (te - q);
-  q = T(my) / am;  split[8 * P + o] = h * (tr + q);   split[12 * P + o] = h * (tr - q);
-  split[9 * P + o] = h * (tmx + qxy); split[13 * P + o] = h * (tmx - qxy);
-  q = T(g2) / am;  split[10 * P + o] = h * (tmy + q); split[14 * P + o] = h * (tmy - q);
-  q = T(g3) / am;  split[11 * P + o] = h * (te + q);  split[15 * P + o] = h * (te - q);
-  // Roe preparation (x pass; the y pass is the same except in ex4)
-  double t0 = 1. / rho;
-  double vex = mx * t0, vey = my * t0;
-  double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
-  T w = sqrt_abs<T>(rho);
-  roe[0 * P + o] = w;
-  roe[1 * P + o] = T(vex);
-  roe[2 * P + o] = T(vey);
-  roe[3 * P + o] = T((pre + e) * t0);
-  if (p.roe_reg_ex4) {
+  const int64_t S = p.sg.plane;
+  if (!p.seg_alpha) {
+    const T am = T(amd);
+    T q;
+    q = T(mx) / am;  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
+    q = T(f1) / am;  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
+    T qxy = T(fxy) / am;
+    split[2 * S + o] = h * (tmy + qxy); split[6 * S + o] = h * (tmy - qxy);
+    q = T(f3) / am;  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
+    q = T(my) / am;  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
+    split[9 * S + o] = h * (tmx + qxy); split[13 * S + o] = h * (tmx - qxy);
+    q = T(g2) / am;  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
+    q = T(g3) / am;  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
+  } else {
+    if (which & 1) {
+      // x segments whose local columns s*nxl-2 .. s*nxl+nxl+3 hold column i
+      const int sh = min(p.cut_x - 1, (i + 2) / p.nxl);
+      const int sl = i > 3 ? max(0, (i - 3 + p.nxl - 1) / p.nxl - 1) : 0;
+      for (int sx = sl; sx <= sh; ++sx) {
+        const T am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
+        const int64_t os = seg_x_off(p, i, j, sx);
+        T q;
+        q = T(mx) / am;  split[0 * S + os] = h * (tr + q);  split[4 * S + os] = h * (tr - q);
+        q = T(f1) / am;  split[1 * S + os] = h * (tmx + q); split[5 * S + os] = h * (tmx - q);
+        q = T(fxy) / am; split[2 * S + os] = h * (tmy + q); split[6 * S + os] = h * (tmy - q);
+        q = T(f3) / am;  split[3 * S + os] = h * (te + q);  split[7 * S + os] = h * (te - q);
+      }
+    }
+    if (which & 2) {
+      const int th = min(p.cut_y - 1, (j + 2) / p.nyl);
+      const int tl = j > 3 ? max(0, (j - 3 + p.nyl - 1) / p.nyl - 1) : 0;
+      for (int sy = tl; sy <= th; ++sy) {
+        const T am = T(p.seg_ay[(int64_t)(i + 2) * p.cut_y + sy]);
+        const int64_t os = seg_y_off(p, i, j, sy);
+        double r2 = rho, m2 = mx, n2 = my, e2 = e, fxy2 = fxy, g22 = g2, g32 = g3;
+        if (seg_sees_premirror(p, i, j, sy)) {  // this rank's ghost copy, pre-mirror
+          const double* w = p.wall_save + ((int64_t)j * 3 + (p.total - i)) * 4;
+          r2 = w[0];
+          m2 = w[1];
+          n2 = w[2];
+          e2 = w[3];
+          double ux = m2 / r2, uy = n2 / r2;
+          if (p.flux_guard_eps2 ? (r2 < p.eps2) : (r2 < 1e-8)) {
+            ux = 0.;
+            uy = 0.;
+          }
+          const double pr = g1 * (e2 - 0.5 * r2 * (ux * ux) - 0.5 * r2 * (uy * uy));
+          fxy2 = r2 * ux * uy;
+          g22 = r2 * (uy * uy) + pr;
+          g32 = (e2 + pr) * uy;
+        }
+        const T tr2 = T(r2), tm2 = T(m2), tn2 = T(n2), te2 = T(e2);
+        T q;
+        q = T(n2) / am;   split[8 * S + os] = h * (tr2 + q);  split[12 * S + os] = h * (tr2 - q);
+        q = T(fxy2) / am; split[9 * S + os] = h * (tm2 + q);  split[13 * S + os] = h * (tm2 - q);
+        q = T(g22) / am;  split[10 * S + os] = h * (tn2 + q); split[14 * S + os] = h * (tn2 - q);
+        q = T(g32) / am;  split[11 * S + os] = h * (te2 + q); split[15 * S + os] = h * (te2 - q);
+      }
+    }
+  }
+  // Roe preparation (x pass; the y pass is the same except in ex4 and ex6)
+  if (which & 1) {
+    double t0 = 1. / rho;
+    double vex = mx * t0, vey = my * t0;
+    double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+    roe[0 * P + o] = sqrt_abs<T>(rho);
+    roe[1 * P + o] = T(vex);
+    roe[2 * P + o] = T(vey);
+    roe[3 * P + o] = T((pre + e) * t0);
+  }
+  if (p.roe_reg_ex4 && (which & 2)) {
     // ex4_sedov_2d/main.f90:426
-    t0 = 1. / (rho + 1e-15);
-    vex = mx * t0;
-    vey = my * t0;
-    pre = g1 * (e - 0.5 * (mx * vex + my * vey));
-    roe[4 * P + o] = w;
+    double t0 = 1. / (rho + 1e-15);
+    double vex = mx * t0, vey = my * t0;
+    double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+    roe[4 * P + o] = sqrt_abs<T>(rho);
     roe[5 * P + o] = T(vex);
     roe[6 * P + o] = T(vey);
     roe[7 * P + o] = T((pre + e) * t0);
@@ -259,8 +413,9 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
 
 template <class T>
 __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalars* dsc,
-                         T* __restrict__ split, T* __restrict__ roe) {
-  prep2d_cell<T>(p, u, dsc->alphamax, split, roe, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+                         T* __restrict__ split, T* __restrict__ roe, int which) {
+  prep2d_cell<T>(p, u, dsc->alphamax, split, roe, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                 which);
 }
 
 template <class T>
@@ -288,7 +443,7 @@ __global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalar
 }
 
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
-                        void* roe, cudaStream_t s) {
+                        void* roe, cudaStream_t s, int which) {
   const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (p.g.ndim == 1) {
     const int gb = (p.g.LI + SWFD_BLOCK - 1) / SWFD_BLOCK;
@@ -297,10 +452,30 @@ cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc,
   } else {
     int64_t n = (int64_t)p.g.LI * p.g.LJ;
     const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
-    if (f32) k_prep2d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split, (float*)roe);
-    else k_prep2d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split, (double*)roe);
+    if (f32) k_prep2d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split, (float*)roe, which);
+    else k_prep2d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split, (double*)roe, which);
   }
   return cudaGetLastError();
+}
+
+// the work of wenofd before the interface fluxes: [ex6: alpha per rank row
+// and column, x wall mirror] LF splitting + Roe preparation [ex6: y wall
+// mirror, then the y pass's splitting]; *nk += kernels launched
+cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void* split, void* roe,
+                         cudaStream_t s, int* nk) {
+  if (p.problem != SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    *nk += 1;
+    return launch_prep(p, u, dsc, split, roe, s, 3);
+  }
+  const int64_t ns = seg_alpha_items(p);
+  k_seg_alpha<<<(unsigned)((ns + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p);
+  const int nwx = (min(6 * p.total, p.g.ny + 1) + 1) * 3, nwy = p.total * 3;
+  k_wall_x<<<(nwx + 127) / 128, 128, 0, s>>>(p, u);
+  cudaError_t e = launch_prep(p, u, dsc, split, roe, s, 1);
+  if (e != cudaSuccess) return e;
+  k_wall_y<<<(nwy + 127) / 128, 128, 0, s>>>(p, u);
+  *nk += 5;
+  return launch_prep(p, u, dsc, split, roe, s, 2);
 }
 
 // ---------------------------------------------------------------------------
@@ -413,65 +588,79 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
 // resident blocks per SM: the FP64 pipe saturates with 3 (168 registers);
 // the FP32 pipe needs more warps in flight
 #define SWFD_FLUX_MINB(T) (sizeof(T) == 8 ? 3 : 4)
-// the 32 interfaces of chunk c (x chunks first, then y chunks)
-template <class T>
+// the 32 interfaces of chunk c (x chunks first, then y chunks).  SEG: the
+// problem may have rank segments (ex6); without them the face index maps
+// directly to the cell offset.
+template <class T, bool SEG>
 __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict__ split,
                                            const T* __restrict__ roe, T am, T* __restrict__ flux,
                                            int64_t c, int64_t chunks_x, int lane) {
   const Geom& g = p.g;
-  const int64_t P = g.plane, pit = g.pitch;
-  const int lx = g.nx + 2;
-  const int64_t nx_int = (int64_t)lx * g.ny;
-  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);
+  const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
   const T g1 = T(p.gamma1), weps = T(p.weno_eps);
   {
     T op[4], on[4];
     if (c < chunks_x) {
       int64_t t = (int64_t)c * 32 + lane;
-      if (t >= nx_int) return;
-      const int i = (int)(t % lx), j = (int)(t / lx) + 1;
-      const int64_t o = g.at(i, j);
+      if (t >= flux_faces_x(p)) return;
+      const int lsx = p.nxl + 2, lx = p.cut_x * lsx;
+      const int r = (int)(t % lx), j = (int)(t / lx) + 1;
+      const int sx = SEG ? r / lsx : 0, i = SEG ? sx * p.nxl + r % lsx : r;
+      const int64_t o = g.at(i, j), os = SEG ? seg_x_off(p, i, j, sx) : o;
+      if (SEG && p.seg_alpha) am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
       Eigen2D<T> E;
       roe_eigen2d<T>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
                      ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
                      ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
-      interface_flux<0>(E, split + o - 2, split + 4 * P + o - 2, P, 1, weps, op, on);
+      interface_flux<0>(E, split + os - 2, split + 4 * S + os - 2, S, 1, weps, op, on);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        flux[k * P + o] = p.alpha_premul ? am * op[k] : op[k];
-        flux[(4 + k) * P + o] = p.alpha_premul ? am * on[k] : on[k];
+        flux[k * S + os] = p.alpha_premul ? am * op[k] : op[k];
+        flux[(4 + k) * S + os] = p.alpha_premul ? am * on[k] : on[k];
       }
     } else {
       int64_t t = (int64_t)(c - chunks_x) * 32 + lane;
-      if (t >= ny_int) return;
-      const int i = (int)(t % g.nx) + 1, j = (int)(t / g.nx);
-      const int64_t o = g.at(i, j);
-      const T* r = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+      if (t >= flux_faces_y(p)) return;
+      const int lsy = p.nyl + 2;
+      const int i = (int)(t % g.nx) + 1, r = (int)(t / g.nx);
+      const int sy = SEG ? r / lsy : 0, j = SEG ? sy * p.nyl + r % lsy : r;
+      const int64_t o = g.at(i, j), os = SEG ? seg_y_off(p, i, j, sy) : o;
+      if (SEG && p.seg_alpha) am = T(p.seg_ay[(int64_t)(i + 2) * p.cut_y + sy]);
+      const T* rr = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+      T wr = ldt(rr + o + pit), vxr = ldt(rr + P + o + pit), vyr = ldt(rr + 2 * P + o + pit),
+        hr = ldt(rr + 3 * P + o + pit);
+      if (SEG && seg_sees_premirror(p, i, j + 1, sy)) {
+        // the ex6 rank's ghost row j+1 (local nyl+2), pre-mirror, with the
+        // y pass's preparation (ex4_sedov_2d/main.f90:426)
+        const double* w = p.wall_save + ((int64_t)(j + 1) * 3 + (p.total - i)) * 4;
+        const double t0 = 1. / (w[0] + 1e-15);
+        const double vex = w[1] * t0, vey = w[2] * t0;
+        const double pre = p.gamma1 * (w[3] - 0.5 * (w[1] * vex + w[2] * vey));
+        wr = sqrt_abs<T>(w[0]);
+        vxr = T(vex);
+        vyr = T(vey);
+        hr = T((pre + w[3]) * t0);
+      }
       Eigen2D<T> E;
-      roe_eigen2d<T>(g1, 1, ldt(r + o), ldt(r + o + pit), ldt(r + P + o), ldt(r + P + o + pit),
-                     ldt(r + 2 * P + o), ldt(r + 2 * P + o + pit), ldt(r + 3 * P + o),
-                     ldt(r + 3 * P + o + pit), E);
-      interface_flux<1>(E, split + 8 * P + o - 2 * pit, split + 12 * P + o - 2 * pit, P, pit,
+      roe_eigen2d<T>(g1, 1, ldt(rr + o), wr, ldt(rr + P + o), vxr, ldt(rr + 2 * P + o), vyr,
+                     ldt(rr + 3 * P + o), hr, E);
+      interface_flux<1>(E, split + 8 * S + os - 2 * spit, split + 12 * S + os - 2 * spit, S, spit,
                         weps, op, on);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        flux[(8 + k) * P + o] = p.alpha_premul ? am * op[k] : op[k];
-        flux[(12 + k) * P + o] = p.alpha_premul ? am * on[k] : on[k];
+        flux[(8 + k) * S + os] = p.alpha_premul ? am * op[k] : op[k];
+        flux[(12 + k) * S + os] = p.alpha_premul ? am * on[k] : on[k];
       }
     }
   }
 }
 
-template <class T>
+template <class T, bool SEG>
 __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
               const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
-  const Geom& g = p.g;
-  const int lx = g.nx + 2;                       // x interfaces per row (0..nx+1)
-  const int64_t nx_int = (int64_t)lx * g.ny;     // rows 1..ny
-  const int64_t ny_int = (int64_t)g.nx * (g.ny + 2);  // columns 1..nx, rows 0..ny+1
-  const int64_t chunks_x = (nx_int + 31) / 32;
-  const int64_t chunks = chunks_x + (ny_int + 31) / 32;
+  const int64_t chunks_x = (flux_faces_x(p) + 31) / 32;
+  const int64_t chunks = chunks_x + (flux_faces_y(p) + 31) / 32;
   const int lane = threadIdx.x & 31;
   const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
   for (;;) {
@@ -479,7 +668,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
-    flux_chunk<T>(p, split, roe, am, flux, c, chunks_x, lane);
+    flux_chunk<T, SEG>(p, split, roe, am, flux, c, chunks_x, lane);
   }
 }
 
@@ -490,7 +679,7 @@ static int flux_grid() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T>, SWFD_FLUX_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T, false>, SWFD_FLUX_BLOCK, 0);
     grid = sms * (per > 0 ? per : 1);
   }
   return grid;
@@ -512,11 +701,17 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
   }
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  if (f32)
-    k_flux_xy<float><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
+  if (f32 && p.seg_alpha)
+    k_flux_xy<float, true><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
         p, (const float*)split, (const float*)roe, dsc, (float*)flux, work);
+  else if (f32)
+    k_flux_xy<float, false><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
+        p, (const float*)split, (const float*)roe, dsc, (float*)flux, work);
+  else if (p.seg_alpha)
+    k_flux_xy<double, true><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
+        p, (const double*)split, (const double*)roe, dsc, (double*)flux, work);
   else
-    k_flux_xy<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
+    k_flux_xy<double, false><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
         p, (const double*)split, (const double*)roe, dsc, (double*)flux, work);
   return cudaGetLastError();
 }
@@ -530,16 +725,18 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
 // The flux difference is formed in T; the RK combination accumulates into the
 // FP64 state in both precisions.
 // ---------------------------------------------------------------------------
+// ox, oy: the cell's offsets in the x and y flux planes (its own rank
+// segment's copy; the cell offset itself without segments)
 template <class T>
-__device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, int c, int64_t o,
-                                   double amd) {
-  const int64_t P = p.g.plane, pit = p.g.pitch;
-  const T* fpf = flux + c * P;
-  const T* fnf = flux + (4 + c) * P;
-  const T* gpf = flux + (8 + c) * P;
-  const T* gnf = flux + (12 + c) * P;
-  T A = (ldt(fpf + o) - ldt(fnf + o + 1)) - (ldt(fpf + o - 1) - ldt(fnf + o));
-  T B = (ldt(gpf + o) - ldt(gnf + o + pit)) - (ldt(gpf + o - pit) - ldt(gnf + o));
+__device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, int c, int64_t ox,
+                                   int64_t oy, double amd) {
+  const int64_t S = p.sg.plane, pit = p.sg.pitch;
+  const T* fpf = flux + c * S;
+  const T* fnf = flux + (4 + c) * S;
+  const T* gpf = flux + (8 + c) * S;
+  const T* gnf = flux + (12 + c) * S;
+  T A = (ldt(fpf + ox) - ldt(fnf + ox + 1)) - (ldt(fpf + ox - 1) - ldt(fnf + ox));
+  T B = (ldt(gpf + oy) - ldt(gnf + oy + pit)) - (ldt(gpf + oy - pit) - ldt(gnf + oy));
   const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
   if (p.alpha_premul) return -A / dx - B / dy;  // ex4_sedov_2d/main.f90:644-645
   return -(am * A) / dx - (am * B) / dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
@@ -560,6 +757,14 @@ __device__ __forceinline__ T rhs1d(const Params& p, const T* __restrict__ flux, 
 
 __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
 
+// flux difference of interior cell (i, j) of a 2D problem
+template <class T>
+__device__ __forceinline__ T rhs2d_cell(const Params& p, const T* __restrict__ flux, int c, int i,
+                                        int j, double amd) {
+  const int sx = p.seg_alpha ? (i - 1) / p.nxl : 0, sy = p.seg_alpha ? (j - 1) / p.nyl : 0;
+  return rhs2d<T>(p, flux, c, seg_x_off(p, i, j, sx), seg_y_off(p, i, j, sy), amd);
+}
+
 // u0 may alias out (stage 3 writes the step-start buffer); each element of
 // u0 is read only by the thread that then writes it.
 template <class T>
@@ -577,7 +782,8 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
     for (int c = 0; c < g.nc; ++c) {
       double r = 0.0;
       if (interior)
-        r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am) : rhs2d<T>(p, flux, c, o, am));
+        r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am)
+                                   : rhs2d_cell<T>(p, flux, c, i, j, am));
       double v = ld(u + c * P + o) + dt * r;
       if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
       else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
@@ -634,7 +840,7 @@ __global__ void k_rhs(Params p, const T* __restrict__ flux, const DevScalars* ds
     double r = 0.0;
     if (interior)
       r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, dsc->alphamax)
-                                 : rhs2d<T>(p, flux, c, o, dsc->alphamax));
+                                 : rhs2d_cell<T>(p, flux, c, i, j, dsc->alphamax));
     rhs[c * P + o] = r;
   }
 }
@@ -757,8 +963,11 @@ __global__ void kb_alpha(const BatchSlot* __restrict__ tab, int in) {
   if (!sl.active) return;
   double a = 0.0;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
-       t += (int64_t)gridDim.x * blockDim.x)
-    a = fmax(a, alpha_cell(sl.p, sl.st[in], t));
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double at = alpha_cell(sl.p, sl.st[in], t);
+    alpha_store(sl.p, t, at);
+    a = fmax(a, at);
+  }
   a = block_max(a);
   if (threadIdx.x == 0)
     atomicMax(&sl.dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
@@ -772,13 +981,36 @@ __global__ void kb_alpha_final(const BatchSlot* __restrict__ tab, int n, int sta
 }
 
 template <class T>
-__global__ void kb_prep(const BatchSlot* __restrict__ tab, int in) {
+// pass 1: the x part of slots with rank segments, everything of the others;
+// pass 2: the y part of slots with rank segments (after their y wall mirror)
+__global__ void kb_prep(const BatchSlot* __restrict__ tab, int in, int pass) {
   const BatchSlot& sl = tab[blockIdx.y];
   if (!sl.active) return;
+  const int which = sl.p.seg_alpha ? pass : (pass == 1 ? 3 : 0);
+  if (!which) return;
   const double am = sl.dsc->alphamax;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
        t += (int64_t)gridDim.x * blockDim.x)
-    prep2d_cell<T>(sl.p, sl.st[in], am, (T*)sl.split, (T*)sl.roe, t);
+    prep2d_cell<T>(sl.p, sl.st[in], am, (T*)sl.split, (T*)sl.roe, t, which);
+}
+
+// ex6 slots: alpha per rank row / column and the wall mirrors
+__global__ void kb_seg_alpha(const BatchSlot* __restrict__ tab) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active || !sl.p.seg_alpha) return;
+  const int64_t n = seg_alpha_items(sl.p);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    seg_alpha_item(sl.p, t);
+}
+__global__ void kb_walls(const BatchSlot* __restrict__ tab, int in, int ydir) {
+  const BatchSlot& sl = tab[blockIdx.y];
+  if (!sl.active || sl.p.problem != SWFD_PROBLEM_SHOCK_DIFFRACTION) return;
+  const int n = ydir ? sl.p.total * 3 : (min(6 * sl.p.total, sl.p.g.ny + 1) + 1) * 3;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    if (ydir) wall_y_item(sl.p, sl.st[in], t);
+    else wall_x_item(sl.p, sl.st[in], t);
+  }
 }
 
 // all slots' interfaces in one persistent launch; chunk c belongs to the slot
@@ -803,7 +1035,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     const BatchSlot& sl = tab[lo];
     if (!sl.active) continue;
     const T am = sl.p.alpha_premul ? T(sl.dsc->alphamax) : T(1.0);
-    flux_chunk<T>(sl.p, (const T*)sl.split, (const T*)sl.roe, am, (T*)sl.flux, c - prefix[lo],
+    flux_chunk<T, true>(sl.p, (const T*)sl.split, (const T*)sl.roe, am, (T*)sl.flux, c - prefix[lo],
                   sl.chunks_x, lane);
   }
 }
@@ -871,12 +1103,24 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
   kb_stage_reset<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
   kb_alpha<<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
   kb_alpha_final<<<gs, 128, 0, s>>>(b.tab, n, stage);
+  if (b.segmented) {
+    kb_seg_alpha<<<grid, SWFD_BLOCK, 0, s>>>(b.tab);
+    kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 0);
+  }
   if (b.fp32) {
-    kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+    kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 1);
+    if (b.segmented) {
+      kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 1);
+      kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 2);
+    }
     kb_flux<float><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
     kb_rk<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
   } else {
-    kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+    kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 1);
+    if (b.segmented) {
+      kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 1);
+      kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 2);
+    }
     kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
     kb_rk<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
   }

@@ -73,6 +73,9 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
   Params p;
   st = make_params(*cfg, p, err);
   if (st != SWFD_OK) return static_fail(st, err);
+  if (p.seg_alpha)
+    return static_fail(SWFD_ERR_UNSUPPORTED,
+                       "shock diffraction needs per-rank buffers: use swfd_flux_divergence");
   const Geom& g = p.g;
   // intermediates: SoA state (nc planes), split fluxes (4 nc), Roe averages
   // (8), interface fluxes (4 nc), SoA RHS (nc), device scalars

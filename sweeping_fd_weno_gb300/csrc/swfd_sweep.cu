@@ -314,6 +314,7 @@ __global__ void k_pressure_pass_seq(Params p, double* __restrict__ u, int orderi
     double pres = sweep_pres(g, g1, vi);
     if (pres <= eps || vi[0] <= eps) {
       double vit[4];
+      const double pp = sweep_pres(g, g1, vp);
       nod_lim(g, g1, eps, vi, vp, ub, vit, np_, nn);
       for (int c = 0; c < g.nc; ++c) {
         double d = vi[c] - vit[c];
@@ -321,6 +322,10 @@ __global__ void k_pressure_pass_seq(Params p, double* __restrict__ u, int orderi
         vp[c] = vp[c] + 1.0 * (d);
         u[c * P + c1] = vp[c];
       }
+      // ex6 (ex6_shock_diffraction/main.f90:1413-1423, ordering-I passes)
+      if (p.sweep_check && ordering == 1 &&
+          pres + pp > sweep_pres(g, g1, vit) + sweep_pres(g, g1, vp) + eps)
+        dsc->error |= ERR_BIT_CHECK;
     }
     for (int c = 0; c < g.nc; ++c) vi[c] = vp[c];
     c0 = c1;
@@ -472,6 +477,7 @@ __global__ void k_chain_walk(Params p, double* u, int ordering, int forward, Swe
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
   long long npos_ = 0, nneg = 0;
+  int fail = 0;
   int64_t covered = -1;
   int base = 0;
   while (base < m) {
@@ -490,11 +496,13 @@ __global__ void k_chain_walk(Params p, double* u, int ordering, int forward, Swe
     int64_t e = 0;
     if (lane == first) {
       int merged;
-      e = run_chain<KIND, true>(p, u, ordering, forward, N, f, -1, ub, &merged, npos_, nneg);
+      e = run_chain<KIND, true>(p, u, ordering, forward, N, f, -1, ub, &merged, npos_, nneg,
+                                &fail);
     }
     covered = __shfl_sync(0xffffffffu, e, first);
     base += first + 1;
   }
+  if (KIND == 0 && fail) atomicOr(&dsc->error, ERR_BIT_CHECK);
   if (KIND == 0 && (npos_ | nneg)) {  // each lane adds the chains it ran
     atomicAdd((unsigned long long*)&dsc->t_pos, (unsigned long long)npos_);
     atomicAdd((unsigned long long*)&dsc->t_neg, (unsigned long long)nneg);
@@ -512,11 +520,14 @@ __global__ void k_chain_write(Params p, double* u, int ordering, int forward, Sw
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
   long long npos_ = 0, nneg = 0;
+  int fail = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     if (!(all_roots || sc.root[k])) continue;
     int merged;
-    run_chain<KIND, true>(p, u, ordering, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg);
+    run_chain<KIND, true>(p, u, ordering, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg,
+                          &fail);
   }
+  if (KIND == 0 && fail) atomicOr(&dsc->error, ERR_BIT_CHECK);
   if (KIND == 0 && (npos_ | nneg)) {
     atomicAdd((unsigned long long*)&dsc->t_pos, (unsigned long long)npos_);
     atomicAdd((unsigned long long*)&dsc->t_neg, (unsigned long long)nneg);
@@ -710,6 +721,7 @@ __global__ void kb_walk(const BatchSlot* __restrict__ tab, int out, int ordering
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = sl.dsc->ubar[c];
   long long npos_ = 0, nneg = 0;
+  int fail = 0;
   int64_t covered = -1;
   int base = 0;
   while (base < m) {
@@ -728,11 +740,12 @@ __global__ void kb_walk(const BatchSlot* __restrict__ tab, int out, int ordering
     int64_t e = 0;
     if (lane == first) {
       int merged;
-      e = run_chain<KIND, true>(p, u, ord, forward, N, f, -1, ub, &merged, npos_, nneg);
+      e = run_chain<KIND, true>(p, u, ord, forward, N, f, -1, ub, &merged, npos_, nneg, &fail);
     }
     covered = __shfl_sync(0xffffffffu, e, first);
     base += first + 1;
   }
+  if (KIND == 0 && fail) atomicOr(&sl.dsc->error, ERR_BIT_CHECK);
   if (KIND == 0 && (npos_ | nneg)) {
     atomicAdd((unsigned long long*)&sl.dsc->t_pos, (unsigned long long)npos_);
     atomicAdd((unsigned long long*)&sl.dsc->t_neg, (unsigned long long)nneg);
@@ -754,11 +767,13 @@ __global__ void kb_write(const BatchSlot* __restrict__ tab, int out, int orderin
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = sl.dsc->ubar[c];
   long long npos_ = 0, nneg = 0;
+  int fail = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     if (!(all_roots || sc.root[k])) continue;
     int merged;
-    run_chain<KIND, true>(p, u, ord, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg);
+    run_chain<KIND, true>(p, u, ord, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg, &fail);
   }
+  if (KIND == 0 && fail) atomicOr(&sl.dsc->error, ERR_BIT_CHECK);
   if (KIND == 0 && (npos_ | nneg)) {
     atomicAdd((unsigned long long*)&sl.dsc->t_pos, (unsigned long long)npos_);
     atomicAdd((unsigned long long*)&sl.dsc->t_neg, (unsigned long long)nneg);
@@ -802,7 +817,7 @@ __global__ void kb_sweep_begin(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n
   if (s >= n || !slot_in(tab[s], 0)) return;
   DevScalars* d = tab[s].dsc;
   const Params& p = tab[s].p;
-  if (p.problem == SWFD_PROBLEM_SEDOV_2D) {
+  if (p.stop_sweep) {
     const double* ub = d->ubar;
     if (p.gamma1 * (ub[3] - 0.5 * (ub[1] * ub[1] + ub[2] * ub[2]) / ub[0]) <= 0.) {
       d->error |= ERR_BIT_PUBAR;
@@ -863,7 +878,9 @@ __global__ void kb_q_end(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n) {
   DevScalars* d = tab[s].dsc;
   d->pre_count++;
   bool stop = false;
-  if (d->bad_count == 0) {
+  if (d->error & ERR_BIT_CHECK) {  // ex6 stopped inside the passes
+    stop = true;
+  } else if (d->bad_count == 0) {
     long long k = d->sweep_count - 1;
     if (k >= 0 && k < d->track_cap) {
       d->tracks[k] = d->q;

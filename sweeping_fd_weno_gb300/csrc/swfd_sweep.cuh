@@ -111,19 +111,27 @@ struct Chain {
   // one step: this (cell q) acts on nx (cell q+1); afterwards this holds the
   // final value of cell q and nx the modified value of cell q+1
   __device__ __forceinline__ void step(const Params& p, Chain& nx, const double* ub,
-                                       long long& npos_, long long& nneg) {
+                                       long long& npos_, long long& nneg, int* fail = nullptr) {
     if (KIND == 1) {
       const double delta = p.g.ndim == 1 ? 1e-13 : 1e-12;
       nx.s[0] = nx.s[0] + 1.0 * (s[0] - delta);
       s[0] = delta;
     } else {
-      double vit[4];
+      double vit[4], pi = 0., pp = 0.;
+      if (fail) {
+        pi = sweep_pres(p.g, p.gamma1, s);
+        pp = sweep_pres(p.g, p.gamma1, nx.s);
+      }
       nod_lim(p.g, p.gamma1, p.eps, s, nx.s, ub, vit, npos_, nneg);
       for (int c = 0; c < p.g.nc; ++c) {
         double d = s[c] - vit[c];
         s[c] = vit[c];
         nx.s[c] = nx.s[c] + 1.0 * (d);
       }
+      // ex6: the pair's total pressure must not increase
+      // (ex6_shock_diffraction/main.f90:1413-1423)
+      if (fail && pi + pp > sweep_pres(p.g, p.gamma1, s) + sweep_pres(p.g, p.gamma1, nx.s) + p.eps)
+        *fail = 1;
     }
   }
 };
@@ -139,8 +147,11 @@ __device__ __forceinline__ int64_t walk_cell(const Geom& g, int ordering, int fo
 template <int KIND, bool WRITE>
 __device__ inline int64_t run_chain(const Params& p, double* u, int ordering, int forward, int64_t N,
                              int64_t q0, int64_t stop, const double* ub, int* merged,
-                             long long& npos_, long long& nneg) {
+                             long long& npos_, long long& nneg, int* fail = nullptr) {
   const Geom& g = p.g;
+  // the ex6 check runs in the ordering-I passes (ex6_shock_diffraction/main.f90:1413-1423,
+  // 1472-1482; the ordering-II checks do not stop)
+  int* chk = (KIND == 0 && WRITE && p.sweep_check && ordering == 1) ? fail : nullptr;
   Chain<KIND> cur, nxt;
   int64_t cq = walk_cell(g, ordering, forward, N, q0);
   cur.load(p, u, cq);
@@ -153,7 +164,7 @@ __device__ inline int64_t run_chain(const Params& p, double* u, int ordering, in
     }
     int64_t cn = walk_cell(g, ordering, forward, N, q + 1);
     nxt.load(p, u, cn);
-    cur.step(p, nxt, ub, npos_, nneg);
+    cur.step(p, nxt, ub, npos_, nneg, chk);
     if (WRITE) cur.store(p, u, cq);
     ++q;
     cq = cn;

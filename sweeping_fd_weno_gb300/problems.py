@@ -17,7 +17,7 @@ def reference_defaults(problem: int) -> dict:
                 literals=abi.LITERALS_DOUBLE, precision=abi.PRECISION_FP64,
                 ubar_mode=abi.UBAR_SEQUENTIAL, sweep_mode=abi.SWEEP_PARALLEL, device=0, gamma=1.4,
                 e_background=0.0,
-                e_blast=0.0, ny=1)
+                e_blast=0.0, ny=1, total=0, cut_x=0, cut_y=0)
     if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425
         base.update(nx=800, ny=1, swp_num=50, cfl=1.2, time_terminal=0.001,
                     e_background=1e-9 / (1.4 - 1.0), e_blast=3200000.0)
@@ -28,13 +28,26 @@ def reference_defaults(problem: int) -> dict:
                     e_blast=0.244816)
     elif problem == abi.JET_2D:      # ex5_mach2000_jet/main.f90:4-6,597
         base.update(nx=800, ny=200, cfl=1.0 / 4.0, time_terminal=0.001, gamma=5.0 / 3.0)
+    elif problem == abi.SHOCK_DIFFRACTION:  # ex6_shock_diffraction/main.f90:16-20,695
+        base.update(shock_grid(80), cfl=0.9, time_terminal=2.3)
     else:
         raise ValueError(f"unknown problem {problem}")
     return base
 
 
+def shock_grid(total: int, cut_x: int = 4, cut_y: int = 8) -> dict:
+    """Grid of the shock-diffraction example for its `total` and rank grid:
+    nx = cut_x*(13*total/cut_x), ny = cut_y*(11*total/cut_y) in integer
+    arithmetic (ex6_shock_diffraction/main.f90:16-18)."""
+    return dict(total=total, cut_x=cut_x, cut_y=cut_y, nx=cut_x * (13 * total // cut_x),
+                ny=cut_y * (11 * total // cut_y))
+
+
 def make_config(problem: int, **overrides) -> abi.SwfdConfig:
     d = reference_defaults(problem)
+    if problem == abi.SHOCK_DIFFRACTION and "total" in overrides:
+        d.update(shock_grid(overrides["total"], overrides.get("cut_x", 4),
+                            overrides.get("cut_y", 8)))
     unknown = set(overrides) - set(d) - {"reserved"}
     if unknown:
         raise KeyError(f"unknown config fields {sorted(unknown)}")
@@ -59,6 +72,11 @@ def workload(name: str, **overrides) -> abi.SwfdConfig:
     if name == "jet":
         # Mach-2000-type jet, 800x200 half domain with the y=0 symmetry plane, T=0.001
         return make_config(abi.JET_2D, **overrides)
+    if name.startswith("shock"):
+        # Mach 5.09 shock diffraction around a step; name 'shock<total>'
+        # (total 20..80: 260x216 .. 1040x880 cells)
+        return make_config(abi.SHOCK_DIFFRACTION, total=int(name[len("shock"):] or 80),
+                           **overrides)
     if name.startswith("sedov2d"):
         n = int(name[len("sedov2d"):] or 640)
         return make_config(abi.SEDOV_2D, nx=n, ny=n, **overrides)

@@ -30,6 +30,7 @@ CASES = {
                                                      e_background=1e-12), 40),
     "sedov2d_32_6steps": (abi.SEDOV_2D, dict(nx=32, ny=32), 6),
     "jet_80x20_6steps": (abi.JET_2D, dict(nx=80, ny=20), 6),
+    "shock8_20steps": (abi.SHOCK_DIFFRACTION, dict(total=8), 20),
 }
 
 

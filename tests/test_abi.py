@@ -58,3 +58,18 @@ def test_null_handle_is_rejected(swfd):
     lib = abi.load()
     assert lib.swfd_step(None, None) == abi.ERR_INVALID
     assert lib.swfd_destroy(None) == abi.OK
+
+
+def test_shock_diffraction_config_checks(swfd):
+    """The wall rows must sit inside one rank, away from its ghost rows."""
+    import ctypes as C
+    from sweeping_fd_weno_gb300 import problems
+    lib = abi.load()
+    h = C.c_void_p()
+    cfg = problems.workload("shock8")       # step top at local row 4 of its rank
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
+    cfg = problems.workload("shock12")
+    cfg.nx += 4                              # not cut_x*(13*total/cut_x)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.workload("shock12", cut_x=3)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
