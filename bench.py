@@ -271,43 +271,67 @@ def bench_batched(args, local, flush):
     }
 
 
-def serving_draw(precision, device):
-    """Requests of the serving mix: the vortex (45^2..360^2, T=0.01) or a
-    point-energy instance (128^2..640^2, shortened to T=0.02)."""
+def serving_draw(device, plain_fp64=False):
+    """Requests of the serving mix, drawn uniformly from three problems: the
+    vortex (45^2..360^2, T=0.01), a point-energy instance (128^2..640^2,
+    shortened to T=0.02) and the Mach 5.09 shock diffraction (total 20..80:
+    260x216..1040x880, shortened to T=0.05).  The first two run in FP32-bulk
+    (accepted: relative L1 density error < 1e-6), the shock in FP64; with
+    plain_fp64 every request is FP64."""
     from sweeping_fd_weno_gb300 import abi, problems
+    from sweeping_fd_weno_gb300.serving import fp32_accepted
 
     def draw(rng):
-        if rng.integers(0, 2) == 0:
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
             n = int(rng.choice([45, 90, 180, 360]))
-            return problems.make_config(abi.VORTEX_2D, nx=n, ny=n, precision=precision,
-                                        device=device)
-        n = int(rng.integers(128, 641))
-        return problems.make_config(abi.SEDOV_2D, nx=n, ny=n, time_terminal=0.02,
-                                    precision=precision, device=device)
+            c = problems.make_config(abi.VORTEX_2D, nx=n, ny=n, device=device)
+        elif kind == 1:
+            n = int(rng.integers(128, 641))
+            c = problems.make_config(abi.SEDOV_2D, nx=n, ny=n, time_terminal=0.02, device=device)
+        else:
+            total = int(rng.choice([20, 40, 60, 80]))
+            c = problems.make_config(abi.SHOCK_DIFFRACTION, total=total, time_terminal=0.05,
+                                     device=device)
+        c.precision = (abi.PRECISION_FP32_BULK if fp32_accepted(c) and not plain_fp64
+                       else abi.PRECISION_FP64)
+        return c
     return draw
 
 
 def bench_serving(args, local):
-    """Poisson arrivals (mean 50 req/s) served by continuous batching (FP32 bulk)
-    and, for comparison, one at a time by the plain FP64 path."""
+    """Poisson arrivals (mean 50 req/s) served by continuous batching (an
+    FP32-bulk batch and an FP64 batch side by side) and, for comparison, one
+    at a time by the plain FP64 path."""
     from sweeping_fd_weno_gb300 import Batch, abi
     from sweeping_fd_weno_gb300.serving import (poisson_arrivals, serve_batched,
                                                 serve_one_at_a_time)
     arr = poisson_arrivals(args.serve_rate, args.serve_requests, SERVE_SEED,
-                           serving_draw(abi.PRECISION_FP32_BULK, local))
+                           serving_draw(local))
     with Batch(max_slots=args.serve_slots, max_nx=640, max_ny=640,
-               precision=abi.PRECISION_FP32_BULK, ubar_mode=abi.UBAR_TREE, device=local) as b:
-        rb = serve_batched(arr, b, step_chunk=args.serve_chunk)
+               precision=abi.PRECISION_FP32_BULK, ubar_mode=abi.UBAR_TREE, device=local) as b32, \
+            Batch(max_slots=max(4, args.serve_slots // 4), max_nx=1040, max_ny=880,
+                  precision=abi.PRECISION_FP64, ubar_mode=abi.UBAR_SEQUENTIAL,
+                  device=local) as b64:
+        rb = serve_batched(arr, [b32, b64], step_chunk=args.serve_chunk)
     # the same stream (same seed: same arrivals and requests) in plain FP64
     plain = poisson_arrivals(args.serve_rate, args.serve_requests, SERVE_SEED,
-                             serving_draw(abi.PRECISION_FP64, local))
+                             serving_draw(local, plain_fp64=True))
     rp = serve_one_at_a_time(plain)
     sb, sp = rb.summary(), rp.summary()
+    kinds = {}
+    for _, c in arr:
+        kinds[int(c.problem)] = kinds.get(int(c.problem), 0) + 1
     return {
         "workload": f"{len(arr)} requests, Poisson arrivals mean {args.serve_rate:g}/s "
-                    f"(numpy default_rng({SERVE_SEED})): vortex 45^2..360^2 to T=0.01 or "
-                    "point energy 128^2..640^2 to T=0.02",
-        "batched_fp32_bulk": sb, "plain_fp64_one_at_a_time": sp,
+                    f"(numpy default_rng({SERVE_SEED})), uniformly: vortex 45^2..360^2 to "
+                    "T=0.01, point energy 128^2..640^2 to T=0.02, shock diffraction total "
+                    "20..80 to T=0.05",
+        "requests_by_problem": {"vortex": kinds.get(3, 0), "point_energy": kinds.get(4, 0),
+                                "shock_diffraction": kinds.get(6, 0)},
+        "precision": "FP32-bulk batch (vortex, point energy) beside an FP64 batch (shock "
+                     "diffraction: FP32 error 1e-3 fails the 1e-6 bar)",
+        "batched": sb, "plain_fp64_one_at_a_time": sp,
         "throughput_ratio": (sb["value"] / sp["value"]) if sp["value"] else None,
         "slots": args.serve_slots, "step_chunk": args.serve_chunk,
     }

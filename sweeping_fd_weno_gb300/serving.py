@@ -1,12 +1,14 @@
 """Serving loops: a stream of independent Euler solves arriving over time.
 
 `serve_batched` is continuous batching over the batched engine: a request is
-admitted as soon as it has arrived and the batch has a free slot and enough
+admitted as soon as it has arrived and its batch has a free slot and enough
 of its HBM budget; while any request runs, the loop advances every running
-request together by `step_chunk` SSP-RK3 steps (one graph launch); finished
-requests are polled, their final state read back to the host, their
+request together by `step_chunk` SSP-RK3 steps (one graph launch per batch);
+finished requests are polled, their final state read back to the host, their
 time-to-solution (arrival to result on the host) recorded and their slots
-released for the requests still waiting.
+released for the requests still waiting.  Requests whose problem does not
+meet the FP32-bulk accuracy bar go to an FP64 batch that runs beside the
+FP32-bulk one.
 
 `serve_one_at_a_time` is the plain form the batched one is compared with:
 the same stream, first come first served, each request solved alone by a
@@ -16,10 +18,12 @@ from __future__ import annotations
 
 import time
 from collections import deque
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import abi
 from .batch import Batch
 from .solver import Solver
 
@@ -47,45 +51,81 @@ class ServeResult:
                 "launches": self.launches}
 
 
-def serve_batched(arrivals, batch: Batch, step_chunk: int = 4, timeout: float = 600.0,
+def fp32_accepted(cfg) -> bool:
+    """The FP32-bulk form is accepted where its relative L1 density error
+    against FP64 stays below 1e-6: the vortex and the point-energy problems.
+    The jet (kinetic-dominated) and the shock diffraction (~1e-3) stay FP64."""
+    return cfg.problem in (abi.VORTEX_2D, abi.SEDOV_2D)
+
+
+def serve_batched(arrivals, batches, step_chunk: int = 4, timeout: float = 600.0,
                   keep=None) -> ServeResult:
     """arrivals: list of (arrival time in s after the start, swfd_config).
-    `keep` (optional dict) receives each request's final (state, time)."""
+    batches: one Batch, or several (e.g. an FP32-bulk one and an FP64 one):
+    a request goes to the first batch of its own precision.  Batches with
+    running requests advance concurrently, each on its own stream, driven
+    from its own host thread.  `keep` (optional dict) receives each request's
+    final (state, time)."""
+    if isinstance(batches, Batch):
+        batches = [batches]
+    pool = ThreadPoolExecutor(max_workers=len(batches)) if len(batches) > 1 else None
+
+    def route(c):
+        for k, b in enumerate(batches):
+            if b.cfg.precision == c.precision:
+                return k
+        raise ValueError(f"no batch for precision {c.precision}")
+
     pending = deque(sorted(((t, k, c) for k, (t, c) in enumerate(arrivals)), key=lambda x: x[0]))
     waiting = deque()
     arrived_at, cells_of = {}, {}
     res = ServeResult()
     n_total, done = len(pending), 0
     t0 = time.perf_counter()
-    while done < n_total:
-        now = time.perf_counter() - t0
-        if now > timeout:
-            raise TimeoutError(f"serving stream not finished after {timeout} s")
-        while pending and pending[0][0] <= now:
-            waiting.append(pending.popleft())
-        while waiting:
-            t, k, c = waiting[0]
-            if not batch.admit(c, k):
-                break
-            waiting.popleft()
-            arrived_at[k] = t
-            cells_of[k] = c.nx * c.ny
-        if batch.info()["running"] == 0:
-            if pending:
-                time.sleep(max(0.0, min(pending[0][0] - (time.perf_counter() - t0), 0.005)))
-            continue
-        batch.run(step_chunk)
-        res.launches += 1
-        for rid, st in batch.poll():
-            u, tt = batch.download(rid)
-            _, steps = batch.progress(rid)
-            res.latencies[rid] = time.perf_counter() - t0 - arrived_at[rid]
-            res.status[rid] = st
-            res.updates[rid] = cells_of[rid] * 3 * steps
-            if keep is not None:
-                keep[rid] = (u, tt)
-            batch.release(rid)
-            done += 1
+    try:
+        while done < n_total:
+            now = time.perf_counter() - t0
+            if now > timeout:
+                raise TimeoutError(f"serving stream not finished after {timeout} s")
+            while pending and pending[0][0] <= now:
+                waiting.append(pending.popleft())
+            still = deque()
+            full = set()
+            while waiting:  # first come first served within each batch
+                t, k, c = waiting.popleft()
+                bi = route(c)
+                if bi in full or not batches[bi].admit(c, k):
+                    full.add(bi)
+                    still.append((t, k, c))
+                    continue
+                arrived_at[k] = t
+                cells_of[k] = c.nx * c.ny
+            waiting = still
+            busy = [b for b in batches if b.info()["running"] > 0]
+            if not busy:
+                if pending:
+                    time.sleep(max(0.0, min(pending[0][0] - (time.perf_counter() - t0), 0.005)))
+                continue
+            if pool and len(busy) > 1:
+                list(pool.map(lambda b: b.run(step_chunk), busy))
+            else:
+                for b in busy:
+                    b.run(step_chunk)
+            res.launches += len(busy)
+            for b in busy:
+                for rid, st in b.poll():
+                    u, tt = b.download(rid)
+                    _, steps = b.progress(rid)
+                    res.latencies[rid] = time.perf_counter() - t0 - arrived_at[rid]
+                    res.status[rid] = st
+                    res.updates[rid] = cells_of[rid] * 3 * steps
+                    if keep is not None:
+                        keep[rid] = (u, tt)
+                    b.release(rid)
+                    done += 1
+    finally:
+        if pool:
+            pool.shutdown()
     res.wall = time.perf_counter() - t0
     return res
 
