@@ -352,6 +352,57 @@ static void prep_cell(const oracle* o, int ydir, const double* a, double* w, dou
   *h = (pre + eng) * t0;
 }
 
+/* use_limiter = 1: positivity limiter of one split flux (ex3_vortex_accuracy_2d/main.f90:241-329,
+ * y pass :444-530; ex6 clamps theta at 0, ex6_shock_diffraction/main.f90:330,351,379,398).
+ * ave: the split flux of the interface's left cell; out: its reconstructed flux. */
+static void zs_limit(oracle* o, const double* ave, double* out) {
+  const double g1 = o->gamma1;
+  const int clamp = o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
+  const double d_ave = ave[0], m_ave = ave[1], n_ave = ave[2], e_ave = ave[3];
+  const double p_ave = g1 * (e_ave - 0.5 * (m_ave * m_ave) / d_ave - 0.5 * (n_ave * n_ave) / d_ave);
+  double point[2][4];
+  double theta = 1.0;
+  for (int c = 0; c < 4; ++c) {
+    point[0][c] = out[c];
+    point[1][c] = (ave[c] - out[c] / 12.) / (11. / 12.);
+  }
+  for (int ig = 0; ig < 2; ++ig) {
+    double d_l = point[ig][0];
+    if (d_l < 0.) theta = fmin(theta, fabs(d_ave - 0.) / fabs(d_ave - d_l));
+  }
+  if (clamp) theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    out[0] = theta * out[0] + (1. - theta) * d_ave;
+    o->den_count++;
+  }
+  theta = 1.;
+  point[0][0] = out[0];
+  point[1][0] = (ave[0] - out[0] / 12.) / (11. / 12.);
+  for (int ig = 0; ig < 2; ++ig) {
+    double d_l = point[ig][0], m_l = point[ig][1], n_l = point[ig][2], e_l = point[ig][3];
+    double p_l = g1 * (e_l - (m_l * m_l) / d_l / 2. - (n_l * n_l) / d_l / 2.);
+    if (p_l < 0.) theta = fmin(theta, fabs(p_ave - 0.) / fabs(p_ave - p_l));
+  }
+  if (clamp) theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    o->pre_count++;
+    for (int c = 0; c < 4; ++c) out[c] = theta * out[c] + (1. - theta) * ave[c];
+  }
+}
+
+/* the limiter on both split fluxes of an interface whose left cell is (i, j) */
+static void limit_interface(oracle* o, const double* pos, const double* neg, int i, int j,
+                            double* op, double* on) {
+  if (o->cfg.use_limiter != 1) return;
+  double a[4], b[4];
+  for (int c = 0; c < 4; ++c) {
+    a[c] = pos[IX(o, c, i, j)];
+    b[c] = neg[IX(o, c, i, j)];
+  }
+  zs_limit(o, a, op);
+  zs_limit(o, b, on);
+}
+
 /* wenofd (ex3_vortex_accuracy_2d/main.f90:115-534; ex4_sedov_2d/main.f90:179-637) */
 static void wenofd2d(oracle* o) {
   const int nx = o->nx, ny = o->ny;
@@ -388,6 +439,7 @@ static void wenofd2d(oracle* o) {
       interface2d(o, 0, o->wk_w[i], o->wk_w[i + 1], o->wk_vx[i], o->wk_vx[i + 1], o->wk_vy[i],
                   o->wk_vy[i + 1], o->wk_h[i], o->wk_h[i + 1], (const double(*)[4])sp,
                   (const double(*)[4])sn, op, on);
+      limit_interface(o, o->fp, o->fn, i, j, op, on);
       for (int c = 0; c < 4; ++c) {
         U(o->fpf, c, i, j) = premul ? am * op[c] : op[c];
         U(o->fnf, c, i, j) = premul ? am * on[c] : on[c];
@@ -411,6 +463,7 @@ static void wenofd2d(oracle* o) {
       interface2d(o, 1, o->wk_w[j], o->wk_w[j + 1], o->wk_vx[j], o->wk_vx[j + 1], o->wk_vy[j],
                   o->wk_vy[j + 1], o->wk_h[j], o->wk_h[j + 1], (const double(*)[4])sp,
                   (const double(*)[4])sn, op, on);
+      limit_interface(o, o->gp, o->gn, i, j, op, on);
       for (int c = 0; c < 4; ++c) {
         U(o->gpf, c, i, j) = premul ? am * op[c] : op[c];
         U(o->gnf, c, i, j) = premul ? am * on[c] : on[c];
@@ -1115,6 +1168,7 @@ static void ex6_wenofd(oracle* r) {
       interface2d(r, 0, r->wk_w[i], r->wk_w[i + 1], r->wk_vx[i], r->wk_vx[i + 1], r->wk_vy[i],
                   r->wk_vy[i + 1], r->wk_h[i], r->wk_h[i + 1], (const double(*)[4])sp,
                   (const double(*)[4])sn, op, on);
+      limit_interface(r, r->fp, r->fn, i, j, op, on);
       for (int c = 0; c < 4; ++c) {
         UR(r, r->fpf, c, i, j) = al * op[c];
         UR(r, r->fnf, c, i, j) = al * on[c];
@@ -1156,6 +1210,7 @@ static void ex6_wenofd(oracle* r) {
       interface2d(r, 1, r->wk_w[j], r->wk_w[j + 1], r->wk_vx[j], r->wk_vx[j + 1], r->wk_vy[j],
                   r->wk_vy[j + 1], r->wk_h[j], r->wk_h[j + 1], (const double(*)[4])sp,
                   (const double(*)[4])sn, op, on);
+      limit_interface(r, r->gp, r->gn, i, j, op, on);
       for (int c = 0; c < 4; ++c) {
         UR(r, r->gpf, c, i, j) = al * op[c];
         UR(r, r->gnf, c, i, j) = al * on[c];
@@ -1693,7 +1748,13 @@ void oracle_get_stats(const oracle* o, int64_t* out) {
     if (k == 0 || o->pos_track[k] > mp) mp = o->pos_track[k];
   }
   out[0] = o->sweep_count; out[1] = tot; out[2] = mx; out[3] = tn; out[4] = mn;
-  out[5] = tp; out[6] = mp; out[7] = o->den_count; out[8] = o->pre_count; out[9] = o->fail_count;
+  int64_t den = o->den_count, pre = o->pre_count;
+  if (o->rk) /* the ranks' limiter counts, summed (ex6_shock_diffraction/main.f90:1167-1173) */
+    for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+      den += o->rk[k]->den_count;
+      pre += o->rk[k]->pre_count;
+    }
+  out[5] = tp; out[6] = mp; out[7] = den; out[8] = pre; out[9] = o->fail_count;
 }
 
 int64_t oracle_get_tracks(const oracle* o, int32_t* sweep, int32_t* neg, int32_t* pos, int64_t cap) {

@@ -31,8 +31,8 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
     return bad(SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
   if (c.precision != SWFD_PRECISION_FP64 && c.precision != SWFD_PRECISION_FP32_BULK)
     return bad(SWFD_ERR_INVALID, "unknown precision");
-  if (c.use_limiter != 0 && c.use_limiter != 2)
-    return bad(SWFD_ERR_UNSUPPORTED, "use_limiter must be 0 or 2");
+  if (c.use_limiter != 0 && c.use_limiter != 1 && c.use_limiter != 2)
+    return bad(SWFD_ERR_INVALID, "use_limiter must be 0, 1 or 2");
   if (c.ubar_mode != SWFD_UBAR_SEQUENTIAL)
     return bad(SWFD_ERR_UNSUPPORTED, "ubar_mode: only sequential is built");
   if (c.swp_num < 1) return bad(SWFD_ERR_INVALID, "swp_num must be >= 1");
@@ -183,6 +183,10 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   g.pitch = ((g.LI + 31) / 32) * 32;
   g.plane = (int64_t)g.pitch * g.LJ;
   p.stop_sweep = c.problem == SWFD_PROBLEM_SEDOV_2D || c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
+  // the positivity limiter exists in the 2D examples only (ex2 has no
+  // use_limiter == 1 branch)
+  p.limiter = c.use_limiter == 1 && g.ndim == 2;
+  p.limiter_clamp = c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
   if (!p.seg_alpha) {
     p.cut_x = p.cut_y = 1;
     p.nxl = g.nx;

@@ -309,6 +309,9 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   if (st != SWFD_OK) return bfail(b, st, err);
   if (c.problem == SWFD_PROBLEM_SEDOV_1D)
     return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine holds 2D problems");
+  if (c.use_limiter == 1)
+    return bfail(b, SWFD_ERR_UNSUPPORTED,
+                 "the batched engine runs the sweeping form (use_limiter 0 or 2)");
   if (c.nx > b->cfg.max_nx || c.ny > b->cfg.max_ny)
     return bfail(b, SWFD_ERR_INVALID, "grid larger than the batch's max_nx x max_ny");
   if (find_slot(b, request_id) >= 0) return bfail(b, SWFD_ERR_INVALID, "request id in use");

@@ -52,6 +52,8 @@ struct Params {
   double jet_in[4] = {0, 0, 0, 0};
   double jet_amb[4] = {0, 0, 0, 0};
   int stop_sweep = 0;    // P(u_bar) <= 0 and swp_num exhaustion stop the run (ex4, ex6)
+  int limiter = 0;       // use_limiter = 1: the positivity flux limiter in wenofd
+  int limiter_clamp = 0; // ex6 clamps its theta at 0 (theta = max(theta, 0.))
   // Shock diffraction (ex6_shock_diffraction/main.f90).  The reference's
   // rank grid cut_x x cut_y (ranks of nxl x nyl cells) is part of its
   // arithmetic: the x pass of row j uses the max alpha over the cells of
@@ -93,12 +95,22 @@ __host__ __device__ __forceinline__ int64_t seg_y_off(const Params& p, int i, in
 
 // interfaces of one stage: x faces of rows 1..ny, per rank segment its
 // local faces 0..nxl+1 (without segments: 0..nx+1); y faces of columns
-// 1..nx, per segment its local faces 0..nyl+1
-__host__ __device__ __forceinline__ int64_t flux_faces_x(const Params& p) {
-  return (int64_t)p.cut_x * (p.nxl + 2) * p.g.ny;
+// 1..nx, per segment its local faces 0..nyl+1.  With the limiter every face
+// the reference computes is computed, because the limiter counts events on
+// all of them: the x pass of each rank runs over its local rows 0..nyl+1 and
+// the y pass over its local columns 0..nxl+1 (rows and columns where ranks
+// overlap are computed, and counted, by both).
+__host__ __device__ __forceinline__ int64_t flux_rows_x(const Params& p, bool lim) {
+  return lim ? (int64_t)p.cut_y * (p.nyl + 2) : (int64_t)p.g.ny;
 }
-__host__ __device__ __forceinline__ int64_t flux_faces_y(const Params& p) {
-  return (int64_t)p.g.nx * p.cut_y * (p.nyl + 2);
+__host__ __device__ __forceinline__ int64_t flux_cols_y(const Params& p, bool lim) {
+  return lim ? (int64_t)p.cut_x * (p.nxl + 2) : (int64_t)p.g.nx;
+}
+__host__ __device__ __forceinline__ int64_t flux_faces_x(const Params& p, bool lim = false) {
+  return (int64_t)p.cut_x * (p.nxl + 2) * flux_rows_x(p, lim);
+}
+__host__ __device__ __forceinline__ int64_t flux_faces_y(const Params& p, bool lim = false) {
+  return flux_cols_y(p, lim) * p.cut_y * (p.nyl + 2);
 }
 
 

@@ -588,13 +588,61 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
 // resident blocks per SM: the FP64 pipe saturates with 3 (168 registers);
 // the FP32 pipe needs more warps in flight
 #define SWFD_FLUX_MINB(T) (sizeof(T) == 8 ? 3 : 4)
+// use_limiter = 1: the positivity limiter of one split flux at its interface
+// (ex3_vortex_accuracy_2d/main.f90:241-329, y pass :444-530; ex6 clamps theta
+// at 0, ex6_shock_diffraction/main.f90:330,351,379,398).  sp: the split flux
+// of the interface's left cell (components S apart), out: its reconstructed
+// flux, limited in place; nd, np count the density and pressure limitings.
+template <class T>
+__device__ __forceinline__ void zs_limit(const Params& p, const T* __restrict__ sp, int64_t S,
+                                         T out[4], int& nd, int& np) {
+  const T g1 = T(p.gamma1);
+  const T d_ave = ldt(sp), m_ave = ldt(sp + S), n_ave = ldt(sp + 2 * S), e_ave = ldt(sp + 3 * S);
+  const T ave[4] = {d_ave, m_ave, n_ave, e_ave};
+  const T p_ave = g1 * (e_ave - T(0.5) * (m_ave * m_ave) / d_ave - T(0.5) * (n_ave * n_ave) / d_ave);
+  T pt[2][4];
+  for (int c = 0; c < 4; ++c) {
+    pt[0][c] = out[c];
+    pt[1][c] = (ave[c] - out[c] / T(12.)) / T(11. / 12.);
+  }
+  T theta = T(1.);
+  for (int ig = 0; ig < 2; ++ig) {
+    const T d_l = pt[ig][0];
+    if (d_l < T(0.)) theta = fmin(theta, fabs(d_ave - T(0.)) / fabs(d_ave - d_l));
+  }
+  if (p.limiter_clamp) theta = fmax(theta, T(0.));
+  if (theta < T(1.)) {
+    out[0] = theta * out[0] + (T(1.) - theta) * d_ave;
+    ++nd;
+  }
+  theta = T(1.);
+  pt[0][0] = out[0];
+  pt[1][0] = (ave[0] - out[0] / T(12.)) / T(11. / 12.);
+  for (int ig = 0; ig < 2; ++ig) {
+    const T d_l = pt[ig][0], m_l = pt[ig][1], n_l = pt[ig][2], e_l = pt[ig][3];
+    const T p_l = g1 * (e_l - (m_l * m_l) / d_l / T(2.) - (n_l * n_l) / d_l / T(2.));
+    if (p_l < T(0.)) theta = fmin(theta, fabs(p_ave - T(0.)) / fabs(p_ave - p_l));
+  }
+  if (p.limiter_clamp) theta = fmax(theta, T(0.));
+  if (theta < T(1.)) {
+    ++np;
+    for (int c = 0; c < 4; ++c) out[c] = theta * out[c] + (T(1.) - theta) * ave[c];
+  }
+}
+
+__device__ __forceinline__ void count_limited(unsigned long long* cnt, int nd, int np) {
+  if (nd) atomicAdd(cnt, (unsigned long long)nd);
+  if (np) atomicAdd(cnt + 1, (unsigned long long)np);
+}
+
 // the 32 interfaces of chunk c (x chunks first, then y chunks).  SEG: the
 // problem may have rank segments (ex6); without them the face index maps
 // directly to the cell offset.
-template <class T, bool SEG>
+template <class T, bool SEG, bool LIM = false>
 __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict__ split,
                                            const T* __restrict__ roe, T am, T* __restrict__ flux,
-                                           int64_t c, int64_t chunks_x, int lane) {
+                                           int64_t c, int64_t chunks_x, int lane,
+                                           unsigned long long* cnt) {
   const Geom& g = p.g;
   const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
   const T g1 = T(p.gamma1), weps = T(p.weno_eps);
@@ -602,9 +650,10 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
     T op[4], on[4];
     if (c < chunks_x) {
       int64_t t = (int64_t)c * 32 + lane;
-      if (t >= flux_faces_x(p)) return;
+      if (t >= flux_faces_x(p, LIM)) return;
       const int lsx = p.nxl + 2, lx = p.cut_x * lsx;
-      const int r = (int)(t % lx), j = (int)(t / lx) + 1;
+      const int r = (int)(t % lx), rr = (int)(t / lx);
+      const int j = LIM ? (rr / (p.nyl + 2)) * p.nyl + rr % (p.nyl + 2) : rr + 1;
       const int sx = SEG ? r / lsx : 0, i = SEG ? sx * p.nxl + r % lsx : r;
       const int64_t o = g.at(i, j), os = SEG ? seg_x_off(p, i, j, sx) : o;
       if (SEG && p.seg_alpha) am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
@@ -613,6 +662,12 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
                      ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
                      ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
       interface_flux<0>(E, split + os - 2, split + 4 * S + os - 2, S, 1, weps, op, on);
+      if (LIM) {
+        int nd = 0, np = 0;
+        zs_limit<T>(p, split + os, S, op, nd, np);
+        zs_limit<T>(p, split + 4 * S + os, S, on, nd, np);
+        count_limited(cnt, nd, np);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         flux[k * S + os] = p.alpha_premul ? am * op[k] : op[k];
@@ -620,9 +675,10 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
       }
     } else {
       int64_t t = (int64_t)(c - chunks_x) * 32 + lane;
-      if (t >= flux_faces_y(p)) return;
+      if (t >= flux_faces_y(p, LIM)) return;
       const int lsy = p.nyl + 2;
-      const int i = (int)(t % g.nx) + 1, r = (int)(t / g.nx);
+      const int ncol = (int)flux_cols_y(p, LIM), ci = (int)(t % ncol), r = (int)(t / ncol);
+      const int i = LIM ? (ci / (p.nxl + 2)) * p.nxl + ci % (p.nxl + 2) : ci + 1;
       const int sy = SEG ? r / lsy : 0, j = SEG ? sy * p.nyl + r % lsy : r;
       const int64_t o = g.at(i, j), os = SEG ? seg_y_off(p, i, j, sy) : o;
       if (SEG && p.seg_alpha) am = T(p.seg_ay[(int64_t)(i + 2) * p.cut_y + sy]);
@@ -646,6 +702,12 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
                      ldt(rr + 3 * P + o), hr, E);
       interface_flux<1>(E, split + 8 * S + os - 2 * spit, split + 12 * S + os - 2 * spit, S, spit,
                         weps, op, on);
+      if (LIM) {
+        int nd = 0, np = 0;
+        zs_limit<T>(p, split + 8 * S + os, S, op, nd, np);
+        zs_limit<T>(p, split + 12 * S + os, S, on, nd, np);
+        count_limited(cnt, nd, np);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         flux[(8 + k) * S + os] = p.alpha_premul ? am * op[k] : op[k];
@@ -655,12 +717,12 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
   }
 }
 
-template <class T, bool SEG>
+template <class T, bool SEG, bool LIM>
 __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
               const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
-  const int64_t chunks_x = (flux_faces_x(p) + 31) / 32;
-  const int64_t chunks = chunks_x + (flux_faces_y(p) + 31) / 32;
+  const int64_t chunks_x = (flux_faces_x(p, LIM) + 31) / 32;
+  const int64_t chunks = chunks_x + (flux_faces_y(p, LIM) + 31) / 32;
   const int lane = threadIdx.x & 31;
   const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
   for (;;) {
@@ -668,7 +730,8 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
-    flux_chunk<T, SEG>(p, split, roe, am, flux, c, chunks_x, lane);
+    flux_chunk<T, SEG, LIM>(p, split, roe, am, flux, c, chunks_x, lane,
+                       (unsigned long long*)&dsc->den_count);
   }
 }
 
@@ -679,10 +742,29 @@ static int flux_grid() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T, false>, SWFD_FLUX_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T, false, false>, SWFD_FLUX_BLOCK,
+                                                  0);
     grid = sms * (per > 0 ? per : 1);
   }
   return grid;
+}
+
+// the flux kernel variant of the problem: rank segments (ex6), limiter
+template <class T>
+static void launch_flux_xy(const Params& p, const void* split, const void* roe,
+                           const DevScalars* dsc, void* flux, int* work, cudaStream_t s) {
+  const T* sp = (const T*)split;
+  const T* rp = (const T*)roe;
+  T* fp = (T*)flux;
+  const int grid = flux_grid<T>();
+  if (p.seg_alpha && p.limiter)
+    k_flux_xy<T, true, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+  else if (p.seg_alpha)
+    k_flux_xy<T, true, false><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+  else if (p.limiter)
+    k_flux_xy<T, false, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+  else
+    k_flux_xy<T, false, false><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
 }
 
 cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
@@ -701,18 +783,10 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
   }
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  if (f32 && p.seg_alpha)
-    k_flux_xy<float, true><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
-        p, (const float*)split, (const float*)roe, dsc, (float*)flux, work);
-  else if (f32)
-    k_flux_xy<float, false><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(
-        p, (const float*)split, (const float*)roe, dsc, (float*)flux, work);
-  else if (p.seg_alpha)
-    k_flux_xy<double, true><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
-        p, (const double*)split, (const double*)roe, dsc, (double*)flux, work);
+  if (f32)
+    launch_flux_xy<float>(p, split, roe, dsc, flux, work, s);
   else
-    k_flux_xy<double, false><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(
-        p, (const double*)split, (const double*)roe, dsc, (double*)flux, work);
+    launch_flux_xy<double>(p, split, roe, dsc, flux, work, s);
   return cudaGetLastError();
 }
 
@@ -1036,7 +1110,8 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     if (!sl.active) continue;
     const T am = sl.p.alpha_premul ? T(sl.dsc->alphamax) : T(1.0);
     flux_chunk<T, true>(sl.p, (const T*)sl.split, (const T*)sl.roe, am, (T*)sl.flux, c - prefix[lo],
-                  sl.chunks_x, lane);
+                  sl.chunks_x, lane,
+                        (unsigned long long*)&sl.dsc->den_count);
   }
 }
 
