@@ -379,6 +379,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="vortex360")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_bulk"],
+                    help="arithmetic of the main measurement (the headline is fp64)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--reference-nx", type=int, default=180)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
@@ -412,7 +414,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    cfg = problems.workload(args.workload, device=local)
+    main_prec = abi.PRECISION_FP64 if args.precision == "fp64" else abi.PRECISION_FP32_BULK
+    cfg = problems.workload(args.workload, device=local, precision=main_prec)
     solver = Solver(cfg)
     solver.init_problem()
     cells = solver.nx * solver.ny
@@ -559,10 +562,13 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex (no dataset)",
-        "config": {"workload": f"{args.workload}_fp64", "nx": solver.nx, "ny": solver.ny,
-                   "stages_per_step": 3, "precision": "plain FP64 (double literals)",
+        "config": {"workload": f"{args.workload}_{args.precision}", "nx": solver.nx,
+                   "ny": solver.ny, "stages_per_step": 3,
+                   "precision": "plain FP64 (double literals)" if args.precision == "fp64"
+                   else "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, sweeps)",
                    "l2": "flushed between timed steps (256 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "clocks": clk,

@@ -182,6 +182,13 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   }
   g.pitch = ((g.LI + 31) / 32) * 32;
   g.plane = (int64_t)g.pitch * g.LJ;
+  // cell and face indices are decomposed in 32-bit arithmetic on the device
+  if ((int64_t)(g.LI + 6 * 64) * (g.LJ + 6 * 64) >= (int64_t)1 << 31) {
+    err = "grid too large (cells and faces are indexed in 32 bits)";
+    return SWFD_ERR_INVALID;
+  }
+  p.fdx_inv = (float)(1.0 / p.dx);
+  p.fdy_inv = g.ndim == 2 ? (float)(1.0 / p.dy) : 0.f;
   p.stop_sweep = c.problem == SWFD_PROBLEM_SEDOV_2D || c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
   // the positivity limiter exists in the 2D examples only (ex2 has no
   // use_limiter == 1 branch)

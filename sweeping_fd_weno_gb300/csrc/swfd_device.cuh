@@ -1,6 +1,9 @@
 // swfd_device.cuh -- device arithmetic shared by the kernels.
 //
-// Every expression keeps the reference's Fortran operation order.  The
+// Every expression keeps the reference's Fortran operation order in FP64.
+// The FP32-bulk instantiations (T = float) are not bit-exact by design and
+// use single-precision math throughout, with reciprocals where several
+// divisions share a denominator.  The
 // library is compiled with -fmad=false so that no multiply-add is contracted
 // (the x86-64 reference build has no FMA).  Terms the reference multiplies by
 // the constants 0 or 1 inside the eigenvector products are left out: x*1 is
@@ -25,6 +28,11 @@ namespace swfd {
 
 template <class T>
 __device__ __forceinline__ T tsq(T a) { return a * a; }
+// single-precision math stays single precision (no promotion to double)
+__device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double tabs(double a) { return fabs(a); }
+__device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double dsq(double a) { return a * a; }
 
 // beta(1:3) (weno5.f90:100-102); am2..ap2 = average(-2..2)
@@ -48,7 +56,13 @@ __device__ __forceinline__ T weno_right(T am2, T am1, T a0, T ap1, T ap2, T eps)
   T a2 = T(0.6) / tsq(eps + b2);
   T a3 = T(0.1) / tsq(eps + b3);
   T s = a1 + a2 + a3;
-  T w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  T w1, w2, w3;
+  if constexpr (sizeof(T) == 4) {  // FP32-bulk: one reciprocal for the three weights
+    const T rs = T(1.) / s;
+    w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
+  } else {  // the reference's three divisions (weno5.f90:134-140)
+    w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  }
   return w1 * um3 + w2 * um2 + w3 * um1;
 }
 
@@ -64,7 +78,13 @@ __device__ __forceinline__ T weno_left(T am2, T am1, T a0, T ap1, T ap2, T eps) 
   T a2 = T(0.6) / tsq(eps + b2);
   T a3 = T(0.3) / tsq(eps + b3);
   T s = a1 + a2 + a3;
-  T w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  T w1, w2, w3;
+  if constexpr (sizeof(T) == 4) {
+    const T rs = T(1.) / s;
+    w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
+  } else {  // weno5.f90:104-110
+    w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  }
   return w1 * up3 + w2 * up2 + w3 * up1;
 }
 
@@ -88,7 +108,7 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   T vym = t0 * vyl + t1 * vyr;
   T hm = t0 * hl + t1 * hr;
   T qm = T(0.5) * (vxm * vxm + vym * vym);
-  T cm = sqrt(fabs(g1 * (hm - qm))) + T(1.e-15);
+  T cm = tsqrt(tabs(g1 * (hm - qm))) + T(1.e-15);
   T vn = ydir ? vym : vxm;
   T vt = ydir ? vxm : vym;
   t0 = vn * cm;

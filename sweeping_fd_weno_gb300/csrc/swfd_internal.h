@@ -44,6 +44,7 @@ struct Params {
   int dt_rule = 0;       // 1: dx*cfl/a; 3: dx**(5/3)*cfl/a; 4: min(dx,dy)*cfl/a clamped
   double gamma = 1.4, gamma1 = 0.4, eps = 1e-13, eps2 = 1e-8, weno_eps = 1e-6;
   double dx = 0, dy = 0;
+  float fdx_inv = 0.f, fdy_inv = 0.f;  // FP32-bulk flux differences: 1/dx, 1/dy
   double dt_num_x = 0;   // dx*cfl   (or dx**(5/3)*cfl for dt_rule 3)
   double dt_num_y = 0;   // dy*cfl
   double time_terminal = 0;

@@ -18,7 +18,7 @@ __device__ __forceinline__ void bc2d_cell(const Params& p, double* __restrict__ 
   const int nx = g.nx, ny = g.ny;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
-  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
   bool gi = (i < 1 || i > nx), gj = (j < 1 || j > ny);
   if (p.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
     // ex6_shock_diffraction/main.f90:895-940 in its order: fixed bottom rows,
@@ -118,7 +118,7 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
   int64_t ncell = (int64_t)g.LI * g.LJ;
   double a = 0.0;
   if (t < ncell) {
-    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
     int64_t o = g.at(i, j);
     const double g1 = p.gamma1, gamma = p.gamma;
     if (g.ndim == 1) {
@@ -127,6 +127,20 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
       double pres = g1 * (u3 - u2 * u2 / u1 / 2.);
       double sound = sqrt(gamma * pres / u1);
       a = fabs(u2 / u1) + sound;
+    } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
+      // FP32-bulk: the same quantities in FP64 with one reciprocal per cell
+      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
+             u4 = ld(u + 3 * g.plane + o);
+      const double ri = 1.0 / u1;
+      double pres;
+      if (!p.alpha_guarded) {
+        pres = g1 * (u4 - 0.5 * (u2 * u2 + u3 * u3) * ri);
+      } else {
+        const double vx = u1 >= p.eps2 ? u2 * ri : 0., vy = u1 >= p.eps2 ? u3 * ri : 0.;
+        pres = g1 * (u4 - 0.5 * u1 * (vx * vx + vy * vy));
+      }
+      const double sound = sqrt(gamma * pres * ri);
+      a = fmax(fabs(u2 * ri), fabs(u3 * ri)) + sound;
     } else {
       double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
              u4 = ld(u + 3 * g.plane + o);
@@ -156,7 +170,7 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
 __device__ __forceinline__ void alpha_store(const Params& p, int64_t t, double a) {
   const Geom& g = p.g;
   if (!p.alpha_plane || t >= (int64_t)g.LI * g.LJ) return;
-  p.alpha_plane[g.at((int)(t % g.LI) - 2, (int)(t / g.LI) - 2)] = a;
+  p.alpha_plane[g.at(((int)t % g.LI) - 2, ((int)t / g.LI) - 2)] = a;
 }
 
 __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
@@ -192,7 +206,7 @@ __device__ __forceinline__ void seg_alpha_item(const Params& p, int64_t t) {
   const Geom& g = p.g;
   const int64_t nrow = (int64_t)g.LJ * p.cut_x;
   if (t < nrow) {
-    const int j = (int)(t / p.cut_x) - 2, sx = (int)(t % p.cut_x);
+    const int j = ((int)t / p.cut_x) - 2, sx = ((int)t % p.cut_x);
     const int i0 = sx * p.nxl - 2, i1 = sx * p.nxl + p.nxl + 3;
     double a = 0.;
     for (int i = i0; i <= i1; ++i) a = fmax(a, p.alpha_plane[g.at(i, j)]);
@@ -201,7 +215,7 @@ __device__ __forceinline__ void seg_alpha_item(const Params& p, int64_t t) {
   }
   t -= nrow;
   if (t >= (int64_t)g.LI * p.cut_y) return;
-  const int i = (int)(t / p.cut_y) - 2, sy = (int)(t % p.cut_y);
+  const int i = ((int)t / p.cut_y) - 2, sy = ((int)t % p.cut_y);
   const int j0 = sy * p.nyl - 2, j1 = sy * p.nyl + p.nyl + 3;
   double a = 0.;
   for (int j = j0; j <= j1; ++j) a = fmax(a, p.alpha_plane[g.at(i, j)]);
@@ -311,12 +325,14 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   const Geom& g = p.g;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
-  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
   const int64_t o = g.at(i, j), P = g.plane;
   const double g1 = p.gamma1;
   double rho = ld(u + o), mx = ld(u + P + o), my = ld(u + 2 * P + o), e = ld(u + 3 * P + o);
+  constexpr bool F32 = sizeof(T) == 4;  // FP32-bulk: FP64 with one reciprocal per cell
+  const double ri = F32 ? 1. / rho : 0.;
   // fflux / gflux
-  double vx = mx / rho, vy = my / rho;
+  double vx = F32 ? mx * ri : mx / rho, vy = F32 ? my * ri : my / rho;
   bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
   if (guard) {
     vx = 0.;
@@ -330,7 +346,19 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   const T h = T(0.5);
   const T tr = T(rho), tmx = T(mx), tmy = T(my), te = T(e);
   const int64_t S = p.sg.plane;
-  if (!p.seg_alpha) {
+  if (!p.seg_alpha && F32) {
+    const T ram = T(1.) / T(amd);
+    T q;
+    q = T(mx) * ram;  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
+    q = T(f1) * ram;  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
+    T qxy = T(fxy) * ram;
+    split[2 * S + o] = h * (tmy + qxy); split[6 * S + o] = h * (tmy - qxy);
+    q = T(f3) * ram;  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
+    q = T(my) * ram;  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
+    split[9 * S + o] = h * (tmx + qxy); split[13 * S + o] = h * (tmx - qxy);
+    q = T(g2) * ram;  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
+    q = T(g3) * ram;  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
+  } else if (!p.seg_alpha) {
     const T am = T(amd);
     T q;
     q = T(mx) / am;  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
@@ -391,7 +419,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   }
   // Roe preparation (x pass; the y pass is the same except in ex4 and ex6)
   if (which & 1) {
-    double t0 = 1. / rho;
+    double t0 = F32 ? ri : 1. / rho;
     double vex = mx * t0, vey = my * t0;
     double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
     roe[0 * P + o] = sqrt_abs<T>(rho);
@@ -638,21 +666,31 @@ __device__ __forceinline__ void count_limited(unsigned long long* cnt, int nd, i
 // the 32 interfaces of chunk c (x chunks first, then y chunks).  SEG: the
 // problem may have rank segments (ex6); without them the face index maps
 // directly to the cell offset.
+// per-launch constants of the flux kernel, converted to T once
+template <class T>
+struct FluxConst {
+  T g1, weps;
+};
+template <class T>
+__device__ __forceinline__ FluxConst<T> flux_const(const Params& p) {
+  return FluxConst<T>{T(p.gamma1), T(p.weno_eps)};
+}
+
 template <class T, bool SEG, bool LIM = false>
 __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict__ split,
                                            const T* __restrict__ roe, T am, T* __restrict__ flux,
                                            int64_t c, int64_t chunks_x, int lane,
-                                           unsigned long long* cnt) {
+                                           unsigned long long* cnt, const FluxConst<T>& cst) {
   const Geom& g = p.g;
   const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
-  const T g1 = T(p.gamma1), weps = T(p.weno_eps);
+  const T g1 = cst.g1, weps = cst.weps;
   {
     T op[4], on[4];
     if (c < chunks_x) {
       int64_t t = (int64_t)c * 32 + lane;
       if (t >= flux_faces_x(p, LIM)) return;
       const int lsx = p.nxl + 2, lx = p.cut_x * lsx;
-      const int r = (int)(t % lx), rr = (int)(t / lx);
+      const int r = ((int)t % lx), rr = ((int)t / lx);
       const int j = LIM ? (rr / (p.nyl + 2)) * p.nyl + rr % (p.nyl + 2) : rr + 1;
       const int sx = SEG ? r / lsx : 0, i = SEG ? sx * p.nxl + r % lsx : r;
       const int64_t o = g.at(i, j), os = SEG ? seg_x_off(p, i, j, sx) : o;
@@ -677,7 +715,7 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
       int64_t t = (int64_t)(c - chunks_x) * 32 + lane;
       if (t >= flux_faces_y(p, LIM)) return;
       const int lsy = p.nyl + 2;
-      const int ncol = (int)flux_cols_y(p, LIM), ci = (int)(t % ncol), r = (int)(t / ncol);
+      const int ncol = (int)flux_cols_y(p, LIM), ci = ((int)t % ncol), r = ((int)t / ncol);
       const int i = LIM ? (ci / (p.nxl + 2)) * p.nxl + ci % (p.nxl + 2) : ci + 1;
       const int sy = SEG ? r / lsy : 0, j = SEG ? sy * p.nyl + r % lsy : r;
       const int64_t o = g.at(i, j), os = SEG ? seg_y_off(p, i, j, sy) : o;
@@ -725,13 +763,14 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
   const int64_t chunks = chunks_x + (flux_faces_y(p, LIM) + 31) / 32;
   const int lane = threadIdx.x & 31;
   const T am = p.alpha_premul ? T(dsc->alphamax) : T(1.0);
+  const FluxConst<T> cst = flux_const<T>(p);
   for (;;) {
     int c = 0;
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
     flux_chunk<T, SEG, LIM>(p, split, roe, am, flux, c, chunks_x, lane,
-                       (unsigned long long*)&dsc->den_count);
+                            (unsigned long long*)&dsc->den_count, cst);
   }
 }
 
@@ -811,9 +850,16 @@ __device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, 
   const T* gnf = flux + (12 + c) * S;
   T A = (ldt(fpf + ox) - ldt(fnf + ox + 1)) - (ldt(fpf + ox - 1) - ldt(fnf + ox));
   T B = (ldt(gpf + oy) - ldt(gnf + oy + pit)) - (ldt(gpf + oy - pit) - ldt(gnf + oy));
-  const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
-  if (p.alpha_premul) return -A / dx - B / dy;  // ex4_sedov_2d/main.f90:644-645
-  return -(am * A) / dx - (am * B) / dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
+  if constexpr (sizeof(T) == 4) {  // FP32-bulk: reciprocals of dx, dy
+    const T ix = p.fdx_inv, iy = p.fdy_inv;
+    if (p.alpha_premul) return -A * ix - B * iy;
+    const T am = T(amd);
+    return -(am * A) * ix - (am * B) * iy;
+  } else {
+    const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
+    if (p.alpha_premul) return -A / dx - B / dy;  // ex4_sedov_2d/main.f90:644-645
+    return -(am * A) / dx - (am * B) / dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
+  }
 }
 
 template <class T>
@@ -849,7 +895,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
   int64_t ncell = (int64_t)g.LI * g.LJ;
   int bad = 0;
   if (t < ncell) {
-    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
     const int64_t o = g.at(i, j), P = g.plane;
     bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
     double nv[4];
@@ -860,6 +906,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
                                    : rhs2d_cell<T>(p, flux, c, i, j, am));
       double v = ld(u + c * P + o) + dt * r;
       if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
+      else if (stage == 3 && sizeof(T) == 4) v = (u0[c * P + o] + 2.0 * v) * (1.0 / 3.0);
       else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
       nv[c] = v;
       out[c * P + o] = v;
@@ -868,8 +915,15 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       // checkpositivity (ex3_vortex_accuracy_2d/main.f90:640-647,
       // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
       double pe;
-      if (g.ndim == 1) pe = nv[2] - nv[1] * nv[1] / nv[0] / 2.;
-      else pe = nv[3] - nv[2] * nv[2] / nv[0] / 2. - nv[1] * nv[1] / nv[0] / 2.;
+      if (sizeof(T) == 4) {  // FP32-bulk: FP64 with one reciprocal
+        const double ri = 0.5 / nv[0];
+        if (g.ndim == 1) pe = nv[2] - nv[1] * nv[1] * ri;
+        else pe = nv[3] - (nv[2] * nv[2] + nv[1] * nv[1]) * ri;
+      } else if (g.ndim == 1) {
+        pe = nv[2] - nv[1] * nv[1] / nv[0] / 2.;
+      } else {
+        pe = nv[3] - nv[2] * nv[2] / nv[0] / 2. - nv[1] * nv[1] / nv[0] / 2.;
+      }
       if (p.pos_strict) bad = (nv[0] < p.eps) || (pe < p.eps);
       else bad = (nv[0] <= p.eps) || (pe <= p.eps);
     }
@@ -907,7 +961,7 @@ __global__ void k_rhs(Params p, const T* __restrict__ flux, const DevScalars* ds
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
-  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
   const int64_t o = g.at(i, j), P = g.plane;
   bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
   for (int c = 0; c < g.nc; ++c) {
@@ -936,7 +990,7 @@ __global__ void k_positivity(Params p, const double* __restrict__ u, DevScalars*
   int64_t ncell = (int64_t)g.LI * g.LJ;
   int bad = 0;
   if (t < ncell) {
-    int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+    int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
     const int64_t o = g.at(i, j), P = g.plane;
     bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
     if (interior) {
@@ -971,7 +1025,7 @@ __global__ void k_f2s(Params p, const double* __restrict__ src, double* __restri
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
-  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
   for (int c = 0; c < g.nc; ++c) dst[c * g.plane + g.at(i, j)] = src[t * g.nc + c];
 }
 __global__ void k_s2f(Params p, const double* __restrict__ src, double* __restrict__ dst) {
@@ -979,7 +1033,7 @@ __global__ void k_s2f(Params p, const double* __restrict__ src, double* __restri
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t ncell = (int64_t)g.LI * g.LJ;
   if (t >= ncell) return;
-  int i = (int)(t % g.LI) - 2, j = (int)(t / g.LI) - 2;
+  int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
   for (int c = 0; c < g.nc; ++c) dst[t * g.nc + c] = src[c * g.plane + g.at(i, j)];
 }
 cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* dst, cudaStream_t s) {
@@ -1111,7 +1165,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     const T am = sl.p.alpha_premul ? T(sl.dsc->alphamax) : T(1.0);
     flux_chunk<T, true>(sl.p, (const T*)sl.split, (const T*)sl.roe, am, (T*)sl.flux, c - prefix[lo],
                   sl.chunks_x, lane,
-                        (unsigned long long*)&sl.dsc->den_count);
+                        (unsigned long long*)&sl.dsc->den_count, flux_const<T>(sl.p));
   }
 }
 

@@ -19,7 +19,7 @@ __global__ void k_rho_min(Params p, const double* __restrict__ u, DevScalars* ds
   int64_t n = (int64_t)g.nx * g.ny;
   double v = 1e20;
   if (t < n) {
-    int i = (int)(t % g.nx) + 1, j = (int)(t / g.nx) + 1;
+    int i = ((int)t % g.nx) + 1, j = ((int)t / g.nx) + 1;
     v = fmin(u[g.at(i, j)], v);
   }
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -352,7 +352,7 @@ __global__ void k_exit_count(Params p, const double* __restrict__ u, DevScalars*
   if (t < n) {
     int64_t o;
     if (g.ndim == 1) o = t;
-    else o = g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1);
+    else o = g.at(((int)t % g.nx) + 1, ((int)t / g.nx) + 1);
     double v[4];
     for (int c = 0; c < g.nc; ++c) v[c] = u[c * g.plane + o];
     double pr = sweep_pres(g, p.gamma1, v);
@@ -600,7 +600,7 @@ __global__ void kb_rho_min(const BatchSlot* __restrict__ tab, int out) {
   double v = 1e20;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x)
-    v = fmin(u[g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1)], v);
+    v = fmin(u[g.at(((int)t % g.nx) + 1, ((int)t / g.nx) + 1)], v);
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
   if ((threadIdx.x & 31) == 0) atomicMin(&sl.dsc->rho_min_key, order_key(v));
 }
@@ -797,7 +797,7 @@ __global__ void kb_ubar(const BatchSlot* __restrict__ tab, int out, int tree) {
   double acc[4] = {0, 0, 0, 0};
   const int64_t n = (int64_t)g.nx * g.ny;
   for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
-    const int64_t o = g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1);
+    const int64_t o = g.at(((int)t % g.nx) + 1, ((int)t / g.nx) + 1);
     for (int c = 0; c < 4; ++c) acc[c] = acc[c] + w * u[c * g.plane + o];
   }
   for (int c = 0; c < 4; ++c) red[c][threadIdx.x] = acc[c];
@@ -859,7 +859,7 @@ __global__ void kb_exit_count(const BatchSlot* __restrict__ tab, int out) {
     int64_t t = base + threadIdx.x;
     int bad = 0;
     if (t < n) {
-      const int64_t o = g.at((int)(t % g.nx) + 1, (int)(t / g.nx) + 1);
+      const int64_t o = g.at(((int)t % g.nx) + 1, ((int)t / g.nx) + 1);
       double v[4];
       for (int c = 0; c < 4; ++c) v[c] = u[c * g.plane + o];
       double pr = sweep_pres(g, p.gamma1, v);

@@ -13,12 +13,12 @@ __device__ __forceinline__ int64_t pos_cell(const Geom& g, int ordering, int64_t
   if (ordering == 0) return pos;  // 1D: position p is cell p-2, offset p
   int i, j;
   if (ordering == 1) {
-    j = (int)(pos / g.nx) + 1;
-    int t = (int)(pos % g.nx);
+    j = ((int)pos / g.nx) + 1;
+    int t = ((int)pos % g.nx);
     i = (j & 1) ? t + 1 : g.nx - t;
   } else {
-    i = (int)(pos / g.ny) + 1;
-    int t = (int)(pos % g.ny);
+    i = ((int)pos / g.ny) + 1;
+    int t = ((int)pos % g.ny);
     j = (i & 1) ? t + 1 : g.ny - t;
   }
   return g.at(i, j);
