@@ -213,7 +213,8 @@ def bench_batched(args, local, flush):
     ms = e0.elapsed_time(e1)
     done = [b.progress(k)[1] - before[k] for k in range(len(sizes))]
     upd = sum(n * n * 3 * d for n, d in zip(sizes, done))
-    value = upd / (ms * 1e-3)
+    from sweeping_fd_weno_gb300.replicas import aggregate
+    value = aggregate(upd, ms * 1e-3)[2]  # every replica's instances over the slowest
     # accuracy: the smallest instances against the FP64 path after the same steps
     check = sorted(range(len(sizes)), key=lambda k: sizes[k])[:3]
     errs = []
@@ -449,12 +450,10 @@ def main():
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
     prof = solver.profile()
     solver.set_profiling(False)
-    t_max = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    total_ms = float(t_max.item())
-    updates = cells * 3 * args.steps * world
-    value = updates / (total_ms * 1e-3)
+    # whole job: every replica's updates over the slowest replica's time
+    from sweeping_fd_weno_gb300.replicas import aggregate
+    updates, max_s, value = aggregate(cells * 3 * args.steps, total_ms * 1e-3)
+    total_ms = max_s * 1e3
 
     # end to end through the public API with host buffers: upload the step's
     # input from pinned memory, step, read the result back
@@ -470,12 +469,9 @@ def main():
         solver.step()
         solver.state(out=hu)
     e2e_s = time.perf_counter() - t0
-    t_e2e = torch.tensor([e2e_s], device=f"cuda:{local}", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(t_e2e, op=dist.ReduceOp.MAX)
-    e2e_s = float(t_e2e.item())
+    _, e2e_s, e2e_value = aggregate(cells * 3 * args.e2e_steps, e2e_s)
     state_bytes = int(np.prod(solver.shape)) * 8
-    e2e = {"value": cells * 3 * args.e2e_steps * world / e2e_s, "unit": UNIT,
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
            "steps": args.e2e_steps}
 
@@ -551,7 +547,7 @@ def main():
         for _ in range(args.steps):
             s64.step()
         r64, r32 = s64.state()[3:-3, 3:-3, 0], s32.state()[3:-3, 3:-3, 0]
-        fp32 = {"value": cells * 3 * args.steps * world / (ms32 * 1e-3),
+        fp32 = {"value": aggregate(cells * 3 * args.steps, ms32 * 1e-3)[2],
                 "ms_per_step": ms32 / args.steps,
                 "speedup_vs_fp64": total_ms / ms32 if ms32 else None,
                 "rel_l1_density_err_vs_fp64": float(np.abs(r32 - r64).sum() / np.abs(r64).sum()),
