@@ -338,35 +338,50 @@ def bench_serving(args, local):
     }
 
 
-def run_reference(args, rank):
-    """The reference's algorithm on the host CPU (its quad-literal build arithmetic)."""
-    if rank != 0:
-        return 0
+def _reference_worker(args):
+    """One serial reference-arithmetic solve (a worker of the reference arm)."""
+    n, warmup, steps = args
     import oracle
     from sweeping_fd_weno_gb300 import problems
-    oracle.build()
-    n = args.reference_nx
-    cfg = problems.workload(f"vortex{n}", literals=1)
-    o = oracle.Oracle(cfg)
+    o = oracle.Oracle(problems.workload(f"vortex{n}", literals=1))
     o.init_problem()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         o.step()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         o.step()
-    el = time.perf_counter() - t0
-    v = n * n * 3 * args.steps / el
+    return n * n * 3 * steps, time.perf_counter() - t0
+
+
+def run_reference(args, rank):
+    """The reference's algorithm on the host CPU: the CPU restatement in its
+    quad-literal mode (the arithmetic of the reference's -fdefault-real-8
+    build).  The reference's vortex program is serial, so every host core runs
+    its own solve; the value is all cores' updates over the slowest core's
+    timed steps."""
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    n = args.reference_nx
+    cores = os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(cores) as pool:
+        out = pool.map(_reference_worker, [(n, args.warmup, args.steps)] * cores)
+    upd = sum(u for u, _ in out)
+    el = max(t for _, t in out)
+    v = upd / el
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex",
         "config": {"workload": "vortex360_fp64", "sample_nx": n, "ny": n},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} SSP-RK3 steps of a {n}x{n} vortex, REAL(16) "
-                                   "literals as the reference's -fdefault-real-8 build; the "
-                                   "reference itself is serial Fortran and no Fortran compiler "
-                                   "exists here"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} SSP-RK3 steps of a {n}x{n} vortex per core "
+                                   f"({cores} independent solves), REAL(16) literals as the "
+                                   "reference's -fdefault-real-8 build; the reference itself is "
+                                   "serial Fortran and no Fortran compiler exists here"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
