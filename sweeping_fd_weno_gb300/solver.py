@@ -148,55 +148,18 @@ class Solver:
 
     # -- output (ex3_vortex_accuracy_2d/main.f90:720-841) ----------------------
     def stats_text(self) -> str:
-        """The statistics block printed by ``output`` (list-directed style)."""
-        s = self.stats()
-        n = max(s["sweep_count"], 1)
-        lines = []
+        """The statistics block printed by ``output`` (list-directed records)."""
+        from .output import stats_block
+        return stats_block(self.stats())
 
-        def line(label, v):
-            if isinstance(v, float):
-                lines.append(f" {label} {_fortran_real(v)}")
-            else:
-                lines.append(f" {label} {v:11d}")
+    def write_output(self, out_dir=".", new_table=False, ierror=None) -> str:
+        """The example's ``output``: its .dat files in out_dir; returns the
+        printed text (errors and orders where computed, then the statistics)."""
+        from .output import write_output
+        return write_output(self, out_dir, new_table=new_table, ierror=ierror)
 
-        line("total sweep = ", s["total_sweep"])
-        line("avg sweep = ", s["total_sweep"] / n if s["sweep_count"] else float("nan"))
-        line("max sweep = ", s["max_sweep"])
-        line("total negative pairs = ", s["total_neg"])
-        line("avg negative pairs = ", s["total_neg"] / n if s["sweep_count"] else float("nan"))
-        line("max negative pairs = ", s["max_neg"])
-        line("total positive neighbors = ", s["total_pos"])
-        line("avg positive neighbors = ", s["total_pos"] / n if s["sweep_count"] else float("nan"))
-        line("max positive neighbors = ", s["max_pos"])
-        lines.append(f" # of limiter {s['den_count']:11d} {s['pre_count']:11d}")
-        return "\n".join(lines) + "\n"
-
-    def write_dat(self, out_dir: str | Path = "."):
-        """den.dat / pre.dat (+ m1.dat, m2.dat in 2D) of the interior cells."""
-        out = Path(out_dir)
-        out.mkdir(parents=True, exist_ok=True)
-        u = self.state()
-        g1 = self.cfg.gamma - 1.0
-        if self.ndim == 1:
-            x = -2.0 + np.arange(1, self.nx + 1) * (4.0 / self.nx) - (4.0 / self.nx) / 2.0
-            r = u[0, 3:self.nx + 3, :]
-            pre = g1 * (r[:, 2] - 0.5 * r[:, 1] ** 2 / r[:, 0])
-            _write_cols(out / "den.dat", [x, r[:, 0]])
-            _write_cols(out / "pre.dat", [x, pre])
-            _write_cols(out / "vel.dat", [x, r[:, 1] / r[:, 0]])
-            return
-        dx = self._dx()
-        dy = self._dy()
-        rows = u[3:self.ny + 3, 3:self.nx + 3, :]
-        jj, ii = np.meshgrid(np.arange(1, self.ny + 1), np.arange(1, self.nx + 1), indexing="ij")
-        x = dx * (ii - 0.5)
-        y = dy * (jj - 0.5)
-        rho, m1, m2, e = (rows[..., c] for c in range(4))
-        pre = g1 * (e - 0.5 * m1 ** 2 / rho - 0.5 * m2 ** 2 / rho)
-        _write_cols(out / "den.dat", [x.ravel(), y.ravel(), rho.ravel()])
-        _write_cols(out / "pre.dat", [x.ravel(), y.ravel(), pre.ravel()])
-        _write_cols(out / "m1.dat", [x.ravel(), y.ravel(), m1.ravel()])
-        _write_cols(out / "m2.dat", [x.ravel(), y.ravel(), m2.ravel()])
+    def write_dat(self, out_dir=".") -> str:
+        return self.write_output(out_dir)
 
     def _dx(self):
         p = self.cfg.problem
@@ -204,6 +167,8 @@ class Solver:
             return 10.0 / self.nx
         if p == abi.SEDOV_2D:
             return 1.3 / self.nx
+        if p == abi.SHOCK_DIFFRACTION:  # (13/cut_x - 0)/nxl, the same for every rank
+            return (13.0 / self.cfg.cut_x) / (self.nx // self.cfg.cut_x)
         return 1.0 / self.nx
 
     def _dy(self):
@@ -212,22 +177,8 @@ class Solver:
             return 10.0 / self.ny
         if p == abi.SEDOV_2D:
             return 1.3 / self.ny
+        if p == abi.SHOCK_DIFFRACTION:
+            return (11.0 / self.cfg.cut_y) / (self.ny // self.cfg.cut_y)
         return 0.25 / self.ny
 
 
-def _fortran_real(v: float) -> str:
-    """gfortran list-directed REAL(8): 0.1 <= |v| < 1e16 as F, else E with 3-digit exponent."""
-    if v != v:
-        return "             NaN"
-    a = abs(v)
-    if a != 0.0 and (a < 0.1 or a >= 1e16):
-        m, e = f"{v:.16E}".split("E")
-        return f"{m}E{int(e):+04d}"
-    digits = 17 - (len(str(int(a))) if a >= 1 else 0)
-    return f"{v:.{max(digits, 1)}f}"
-
-
-def _write_cols(path: Path, cols):
-    with open(path, "w") as f:
-        for row in zip(*cols):
-            f.write("".join(f"  {_fortran_real(float(v))}" for v in row) + "\n")
