@@ -272,6 +272,44 @@ def bench_batched(args, local, flush):
     }
 
 
+def bench_batched_full(args, local):
+    """The point-energy configuration run to completion: every instance to
+    T = 1 in the batched engine (graph launches of --batch-chunk steps, each
+    instance retiring at its own time); wall time, whole-run cell-updates/s and
+    the instances' completion times."""
+    import numpy as np
+    from sweeping_fd_weno_gb300 import Batch, abi, problems
+    sizes = point_energy_sizes(args.batch_instances)
+    b = Batch(max_slots=len(sizes), max_nx=640, max_ny=640,
+              precision=abi.PRECISION_FP32_BULK, ubar_mode=abi.UBAR_TREE, device=local)
+    for k, n in enumerate(sizes):
+        if not b.admit(problems.make_config(abi.SEDOV_2D, nx=n, ny=n, device=local), k):
+            raise RuntimeError(f"instance {k} not admitted")
+    t0 = time.perf_counter()
+    done, steps_of, status = {}, {}, {}
+    launches = 0
+    while len(done) < len(sizes):
+        b.run(args.batch_chunk)
+        launches += 1
+        for rid, st in b.poll():
+            done[rid] = time.perf_counter() - t0
+            steps_of[rid] = b.progress(rid)[1]
+            status[rid] = st
+        if time.perf_counter() - t0 > args.batch_full_timeout:
+            break
+    wall = time.perf_counter() - t0
+    upd = sum(sizes[k] ** 2 * 3 * steps_of[k] for k in done)
+    b.close()
+    t = np.array(sorted(done.values()))
+    return {"workload": f"{len(sizes)} point-energy instances 128^2..640^2 to T=1, FP32-bulk",
+            "finished": len(done), "failed": sum(1 for v in status.values() if v != 0),
+            "wall_s": wall, "cell_updates": upd, "value": upd / wall, "unit": UNIT,
+            "graph_launches": launches, "steps_per_launch": args.batch_chunk,
+            "steps_min_max": [min(steps_of.values()), max(steps_of.values())] if steps_of else None,
+            "completion_p50_s": float(np.percentile(t, 50)) if len(t) else None,
+            "completion_p99_s": float(np.percentile(t, 99)) if len(t) else None}
+
+
 def serving_draw(device, plain_fp64=False):
     """Requests of the serving mix, drawn uniformly from three problems: the
     vortex (45^2..360^2, T=0.01), a point-energy instance (128^2..640^2,
@@ -412,6 +450,10 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-chunk", type=int, default=4)
+    ap.add_argument("--batch-full", action="store_true",
+                    help="also run the point-energy batch to T=1 (minutes)")
+    ap.add_argument("--batch-chunk", type=int, default=64)
+    ap.add_argument("--batch-full-timeout", type=float, default=1800.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -596,6 +638,8 @@ def main():
                 point_energy_sizes(args.batch_instances))
     if not args.no_serving:
         line["serving"] = bench_serving(args, local)
+    if args.batch_full:
+        line["batched_to_completion"] = bench_batched_full(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
     if rank == 0:

@@ -134,10 +134,10 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
       const double ri = 1.0 / u1;
       double pres;
       if (!p.alpha_guarded) {
-        pres = g1 * (u4 - 0.5 * (u2 * u2 + u3 * u3) * ri);
+        pres = g1 * fma(-0.5 * ri, fma(u2, u2, u3 * u3), u4);
       } else {
         const double vx = u1 >= p.eps2 ? u2 * ri : 0., vy = u1 >= p.eps2 ? u3 * ri : 0.;
-        pres = g1 * (u4 - 0.5 * u1 * (vx * vx + vy * vy));
+        pres = g1 * fma(-0.5 * u1, fma(vx, vx, vy * vy), u4);
       }
       const double sound = sqrt(gamma * pres * ri);
       a = fmax(fabs(u2 * ri), fabs(u3 * ri)) + sound;
@@ -331,6 +331,52 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   double rho = ld(u + o), mx = ld(u + P + o), my = ld(u + 2 * P + o), e = ld(u + 3 * P + o);
   constexpr bool F32 = sizeof(T) == 4;  // FP32-bulk: FP64 with one reciprocal per cell
   const double ri = F32 ? 1. / rho : 0.;
+  if constexpr (F32) {
+    if (!p.seg_alpha) {
+      // FP32-bulk: the pressure recovered in FP64 (fused multiply-adds, one
+      // reciprocal), the fluxes and the splitting in FP32; the Roe enthalpy
+      // reuses the recovered pressure
+      double vx = mx * ri, vy = my * ri;
+      const bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
+      if (guard) vx = vy = 0.;
+      const double pres = g1 * fma(-0.5 * rho, fma(vx, vx, vy * vy), e);
+      const float fr = (float)rho, fm = (float)mx, fn = (float)my, fe = (float)e;
+      const float fvx = (float)vx, fvy = (float)vy, fp = (float)pres;
+      const float fxy = fr * fvx * fvy;
+      const float f1 = fmaf(fr * fvx, fvx, fp), f3 = (fe + fp) * fvx;
+      const float g2 = fmaf(fr * fvy, fvy, fp), g3 = (fe + fp) * fvy;
+      const float ram = 1.f / (float)amd, hf = 0.5f;
+      const int64_t S = p.sg.plane;
+      float q;
+      q = fm * ram;  split[0 * S + o] = hf * (fr + q);  split[4 * S + o] = hf * (fr - q);
+      q = f1 * ram;  split[1 * S + o] = hf * (fm + q);  split[5 * S + o] = hf * (fm - q);
+      const float qxy = fxy * ram;
+      split[2 * S + o] = hf * (fn + qxy); split[6 * S + o] = hf * (fn - qxy);
+      q = f3 * ram;  split[3 * S + o] = hf * (fe + q);  split[7 * S + o] = hf * (fe - q);
+      q = fn * ram;  split[8 * S + o] = hf * (fr + q);  split[12 * S + o] = hf * (fr - q);
+      split[9 * S + o] = hf * (fm + qxy); split[13 * S + o] = hf * (fm - qxy);
+      q = g2 * ram;  split[10 * S + o] = hf * (fn + q); split[14 * S + o] = hf * (fn - q);
+      q = g3 * ram;  split[11 * S + o] = hf * (fe + q); split[15 * S + o] = hf * (fe - q);
+      if (which & 1) {
+        const double vex = guard ? mx * ri : vx, vey = guard ? my * ri : vy;
+        const double pre = guard ? g1 * fma(-0.5, fma(mx, vex, my * vey), e) : pres;
+        roe[0 * P + o] = sqrtf(fabsf(fr));
+        roe[1 * P + o] = (float)vex;
+        roe[2 * P + o] = (float)vey;
+        roe[3 * P + o] = (float)((pre + e) * ri);
+      }
+      if (p.roe_reg_ex4 && (which & 2)) {  // ex4_sedov_2d/main.f90:426
+        const double t0 = 1. / (rho + 1e-15);
+        const double vex = mx * t0, vey = my * t0;
+        const double pre = g1 * fma(-0.5, fma(mx, vex, my * vey), e);
+        roe[4 * P + o] = sqrtf(fabsf(fr));
+        roe[5 * P + o] = (float)vex;
+        roe[6 * P + o] = (float)vey;
+        roe[7 * P + o] = (float)((pre + e) * t0);
+      }
+      return;
+    }
+  }
   // fflux / gflux
   double vx = F32 ? mx * ri : mx / rho, vy = F32 ? my * ri : my / rho;
   bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
@@ -904,10 +950,16 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       if (interior)
         r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am)
                                    : rhs2d_cell<T>(p, flux, c, i, j, am));
-      double v = ld(u + c * P + o) + dt * r;
-      if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
-      else if (stage == 3 && sizeof(T) == 4) v = (u0[c * P + o] + 2.0 * v) * (1.0 / 3.0);
-      else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+      double v;
+      if (sizeof(T) == 4) {  // FP32-bulk: the FP64 accumulation with fused multiply-adds
+        v = fma(dt, r, ld(u + c * P + o));
+        if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
+        else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
+      } else {
+        v = ld(u + c * P + o) + dt * r;
+        if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
+        else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+      }
       nv[c] = v;
       out[c * P + o] = v;
     }
@@ -916,9 +968,9 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
       double pe;
       if (sizeof(T) == 4) {  // FP32-bulk: FP64 with one reciprocal
-        const double ri = 0.5 / nv[0];
-        if (g.ndim == 1) pe = nv[2] - nv[1] * nv[1] * ri;
-        else pe = nv[3] - (nv[2] * nv[2] + nv[1] * nv[1]) * ri;
+        const double ri = -0.5 / nv[0];
+        if (g.ndim == 1) pe = fma(nv[1] * nv[1], ri, nv[2]);
+        else pe = fma(fma(nv[2], nv[2], nv[1] * nv[1]), ri, nv[3]);
       } else if (g.ndim == 1) {
         pe = nv[2] - nv[1] * nv[1] / nv[0] / 2.;
       } else {
