@@ -47,6 +47,8 @@ FLUX_FP64_INST_PER_INTERFACE = 1197
 # DRAM bytes of one k_flux_xy<double> launch per interior cell, from an ncu
 # capture of the 1024x1024 vortex (313.6 MB per launch, inputs above L2)
 FLUX_DRAM_BYTES_PER_CELL = 313.6e6 / (1024 * 1024)
+# the same for k_flux_xy<float> of the FP32-bulk form (134.4 MB per launch)
+FLUX_F32_DRAM_BYTES_PER_CELL = 134.4e6 / (1024 * 1024)
 
 
 def env_int(k, d):
@@ -547,32 +549,46 @@ def main():
     # per launch (both directions of one stage): read the split fluxes (8
     # doubles) and Roe averages (4 doubles) of every cell once per direction,
     # write 8 doubles per interface
-    launch_bytes = 2 * cells * (12 + 8) * 8.0
+    f32 = args.precision != "fp64"
+    launch_bytes = 2 * cells * (12 + 8) * (4.0 if f32 else 8.0)
     achieved = launch_bytes / (flux_ms_per_launch * 1e-3) / 1e9
-    launch_inst = 2 * cells * FLUX_FP64_INST_PER_INTERFACE
-    fp64_inst_rate = launch_inst / (flux_ms_per_launch * 1e-3) / 1e9
-    fp64_peak_inst = fp64.value / 2.0  # the probe counts a DFMA as 2 flops
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak,
-        "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_flux_xy<double> "
-                          "on the 1024x1024 vortex (313.6 MB), scaled per cell to this grid",
         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-        "kernel": "k_flux_xy (characteristic WENO5 interface fluxes, both directions)",
         "launch_ms": flux_ms_per_launch,
-        "compute_bound": "fp64",
-        "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,
-                 "frac": fp64_inst_rate / fp64_peak_inst if fp64_peak_inst else None,
-                 "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains; 2 flops each)",
-                 "inst_per_interface": FLUX_FP64_INST_PER_INTERFACE,
-                 "achieved_gflops_source_count": 2 * cells * FLUX_FLOPS_PER_INTERFACE
-                 / (flux_ms_per_launch * 1e-3) / 1e9,
-                 "flops_per_interface": FLUX_FLOPS_PER_INTERFACE},
         "stage_hbm": {"achieved": STAGE_BYTES_PER_CELL * value / 1e9, "peak": hbm_peak,
                       "frac": STAGE_BYTES_PER_CELL * value / 1e9 / hbm_peak,
                       "bytes_per_cell_stage": STAGE_BYTES_PER_CELL},
     }
+    if not f32:
+        launch_inst = 2 * cells * FLUX_FP64_INST_PER_INTERFACE
+        fp64_inst_rate = launch_inst / (flux_ms_per_launch * 1e-3) / 1e9
+        fp64_peak_inst = fp64.value / 2.0  # the probe counts a DFMA as 2 flops
+        roofline.update({
+            "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                              "k_flux_xy<double> on the 1024x1024 vortex (313.6 MB), scaled "
+                              "per cell to this grid",
+            "kernel": "k_flux_xy<double> (characteristic WENO5 interface fluxes, both directions)",
+            "compute_bound": "fp64",
+            "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,
+                     "frac": fp64_inst_rate / fp64_peak_inst if fp64_peak_inst else None,
+                     "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains; 2 flops "
+                                    "each)",
+                     "inst_per_interface": FLUX_FP64_INST_PER_INTERFACE,
+                     "achieved_gflops_source_count": 2 * cells * FLUX_FLOPS_PER_INTERFACE
+                     / (flux_ms_per_launch * 1e-3) / 1e9,
+                     "flops_per_interface": FLUX_FLOPS_PER_INTERFACE}})
+    else:
+        roofline.update({
+            "traffic": FLUX_F32_DRAM_BYTES_PER_CELL * cells,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                              "k_flux_xy<float> on the 1024x1024 vortex (134.4 MB), scaled "
+                              "per cell to this grid",
+            "kernel": "k_flux_xy<float> (characteristic WENO5 interface fluxes, both directions)",
+            "compute_bound": "none: latency-bound (ncu on the 1024x1024 vortex: FMA pipe "
+                             "35 %, DRAM 9 %, issue 55 % active, long-scoreboard stalls)"})
     # the FP32-bulk precision form on the same workload, from the same state:
     # timed the same way, with its relative L1 density error against FP64
     fp32 = None

@@ -447,12 +447,8 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
                 bool events) {
   swfd_handle* h = b.h;
   const Params& p = h->p;
-  B_OK(b, launch_alpha(p, in, h->dsc, s));
-  b.k(2);
-  if (k == 1) {
-    B_OK(b, launch_dt(p, h->dsc, s));
-    b.k(1);
-  }
+  B_OK(b, launch_alpha(p, in, h->dsc, s, k == 1));
+  b.k(1);
   {
     int nk = 0;
     B_OK(b, launch_split(p, in, h->dsc, h->split, h->roe, s, &nk));
@@ -469,12 +465,11 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
     B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1) + 1], s)
                     : cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s,
                                                cudaEventRecordExternal));
-  B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s));
+  const bool sweeps = h->cfg.use_limiter == 2;
+  const cudaGraphConditionalHandle hs = sweeps ? b.handle() : 0;
+  B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s, hs, sweeps));
   b.k(1);
-  if (h->cfg.use_limiter == 2) {
-    cudaGraphConditionalHandle hs = b.handle();
-    B_OK(b, launch_cond_postag(hs, h->dsc, s));
-    b.k(1);
+  if (sweeps) {
     int* saved = b.count;
     h->k_sweep_fixed = 0;  // every stage emits the same sweep: count it once
     b.count = &h->k_sweep_fixed;

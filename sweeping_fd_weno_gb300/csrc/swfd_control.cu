@@ -11,11 +11,6 @@ __device__ __forceinline__ double decode_key(unsigned long long k) {
   return __longlong_as_double((long long)b);
 }
 
-// IF postag == 1 (ex3_vortex_accuracy_2d/main.f90:590-595)
-__global__ void k_cond_postag(cudaGraphConditionalHandle h, DevScalars* d) {
-  set_cond(h, &d->cond, d->postag ? 1u : 0u);
-}
-
 // IF rho_min < 1d-12 (ex3_vortex_accuracy_2d/main.f90:1155-1156); den_count (:1187)
 __global__ void k_cond_density(cudaGraphConditionalHandle h, DevScalars* d) {
   bool go = decode_key(d->rho_min_key) < 1e-12;
@@ -97,10 +92,6 @@ __global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d,
   set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
-cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s) {
-  k_cond_postag<<<1, 1, 0, s>>>(h, d);
-  return cudaGetLastError();
-}
 cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s) {
   k_cond_density<<<1, 1, 0, s>>>(h, d);
   return cudaGetLastError();

@@ -5,7 +5,6 @@
 
 namespace swfd {
 
-cudaError_t launch_cond_postag(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s);
 cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s);
 cudaError_t launch_count_density(DevScalars* d, cudaStream_t s);
 cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, DevScalars* d,

@@ -139,6 +139,7 @@ struct DevScalars {
   int q;                 // current sweep iteration (1-based)
   int ordering;          // ordering of the current pass (0: 1D, 1: I, 2: II)
   int flux_work;         // chunk counter of the persistent flux kernel
+  int flux_done;         // its warps that found the chunks exhausted (follows flux_work)
   long long t_pos, t_neg;
   long long sweep_count, den_count, pre_count, fail_count;
   long long steps;        // steps taken by the current solve launch
@@ -150,6 +151,8 @@ struct DevScalars {
   int dens_active;        // this instance runs the density sweep of this stage
   double t_end;           // time_terminal of the instance
   int cond;               // eager launch mode: value of the last conditional decision
+  int alpha_done;         // findalpha blocks finished (the last one re-arms it)
+  int rk_done;            // RK-stage blocks finished (the last one re-arms it)
 };
 
 // The value of a conditional node: set on the graph's handle, or written to
@@ -188,6 +191,8 @@ struct BatchCtl {
   long long steps;        // steps taken by the current launch
   long long steps_limit;
   int cond;               // eager launch mode: value of the last conditional decision
+  int alpha_done;         // findalpha blocks finished (the last one re-arms it)
+  int rk_done;            // RK-stage blocks finished (the last one re-arms it)
 };
 
 // What a batched launch needs (host side).
@@ -257,18 +262,23 @@ void init_host_state(const Params& p, const swfd_config& cfg, double* u);
 
 // kernels.cu
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
-cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
+// findalpha into dsc->alphamax; with_dt: the dt rule follows (stage 1).
+// dsc's alpha_bits and alpha_done are zero between launches.
+cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
+                         bool with_dt = false);
 // split, roe and flux planes hold doubles (FP64) or floats (FP32 bulk)
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
                         void* roe, cudaStream_t s, int which = 3);
 cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void* split, void* roe,
                          cudaStream_t s, int* nk);
-// work: one device int of scratch (the chunk counter of the 2D kernel)
+// work: two device ints, zero between launches (the chunk counter of the 2D
+// kernel and its count of finished warps; the kernel leaves them zero)
 cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
                         const DevScalars* dsc, void* flux, int* work, cudaStream_t s);
-cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s);
+// decide: set the IF condition hs (0: the condition word) from postag
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
-                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s);
+                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
+                      cudaGraphConditionalHandle hs, bool decide);
 cudaError_t launch_rhs(const Params& p, const void* flux, const DevScalars* dsc, double* rhs,
                        cudaStream_t s);
 cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);

@@ -173,26 +173,42 @@ __device__ __forceinline__ void alpha_store(const Params& p, int64_t t, double a
   p.alpha_plane[g.at(((int)t % g.LI) - 2, ((int)t / g.LI) - 2)] = a;
 }
 
-__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double a = alpha_cell(p, u, t);
-  alpha_store(p, t, a);
-  a = block_max(a);
-  if (threadIdx.x == 0) atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
-}
-
 __device__ __forceinline__ void alpha_final_body(DevScalars* dsc) {
   dsc->alphamax = __longlong_as_double((long long)dsc->alpha_bits);
   if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
 }
-__global__ void k_alpha_final(DevScalars* dsc) { alpha_final_body(dsc); }
 
-cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(&dsc->alpha_bits, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
+__device__ __forceinline__ void dt_body(const Params& p, DevScalars* dsc);
+
+// Every block folds its maximum into alpha_bits (alpha >= 0, so the bit
+// patterns order as the values do).  The last block to finish turns the
+// maximum into alphamax -- and, after the stage-1 findalpha, into dt -- and
+// re-arms the accumulator and the block counter for the next launch, so a
+// stage needs neither a reset nor a single-thread finishing kernel.  It also
+// clears postag, which the RK kernel of the same stage accumulates.
+__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc, int with_dt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double a = alpha_cell(p, u, t);
+  alpha_store(p, t, a);
+  a = block_max(a);
+  if (threadIdx.x != 0) return;
+  atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+  __threadfence();
+  if (atomicAdd(&dsc->alpha_done, 1) != (int)gridDim.x - 1) return;
+  __threadfence();
+  const unsigned long long m = atomicExch(&dsc->alpha_bits, 0ull);
+  dsc->alpha_done = 0;
+  dsc->postag = 0;
+  dsc->alphamax = __longlong_as_double((long long)m);
+  if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
+  if (with_dt) dt_body(p, dsc);
+}
+
+cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
+                         bool with_dt) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
-  k_alpha<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc);
-  k_alpha_final<<<1, 1, 0, s>>>(dsc);
+  k_alpha<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc,
+                                                                               with_dt ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -281,12 +297,6 @@ __device__ __forceinline__ void dt_body(const Params& p, DevScalars* dsc) {
   }
   dsc->dt = dt;
   if (!isfinite(dt)) dsc->error |= 2;
-}
-__global__ void k_dt(Params p, DevScalars* dsc) { dt_body(p, dsc); }
-
-cudaError_t launch_dt(const Params& p, DevScalars* dsc, cudaStream_t s) {
-  k_dt<<<1, 1, 0, s>>>(p, dsc);
-  return cudaGetLastError();
 }
 
 __global__ void k_time_advance(DevScalars* dsc) { dsc->time = dsc->time + dsc->dt; }
@@ -818,6 +828,16 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
     flux_chunk<T, SEG, LIM>(p, split, roe, am, flux, c, chunks_x, lane,
                             (unsigned long long*)&dsc->den_count, cst);
   }
+  // work[1] counts the warps that found the chunks exhausted: the last one
+  // out re-arms both counters for the next launch (every other warp's final
+  // fetch precedes its increment of work[1])
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(work + 1, 1) == (int)(gridDim.x * (blockDim.x >> 5)) - 1) {
+      atomicExch(work, 0);
+      atomicExch(work + 1, 0);
+    }
+  }
 }
 
 template <class T>
@@ -866,8 +886,6 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
                                            (double*)flux);
     return cudaGetLastError();
   }
-  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
   if (f32)
     launch_flux_xy<float>(p, split, roe, dsc, flux, work, s);
   else
@@ -983,26 +1001,38 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
   return bad;
 }
 
+// postag starts the stage at 0 (findalpha clears it).  The last block to
+// finish takes the stage's positivity decision: where the stage sweeps it
+// sets the sweep's IF condition from postag
+// (ex3_vortex_accuracy_2d/main.f90:590-595).
 template <class T>
 __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
-                     const T* __restrict__ flux, DevScalars* dsc, double* out) {
+                     const T* __restrict__ flux, DevScalars* dsc, double* out,
+                     cudaGraphConditionalHandle hs, int decide) {
   int bad = rk_cell<T>(p, stage, u, u0, flux, dsc->dt, dsc->alphamax, out,
                        (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
-  if (block_or(bad) && threadIdx.x == 0) atomicOr(&dsc->postag, 1);
+  bad = block_or(bad);
+  if (threadIdx.x != 0) return;
+  if (bad) atomicOr(&dsc->postag, 1);
+  __threadfence();
+  if (atomicAdd(&dsc->rk_done, 1) != (int)gridDim.x - 1) return;
+  __threadfence();
+  const int tag = atomicOr(&dsc->postag, 0);
+  dsc->rk_done = 0;
+  if (decide) set_cond(hs, &dsc->cond, tag ? 1u : 0u);
 }
 
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
-                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s) {
+                      const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
+                      cudaGraphConditionalHandle hs, bool decide) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
-  cudaError_t e = cudaMemsetAsync((void*)&dsc->postag, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
   const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
   if (p.precision == SWFD_PRECISION_FP32_BULK)
     k_rk<float><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const float*)flux,
-                                          const_cast<DevScalars*>(dsc), out);
+                                          const_cast<DevScalars*>(dsc), out, hs, decide ? 1 : 0);
   else
     k_rk<double><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const double*)flux,
-                                           const_cast<DevScalars*>(dsc), out);
+                                           const_cast<DevScalars*>(dsc), out, hs, decide ? 1 : 0);
   return cudaGetLastError();
 }
 
