@@ -46,10 +46,17 @@ enum {
   SWFD_ERR_TIMEOUT = -7,        /* a bounded device-side wait expired */
   SWFD_ERR_UNSUPPORTED = -8,    /* option recognised but not implemented */
   SWFD_ERR_MAX_STEPS = -9,      /* run_to stopped at its step limit */
-  SWFD_ERR_SWEEP_CHECK = -10    /* a nodal adjustment raised the pair's total
+  SWFD_ERR_SWEEP_CHECK = -10,   /* a nodal adjustment raised the pair's total
                                    pressure (ex6_shock_diffraction/main.f90:1413-1423,
                                    1472-1482 `stop`) */
+  SWFD_ERR_RESTART_LIMIT = -11  /* the dt-halving restart RK (rk_choice 2) found no
+                                   positive state within SWFD_RESTART_LIMIT halvings;
+                                   the reference would loop on (ex2_sedov_1d/main.f90:
+                                   340-348 `goto 110`) */
 };
+
+/* Bound on the dt halvings of one restart-RK step (dt/2^1100 is 0). */
+#define SWFD_RESTART_LIMIT 1100
 
 /* Problem = one reference example, with all of its per-example switches
  * (operation order, epsilons, comparison operators, boundary conditions). */
@@ -91,8 +98,8 @@ typedef struct swfd_config {
   int32_t abi_version;   /* must be SWFD_ABI_VERSION */
   int32_t problem;       /* SWFD_PROBLEM_* */
   int32_t nx, ny;        /* interior cells; ny is ignored in 1D */
-  int32_t use_limiter;   /* 2 = sweeping (reference default), 0 = none;
-                            1 (Zhang-Shu flux limiter) -> SWFD_ERR_UNSUPPORTED */
+  int32_t use_limiter;   /* 2 = sweeping (reference default), 0 = none,
+                            1 = Zhang-Shu positivity-preserving flux limiter */
   int32_t swp_num;       /* max forward/backward sweep pairs per RK stage */
   int32_t literals;      /* SWFD_LITERALS_* */
   int32_t precision;     /* SWFD_PRECISION_* */
@@ -109,7 +116,12 @@ typedef struct swfd_config {
                             cells; the step top is row 6*total); 0 otherwise */
   int32_t cut_x, cut_y;  /* shock diffraction: the reference's rank grid (4 x 8);
                             nx = cut_x*(13*total/cut_x), ny = cut_y*(11*total/cut_y) */
-  int32_t reserved[4];   /* zero */
+  int32_t rk_choice;     /* the reference's RK_choice: 1 (or 0) = SSP-RK3 with the
+                            sweeping post-process (rk3); 2 = the dt-halving
+                            restart RK of ex2 (`rk`, ex2_sedov_1d/main.f90:330-374:
+                            a stage that fails checkpositivity restarts the step
+                            from u0 with dt/2; no sweeps).  2 is 1D only. */
+  int32_t reserved[3];   /* zero */
 } swfd_config;
 
 /* Sweep statistics exactly as the reference counts them
@@ -161,6 +173,10 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out);
  * (ex3_vortex_accuracy_2d/main.f90:51-56), bounded by max_steps (<= 0: none).
  * nsteps_out may be NULL. */
 swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out);
+
+/* Restart RK (rk_choice 2): dt halvings over all steps so far (the
+ * `goto 110` restarts of ex2_sedov_1d/main.f90:350,360,370); 0 otherwise. */
+swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts);
 
 /* sweep_lim on the current state, as called after an RK stage whose
  * checkpositivity flagged a cell (ex3_vortex_accuracy_2d/main.f90:888-1137). */

@@ -41,6 +41,7 @@ def load():
         "oracle_get_time": (C.c_double, [P]),
         "oracle_set_time": (None, [P, C.c_double]),
         "oracle_get_dt": (C.c_double, [P]),
+        "oracle_get_restarts": (C.c_int64, [P]),
         "oracle_get_alphamax": (C.c_double, [P]),
         "oracle_get_dx": (C.c_double, [P]),
         "oracle_get_dy": (C.c_double, [P]),
@@ -117,6 +118,11 @@ class Oracle:
     @property
     def dt(self):
         return self.lib.oracle_get_dt(self.o)
+
+    @property
+    def restarts(self):
+        """dt halvings of the restart RK (rk_choice 2) over all steps"""
+        return self.lib.oracle_get_restarts(self.o)
 
     @property
     def dx(self):

@@ -61,6 +61,7 @@ typedef struct oracle {
   /* statistics (ex3_vortex_accuracy_2d/main.f90:14,24-31) */
   int64_t sweep_count, den_count, pre_count, fail_count;
   int64_t t_pos_count, t_neg_count;
+  int64_t restarts;       /* restart RK: dt halvings of all steps */
   int32_t *sweep_track, *neg_track, *pos_track;
   int64_t track_cap;
   int status;
@@ -1432,8 +1433,53 @@ static void ex6_init(oracle* o) {
 }
 
 /* rk / rk3 (ex3_vortex_accuracy_2d/main.f90:564-632; ex2_sedov_1d/main.f90:287-328) */
+/* The dt-halving restart RK of ex2 (RK_choice /= 1, ex2_sedov_1d/main.f90:
+ * 330-374).  A stage whose result fails checkpositivity sends the step back to
+ * label 110: u = u0, dt = dt/2, alphamax = alphatemp, and stage 1 is redone
+ * with the fluxes of the last wenofd (the reference does not call wenofd
+ * again there).  No sweeps; ex2's bc is empty.  The reference loops without
+ * bound; here SWFD_RESTART_LIMIT halvings end the step with an error. */
+static int step_restart1d(oracle* o) {
+  const size_t n = state_len(o);
+  double* u = o->u;
+  wenofd_any(o);
+  compute_dt(o);
+  const double alphatemp = o->alphamax;
+  int postag = 0, restarts = 0;
+  for (;;) {
+    if (postag == 1) {
+      if (restarts >= SWFD_RESTART_LIMIT) return o->status = SWFD_ERR_RESTART_LIMIT;
+      ++restarts;
+      memcpy(u, o->u0, n * sizeof(double));
+      o->dt = o->dt / 2.;
+      o->alphamax = alphatemp;
+    }
+    memcpy(o->u0, u, n * sizeof(double));
+    int stage;
+    for (stage = 1; stage <= 3; ++stage) {
+      if (stage > 1) wenofd_any(o);
+      scheme_any(o);
+      const double dt = o->dt;
+      for (size_t k = 0; k < n; ++k) {
+        double v = u[k] + dt * o->rhs[k];
+        if (stage == 1) u[k] = v;
+        else if (stage == 2) u[k] = rk2(o, o->u0[k], v);
+        else u[k] = rk3(o, o->u0[k], v);
+      }
+      postag = check_any(o);
+      if (postag == 1) break;
+    }
+    if (stage > 3) break;
+  }
+  o->restarts += restarts;
+  o->postag = 0;
+  o->time = o->time + o->dt;
+  return SWFD_OK;
+}
+
 int oracle_step(oracle* o) {
   if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) return ex6_step(o);
+  if (o->cfg.rk_choice == 2) return step_restart1d(o);
   const size_t n = state_len(o);
   double* u = o->u;
   int st;
@@ -1667,6 +1713,7 @@ void oracle_set_state(oracle* o, const double* in) {
 double oracle_get_time(const oracle* o) { return o->time; }
 void oracle_set_time(oracle* o, double t) { o->time = t; }
 double oracle_get_dt(const oracle* o) { return o->dt; }
+int64_t oracle_get_restarts(const oracle* o) { return o->restarts; }
 double oracle_get_alphamax(const oracle* o) { return o->alphamax; }
 double oracle_get_dx(const oracle* o) { return o->dx; }
 double oracle_get_dy(const oracle* o) { return o->dy; }

@@ -25,6 +25,8 @@ ERR_TIMEOUT = -7
 ERR_UNSUPPORTED = -8
 ERR_MAX_STEPS = -9
 ERR_SWEEP_CHECK = -10
+ERR_RESTART_LIMIT = -11
+RESTART_LIMIT = 1100
 
 # problems (one per reference example)
 SEDOV_1D = 2   # ex2_sedov_1d
@@ -64,7 +66,8 @@ class SwfdConfig(C.Structure):
         ("total", C.c_int32),
         ("cut_x", C.c_int32),
         ("cut_y", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("rk_choice", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
     def as_dict(self) -> dict:
@@ -116,6 +119,7 @@ _SIGS = {
     "swfd_get_time": (C.c_int32, [_P, _DP]),
     "swfd_set_time": (C.c_int32, [_P, C.c_double]),
     "swfd_get_sweep_stats": (C.c_int32, [_P, C.POINTER(SwfdSweepStats)]),
+    "swfd_get_restarts": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "swfd_get_sweep_tracks": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32), C.c_int64,
                                           C.POINTER(C.c_int64)]),

@@ -39,6 +39,9 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
   if (c.sweep_mode != SWFD_SWEEP_PARALLEL && c.sweep_mode != SWFD_SWEEP_SEQUENTIAL)
     return bad(SWFD_ERR_INVALID, "unknown sweep_mode");
   if (!(c.gamma > 1.0)) return bad(SWFD_ERR_INVALID, "gamma must be > 1");
+  if (c.rk_choice < 0 || c.rk_choice > 2) return bad(SWFD_ERR_INVALID, "rk_choice must be 0, 1 or 2");
+  if (c.rk_choice == 2 && c.problem != SWFD_PROBLEM_SEDOV_1D)
+    return bad(SWFD_ERR_INVALID, "rk_choice 2 (the dt-halving restart RK) exists only in ex2");
   if (c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
     // ex6_shock_diffraction/main.f90:16-18: nx = 13*total/cut_x per rank,
     // ny = 11*total/cut_y per rank
@@ -348,6 +351,9 @@ swfd_status check_device_error(swfd_handle* h) {
   CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   h->hsc->error = 0;
+  if (e & ERR_BIT_RESTART)
+    return fail(h, SWFD_ERR_RESTART_LIMIT, "restart RK: no positive state within "
+                                           "SWFD_RESTART_LIMIT dt halvings");
   if (e & ERR_BIT_CHECK)
     return fail(h, SWFD_ERR_SWEEP_CHECK,
                 "Sweep check failed: total pressure increased after adjustment");
@@ -467,7 +473,7 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
                                                cudaEventRecordExternal));
   const bool sweeps = h->cfg.use_limiter == 2;
   const cudaGraphConditionalHandle hs = sweeps ? b.handle() : 0;
-  B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s, hs, sweeps));
+  B_OK(b, launch_rk(p, k, in, u0, h->flux, h->dsc, out, s, hs, sweeps ? 1 : 0));
   b.k(1);
   if (sweeps) {
     int* saved = b.count;
@@ -482,8 +488,75 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
   }
 }
 
+// The dt-halving restart RK of ex2 (rk_choice 2, ex2_sedov_1d/main.f90:330-374):
+//   wenofd(X); dt; alphatemp = alphamax
+//   WHILE (restart) { [dt = dt/2, alphamax = alphatemp]; stage 1: X -> Y;
+//     IF (positive) { wenofd(Y); stage 2: Y, X -> Z;
+//       IF (positive) { wenofd(Z); stage 3: Z, X -> Y } }
+//     restart = !positive }
+//   X = Y
+// The loop never overwrites u0 = X (stage 3 writes Y), so the reference's
+// `u = u0` needs no copy, and a restarted stage 1 uses the fluxes of the
+// last wenofd, as the reference's does.  ex2's bc is a no-op; no sweeps.
+void emit_step_restart(Builder& b, cudaStream_t s) {
+  swfd_handle* h = b.h;
+  const Params& p = h->p;
+  double* X = h->st[h->cur];
+  double* Y = h->st[(h->cur + 1) % 3];
+  double* Z = h->st[(h->cur + 2) % 3];
+  int* saved = b.count;
+  auto wenofd = [&](cudaStream_t sx, double* in, bool with_dt) {
+    B_OK(b, launch_alpha(p, in, h->dsc, sx, with_dt));
+    int nk = 0;
+    B_OK(b, launch_split(p, in, h->dsc, h->split, h->roe, sx, &nk));
+    B_OK(b, launch_flux(p, h->split, p.g.ndim == 1 ? in : h->roe, h->dsc, h->flux,
+                        &h->dsc->flux_work, sx));
+    b.k(2 + nk);
+  };
+  h->k_rs_fixed = 0;
+  b.count = &h->k_rs_fixed;
+  wenofd(s, X, true);
+  const cudaGraphConditionalHandle hw = b.handle();
+  B_OK(b, launch_restart_init(hw, h->dsc, s));
+  b.k(1);
+  b.cond(s, cudaGraphCondTypeWhile, hw, [&](cudaStream_t sl) {
+    h->k_rs_iter = 0;
+    b.count = &h->k_rs_iter;
+    B_OK(b, launch_restart_begin(h->dsc, sl));
+    const cudaGraphConditionalHandle h2 = b.handle();
+    B_OK(b, launch_rk(p, 1, X, X, h->flux, h->dsc, Y, sl, h2, 2));
+    b.k(2);
+    b.cond(sl, cudaGraphCondTypeIf, h2, [&](cudaStream_t s2) {
+      h->k_rs_s2 = 0;
+      b.count = &h->k_rs_s2;
+      wenofd(s2, Y, false);
+      const cudaGraphConditionalHandle h3 = b.handle();
+      B_OK(b, launch_rk(p, 2, Y, X, h->flux, h->dsc, Z, s2, h3, 2));
+      b.k(1);
+      b.cond(s2, cudaGraphCondTypeIf, h3, [&](cudaStream_t s3) {
+        h->k_rs_s3 = 0;
+        b.count = &h->k_rs_s3;
+        wenofd(s3, Z, false);
+        B_OK(b, launch_rk(p, 3, Z, X, h->flux, h->dsc, Y, s3, 0, 0));
+        b.k(1);
+      });
+    });
+    b.count = &h->k_rs_iter;
+    B_OK(b, launch_restart_end(hw, h->dsc, sl));
+    b.k(1);
+  });
+  b.count = &h->k_rs_fixed;
+  B_OK(b, launch_restart_commit(p, Y, X, h->dsc, s));
+  b.k(1);
+  b.count = saved;
+}
+
 void emit_step(Builder& b, cudaStream_t s, bool events) {
   swfd_handle* h = b.h;
+  if (h->cfg.rk_choice == 2) {
+    emit_step_restart(b, s);
+    return;
+  }
   double* X = h->st[h->cur];
   double* Y = h->st[(h->cur + 1) % 3];
   double* Z = h->st[(h->cur + 2) % 3];
@@ -528,6 +601,7 @@ swfd_status build_graph(swfd_handle* h, int kind, cudaGraphExec_t* out) {
   Builder b;
   b.h = h;
   b.cap = h->cap;
+  b.max_depth = SWFD_CAP_DEPTH - 1;
   cudaStream_t s = h->cap[0];
   CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   cudaStreamCaptureStatus cs;
@@ -576,6 +650,12 @@ void account(swfd_handle* h, const DevScalars& before, const DevScalars& after, 
   if (h->eager) {  // counted as launched
     h->prof.kernel_launches += h->eager_launches;
     h->eager_launches = 0;
+  } else if (h->cfg.rk_choice == 2) {
+    const int64_t it = after.rk_runs[1] - before.rk_runs[1];
+    const int64_t s2 = after.rk_runs[2] - before.rk_runs[2];
+    const int64_t s3 = after.rk_runs[3] - before.rk_runs[3];
+    h->prof.kernel_launches += steps * (h->k_rs_fixed + 1) + it * h->k_rs_iter +
+                               s2 * h->k_rs_s2 + s3 * h->k_rs_s3 + extra;
   } else {
     h->prof.kernel_launches += steps * (h->k_stage + 1) + sweeps * h->k_sweep_fixed +
                                dens * h->k_density + qs * h->k_q + extra;
@@ -617,6 +697,7 @@ const char* swfd_status_string(swfd_status s) {
     case SWFD_ERR_UNSUPPORTED: return "unsupported option";
     case SWFD_ERR_MAX_STEPS: return "step limit reached";
     case SWFD_ERR_SWEEP_CHECK: return "sweep check failed: total pressure increased";
+    case SWFD_ERR_RESTART_LIMIT: return "restart RK: dt-halving limit reached";
     default: return "unknown status";
   }
 }
@@ -633,6 +714,7 @@ swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
   cfg->ubar_mode = SWFD_UBAR_SEQUENTIAL;
   cfg->device = 0;
   cfg->gamma = 1.4;
+  cfg->rk_choice = 1;
   switch (problem) {
     case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:4-7,423-425
       cfg->nx = 800;
@@ -731,7 +813,7 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     return cleanup_fail(e);
   for (int k = 0; k < 8; ++k)
     if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < SWFD_CAP_DEPTH; ++k)
     if ((e = cudaStreamCreateWithFlags(&h->cap[k], cudaStreamNonBlocking)) != cudaSuccess)
       return cleanup_fail(e);
   h->track_cap = 1024;
@@ -772,7 +854,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   if (h->g_step) cudaGraphExecDestroy(h->g_step);
   if (h->g_solve) cudaGraphExecDestroy(h->g_solve);
   if (h->g_sweep) cudaGraphExecDestroy(h->g_sweep);
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < SWFD_CAP_DEPTH; ++k)
     if (h->cap[k]) cudaStreamDestroy(h->cap[k]);
   cudaFree(h->d_tracks);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -837,7 +919,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   ST(launch_kind(h, GRAPH_STEP, h->g_step));
   swfd_status st = check_device_error(h);
   account(h, before, *h->hsc, 1, 0);
-  if (h->prof_on) {
+  if (h->prof_on && h->cfg.rk_choice != 2) {  // the restart RK records no flux events
     for (int k = 0; k < 3; ++k) {
       float ms = 0.f;
       CU(h, cudaEventElapsedTime(&ms, h->ev[2 * k], h->ev[2 * k + 1]));
@@ -938,6 +1020,14 @@ swfd_status fetch_tracks(swfd_handle* h, std::vector<int32_t>& tr, int64_t& n) {
   return SWFD_OK;
 }
 }  // namespace
+
+swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts) {
+  if (!h || !restarts) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  CU(h, cudaSetDevice(h->device));
+  ST(sync_scalars(h));
+  *restarts = h->hsc->restart_total;
+  return SWFD_OK;
+}
 
 swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
   if (!h || !s) return fail(h, SWFD_ERR_INVALID, "NULL argument");

@@ -115,6 +115,7 @@ BatchLaunch launch_desc(swfd_batch* b) {
 swfd_status build_run_graph(swfd_batch* b) {
   Builder bd;
   bd.cap = b->cap;
+  bd.max_depth = 3;
   const BatchLaunch L = launch_desc(b);
   cudaStream_t s = b->cap[0];
   BCU(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));

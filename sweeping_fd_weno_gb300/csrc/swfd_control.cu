@@ -11,6 +11,49 @@ __device__ __forceinline__ double decode_key(unsigned long long k) {
   return __longlong_as_double((long long)b);
 }
 
+// restart RK (ex2_sedov_1d/main.f90:330-374).  After the step's first
+// wenofd and dt: alphatemp = alphamax (:337), enter the loop.
+__global__ void k_restart_init(cudaGraphConditionalHandle hw, DevScalars* d) {
+  d->alphatemp = d->alphamax;
+  d->restarts = 0;
+  set_cond(hw, &d->cond, 1u);
+}
+
+// label 110 (:339-346): a restart halves dt and restores alphamax; stage 1
+// reads u0 itself, so `u = u0` is implicit.  postag starts at 0.
+__global__ void k_restart_begin(DevScalars* d) {
+  if (d->restarts > 0) {
+    d->dt = d->dt / 2.;
+    d->alphamax = d->alphatemp;
+  }
+  d->postag = 0;
+}
+
+// `if (postag == 1) goto 110` (:350, :360, :370), bounded by SWFD_RESTART_LIMIT
+__global__ void k_restart_end(cudaGraphConditionalHandle hw, DevScalars* d) {
+  unsigned go = 0;
+  if (d->postag) {
+    if (d->restarts >= SWFD_RESTART_LIMIT) {
+      d->error |= ERR_BIT_RESTART;
+    } else {
+      d->restarts++;
+      d->restart_total++;
+      go = 1;
+    }
+  }
+  set_cond(hw, &d->cond, go);
+}
+
+// the accepted stage-3 state becomes u (whole planes, ghosts included),
+// unless the step gave up
+__global__ void k_restart_commit(const double* __restrict__ src, double* __restrict__ dst,
+                                 int64_t n, const DevScalars* d) {
+  if (d->error & ERR_BIT_RESTART) return;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    dst[k] = src[k];
+}
+
 // IF rho_min < 1d-12 (ex3_vortex_accuracy_2d/main.f90:1155-1156); den_count (:1187)
 __global__ void k_cond_density(cudaGraphConditionalHandle h, DevScalars* d) {
   bool go = decode_key(d->rho_min_key) < 1e-12;
@@ -92,6 +135,25 @@ __global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d,
   set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
+cudaError_t launch_restart_init(cudaGraphConditionalHandle hw, DevScalars* d, cudaStream_t s) {
+  k_restart_init<<<1, 1, 0, s>>>(hw, d);
+  return cudaGetLastError();
+}
+cudaError_t launch_restart_begin(DevScalars* d, cudaStream_t s) {
+  k_restart_begin<<<1, 1, 0, s>>>(d);
+  return cudaGetLastError();
+}
+cudaError_t launch_restart_end(cudaGraphConditionalHandle hw, DevScalars* d, cudaStream_t s) {
+  k_restart_end<<<1, 1, 0, s>>>(hw, d);
+  return cudaGetLastError();
+}
+cudaError_t launch_restart_commit(const Params& p, const double* src, double* dst,
+                                  const DevScalars* d, cudaStream_t s) {
+  const int64_t n = (int64_t)p.g.nc * p.g.plane;
+  const unsigned gb = (unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+  k_restart_commit<<<gb, 256, 0, s>>>(src, dst, n, d);
+  return cudaGetLastError();
+}
 cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s) {
   k_cond_density<<<1, 1, 0, s>>>(h, d);
   return cudaGetLastError();

@@ -5,6 +5,11 @@
 
 namespace swfd {
 
+cudaError_t launch_restart_init(cudaGraphConditionalHandle hw, DevScalars* d, cudaStream_t s);
+cudaError_t launch_restart_begin(DevScalars* d, cudaStream_t s);
+cudaError_t launch_restart_end(cudaGraphConditionalHandle hw, DevScalars* d, cudaStream_t s);
+cudaError_t launch_restart_commit(const Params& p, const double* src, double* dst,
+                                  const DevScalars* d, cudaStream_t s);
 cudaError_t launch_cond_density(cudaGraphConditionalHandle h, DevScalars* d, cudaStream_t s);
 cudaError_t launch_count_density(DevScalars* d, cudaStream_t s);
 cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, DevScalars* d,

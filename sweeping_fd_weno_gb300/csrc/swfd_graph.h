@@ -22,6 +22,7 @@ namespace swfd {
 struct Builder {
   swfd_handle* h = nullptr;
   cudaStream_t* cap = nullptr;  // capture streams, one per nesting depth
+  int max_depth = 0;            // capture streams available beyond depth 0
   cudaGraph_t root = nullptr;
   int depth = 0;
   int* count = nullptr;  // kernels emitted into the current section
@@ -53,6 +54,10 @@ struct Builder {
       } else {
         while (err == cudaSuccess && read_cond(s)) body(s);
       }
+      return;
+    }
+    if (depth + 1 > max_depth) {
+      err = cudaErrorInvalidValue;
       return;
     }
     cudaStreamCaptureStatus cs;

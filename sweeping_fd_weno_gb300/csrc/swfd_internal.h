@@ -123,8 +123,12 @@ enum : int {
   ERR_BIT_DT = 2,        // dt not finite
   ERR_BIT_PUBAR = 4,     // P(u_bar) <= 0 (ex4 stop)
   ERR_BIT_NOCONV = 8,    // sweep reached swp_num (ex4 stop)
-  ERR_BIT_CHECK = 16     // nodal adjustment raised the total pressure (ex6 stop)
+  ERR_BIT_CHECK = 16,    // nodal adjustment raised the total pressure (ex6 stop)
+  ERR_BIT_RESTART = 32   // restart RK: SWFD_RESTART_LIMIT dt halvings without a positive state
 };
+
+// conditional nesting depth of the graphs: solve WHILE > restart WHILE > IF > IF
+#define SWFD_CAP_DEPTH 6
 
 struct DevScalars {
   double alphamax;
@@ -153,6 +157,10 @@ struct DevScalars {
   int cond;               // eager launch mode: value of the last conditional decision
   int alpha_done;         // findalpha blocks finished (the last one re-arms it)
   int rk_done;            // RK-stage blocks finished (the last one re-arms it)
+  int restarts;           // restart RK: dt halvings of the current step
+  double alphatemp;       // restart RK: alphamax of the step's first findalpha
+  long long restart_total;  // restart RK: dt halvings of all steps
+  long long rk_runs[4];   // RK stages run, by stage (1..3)
 };
 
 // The value of a conditional node: set on the graph's handle, or written to
@@ -236,11 +244,14 @@ struct swfd_handle {
   // CUDA graphs, built on first use: one SSP-RK3 step (with flux events),
   // a solve (WHILE time <= T - 1d-10 over the step), and sweep_lim alone
   cudaGraphExec_t g_step = nullptr, g_solve = nullptr, g_sweep = nullptr;
-  cudaStream_t cap[4] = {};  // capture streams, one per conditional nesting depth
+  cudaStream_t cap[SWFD_CAP_DEPTH] = {};  // capture streams, one per conditional nesting depth
   int* d_tracks = nullptr;   // device sweep tracks (3 x track_cap)
   int64_t track_cap = 0;
   // kernels per graph section, for launch accounting
   int k_stage = 0, k_sweep_fixed = 0, k_density = 0, k_q = 0, k_step = 0;
+  // restart RK: kernels per step outside the loop, per loop iteration, per
+  // stage 2 and per stage 3 run
+  int k_rs_fixed = 0, k_rs_iter = 0, k_rs_s2 = 0, k_rs_s3 = 0;
   // eager launch mode (SWFD_LAUNCH=eager): the graph sections run as plain
   // stream launches and the conditions are read back on the host; for
   // profilers that do not look inside graphs with conditional nodes
@@ -275,10 +286,10 @@ cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void
 // kernel and its count of finished warps; the kernel leaves them zero)
 cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
                         const DevScalars* dsc, void* flux, int* work, cudaStream_t s);
-// decide: set the IF condition hs (0: the condition word) from postag
+// decide 1 / 2: set the IF condition hs (0: the condition word) to postag / !postag
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
                       const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
-                      cudaGraphConditionalHandle hs, bool decide);
+                      cudaGraphConditionalHandle hs, int decide);
 cudaError_t launch_rhs(const Params& p, const void* flux, const DevScalars* dsc, double* rhs,
                        cudaStream_t s);
 cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);

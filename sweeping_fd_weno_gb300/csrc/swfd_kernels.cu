@@ -1002,9 +1002,10 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
 }
 
 // postag starts the stage at 0 (findalpha clears it).  The last block to
-// finish takes the stage's positivity decision: where the stage sweeps it
-// sets the sweep's IF condition from postag
-// (ex3_vortex_accuracy_2d/main.f90:590-595).
+// finish counts the stage and takes its positivity decision: decide 1 sets
+// the IF condition hs to postag (the sweep, ex3_vortex_accuracy_2d/main.f90:
+// 590-595), decide 2 to !postag (the restart RK's next stage,
+// ex2_sedov_1d/main.f90:349-364).
 template <class T>
 __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
                      const T* __restrict__ flux, DevScalars* dsc, double* out,
@@ -1019,20 +1020,22 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
   __threadfence();
   const int tag = atomicOr(&dsc->postag, 0);
   dsc->rk_done = 0;
-  if (decide) set_cond(hs, &dsc->cond, tag ? 1u : 0u);
+  dsc->rk_runs[stage]++;
+  if (decide == 1) set_cond(hs, &dsc->cond, tag ? 1u : 0u);
+  else if (decide == 2) set_cond(hs, &dsc->cond, tag ? 0u : 1u);
 }
 
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
                       const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
-                      cudaGraphConditionalHandle hs, bool decide) {
+                      cudaGraphConditionalHandle hs, int decide) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
   const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
   if (p.precision == SWFD_PRECISION_FP32_BULK)
     k_rk<float><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const float*)flux,
-                                          const_cast<DevScalars*>(dsc), out, hs, decide ? 1 : 0);
+                                          const_cast<DevScalars*>(dsc), out, hs, decide);
   else
     k_rk<double><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const double*)flux,
-                                           const_cast<DevScalars*>(dsc), out, hs, decide ? 1 : 0);
+                                           const_cast<DevScalars*>(dsc), out, hs, decide);
   return cudaGetLastError();
 }
 

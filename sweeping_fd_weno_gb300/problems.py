@@ -17,8 +17,8 @@ def reference_defaults(problem: int) -> dict:
                 literals=abi.LITERALS_DOUBLE, precision=abi.PRECISION_FP64,
                 ubar_mode=abi.UBAR_SEQUENTIAL, sweep_mode=abi.SWEEP_PARALLEL, device=0, gamma=1.4,
                 e_background=0.0,
-                e_blast=0.0, ny=1, total=0, cut_x=0, cut_y=0)
-    if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425
+                e_blast=0.0, ny=1, total=0, cut_x=0, cut_y=0, rk_choice=1)
+    if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425 (RK_choice = 1)
         base.update(nx=800, ny=1, swp_num=50, cfl=1.2, time_terminal=0.001,
                     e_background=1e-9 / (1.4 - 1.0), e_blast=3200000.0)
     elif problem == abi.VORTEX_2D:   # ex3_vortex_accuracy_2d/main.f90:5-7,570

@@ -113,6 +113,12 @@ class Solver:
         self._chk(self.lib.swfd_find_alpha(self.h, C.byref(v)))
         return v.value
 
+    def restarts(self) -> int:
+        """dt halvings of the restart RK (rk_choice 2) over all steps"""
+        n = C.c_int64(0)
+        self._chk(self.lib.swfd_get_restarts(self.h, C.byref(n)))
+        return n.value
+
     def stats(self) -> dict:
         s = abi.SwfdSweepStats()
         self._chk(self.lib.swfd_get_sweep_stats(self.h, C.byref(s)))

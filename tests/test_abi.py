@@ -42,6 +42,10 @@ def test_create_rejects_bad_configs_without_cuda(swfd):
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     cfg = problems.make_config(abi.VORTEX_2D, use_limiter=3)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.VORTEX_2D, rk_choice=2)    # the restart RK is ex2's only
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.SEDOV_1D, rk_choice=3)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     cfg = problems.make_config(abi.VORTEX_2D, swp_num=0)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     assert "swp_num" in abi.last_error()
@@ -50,7 +54,7 @@ def test_create_rejects_bad_configs_without_cuda(swfd):
 
 def test_status_strings(swfd):
     lib = abi.load()
-    for st in range(0, -10, -1):
+    for st in range(0, -12, -1):
         assert lib.swfd_status_string(st)
     assert lib.swfd_status_string(abi.ERR_SWEEP_NOCONV) == b"sweep did not converge within swp_num"
 
