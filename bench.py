@@ -250,9 +250,10 @@ def bench_batched(args, local, flush):
                     a = torch.cuda.Event(enable_timing=True)
                     z = torch.cuda.Event(enable_timing=True)
                     a.record(se)
-                s.step()
+                s.step_async()
                 z.record(se)
                 torch.cuda.synchronize()
+                s.finish()
                 tot_ms += a.elapsed_time(z)
             tot_upd += n * n * 3 * args.plain_steps
             s.close()
@@ -493,16 +494,20 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     evs = []
+    # steps are enqueued without a host round trip (step_async), so each
+    # event pair brackets one step graph on the device; finish() then waits
+    # and reports their status
     for _ in range(args.steps):
         with torch.cuda.stream(ext):
             flush.zero_()  # evict L2 (129 MB) between timed steps
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(ext)
-        solver.step()
+        solver.step_async()
         e1.record(ext)
         evs.append((e0, e1))
     torch.cuda.synchronize()
+    solver.finish()
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -612,10 +617,11 @@ def main():
                 a = torch.cuda.Event(enable_timing=True)
                 b = torch.cuda.Event(enable_timing=True)
                 a.record(ext32)
-            s32.step()
+            s32.step_async()
             b.record(ext32)
             ev32.append((a, b))
         torch.cuda.synchronize()
+        s32.finish()
         ms32 = sum(a.elapsed_time(b) for a, b in ev32)
         for _ in range(args.steps):
             s64.step()

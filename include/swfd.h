@@ -174,6 +174,14 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out);
  * nsteps_out may be NULL. */
 swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out);
 
+/* swfd_step without waiting: enqueue one step on the handle's stream
+ * (swfd_get_stream) and return.  swfd_finish waits for the enqueued steps and
+ * reports their status; every other call on the handle finishes them first
+ * (the device state is stream-ordered either way).  With profiling on,
+ * swfd_finish adds the flux timings of the last enqueued step. */
+swfd_status swfd_step_async(swfd_handle* h);
+swfd_status swfd_finish(swfd_handle* h);
+
 /* Restart RK (rk_choice 2): dt halvings over all steps so far (the
  * `goto 110` restarts of ex2_sedov_1d/main.f90:350,360,370); 0 otherwise. */
 swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts);

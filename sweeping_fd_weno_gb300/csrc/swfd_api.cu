@@ -363,6 +363,15 @@ swfd_status check_device_error(swfd_handle* h) {
               std::string("non-finite ") + ((e & ERR_BIT_ALPHA) ? "alphamax" : "dt") + " on the device");
 }
 
+swfd_status finish_pending(swfd_handle* h);
+
+// a call that reads or writes the handle's state first finishes the steps
+// swfd_step_async enqueued (their status is reported here)
+#define SETTLE(h)                               \
+  do {                                          \
+    if ((h)->pending) ST(finish_pending(h));    \
+  } while (0)
+
 // the device track arrays must hold sweep_count + extra entries
 swfd_status ensure_tracks(swfd_handle* h, int64_t extra) {
   ST(sync_scalars(h));
@@ -677,6 +686,22 @@ swfd_status reset_scalars(swfd_handle* h) {
   return SWFD_OK;
 }
 
+swfd_status finish_pending(swfd_handle* h) {
+  const int64_t n = h->pending;
+  h->pending = 0;
+  swfd_status st = check_device_error(h);
+  account(h, h->pending_before, *h->hsc, n, 0);
+  if (h->prof_on && h->cfg.rk_choice != 2) {  // the last step's flux launches
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      CU(h, cudaEventElapsedTime(&ms, h->ev[2 * k], h->ev[2 * k + 1]));
+      h->prof.flux_ms += ms;
+      h->prof.flux_launches += 1;
+    }
+  }
+  return st;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -864,6 +889,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
 
 swfd_status swfd_upload_state(swfd_handle* h, const double* u) {
   if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   CU(h, cudaMemcpyAsync(h->d_stage, u, hb, cudaMemcpyHostToDevice, h->stream));
@@ -874,6 +900,7 @@ swfd_status swfd_upload_state(swfd_handle* h, const double* u) {
 
 swfd_status swfd_download_state(swfd_handle* h, double* u) {
   if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   CU(h, launch_soa_to_fortran(h->p, cur_state(h), h->d_stage, h->stream));
@@ -884,6 +911,7 @@ swfd_status swfd_download_state(swfd_handle* h, double* u) {
 
 swfd_status swfd_init_problem(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   std::vector<double> u((size_t)host_len(h->p));
   init_host(h, u.data());
   ST(swfd_upload_state(h, u.data()));
@@ -897,12 +925,14 @@ swfd_status swfd_init_problem(swfd_handle* h) {
 
 swfd_status swfd_get_time(swfd_handle* h, double* t) {
   if (!h || !t) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   *t = h->time;
   return SWFD_OK;
 }
 
 swfd_status swfd_set_time(swfd_handle* h, double t) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   h->time = t;
   CU(h, cudaMemcpyAsync(&h->dsc->time, &h->time, sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -912,6 +942,7 @@ swfd_status swfd_set_time(swfd_handle* h, double t) {
 
 swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_STEP, &h->g_step));
   ST(ensure_tracks(h, 3));
@@ -931,8 +962,33 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   return st;
 }
 
+swfd_status swfd_step_async(swfd_handle* h) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  if (h->eager) return swfd_step(h, nullptr);  // eager sections read conditions on the host
+  CU(h, cudaSetDevice(h->device));
+  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  // a step records at most three sweeps: grow the track arrays (after
+  // finishing what is enqueued) before the pending steps could overflow them
+  if (h->hsc->sweep_count + 3 * (h->pending + 1) > h->track_cap) {
+    SETTLE(h);
+    ST(ensure_tracks(h, 3));
+  }
+  if (h->pending == 0) h->pending_before = *h->hsc;
+  CU(h, cudaGraphLaunch(h->g_step, h->stream));
+  h->pending++;
+  return SWFD_OK;
+}
+
+swfd_status swfd_finish(swfd_handle* h) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  CU(h, cudaSetDevice(h->device));
+  if (!h->pending) return SWFD_OK;
+  return finish_pending(h);
+}
+
 swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_SOLVE, &h->g_solve));
   int64_t done = 0;
@@ -964,6 +1020,7 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
 
 swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
   if (!h || !rhs) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   const Params& p = h->p;
   double* u = cur_state(h);
@@ -981,6 +1038,7 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
 
 swfd_status swfd_sweep(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_SWEEP, &h->g_sweep));
   ST(ensure_tracks(h, 1));
@@ -993,6 +1051,7 @@ swfd_status swfd_sweep(swfd_handle* h) {
 
 swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
   if (!h || !postag) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   CU(h, launch_positivity(h->p, cur_state(h), h->dsc, h->stream));
   ST(sync_scalars(h));
@@ -1002,6 +1061,7 @@ swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
 
 swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax) {
   if (!h || !alphamax) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   CU(h, launch_alpha(h->p, cur_state(h), h->dsc, h->stream));
   ST(sync_scalars(h));
@@ -1023,6 +1083,7 @@ swfd_status fetch_tracks(swfd_handle* h, std::vector<int32_t>& tr, int64_t& n) {
 
 swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts) {
   if (!h || !restarts) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   ST(sync_scalars(h));
   *restarts = h->hsc->restart_total;
@@ -1031,6 +1092,7 @@ swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts) {
 
 swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
   if (!h || !s) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   std::vector<int32_t> tr;
   int64_t n = 0;
@@ -1055,6 +1117,7 @@ swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
 swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos,
                                   int64_t cap, int64_t* count) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   std::vector<int32_t> tr;
   int64_t n = 0;
@@ -1145,6 +1208,7 @@ swfd_status swfd_set_profiling(swfd_handle* h, int32_t on) {
 
 swfd_status swfd_get_profile(swfd_handle* h, swfd_profile* prof) {
   if (!h || !prof) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
   *prof = h->prof;
   return SWFD_OK;
 }

@@ -252,6 +252,10 @@ struct swfd_handle {
   // restart RK: kernels per step outside the loop, per loop iteration, per
   // stage 2 and per stage 3 run
   int k_rs_fixed = 0, k_rs_iter = 0, k_rs_s2 = 0, k_rs_s3 = 0;
+  // steps enqueued by swfd_step_async and not yet finished, and the scalars
+  // before the first of them
+  int64_t pending = 0;
+  swfd::DevScalars pending_before{};
   // eager launch mode (SWFD_LAUNCH=eager): the graph sections run as plain
   // stream launches and the conditions are read back on the host; for
   // profilers that do not look inside graphs with conditional nodes

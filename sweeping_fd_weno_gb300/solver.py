@@ -88,6 +88,14 @@ class Solver:
         self._chk(self.lib.swfd_step(self.h, C.byref(dt)))
         return dt.value
 
+    def step_async(self):
+        """Enqueue one step on the solver's stream without waiting; finish()
+        (or any other call) waits for it and reports its status."""
+        self._chk(self.lib.swfd_step_async(self.h))
+
+    def finish(self):
+        self._chk(self.lib.swfd_finish(self.h))
+
     def run(self, max_steps: int = 0) -> int:
         n = C.c_int64()
         st = self.lib.swfd_run(self.h, int(max_steps), C.byref(n))
