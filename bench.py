@@ -51,6 +51,26 @@ FLUX_DRAM_BYTES_PER_CELL = 313.6e6 / (1024 * 1024)
 FLUX_F32_DRAM_BYTES_PER_CELL = 134.4e6 / (1024 * 1024)
 
 
+def precision_errors(u32, u64, gamma=1.4):
+    """The FP32-bulk state against the FP64 path's (value-for-value the
+    oracle's) on the interior cells: relative L1 and Linf errors of density and
+    pressure, and the relative drift of total mass and total energy."""
+    import numpy as np
+    a, b = u32[3:-3, 3:-3], u64[3:-3, 3:-3]
+
+    def pres(u):
+        return (gamma - 1.0) * (u[..., 3] - 0.5 * (u[..., 1] ** 2 + u[..., 2] ** 2) / u[..., 0])
+
+    out = {}
+    for name, x, y in (("density", a[..., 0], b[..., 0]), ("pressure", pres(a), pres(b))):
+        d = np.abs(x - y)
+        out[f"rel_l1_{name}"] = float(d.sum() / np.abs(y).sum())
+        out[f"rel_linf_{name}"] = float(d.max() / np.abs(y).max())
+    out["mass_drift"] = float((a[..., 0].sum() - b[..., 0].sum()) / b[..., 0].sum())
+    out["energy_drift"] = float((a[..., 3].sum() - b[..., 3].sum()) / b[..., 3].sum())
+    return out
+
+
 def env_int(k, d):
     try:
         return int(os.environ.get(k, d))
@@ -203,6 +223,7 @@ def bench_batched(args, local, flush):
         if not b.admit(cfg_of(n), k):
             raise RuntimeError(f"instance {k} ({n}^2) not admitted")
     t_adm = time.perf_counter() - t_adm
+    tile_cells = b.autotune()   # cell-tile size of the per-cell kernels for this mix
     ext = torch.cuda.ExternalStream(b.stream_ptr(), device=dev)
     b.run(args.warmup)
     before = [b.progress(k)[1] for k in range(len(sizes))]
@@ -219,7 +240,7 @@ def bench_batched(args, local, flush):
     value = aggregate(upd, ms * 1e-3)[2]  # every replica's instances over the slowest
     # accuracy: the smallest instances against the FP64 path after the same steps
     check = sorted(range(len(sizes)), key=lambda k: sizes[k])[:3]
-    errs = []
+    errs, full = [], {}
     for k in check:
         u32, _ = b.download(k)
         s = Solver(cfg_of(sizes[k]))
@@ -230,6 +251,7 @@ def bench_batched(args, local, flush):
         s.close()
         r32, r64 = u32[3:-3, 3:-3, 0], u64[3:-3, 3:-3, 0]
         errs.append(float(np.abs(r32 - r64).sum() / np.abs(r64).sum()))
+        full[f"{sizes[k]}^2"] = precision_errors(u32, u64)
     b.close()
     # the plain FP64 path (and the FP32 path unbatched), one instance at a time
     rng = np.random.default_rng(BATCH_SEED + 1)
@@ -240,6 +262,7 @@ def bench_batched(args, local, flush):
         for n in sample:
             s = Solver(cfg_of(n, precision=prec))
             s.init_problem()
+            s.autotune()
             se = torch.cuda.ExternalStream(s.stream_ptr(), device=dev)
             for _ in range(args.warmup):   # the same steps as the batch's timed ones
                 s.step()
@@ -266,12 +289,13 @@ def bench_batched(args, local, flush):
         "precision": "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, positivity, sweeps)",
         "cells": int(sum(n * n for n in sizes)),
         "value": value, "unit": UNIT, "ms": ms, "steps": args.batch_steps,
-        "graph_launches": 1, "admission_s": t_adm,
+        "graph_launches": 1, "admission_s": t_adm, "tile_cells": tile_cells,
         "l2": "not flushed: the batch's resident state (GBs) is far above L2",
         "plain_fp64_one_at_a_time": plain["fp64"],
         "fp32_bulk_one_at_a_time": plain["fp32_bulk_single"],
         "speedup_vs_plain_fp64": value / plain["fp64"]["value"],
         "rel_l1_density_err_vs_fp64": {f"{sizes[k]}^2": e for k, e in zip(check, errs)},
+        "errors_vs_fp64": full,
     }
 
 
@@ -479,6 +503,7 @@ def main():
     cfg = problems.workload(args.workload, device=local, precision=main_prec)
     solver = Solver(cfg)
     solver.init_problem()
+    flux_min_blocks = solver.autotune()  # launch shape of the flux kernel on this state
     cells = solver.nx * solver.ny
     ext = torch.cuda.ExternalStream(solver.stream_ptr(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -609,6 +634,7 @@ def main():
             s32.step()
         s32.set_state(s64.state(out=u_start))
         s32.time = s64.time
+        minb32 = s32.autotune()
         torch.cuda.synchronize()
         ev32 = []
         for _ in range(args.steps):
@@ -625,11 +651,14 @@ def main():
         ms32 = sum(a.elapsed_time(b) for a, b in ev32)
         for _ in range(args.steps):
             s64.step()
-        r64, r32 = s64.state()[3:-3, 3:-3, 0], s32.state()[3:-3, 3:-3, 0]
+        u64f, u32f = s64.state(), s32.state()
+        r64, r32 = u64f[3:-3, 3:-3, 0], u32f[3:-3, 3:-3, 0]
         fp32 = {"value": aggregate(cells * 3 * args.steps, ms32 * 1e-3)[2],
                 "ms_per_step": ms32 / args.steps,
                 "speedup_vs_fp64": total_ms / ms32 if ms32 else None,
+                "flux_min_blocks": minb32,
                 "rel_l1_density_err_vs_fp64": float(np.abs(r32 - r64).sum() / np.abs(r64).sum()),
+                "errors_vs_fp64": precision_errors(u32f, u64f),
                 "arithmetic": "FP32 LF splitting, WENO5 fluxes and flux differences; FP64 pressure "
                               "recovery, RK accumulation, positivity, CFL reduction and sweeps"}
         s32.close()
@@ -645,6 +674,7 @@ def main():
                    "precision": "plain FP64 (double literals)" if args.precision == "fp64"
                    else "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, sweeps)",
                    "l2": "flushed between timed steps (256 MiB write)",
+                   "flux_min_blocks": flux_min_blocks,
                    "parallelism": f"replicas x{world}"},
         "clocks": clk,
         "e2e": e2e,

@@ -180,6 +180,15 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out);
  * (the device state is stream-ordered either way).  With profiling on,
  * swfd_finish adds the flux timings of the last enqueued step. */
 swfd_status swfd_step_async(swfd_handle* h);
+
+/* Autotuner.  swfd_autotune times the launch shapes of the flux kernel
+ * (resident blocks per SM against registers per thread) on the handle's
+ * current state and keeps the fastest for the handle's later steps; results
+ * do not change.  Problems with rank segments or the flux limiter keep the
+ * default shape (*flux_min_blocks = 0).  swfd_batch_autotune times the cell-tile
+ * size of the batch's per-cell kernels on the running instances and keeps
+ * the fastest. */
+swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks);
 swfd_status swfd_finish(swfd_handle* h);
 
 /* Restart RK (rk_choice 2): dt halvings over all steps so far (the
@@ -266,6 +275,7 @@ swfd_status swfd_batch_progress(swfd_batch* b, int64_t request_id, double* time_
                                 int64_t* steps_out);
 /* The CUDA stream (cudaStream_t) the batch's graph runs on. */
 swfd_status swfd_batch_get_stream(swfd_batch* b, void** stream);
+swfd_status swfd_batch_autotune(swfd_batch* b, int32_t* tile_cells);
 
 /* Instrumentation (no counterpart in the reference, which only prints a
  * wall-clock "CPU Time", ex4_sedov_2d/main.f90:111,118-119). */

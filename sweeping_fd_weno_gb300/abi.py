@@ -121,6 +121,8 @@ _SIGS = {
     "swfd_get_sweep_stats": (C.c_int32, [_P, C.POINTER(SwfdSweepStats)]),
     "swfd_get_restarts": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "swfd_step_async": (C.c_int32, [_P]),
+    "swfd_autotune": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "swfd_batch_autotune": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "swfd_finish": (C.c_int32, [_P]),
     "swfd_get_sweep_tracks": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32), C.c_int64,

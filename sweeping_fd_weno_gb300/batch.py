@@ -85,6 +85,13 @@ class Batch:
         abi.check(self.lib.swfd_batch_progress(self.h, int(request_id), C.byref(t), C.byref(n)))
         return t.value, n.value
 
+    def autotune(self) -> int:
+        """Time the cell-tile sizes of the per-cell kernels on the running
+        instances and keep the fastest; returns the tile size in cells."""
+        v = C.c_int32(0)
+        abi.check(self.lib.swfd_batch_autotune(self.h, C.byref(v)))
+        return v.value
+
     def stream_ptr(self) -> int:
         v = C.c_void_p()
         abi.check(self.lib.swfd_batch_get_stream(self.h, C.byref(v)))

@@ -979,6 +979,48 @@ swfd_status swfd_step_async(swfd_handle* h) {
   return SWFD_OK;
 }
 
+swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
+  if (!h || !flux_min_blocks) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
+  CU(h, cudaSetDevice(h->device));
+  *flux_min_blocks = 0;
+  Params& p = h->p;
+  if (p.g.ndim != 2 || p.seg_alpha || p.limiter) return SWFD_OK;
+  // the flux kernel's inputs for the current state (findalpha and the
+  // splitting only rewrite per-stage scratch: alphamax, split and Roe planes)
+  double* u = cur_state(h);
+  CU(h, launch_alpha(p, u, h->dsc, h->stream));
+  int nk = 0;
+  CU(h, launch_split(p, u, h->dsc, h->split, h->roe, h->stream, &nk));
+  int cand[8];
+  const int nc = flux_min_blocks_candidates(p.precision == SWFD_PRECISION_FP32_BULK, cand);
+  const int saved = p.flux_minb;
+  float best = 0.f;
+  int pick = cand[0];
+  for (int k = 0; k < nc; ++k) {
+    p.flux_minb = cand[k];
+    CU(h, launch_flux(p, h->split, h->roe, h->dsc, h->flux, &h->dsc->flux_work, h->stream));
+    CU(h, cudaEventRecord(h->ev[0], h->stream));
+    for (int r = 0; r < 5; ++r)
+      CU(h, launch_flux(p, h->split, h->roe, h->dsc, h->flux, &h->dsc->flux_work, h->stream));
+    CU(h, cudaEventRecord(h->ev[1], h->stream));
+    CU(h, cudaEventSynchronize(h->ev[1]));
+    float ms = 0.f;
+    CU(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    if (k == 0 || ms < best) best = ms, pick = cand[k];
+  }
+  p.flux_minb = pick;
+  if (pick != saved) {  // the graphs hold the parameters by value: capture them again
+    if (h->g_step) cudaGraphExecDestroy(h->g_step);
+    if (h->g_solve) cudaGraphExecDestroy(h->g_solve);
+    if (h->g_sweep) cudaGraphExecDestroy(h->g_sweep);
+    h->g_step = h->g_solve = h->g_sweep = nullptr;
+  }
+  ST(check_device_error(h));
+  *flux_min_blocks = pick;
+  return SWFD_OK;
+}
+
 swfd_status swfd_finish(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   CU(h, cudaSetDevice(h->device));

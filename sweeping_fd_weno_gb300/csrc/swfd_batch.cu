@@ -50,6 +50,9 @@ struct swfd_batch {
   BatchCtl* h_ctl = nullptr;
   long long* d_prefix = nullptr;
   std::vector<long long> prefix;
+  long long* d_tprefix = nullptr;  // cell-tile prefix of the per-cell kernels
+  std::vector<long long> tprefix;
+  int tile_cells = 2048;           // cells per tile (swfd_batch_autotune picks it)
   DevScalars* d_dsc = nullptr;  // one DevScalars per slot, contiguous: one read-back per run
   DevScalars* h_dsc = nullptr;  // pinned mirror
   cudaGraphExec_t g_run = nullptr;
@@ -102,6 +105,7 @@ BatchLaunch launch_desc(swfd_batch* b) {
   L.tab = b->d_tab;
   L.ctl = b->d_ctl;
   L.prefix = b->d_prefix;
+  L.tprefix = b->d_tprefix;
   L.n_slots = b->cfg.max_slots;
   L.max_cell = b->max_cell;
   L.fp32 = b->cfg.precision == SWFD_PRECISION_FP32_BULK;
@@ -248,12 +252,14 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   b->slots.resize(n);
   b->tab.assign(n, BatchSlot{});
   b->prefix.assign(n + 1, 0);
+  b->tprefix.assign(n + 1, 0);
   b->max_cell = (long long)(cfg->max_nx + 6) * (cfg->max_ny + 6);
   b->stage_bytes = (size_t)4 * b->max_cell * sizeof(double);
   if ((e = cudaMalloc(&b->d_tab, n * sizeof(BatchSlot))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_ctl, sizeof(BatchCtl))) != cudaSuccess) return bad(e);
   if ((e = cudaMallocHost(&b->h_ctl, sizeof(BatchCtl))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_prefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
+  if ((e = cudaMalloc(&b->d_tprefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
   if ((e = cudaMallocHost(&b->h_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
@@ -288,6 +294,7 @@ swfd_status swfd_batch_destroy(swfd_batch* b) {
   cudaFree(b->d_tab);
   cudaFree(b->d_ctl);
   cudaFree(b->d_prefix);
+  cudaFree(b->d_tprefix);
   cudaFree(b->d_stage);
   cudaFree(b->d_dsc);
   if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -400,6 +407,81 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   return SWFD_OK;
 }
 
+namespace {
+// the running slots' work plan: flux-chunk and cell-tile prefixes and the
+// batch scalars of a launch of up to max_steps steps
+swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
+  const int n = b->cfg.max_slots;
+  int running = 0;
+  long long chunks = 0, tiles = 0;
+  for (int k = 0; k < n; ++k) {
+    b->prefix[k] = chunks;
+    b->tprefix[k] = tiles;
+    if (b->slots[k].state == 1) {
+      ++running;
+      chunks += b->tab[k].chunks;
+      tiles += (b->tab[k].ncell + b->tile_cells - 1) / b->tile_cells;
+    }
+  }
+  b->prefix[n] = chunks;
+  b->tprefix[n] = tiles;
+  BCU(b, cudaMemcpyAsync(b->d_prefix, b->prefix.data(), (n + 1) * sizeof(long long),
+                         cudaMemcpyHostToDevice, b->stream));
+  BCU(b, cudaMemcpyAsync(b->d_tprefix, b->tprefix.data(), (n + 1) * sizeof(long long),
+                         cudaMemcpyHostToDevice, b->stream));
+  BatchCtl& c = *b->h_ctl;
+  c = BatchCtl{};
+  c.n_active = running;
+  c.total_chunks = chunks;
+  c.total_tiles = tiles;
+  c.tile_cells = b->tile_cells;
+  c.steps_limit = max_steps;
+  BCU(b, cudaMemcpyAsync(b->d_ctl, &c, sizeof(BatchCtl), cudaMemcpyHostToDevice, b->stream));
+  return SWFD_OK;
+}
+}  // namespace
+
+// cell-tile sizes the batch autotuner times, on findalpha over the running
+// instances (it reads the state and writes only per-stage scratch)
+swfd_status swfd_batch_autotune(swfd_batch* b, int32_t* tile_cells) {
+  if (!b || !tile_cells) return bfail(b, SWFD_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(b->mu);
+  BCU(b, cudaSetDevice(b->cfg.device));
+  *tile_cells = b->tile_cells;
+  int running = 0;
+  for (const SlotHost& sh : b->slots) running += sh.state == 1;
+  if (!running) return SWFD_OK;
+  static const int cand[] = {512, 1024, 2048, 4096, 8192};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BCU(b, cudaEventCreate(&e0));
+  BCU(b, cudaEventCreate(&e1));
+  const BatchLaunch L = launch_desc(b);
+  float best = 0.f;
+  int pick = b->tile_cells;
+  swfd_status st = SWFD_OK;
+  for (int k = 0; k < (int)(sizeof(cand) / sizeof(cand[0])) && st == SWFD_OK; ++k) {
+    b->tile_cells = cand[k];
+    if ((st = upload_plan(b, 1)) != SWFD_OK) break;
+    cudaError_t e = launch_batch_alpha(L, 0, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_batch_alpha(L, 0, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      st = bfail(b, SWFD_ERR_CUDA, cudaGetErrorString(e));
+      break;
+    }
+    if (k == 0 || ms < best) best = ms, pick = cand[k];
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tile_cells = pick;
+  *tile_cells = pick;
+  return st;
+}
+
 swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out) {
   if (!b) return bfail(b, SWFD_ERR_INVALID, "NULL handle");
   std::lock_guard<std::mutex> lk(b->mu);
@@ -408,25 +490,17 @@ swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out)
   BCU(b, cudaSetDevice(b->cfg.device));
   const int n = b->cfg.max_slots;
   int running = 0;
-  long long total = 0;
-  for (int k = 0; k < n; ++k) {
-    b->prefix[k] = total;
+  for (int k = 0; k < n; ++k)
     if (b->slots[k].state == 1) {
       ++running;
-      total += b->tab[k].chunks;
       swfd_status st = ensure_slot_tracks(b, k, 3 * max_steps);
       if (st != SWFD_OK) return st;
     }
-  }
-  b->prefix[n] = total;
   if (!running) return SWFD_OK;
-  BCU(b, cudaMemcpyAsync(b->d_prefix, b->prefix.data(), (n + 1) * sizeof(long long),
-                         cudaMemcpyHostToDevice, b->stream));
-  BatchCtl c{};
-  c.n_active = running;
-  c.total_chunks = total;
-  c.steps_limit = max_steps;
-  BCU(b, cudaMemcpyAsync(b->d_ctl, &c, sizeof(BatchCtl), cudaMemcpyHostToDevice, b->stream));
+  {
+    swfd_status st = upload_plan(b, max_steps);
+    if (st != SWFD_OK) return st;
+  }
   BCU(b, cudaGraphLaunch(b->g_run, b->stream));
   BCU(b, cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, b->stream));
   BCU(b, cudaMemcpyAsync(b->tab.data(), b->d_tab, n * sizeof(BatchSlot), cudaMemcpyDeviceToHost,

@@ -55,6 +55,7 @@ struct Params {
   int stop_sweep = 0;    // P(u_bar) <= 0 and swp_num exhaustion stop the run (ex4, ex6)
   int limiter = 0;       // use_limiter = 1: the positivity flux limiter in wenofd
   int limiter_clamp = 0; // ex6 clamps its theta at 0 (theta = max(theta, 0.))
+  int flux_minb = 0;     // flux kernel launch shape chosen by swfd_autotune (0: default)
   // Shock diffraction (ex6_shock_diffraction/main.f90).  The reference's
   // rank grid cut_x x cut_y (ranks of nxl x nyl cells) is part of its
   // arithmetic: the x pass of row j uses the max alpha over the cells of
@@ -196,11 +197,11 @@ struct BatchCtl {
   int flux_work;          // chunk counter of the persistent flux kernel
   int n_active;           // slots still being advanced
   long long total_chunks;
+  long long total_tiles;  // cell tiles of the running slots (tile_cells cells each)
+  int tile_cells;         // cells per tile of the per-cell batched kernels
   long long steps;        // steps taken by the current launch
   long long steps_limit;
   int cond;               // eager launch mode: value of the last conditional decision
-  int alpha_done;         // findalpha blocks finished (the last one re-arms it)
-  int rk_done;            // RK-stage blocks finished (the last one re-arms it)
 };
 
 // What a batched launch needs (host side).
@@ -208,6 +209,7 @@ struct BatchLaunch {
   BatchSlot* tab;           // device slot table
   BatchCtl* ctl;            // device batch scalars
   const long long* prefix;  // device flux-chunk prefix (n_slots + 1)
+  const long long* tprefix; // device cell-tile prefix (n_slots + 1)
   int n_slots;
   long long max_cell;       // largest slot (LI*LJ)
   int fp32;
@@ -306,6 +308,11 @@ cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* u
 cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
                                cudaGraphConditionalHandle h_sweep, cudaStream_t s);
 cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s);
+// findalpha over the running slots' state `in` (the batch autotuner's probe)
+cudaError_t launch_batch_alpha(const BatchLaunch& b, int in, cudaStream_t s);
+// launch-shape candidates of the flux kernel (resident blocks per SM); returns
+// their number, the default first
+int flux_min_blocks_candidates(bool f32, int* out);
 cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
 cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,
                                   cudaStream_t s);

@@ -572,6 +572,42 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
                                                const T* __restrict__ sn, int64_t P, int64_t step,
                                                T weps, T outp[4], T outn[4]) {
   T ur[4], ul[4];
+  if constexpr (sizeof(T) == 4) {
+    // FP32: the 5 x 4 stencil values of each split flux are loaded once into
+    // registers (40 loads instead of 160 per interface) and projected from
+    // there; the arithmetic is the same as below
+    T a[5][4], b[5][4];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        a[m][c] = ldt(sp + m * step + c * P);
+        b[m][c] = ldt(sn + m * step + c * P);
+      }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      T cp[5], cn[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const T *x = a[m], *y = b[m];
+        if (k == 0) {
+          cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, x[0], x[1], x[2], x[3]);
+          cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, y[0], y[1], y[2], y[3]);
+        } else if (k == 1) {
+          cp[m] = proj_row2<YDIR>(E.vt, x[0], x[1], x[2]);
+          cn[m] = proj_row2<YDIR>(E.vt, y[0], y[1], y[2]);
+        } else if (k == 2) {
+          cp[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, x[0], x[1], x[2], x[3]);
+          cn[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, y[0], y[1], y[2], y[3]);
+        } else {
+          cp[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, x[0], x[1], x[2], x[3]);
+          cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, y[0], y[1], y[2], y[3]);
+        }
+      }
+      ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
+      ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+    }
+  } else
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     T cp[5], cn[5];
@@ -811,8 +847,8 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
   }
 }
 
-template <class T, bool SEG, bool LIM>
-__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
+template <class T, bool SEG, bool LIM, int MINB = SWFD_FLUX_MINB(T)>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
     k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
               const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
   const int64_t chunks_x = (flux_faces_x(p, LIM) + 31) / 32;
@@ -840,18 +876,38 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
   }
 }
 
-template <class T>
+template <class T, int MINB = SWFD_FLUX_MINB(T)>
 static int flux_grid() {
   static int grid = 0;
   if (!grid) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T, false, false>, SWFD_FLUX_BLOCK,
-                                                  0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy<T, false, false, MINB>,
+                                                  SWFD_FLUX_BLOCK, 0);
     grid = sms * (per > 0 ? per : 1);
   }
   return grid;
+}
+
+// Launch-shape variants of the common flux kernel (no rank segments, no
+// limiter) that swfd_autotune times: resident blocks per SM, traded against
+// registers per thread (FP64: 3 = 168 registers, 2 = 255; FP32: 4 = 128,
+// 5 = 102, 6 = 85).  The first entry is the default.
+int flux_min_blocks_candidates(bool f32, int* out) {
+  if (f32) {
+    out[0] = 4, out[1] = 5, out[2] = 6;
+    return 3;
+  }
+  out[0] = 3, out[1] = 2;
+  return 2;
+}
+
+template <class T, int MINB>
+static void launch_flux_minb(const Params& p, const T* sp, const T* rp, const DevScalars* dsc,
+                             T* fp, int* work, cudaStream_t s) {
+  k_flux_xy<T, false, false, MINB><<<flux_grid<T, MINB>(), SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp,
+                                                                                    dsc, fp, work);
 }
 
 // the flux kernel variant of the problem: rank segments (ex6), limiter
@@ -862,6 +918,14 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
   const T* rp = (const T*)roe;
   T* fp = (T*)flux;
   const int grid = flux_grid<T>();
+  if (!p.seg_alpha && !p.limiter && p.flux_minb && p.flux_minb != SWFD_FLUX_MINB(T)) {
+    if constexpr (sizeof(T) == 8) {
+      if (p.flux_minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
+    } else {
+      if (p.flux_minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
+      if (p.flux_minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
+    }
+  }
   if (p.seg_alpha && p.limiter)
     k_flux_xy<T, true, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
   else if (p.seg_alpha)
@@ -1171,19 +1235,41 @@ __global__ void kb_stage_reset(BatchSlot* __restrict__ tab, BatchCtl* ctl, int n
   tab[s].dsc->postag = 0;
 }
 
-__global__ void kb_alpha(const BatchSlot* __restrict__ tab, int in) {
-  const BatchSlot& sl = tab[blockIdx.y];
-  if (!sl.active) return;
-  double a = 0.0;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const double at = alpha_cell(sl.p, sl.st[in], t);
-    alpha_store(sl.p, t, at);
-    a = fmax(a, at);
+// The per-cell batched kernels walk the running slots' cells as equal tiles
+// of ctl->tile_cells cells (the last tile of a slot may be short): tile k
+// belongs to the slot s with tp[s] <= k < tp[s+1].  A persistent grid takes
+// the tiles round robin, so every block does the same work whatever the mix
+// of grid sizes.
+__device__ __forceinline__ int tile_slot(const long long* __restrict__ tp, int n, long long k) {
+  int lo = 0, hi = n - 1;  // last slot with tp[s] <= k
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tp[mid] <= k) lo = mid;
+    else hi = mid - 1;
   }
-  a = block_max(a);
-  if (threadIdx.x == 0)
-    atomicMax(&sl.dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+  return lo;
+}
+
+__global__ void kb_alpha(const BatchSlot* __restrict__ tab, const long long* __restrict__ tp,
+                         int n, const BatchCtl* __restrict__ ctl, int in) {
+  const long long total = ctl->total_tiles;
+  const int tc = ctl->tile_cells;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(tp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;  // uniform over the block
+    const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
+    double a = 0.0;
+    for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+      const double at = alpha_cell(sl.p, sl.st[in], t);
+      alpha_store(sl.p, t, at);
+      a = fmax(a, at);
+    }
+    a = block_max(a);
+    if (threadIdx.x == 0)
+      atomicMax(&sl.dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+    __syncthreads();  // block_max's shared words are reused by the next tile
+  }
 }
 
 __global__ void kb_alpha_final(const BatchSlot* __restrict__ tab, int n, int stage) {
@@ -1196,15 +1282,21 @@ __global__ void kb_alpha_final(const BatchSlot* __restrict__ tab, int n, int sta
 template <class T>
 // pass 1: the x part of slots with rank segments, everything of the others;
 // pass 2: the y part of slots with rank segments (after their y wall mirror)
-__global__ void kb_prep(const BatchSlot* __restrict__ tab, int in, int pass) {
-  const BatchSlot& sl = tab[blockIdx.y];
-  if (!sl.active) return;
-  const int which = sl.p.seg_alpha ? pass : (pass == 1 ? 3 : 0);
-  if (!which) return;
-  const double am = sl.dsc->alphamax;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
-       t += (int64_t)gridDim.x * blockDim.x)
-    prep2d_cell<T>(sl.p, sl.st[in], am, (T*)sl.split, (T*)sl.roe, t, which);
+__global__ void kb_prep(const BatchSlot* __restrict__ tab, const long long* __restrict__ tp, int n,
+                        const BatchCtl* __restrict__ ctl, int in, int pass) {
+  const long long total = ctl->total_tiles;
+  const int tc = ctl->tile_cells;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(tp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;
+    const int which = sl.p.seg_alpha ? pass : (pass == 1 ? 3 : 0);
+    if (!which) continue;
+    const double am = sl.dsc->alphamax;
+    const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
+    for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x)
+      prep2d_cell<T>(sl.p, sl.st[in], am, (T*)sl.split, (T*)sl.roe, t, which);
+  }
 }
 
 // ex6 slots: alpha per rank row / column and the wall mirrors
@@ -1255,28 +1347,39 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
 }
 
 template <class T>
-__global__ void kb_rk(const BatchSlot* __restrict__ tab, BatchCtl* ctl, int stage, int in,
-                      int out) {
-  const BatchSlot& sl = tab[blockIdx.y];
-  if (!sl.active) return;
-  DevScalars* d = sl.dsc;
-  const double dt = d->dt, am = d->alphamax;
-  int bad = 0;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
-       t += (int64_t)gridDim.x * blockDim.x)
-    bad |= rk_cell<T>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux, dt, am, sl.st[out], t);
-  if (block_or(bad) && threadIdx.x == 0) {
-    atomicOr(&d->postag, 1);
-    if (sl.use_limiter == 2) atomicOr(&ctl->any_postag, 1);
+__global__ void kb_rk(const BatchSlot* __restrict__ tab, const long long* __restrict__ tp, int n,
+                      BatchCtl* ctl, int stage, int in, int out) {
+  const long long total = ctl->total_tiles;
+  const int tc = ctl->tile_cells;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(tp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;
+    DevScalars* d = sl.dsc;
+    const double dt = d->dt, am = d->alphamax;
+    const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
+    int bad = 0;
+    for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x)
+      bad |= rk_cell<T>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux, dt, am, sl.st[out],
+                        t);
+    if (block_or(bad) && threadIdx.x == 0) {
+      atomicOr(&d->postag, 1);
+      if (sl.use_limiter == 2) atomicOr(&ctl->any_postag, 1);
+    }
   }
 }
 
-__global__ void kb_bc(const BatchSlot* __restrict__ tab, int out) {
-  const BatchSlot& sl = tab[blockIdx.y];
-  if (!sl.active) return;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < sl.ncell;
-       t += (int64_t)gridDim.x * blockDim.x)
-    bc2d_cell(sl.p, sl.st[out], t);
+__global__ void kb_bc(const BatchSlot* __restrict__ tab, const long long* __restrict__ tp, int n,
+                      const BatchCtl* __restrict__ ctl, int out) {
+  const long long total = ctl->total_tiles;
+  const int tc = ctl->tile_cells;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(tp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;
+    const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
+    for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x) bc2d_cell(sl.p, sl.st[out], t);
+  }
 }
 
 // time = time + dt; an instance that reaches its T (or hits an error) stops
@@ -1301,6 +1404,18 @@ __global__ void kb_run_cond(cudaGraphConditionalHandle h, BatchCtl* ctl, int adv
   set_cond(h, &ctl->cond, (ctl->n_active > 0 && ctl->steps < ctl->steps_limit) ? 1u : 0u);
 }
 
+// persistent grid of the tiled per-cell kernels: 8 blocks of 256 per SM
+static int batch_tile_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid = 8 * (sms > 0 ? sms : 1);
+  }
+  return grid;
+}
+
 static int batch_grid_x(int n_slots, long long max_cell) {
   long long want = (4096 + n_slots - 1) / n_slots;
   long long cap = (max_cell + SWFD_BLOCK - 1) / SWFD_BLOCK;
@@ -1314,37 +1429,42 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
   const int n = b.n_slots;
   const int gs = (n + 127) / 128;
   const dim3 grid(batch_grid_x(n, b.max_cell), n);
+  const int tg = batch_tile_grid();
   kb_stage_reset<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
-  kb_alpha<<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in);
+  kb_alpha<<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in);
   kb_alpha_final<<<gs, 128, 0, s>>>(b.tab, n, stage);
   if (b.segmented) {
     kb_seg_alpha<<<grid, SWFD_BLOCK, 0, s>>>(b.tab);
     kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 0);
   }
   if (b.fp32) {
-    kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 1);
+    kb_prep<float><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in, 1);
     if (b.segmented) {
       kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 1);
-      kb_prep<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 2);
+      kb_prep<float><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in, 2);
     }
     kb_flux<float><<<flux_grid<float>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
-    kb_rk<float><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
+    kb_rk<float><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, stage, in, out);
   } else {
-    kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 1);
+    kb_prep<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in, 1);
     if (b.segmented) {
       kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 1);
-      kb_prep<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, in, 2);
+      kb_prep<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in, 2);
     }
     kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
-    kb_rk<double><<<grid, SWFD_BLOCK, 0, s>>>(b.tab, b.ctl, stage, in, out);
+    kb_rk<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, stage, in, out);
   }
   if (h_sweep) kb_cond_any_postag<<<1, 1, 0, s>>>(h_sweep, b.ctl);
   return cudaGetLastError();
 }
 
+cudaError_t launch_batch_alpha(const BatchLaunch& b, int in, cudaStream_t s) {
+  kb_alpha<<<batch_tile_grid(), SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, b.n_slots, b.ctl, in);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s) {
-  const dim3 grid(batch_grid_x(b.n_slots, b.max_cell), b.n_slots);
-  kb_bc<<<grid, SWFD_BLOCK, 0, s>>>(b.tab, out);
+  kb_bc<<<batch_tile_grid(), SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, b.n_slots, b.ctl, out);
   return cudaGetLastError();
 }
 

@@ -93,6 +93,13 @@ class Solver:
         (or any other call) waits for it and reports its status."""
         self._chk(self.lib.swfd_step_async(self.h))
 
+    def autotune(self) -> int:
+        """Time the flux kernel's launch shapes on the current state and keep
+        the fastest; returns its resident blocks per SM (0: not tuned)."""
+        v = C.c_int32(0)
+        self._chk(self.lib.swfd_autotune(self.h, C.byref(v)))
+        return v.value
+
     def finish(self):
         self._chk(self.lib.swfd_finish(self.h))
 

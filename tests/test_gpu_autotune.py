@@ -1,0 +1,47 @@
+"""The autotuners change launch shapes only: results stay value for value
+those of the default shapes."""
+import numpy as np
+import pytest
+
+from sweeping_fd_weno_gb300 import Batch, Solver, abi, problems
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32_BULK])
+def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
+    cfg = problems.make_config(abi.VORTEX_2D, nx=64, ny=64, precision=precision)
+    a, b = Solver(cfg), Solver(cfg)
+    for s in (a, b):
+        s.init_problem()
+    minb = b.autotune()
+    assert minb in ((3, 2) if precision == abi.PRECISION_FP64 else (4, 5, 6))
+    for _ in range(4):
+        assert a.step() == b.step()
+    assert np.array_equal(a.state(), b.state())
+    a.close()
+    b.close()
+
+
+def test_flux_tuning_skips_segmented_and_limited_problems(swfd):
+    s = Solver(problems.make_config(abi.VORTEX_2D, nx=48, ny=48, use_limiter=1))
+    s.init_problem()
+    assert s.autotune() == 0
+    s.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32_BULK])
+def test_batch_tile_tuning_keeps_results(swfd, precision):
+    mix = [dict(nx=45, ny=45), dict(nx=64, ny=48), dict(nx=96, ny=80)]
+    out = []
+    for tune in (False, True):
+        with Batch(max_slots=4, max_nx=128, max_ny=128, precision=precision) as b:
+            for k, m in enumerate(mix):
+                assert b.admit(problems.make_config(abi.VORTEX_2D, precision=precision, **m), k)
+            if tune:
+                assert b.autotune() in (512, 1024, 2048, 4096, 8192)
+            b.run(5)
+            out.append([b.download(k) for k in range(len(mix))])
+    for (ua, ta), (ub, tb) in zip(*out):
+        assert ta == tb
+        assert np.array_equal(ua, ub)
