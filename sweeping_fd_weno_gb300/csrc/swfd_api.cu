@@ -997,7 +997,12 @@ swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
   const int saved = p.flux_minb;
   float best = 0.f;
   int pick = cand[0];
-  for (int k = 0; k < nc; ++k) {
+  // SWFD_FLUX_MIN_BLOCKS pins one of the candidates (reproducible profiles)
+  int pinned = 0;
+  if (const char* env = getenv("SWFD_FLUX_MIN_BLOCKS"))
+    for (int k = 0; k < nc; ++k)
+      if (atoi(env) == cand[k]) pinned = cand[k];
+  for (int k = 0; k < nc && !pinned; ++k) {
     p.flux_minb = cand[k];
     CU(h, launch_flux(p, h->split, h->roe, h->dsc, h->flux, &h->dsc->flux_work, h->stream));
     CU(h, cudaEventRecord(h->ev[0], h->stream));
@@ -1009,6 +1014,7 @@ swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
     CU(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
     if (k == 0 || ms < best) best = ms, pick = cand[k];
   }
+  if (pinned) pick = pinned;
   p.flux_minb = pick;
   if (pick != saved) {  // the graphs hold the parameters by value: capture them again
     if (h->g_step) cudaGraphExecDestroy(h->g_step);
