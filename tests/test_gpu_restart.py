@@ -80,3 +80,24 @@ def test_restart_rk_fp32_bulk_tracks_fp64(swfd):
     assert np.abs(ua - ub).sum() / np.abs(ua).sum() < 1e-4
     a.close()
     b.close()
+
+
+def test_restart_limit_matches_oracle(swfd, oracle_mod):
+    """A uniform state below the positivity threshold fails every stage 1:
+    both stop the step after SWFD_RESTART_LIMIT halvings with the same status,
+    and the GPU leaves u at u0."""
+    kw, _ = CASES["cfl1.2"]
+    g, o = pair(oracle_mod, kw)
+    u = o.state()
+    u[...] = 0.0
+    u[..., 0] = 1.0
+    u[..., 2] = 1e-14      # uniform: RHS = 0, and E - m^2/(2 rho) <= eps = 1e-13
+    g.set_state(u)
+    o.set_state(u)
+    with pytest.raises(RuntimeError, match=str(abi.ERR_RESTART_LIMIT)):
+        o.step()
+    with pytest.raises(abi.SwfdError) as e:
+        g.step()
+    assert e.value.status == abi.ERR_RESTART_LIMIT
+    assert np.array_equal(g.state(), u)
+    g.close()

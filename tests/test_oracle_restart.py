@@ -44,3 +44,19 @@ def test_restarts_halve_dt_and_keep_positivity(oracle_mod, cfl, steps, min_resta
         assert (u[:, 0] > 1e-13).all()
         assert (u[:, 2] - u[:, 1] ** 2 / u[:, 0] / 2.0 > 1e-13).all()
     assert o.restarts >= min_restarts
+
+
+def test_a_state_that_never_turns_positive_ends_at_the_restart_limit(oracle_mod):
+    """A uniform state whose pressure term is below eps has RHS = 0, so every
+    stage 1 returns u0 and fails checkpositivity however small dt gets: the
+    oracle stops after SWFD_RESTART_LIMIT halvings (the reference would loop
+    on)."""
+    o = make(oracle_mod, rk_choice=2)
+    u = o.state()
+    u[...] = 0.0
+    u[..., 0] = 1.0
+    u[..., 2] = 1e-14      # uniform: RHS = 0, and E - m^2/(2 rho) <= eps = 1e-13
+    o.set_state(u)
+    with pytest.raises(RuntimeError, match=str(abi.ERR_RESTART_LIMIT)):
+        o.step()
+    assert o.restarts == 0 or o.restarts <= abi.RESTART_LIMIT
