@@ -61,6 +61,10 @@ enum {
 /* Problem = one reference example, with all of its per-example switches
  * (operation order, epsilons, comparison operators, boundary conditions). */
 enum {
+  SWFD_PROBLEM_MATLAB_1D = 1,  /* ex1_double_rarefaction_1d/FD_WENO_Application.m: the
+                                  MATLAB script's own 1D scheme (per-field Lax-Friedrichs
+                                  alpha, WENO eps 1e-5, sweep after every stage); its
+                                  `problem` number is config.variant (5 as shipped) */
   SWFD_PROBLEM_SEDOV_1D = 2,   /* ex2_sedov_1d/main.f90 */
   SWFD_PROBLEM_VORTEX_2D = 3,  /* ex3_vortex_accuracy_2d/main.f90 */
   SWFD_PROBLEM_SEDOV_2D = 4,   /* ex4_sedov_2d/main.f90 on one 1x1 block */
@@ -121,7 +125,10 @@ typedef struct swfd_config {
                             restart RK of ex2 (`rk`, ex2_sedov_1d/main.f90:330-374:
                             a stage that fails checkpositivity restarts the step
                             from u0 with dt/2; no sweeps).  2 is 1D only. */
-  int32_t reserved[3];   /* zero */
+  int32_t variant;       /* SWFD_PROBLEM_MATLAB_1D: the script's `problem` (1 linear
+                            advection, 2 nonlinear, 3 Sod, 4 Lax, 5 double rarefaction,
+                            6 point energy, 7 jet ambient state); 0 otherwise */
+  int32_t reserved[2];   /* zero */
 } swfd_config;
 
 /* Sweep statistics exactly as the reference counts them

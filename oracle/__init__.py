@@ -81,7 +81,7 @@ class Oracle:
         self.lib = load()
         self.cfg = cfg
         self.o = self.lib.oracle_create(C.byref(cfg))
-        ndim = 1 if cfg.problem == 2 else 2
+        ndim = 1 if cfg.problem in (1, 2) else 2  # the MATLAB script and ex2 are 1D
         self.shape = (1, cfg.nx + 6, 3) if ndim == 1 else (cfg.ny + 6, cfg.nx + 6, 4)
 
     def close(self):

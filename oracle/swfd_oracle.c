@@ -984,6 +984,380 @@ static int sweep_lim1d(oracle* o) {
 }
 
 /* ------------------------------------------------------------------ */
+/* ex1: the MATLAB script ex1_double_rarefaction_1d/FD_WENO_Application.m */
+/* with its helpers (get_variables.m, get_pressure_data.m, scalar_pos.m, */
+/* apply_sweep.m, swp_alg_triag_nxt.m, node_adj_scale_lim_triag.m).     */
+/* MATLAB evaluates its operators left to right with the precedence of  */
+/* its documentation (unary minus before * and /); x.^2 is taken as x*x, */
+/* a row times a column (the weighted means) as a left-to-right sum and  */
+/* a 3x3 matrix times a vector row by row left to right.  MATLAB itself  */
+/* is not available, so these choices are not pinned against its output. */
+/* The script keeps no ghost cells: o->u's interior 1..n is its u(:,1:n) */
+/* and the ghosts hold the padding FD_WENO_Step would build from it.     */
+/* ------------------------------------------------------------------ */
+static int ex1_periodic(const oracle* o) {
+  const int pr = o->cfg.variant; /* FD_WENO_Application.m:27-150 */
+  return pr == 1 || pr == 2 || pr == 6;
+}
+
+/* the padding of FD_WENO_Step (:394-411): wrap or constant extension */
+static void ex1_pad(const oracle* o, const double* u, double* pad, int ldp) {
+  const int n = o->nx, per = ex1_periodic(o);
+  for (int J = 1; J <= n + 6; ++J) {
+    int i;
+    if (J <= 3) i = per ? n - 3 + J : 1;
+    else if (J > n + 3) i = per ? J - n - 3 : n;
+    else i = J - 3;
+    for (int c = 0; c < 3; ++c) pad[c * ldp + J] = u[c + 3 * (i + 2)];
+  }
+}
+
+/* scalarWeno (:588-629): out[0] the value at the right face from the left
+ * (umOut), out[1] the value at the left face of cell 4 from the right (upOut) */
+static void ex1_scalar_weno(const double* s, double* um_out, double* up_out) {
+  const double umm = s[0], um = s[1], u = s[2], up = s[3], upp = s[4], uppp = s[5];
+  const double c13 = 1. / 3., c76 = 7. / 6., c116 = 11. / 6., c16 = 1. / 6., c56 = 5. / 6.;
+  const double c1312 = 13. / 12., c14 = 1. / 4., eps = 10e-6;
+  const double cw1 = 1. / 10., cw2 = 3. / 5., cw3 = 3. / 10.;
+  double um1 = c13 * umm - c76 * um + c116 * u;
+  double um2 = -c16 * um + c56 * u + c13 * up;
+  double um3 = c13 * u + c56 * up - c16 * upp;
+  double b1 = c1312 * sq(umm - 2 * um + u) + c14 * sq(umm - 4 * um + 3 * u);
+  double b2 = c1312 * sq(um - 2 * u + up) + c14 * sq(um - up);
+  double b3 = c1312 * sq(u - 2 * up + upp) + c14 * sq(3 * u - 4 * up + upp);
+  double w1 = cw1 / sq(b1 + eps), w2 = cw2 / sq(b2 + eps), w3 = cw3 / sq(b3 + eps);
+  double sw = w1 + w2 + w3;
+  *um_out = w1 / sw * um1 + w2 / sw * um2 + w3 / sw * um3;
+  double up1 = c116 * up - c76 * upp + c13 * uppp;
+  double up2 = c13 * u + c56 * up - c16 * upp;
+  double up3 = -c16 * um + c56 * u + c13 * up;
+  b1 = c1312 * sq(uppp - 2 * upp + up) + c14 * sq(uppp - 4 * upp + 3 * up);
+  b2 = c1312 * sq(upp - 2 * up + u) + c14 * sq(upp - u);
+  b3 = c1312 * sq(up - 2 * u + um) + c14 * sq(3 * up - 4 * u + um);
+  w1 = cw1 / sq(b1 + eps), w2 = cw2 / sq(b2 + eps), w3 = cw3 / sq(b3 + eps);
+  sw = w1 + w2 + w3;
+  *up_out = w1 / sw * up1 + w2 / sw * up2 + w3 / sw * up3;
+}
+
+/* FD_WENO_Step (:392-585): fP(:,k) the flux at the right face of cell k,
+ * fM(:,k) at its left face; u is the interior state (3 x n, ghosts unused) */
+static void ex1_fluxes(const oracle* o, const double* u, double* fP, double* fM) {
+  const int n = o->nx, N = n + 6, L = N + 1, per = ex1_periodic(o);
+  const double g1 = o->gamma - 1;
+  double* pad = malloc(3 * L * sizeof(double));
+  double* ar = malloc(12 * L * sizeof(double));
+  double *ro = ar, *m = ar + L, *E = ar + 2 * L, *v = ar + 3 * L, *p = ar + 4 * L,
+         *H1 = ar + 5 * L, *vxm = ar + 6 * L, *hxm = ar + 7 * L, *qm = ar + 8 * L,
+         *cm = ar + 9 * L, *t2 = ar + 10 * L, *sr = ar + 11 * L;
+  /* get_variables (get_variables.m), then the padding */
+  double* iv = malloc(5 * L * sizeof(double));
+  for (int i = 1; i <= n; ++i) {
+    const double r = u[0 + 3 * (i + 2)], mm = u[1 + 3 * (i + 2)], e = u[2 + 3 * (i + 2)];
+    iv[i] = r, iv[L + i] = mm, iv[2 * L + i] = e;
+    iv[3 * L + i] = mm / r;
+    iv[4 * L + i] = g1 * (e - 1. / 2. * (mm * mm) / r);
+  }
+  for (int J = 1; J <= N; ++J) {
+    int i;
+    if (J <= 3) i = per ? n - 3 + J : 1;
+    else if (J > n + 3) i = per ? J - n - 3 : n;
+    else i = J - 3;
+    ro[J] = iv[i], m[J] = iv[L + i], E[J] = iv[2 * L + i], v[J] = iv[3 * L + i];
+    p[J] = iv[4 * L + i];
+  }
+  free(iv);
+  for (int J = 1; J <= N; ++J) {
+    sr[J] = sqrt(ro[J]);
+    H1[J] = (p[J] + E[J]) / ro[J];
+  }
+  /* Roe averages at J+1/2 (circshift wraps the last), per-field alpha */
+  double a1 = 0, a2 = 0, a3 = 0;
+  for (int J = 1; J <= N; ++J) {
+    const int Jn = J == N ? 1 : J + 1;
+    const double t0 = sr[J] / (sr[J] + sr[Jn]);
+    const double t1 = 1 - t0;
+    vxm[J] = t0 * v[J] + t1 * v[Jn];
+    hxm[J] = t0 * H1[J] + t1 * H1[Jn];
+    qm[J] = 0.5 * (vxm[J] * vxm[J]);
+    cm[J] = sqrt(g1 * (hxm[J] - qm[J]));
+    t2[J] = vxm[J] * cm[J];
+    const double l1 = fabs(vxm[J] - cm[J]), l2 = fabs(vxm[J]), l3 = fabs(vxm[J] + cm[J]);
+    if (J == 1) a1 = l1, a2 = l2, a3 = l3;
+    else a1 = fmax(a1, l1), a2 = fmax(a2, l2), a3 = fmax(a3, l3);
+  }
+  const double al[3] = {a1, a2, a3};
+  /* the flux at interface J+1/2 from cells J-2..J+3 (:445-517) */
+  for (int kk = 0; kk <= n; ++kk) {
+    const int J = kk + 3;
+    if (kk == 0 && per) continue;
+    const double V = vxm[J], H = hxm[J], q = qm[J], c = cm[J], T2 = t2[J];
+    const double rcm = 1 / c;
+    const double b1 = g1 * (rcm * rcm), b2 = q * b1, t0h = V * rcm, t1h = b1 * V, t2h = 0.5 * b1;
+    const double Lm[3][3] = {{0.5 * (b2 + t0h), -0.5 * (t1h + rcm), t2h},
+                             {1 - b2, t1h, -b1},
+                             {0.5 * (b2 - t0h), -0.5 * (t1h - rcm), t2h}};
+    double gp[3][6], gm[3][6];
+    for (int idx = 0; idx < 6; ++idx) {
+      const int i = J - 2 + idx;
+      const double uu[3] = {ro[i], m[i], E[i]};
+      const double fu[3] = {m[i], ro[i] * (v[i] * v[i]) + p[i], v[i] * (E[i] + p[i])};
+      for (int r = 0; r < 3; ++r) {
+        const double w = Lm[r][0] * uu[0] + Lm[r][1] * uu[1] + Lm[r][2] * uu[2];
+        const double g = Lm[r][0] * fu[0] + Lm[r][1] * fu[1] + Lm[r][2] * fu[2];
+        gp[r][idx] = 1. / 2. * (g + al[r] * w);
+        gm[r][idx] = 1. / 2. * (g - al[r] * w);
+      }
+    }
+    double gh[3];
+    for (int r = 0; r < 3; ++r) {
+      double um_p, up_p, um_m, up_m;
+      ex1_scalar_weno(gm[r], &um_m, &up_m);
+      ex1_scalar_weno(gp[r], &um_p, &up_p);
+      gh[r] = up_m + um_p;
+    }
+    double f[3];
+    f[0] = 1 * gh[0] + 1 * gh[1] + 1 * gh[2];
+    f[1] = (V - c) * gh[0] + V * gh[1] + (V + c) * gh[2];
+    f[2] = (H - T2) * gh[0] + q * gh[1] + (H + T2) * gh[2];
+    for (int r = 0; r < 3; ++r) {
+      if (kk >= 1) fP[r + 3 * (kk - 1)] = f[r];
+      if (kk == 0) fM[r] = f[r];
+    }
+  }
+  for (int k = 1; k <= n; ++k)
+    for (int r = 0; r < 3; ++r) {
+      if (k >= 2) fM[r + 3 * (k - 1)] = fP[r + 3 * (k - 2)];
+      else if (per) fM[r] = fP[r + 3 * (n - 1)];
+    }
+  free(pad);
+  free(ar);
+}
+
+/* get_pressure_data.m: min of P = E - m^2/rho/2 and P of the weighted mean */
+static void ex1_pressure_data(const oracle* o, const double* u, double* pmin, double* pu_avg) {
+  const int n = o->nx;
+  const double w = o->weight;
+  double ra = 0, ma = 0, ea = 0, mn = 0;
+  for (int i = 1; i <= n; ++i) {
+    const double* x = u + 3 * (i + 2);
+    const double P = x[2] - 1. / 2. * ((x[1] * x[1]) / x[0]);
+    mn = (i == 1) ? P : fmin(mn, P);
+    ra = ra + x[0] * w, ma = ma + x[1] * w, ea = ea + x[2] * w;
+  }
+  *pmin = mn;
+  *pu_avg = ea - 1. / 2. * ((ma * ma) / ra);
+}
+
+/* scalar_pos.m: the density sweep, forward then backward, floor m = 1e-16 */
+static void ex1_scalar_pos(oracle* o, double* u) {
+  const int n = o->nx;
+  const double m = 1e-16, w = o->weight;
+  for (int j = 1; j <= n - 1; ++j) {
+    const double vj = u[3 * (j + 2)], vp = u[3 * (j + 3)];
+    if (vj < m) {
+      u[3 * (j + 3)] = vp + (w / w) * (vj - m);
+      u[3 * (j + 2)] = m;
+    }
+  }
+  for (int j = n; j >= 2; --j) {
+    const double vj = u[3 * (j + 2)], vp = u[3 * (j + 1)];
+    if (vj < m) {
+      u[3 * (j + 1)] = vp + (w / w) * (vj - m);
+      u[3 * (j + 2)] = m;
+    }
+  }
+  o->den_count++;
+}
+
+/* the pressure of the sweep functions, with their own gamma = 1.4 */
+static double ex1_P14(const double* x) { return (1.4 - 1) * (x[2] - 1. / 2. * ((x[1] * x[1]) / x[0])); }
+
+/* node_adj_scale_lim_triag.m */
+static void ex1_node_adj(oracle* o, const double* v1, const double* v2, const double* vb,
+                         double* out) {
+  const double epsi = 1e-13;
+  double t;
+  if (ex1_P14(v2) > epsi) {
+    t = (ex1_P14(v1) - epsi) / (ex1_P14(v1) - ex1_P14(v2));
+    o->t_pos_count++;
+  } else {
+    const double t1 = (ex1_P14(v1) - epsi) / (ex1_P14(v1) - ex1_P14(vb));
+    const double d1 = sqrt(sq(vb[2] - v1[2]) + sq(vb[1] - v1[1]) + sq(vb[0] - v1[0]));
+    const double d2 = sqrt(sq(v2[2] - v1[2]) + sq(v2[1] - v1[1]) + sq(v2[0] - v1[0]));
+    t = fmin(t1 * d1 / d2, 0.25);
+    o->t_neg_count++;
+  }
+  for (int c = 0; c < 3; ++c) out[c] = (1 - t) * v1[c] + t * v2[c];
+}
+
+/* swp_alg_triag_nxt.m */
+static void ex1_swp_alg(oracle* o, double* u) {
+  const int n = o->nx;
+  const double w = o->weight, epsi = 1e-12;
+  double ub[3] = {0, 0, 0};
+  for (int c = 0; c < 3; ++c)
+    for (int i = 1; i <= n; ++i) ub[c] = ub[c] + u[c + 3 * (i + 2)] * w;
+  o->sweep_count++;
+  track_push(o);
+  o->t_pos_count = o->t_neg_count = 0;
+  int q;
+  for (q = 1; q <= o->cfg.swp_num; ++q) {
+    for (int pass = 0; pass < 2; ++pass)
+      for (int s = 1; s <= n - 1; ++s) {
+        const int j = pass == 0 ? s : n - s + 1, jp = pass == 0 ? j + 1 : j - 1;
+        double* vj = u + 3 * (j + 2);
+        double* vp = u + 3 * (jp + 2);
+        if (ex1_P14(vj) <= epsi || vj[0] < 0) {
+          double vjt[3], a[3], b[3];
+          for (int c = 0; c < 3; ++c) a[c] = vj[c], b[c] = vp[c];
+          ex1_node_adj(o, a, b, ub, vjt);
+          for (int c = 0; c < 3; ++c) {
+            const double d = a[c] - vjt[c];
+            vj[c] = vjt[c];
+            vp[c] = b[c] + (w / w) * d;
+          }
+        }
+      }
+    o->pre_count++;
+    double pmin, pu;
+    ex1_pressure_data(o, u, &pmin, &pu);
+    double rmin = 0;
+    for (int i = 1; i <= n; ++i) rmin = (i == 1) ? u[3 * (i + 2)] : fmin(rmin, u[3 * (i + 2)]);
+    if (pmin > epsi && rmin > epsi) break;
+  }
+  if (q > o->cfg.swp_num) {
+    q = o->cfg.swp_num;
+    o->fail_count++;
+  }
+  o->sweep_track[o->sweep_count - 1] = q;
+  o->neg_track[o->sweep_count - 1] = (int32_t)o->t_neg_count;
+  o->pos_track[o->sweep_count - 1] = (int32_t)o->t_pos_count;
+}
+
+/* apply_sweep.m */
+static void ex1_apply_sweep(oracle* o, double* u) {
+  const int n = o->nx;
+  double rmin = 0;
+  for (int i = 1; i <= n; ++i) rmin = (i == 1) ? u[3 * (i + 2)] : fmin(rmin, u[3 * (i + 2)]);
+  if (rmin <= 1e-13) ex1_scalar_pos(o, u);
+  double pmin, pu;
+  ex1_pressure_data(o, u, &pmin, &pu);
+  if (pmin <= 1e-13 && pu > 0) {
+    ex1_scalar_pos(o, u);
+    ex1_pressure_data(o, u, &pmin, &pu);
+    if (pu > 1e-13) ex1_swp_alg(o, u);
+  }
+}
+
+/* one pass of the script's time loop (:212-289) */
+static int ex1_step(oracle* o) {
+  const int n = o->nx, ln = 3 * (n + 6);
+  const double g = o->gamma, g1 = g - 1, h = o->dx;
+  double* u = o->u;
+  /* eigenvalues of the cell states and the time step (:217-252) */
+  double a1 = 0, a2 = 0, a3 = 0;
+  for (int i = 1; i <= n; ++i) {
+    const double ro = u[3 * (i + 2)], m = u[1 + 3 * (i + 2)], E = u[2 + 3 * (i + 2)];
+    const double v = m / ro;
+    const double p = E * g1 - 1. / 2. * ro * (v * v) * g1;
+    const double c = sqrt((g * p) / ro);
+    const double l1 = fabs(v - c), l2 = fabs(v), l3 = fabs(v + c);
+    if (i == 1) a1 = l1, a2 = l2, a3 = l3;
+    else a1 = fmax(a1, l1), a2 = fmax(a2, l2), a3 = fmax(a3, l3);
+  }
+  const double alpha = fmax(fmax(a1, a2), a3);
+  o->alphamax = alpha;
+  double k = o->cfg.cfl * h / alpha;
+  if (o->cfg.time_terminal - o->time < k) k = o->cfg.time_terminal - o->time;
+  const double l = k / h;
+  o->dt = k;
+  double* uh = calloc(ln, sizeof(double));
+  double* fP = calloc(3 * n, sizeof(double));
+  double* fM = calloc(3 * n, sizeof(double));
+  const int sweeping = o->cfg.use_limiter == 2;
+  for (int stage = 1; stage <= 3; ++stage) {
+    ex1_fluxes(o, stage == 1 ? u : uh, fP, fM);
+    for (int i = 1; i <= n; ++i)
+      for (int c = 0; c < 3; ++c) {
+        const size_t a = c + 3 * (size_t)(i + 2);
+        const double d = l * (fP[c + 3 * (i - 1)] - fM[c + 3 * (i - 1)]);
+        if (stage == 1) uh[a] = u[a] - d;
+        else if (stage == 2) uh[a] = 3. / 4. * u[a] + 1. / 4. * (uh[a] - d);
+        else uh[a] = 1. / 3. * u[a] + 2. / 3. * (uh[a] - d);
+      }
+    if (sweeping) ex1_apply_sweep(o, uh);
+  }
+  memcpy(u, uh, ln * sizeof(double));
+  double* pad = malloc(3 * (n + 7) * sizeof(double));
+  ex1_pad(o, u, pad, n + 7);
+  for (int J = 1; J <= 3; ++J)
+    for (int c = 0; c < 3; ++c) {
+      u[c + 3 * (J - 1)] = pad[c * (n + 7) + J];                   /* cells -2..0 */
+      u[c + 3 * (n + 2 + J)] = pad[c * (n + 7) + n + 3 + J];       /* cells n+1..n+3 */
+    }
+  free(pad);
+  free(uh);
+  free(fP);
+  free(fM);
+  o->time = o->time + k;
+  return SWFD_OK;
+}
+
+/* initial data of the script's problems (:27-150, :188-205) on the cell
+ * midpoints of xL:h:xR; MATLAB's colon builds the second half of its nodes
+ * from the right end (a + n*d) */
+static void ex1_init(oracle* o) {
+  const int n = o->nx, pr = o->cfg.variant;
+  const double g = o->gamma, pi = 3.141592653589793;
+  double xl = 0, xr = 2 * pi;
+  if (pr == 3) xl = -1, xr = 1;
+  else if (pr == 4) xl = -5, xr = 5;
+  else if (pr == 5) xl = -0.5, xr = 0.5;
+  else if (pr == 6) xl = -3, xr = 3;
+  else if (pr == 7) xl = -0.05, xr = 0.05;
+  const double h = (xr - xl) / n;
+  o->dx = h;
+  const double hi = xl + n * h;
+  for (int i = 1; i <= n; ++i) {
+    const int k0 = i - 1, k1 = i;
+    const double x0 = (2 * k0 <= n) ? xl + k0 * h : hi - (n - k0) * h;
+    const double x1 = (2 * k1 <= n) ? xl + k1 * h : hi - (n - k1) * h;
+    const double x = (x0 + x1) / 2;
+    o->x[i + 2] = x;
+    double ro = 0, v = 0, p = 0;
+    const int i1 = x <= 0, i2 = x > 0;
+    switch (pr) {
+      case 1: ro = 1 + 0.2 * sin(x), v = 1, p = 1; break;
+      case 2: ro = 1 + 1. / 2. * sin(x), v = 1. / 2. * sin(x), p = pow(1 + 1. / 2. * sin(x), g); break;
+      case 3: ro = 0 + 1 * i1 + 0.125 * i2, v = 0, p = 0 + 1 * i1 + 0.1 * i2; break;
+      case 4: ro = 0 + 0.445 * i1 + 0.5 * i2, v = 0 + 0.698 * i1 + 0 * i2,
+              p = 0 + 3.528 * i1 + 0.571 * i2; break;
+      case 5: ro = 0 + 7 * i1 + 7 * i2, v = 0 + -1 * i1 + 1 * i2, p = 0 + 0.2 * i1 + 0.2 * i2; break;
+      case 6: {
+        const int j1 = x >= (-2. / 402.), j2 = x > (2. / 402.);
+        const double E0 = 0 + (3200000. * 201.) * j1 - (3200000. * 201.) * j2 + 1e-12 * 1;
+        ro = 1, v = 0;
+        p = (g - 1) * (E0 - 1. / 2. * ro * (v * v));
+        break;
+      }
+      default: ro = 5, v = 0, p = 0.4127; break;
+    }
+    const double m = v * ro;
+    const double E = p / (g - 1) + 1. / 2. * ro * (v * v);
+    U1(o->u, 0, i) = ro, U1(o->u, 1, i) = m, U1(o->u, 2, i) = E;
+  }
+  o->weight = 1. * 1. / n; /* ones(1,nSteps)*1/nSteps */
+  double* pad = malloc(3 * (n + 7) * sizeof(double));
+  ex1_pad(o, o->u, pad, n + 7);
+  for (int J = 1; J <= 3; ++J)
+    for (int c = 0; c < 3; ++c) {
+      o->u[c + 3 * (J - 1)] = pad[c * (n + 7) + J];
+      o->u[c + 3 * (n + 2 + J)] = pad[c * (n + 7) + n + 3 + J];
+    }
+  free(pad);
+}
+
+/* ------------------------------------------------------------------ */
 /* stage / step / loop                                                 */
 /* ------------------------------------------------------------------ */
 static void wenofd_any(oracle* o) {
@@ -1479,6 +1853,7 @@ static int step_restart1d(oracle* o) {
 
 int oracle_step(oracle* o) {
   if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) return ex6_step(o);
+  if (o->problem == SWFD_PROBLEM_MATLAB_1D) return ex1_step(o);
   if (o->cfg.rk_choice == 2) return step_restart1d(o);
   const size_t n = state_len(o);
   double* u = o->u;
@@ -1511,6 +1886,7 @@ int oracle_step(oracle* o) {
 
 /* time <= time_terminal - 1d-10 (ex3_vortex_accuracy_2d/main.f90:51) */
 int oracle_time_loop_continue(const oracle* o) {
+  if (o->problem == SWFD_PROBLEM_MATLAB_1D) return o->time < o->cfg.time_terminal; /* :212 */
   if (o->quad) return (Q)o->time <= (Q)o->cfg.time_terminal - (Q)1e-10f128;
   return o->time <= o->cfg.time_terminal - 1e-10;
 }
@@ -1547,6 +1923,9 @@ void oracle_init(oracle* o) {
   o->sweep_count = o->den_count = o->pre_count = o->fail_count = 0;
   o->status = 0;
   switch (o->problem) {
+    case SWFD_PROBLEM_MATLAB_1D:
+      ex1_init(o);
+      break;
     case SWFD_PROBLEM_SEDOV_1D: { /* ex2_sedov_1d/main.f90:405-428 */
       double xleft = -2., xright = 2.;
       o->dx = (xright - xleft) / nx;
@@ -1624,7 +2003,7 @@ oracle* oracle_create(const swfd_config* cfg) {
   o->cfg = *cfg;
   o->problem = cfg->problem;
   o->quad = cfg->literals == SWFD_LITERALS_QUAD;
-  o->ndim = (cfg->problem == SWFD_PROBLEM_SEDOV_1D) ? 1 : 2;
+  o->ndim = (cfg->problem == SWFD_PROBLEM_SEDOV_1D || cfg->problem == SWFD_PROBLEM_MATLAB_1D) ? 1 : 2;
   o->nc = o->ndim == 1 ? 3 : 4;
   o->nx = cfg->nx;
   o->ny = o->ndim == 1 ? 1 : cfg->ny;

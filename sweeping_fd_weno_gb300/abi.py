@@ -29,6 +29,7 @@ ERR_RESTART_LIMIT = -11
 RESTART_LIMIT = 1100
 
 # problems (one per reference example)
+MATLAB_1D = 1  # ex1_double_rarefaction_1d (MATLAB)
 SEDOV_1D = 2   # ex2_sedov_1d
 VORTEX_2D = 3  # ex3_vortex_accuracy_2d
 SEDOV_2D = 4   # ex4_sedov_2d
@@ -67,7 +68,8 @@ class SwfdConfig(C.Structure):
         ("cut_x", C.c_int32),
         ("cut_y", C.c_int32),
         ("rk_choice", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("variant", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
     def as_dict(self) -> dict:

@@ -21,6 +21,19 @@ namespace swfd {
 // grid spacing exactly as each initdata computes it.
 // Options this build implements; everything else is rejected before any
 // CUDA call.
+// the MATLAB script's domain and boundary treatment per `problem`
+// (ex1_double_rarefaction_1d/FD_WENO_Application.m:27-150)
+void matlab_domain(int variant, double* xl, double* xr) {
+  const double pi = 3.141592653589793;
+  *xl = 0, *xr = 2 * pi;
+  if (variant == 3) *xl = -1, *xr = 1;
+  else if (variant == 4) *xl = -5, *xr = 5;
+  else if (variant == 5) *xl = -0.5, *xr = 0.5;
+  else if (variant == 6) *xl = -3, *xr = 3;
+  else if (variant == 7) *xl = -0.05, *xr = 0.05;
+}
+int matlab_periodic(int variant) { return variant == 1 || variant == 2 || variant == 6; }
+
 swfd_status check_config(const swfd_config& c, std::string& err) {
   auto bad = [&](swfd_status st, const char* m) {
     err = m;
@@ -40,6 +53,14 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
     return bad(SWFD_ERR_INVALID, "unknown sweep_mode");
   if (!(c.gamma > 1.0)) return bad(SWFD_ERR_INVALID, "gamma must be > 1");
   if (c.rk_choice < 0 || c.rk_choice > 2) return bad(SWFD_ERR_INVALID, "rk_choice must be 0, 1 or 2");
+  if (c.problem == SWFD_PROBLEM_MATLAB_1D) {
+    if (c.variant < 1 || c.variant > 7) return bad(SWFD_ERR_INVALID, "variant: the script's problem 1..7");
+    if (c.use_limiter == 1)
+      return bad(SWFD_ERR_UNSUPPORTED, "the MATLAB script has no flux limiter (use_limiter 0 or 2)");
+    if (c.precision != SWFD_PRECISION_FP64)
+      return bad(SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs in FP64 only");
+    if (c.rk_choice == 2) return bad(SWFD_ERR_INVALID, "rk_choice 2 (the restart RK) exists only in ex2");
+  }
   if (c.rk_choice == 2 && c.problem != SWFD_PROBLEM_SEDOV_1D)
     return bad(SWFD_ERR_INVALID, "rk_choice 2 (the dt-halving restart RK) exists only in ex2");
   if (c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
@@ -79,6 +100,19 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
     return SWFD_ERR_INVALID;
   }
   switch (c.problem) {
+    case SWFD_PROBLEM_MATLAB_1D: {  // FD_WENO_Application.m:170-175: h = (xR-xL)/nSteps
+      g.ndim = 1;
+      g.nc = 3;
+      g.nx = c.nx;
+      g.ny = 1;
+      g.LI = c.nx + 6;
+      g.LJ = 1;
+      double xl, xr;
+      matlab_domain(c.variant, &xl, &xr);
+      p.dx = (xr - xl) / c.nx;
+      p.dy = 0;
+      break;
+    }
     case SWFD_PROBLEM_SEDOV_1D: {
       g.ndim = 1;
       g.nc = 3;
@@ -239,6 +273,55 @@ void init_host_state(const Params& p, const swfd_config& cfg, double* u) {
   };
   std::fill(u, u + (size_t)g.nc * g.LI * g.LJ, 0.0);
   switch (p.problem) {
+    case SWFD_PROBLEM_MATLAB_1D: {
+      // FD_WENO_Application.m:27-150,170-205: cell midpoints of xL:h:xR
+      // (MATLAB's colon builds its second half from the right end a + n*d),
+      // rho, v, p of the problem, then m = v*rho, E = p/(gamma-1) + rho v^2/2
+      double xl, xr;
+      matlab_domain(cfg.variant, &xl, &xr);
+      const double h = p.dx, hi = xl + nx * h, gm = p.gamma;
+      for (int i = 1; i <= nx; ++i) {
+        const int k0 = i - 1, k1 = i;
+        const double x0 = (2 * k0 <= nx) ? xl + k0 * h : hi - (nx - k0) * h;
+        const double x1 = (2 * k1 <= nx) ? xl + k1 * h : hi - (nx - k1) * h;
+        const double x = (x0 + x1) / 2;
+        const int i1 = x <= 0, i2 = x > 0;
+        double ro = 0, v = 0, pr = 0;
+        switch (cfg.variant) {
+          case 1: ro = 1 + 0.2 * sin(x), v = 1, pr = 1; break;
+          case 2:
+            ro = 1 + 1. / 2. * sin(x), v = 1. / 2. * sin(x), pr = pow(1 + 1. / 2. * sin(x), gm);
+            break;
+          case 3: ro = 0 + 1 * i1 + 0.125 * i2, v = 0, pr = 0 + 1 * i1 + 0.1 * i2; break;
+          case 4:
+            ro = 0 + 0.445 * i1 + 0.5 * i2, v = 0 + 0.698 * i1 + 0 * i2;
+            pr = 0 + 3.528 * i1 + 0.571 * i2;
+            break;
+          case 5:
+            ro = 0 + 7 * i1 + 7 * i2, v = 0 + -1 * i1 + 1 * i2, pr = 0 + 0.2 * i1 + 0.2 * i2;
+            break;
+          case 6: {
+            const int j1 = x >= (-2. / 402.), j2 = x > (2. / 402.);
+            const double e0 = 0 + (3200000. * 201.) * j1 - (3200000. * 201.) * j2 + 1e-12 * 1;
+            ro = 1, v = 0;
+            pr = (gm - 1) * (e0 - 1. / 2. * ro * (v * v));
+            break;
+          }
+          default: ro = 5, v = 0, pr = 0.4127; break;
+        }
+        U(0, i, -2) = ro;
+        U(1, i, -2) = v * ro;
+        U(2, i, -2) = pr / (gm - 1) + 1. / 2. * ro * (v * v);
+      }
+      // the ghosts hold FD_WENO_Step's padding (wrap or constant extension)
+      const int per = matlab_periodic(cfg.variant);
+      for (int k = 1; k <= 3; ++k)
+        for (int c = 0; c < 3; ++c) {
+          U(c, k - 3, -2) = U(c, per ? nx - 3 + k : 1, -2);
+          U(c, nx + k, -2) = U(c, per ? k : nx, -2);
+        }
+      break;
+    }
     case SWFD_PROBLEM_SEDOV_1D:  // ex2_sedov_1d/main.f90:405-428
       for (int i = -2; i <= nx + 3; ++i) {
         U(0, i, -2) = 1.;
@@ -769,6 +852,14 @@ swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
       cfg->time_terminal = 0.001;
       cfg->gamma = 5. / 3.;
       break;
+    case SWFD_PROBLEM_MATLAB_1D:  // FD_WENO_Application.m:10,95-110,158-165 (problem = 5)
+      cfg->variant = 5;
+      cfg->nx = 200;
+      cfg->ny = 1;
+      cfg->swp_num = 200000;
+      cfg->cfl = 0.85;
+      cfg->time_terminal = 0.3;
+      break;
     case SWFD_PROBLEM_SHOCK_DIFFRACTION:  // ex6_shock_diffraction/main.f90:16-20,695
       cfg->total = 80;
       cfg->cut_x = 4;
@@ -830,6 +921,9 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     h->p.wall_save = h->p.seg_ay + (size_t)g.LI * h->p.cut_y;
   }
   if ((e = cudaMalloc(&h->rhs_tmp, g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
+  if (cfg->problem == SWFD_PROBLEM_MATLAB_1D &&
+      (e = cudaMalloc(&h->m1_wk, matlab1d_workspace(g.nx) * sizeof(double))) != cudaSuccess)
+    return cleanup_fail(e);
   if ((e = cudaMalloc(&h->dsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMallocHost(&h->hsc, sizeof(DevScalars))) != cudaSuccess) return cleanup_fail(e);
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
@@ -870,6 +964,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->flux);
   cudaFree(h->seg_buf);
   cudaFree(h->rhs_tmp);
+  cudaFree(h->m1_wk);
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);
@@ -940,10 +1035,31 @@ swfd_status swfd_set_time(swfd_handle* h, double t) {
   return SWFD_OK;
 }
 
+// the MATLAB script's scheme: up to max_steps steps in one launch
+swfd_status matlab1d_steps(swfd_handle* h, long long max_steps, int64_t* steps_out) {
+  ST(ensure_tracks(h, 3 * max_steps));
+  DevScalars before = *h->hsc;
+  CU(h, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), h->stream));
+  CU(h, launch_matlab1d(h->p, cur_state(h), h->m1_wk, h->dsc, max_steps,
+                        matlab_periodic(h->cfg.variant), h->cfg.use_limiter == 2, h->cfg.swp_num,
+                        h->cfg.cfl, h->stream));
+  swfd_status st = check_device_error(h);
+  if (steps_out) *steps_out = h->hsc->steps;
+  h->prof.kernel_launches += 1;
+  h->prof.stages += 3 * h->hsc->steps;
+  h->prof.sweep_invocations += h->hsc->sweep_count - before.sweep_count;
+  return st;
+}
+
 swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
   CU(h, cudaSetDevice(h->device));
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
+    swfd_status st = matlab1d_steps(h, 1, nullptr);
+    if (dt_out) *dt_out = h->hsc->dt;
+    return st;
+  }
   ST(build_graph(h, GRAPH_STEP, &h->g_step));
   ST(ensure_tracks(h, 3));
   DevScalars before = *h->hsc;
@@ -964,7 +1080,8 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
 
 swfd_status swfd_step_async(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
-  if (h->eager) return swfd_step(h, nullptr);  // eager sections read conditions on the host
+  if (h->eager || h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+    return swfd_step(h, nullptr);  // eager sections read conditions on the host
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_STEP, &h->g_step));
   // a step records at most three sweeps: grow the track arrays (after
@@ -1038,6 +1155,31 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
   CU(h, cudaSetDevice(h->device));
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
+    // while t < tFinal (FD_WENO_Application.m:212), tested on the device
+    int64_t done = 0;
+    swfd_status st = SWFD_OK;
+    const int64_t chunk = 4096;
+    while (h->time < h->cfg.time_terminal) {
+      if (max_steps > 0 && done >= max_steps) {
+        st = SWFD_ERR_MAX_STEPS;
+        break;
+      }
+      const long long lim =
+          (long long)(max_steps > 0 ? std::min<int64_t>(chunk, max_steps - done) : chunk);
+      int64_t steps = 0;
+      const double t_before = h->time;
+      st = matlab1d_steps(h, lim, &steps);
+      done += steps;
+      if (st != SWFD_OK || steps < lim) break;
+      if (!(h->time > t_before)) {  // k = 0 (an infinite alpha): the script would loop forever
+        st = fail(h, SWFD_ERR_NONFINITE, "the time step is 0: the time loop does not advance");
+        break;
+      }
+    }
+    if (nsteps_out) *nsteps_out = done;
+    return st;
+  }
   ST(build_graph(h, GRAPH_SOLVE, &h->g_solve));
   int64_t done = 0;
   const int64_t chunk = 4096;  // steps per graph launch (bounds the track growth)
@@ -1069,6 +1211,8 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
 swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
   if (!h || !rhs) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
   const Params& p = h->p;
   double* u = cur_state(h);
@@ -1087,6 +1231,8 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
 swfd_status swfd_sweep(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_SWEEP, &h->g_sweep));
   ST(ensure_tracks(h, 1));
@@ -1100,6 +1246,8 @@ swfd_status swfd_sweep(swfd_handle* h) {
 swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
   if (!h || !postag) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
   CU(h, launch_positivity(h->p, cur_state(h), h->dsc, h->stream));
   ST(sync_scalars(h));
@@ -1110,6 +1258,8 @@ swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
 swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax) {
   if (!h || !alphamax) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
   CU(h, launch_alpha(h->p, cur_state(h), h->dsc, h->stream));
   ST(sync_scalars(h));

@@ -258,6 +258,7 @@ struct swfd_handle {
   // before the first of them
   int64_t pending = 0;
   swfd::DevScalars pending_before{};
+  double* m1_wk = nullptr;  // the MATLAB 1D scheme's workspace
   // eager launch mode (SWFD_LAUNCH=eager): the graph sections run as plain
   // stream launches and the conditions are read back on the host; for
   // profilers that do not look inside graphs with conditional nodes
@@ -292,6 +293,13 @@ cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void
 // kernel and its count of finished warps; the kernel leaves them zero)
 cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
                         const DevScalars* dsc, void* flux, int* work, cudaStream_t s);
+// the MATLAB script's scheme (swfd_matlab1d.cu): up to max_steps steps of
+// `while t < tFinal` in one single-block launch; wk holds
+// matlab1d_workspace(nx) doubles
+int64_t matlab1d_workspace(int n);
+cudaError_t launch_matlab1d(const Params& p, double* u, double* wk, DevScalars* d,
+                            long long max_steps, int periodic, int sweeping, int swp_num,
+                            double cfl, cudaStream_t s);
 // decide 1 / 2: set the IF condition hs (0: the condition word) to postag / !postag
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
                       const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,

@@ -17,8 +17,10 @@ def reference_defaults(problem: int) -> dict:
                 literals=abi.LITERALS_DOUBLE, precision=abi.PRECISION_FP64,
                 ubar_mode=abi.UBAR_SEQUENTIAL, sweep_mode=abi.SWEEP_PARALLEL, device=0, gamma=1.4,
                 e_background=0.0,
-                e_blast=0.0, ny=1, total=0, cut_x=0, cut_y=0, rk_choice=1)
-    if problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425 (RK_choice = 1)
+                e_blast=0.0, ny=1, total=0, cut_x=0, cut_y=0, rk_choice=1, variant=0)
+    if problem == abi.MATLAB_1D:     # FD_WENO_Application.m:10,17,95-110,207 (problem = 5)
+        base.update(matlab_problem(5), swp_num=200000)
+    elif problem == abi.SEDOV_1D:      # ex2_sedov_1d/main.f90:4-7,423-425 (RK_choice = 1)
         base.update(nx=800, ny=1, swp_num=50, cfl=1.2, time_terminal=0.001,
                     e_background=1e-9 / (1.4 - 1.0), e_blast=3200000.0)
     elif problem == abi.VORTEX_2D:   # ex3_vortex_accuracy_2d/main.f90:5-7,570
@@ -33,6 +35,25 @@ def reference_defaults(problem: int) -> dict:
     else:
         raise ValueError(f"unknown problem {problem}")
     return base
+
+
+# The MATLAB script's problems (ex1_double_rarefaction_1d/FD_WENO_Application.m
+# :27-150 and its nArray :158-165): gamma, final time and grid size.  The
+# script defines cfl = 0.85 for problem 5 only; the others take the same.
+MATLAB_PROBLEMS = {
+    1: dict(gamma=1.4, time_terminal=2.0, nx=80),      # linear advection (nArray 20..320)
+    2: dict(gamma=3.0, time_terminal=0.3, nx=80),      # nonlinear (nArray 20..320)
+    3: dict(gamma=1.4, time_terminal=0.4, nx=200),     # Sod shock tube
+    4: dict(gamma=1.4, time_terminal=1.3, nx=200),     # Lax
+    5: dict(gamma=1.4, time_terminal=0.3, nx=200),     # double rarefaction (as shipped)
+    6: dict(gamma=1.4, time_terminal=0.0004, nx=801),  # point energy
+    7: dict(gamma=1.4, time_terminal=0.00001, nx=200), # jet ambient state (no nArray)
+}
+
+
+def matlab_problem(variant: int) -> dict:
+    d = dict(MATLAB_PROBLEMS[variant])
+    return dict(d, variant=variant, ny=1, cfl=0.85, use_limiter=2)
 
 
 def shock_grid(total: int, cut_x: int = 4, cut_y: int = 8) -> dict:

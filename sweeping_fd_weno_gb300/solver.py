@@ -29,7 +29,7 @@ class Solver:
         h = C.c_void_p()
         abi.check(self.lib.swfd_create(C.byref(cfg), C.byref(h)))
         self.h = h
-        self.ndim = 1 if cfg.problem == abi.SEDOV_1D else 2
+        self.ndim = 1 if cfg.problem in (abi.SEDOV_1D, abi.MATLAB_1D) else 2
         self.nc = 3 if self.ndim == 1 else 4
         self.nx = cfg.nx
         self.ny = 1 if self.ndim == 1 else cfg.ny

@@ -24,8 +24,8 @@ def test_library_exports_every_declared_symbol(swfd):
     assert sorted(abi.exported_names()) == names
 
 
-@pytest.mark.parametrize("problem", [abi.SEDOV_1D, abi.VORTEX_2D, abi.SEDOV_2D, abi.JET_2D,
-                                     abi.SHOCK_DIFFRACTION])
+@pytest.mark.parametrize("problem", [abi.MATLAB_1D, abi.SEDOV_1D, abi.VORTEX_2D, abi.SEDOV_2D,
+                                     abi.JET_2D, abi.SHOCK_DIFFRACTION])
 def test_config_default_matches_reference_parameters(swfd, problem):
     c = abi.config_default(problem).as_dict()
     ref = problems.reference_defaults(problem)
@@ -46,6 +46,10 @@ def test_create_rejects_bad_configs_without_cuda(swfd):
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     cfg = problems.make_config(abi.SEDOV_1D, rk_choice=3)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.MATLAB_1D, variant=9)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    cfg = problems.make_config(abi.MATLAB_1D, precision=abi.PRECISION_FP32_BULK)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
     cfg = problems.make_config(abi.VORTEX_2D, swp_num=0)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     assert "swp_num" in abi.last_error()

@@ -53,7 +53,7 @@ def test_point_energy_fp32_bulk_close_to_fp64(swfd, oracle_mod, case):
     for _ in range(steps):
         g.step()
         o.step()
-    ndim = 1 if p == abi.SEDOV_1D else 2
+    ndim = 1 if p in (abi.SEDOV_1D, abi.MATLAB_1D) else 2
     ug, uo = interior(g.state(), ndim), interior(o.state(), ndim)
     err = rel_l1(ug[..., 0], uo[..., 0])
     assert err < 1e-6, err
