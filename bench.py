@@ -365,6 +365,45 @@ def serving_draw(device, plain_fp64=False):
     return draw
 
 
+def bench_point_energy_1d(args, local):
+    """The reference's CPU-runnable case (1D point energy, 800 cells on [-2,2],
+    E=1e-12 background, CFL 0.6, swp_num 2, T = 0.001): the whole run on the
+    GPU (the time loop on the device, one solve graph) next to the oracle on
+    one host core -- a CPU baseline leg -- and the MATLAB script of ex1 (its
+    double rarefaction as shipped) on the GPU."""
+    import numpy as np
+    import oracle
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, abi, problems
+    out = {}
+    for name, cfg in (("point_energy_1d", problems.workload("sedov1d_fp64", device=local)),
+                      ("matlab_double_rarefaction",
+                       problems.make_config(abi.MATLAB_1D, device=local,
+                                            **problems.matlab_problem(5)))):
+        s = Solver(cfg)
+        s.init_problem()
+        s.run(3)                      # captures the solve graph
+        s.init_problem()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n = s.run()
+        torch.cuda.synchronize()
+        gpu_s = time.perf_counter() - t0
+        u = s.state()
+        s.close()
+        o = oracle.Oracle(cfg)
+        o.init_problem()
+        t0 = time.perf_counter()
+        n_o = o.run()
+        cpu_s = time.perf_counter() - t0
+        out[name] = {"cells": int(cfg.nx), "steps": int(n), "t_end": float(cfg.time_terminal),
+                     "gpu_s": gpu_s, "gpu_us_per_step": gpu_s / n * 1e6,
+                     "cpu_oracle_s": cpu_s, "cpu_cores": 1,
+                     "same_result": bool(n == n_o and np.array_equal(u, o.state())),
+                     "speedup_vs_cpu": cpu_s / gpu_s}
+    return out
+
+
 def bench_serving(args, local):
     """Poisson arrivals (mean 50 req/s) served by continuous batching (an
     FP32-bulk batch and an FP64 batch side by side) and, for comparison, one
@@ -692,6 +731,8 @@ def main():
         line["serving"] = bench_serving(args, local)
     if args.batch_full:
         line["batched_to_completion"] = bench_batched_full(args, local)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["one_d"] = bench_point_energy_1d(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
     if rank == 0:

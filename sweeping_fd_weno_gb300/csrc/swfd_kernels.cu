@@ -204,11 +204,28 @@ __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc,
   if (with_dt) dt_body(p, dsc);
 }
 
+// Threads per block of the per-cell kernels: 256, or fewer (down to one warp)
+// on grids too small to give every SM two blocks, so that the FP64 work of a
+// small grid (2 FP64 instructions per clock per SM) spreads over the SMs.
+// The per-cell results do not depend on it.
+static int cell_block(int64_t cells) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int b = SWFD_BLOCK;
+  while (b > 32 && (cells + b - 1) / b < 2 * sms) b >>= 1;
+  return b;
+}
+
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
                          bool with_dt) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
-  k_alpha<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(p, u, dsc,
-                                                                               with_dt ? 1 : 0);
+  const int b = cell_block(n);
+  k_alpha<<<(unsigned)((n + b - 1) / b), b, 0, s>>>(p, u, dsc, with_dt ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -530,14 +547,15 @@ cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc,
                         void* roe, cudaStream_t s, int which) {
   const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (p.g.ndim == 1) {
-    const int gb = (p.g.LI + SWFD_BLOCK - 1) / SWFD_BLOCK;
-    if (f32) k_prep1d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split);
-    else k_prep1d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split);
+    const int b = cell_block(p.g.LI), gb = (p.g.LI + b - 1) / b;
+    if (f32) k_prep1d<float><<<gb, b, 0, s>>>(p, u, dsc, (float*)split);
+    else k_prep1d<double><<<gb, b, 0, s>>>(p, u, dsc, (double*)split);
   } else {
     int64_t n = (int64_t)p.g.LI * p.g.LJ;
-    const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
-    if (f32) k_prep2d<float><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (float*)split, (float*)roe, which);
-    else k_prep2d<double><<<gb, SWFD_BLOCK, 0, s>>>(p, u, dsc, (double*)split, (double*)roe, which);
+    const int b = cell_block(n);
+    const unsigned gb = (unsigned)((n + b - 1) / b);
+    if (f32) k_prep2d<float><<<gb, b, 0, s>>>(p, u, dsc, (float*)split, (float*)roe, which);
+    else k_prep2d<double><<<gb, b, 0, s>>>(p, u, dsc, (double*)split, (double*)roe, which);
   }
   return cudaGetLastError();
 }
@@ -942,12 +960,12 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
   const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (g.ndim == 1) {
     // the 1D eigenvectors come from the state, which the caller passes as roe
-    const int gb = (g.nx + 2 + 127) / 128;
+    const int b = cell_block(g.nx + 2), gb = (g.nx + 2 + b - 1) / b;
     if (f32)
-      k_flux1d<float><<<gb, 128, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
+      k_flux1d<float><<<gb, b, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
     else
-      k_flux1d<double><<<gb, 128, 0, s>>>(p, (const double*)roe, (const double*)split,
-                                           (double*)flux);
+      k_flux1d<double><<<gb, b, 0, s>>>(p, (const double*)roe, (const double*)split,
+                                         (double*)flux);
     return cudaGetLastError();
   }
   if (f32)
@@ -1093,13 +1111,14 @@ cudaError_t launch_rk(const Params& p, int stage, const double* u, const double*
                       const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
                       cudaGraphConditionalHandle hs, int decide) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
-  const unsigned gb = (unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK);
+  const int b = cell_block(n);
+  const unsigned gb = (unsigned)((n + b - 1) / b);
   if (p.precision == SWFD_PRECISION_FP32_BULK)
-    k_rk<float><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const float*)flux,
-                                          const_cast<DevScalars*>(dsc), out, hs, decide);
+    k_rk<float><<<gb, b, 0, s>>>(p, stage, u, u0, (const float*)flux,
+                                 const_cast<DevScalars*>(dsc), out, hs, decide);
   else
-    k_rk<double><<<gb, SWFD_BLOCK, 0, s>>>(p, stage, u, u0, (const double*)flux,
-                                           const_cast<DevScalars*>(dsc), out, hs, decide);
+    k_rk<double><<<gb, b, 0, s>>>(p, stage, u, u0, (const double*)flux,
+                                  const_cast<DevScalars*>(dsc), out, hs, decide);
   return cudaGetLastError();
 }
 
