@@ -424,6 +424,19 @@ def bench_serving(args, local):
                              serving_draw(local, plain_fp64=True))
     rp = serve_one_at_a_time(plain)
     sb, sp = rb.summary(), rp.summary()
+    # the same kind of stream through the C host request loop over the batch
+    # C-ABI (host/swfd_serve.c, its own seeded draw of the same mix)
+    c_host = None
+    serve = ROOT / "sweeping_fd_weno_gb300" / "_lib" / "swfd_serve"
+    if serve.exists():
+        r = subprocess.run([str(serve), "--requests", str(args.serve_requests), "--rate",
+                            str(args.serve_rate), "--seed", str(SERVE_SEED), "--slots",
+                            str(args.serve_slots), "--chunk", str(args.serve_chunk),
+                            "--device", str(local)], capture_output=True, text=True, timeout=900)
+        if r.returncode == 0:
+            c_host = json.loads(r.stdout.strip().splitlines()[-1])
+        else:
+            c_host = {"error": r.stderr.strip()[-300:]}
     kinds = {}
     for _, c in arr:
         kinds[int(c.problem)] = kinds.get(int(c.problem), 0) + 1
@@ -439,6 +452,7 @@ def bench_serving(args, local):
         "batched": sb, "plain_fp64_one_at_a_time": sp,
         "throughput_ratio": (sb["value"] / sp["value"]) if sp["value"] else None,
         "slots": args.serve_slots, "step_chunk": args.serve_chunk,
+        "c_host_loop": c_host,
     }
 
 

@@ -72,6 +72,20 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
             print(r.stdout, r.stderr)
         if r.returncode != 0:
             raise RuntimeError("nvcc link of libswfd.so failed")
+    # the C host request loop over the batch API (host/swfd_serve.c)
+    serve, src = OUT / "swfd_serve", PKG / "host" / "swfd_serve.c"
+    if force or not serve.exists() or serve.stat().st_mtime < max(src.stat().st_mtime,
+                                                                  lib.stat().st_mtime):
+        cuda_lib = Path(cc).resolve().parent.parent / "lib64"
+        cmd = ["gcc", "-O2", "-std=c11", "-Wall", "-I", str(PKG.parent / "include"), str(src),
+               "-L", str(OUT), "-lswfd", "-L", str(cuda_lib), "-lcudart", "-lpthread", "-lm",
+               "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + str(cuda_lib), "-o", str(serve)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            print(" ".join(cmd))
+            print(r.stdout, r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("gcc build of swfd_serve failed")
     return lib
 
 
