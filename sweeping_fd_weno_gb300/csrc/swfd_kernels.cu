@@ -671,10 +671,20 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
 template <class T>
 __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
                          T* __restrict__ flux) {
+  // eight lanes per cell: lanes 0..5 of a group each reconstruct one
+  // characteristic field (k = lane / 2) of one side (lane % 2: the positive
+  // flux at the right face, the negative one), so that the six WENO chains of
+  // a cell run side by side instead of one after another in one thread (a
+  // tiny 1D grid leaves the FP64 pipes idle and its time is the length of
+  // these dependent chains); the group then exchanges the six values and
+  // lanes 0..5 form the six output components.  Every value is computed by
+  // the same expression as in a one-thread-per-cell form.
   const Geom& g = p.g;
-  int m = blockIdx.x * blockDim.x + threadIdx.x;  // 0..n+1
-  if (m > g.nx + 1) return;
-  const int64_t P = g.plane, o = g.at(m, -2);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = t >> 3, sub = t & 7;  // cell 0..n+1, lane in its group
+  const bool active = m <= g.nx + 1;
+  const int mm = active ? m : g.nx + 1;  // inactive lanes repeat the last cell
+  const int64_t P = g.plane, o = g.at(mm, -2);
   const double g1d = p.gamma1;
   double u1 = ld(u + o), u2 = ld(u + P + o), u3 = ld(u + 2 * P + o);
   double vxd = u2 / u1;
@@ -693,28 +703,31 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
   T L[3][3] = {{T(0.5) * (b2 + t0), -T(0.5) * (t1 + rcm), t2},
                {T(1.) - b2, t1, -b1},
                {T(0.5) * (b2 - t0), -T(0.5) * (t1 - rcm), t2}};
-  T ur[3], ul[3];
   const T weps = T(p.weno_eps);
+  const int k = sub < 6 ? sub >> 1 : 0, side = sub & 1;
+  const T* sp = split + (side ? 3 * P : 0);
+  T cs[5];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    T cp[5], cn[5];
-#pragma unroll
-    for (int jj = 0; jj < 5; ++jj) {
-      const int64_t s = o + jj - 2;
-      cp[jj] = L[k][0] * ldt(split + s) + L[k][1] * ldt(split + P + s) +
-               L[k][2] * ldt(split + 2 * P + s);
-      cn[jj] = L[k][0] * ldt(split + 3 * P + s) + L[k][1] * ldt(split + 4 * P + s) +
-               L[k][2] * ldt(split + 5 * P + s);
-    }
-    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
-    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+  for (int jj = 0; jj < 5; ++jj) {
+    const int64_t s = o + jj - 2;
+    cs[jj] = L[k][0] * ldt(sp + s) + L[k][1] * ldt(sp + P + s) + L[k][2] * ldt(sp + 2 * P + s);
   }
-  flux[o] = ur[0] + ur[1] + ur[2];
-  flux[P + o] = r10 * ur[0] + vxm * ur[1] + r12 * ur[2];
-  flux[2 * P + o] = r20 * ur[0] + qm * ur[1] + r22 * ur[2];
-  flux[3 * P + o] = ul[0] + ul[1] + ul[2];
-  flux[4 * P + o] = r10 * ul[0] + vxm * ul[1] + r12 * ul[2];
-  flux[5 * P + o] = r20 * ul[0] + qm * ul[1] + r22 * ul[2];
+  const T v = side ? weno_left(cs[0], cs[1], cs[2], cs[3], cs[4], weps)
+                   : weno_right(cs[0], cs[1], cs[2], cs[3], cs[4], weps);
+  const int base = threadIdx.x & ~7 & 31;
+  const T ur0 = __shfl_sync(0xffffffffu, v, base + 0), ul0 = __shfl_sync(0xffffffffu, v, base + 1);
+  const T ur1 = __shfl_sync(0xffffffffu, v, base + 2), ul1 = __shfl_sync(0xffffffffu, v, base + 3);
+  const T ur2 = __shfl_sync(0xffffffffu, v, base + 4), ul2 = __shfl_sync(0xffffffffu, v, base + 5);
+  if (!active) return;
+  switch (sub) {
+    case 0: flux[o] = ur0 + ur1 + ur2; break;
+    case 1: flux[P + o] = r10 * ur0 + vxm * ur1 + r12 * ur2; break;
+    case 2: flux[2 * P + o] = r20 * ur0 + qm * ur1 + r22 * ur2; break;
+    case 3: flux[3 * P + o] = ul0 + ul1 + ul2; break;
+    case 4: flux[4 * P + o] = r10 * ul0 + vxm * ul1 + r12 * ul2; break;
+    case 5: flux[5 * P + o] = r20 * ul0 + qm * ul1 + r22 * ul2; break;
+    default: break;
+  }
 }
 
 // Both directions in one persistent launch: a grid of exactly the resident
@@ -960,7 +973,8 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
   const bool f32 = p.precision == SWFD_PRECISION_FP32_BULK;
   if (g.ndim == 1) {
     // the 1D eigenvectors come from the state, which the caller passes as roe
-    const int b = cell_block(g.nx + 2), gb = (g.nx + 2 + b - 1) / b;
+    const int64_t lanes = 8 * (int64_t)(g.nx + 2);  // eight lanes per cell
+    const int b = cell_block(lanes), gb = (int)((lanes + b - 1) / b);
     if (f32)
       k_flux1d<float><<<gb, b, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
     else
@@ -1088,12 +1102,8 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
 // the IF condition hs to postag (the sweep, ex3_vortex_accuracy_2d/main.f90:
 // 590-595), decide 2 to !postag (the restart RK's next stage,
 // ex2_sedov_1d/main.f90:349-364).
-template <class T>
-__global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
-                     const T* __restrict__ flux, DevScalars* dsc, double* out,
-                     cudaGraphConditionalHandle hs, int decide) {
-  int bad = rk_cell<T>(p, stage, u, u0, flux, dsc->dt, dsc->alphamax, out,
-                       (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void rk_block_done(DevScalars* dsc, int bad, int stage,
+                                              cudaGraphConditionalHandle hs, int decide) {
   bad = block_or(bad);
   if (threadIdx.x != 0) return;
   if (bad) atomicOr(&dsc->postag, 1);
@@ -1107,10 +1117,75 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
   else if (decide == 2) set_cond(hs, &dsc->cond, tag ? 0u : 1u);
 }
 
+template <class T>
+__global__ void k_rk(Params p, int stage, const double* __restrict__ u, const double* u0,
+                     const T* __restrict__ flux, DevScalars* dsc, double* out,
+                     cudaGraphConditionalHandle hs, int decide) {
+  int bad = rk_cell<T>(p, stage, u, u0, flux, dsc->dt, dsc->alphamax, out,
+                       (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  rk_block_done(dsc, bad, stage, hs, decide);
+}
+
+// 1D: four lanes per cell, lane c < 3 forming component c (its RHS and RK
+// combination are a chain of their own), lane 0 testing the cell's
+// positivity from the three new values; the expressions are rk_cell's.
+template <class T>
+__global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const double* u0,
+                       const T* __restrict__ flux, DevScalars* dsc, double* out,
+                       cudaGraphConditionalHandle hs, int decide) {
+  const Geom& g = p.g;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int cell = (int)(t >> 2), c = (int)(t & 3);
+  const bool in_grid = cell < g.LI;
+  const int i = cell - 2;
+  const bool interior = in_grid && i >= 1 && i <= g.nx;
+  const int64_t P = g.plane, o = in_grid ? g.at(i, -2) : 0;
+  double v = 0.0;
+  if (in_grid && c < 3) {
+    const double dt = dsc->dt;
+    double r = 0.0;
+    if (interior) r = (double)rhs1d<T>(p, flux, c, o, dsc->alphamax);
+    if (sizeof(T) == 4) {
+      v = fma(dt, r, ld(u + c * P + o));
+      if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
+      else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
+    } else {
+      v = ld(u + c * P + o) + dt * r;
+      if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
+      else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+    }
+    out[c * P + o] = v;
+  }
+  const int base = threadIdx.x & ~3 & 31;
+  const double n0 = __shfl_sync(0xffffffffu, v, base), n1 = __shfl_sync(0xffffffffu, v, base + 1),
+               n2 = __shfl_sync(0xffffffffu, v, base + 2);
+  int bad = 0;
+  if (interior && c == 0) {
+    double pe;
+    if (sizeof(T) == 4) pe = fma(n1 * n1, -0.5 / n0, n2);
+    else pe = n2 - n1 * n1 / n0 / 2.;
+    if (p.pos_strict) bad = (n0 < p.eps) || (pe < p.eps);
+    else bad = (n0 <= p.eps) || (pe <= p.eps);
+  }
+  rk_block_done(dsc, bad, stage, hs, decide);
+}
+
 cudaError_t launch_rk(const Params& p, int stage, const double* u, const double* u0,
                       const void* flux, const DevScalars* dsc, double* out, cudaStream_t s,
                       cudaGraphConditionalHandle hs, int decide) {
   int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  if (p.g.ndim == 1) {  // four lanes per cell
+    const int64_t lanes = 4 * n;
+    const int b = cell_block(lanes);
+    const unsigned gb = (unsigned)((lanes + b - 1) / b);
+    if (p.precision == SWFD_PRECISION_FP32_BULK)
+      k_rk1d<float><<<gb, b, 0, s>>>(p, stage, u, u0, (const float*)flux,
+                                     const_cast<DevScalars*>(dsc), out, hs, decide);
+    else
+      k_rk1d<double><<<gb, b, 0, s>>>(p, stage, u, u0, (const double*)flux,
+                                      const_cast<DevScalars*>(dsc), out, hs, decide);
+    return cudaGetLastError();
+  }
   const int b = cell_block(n);
   const unsigned gb = (unsigned)((n + b - 1) / b);
   if (p.precision == SWFD_PRECISION_FP32_BULK)
