@@ -327,6 +327,9 @@ swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const double* u,
 /* Measured FP64 FMA throughput of the device in GFLOP/s (2 flops per FMA):
  * the denominator of the FP64-pipe roofline of the FP64 path. */
 swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops);
+/* The FP32-bulk form's reciprocal (an FP32 seed refined by two Newton steps
+ * in FP64) applied to n host values on the device, for its error test. */
+swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n, double* out);
 
 /* Last error message of the handle (or of the process when h is NULL). */
 swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len);

@@ -35,6 +35,22 @@ __device__ __forceinline__ double tabs(double a) { return fabs(a); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double dsq(double a) { return a * a; }
 
+// 1/x for the FP32-bulk form, whose results are not bit-exact by design:
+// the FP32 reciprocal as the seed and two Newton-Raphson steps
+// r <- r + r (1 - x r) in FP64.  Each step squares the relative error
+// (2^-23 -> 2^-46 -> below 2^-53), so the result is within an ulp or two of
+// 1/x for fewer FP64 instructions than the IEEE division; magnitudes the
+// FP32 seed cannot hold (decided on the exponent bits) take the division.
+__device__ __forceinline__ double rcp_bulk(double x) {
+  const int ex = (__double2hiint(x) >> 20) & 0x7ff;
+  if (ex < 1023 - 120 || ex > 1023 + 120) return 1.0 / x;
+  double r = (double)__frcp_rn((float)x);
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
 // beta(1:3) (weno5.f90:100-102); am2..ap2 = average(-2..2)
 template <class T>
 __device__ __forceinline__ void weno_beta(T am2, T am1, T a0, T ap1, T ap2, T& b1, T& b2, T& b3) {

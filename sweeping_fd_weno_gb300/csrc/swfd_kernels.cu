@@ -128,10 +128,11 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
       double sound = sqrt(gamma * pres / u1);
       a = fabs(u2 / u1) + sound;
     } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
-      // FP32-bulk: the same quantities in FP64 with one reciprocal per cell
+      // FP32-bulk: the pressure recovered in FP64 (one reciprocal per cell);
+      // the CFL quantities (velocities, sound speed, their max) in FP32
       double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
              u4 = ld(u + 3 * g.plane + o);
-      const double ri = 1.0 / u1;
+      const double ri = rcp_bulk(u1);
       double pres;
       if (!p.alpha_guarded) {
         pres = g1 * fma(-0.5 * ri, fma(u2, u2, u3 * u3), u4);
@@ -139,8 +140,9 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
         const double vx = u1 >= p.eps2 ? u2 * ri : 0., vy = u1 >= p.eps2 ? u3 * ri : 0.;
         pres = g1 * fma(-0.5 * u1, fma(vx, vx, vy * vy), u4);
       }
-      const double sound = sqrt(gamma * pres * ri);
-      a = fmax(fabs(u2 * ri), fabs(u3 * ri)) + sound;
+      const float fri = (float)ri;
+      const float sound = sqrtf((float)gamma * (float)pres * fri);
+      a = (double)(fmaxf(fabsf((float)u2 * fri), fabsf((float)u3 * fri)) + sound);
     } else {
       double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
              u4 = ld(u + 3 * g.plane + o);
@@ -357,7 +359,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   const double g1 = p.gamma1;
   double rho = ld(u + o), mx = ld(u + P + o), my = ld(u + 2 * P + o), e = ld(u + 3 * P + o);
   constexpr bool F32 = sizeof(T) == 4;  // FP32-bulk: FP64 with one reciprocal per cell
-  const double ri = F32 ? 1. / rho : 0.;
+  const double ri = F32 ? rcp_bulk(rho) : 0.;
   if constexpr (F32) {
     if (!p.seg_alpha) {
       // FP32-bulk: the pressure recovered in FP64 (fused multiply-adds, one
@@ -1082,7 +1084,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
       double pe;
       if (sizeof(T) == 4) {  // FP32-bulk: FP64 with one reciprocal
-        const double ri = -0.5 / nv[0];
+        const double ri = -0.5 * rcp_bulk(nv[0]);
         if (g.ndim == 1) pe = fma(nv[1] * nv[1], ri, nv[2]);
         else pe = fma(fma(nv[2], nv[2], nv[1] * nv[1]), ri, nv[3]);
       } else if (g.ndim == 1) {
@@ -1162,7 +1164,7 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
   int bad = 0;
   if (interior && c == 0) {
     double pe;
-    if (sizeof(T) == 4) pe = fma(n1 * n1, -0.5 / n0, n2);
+    if (sizeof(T) == 4) pe = fma(n1 * n1, -0.5 * rcp_bulk(n0), n2);
     else pe = n2 - n1 * n1 / n0 / 2.;
     if (p.pos_strict) bad = (n0 < p.eps) || (pe < p.eps);
     else bad = (n0 <= p.eps) || (pe <= p.eps);

@@ -2,6 +2,7 @@
 // is bounded by the FP64 pipe, whose peak is not a published constant of
 // this part; this kernel measures it (independent DFMA chains, 8 per thread).
 #include "swfd_internal.h"
+#include "swfd_device.cuh"
 
 namespace {
 
@@ -17,7 +18,31 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
   if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+__global__ void k_rcp_bulk(const double* __restrict__ x, double* __restrict__ out, int64_t n) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = swfd::rcp_bulk(x[k]);
+}
+
 }  // namespace
+
+// the FP32-bulk reciprocal on host values, for its error-bound test
+extern "C" swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n,
+                                           double* out) {
+  if (!x || !out || n < 0 || n > (int64_t)1 << 26) return SWFD_ERR_INVALID;
+  if (n == 0) return SWFD_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return SWFD_ERR_CUDA;
+  double* d = nullptr;
+  if (cudaMalloc(&d, 2 * n * sizeof(double)) != cudaSuccess) return SWFD_ERR_OOM;
+  cudaError_t e = cudaMemcpy(d, x, n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_rcp_bulk<<<256, 256>>>(d, d + n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? SWFD_OK : SWFD_ERR_CUDA;
+}
 
 extern "C" swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops) {
   if (!gflops) return SWFD_ERR_INVALID;
