@@ -40,8 +40,12 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
     return st;
   };
   if (c.abi_version != SWFD_ABI_VERSION) return bad(SWFD_ERR_INVALID, "abi_version mismatch");
-  if (c.literals != SWFD_LITERALS_DOUBLE)
-    return bad(SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
+  if (c.literals != SWFD_LITERALS_DOUBLE && c.literals != SWFD_LITERALS_QUAD)
+    return bad(SWFD_ERR_INVALID, "unknown literals mode");
+  if (c.literals == SWFD_LITERALS_QUAD &&
+      (c.precision != SWFD_PRECISION_FP64 || c.problem == SWFD_PROBLEM_MATLAB_1D))
+    return bad(SWFD_ERR_UNSUPPORTED,
+               "literals QUAD: the FP64 form of the Fortran examples only");
   if (c.precision != SWFD_PRECISION_FP64 && c.precision != SWFD_PRECISION_FP32_BULK)
     return bad(SWFD_ERR_INVALID, "unknown precision");
   if (c.use_limiter != 0 && c.use_limiter != 1 && c.use_limiter != 2)
@@ -244,6 +248,24 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
     p.sg.LJ = g.LJ + 6 * (p.cut_y - 1);
     p.sg.pitch = ((p.sg.LI + 31) / 32) * 32;
     p.sg.plane = (int64_t)p.sg.pitch * p.sg.LJ;
+  }
+  // DO WHILE (time <= time_terminal - 1d-10), and the literal-dependent
+  // constants of the reference's -fdefault-real-8 build (1d-6, 1d-12, 1d-15,
+  // 1d-8, 1d-10 and 13d0/12d0 as binary128, each the nearest binary128 to the
+  // decimal value: a correctly rounded quotient of exact binary64 integers)
+  p.t_loop = c.time_terminal - 1e-10;
+  if (c.literals == SWFD_LITERALS_QUAD) {
+    using namespace qd;
+    const q128 one = from_double(1.0);
+    p.quad = 1;
+    p.q_c1312 = div(from_double(13.0), from_double(12.0));
+    p.q_weno_eps = div(one, from_double(p.weno_eps == 1e-12 ? 1e12 : 1e6));
+    p.q_1em15 = div(one, from_double(1e15));
+    const q128 c8 = div(one, from_double(1e8));
+    p.lim8_lt = ru(c8);  // rho < c  <=>  rho < ru(c)
+    p.lim8_gt = rd(c8);  // rho > c  <=>  rho > rd(c)
+    p.lim8_le = rd(c8);  // rho <= c <=>  rho <= rd(c)
+    p.t_loop = rd(sub(from_double(c.time_terminal), div(one, from_double(1e10))));
   }
   return SWFD_OK;
 }
@@ -671,14 +693,13 @@ void emit_kind(Builder& b, cudaStream_t s, int kind) {
     B_OK(b, launch_time_advance(h->dsc, s));
     b.k(1);
   } else if (kind == GRAPH_SOLVE) {
-    const double T = h->cfg.time_terminal;
     B_OK(b, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), s));
     cudaGraphConditionalHandle hr = b.handle();
-    B_OK(b, launch_run_cond(hr, h->dsc, T, s));
+    B_OK(b, launch_run_cond(hr, h->dsc, h->p.t_loop, s));
     b.k(1);
     b.cond(s, cudaGraphCondTypeWhile, hr, [&](cudaStream_t sb) {
       emit_step(b, sb, false);
-      B_OK(b, launch_time_advance_cond(hr, h->dsc, T, sb));
+      B_OK(b, launch_time_advance_cond(hr, h->dsc, h->p.t_loop, sb));
       b.k(1);
     });
   } else {
@@ -1186,7 +1207,7 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   swfd_status st = SWFD_OK;
   // DO WHILE (time <= time_terminal - 1d-10)  (ex3_vortex_accuracy_2d/main.f90:51),
   // evaluated on the device after every step
-  while (h->time <= h->cfg.time_terminal - 1e-10) {
+  while (h->time <= h->p.t_loop) {
     if (max_steps > 0 && done >= max_steps) {
       st = SWFD_ERR_MAX_STEPS;
       break;
@@ -1333,8 +1354,10 @@ swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, 
 swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps, int32_t literals,
                              int32_t device, double* uleft, double* uright) {
   if (n < 0 || (n > 0 && !stencils)) return fail(nullptr, SWFD_ERR_INVALID, "bad arguments");
-  if (literals != SWFD_LITERALS_DOUBLE)
-    return fail(nullptr, SWFD_ERR_UNSUPPORTED, "literals: only SWFD_LITERALS_DOUBLE is built");
+  if (literals != SWFD_LITERALS_DOUBLE && literals != SWFD_LITERALS_QUAD)
+    return fail(nullptr, SWFD_ERR_INVALID, "unknown literals mode");
+  if (literals == SWFD_LITERALS_QUAD && weno_eps != 1e-6 && weno_eps != 1e-12)
+    return fail(nullptr, SWFD_ERR_INVALID, "literals QUAD: the reference's epsilons 1e-6, 1e-12");
   if (n == 0) return SWFD_OK;
   CU(nullptr, cudaSetDevice(device));
   double *ds = nullptr, *dl = nullptr, *dr = nullptr;
@@ -1354,7 +1377,8 @@ swfd_status swfd_weno5_batch(const double* stencils, int64_t n, double weno_eps,
       (e = cudaMalloc(&dr, n * sizeof(double))) != cudaSuccess ||
       (e = cudaMemcpyAsync(ds, stencils, 5 * n * sizeof(double), cudaMemcpyHostToDevice, s)) !=
           cudaSuccess ||
-      (e = launch_weno_batch(ds, n, weno_eps, dl, dr, s)) != cudaSuccess ||
+      (e = launch_weno_batch(ds, n, weno_eps, literals == SWFD_LITERALS_QUAD, dl, dr, s)) !=
+          cudaSuccess ||
       (uleft && (e = cudaMemcpyAsync(uleft, dl, n * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
                     cudaSuccess) ||
       (uright && (e = cudaMemcpyAsync(uright, dr, n * sizeof(double), cudaMemcpyDeviceToHost, s)) !=

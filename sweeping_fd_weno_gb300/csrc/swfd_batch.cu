@@ -315,6 +315,8 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
   c.ubar_mode = SWFD_UBAR_SEQUENTIAL;  // validated as the single-instance path
   swfd_status st = check_config(c, err);
   if (st != SWFD_OK) return bfail(b, st, err);
+  if (c.literals != SWFD_LITERALS_DOUBLE)
+    return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine runs the binary64 literals");
   if (c.problem == SWFD_PROBLEM_SEDOV_1D || c.problem == SWFD_PROBLEM_MATLAB_1D)
     return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine holds 2D problems");
   if (c.use_limiter == 1)

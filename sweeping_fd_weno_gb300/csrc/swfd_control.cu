@@ -122,16 +122,16 @@ __global__ void k_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num
 
 // DO WHILE (time <= time_terminal - 1d-10) (ex3_vortex_accuracy_2d/main.f90:51),
 // bounded by the launch's step limit and stopped by an error
-__global__ void k_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end) {
-  bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
+__global__ void k_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop) {
+  bool go = (d->time <= t_loop) && (d->steps < d->steps_limit) && (d->error == 0);
   set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
 // time = time + dt (:53), then the loop test
-__global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end) {
+__global__ void k_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop) {
   d->time = d->time + d->dt;
   d->steps++;
-  bool go = (d->time <= t_end - 1e-10) && (d->steps < d->steps_limit) && (d->error == 0);
+  bool go = (d->time <= t_loop) && (d->steps < d->steps_limit) && (d->error == 0);
   set_cond(h, &d->cond, go ? 1u : 0u);
 }
 
@@ -176,14 +176,14 @@ cudaError_t launch_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_nu
   k_q_end<<<1, 1, 0, s>>>(h, d, swp_num, stop_on_fail);
   return cudaGetLastError();
 }
-cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
+cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop,
                             cudaStream_t s) {
-  k_run_cond<<<1, 1, 0, s>>>(h, d, t_end);
+  k_run_cond<<<1, 1, 0, s>>>(h, d, t_loop);
   return cudaGetLastError();
 }
-cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
+cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop,
                                      cudaStream_t s) {
-  k_time_advance_cond<<<1, 1, 0, s>>>(h, d, t_end);
+  k_time_advance_cond<<<1, 1, 0, s>>>(h, d, t_loop);
   return cudaGetLastError();
 }
 

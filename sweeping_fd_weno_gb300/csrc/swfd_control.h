@@ -17,9 +17,9 @@ cudaError_t launch_sweep_begin(cudaGraphConditionalHandle h, const Params& p, De
 cudaError_t launch_q_begin(const Params& p, DevScalars* d, cudaStream_t s);
 cudaError_t launch_q_end(cudaGraphConditionalHandle h, DevScalars* d, int swp_num, int stop_on_fail,
                          cudaStream_t s);
-cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
+cudaError_t launch_run_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop,
                             cudaStream_t s);
-cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_end,
+cudaError_t launch_time_advance_cond(cudaGraphConditionalHandle h, DevScalars* d, double t_loop,
                                      cudaStream_t s);
 
 }  // namespace swfd

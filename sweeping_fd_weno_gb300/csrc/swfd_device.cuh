@@ -60,6 +60,59 @@ __device__ __forceinline__ void weno_beta(T am2, T am1, T a0, T ap1, T ap2, T& b
   b3 = c1312 * tsq(am2 - T(2.0) * am1 + a0) + T(0.25) * tsq(am2 - T(4.0) * am1 + T(3.0) * a0);
 }
 
+// literals = QUAD (the reference build): the smoothness indicators and the
+// alphas of the nonlinear weights in binary128, as gfortran evaluates
+// 13d0/12d0*(..)**2 + 0.25d0*(..)**2 and 0.3/(1d-6+beta)**2 under
+// -fdefault-real-8, each rounded to binary64 once (weno5.f90:100-106,
+// 134-140); the candidate values and the weights stay binary64
+struct QuadWeno {
+  qd::q128 c1312, eps;  // 13d0/12d0 and the epsilon in binary128
+};
+static __device__ __noinline__ void weno_beta_qd(double am2, double am1, double a0, double ap1,
+                                             double ap2, const QuadWeno& qw, double& b1,
+                                             double& b2, double& b3) {
+  using namespace qd;
+  const q128 m2 = from_double(am2), m1 = from_double(am1), z = from_double(a0);
+  const q128 p1 = from_double(ap1), p2 = from_double(ap2), three = from_double(3.0);
+  q128 s = add(sub(z, scale2(p1, 1)), p2);
+  q128 t = add(sub(mul(three, z), scale2(p1, 2)), p2);
+  b1 = to_double(add(mul(qw.c1312, mul(s, s)), scale2(mul(t, t), -2)));
+  s = add(sub(m1, scale2(z, 1)), p1);
+  b2 = to_double(add(mul(qw.c1312, mul(s, s)), scale2(from_double(dsq(am1 - ap1)), -2)));
+  s = add(sub(m2, scale2(m1, 1)), z);
+  t = add(sub(m2, scale2(m1, 2)), mul(three, z));
+  b3 = to_double(add(mul(qw.c1312, mul(s, s)), scale2(mul(t, t), -2)));
+}
+__device__ __forceinline__ double weno_alpha_qd(double lin, double beta, const QuadWeno& qw) {
+  using namespace qd;
+  const q128 s = add(qw.eps, from_double(beta));
+  return to_double(div(from_double(lin), mul(s, s)));
+}
+static __device__ __noinline__ double weno_right_qd(double am2, double am1, double a0, double ap1,
+                                                double ap2, const QuadWeno& qw) {
+  const double um1 = SWFD_C13 * am2 + SWFD_CM76 * am1 + SWFD_C116 * a0;
+  const double um2 = SWFD_CM16 * am1 + SWFD_C56 * a0 + SWFD_C13 * ap1;
+  const double um3 = SWFD_C13 * a0 + SWFD_C56 * ap1 + SWFD_CM16 * ap2;
+  double b1, b2, b3;
+  weno_beta_qd(am2, am1, a0, ap1, ap2, qw, b1, b2, b3);
+  const double a1 = weno_alpha_qd(0.3, b1, qw), a2 = weno_alpha_qd(0.6, b2, qw),
+               a3 = weno_alpha_qd(0.1, b3, qw);
+  const double s = a1 + a2 + a3;
+  return a1 / s * um3 + a2 / s * um2 + a3 / s * um1;
+}
+static __device__ __noinline__ double weno_left_qd(double am2, double am1, double a0, double ap1,
+                                               double ap2, const QuadWeno& qw) {
+  const double up1 = SWFD_CM16 * am2 + SWFD_C56 * am1 + SWFD_C13 * a0;
+  const double up2 = SWFD_C13 * am1 + SWFD_C56 * a0 + SWFD_CM16 * ap1;
+  const double up3 = SWFD_C116 * a0 + SWFD_CM76 * ap1 + SWFD_C13 * ap2;
+  double b1, b2, b3;
+  weno_beta_qd(am2, am1, a0, ap1, ap2, qw, b1, b2, b3);
+  const double a1 = weno_alpha_qd(0.1, b1, qw), a2 = weno_alpha_qd(0.6, b2, qw),
+               a3 = weno_alpha_qd(0.3, b3, qw);
+  const double s = a1 + a2 + a3;
+  return a1 / s * up3 + a2 / s * up2 + a3 / s * up1;
+}
+
 // weno_right (weno5.f90:120-146)
 template <class T>
 __device__ __forceinline__ T weno_right(T am2, T am1, T a0, T ap1, T ap2, T eps) {
@@ -115,16 +168,35 @@ struct Eigen2D {
   T l4_0, l4_n, l4_t, l4_3;                  // evl row 4 (row 2 is [-vt, 0, 1, 0])
 };
 
-template <class T>
+// qreg (QD, ex4 and ex6 of the QUAD build only): the 1d-15 regularisers in
+// binary128 (ex4_sedov_2d/main.f90:199-210)
+template <class T, bool QD = false>
 __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T vxr, T vyl,
-                                            T vyr, T hl, T hr, Eigen2D<T>& E) {
-  T t0 = wl / (wl + wr + T(1.e-15));
+                                            T vyr, T hl, T hr, Eigen2D<T>& E,
+                                            const qd::q128* qreg = nullptr) {
+  T t0;
+  if constexpr (QD) {
+    if (qreg)
+      t0 = qd::to_double(qd::div(qd::from_double(wl), qd::add(qd::from_double(wl + wr), *qreg)));
+    else
+      t0 = wl / (wl + wr + T(1.e-15));
+  } else {
+    t0 = wl / (wl + wr + T(1.e-15));
+  }
   T t1 = T(1.) - t0;
   T vxm = t0 * vxl + t1 * vxr;
   T vym = t0 * vyl + t1 * vyr;
   T hm = t0 * hl + t1 * hr;
   T qm = T(0.5) * (vxm * vxm + vym * vym);
-  T cm = tsqrt(tabs(g1 * (hm - qm))) + T(1.e-15);
+  T cm;
+  if constexpr (QD) {
+    if (qreg)
+      cm = qd::to_double(qd::add(qd::from_double(tsqrt(tabs(g1 * (hm - qm)))), *qreg));
+    else
+      cm = tsqrt(tabs(g1 * (hm - qm))) + T(1.e-15);
+  } else {
+    cm = tsqrt(tabs(g1 * (hm - qm))) + T(1.e-15);
+  }
   T vn = ydir ? vym : vxm;
   T vt = ydir ? vxm : vym;
   t0 = vn * cm;

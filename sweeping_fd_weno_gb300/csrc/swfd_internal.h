@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/swfd.h"
+#include "swfd_quad.cuh"
 
 namespace swfd {
 
@@ -45,6 +46,15 @@ struct Params {
   double gamma = 1.4, gamma1 = 0.4, eps = 1e-13, eps2 = 1e-8, weno_eps = 1e-6;
   double dx = 0, dy = 0;
   float fdx_inv = 0.f, fdy_inv = 0.f;  // FP32-bulk flux differences: 1/dx, 1/dy
+  // literals = SWFD_LITERALS_QUAD (the reference's -fdefault-real-8 build):
+  // the subexpressions with a double-kind literal in binary128
+  int quad = 0;
+  qd::q128 q_c1312, q_weno_eps, q_1em15;  // 13d0/12d0, the WENO epsilon, 1d-15
+  // rho < 1d-8, rho > 1d-8, rho <= 1d-8 as binary64 comparisons with these
+  // bounds: the literal itself, or the binary64 neighbours of its binary128
+  // value (no binary64 lies between them)
+  double lim8_lt = 1e-8, lim8_gt = 1e-8, lim8_le = 1e-8;
+  double t_loop = 0;  // the time loop test time <= T - 1d-10, as time <= t_loop
   double dt_num_x = 0;   // dx*cfl   (or dx**(5/3)*cfl for dt_rule 3)
   double dt_num_y = 0;   // dy*cfl
   double time_terminal = 0;
@@ -310,7 +320,10 @@ cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc,
 cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* dst, cudaStream_t s);
-cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
+// quad: the reference build's binary128 smoothness indicators and alphas
+// (eps 1d-6 or 1d-12)
+cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, int quad, double* ul,
+                              double* ur,
                               cudaStream_t s);
 
 cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,

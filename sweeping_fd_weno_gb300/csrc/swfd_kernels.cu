@@ -347,6 +347,14 @@ __device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf(
 // with the ex4 regularisers, the y Roe planes), 3 = both.  With rank
 // segments (ex6) a cell near a rank boundary is split once per segment whose
 // local range holds it, with that segment's alpha.
+// 1/(den + 1d-15) of the y-pass preparation of ex4 and ex6
+// (ex4_sedov_2d/main.f90:426); in binary128 for the QUAD build
+__device__ __forceinline__ double reg_recip(const Params& p, double den) {
+  if (p.quad)
+    return qd::to_double(qd::div(qd::from_double(1.0), qd::add(qd::from_double(den), p.q_1em15)));
+  return 1. / (den + 1e-15);
+}
+
 template <class T>
 __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __restrict__ u,
                                             double amd, T* __restrict__ split, T* __restrict__ roe,
@@ -366,7 +374,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
       // reciprocal), the fluxes and the splitting in FP32; the Roe enthalpy
       // reuses the recovered pressure
       double vx = mx * ri, vy = my * ri;
-      const bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
+      const bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
       if (guard) vx = vy = 0.;
       const double pres = g1 * fma(-0.5 * rho, fma(vx, vx, vy * vy), e);
       const float fr = (float)rho, fm = (float)mx, fn = (float)my, fe = (float)e;
@@ -408,7 +416,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   }
   // fflux / gflux
   double vx = F32 ? mx * ri : mx / rho, vy = F32 ? my * ri : my / rho;
-  bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < 1e-8);
+  bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
   if (guard) {
     vx = 0.;
     vy = 0.;
@@ -474,7 +482,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
           n2 = w[2];
           e2 = w[3];
           double ux = m2 / r2, uy = n2 / r2;
-          if (p.flux_guard_eps2 ? (r2 < p.eps2) : (r2 < 1e-8)) {
+          if (p.flux_guard_eps2 ? (r2 < p.eps2) : (r2 < p.lim8_lt)) {
             ux = 0.;
             uy = 0.;
           }
@@ -504,7 +512,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   }
   if (p.roe_reg_ex4 && (which & 2)) {
     // ex4_sedov_2d/main.f90:426
-    double t0 = 1. / (rho + 1e-15);
+    double t0 = reg_recip(p, rho);
     double vex = mx * t0, vey = my * t0;
     double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
     roe[4 * P + o] = sqrt_abs<T>(rho);
@@ -532,8 +540,8 @@ __global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalar
   double rho = ld(u + o), mx = ld(u + P + o), e = ld(u + 2 * P + o);
   // fflux (ex2_sedov_1d/main.f90:57-73)
   double vx = 0.;
-  if (rho > 1e-8) vx = mx / rho;
-  if (rho <= 1e-8) vx = 0.;
+  if (rho > p.lim8_gt) vx = mx / rho;
+  if (rho <= p.lim8_le) vx = 0.;
   double pres = g1 * (e - 0.5 * rho * (vx * vx));
   double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
   double a[3] = {rho, mx, e};
@@ -587,10 +595,11 @@ cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void
 // column i).  sp/sn point at stencil cell -2, component 0 of the positive /
 // negative split flux; components are P apart, stencil cells `step` apart.
 // ---------------------------------------------------------------------------
-template <int YDIR, class T>
+template <int YDIR, class T, bool QD = false>
 __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __restrict__ sp,
                                                const T* __restrict__ sn, int64_t P, int64_t step,
-                                               T weps, T outp[4], T outn[4]) {
+                                               T weps, T outp[4], T outn[4],
+                                               const QuadWeno* qw = nullptr) {
   T ur[4], ul[4];
   if constexpr (sizeof(T) == 4) {
     // FP32: the 5 x 4 stencil values of each split flux are loaded once into
@@ -651,8 +660,13 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
         cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, b0, b1, b2, b3);
       }
     }
-    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
-    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+    if constexpr (QD) {
+      ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], *qw);
+      ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], *qw);
+    } else {
+      ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
+      ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+    }
   }
   // evr . ur (main.f90:226-229): row 1 [1,0,1,1]; normal-momentum row
   // [vn-c, 0, vn, vn+c]; tangential row [vt, 1, vt, vt]; energy row
@@ -670,7 +684,7 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
 
 // 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157); vxm and hm come
 // from the FP64 state (pressure recovery), the rest is in T
-template <class T>
+template <class T, bool QD = false>
 __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
                          T* __restrict__ flux) {
   // eight lanes per cell: lanes 0..5 of a group each reconstruct one
@@ -714,8 +728,15 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
     const int64_t s = o + jj - 2;
     cs[jj] = L[k][0] * ldt(sp + s) + L[k][1] * ldt(sp + P + s) + L[k][2] * ldt(sp + 2 * P + s);
   }
-  const T v = side ? weno_left(cs[0], cs[1], cs[2], cs[3], cs[4], weps)
-                   : weno_right(cs[0], cs[1], cs[2], cs[3], cs[4], weps);
+  T v;
+  if constexpr (QD) {
+    const QuadWeno qw{p.q_c1312, p.q_weno_eps};
+    v = side ? weno_left_qd(cs[0], cs[1], cs[2], cs[3], cs[4], qw)
+             : weno_right_qd(cs[0], cs[1], cs[2], cs[3], cs[4], qw);
+  } else {
+    v = side ? weno_left(cs[0], cs[1], cs[2], cs[3], cs[4], weps)
+             : weno_right(cs[0], cs[1], cs[2], cs[3], cs[4], weps);
+  }
   const int base = threadIdx.x & ~7 & 31;
   const T ur0 = __shfl_sync(0xffffffffu, v, base + 0), ul0 = __shfl_sync(0xffffffffu, v, base + 1);
   const T ur1 = __shfl_sync(0xffffffffu, v, base + 2), ul1 = __shfl_sync(0xffffffffu, v, base + 3);
@@ -801,7 +822,7 @@ __device__ __forceinline__ FluxConst<T> flux_const(const Params& p) {
   return FluxConst<T>{T(p.gamma1), T(p.weno_eps)};
 }
 
-template <class T, bool SEG, bool LIM = false>
+template <class T, bool SEG, bool LIM = false, bool QD = false>
 __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict__ split,
                                            const T* __restrict__ roe, T am, T* __restrict__ flux,
                                            int64_t c, int64_t chunks_x, int lane,
@@ -809,6 +830,13 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
   const Geom& g = p.g;
   const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
   const T g1 = cst.g1, weps = cst.weps;
+  QuadWeno qw;
+  const qd::q128* qreg = nullptr;
+  if constexpr (QD) {
+    qw.c1312 = p.q_c1312;
+    qw.eps = p.q_weno_eps;
+    if (p.roe_reg_ex4) qreg = &p.q_1em15;
+  }
   {
     T op[4], on[4];
     if (c < chunks_x) {
@@ -821,10 +849,11 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
       const int64_t o = g.at(i, j), os = SEG ? seg_x_off(p, i, j, sx) : o;
       if (SEG && p.seg_alpha) am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
       Eigen2D<T> E;
-      roe_eigen2d<T>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
+      roe_eigen2d<T, QD>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
                      ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
-                     ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
-      interface_flux<0>(E, split + os - 2, split + 4 * S + os - 2, S, 1, weps, op, on);
+                     ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E, qreg);
+      interface_flux<0, T, QD>(E, split + os - 2, split + 4 * S + os - 2, S, 1, weps, op, on,
+                               &qw);
       if (LIM) {
         int nd = 0, np = 0;
         zs_limit<T>(p, split + os, S, op, nd, np);
@@ -852,7 +881,9 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
         // the ex6 rank's ghost row j+1 (local nyl+2), pre-mirror, with the
         // y pass's preparation (ex4_sedov_2d/main.f90:426)
         const double* w = p.wall_save + ((int64_t)(j + 1) * 3 + (p.total - i)) * 4;
-        const double t0 = 1. / (w[0] + 1e-15);
+        double t0;
+        if constexpr (QD) t0 = reg_recip(p, w[0]);
+        else t0 = 1. / (w[0] + 1e-15);
         const double vex = w[1] * t0, vey = w[2] * t0;
         const double pre = p.gamma1 * (w[3] - 0.5 * (w[1] * vex + w[2] * vey));
         wr = sqrt_abs<T>(w[0]);
@@ -861,10 +892,10 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
         hr = T((pre + w[3]) * t0);
       }
       Eigen2D<T> E;
-      roe_eigen2d<T>(g1, 1, ldt(rr + o), wr, ldt(rr + P + o), vxr, ldt(rr + 2 * P + o), vyr,
-                     ldt(rr + 3 * P + o), hr, E);
-      interface_flux<1>(E, split + 8 * S + os - 2 * spit, split + 12 * S + os - 2 * spit, S, spit,
-                        weps, op, on);
+      roe_eigen2d<T, QD>(g1, 1, ldt(rr + o), wr, ldt(rr + P + o), vxr, ldt(rr + 2 * P + o), vyr,
+                     ldt(rr + 3 * P + o), hr, E, qreg);
+      interface_flux<1, T, QD>(E, split + 8 * S + os - 2 * spit, split + 12 * S + os - 2 * spit,
+                               S, spit, weps, op, on, &qw);
       if (LIM) {
         int nd = 0, np = 0;
         zs_limit<T>(p, split + 8 * S + os, S, op, nd, np);
@@ -880,7 +911,7 @@ __device__ __forceinline__ void flux_chunk(const Params& p, const T* __restrict_
   }
 }
 
-template <class T, bool SEG, bool LIM, int MINB = SWFD_FLUX_MINB(T)>
+template <class T, bool SEG, bool LIM, int MINB = SWFD_FLUX_MINB(T), bool QD = false>
 __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
     k_flux_xy(Params p, const T* __restrict__ split, const T* __restrict__ roe,
               const DevScalars* dsc, T* __restrict__ flux, int* __restrict__ work) {
@@ -894,7 +925,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
-    flux_chunk<T, SEG, LIM>(p, split, roe, am, flux, c, chunks_x, lane,
+    flux_chunk<T, SEG, LIM, QD>(p, split, roe, am, flux, c, chunks_x, lane,
                             (unsigned long long*)&dsc->den_count, cst);
   }
   // work[1] counts the warps that found the chunks exhausted: the last one
@@ -951,6 +982,20 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
   const T* rp = (const T*)roe;
   T* fp = (T*)flux;
   const int grid = flux_grid<T>();
+  if constexpr (sizeof(T) == 8) {
+    if (p.quad) {  // the binary128 subexpressions of the reference build
+      constexpr int M = SWFD_FLUX_MINB(T);
+      if (p.seg_alpha && p.limiter)
+        k_flux_xy<T, true, true, M, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+      else if (p.seg_alpha)
+        k_flux_xy<T, true, false, M, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+      else if (p.limiter)
+        k_flux_xy<T, false, true, M, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+      else
+        k_flux_xy<T, false, false, M, true><<<grid, SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work);
+      return;
+    }
+  }
   if (!p.seg_alpha && !p.limiter && p.flux_minb && p.flux_minb != SWFD_FLUX_MINB(T)) {
     if constexpr (sizeof(T) == 8) {
       if (p.flux_minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
@@ -979,6 +1024,9 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
     const int b = cell_block(lanes), gb = (int)((lanes + b - 1) / b);
     if (f32)
       k_flux1d<float><<<gb, b, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
+    else if (p.quad)
+      k_flux1d<double, true><<<gb, b, 0, s>>>(p, (const double*)roe, (const double*)split,
+                                               (double*)flux);
     else
       k_flux1d<double><<<gb, b, 0, s>>>(p, (const double*)roe, (const double*)split,
                                          (double*)flux);
@@ -1049,6 +1097,20 @@ __device__ __forceinline__ T rhs2d_cell(const Params& p, const T* __restrict__ f
 
 // u0 may alias out (stage 3 writes the step-start buffer); each element of
 // u0 is read only by the thread that then writes it.
+// u = 0.75d0*u0 + 0.25d0*v and u = (u0 + 2d0*v)/3d0
+// (ex3_vortex_accuracy_2d/main.f90:604,621); in binary128 for the QUAD build
+// (0.75*u0 and 0.25*v are exact there)
+__device__ __forceinline__ double rk_combine(const Params& p, int stage, double u0, double v) {
+  if (p.quad) {
+    using namespace qd;
+    if (stage == 2)
+      return to_double(add(mul(from_double(0.75), from_double(u0)), scale2(from_double(v), -2)));
+    return to_double(div(add(from_double(u0), scale2(from_double(v), 1)), from_double(3.0)));
+  }
+  if (stage == 2) return 0.75 * u0 + 0.25 * v;
+  return (u0 + 2.0 * v) / 3.0;
+}
+
 template <class T>
 __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double* __restrict__ u,
                                        const double* u0, const T* __restrict__ flux, double dt,
@@ -1073,8 +1135,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
         else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
       } else {
         v = ld(u + c * P + o) + dt * r;
-        if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
-        else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+        if (stage >= 2) v = rk_combine(p, stage, u0[c * P + o], v);
       }
       nv[c] = v;
       out[c * P + o] = v;
@@ -1153,8 +1214,7 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
       else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
     } else {
       v = ld(u + c * P + o) + dt * r;
-      if (stage == 2) v = 0.75 * u0[c * P + o] + 0.25 * v;
-      else if (stage == 3) v = (u0[c * P + o] + 2.0 * v) / 3.0;
+      if (stage >= 2) v = rk_combine(p, stage, u0[c * P + o], v);
     }
     out[c * P + o] = v;
   }
@@ -1295,19 +1355,27 @@ cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* ds
 // ---------------------------------------------------------------------------
 // batch of scalar WENO5 reconstructions (the MODULE weno5 entry points)
 // ---------------------------------------------------------------------------
-__global__ void k_weno_batch(const double* __restrict__ st, int64_t n, double eps,
-                             double* __restrict__ ul, double* __restrict__ ur) {
+__global__ void k_weno_batch(const double* __restrict__ st, int64_t n, double eps, int quad,
+                             QuadWeno qw, double* __restrict__ ul, double* __restrict__ ur) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const double* a = st + 5 * k;
+  if (quad) {
+    if (ul) ul[k] = weno_left_qd(a[0], a[1], a[2], a[3], a[4], qw);
+    if (ur) ur[k] = weno_right_qd(a[0], a[1], a[2], a[3], a[4], qw);
+    return;
+  }
   if (ul) ul[k] = weno_left<double>(a[0], a[1], a[2], a[3], a[4], eps);
   if (ur) ur[k] = weno_right<double>(a[0], a[1], a[2], a[3], a[4], eps);
 }
-cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, double* ul, double* ur,
-                              cudaStream_t s) {
+cudaError_t launch_weno_batch(const double* st, int64_t n, double eps, int quad, double* ul,
+                              double* ur, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_weno_batch<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(st, n, eps, ul,
-                                                                                  ur);
+  QuadWeno qw;
+  qw.c1312 = qd::div(qd::from_double(13.0), qd::from_double(12.0));
+  qw.eps = qd::div(qd::from_double(1.0), qd::from_double(eps == 1e-12 ? 1e12 : 1e6));
+  k_weno_batch<<<(unsigned)((n + SWFD_BLOCK - 1) / SWFD_BLOCK), SWFD_BLOCK, 0, s>>>(
+      st, n, eps, quad, qw, ul, ur);
   return cudaGetLastError();
 }
 

@@ -73,6 +73,8 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
   Params p;
   st = make_params(*cfg, p, err);
   if (st != SWFD_OK) return static_fail(st, err);
+  if (p.quad)
+    return static_fail(SWFD_ERR_UNSUPPORTED, "swfd_flux_divergence_static: binary64 literals only");
   if (p.problem == SWFD_PROBLEM_MATLAB_1D)
     return static_fail(SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   if (p.seg_alpha)

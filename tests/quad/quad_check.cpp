@@ -1,0 +1,96 @@
+// Checks the software binary128 arithmetic of swfd_quad.cuh against GCC's
+// _Float128 (IEEE binary128, round to nearest even) on random and edge-case
+// binary64 operands.  Prints the number of mismatches per operation.
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "swfd_quad.cuh"
+
+using namespace swfd::qd;
+typedef _Float128 F;
+
+static uint64_t st = 0x243f6a8885a308d3ull;
+static uint64_t rnd() {
+  st ^= st << 13;
+  st ^= st >> 7;
+  st ^= st << 17;
+  return st;
+}
+static double rdouble(int mode) {
+  double x;
+  if (mode == 0) {  // any finite bit pattern
+    uint64_t b;
+    do {
+      b = rnd();
+    } while (((b >> 52) & 0x7ff) == 0x7ff);
+    memcpy(&x, &b, 8);
+  } else {  // magnitudes near 1 with varied exponents
+    x = ((double)(rnd() >> 11) / 9007199254740992.0 + 0.5) * ldexp(1.0, (int)(rnd() % 81) - 40);
+    if (rnd() & 1) x = -x;
+  }
+  return x;
+}
+// the binary128 value of a q128 as _Float128
+static F toF(const q128& a) {
+  if (a.nf) return (F)a.d;
+  if ((a.hi | a.lo) == 0) return a.s ? -(F)0 : (F)0;
+  F m = (F)a.hi * (F)18446744073709551616.0 + (F)a.lo;  // exact: < 2^113
+  F r = ldexpf128(m, a.e - 112);
+  return a.s ? -r : r;
+}
+static bool same(F a, F b) {
+  if (a != a && b != b) return true;
+  return memcmp(&a, &b, sizeof(F)) == 0;
+}
+static bool same_d(double a, double b) {
+  if (a != a && b != b) return true;
+  return memcmp(&a, &b, 8) == 0;
+}
+
+int main(int argc, char** argv) {
+  const long n = argc > 1 ? atol(argv[1]) : 200000;
+  long bad[8] = {0};
+  const char* names[8] = {"from/to", "add", "sub", "mul", "div", "chain", "to_double", "neg0"};
+  for (long i = 0; i < n; ++i) {
+    const int mode = i & 1;
+    double x = rdouble(mode), y = rdouble(mode);
+    if (i % 97 == 0) y = -x;                 // exact cancellation
+    if (i % 89 == 0) y = x * (1 + 0x1p-52);  // near cancellation
+    if (i % 83 == 0) y = 0.0;
+    const q128 qx = from_double(x), qy = from_double(y);
+    if (!same_d(to_double(qx), x)) bad[0]++;
+    const F fx = (F)x, fy = (F)y;
+    if (!same(toF(add(qx, qy)), fx + fy)) bad[1]++;
+    if (!same(toF(sub(qx, qy)), fx - fy)) bad[2]++;
+    if (!same(toF(mul(qx, qy)), fx * fy)) bad[3]++;
+    if (y != 0 && !same(toF(div(qx, qy)), fx / fy)) bad[4]++;
+    // a chain like the WENO smoothness indicator, all in binary128, then rounded
+    const double z = rdouble(1);
+    const q128 c1312 = div(from_double(13), from_double(12));
+    const q128 s = add(sub(qx, mul(from_double(2), qy)), from_double(z));
+    const q128 r = add(mul(c1312, mul(s, s)), mul(from_double(0.25), mul(qy, qy)));
+    const F fs = fx - (F)2 * fy + (F)z;
+    const F fr = (F)13 / (F)12 * (fs * fs) + (F)0.25 * (fy * fy);
+    if (!same(toF(r), fr)) bad[5]++;
+    if (!same_d(to_double(r), (double)fr)) bad[6]++;
+  }
+  // to_double on values near the subnormal range and at rounding ties
+  for (long i = 0; i < n / 4; ++i) {
+    const double x = ldexp((double)(rnd() >> 11), -(int)(rnd() % 60) - 1040);
+    const double y = ldexp((double)(rnd() >> 11), -(int)(rnd() % 30) - 30);
+    const q128 q = mul(from_double(x), from_double(y));
+    const F f = (F)x * (F)y;
+    if (!same_d(to_double(q), (double)f)) bad[6]++;
+  }
+  if (!same_d(to_double(add(from_double(-0.0), from_double(-0.0))), -0.0)) bad[7]++;
+  if (!same_d(to_double(add(from_double(1.5), from_double(-1.5))), 0.0)) bad[7]++;
+  long total = 0;
+  for (int k = 0; k < 8; ++k) {
+    printf("%s %ld\n", names[k], bad[k]);
+    total += bad[k];
+  }
+  return total ? 1 : 0;
+}
