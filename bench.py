@@ -520,6 +520,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-quad", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=256)
@@ -716,6 +717,44 @@ def main():
                               "recovery, RK accumulation, positivity, CFL reduction and sweeps"}
         s32.close()
         s64.close()
+    # the reference build's own arithmetic (literals = QUAD: its binary128
+    # subexpressions in software on the GPU), same workload, timed the same way
+    quad = None
+    if args.precision == "fp64" and not args.no_quad:
+        sq_ = Solver(problems.workload(args.workload, device=local, literals=abi.LITERALS_QUAD))
+        sd_ = Solver(problems.workload(args.workload, device=local))
+        for s_ in (sq_, sd_):
+            s_.init_problem()
+        extq = torch.cuda.ExternalStream(sq_.stream_ptr(), device=torch.device("cuda", local))
+        sq_.step()                            # captures the step graph
+        sq_.init_problem()
+        nq = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        evq = []
+        for _ in range(nq):
+            with torch.cuda.stream(extq):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(extq)
+            sq_.step_async()
+            b.record(extq)
+            evq.append((a, b))
+        torch.cuda.synchronize()
+        sq_.finish()
+        msq = sum(a.elapsed_time(b) for a, b in evq)
+        for _ in range(nq):
+            sd_.step()
+        uq, ud = sq_.state(), sd_.state()
+        quad = {"value": aggregate(cells * 3 * nq, msq * 1e-3)[2], "ms_per_step": msq / nq,
+                "steps": nq, "slowdown_vs_fp64": (msq / nq) / (total_ms / args.steps),
+                "max_rel_diff_vs_double_literals": float(np.max(np.abs(uq - ud)) /
+                                                         np.max(np.abs(ud))),
+                "arithmetic": "the reference's -fdefault-real-8 build: its double-kind "
+                              "literals' subexpressions in binary128 (software, integer pipes), "
+                              "the rest FP64"}
+        sq_.close()
+        sd_.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -735,6 +774,7 @@ def main():
         "roofline": roofline,
         "sweep": {"invocations": prof["sweep_invocations"], "ms": prof["sweep_ms"]},
         "fp32_bulk": fp32,
+        "quad_literals": quad,
     }
     if not args.no_batched:
         line["batched"] = bench_batched(args, local, flush)
