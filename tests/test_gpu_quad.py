@@ -71,3 +71,22 @@ def test_quad_vortex45_full_run(swfd, oracle_mod):
     np.testing.assert_array_equal(g.state(), o.state())
     assert g.stats() == o.stats()
     g.close()
+
+
+def test_quad_solve_graph_and_eager_match(swfd, oracle_mod, monkeypatch):
+    """the solve graph (time loop on the device, binary128 time test) and the
+    eager launch mode of the binary128-literal form"""
+    kw = dict(problem=abi.SEDOV_2D, nx=40, ny=40, time_terminal=0.02)
+    g, o = pair(oracle_mod, kw)
+    n = g.run()
+    assert n == o.run() and n > 3
+    np.testing.assert_array_equal(g.state(), o.state())
+    assert g.stats() == o.stats()
+    g.close()
+    monkeypatch.setenv("SWFD_LAUNCH", "eager")
+    e, o2 = pair(oracle_mod, kw)
+    for _ in range(4):
+        e.step()
+        o2.step()
+    np.testing.assert_array_equal(e.state(), o2.state())
+    e.close()
