@@ -24,7 +24,7 @@
 
 #ifdef __CUDACC__
 #define SWFD_QD __host__ __device__ __forceinline__
-// the division (a 116-step loop) is kept out of line: one copy per kernel
+// the division (a loop of nine quotient digits) is kept out of line
 #define SWFD_QD_CALL static __host__ __device__ __noinline__
 #else
 #define SWFD_QD static inline
@@ -303,27 +303,50 @@ SWFD_QD q128 mul(const q128& a, const q128& b) {
   return round_pack(a.s ^ b.s, e, hi, lo, st);
 }
 
+SWFD_QD double u128_to_double(uint64_t hi, uint64_t lo) {
+  return (double)hi * 18446744073709551616.0 + (double)lo;
+}
+
+// Division: the quotient of the significands in digits of 13 bits.  Each
+// digit is estimated from the binary64 quotient of the partial remainder by
+// the divisor (relative error near 2^-52, so the estimate is the digit or
+// one off), corrected against the exact 128-bit remainder, which then stays
+// below the divisor; 1 + 9*13 = 118 quotient bits and the remainder's
+// sticky bit give the correctly rounded binary128 quotient.
 SWFD_QD_CALL q128 div(const q128& a, const q128& b) {
   if (a.nf || b.nf || is_zero(b)) return make_nf(to_double(a) / to_double(b));
   if (is_zero(a)) return make_zero(a.s ^ b.s);
-  // long division of the significands: 116 quotient bits and the remainder
   uint64_t rh = a.hi, rl = a.lo;
   int32_t e = a.e - b.e;
-  if (!ge128(rh, rl, b.hi, b.lo)) {  // ma < mb: one more quotient bit
+  if (!ge128(rh, rl, b.hi, b.lo)) {  // ma < mb: scale so that mb <= ma < 2 mb
     shl128(rh, rl, 1);
     e -= 1;
   }
-  uint64_t qh = 0, ql = 0;
+  sub128(rh, rl, b.hi, b.lo);  // the leading quotient bit is 1
+  uint64_t qh = 0, ql = 1;
+  const double rb = 1.0 / u128_to_double(b.hi, b.lo);
 #pragma unroll 1
-  for (int i = 0; i < 116; ++i) {
-    shl128(qh, ql, 1);
-    if (ge128(rh, rl, b.hi, b.lo)) {
-      sub128(rh, rl, b.hi, b.lo);
-      ql |= 1;
+  for (int k = 0; k < 9; ++k) {
+    shl128(rh, rl, 13);  // remainder * 2^13 < mb * 2^13 < 2^126
+    double est = u128_to_double(rh, rl) * rb;
+    uint64_t dg = est < 0 ? 0 : (est > 8191.0 ? 8191 : (uint64_t)est);
+    uint64_t ph, pl;  // dg * mb (< 2^126)
+    mul64(b.lo, dg, ph, pl);
+    ph += b.hi * dg;
+    for (int t = 0; t < 3 && !ge128(rh, rl, ph, pl); ++t) {  // estimate too large
+      sub128(ph, pl, b.hi, b.lo);
+      --dg;
     }
-    shl128(rh, rl, 1);
+    sub128(rh, rl, ph, pl);
+    for (int t = 0; t < 3 && ge128(rh, rl, b.hi, b.lo); ++t) {  // too small
+      sub128(rh, rl, b.hi, b.lo);
+      ++dg;
+    }
+    shl128(qh, ql, 13);
+    ql |= dg;
   }
-  return round_pack(a.s ^ b.s, e, qh, ql, (rh | rl) != 0);
+  // the quotient's leading bit is bit 117; round_pack's e refers to bit 115
+  return round_pack(a.s ^ b.s, e - 2, qh, ql, (rh | rl) != 0);
 }
 
 // comparisons of finite values

@@ -52,8 +52,8 @@ static bool same_d(double a, double b) {
 
 int main(int argc, char** argv) {
   const long n = argc > 1 ? atol(argv[1]) : 200000;
-  long bad[8] = {0};
-  const char* names[8] = {"from/to", "add", "sub", "mul", "div", "chain", "to_double", "neg0"};
+  long bad[9] = {0};
+  const char* names[9] = {"from/to", "add", "sub", "mul", "div", "chain", "to_double", "neg0", "div113"};
   for (long i = 0; i < n; ++i) {
     const int mode = i & 1;
     double x = rdouble(mode), y = rdouble(mode);
@@ -76,6 +76,11 @@ int main(int argc, char** argv) {
     const F fr = (F)13 / (F)12 * (fs * fs) + (F)0.25 * (fy * fy);
     if (!same(toF(r), fr)) bad[5]++;
     if (!same_d(to_double(r), (double)fr)) bad[6]++;
+    // division of operands with full 113-bit significands
+    const double w = rdouble(mode);
+    const q128 qn = add(mul(qx, from_double(z)), from_double(w)), qd = mul(qy, add(from_double(z), qx));
+    const F fn = fx * (F)z + (F)w, fd = fy * ((F)z + fx);
+    if (fd != 0 && !same(toF(div(qn, qd)), fn / fd)) bad[8]++;
   }
   // to_double on values near the subnormal range and at rounding ties
   for (long i = 0; i < n / 4; ++i) {
@@ -88,7 +93,7 @@ int main(int argc, char** argv) {
   if (!same_d(to_double(add(from_double(-0.0), from_double(-0.0))), -0.0)) bad[7]++;
   if (!same_d(to_double(add(from_double(1.5), from_double(-1.5))), 0.0)) bad[7]++;
   long total = 0;
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < 9; ++k) {
     printf("%s %ld\n", names[k], bad[k]);
     total += bad[k];
   }
