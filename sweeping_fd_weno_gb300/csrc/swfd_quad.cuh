@@ -24,7 +24,7 @@
 
 #ifdef __CUDACC__
 #define SWFD_QD __host__ __device__ __forceinline__
-// the division (a loop of nine quotient digits) is kept out of line
+// the division (a loop of eight quotient digits) is kept out of line
 #define SWFD_QD_CALL static __host__ __device__ __noinline__
 #else
 #define SWFD_QD static inline
@@ -303,16 +303,14 @@ SWFD_QD q128 mul(const q128& a, const q128& b) {
   return round_pack(a.s ^ b.s, e, hi, lo, st);
 }
 
-SWFD_QD double u128_to_double(uint64_t hi, uint64_t lo) {
-  return (double)hi * 18446744073709551616.0 + (double)lo;
-}
-
-// Division: the quotient of the significands in digits of 13 bits.  Each
-// digit is estimated from the binary64 quotient of the partial remainder by
-// the divisor (relative error near 2^-52, so the estimate is the digit or
-// one off), corrected against the exact 128-bit remainder, which then stays
-// below the divisor; 1 + 9*13 = 118 quotient bits and the remainder's
-// sticky bit give the correctly rounded binary128 quotient.
+// Division: the quotient of the significands in digits of 15 bits.  Each
+// digit is estimated in binary32 from the top 32 bits of the partial
+// remainder and a reciprocal of the divisor's top 32 bits (absolute error
+// below 0.01, so the estimate is the digit or one off), then corrected
+// against the exact 128-bit remainder, which stays below the divisor.  The
+// leading quotient bit and 8 digits give 121 bits; with the remainder's
+// sticky bit that rounds correctly to binary128.  No binary64 arithmetic:
+// the FP64 pipe is the scarce one.
 SWFD_QD_CALL q128 div(const q128& a, const q128& b) {
   if (a.nf || b.nf || is_zero(b)) return make_nf(to_double(a) / to_double(b));
   if (is_zero(a)) return make_zero(a.s ^ b.s);
@@ -324,15 +322,20 @@ SWFD_QD_CALL q128 div(const q128& a, const q128& b) {
   }
   sub128(rh, rl, b.hi, b.lo);  // the leading quotient bit is 1
   uint64_t qh = 0, ql = 1;
-  const double rb = 1.0 / u128_to_double(b.hi, b.lo);
+  // mb in [2^112, 2^113): mb ~ mt * 2^81, so 2^96 / mb ~ 2^15 / mt
+  const uint32_t mt = (uint32_t)(b.hi >> 17);
+  const float rcp = 32768.0f / (float)mt;
+  const uint32_t b0 = (uint32_t)b.lo, b1 = (uint32_t)(b.lo >> 32);
 #pragma unroll 1
-  for (int k = 0; k < 9; ++k) {
-    shl128(rh, rl, 13);  // remainder * 2^13 < mb * 2^13 < 2^126
-    double est = u128_to_double(rh, rl) * rb;
-    uint64_t dg = est < 0 ? 0 : (est > 8191.0 ? 8191 : (uint64_t)est);
-    uint64_t ph, pl;  // dg * mb (< 2^126)
-    mul64(b.lo, dg, ph, pl);
-    ph += b.hi * dg;
+  for (int k = 0; k < 8; ++k) {
+    shl128(rh, rl, 15);  // remainder * 2^15 < mb * 2^15 < 2^128
+    const float est = (float)(uint32_t)(rh >> 32) * rcp;
+    const uint32_t d32 = est >= 32767.0f ? 32767u : (uint32_t)est;
+    uint64_t dg = d32;
+    // dg * mb (< 2^128) from 32-bit limbs of mb's low word
+    const uint64_t l0 = (uint64_t)b0 * d32, l1 = (uint64_t)b1 * d32;
+    uint64_t pl = l0 + (l1 << 32);
+    uint64_t ph = (l1 >> 32) + (pl < l0 ? 1 : 0) + b.hi * dg;
     for (int t = 0; t < 3 && !ge128(rh, rl, ph, pl); ++t) {  // estimate too large
       sub128(ph, pl, b.hi, b.lo);
       --dg;
@@ -342,11 +345,11 @@ SWFD_QD_CALL q128 div(const q128& a, const q128& b) {
       sub128(rh, rl, b.hi, b.lo);
       ++dg;
     }
-    shl128(qh, ql, 13);
+    shl128(qh, ql, 15);
     ql |= dg;
   }
-  // the quotient's leading bit is bit 117; round_pack's e refers to bit 115
-  return round_pack(a.s ^ b.s, e - 2, qh, ql, (rh | rl) != 0);
+  // the quotient's leading bit is bit 120; round_pack's e refers to bit 115
+  return round_pack(a.s ^ b.s, e - 5, qh, ql, (rh | rl) != 0);
 }
 
 // comparisons of finite values

@@ -81,6 +81,12 @@ int main(int argc, char** argv) {
     const q128 qn = add(mul(qx, from_double(z)), from_double(w)), qd = mul(qy, add(from_double(z), qx));
     const F fn = fx * (F)z + (F)w, fd = fy * ((F)z + fx);
     if (fd != 0 && !same(toF(div(qn, qd)), fn / fd)) bad[8]++;
+    // divisors and dividends whose significands are long runs of ones
+    const double h = ldexp(1.0, -(int)(rnd() % 60) - 53), g = ldexp(1.0, -(int)(rnd() % 60) - 53);
+    const q128 q1 = sub(from_double(1.0), from_double(h)), q2 = sub(from_double(x), from_double(x * g));
+    const F f1 = (F)1 - (F)h, f2 = (F)x - (F)(x * g);
+    if (x != 0 && !same(toF(div(q2, q1)), f2 / f1)) bad[8]++;
+    if (x != 0 && !same(toF(div(q1, q2)), f1 / f2)) bad[8]++;
   }
   // to_double on values near the subnormal range and at rounding ties
   for (long i = 0; i < n / 4; ++i) {
