@@ -16,6 +16,7 @@
 #pragma once
 
 #include "swfd_internal.h"
+#include "swfd_sdiv.cuh"
 
 namespace swfd {
 
@@ -34,6 +35,12 @@ __device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double tabs(double a) { return fabs(a); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double dsq(double a) { return a * a; }
+// a / b.  Binary64: sd::div, the correctly rounded quotient (the bits of the
+// hardware division) from integer and FP32 arithmetic, which leaves the FP64
+// pipe -- the bound of the flux kernels -- to the additions and products.
+// Binary32: the hardware division.
+__device__ __forceinline__ double tdiv(double a, double b) { return sd::div(a, b); }
+__device__ __forceinline__ float tdiv(float a, float b) { return a / b; }
 
 // 1/x for the FP32-bulk form, whose results are not bit-exact by design:
 // the FP32 reciprocal as the seed and two Newton-Raphson steps
@@ -98,7 +105,7 @@ static __device__ __noinline__ double weno_right_qd(double am2, double am1, doub
   const double a1 = weno_alpha_qd(0.3, b1, qw), a2 = weno_alpha_qd(0.6, b2, qw),
                a3 = weno_alpha_qd(0.1, b3, qw);
   const double s = a1 + a2 + a3;
-  return a1 / s * um3 + a2 / s * um2 + a3 / s * um1;
+  return sd::div(a1, s) * um3 + sd::div(a2, s) * um2 + sd::div(a3, s) * um1;
 }
 static __device__ __noinline__ double weno_left_qd(double am2, double am1, double a0, double ap1,
                                                double ap2, const QuadWeno& qw) {
@@ -110,7 +117,7 @@ static __device__ __noinline__ double weno_left_qd(double am2, double am1, doubl
   const double a1 = weno_alpha_qd(0.1, b1, qw), a2 = weno_alpha_qd(0.6, b2, qw),
                a3 = weno_alpha_qd(0.3, b3, qw);
   const double s = a1 + a2 + a3;
-  return a1 / s * up3 + a2 / s * up2 + a3 / s * up1;
+  return sd::div(a1, s) * up3 + sd::div(a2, s) * up2 + sd::div(a3, s) * up1;
 }
 
 // weno_right (weno5.f90:120-146)
@@ -121,16 +128,16 @@ __device__ __forceinline__ T weno_right(T am2, T am1, T a0, T ap1, T ap2, T eps)
   T um3 = T(SWFD_C13) * a0 + T(SWFD_C56) * ap1 + T(SWFD_CM16) * ap2;
   T b1, b2, b3;
   weno_beta(am2, am1, a0, ap1, ap2, b1, b2, b3);
-  T a1 = T(0.3) / tsq(eps + b1);
-  T a2 = T(0.6) / tsq(eps + b2);
-  T a3 = T(0.1) / tsq(eps + b3);
+  T a1 = tdiv(T(0.3), tsq(eps + b1));
+  T a2 = tdiv(T(0.6), tsq(eps + b2));
+  T a3 = tdiv(T(0.1), tsq(eps + b3));
   T s = a1 + a2 + a3;
   T w1, w2, w3;
   if constexpr (sizeof(T) == 4) {  // FP32-bulk: one reciprocal for the three weights
     const T rs = T(1.) / s;
     w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
   } else {  // the reference's three divisions (weno5.f90:134-140)
-    w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+    w1 = tdiv(a1, s), w2 = tdiv(a2, s), w3 = tdiv(a3, s);
   }
   return w1 * um3 + w2 * um2 + w3 * um1;
 }
@@ -143,16 +150,16 @@ __device__ __forceinline__ T weno_left(T am2, T am1, T a0, T ap1, T ap2, T eps) 
   T up3 = T(SWFD_C116) * a0 + T(SWFD_CM76) * ap1 + T(SWFD_C13) * ap2;
   T b1, b2, b3;
   weno_beta(am2, am1, a0, ap1, ap2, b1, b2, b3);
-  T a1 = T(0.1) / tsq(eps + b1);
-  T a2 = T(0.6) / tsq(eps + b2);
-  T a3 = T(0.3) / tsq(eps + b3);
+  T a1 = tdiv(T(0.1), tsq(eps + b1));
+  T a2 = tdiv(T(0.6), tsq(eps + b2));
+  T a3 = tdiv(T(0.3), tsq(eps + b3));
   T s = a1 + a2 + a3;
   T w1, w2, w3;
   if constexpr (sizeof(T) == 4) {
     const T rs = T(1.) / s;
     w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
   } else {  // weno5.f90:104-110
-    w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+    w1 = tdiv(a1, s), w2 = tdiv(a2, s), w3 = tdiv(a3, s);
   }
   return w1 * up3 + w2 * up2 + w3 * up1;
 }
@@ -179,9 +186,9 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
     if (qreg)
       t0 = qd::to_double(qd::div(qd::from_double(wl), qd::add(qd::from_double(wl + wr), *qreg)));
     else
-      t0 = wl / (wl + wr + T(1.e-15));
+      t0 = tdiv(wl, wl + wr + T(1.e-15));
   } else {
-    t0 = wl / (wl + wr + T(1.e-15));
+    t0 = tdiv(wl, wl + wr + T(1.e-15));
   }
   T t1 = T(1.) - t0;
   T vxm = t0 * vxl + t1 * vxr;
@@ -208,7 +215,7 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   E.e_np = vn + cm;
   E.e_hm = hm - t0;
   E.e_hp = hm + t0;
-  T rcm = T(1.) / cm;
+  T rcm = tdiv(T(1.), cm);
   T b1 = g1 * rcm * rcm;
   T b2 = qm * b1;
   t0 = vn * rcm;

@@ -352,7 +352,7 @@ __device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf(
 __device__ __forceinline__ double reg_recip(const Params& p, double den) {
   if (p.quad)
     return qd::to_double(qd::div(qd::from_double(1.0), qd::add(qd::from_double(den), p.q_1em15)));
-  return 1. / (den + 1e-15);
+  return sd::div(1., den + 1e-15);
 }
 
 template <class T>
@@ -415,7 +415,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
     }
   }
   // fflux / gflux
-  double vx = F32 ? mx * ri : mx / rho, vy = F32 ? my * ri : my / rho;
+  double vx = F32 ? mx * ri : tdiv(mx, rho), vy = F32 ? my * ri : tdiv(my, rho);
   bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
   if (guard) {
     vx = 0.;
@@ -444,15 +444,15 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   } else if (!p.seg_alpha) {
     const T am = T(amd);
     T q;
-    q = T(mx) / am;  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
-    q = T(f1) / am;  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
-    T qxy = T(fxy) / am;
+    q = tdiv(T(mx), am);  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
+    q = tdiv(T(f1), am);  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
+    T qxy = tdiv(T(fxy), am);
     split[2 * S + o] = h * (tmy + qxy); split[6 * S + o] = h * (tmy - qxy);
-    q = T(f3) / am;  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
-    q = T(my) / am;  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
+    q = tdiv(T(f3), am);  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
+    q = tdiv(T(my), am);  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
     split[9 * S + o] = h * (tmx + qxy); split[13 * S + o] = h * (tmx - qxy);
-    q = T(g2) / am;  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
-    q = T(g3) / am;  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
+    q = tdiv(T(g2), am);  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
+    q = tdiv(T(g3), am);  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
   } else {
     if (which & 1) {
       // x segments whose local columns s*nxl-2 .. s*nxl+nxl+3 hold column i
@@ -462,10 +462,10 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
         const T am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
         const int64_t os = seg_x_off(p, i, j, sx);
         T q;
-        q = T(mx) / am;  split[0 * S + os] = h * (tr + q);  split[4 * S + os] = h * (tr - q);
-        q = T(f1) / am;  split[1 * S + os] = h * (tmx + q); split[5 * S + os] = h * (tmx - q);
-        q = T(fxy) / am; split[2 * S + os] = h * (tmy + q); split[6 * S + os] = h * (tmy - q);
-        q = T(f3) / am;  split[3 * S + os] = h * (te + q);  split[7 * S + os] = h * (te - q);
+        q = tdiv(T(mx), am);  split[0 * S + os] = h * (tr + q);  split[4 * S + os] = h * (tr - q);
+        q = tdiv(T(f1), am);  split[1 * S + os] = h * (tmx + q); split[5 * S + os] = h * (tmx - q);
+        q = tdiv(T(fxy), am); split[2 * S + os] = h * (tmy + q); split[6 * S + os] = h * (tmy - q);
+        q = tdiv(T(f3), am);  split[3 * S + os] = h * (te + q);  split[7 * S + os] = h * (te - q);
       }
     }
     if (which & 2) {
@@ -481,7 +481,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
           m2 = w[1];
           n2 = w[2];
           e2 = w[3];
-          double ux = m2 / r2, uy = n2 / r2;
+          double ux = tdiv(m2, r2), uy = tdiv(n2, r2);
           if (p.flux_guard_eps2 ? (r2 < p.eps2) : (r2 < p.lim8_lt)) {
             ux = 0.;
             uy = 0.;
@@ -493,16 +493,16 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
         }
         const T tr2 = T(r2), tm2 = T(m2), tn2 = T(n2), te2 = T(e2);
         T q;
-        q = T(n2) / am;   split[8 * S + os] = h * (tr2 + q);  split[12 * S + os] = h * (tr2 - q);
-        q = T(fxy2) / am; split[9 * S + os] = h * (tm2 + q);  split[13 * S + os] = h * (tm2 - q);
-        q = T(g22) / am;  split[10 * S + os] = h * (tn2 + q); split[14 * S + os] = h * (tn2 - q);
-        q = T(g32) / am;  split[11 * S + os] = h * (te2 + q); split[15 * S + os] = h * (te2 - q);
+        q = tdiv(T(n2), am);   split[8 * S + os] = h * (tr2 + q);  split[12 * S + os] = h * (tr2 - q);
+        q = tdiv(T(fxy2), am); split[9 * S + os] = h * (tm2 + q);  split[13 * S + os] = h * (tm2 - q);
+        q = tdiv(T(g22), am);  split[10 * S + os] = h * (tn2 + q); split[14 * S + os] = h * (tn2 - q);
+        q = tdiv(T(g32), am);  split[11 * S + os] = h * (te2 + q); split[15 * S + os] = h * (te2 - q);
       }
     }
   }
   // Roe preparation (x pass; the y pass is the same except in ex4 and ex6)
   if (which & 1) {
-    double t0 = F32 ? ri : 1. / rho;
+    double t0 = F32 ? ri : tdiv(1., rho);
     double vex = mx * t0, vey = my * t0;
     double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
     roe[0 * P + o] = sqrt_abs<T>(rho);

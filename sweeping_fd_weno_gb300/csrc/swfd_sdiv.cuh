@@ -1,0 +1,105 @@
+// swfd_sdiv.cuh -- IEEE binary64 division on the integer and FP32 pipes
+// (host and device).
+//
+// A GB300 SM retires two FP64 operations per clock against 128 integer or
+// FP32 ones, and an IEEE binary64 division costs a sequence of FP64
+// operations.  sd::div returns the correctly rounded quotient (round to
+// nearest, ties to even) -- the same bits as the hardware division -- from
+// integer arithmetic on the significands: the leading quotient bit and five
+// digits of 11 bits, each estimated in binary32 and corrected exactly, then
+// rounded with the remainder as sticky bit.  Operands that are zero,
+// subnormal, infinite or NaN, and quotients whose exponent is within a
+// binade of the binary64 limits, take the hardware division, so the result
+// equals a / b for every input.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+
+#ifdef __CUDACC__
+#define SWFD_SD __host__ __device__ __forceinline__
+#else
+#define SWFD_SD static inline
+#endif
+
+namespace swfd {
+namespace sd {
+
+SWFD_SD uint64_t dbits(double x) {
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return u;
+}
+SWFD_SD double dfrom(uint64_t u) {
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+}
+SWFD_SD uint32_t fbits(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  return u;
+}
+SWFD_SD float ffrom(uint32_t u) {
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+}
+// correctly rounded binary32 reciprocal (only an estimate is needed)
+SWFD_SD float rcp32(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+
+SWFD_SD double div(double a, double b) {
+  const uint64_t ua = dbits(a), ub = dbits(b);
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+  // biased exponent of the quotient when ma >= mb; the result's is e or e - 1
+  // before rounding and at most one more after it
+  int32_t e = (int32_t)ea - (int32_t)eb + 1023;
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 2 || e > 2045) return a / b;
+  const uint64_t frac = 0xfffffffffffffull;
+  const uint64_t B = (ub & frac) | (1ull << 52);
+  uint64_t A = (ua & frac) | (1ull << 52);
+  if (A < B) {  // scale so that B <= A < 2B
+    A <<= 1;
+    e -= 1;
+  }
+  A -= B;  // the leading quotient bit is 1
+  uint64_t q = 1;
+  // 2^41 / B from B's top 32 bits (relative error near 2^-23)
+  const float rcp = 1048576.0f * rcp32((float)(uint32_t)(B >> 21));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    A <<= 11;  // A < B * 2^11 < 2^64
+    // A >> 41 (< 2^23) as a float without a conversion instruction
+    const float n = ffrom(0x4b000000u | (uint32_t)(A >> 41)) - 8388608.0f;
+    // the nearest integer to the estimate of A / B (absolute error below
+    // 0.001: truncation of A 2^-11, of B and the float roundings 2^11 * 2^-22),
+    // so it is the digit d = floor(A / B) or d + 1
+    const uint32_t dg = fbits(n * rcp + 8388608.0f) & 0x7fffffu;
+    uint64_t P = B * dg;  // <= B * 2^11 < 2^64
+    uint64_t d = dg;
+    if (P > A) {
+      P -= B;
+      d -= 1;
+    }
+    A -= P;  // now A < B
+    q = (q << 11) | d;
+  }
+  // q holds 56 bits; round to 53 with A != 0 as sticky
+  const uint32_t low = (uint32_t)q & 7u;
+  q >>= 3;
+  if (low > 4u || (low == 4u && (A != 0 || (q & 1)))) q += 1;
+  if (q >> 53) {  // rounded up to 2^53
+    q >>= 1;
+    e += 1;
+  }
+  return dfrom(((ua ^ ub) & 0x8000000000000000ull) | ((uint64_t)e << 52) | (q & frac));
+}
+
+}  // namespace sd
+}  // namespace swfd
