@@ -41,6 +41,15 @@ __device__ __forceinline__ double dsq(double a) { return a * a; }
 // Binary32: the hardware division.
 __device__ __forceinline__ double tdiv(double a, double b) { return sd::div(a, b); }
 __device__ __forceinline__ float tdiv(float a, float b) { return a / b; }
+// x * 2^K.  Binary64: sd::scale, an addition to the exponent field (the bits
+// of the hardware product).  Binary32: the product.
+template <int K>
+__device__ __forceinline__ double tscale(double x) { return sd::scale<K>(x); }
+template <int K>
+__device__ __forceinline__ float tscale(float x) {
+  constexpr float f = K >= 0 ? float(1u << (K >= 0 ? K : 0)) : 1.0f / float(1u << (K < 0 ? -K : 0));
+  return x * f;
+}
 
 // 1/x for the FP32-bulk form, whose results are not bit-exact by design:
 // the FP32 reciprocal as the seed and two Newton-Raphson steps
@@ -62,9 +71,13 @@ __device__ __forceinline__ double rcp_bulk(double x) {
 template <class T>
 __device__ __forceinline__ void weno_beta(T am2, T am1, T a0, T ap1, T ap2, T& b1, T& b2, T& b3) {
   const T c1312 = T(13.0 / 12.0);
-  b1 = c1312 * tsq(a0 - T(2.0) * ap1 + ap2) + T(0.25) * tsq(T(3.0) * a0 - T(4.0) * ap1 + ap2);
-  b2 = c1312 * tsq(am1 - T(2.0) * a0 + ap1) + T(0.25) * tsq(am1 - ap1);
-  b3 = c1312 * tsq(am2 - T(2.0) * am1 + a0) + T(0.25) * tsq(am2 - T(4.0) * am1 + T(3.0) * a0);
+  // 2d0*, 4d0* and 0.25d0* as exponent shifts (tscale): the same values
+  T s1 = a0 - tscale<1>(ap1) + ap2, t1 = T(3.0) * a0 - tscale<2>(ap1) + ap2;
+  T s2 = am1 - tscale<1>(a0) + ap1, t2 = am1 - ap1;
+  T s3 = am2 - tscale<1>(am1) + a0, t3 = am2 - tscale<2>(am1) + T(3.0) * a0;
+  b1 = c1312 * tsq(s1) + tscale<-2>(tsq(t1));
+  b2 = c1312 * tsq(s2) + tscale<-2>(tsq(t2));
+  b3 = c1312 * tsq(s3) + tscale<-2>(tsq(t3));
 }
 
 // literals = QUAD (the reference build): the smoothness indicators and the
@@ -194,7 +207,7 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   T vxm = t0 * vxl + t1 * vxr;
   T vym = t0 * vyl + t1 * vyr;
   T hm = t0 * hl + t1 * hr;
-  T qm = T(0.5) * (vxm * vxm + vym * vym);
+  T qm = tscale<-1>(vxm * vxm + vym * vym);
   T cm;
   if constexpr (QD) {
     if (qreg)
@@ -220,19 +233,19 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   T b2 = qm * b1;
   t0 = vn * rcm;
   t1 = b1 * vn;
-  T t2 = T(0.5) * b1;
+  T t2 = tscale<-1>(b1);
   T t3 = b1 * vt;
-  E.l1_0 = T(0.5) * (b2 + t0);
-  E.l1_n = -T(0.5) * (t1 + rcm);
-  E.l1_t = -T(0.5) * t3;
+  E.l1_0 = tscale<-1>(b2 + t0);
+  E.l1_n = -tscale<-1>(t1 + rcm);  // (-0.5)*x == -(0.5*x)
+  E.l1_t = -tscale<-1>(t3);
   E.l1_3 = t2;
   E.l3_0 = T(1.) - b2;
   E.l3_n = t1;
   E.l3_t = t3;
   E.l3_3 = -b1;
-  E.l4_0 = T(0.5) * (b2 - t0);
-  E.l4_n = -T(0.5) * (t1 - rcm);
-  E.l4_t = -T(0.5) * t3;
+  E.l4_0 = tscale<-1>(b2 - t0);
+  E.l4_n = -tscale<-1>(t1 - rcm);
+  E.l4_t = E.l1_t;
   E.l4_3 = t2;
 }
 

@@ -421,38 +421,38 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
     vx = 0.;
     vy = 0.;
   }
-  double pres = g1 * (e - 0.5 * rho * (vx * vx) - 0.5 * rho * (vy * vy));
+  const double hrho = tscale<-1>(rho);  // 0.5*rho
+  double pres = g1 * (e - hrho * (vx * vx) - hrho * (vy * vy));
   double fxy = rho * vx * vy;
   double f1 = rho * (vx * vx) + pres, f3 = (e + pres) * vx;
   double g2 = rho * (vy * vy) + pres, g3 = (e + pres) * vy;
   // fp = 0.5*(u + f/alpha), fn = 0.5*(u - f/alpha); f/alpha shared by both
-  const T h = T(0.5);
   const T tr = T(rho), tmx = T(mx), tmy = T(my), te = T(e);
   const int64_t S = p.sg.plane;
   if (!p.seg_alpha && F32) {
     const T ram = T(1.) / T(amd);
     T q;
-    q = T(mx) * ram;  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
-    q = T(f1) * ram;  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
+    q = T(mx) * ram;  split[0 * S + o] = tscale<-1>(tr + q);   split[4 * S + o] = tscale<-1>(tr - q);
+    q = T(f1) * ram;  split[1 * S + o] = tscale<-1>(tmx + q);  split[5 * S + o] = tscale<-1>(tmx - q);
     T qxy = T(fxy) * ram;
-    split[2 * S + o] = h * (tmy + qxy); split[6 * S + o] = h * (tmy - qxy);
-    q = T(f3) * ram;  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
-    q = T(my) * ram;  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
-    split[9 * S + o] = h * (tmx + qxy); split[13 * S + o] = h * (tmx - qxy);
-    q = T(g2) * ram;  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
-    q = T(g3) * ram;  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
+    split[2 * S + o] = tscale<-1>(tmy + qxy); split[6 * S + o] = tscale<-1>(tmy - qxy);
+    q = T(f3) * ram;  split[3 * S + o] = tscale<-1>(te + q);   split[7 * S + o] = tscale<-1>(te - q);
+    q = T(my) * ram;  split[8 * S + o] = tscale<-1>(tr + q);   split[12 * S + o] = tscale<-1>(tr - q);
+    split[9 * S + o] = tscale<-1>(tmx + qxy); split[13 * S + o] = tscale<-1>(tmx - qxy);
+    q = T(g2) * ram;  split[10 * S + o] = tscale<-1>(tmy + q); split[14 * S + o] = tscale<-1>(tmy - q);
+    q = T(g3) * ram;  split[11 * S + o] = tscale<-1>(te + q);  split[15 * S + o] = tscale<-1>(te - q);
   } else if (!p.seg_alpha) {
     const T am = T(amd);
     T q;
-    q = tdiv(T(mx), am);  split[0 * S + o] = h * (tr + q);   split[4 * S + o] = h * (tr - q);
-    q = tdiv(T(f1), am);  split[1 * S + o] = h * (tmx + q);  split[5 * S + o] = h * (tmx - q);
+    q = tdiv(T(mx), am);  split[0 * S + o] = tscale<-1>(tr + q);   split[4 * S + o] = tscale<-1>(tr - q);
+    q = tdiv(T(f1), am);  split[1 * S + o] = tscale<-1>(tmx + q);  split[5 * S + o] = tscale<-1>(tmx - q);
     T qxy = tdiv(T(fxy), am);
-    split[2 * S + o] = h * (tmy + qxy); split[6 * S + o] = h * (tmy - qxy);
-    q = tdiv(T(f3), am);  split[3 * S + o] = h * (te + q);   split[7 * S + o] = h * (te - q);
-    q = tdiv(T(my), am);  split[8 * S + o] = h * (tr + q);   split[12 * S + o] = h * (tr - q);
-    split[9 * S + o] = h * (tmx + qxy); split[13 * S + o] = h * (tmx - qxy);
-    q = tdiv(T(g2), am);  split[10 * S + o] = h * (tmy + q); split[14 * S + o] = h * (tmy - q);
-    q = tdiv(T(g3), am);  split[11 * S + o] = h * (te + q);  split[15 * S + o] = h * (te - q);
+    split[2 * S + o] = tscale<-1>(tmy + qxy); split[6 * S + o] = tscale<-1>(tmy - qxy);
+    q = tdiv(T(f3), am);  split[3 * S + o] = tscale<-1>(te + q);   split[7 * S + o] = tscale<-1>(te - q);
+    q = tdiv(T(my), am);  split[8 * S + o] = tscale<-1>(tr + q);   split[12 * S + o] = tscale<-1>(tr - q);
+    split[9 * S + o] = tscale<-1>(tmx + qxy); split[13 * S + o] = tscale<-1>(tmx - qxy);
+    q = tdiv(T(g2), am);  split[10 * S + o] = tscale<-1>(tmy + q); split[14 * S + o] = tscale<-1>(tmy - q);
+    q = tdiv(T(g3), am);  split[11 * S + o] = tscale<-1>(te + q);  split[15 * S + o] = tscale<-1>(te - q);
   } else {
     if (which & 1) {
       // x segments whose local columns s*nxl-2 .. s*nxl+nxl+3 hold column i
@@ -462,10 +462,10 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
         const T am = T(p.seg_ax[(int64_t)(j + 2) * p.cut_x + sx]);
         const int64_t os = seg_x_off(p, i, j, sx);
         T q;
-        q = tdiv(T(mx), am);  split[0 * S + os] = h * (tr + q);  split[4 * S + os] = h * (tr - q);
-        q = tdiv(T(f1), am);  split[1 * S + os] = h * (tmx + q); split[5 * S + os] = h * (tmx - q);
-        q = tdiv(T(fxy), am); split[2 * S + os] = h * (tmy + q); split[6 * S + os] = h * (tmy - q);
-        q = tdiv(T(f3), am);  split[3 * S + os] = h * (te + q);  split[7 * S + os] = h * (te - q);
+        q = tdiv(T(mx), am);  split[0 * S + os] = tscale<-1>(tr + q);  split[4 * S + os] = tscale<-1>(tr - q);
+        q = tdiv(T(f1), am);  split[1 * S + os] = tscale<-1>(tmx + q); split[5 * S + os] = tscale<-1>(tmx - q);
+        q = tdiv(T(fxy), am); split[2 * S + os] = tscale<-1>(tmy + q); split[6 * S + os] = tscale<-1>(tmy - q);
+        q = tdiv(T(f3), am);  split[3 * S + os] = tscale<-1>(te + q);  split[7 * S + os] = tscale<-1>(te - q);
       }
     }
     if (which & 2) {
@@ -493,10 +493,10 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
         }
         const T tr2 = T(r2), tm2 = T(m2), tn2 = T(n2), te2 = T(e2);
         T q;
-        q = tdiv(T(n2), am);   split[8 * S + os] = h * (tr2 + q);  split[12 * S + os] = h * (tr2 - q);
-        q = tdiv(T(fxy2), am); split[9 * S + os] = h * (tm2 + q);  split[13 * S + os] = h * (tm2 - q);
-        q = tdiv(T(g22), am);  split[10 * S + os] = h * (tn2 + q); split[14 * S + os] = h * (tn2 - q);
-        q = tdiv(T(g32), am);  split[11 * S + os] = h * (te2 + q); split[15 * S + os] = h * (te2 - q);
+        q = tdiv(T(n2), am);   split[8 * S + os] = tscale<-1>(tr2 + q);  split[12 * S + os] = tscale<-1>(tr2 - q);
+        q = tdiv(T(fxy2), am); split[9 * S + os] = tscale<-1>(tm2 + q);  split[13 * S + os] = tscale<-1>(tm2 - q);
+        q = tdiv(T(g22), am);  split[10 * S + os] = tscale<-1>(tn2 + q); split[14 * S + os] = tscale<-1>(tn2 - q);
+        q = tdiv(T(g32), am);  split[11 * S + os] = tscale<-1>(te2 + q); split[15 * S + os] = tscale<-1>(te2 - q);
       }
     }
   }
@@ -504,7 +504,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   if (which & 1) {
     double t0 = F32 ? ri : tdiv(1., rho);
     double vex = mx * t0, vey = my * t0;
-    double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+    double pre = g1 * (e - tscale<-1>(mx * vex + my * vey));
     roe[0 * P + o] = sqrt_abs<T>(rho);
     roe[1 * P + o] = T(vex);
     roe[2 * P + o] = T(vey);
@@ -514,7 +514,7 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
     // ex4_sedov_2d/main.f90:426
     double t0 = reg_recip(p, rho);
     double vex = mx * t0, vey = my * t0;
-    double pre = g1 * (e - 0.5 * (mx * vex + my * vey));
+    double pre = g1 * (e - tscale<-1>(mx * vex + my * vey));
     roe[4 * P + o] = sqrt_abs<T>(rho);
     roe[5 * P + o] = T(vex);
     roe[6 * P + o] = T(vey);

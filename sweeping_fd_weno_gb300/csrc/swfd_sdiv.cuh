@@ -1,5 +1,5 @@
-// swfd_sdiv.cuh -- IEEE binary64 division on the integer and FP32 pipes
-// (host and device).
+// swfd_sdiv.cuh -- IEEE binary64 division and scaling by powers of two on the
+// integer and FP32 pipes (host and device).
 //
 // A GB300 SM retires two FP64 operations per clock against 128 integer or
 // FP32 ones, and an IEEE binary64 division costs a sequence of FP64
@@ -10,7 +10,11 @@
 // rounded with the remainder as sticky bit.  Operands that are zero,
 // subnormal, infinite or NaN, and quotients whose exponent is within a
 // binade of the binary64 limits, take the hardware division, so the result
-// equals a / b for every input.
+// equals a / b for every input.  sd::scale<K> (x * 2^K: an addition to the
+// exponent field) falls back in the same way and equals x * 2^K for every
+// input.  (A software product -- 106-bit integer product, rounded -- measured
+// slower than the hardware DMUL in the flux kernel: its dependent integer
+// chain outweighs the FP64 issue it saves.)
 #pragma once
 
 #include <stdint.h>
@@ -18,8 +22,12 @@
 
 #ifdef __CUDACC__
 #define SWFD_SD __host__ __device__ __forceinline__
+// the hardware fallbacks are calls, so that the compiler cannot if-convert
+// them into FP64 instructions that every call would execute
+#define SWFD_SD_SLOW static __host__ __device__ __noinline__
 #else
 #define SWFD_SD static inline
+#define SWFD_SD_SLOW static
 #endif
 
 namespace swfd {
@@ -45,6 +53,9 @@ SWFD_SD float ffrom(uint32_t u) {
   memcpy(&x, &u, 4);
   return x;
 }
+SWFD_SD_SLOW double div_hw(double a, double b) { return a / b; }
+SWFD_SD_SLOW double mul_hw(double a, double b) { return a * b; }
+
 // correctly rounded binary32 reciprocal (only an estimate is needed)
 SWFD_SD float rcp32(float x) {
 #ifdef __CUDA_ARCH__
@@ -60,7 +71,7 @@ SWFD_SD double div(double a, double b) {
   // biased exponent of the quotient when ma >= mb; the result's is e or e - 1
   // before rounding and at most one more after it
   int32_t e = (int32_t)ea - (int32_t)eb + 1023;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 2 || e > 2045) return a / b;
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 2 || e > 2045) return div_hw(a, b);
   const uint64_t frac = 0xfffffffffffffull;
   const uint64_t B = (ub & frac) | (1ull << 52);
   uint64_t A = (ua & frac) | (1ull << 52);
@@ -99,6 +110,17 @@ SWFD_SD double div(double a, double b) {
     e += 1;
   }
   return dfrom(((ua ^ ub) & 0x8000000000000000ull) | ((uint64_t)e << 52) | (q & frac));
+}
+
+// x * 2^K: only the exponent field changes while x and the result are normal
+template <int K>
+SWFD_SD double scale(double x) {
+  constexpr uint32_t lo = K < 0 ? 1 - K : 1, hi = K > 0 ? 2046 - K : 2046;
+  constexpr double f = K >= 0 ? (double)(1ull << (K >= 0 ? K : 0)) : 1.0 / (double)(1ull << (K < 0 ? -K : 0));
+  const uint64_t u = dbits(x);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7ffu;
+  if (e - lo > hi - lo) return mul_hw(x, f);
+  return dfrom(u + ((uint64_t)(int64_t)K << 52));
 }
 
 }  // namespace sd

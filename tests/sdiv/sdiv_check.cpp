@@ -1,4 +1,5 @@
-// Checks sd::div of swfd_sdiv.cuh against the host's IEEE binary64 division
+// Checks sd::div and sd::scale of swfd_sdiv.cuh against the host's IEEE
+// binary64 division and scaling
 // (x86-64 SSE2 or AArch64, round to nearest, ties to even) on random and
 // edge-case operands.  Prints the number of mismatching bit patterns.
 #include <math.h>
@@ -47,7 +48,7 @@ static double pick(int mode) {
 
 int main(int argc, char** argv) {
   const long n = argc > 1 ? atol(argv[1]) : 1000000;
-  long bad = 0, fast = 0;
+  long bad = 0, fast = 0, bads = 0;
   for (long i = 0; i < n; ++i) {
     const double a = pick(i % 4), b = pick((i / 4) % 4);
     if (!same(swfd::sd::div(a, b), a / b)) {
@@ -58,6 +59,9 @@ int main(int argc, char** argv) {
     const double q = pick(1), c = pick(1);
     const double p = q * c;
     if (!same(swfd::sd::div(p, c), p / c)) bad++;
+    if (!same(swfd::sd::scale<1>(a), a * 2.0) || !same(swfd::sd::scale<2>(a), a * 4.0) ||
+        !same(swfd::sd::scale<-1>(a), a * 0.5) || !same(swfd::sd::scale<-2>(a), a * 0.25))
+      bads++;
     const uint32_t ea = (uint32_t)(swfd::sd::dbits(a) >> 52) & 0x7ff;
     fast += ea != 0 && ea != 0x7ff;
   }
@@ -67,10 +71,17 @@ int main(int argc, char** argv) {
   const int ne = sizeof(edge) / sizeof(edge[0]);
   for (int i = 0; i < ne; ++i)
     for (int j = 0; j < ne; ++j)
+    {
       if (!same(swfd::sd::div(edge[i], edge[j]), edge[i] / edge[j])) {
         printf("edge mismatch %a / %a\n", edge[i], edge[j]);
         bad++;
       }
-  printf("div %ld (of %ld, %ld with a normal dividend)\n", bad, 2 * n + ne * ne, fast);
-  return bad ? 1 : 0;
+    }
+  for (int i = 0; i < ne; ++i)
+    if (!same(swfd::sd::scale<-1>(edge[i]), edge[i] * 0.5) ||
+        !same(swfd::sd::scale<1>(edge[i]), edge[i] * 2.0))
+      bads++;
+  printf("div %ld scale %ld (of %ld, %ld with a normal first operand)\n", bad, bads,
+         2 * n + ne * ne, fast);
+  return (bad || bads) ? 1 : 0;
 }

@@ -1,5 +1,6 @@
-"""The software binary64 division of csrc/swfd_sdiv.cuh (host and device
-code) against the host's IEEE division, on the CPU: 2M random and edge-case
+"""The software binary64 division and power-of-two scaling of
+csrc/swfd_sdiv.cuh (host and device code) against the host's IEEE
+arithmetic, on the CPU: 2M random and edge-case
 operand pairs (subnormals, infinities, NaN, exponent limits, long runs of
 ones and zeros, exact quotients) must give the same bits."""
 import shutil
@@ -23,4 +24,4 @@ def test_sdiv_matches_ieee_division(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe), "1000000"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.startswith("div 0 "), r.stdout
+    assert r.stdout.startswith("div 0 scale 0 "), r.stdout
