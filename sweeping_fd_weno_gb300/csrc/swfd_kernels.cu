@@ -124,9 +124,9 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
     if (g.ndim == 1) {
       // ex2_sedov_1d/main.f90:278-283
       double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o);
-      double pres = g1 * (u3 - u2 * u2 / u1 / 2.);
-      double sound = sqrt(gamma * pres / u1);
-      a = fabs(u2 / u1) + sound;
+      double pres = g1 * (u3 - tscale<-1>(tdiv(u2 * u2, u1)));
+      double sound = sqrt(tdiv(gamma * pres, u1));
+      a = fabs(tdiv(u2, u1)) + sound;
     } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
       // FP32-bulk: the pressure recovered in FP64 (one reciprocal per cell);
       // the CFL quantities (velocities, sound speed, their max) in FP32
@@ -148,19 +148,20 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
              u4 = ld(u + 3 * g.plane + o);
       if (!p.alpha_guarded) {
         // ex3_vortex_accuracy_2d/main.f90:556-559
-        double pres = g1 * (u4 - u2 * u2 / u1 / 2. - u3 * u3 / u1 / 2.);
-        double sound = sqrt(gamma * pres / u1);
-        a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+        double pres = g1 * (u4 - tscale<-1>(tdiv(u2 * u2, u1)) - tscale<-1>(tdiv(u3 * u3, u1)));
+        double sound = sqrt(tdiv(gamma * pres, u1));
+        a = fmax(fabs(tdiv(u2, u1)) + sound, fabs(tdiv(u3, u1)) + sound);
       } else {
         // ex5_mach2000_jet/main.f90:571-584
         double vx = 0., vy = 0.;
         if (u1 >= p.eps2) {
-          vx = u2 / u1;
-          vy = u3 / u1;
+          vx = tdiv(u2, u1);
+          vy = tdiv(u3, u1);
         }
-        double pres = g1 * (u4 - 0.5 * u1 * (vx * vx) - 0.5 * u1 * (vy * vy));
-        double sound = sqrt(gamma * pres / u1);
-        a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+        const double hu1 = tscale<-1>(u1);
+        double pres = g1 * (u4 - hu1 * (vx * vx) - hu1 * (vy * vy));
+        double sound = sqrt(tdiv(gamma * pres, u1));
+        a = fmax(fabs(tdiv(u2, u1)) + sound, fabs(tdiv(u3, u1)) + sound);
       }
     }
     a = fmax(0.0, a);
@@ -703,22 +704,22 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
   const int64_t P = g.plane, o = g.at(mm, -2);
   const double g1d = p.gamma1;
   double u1 = ld(u + o), u2 = ld(u + P + o), u3 = ld(u + 2 * P + o);
-  double vxd = u2 / u1;
-  double hmd = (g1d * (u3 - 0.5 * (u2 * u2) / u1) + u3) / u1;
+  double vxd = tdiv(u2, u1);
+  double hmd = tdiv(g1d * (u3 - tdiv(tscale<-1>(u2 * u2), u1)) + u3, u1);
   const T g1 = T(g1d), vxm = T(vxd), hm = T(hmd);
-  T qm = T(0.5) * vxm * vxm;
+  T qm = tscale<-1>(vxm) * vxm;
   T cm = sqrt(g1 * (hm - qm));
   T t0 = vxm * cm;
   T r10 = vxm - cm, r12 = vxm + cm, r20 = hm - t0, r22 = hm + t0;
-  T rcm = T(1.) / cm;
+  T rcm = tdiv(T(1.), cm);
   T b1 = g1 * rcm * rcm;
   T b2 = qm * b1;
   t0 = vxm * rcm;
   T t1 = b1 * vxm;
-  T t2 = T(0.5) * b1;
-  T L[3][3] = {{T(0.5) * (b2 + t0), -T(0.5) * (t1 + rcm), t2},
+  T t2 = tscale<-1>(b1);
+  T L[3][3] = {{tscale<-1>(b2 + t0), -tscale<-1>(t1 + rcm), t2},
                {T(1.) - b2, t1, -b1},
-               {T(0.5) * (b2 - t0), -T(0.5) * (t1 - rcm), t2}};
+               {tscale<-1>(b2 - t0), -tscale<-1>(t1 - rcm), t2}};
   const T weps = T(p.weno_eps);
   const int k = sub < 6 ? sub >> 1 : 0, side = sub & 1;
   const T* sp = split + (side ? 3 * P : 0);
@@ -956,15 +957,16 @@ static int flux_grid() {
 
 // Launch-shape variants of the common flux kernel (no rank segments, no
 // limiter) that swfd_autotune times: resident blocks per SM, traded against
-// registers per thread (FP64: 3 = 168 registers, 2 = 255; FP32: 4 = 128,
-// 5 = 102, 6 = 85).  The first entry is the default.
+// registers per thread (FP64: 3 = 168 registers, 2 = 236, 4 = 128 with about
+// 200 bytes of spills; FP32: 4 = 128, 5 = 102, 6 = 85).  The first entry is
+// the default.
 int flux_min_blocks_candidates(bool f32, int* out) {
   if (f32) {
     out[0] = 4, out[1] = 5, out[2] = 6;
     return 3;
   }
-  out[0] = 3, out[1] = 2;
-  return 2;
+  out[0] = 3, out[1] = 2, out[2] = 4;
+  return 3;
 }
 
 template <class T, int MINB>
@@ -999,6 +1001,7 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
   if (!p.seg_alpha && !p.limiter && p.flux_minb && p.flux_minb != SWFD_FLUX_MINB(T)) {
     if constexpr (sizeof(T) == 8) {
       if (p.flux_minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
+      if (p.flux_minb == 4) return launch_flux_minb<T, 4>(p, sp, rp, dsc, fp, work, s);
     } else {
       if (p.flux_minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
       if (p.flux_minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
@@ -1067,8 +1070,9 @@ __device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, 
     return -(am * A) * ix - (am * B) * iy;
   } else {
     const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
-    if (p.alpha_premul) return -A / dx - B / dy;  // ex4_sedov_2d/main.f90:644-645
-    return -(am * A) / dx - (am * B) / dy;         // ex3_vortex_accuracy_2d/main.f90:541-542
+    // (-x)/d == -(x/d): the divisions on the integer pipes (tdiv)
+    if (p.alpha_premul) return -tdiv(A, dx) - tdiv(B, dy);  // ex4_sedov_2d/main.f90:644-645
+    return -tdiv(am * A, dx) - tdiv(am * B, dy);            // ex3_vortex_accuracy_2d/main.f90:541-542
   }
 }
 
@@ -1082,7 +1086,7 @@ __device__ __forceinline__ T rhs1d(const Params& p, const T* __restrict__ flux, 
   const T am = T(amd);
   T fl_i = am * (ldt(hp + o - 1) - ldt(hn + o));
   T fl_ip1 = am * (ldt(hp + o) - ldt(hn + o + 1));
-  return -(fl_ip1 - fl_i) / T(p.dx);
+  return -tdiv(fl_ip1 - fl_i, T(p.dx));
 }
 
 __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
@@ -1107,8 +1111,8 @@ __device__ __forceinline__ double rk_combine(const Params& p, int stage, double 
       return to_double(add(mul(from_double(0.75), from_double(u0)), scale2(from_double(v), -2)));
     return to_double(div(add(from_double(u0), scale2(from_double(v), 1)), from_double(3.0)));
   }
-  if (stage == 2) return 0.75 * u0 + 0.25 * v;
-  return (u0 + 2.0 * v) / 3.0;
+  if (stage == 2) return 0.75 * u0 + tscale<-2>(v);
+  return tdiv(u0 + tscale<1>(v), 3.0);
 }
 
 template <class T>
@@ -1149,9 +1153,9 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
         if (g.ndim == 1) pe = fma(nv[1] * nv[1], ri, nv[2]);
         else pe = fma(fma(nv[2], nv[2], nv[1] * nv[1]), ri, nv[3]);
       } else if (g.ndim == 1) {
-        pe = nv[2] - nv[1] * nv[1] / nv[0] / 2.;
+        pe = nv[2] - tscale<-1>(tdiv(nv[1] * nv[1], nv[0]));
       } else {
-        pe = nv[3] - nv[2] * nv[2] / nv[0] / 2. - nv[1] * nv[1] / nv[0] / 2.;
+        pe = nv[3] - tscale<-1>(tdiv(nv[2] * nv[2], nv[0])) - tscale<-1>(tdiv(nv[1] * nv[1], nv[0]));
       }
       if (p.pos_strict) bad = (nv[0] < p.eps) || (pe < p.eps);
       else bad = (nv[0] <= p.eps) || (pe <= p.eps);
@@ -1225,7 +1229,7 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
   if (interior && c == 0) {
     double pe;
     if (sizeof(T) == 4) pe = fma(n1 * n1, -0.5 * rcp_bulk(n0), n2);
-    else pe = n2 - n1 * n1 / n0 / 2.;
+    else pe = n2 - tscale<-1>(tdiv(n1 * n1, n0));
     if (p.pos_strict) bad = (n0 < p.eps) || (pe < p.eps);
     else bad = (n0 <= p.eps) || (pe <= p.eps);
   }

@@ -15,8 +15,26 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
     for s in (a, b):
         s.init_problem()
     minb = b.autotune()
-    assert minb in ((3, 2) if precision == abi.PRECISION_FP64 else (4, 5, 6))
+    assert minb in ((3, 2, 4) if precision == abi.PRECISION_FP64 else (4, 5, 6))
     for _ in range(4):
+        assert a.step() == b.step()
+    assert np.array_equal(a.state(), b.state())
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("precision,minb", [(abi.PRECISION_FP64, 2), (abi.PRECISION_FP64, 4),
+                                            (abi.PRECISION_FP32_BULK, 5),
+                                            (abi.PRECISION_FP32_BULK, 6)])
+def test_each_flux_launch_shape_keeps_results(swfd, monkeypatch, precision, minb):
+    # SWFD_FLUX_MIN_BLOCKS pins a candidate: every shape runs, not only the fastest
+    monkeypatch.setenv("SWFD_FLUX_MIN_BLOCKS", str(minb))
+    cfg = problems.make_config(abi.VORTEX_2D, nx=72, ny=56, precision=precision)
+    a, b = Solver(cfg), Solver(cfg)
+    for s in (a, b):
+        s.init_problem()
+    assert b.autotune() == minb
+    for _ in range(3):
         assert a.step() == b.step()
     assert np.array_equal(a.state(), b.state())
     a.close()
