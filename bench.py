@@ -39,14 +39,17 @@ UNIT = "cell-updates/s"
 STAGE_BYTES_PER_CELL = (64 + 96 + 96) / 3.0
 # FP64 work of one interface flux (Roe eigenvectors, 40 projections, 8 WENO5
 # reconstructions, back projection): 800 adds/multiplies + 50 divisions + 1
-# square root in the source; executed, 1197 FP64 pipe instructions (379 DADD,
-# 465 DMUL, 353 DFMA -- the DFMAs are the correctly rounded divisions and the
-# square root), counted by ncu on k_flux_xy<double>
+# square root in the source.  With the hardware division this executes 1197
+# FP64 pipe instructions (379 DADD, 465 DMUL, 353 DFMA -- the DFMAs are the
+# divisions and the square root); with the divisions and the products by
+# 2, 4, 0.25 and 0.5 on the integer pipes (the same bits), 739 (355 DADD,
+# 379 DMUL, 5 DFMA).  Both counted by ncu on k_flux_xy<double>.
 FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
-FLUX_FP64_INST_PER_INTERFACE = 1197
+FLUX_FP64_INST_PER_INTERFACE = 739
+FLUX_FP64_INST_PER_INTERFACE_HW_DIV = 1197
 # DRAM bytes of one k_flux_xy<double> launch per interior cell, from an ncu
-# capture of the 1024x1024 vortex (313.6 MB per launch, inputs above L2)
-FLUX_DRAM_BYTES_PER_CELL = 313.6e6 / (1024 * 1024)
+# capture of the 1024x1024 vortex (310.6 MB per launch, inputs above L2)
+FLUX_DRAM_BYTES_PER_CELL = 310.6e6 / (1024 * 1024)
 # the same for k_flux_xy<float> of the FP32-bulk form (134.4 MB per launch)
 FLUX_F32_DRAM_BYTES_PER_CELL = 134.4e6 / (1024 * 1024)
 
@@ -652,15 +655,24 @@ def main():
         roofline.update({
             "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                              "k_flux_xy<double> on the 1024x1024 vortex (313.6 MB), scaled "
+                              "k_flux_xy<double> on the 1024x1024 vortex (310.6 MB), scaled "
                               "per cell to this grid",
             "kernel": "k_flux_xy<double> (characteristic WENO5 interface fluxes, both directions)",
-            "compute_bound": "fp64",
+            "compute_bound": "fp64 (the FP64 pipe; divisions and power-of-two products run "
+                             "on the integer pipes)",
             "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,
                      "frac": fp64_inst_rate / fp64_peak_inst if fp64_peak_inst else None,
                      "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains; 2 flops "
                                     "each)",
                      "inst_per_interface": FLUX_FP64_INST_PER_INTERFACE,
+                     # the all-hardware instruction stream of the same arithmetic
+                     # (hardware divisions) over the measured time: above 1.0 means
+                     # faster than that stream could run at the FP64 peak
+                     "hw_division_equivalent_frac":
+                         2 * cells * FLUX_FP64_INST_PER_INTERFACE_HW_DIV
+                         / (flux_ms_per_launch * 1e-3) / 1e9 / fp64_peak_inst
+                         if fp64_peak_inst else None,
+                     "hw_division_inst_per_interface": FLUX_FP64_INST_PER_INTERFACE_HW_DIV,
                      "achieved_gflops_source_count": 2 * cells * FLUX_FLOPS_PER_INTERFACE
                      / (flux_ms_per_launch * 1e-3) / 1e9,
                      "flops_per_interface": FLUX_FLOPS_PER_INTERFACE}})
