@@ -74,7 +74,14 @@ enum {
                                    part of its arithmetic (per-rank-row and
                                    per-rank-column Lax-Friedrichs alpha, fluxes at
                                    rank boundaries computed by both ranks) and is
-                                   reproduced on one grid */
+                                   reproduced on one grid */,
+  SWFD_PROBLEM_DETONATION = 7  /* ex7_detonation/main.f90: reactive Euler, five
+                                  components (rho, m_x, m_y, E, rho*Y; the state
+                                  is u(5,-2:nx+3,-2:ny+3)), the chemistry source
+                                  on the fifth; ex6's rank decomposition with
+                                  nx = cut_x*(5*total/cut_x), ny = cut_y*(5*total/cut_y),
+                                  the wall's top row 2*total; literals DOUBLE and
+                                  use_limiter 0 or 2 */
 };
 
 /* How the reference's double-kind literals (1d-6, 13d0/12d0, 0.75d0, ...)
@@ -116,10 +123,12 @@ typedef struct swfd_config {
   double e_blast;        /* point-energy problems: blast energy numerator
                             (1D: E = e_blast/dx, 2D: E = e_blast/(dx*dy)) */
   int32_t sweep_mode;    /* SWFD_SWEEP_PARALLEL (default) or SWFD_SWEEP_SEQUENTIAL */
-  int32_t total;         /* shock diffraction: the reference's `total` (step width in
-                            cells; the step top is row 6*total); 0 otherwise */
-  int32_t cut_x, cut_y;  /* shock diffraction: the reference's rank grid (4 x 8);
-                            nx = cut_x*(13*total/cut_x), ny = cut_y*(11*total/cut_y) */
+  int32_t total;         /* shock diffraction and detonation: the reference's `total`
+                            (step width in cells; the step top is row 6*total,
+                            detonation 2*total); 0 otherwise */
+  int32_t cut_x, cut_y;  /* shock diffraction and detonation: the reference's rank
+                            grid (4 x 8); shock diffraction nx = cut_x*(13*total/cut_x),
+                            ny = cut_y*(11*total/cut_y) */
   int32_t rk_choice;     /* the reference's RK_choice: 1 (or 0) = SSP-RK3 with the
                             sweeping post-process (rk3); 2 = the dt-halving
                             restart RK of ex2 (`rk`, ex2_sedov_1d/main.f90:330-374:

@@ -82,7 +82,8 @@ class Oracle:
         self.cfg = cfg
         self.o = self.lib.oracle_create(C.byref(cfg))
         ndim = 1 if cfg.problem in (1, 2) else 2  # the MATLAB script and ex2 are 1D
-        self.shape = (1, cfg.nx + 6, 3) if ndim == 1 else (cfg.ny + 6, cfg.nx + 6, 4)
+        nc = 5 if cfg.problem == 7 else 4  # ex7: rho, m_x, m_y, E, rho*Y
+        self.shape = (1, cfg.nx + 6, 3) if ndim == 1 else (cfg.ny + 6, cfg.nx + 6, nc)
 
     def close(self):
         if self.o:

@@ -73,6 +73,11 @@ typedef struct oracle {
   struct oracle** rk;
   double* alpha;
   double dle, ule, ple;
+  /* ex7 (detonation): q_const, t_const, k_const (ex7_detonation/main.f90:18),
+   * the wall's top row step*total (:12,188) and the per-line Roe Y ratio */
+  double qc, tc, kc;
+  int wall_rows;
+  double* wk_ratio;
   int ranks_stale; /* the global state was set from outside: rebuild the ranks */
 } oracle;
 
@@ -1405,7 +1410,7 @@ static oracle* ex6_rank_create(const oracle* g, int px, int py) {
   r->problem = g->problem;
   r->quad = g->quad;
   r->ndim = 2;
-  r->nc = 4;
+  r->nc = g->nc;
   r->nx = g->nxl;
   r->ny = g->nyl;
   r->LI = r->nx + 6;
@@ -1432,12 +1437,17 @@ static oracle* ex6_rank_create(const oracle* g, int px, int py) {
   r->wk_vx = calloc(mx, sizeof(double));
   r->wk_vy = calloc(mx, sizeof(double));
   r->wk_h = calloc(mx, sizeof(double));
+  r->wk_ratio = calloc(mx, sizeof(double));
+  r->qc = g->qc;
+  r->tc = g->tc;
+  r->kc = g->kc;
+  r->wall_rows = g->wall_rows;
   return r;
 }
 
 static void ex6_rank_destroy(oracle* r) {
   double* arrs[] = {r->u, r->u0, r->rhs, r->fp, r->fn, r->gp, r->gn, r->fpf, r->fnf, r->gpf, r->gnf,
-                    r->alpha, r->wk_w, r->wk_vx, r->wk_vy, r->wk_h};
+                    r->alpha, r->wk_w, r->wk_vx, r->wk_vy, r->wk_h, r->wk_ratio};
   for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); ++k) free(arrs[k]);
   free(r);
 }
@@ -1462,7 +1472,7 @@ static void ex6_assemble(oracle* o) {
       int px = ex6_owner_x(o, I), py = ex6_owner_y(o, J);
       const oracle* r = o->rk[px + o->cut_x * py];
       int i = I - px * o->nxl, j = J - py * o->nyl;
-      for (int c = 0; c < 4; ++c) o->u[IX(o, c, I, J)] = r->u[IX(r, c, i, j)];
+      for (int c = 0; c < o->nc; ++c) o->u[IX(o, c, I, J)] = r->u[IX(r, c, i, j)];
     }
 }
 
@@ -1473,7 +1483,7 @@ static void ex6_distribute(oracle* o) {
     for (int j = -2; j <= r->ny + 3; ++j)
       for (int i = -2; i <= r->nx + 3; ++i) {
         int I = r->px * o->nxl + i, J = r->py * o->nyl + j;
-        for (int c = 0; c < 4; ++c) r->u[IX(r, c, i, j)] = o->u[IX(o, c, I, J)];
+        for (int c = 0; c < o->nc; ++c) r->u[IX(r, c, i, j)] = o->u[IX(o, c, I, J)];
       }
   }
   o->ranks_stale = 0;
@@ -1610,7 +1620,7 @@ static void ex6_exchange_x(oracle* o) {
     const oracle* rr = o->rk[right];
     for (int j = -2; j <= r->ny + 3; ++j)
       for (int m = 1; m <= 3; ++m)
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < o->nc; ++c) {
           r->u[IX(r, c, r->nx + m, j)] = snap[right][IX(rr, c, m, j)];
           r->u[IX(r, c, 1 - m, j)] = snap[left][IX(rl, c, rl->nx + 1 - m, j)];
         }
@@ -1635,7 +1645,7 @@ static void ex6_exchange_y(oracle* o) {
     const oracle* ru = o->rk[up];
     for (int m = 1; m <= 3; ++m)
       for (int i = -2; i <= r->nx + 3; ++i)
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < o->nc; ++c) {
           r->u[IX(r, c, i, r->ny + m)] = snap[up][IX(ru, c, i, m)];
           r->u[IX(r, c, i, 1 - m)] = snap[down][IX(rd, c, i, rd->ny + 1 - m)];
         }
@@ -1709,7 +1719,7 @@ static void ex6_gather(oracle* o) {
     const oracle* r = o->rk[k];
     for (int j = 1; j <= r->ny; ++j)
       for (int i = 1; i <= r->nx; ++i)
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < o->nc; ++c)
           o->u[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)] = r->u[IX(r, c, i, j)];
   }
 }
@@ -1718,7 +1728,7 @@ static void ex6_scatter(oracle* o) {
     oracle* r = o->rk[k];
     for (int j = 1; j <= r->ny; ++j)
       for (int i = 1; i <= r->nx; ++i)
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < o->nc; ++c)
           r->u[IX(r, c, i, j)] = o->u[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)];
   }
 }
@@ -1806,6 +1816,569 @@ static void ex6_init(oracle* o) {
   ex6_assemble(o);
 }
 
+/* ------------------------------------------------------------------ */
+/* ex7: reactive Euler detonation (ex7_detonation/main.f90).  Five      */
+/* components (rho, m_x, m_y, E, rho*Y), eos p = g1*(E - kinetic - q*Y),*/
+/* the chemistry source -k*Y*exp(-t*rho/p) on the fifth.  The rank      */
+/* layout, exchanges, gather and scatter are ex6's (5 components).      */
+/* ------------------------------------------------------------------ */
+
+/* exp(x) evaluated in binary128 and rounded once to binary64: x = k*ln2 + r
+ * with k the nearest integer to x*(1/ln2) (binary64), r = x - k*ln2 in
+ * binary128, exp(r) by Horner on the Taylor coefficients 1/n! (n <= 24, each
+ * the binary128 quotient of the previous by n), times 2^k exactly.  The
+ * library evaluates the same sequence of binary128 operations, so the two
+ * agree bit for bit. */
+#define EXP7_N 24
+static Q exp7_coef[EXP7_N + 1];
+static int exp7_ready;
+double oracle_exp(double x) {
+  if (x != x) return x;
+  if (x > 710.) return INFINITY;
+  if (x < -746.) return 0.;
+  if (!exp7_ready) {
+    exp7_coef[0] = 1;
+    for (int n = 1; n <= EXP7_N; ++n) exp7_coef[n] = exp7_coef[n - 1] / (Q)n;
+    exp7_ready = 1;
+  }
+  const double kd = rint(x * 1.4426950408889634);
+  const Q ln2 = 0.693147180559945309417232121458176568f128;
+  const Q r = (Q)x - (Q)kd * ln2;
+  Q p = exp7_coef[EXP7_N];
+  for (int n = EXP7_N - 1; n >= 0; --n) p = p * r + exp7_coef[n];
+  /* 2^k as binary128 bits (exponent field k + 16383, zero fraction): exact */
+  const uint64_t bits[2] = {0, (uint64_t)((int)kd + 16383) << 48};
+  Q two_k;
+  memcpy(&two_k, bits, sizeof(two_k));
+  return (double)(p * two_k);
+}
+
+/* eos (:168-174) */
+static inline double ex7_eos(const oracle* r, double rho, double vx, double vy, double e,
+                             double y) {
+  return r->gamma1 * (e - 0.5 * rho * (vx * vx) - 0.5 * rho * (vy * vy) - r->qc * y);
+}
+
+/* fflux / gflux (:110-166) */
+static void ex7_flux(const oracle* r, const double* a, double* f, int gdir) {
+  const double rho = a[0], mx = a[1], my = a[2], e = a[3], y = a[4];
+  double vx = mx / rho, vy = my / rho;
+  if (rho < r->eps2) vx = 0.;
+  if (rho < r->eps2) vy = 0.;
+  const double pres = ex7_eos(r, rho, vx, vy, e, y);
+  if (!gdir) {
+    f[0] = mx;
+    f[1] = rho * (vx * vx) + pres;
+    f[2] = rho * vx * vy;
+    f[3] = (e + pres) * vx;
+    f[4] = y * vx;
+  } else {
+    f[0] = my;
+    f[1] = rho * vx * vy;
+    f[2] = rho * (vy * vy) + pres;
+    f[3] = (e + pres) * vy;
+    f[4] = y * vy;
+  }
+}
+
+/* per-line Roe preparation (x pass :200-215, y pass :474-489):
+ * out = {w, vx, vy, ratio, h} */
+static void ex7_prep(const oracle* r, const double* a, double* out) {
+  const double den = a[0], xmt = a[1], ymt = a[2], eng = a[3], yrho = a[4];
+  const double t0 = 1. / den, vex = xmt * t0, vey = ymt * t0;
+  const double pre = r->gamma1 * (eng - 0.5 * (xmt * vex + ymt * vey) - r->qc * yrho);
+  out[0] = sqrt(fabs(den));
+  out[1] = vex;
+  out[2] = vey;
+  out[3] = yrho * t0;
+  out[4] = (pre + eng) * t0;
+}
+
+/* chemsource (:752-771) */
+static double ex7_chemsource(const oracle* r, const double* a) {
+  const double rho = a[0], mx = a[1], my = a[2], e = a[3], y = a[4];
+  double vx = mx / rho, vy = my / rho;
+  if (lt_lit_1em8(r, rho)) vx = 0.;
+  if (lt_lit_1em8(r, rho)) vy = 0.;
+  const double pres = ex7_eos(r, rho, vx, vy, e, y);
+  return -(r->kc * y * oracle_exp(-(r->tc * rho / pres)));
+}
+
+/* one interface: Roe average, 5x5 eigenvectors, projections, ten WENO5
+ * reconstructions, back projection (x pass :228-334, y pass :506-600);
+ * L, R = {w, vx, vy, ratio, h} of the two cells; every product of the
+ * eigenvector sums is formed, zeros and ones included, in the reference's order */
+static void ex7_interface(const oracle* r, int ydir, const double* L, const double* R,
+                          const double sp[5][5], const double sn[5][5], double* outp,
+                          double* outn) {
+  const double g1 = r->gamma1, q = r->qc;
+  double evr[5][5], evl[5][5], cu_p[5][5], cu_n[5][5], ur[5], ul[5];
+  double t0 = L[0] / (L[0] + R[0] + 1e-15);
+  double t1 = 1. - t0;
+  const double vxm = t0 * L[1] + t1 * R[1];
+  const double vym = t0 * L[2] + t1 * R[2];
+  const double ym = t0 * L[3] + t1 * R[3];
+  const double hm = t0 * L[4] + t1 * R[4];
+  const double qm = 0.5 * (vxm * vxm + vym * vym);
+  const double cm = sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
+  const double rcm = 1. / cm;
+  const double b1 = g1 * rcm * rcm;
+  const double b2 = qm * b1;
+  double t2, t3;
+  if (!ydir) {
+    t0 = vxm * cm;
+    const double er[5][5] = {{1.0, 1.0, 0.0, 0.0, 1.0},
+                             {vxm - cm, vxm, 0., 0., vxm + cm},
+                             {vym, vym, -1., 0., vym},
+                             {hm - t0, qm, -vym, q, hm + t0},
+                             {ym, 0., 0., 1., ym}};
+    memcpy(evr, er, sizeof(er));
+    t0 = vxm * rcm;
+    t1 = b1 * vxm;
+    t2 = 0.5 * b1;
+    t3 = b1 * vym;
+    const double el[5][5] = {{0.5 * (b2 + t0), -0.5 * (t1 + rcm), -0.5 * t3, t2, -t2 * q},
+                             {1. - b2, t1, t3, -b1, b1 * q},
+                             {vym, 0.0, -1.0, 0.0, 0.0},
+                             {-b2 * ym, t1 * ym, t3 * ym, -b1 * ym, 1. + q * ym * b1},
+                             {0.5 * (b2 - t0), -0.5 * (t1 - rcm), -0.5 * t3, t2, -t2 * q}};
+    memcpy(evl, el, sizeof(el));
+  } else {
+    t0 = vym * cm;
+    const double er[5][5] = {{1.0, 1.0, 0.0, 0.0, 1.0},
+                             {vxm, vxm, 1.0, 0., vxm},
+                             {vym - cm, vym, 0., 0., vym + cm},
+                             {hm - t0, qm, vxm, q, hm + t0},
+                             {ym, 0., 0., 1., ym}};
+    memcpy(evr, er, sizeof(er));
+    t0 = vym * rcm;
+    t1 = b1 * vym;
+    t2 = 0.5 * b1;
+    t3 = b1 * vxm;
+    const double el[5][5] = {{0.5 * (b2 + t0), -0.5 * t3, -0.5 * (t1 + rcm), t2, -q * t2},
+                             {1. - b2, t3, t1, -b1, b1 * q},
+                             {-vxm, 1.0, 0.0, 0.0, 0.0},
+                             {-ym * b2, ym * t3, ym * t1, -ym * b1, 1. + ym * b1 * q},
+                             {0.5 * (b2 - t0), -0.5 * t3, -0.5 * (t1 - rcm), t2, -q * t2}};
+    memcpy(evl, el, sizeof(el));
+  }
+  for (int ig = 0; ig < 5; ++ig)
+    for (int k = 0; k < 5; ++k) {
+      cu_p[k][ig] = evl[k][0] * sp[ig][0] + evl[k][1] * sp[ig][1] + evl[k][2] * sp[ig][2] +
+                    evl[k][3] * sp[ig][3] + evl[k][4] * sp[ig][4];
+      cu_n[k][ig] = evl[k][0] * sn[ig][0] + evl[k][1] * sn[ig][1] + evl[k][2] * sn[ig][2] +
+                    evl[k][3] * sn[ig][3] + evl[k][4] * sn[ig][4];
+    }
+  for (int kk = 0; kk < 5; ++kk) {
+    ur[kk] = oracle_weno_right_impl(r, cu_p[kk]);
+    ul[kk] = oracle_weno_left_impl(r, cu_n[kk]);
+  }
+  for (int k = 0; k < 5; ++k) {
+    outp[k] = evr[k][0] * ur[0] + evr[k][1] * ur[1] + evr[k][2] * ur[2] + evr[k][3] * ur[3] +
+              evr[k][4] * ur[4];
+    outn[k] = evr[k][0] * ul[0] + evr[k][1] * ul[1] + evr[k][2] * ul[2] + evr[k][3] * ul[3] +
+              evr[k][4] * ul[4];
+  }
+}
+
+/* findalpha of one rank (:774-808; source_alpha is computed there but never
+ * used, so it is left out) */
+static double ex7_findalpha(oracle* r) {
+  double am = 0.;
+  for (int i = -2; i <= r->nx + 3; ++i)
+    for (int j = -2; j <= r->ny + 3; ++j) {
+      const double u1 = UR(r, r->u, 0, i, j), u2 = UR(r, r->u, 1, i, j),
+                   u3 = UR(r, r->u, 2, i, j), u4 = UR(r, r->u, 3, i, j),
+                   u5 = UR(r, r->u, 4, i, j);
+      const double den = u1;
+      double vx, vy;
+      if (den >= r->eps2) {
+        vx = u2 / den;
+        vy = u3 / den;
+      } else {
+        vx = 0.;
+        vy = 0.;
+      }
+      const double pres =
+          r->gamma1 * (u4 - 0.5 * den * (vx * vx) - 0.5 * den * (vy * vy) - u5 * r->qc);
+      const double sound = sqrt(r->gamma * pres / den);
+      const double a = fmax(fabs(u2 / u1) + sound, fabs(u3 / u1) + sound);
+      ALPHA(r, i, j) = a;
+      am = fmax(am, a);
+    }
+  return am;
+}
+
+/* wenofd of one rank (:176-736): wall mirror at column total for global rows
+ * <= step*total (:186-197), per-row alpha over the rank's local row
+ * (:217-223), fluxes scaled by it (:444-445); wall mirror at row step*total
+ * over columns 1..total (:456-470); per-column alpha (:492-497) and scaling
+ * (:728-729) in the y pass */
+static void ex7_wenofd(oracle* r) {
+  const int nx = r->nx, ny = r->ny, total = r->total;
+  double pr[5], sp[5][5], sn[5][5], op[5], on[5], a[5], f[5];
+  for (int j = 0; j <= ny + 1; ++j) {
+    if (r->px == 0 && r->py * ny + j <= r->wall_rows)
+      for (int i = 0; i <= 2; ++i) {
+        for (int c = 0; c < 5; ++c) UR(r, r->u, c, total - i, j) = UR(r, r->u, c, total + 1 + i, j);
+        UR(r, r->u, 1, total - i, j) = -UR(r, r->u, 1, total + 1 + i, j);
+      }
+    for (int i = 0; i <= nx + 2; ++i) {
+      for (int c = 0; c < 5; ++c) a[c] = UR(r, r->u, c, i, j);
+      ex7_prep(r, a, pr);
+      r->wk_w[i] = pr[0];
+      r->wk_vx[i] = pr[1];
+      r->wk_vy[i] = pr[2];
+      r->wk_ratio[i] = pr[3];
+      r->wk_h[i] = pr[4];
+    }
+    double al = 0.;
+    for (int i = -2; i <= nx + 3; ++i) al = fmax(al, ALPHA(r, i, j));
+    for (int i = -2; i <= nx + 3; ++i) {
+      for (int c = 0; c < 5; ++c) a[c] = UR(r, r->u, c, i, j);
+      ex7_flux(r, a, f, 0);
+      for (int c = 0; c < 5; ++c) {
+        UR(r, r->fp, c, i, j) = 0.5 * (a[c] + f[c] / al);
+        UR(r, r->fn, c, i, j) = 0.5 * (a[c] - f[c] / al);
+      }
+    }
+    for (int i = 0; i <= nx + 1; ++i) {
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 5; ++c) {
+          sp[ig][c] = UR(r, r->fp, c, i + ig - 2, j);
+          sn[ig][c] = UR(r, r->fn, c, i + ig - 2, j);
+        }
+      const double L[5] = {r->wk_w[i], r->wk_vx[i], r->wk_vy[i], r->wk_ratio[i], r->wk_h[i]};
+      const double R[5] = {r->wk_w[i + 1], r->wk_vx[i + 1], r->wk_vy[i + 1], r->wk_ratio[i + 1],
+                           r->wk_h[i + 1]};
+      ex7_interface(r, 0, L, R, (const double(*)[5])sp, (const double(*)[5])sn, op, on);
+      for (int c = 0; c < 5; ++c) {
+        UR(r, r->fpf, c, i, j) = al * op[c];
+        UR(r, r->fnf, c, i, j) = al * on[c];
+      }
+    }
+  }
+  if (r->px == 0)
+    for (int j = -2; j <= ny + 3; ++j)
+      if (r->py * ny + j == r->wall_rows)
+        for (int i = 0; i <= 2; ++i)
+          for (int k = 1; k <= total; ++k) {
+            for (int c = 0; c < 5; ++c) UR(r, r->u, c, k, j - i) = UR(r, r->u, c, k, j + 1 + i);
+            UR(r, r->u, 2, k, j - i) = -UR(r, r->u, 2, k, j + 1 + i);
+          }
+  for (int i = 0; i <= nx + 1; ++i) {
+    for (int j = 0; j <= ny + 2; ++j) {
+      for (int c = 0; c < 5; ++c) a[c] = UR(r, r->u, c, i, j);
+      ex7_prep(r, a, pr);
+      r->wk_w[j] = pr[0];
+      r->wk_vx[j] = pr[1];
+      r->wk_vy[j] = pr[2];
+      r->wk_ratio[j] = pr[3];
+      r->wk_h[j] = pr[4];
+    }
+    double al = 0.;
+    for (int j = -2; j <= ny + 3; ++j) al = fmax(al, ALPHA(r, i, j));
+    for (int j = -2; j <= ny + 3; ++j) {
+      for (int c = 0; c < 5; ++c) a[c] = UR(r, r->u, c, i, j);
+      ex7_flux(r, a, f, 1);
+      for (int c = 0; c < 5; ++c) {
+        UR(r, r->gp, c, i, j) = 0.5 * (a[c] + f[c] / al);
+        UR(r, r->gn, c, i, j) = 0.5 * (a[c] - f[c] / al);
+      }
+    }
+    for (int j = 0; j <= ny + 1; ++j) {
+      for (int ig = 0; ig < 5; ++ig)
+        for (int c = 0; c < 5; ++c) {
+          sp[ig][c] = UR(r, r->gp, c, i, j + ig - 2);
+          sn[ig][c] = UR(r, r->gn, c, i, j + ig - 2);
+        }
+      const double L[5] = {r->wk_w[j], r->wk_vx[j], r->wk_vy[j], r->wk_ratio[j], r->wk_h[j]};
+      const double R[5] = {r->wk_w[j + 1], r->wk_vx[j + 1], r->wk_vy[j + 1], r->wk_ratio[j + 1],
+                           r->wk_h[j + 1]};
+      ex7_interface(r, 1, L, R, (const double(*)[5])sp, (const double(*)[5])sn, op, on);
+      for (int c = 0; c < 5; ++c) {
+        UR(r, r->gpf, c, i, j) = al * op[c];
+        UR(r, r->gnf, c, i, j) = al * on[c];
+      }
+    }
+  }
+}
+
+/* scheme (:738-750): flux differences of the alpha-scaled fluxes plus the
+ * chemistry source on the fifth component */
+static void ex7_scheme(oracle* r) {
+  for (int i = 1; i <= r->nx; ++i)
+    for (int j = 1; j <= r->ny; ++j) {
+      for (int c = 0; c < 5; ++c)
+        UR(r, r->rhs, c, i, j) =
+            -((UR(r, r->fpf, c, i, j) - UR(r, r->fnf, c, i + 1, j)) -
+              (UR(r, r->fpf, c, i - 1, j) - UR(r, r->fnf, c, i, j))) / r->dx -
+            ((UR(r, r->gpf, c, i, j) - UR(r, r->gnf, c, i, j + 1)) -
+             (UR(r, r->gpf, c, i, j - 1) - UR(r, r->gnf, c, i, j))) / r->dy;
+      double a[5];
+      for (int c = 0; c < 5; ++c) a[c] = UR(r, r->u, c, i, j);
+      UR(r, r->rhs, 4, i, j) = UR(r, r->rhs, 4, i, j) + ex7_chemsource(r, a);
+    }
+}
+
+/* checkpositivity over every rank's interior (:890-913) */
+static int ex7_checkpositivity(oracle* o) {
+  int postag = 0;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    const oracle* r = o->rk[k];
+    for (int i = 1; i <= r->nx; ++i)
+      for (int j = 1; j <= r->ny; ++j) {
+        const double u1 = UR(r, r->u, 0, i, j), u2 = UR(r, r->u, 1, i, j),
+                     u3 = UR(r, r->u, 2, i, j), u4 = UR(r, r->u, 3, i, j),
+                     u5 = UR(r, r->u, 4, i, j);
+        if (u1 <= r->eps) postag = 1;
+        if (u4 - u3 * u3 / u1 / 2. - u2 * u2 / u1 / 2. - r->qc * u5 <= r->eps) postag = 1;
+      }
+  }
+  return postag;
+}
+
+static inline void ex7_set(oracle* r, int i, int j, double a, double b, double c, double d,
+                           double e) {
+  UR(r, r->u, 0, i, j) = a;
+  UR(r, r->u, 1, i, j) = b;
+  UR(r, r->u, 2, i, j) = c;
+  UR(r, r->u, 3, i, j) = d;
+  UR(r, r->u, 4, i, j) = e;
+}
+
+/* bc (:915-1071): exchanges twice, then the quiescent bottom and right, the
+ * reflecting top, the inflow left and the quiescent solid block (global
+ * i < total, j < step*total), ghosts included */
+static void ex7_bc(oracle* o) {
+  ex6_exchange_x(o);
+  ex6_exchange_y(o);
+  ex6_exchange_x(o);
+  ex6_exchange_y(o);
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    const int nx = r->nx, ny = r->ny;
+    if (r->py == 0)
+      for (int jj = -2; jj <= 0; ++jj)
+        for (int i = -2; i <= nx + 3; ++i) ex7_set(r, i, jj, 1., 0., 0., 55., 1.);
+    if (r->px == o->cut_x - 1)
+      for (int ii = 1; ii <= 3; ++ii)
+        for (int j = -2; j <= ny + 3; ++j) ex7_set(r, nx + ii, j, 1., 0., 0., 55., 1.);
+    if (r->py == o->cut_y - 1)
+      for (int ii = 1; ii <= 3; ++ii)
+        for (int i = -2; i <= nx + 3; ++i) {
+          for (int c = 0; c < 5; ++c) UR(r, r->u, c, i, ny + ii) = UR(r, r->u, c, i, ny);
+          UR(r, r->u, 2, i, ny + ii) = -UR(r, r->u, 2, i, ny);
+        }
+    if (r->px == 0)
+      for (int ii = -2; ii <= 0; ++ii)
+        for (int j = -2; j <= ny + 3; ++j) ex7_set(r, ii, j, 11., 11. * 6.18, 0., 970., 11.);
+    for (int i = -2; i <= nx + 3; ++i)
+      for (int j = -2; j <= ny + 3; ++j)
+        if (i + r->px * nx < o->total && j + r->py * ny < o->wall_rows)
+          ex7_set(r, i, j, 1., 0., 0., 55., 1.);
+  }
+}
+
+/* initdata (:1196-1260): the post-detonation state where x < 0.5, the
+ * quiescent state elsewhere, on local cells 0..nx+1 x 0..ny+1 of every rank;
+ * then bc */
+static void ex7_init(oracle* o) {
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    oracle* r = o->rk[k];
+    memset(r->u, 0, state_len(r) * sizeof(double));
+    const double xleft = 5. / o->cut_x * r->px;
+    for (int i = 0; i <= r->nx + 1; ++i)
+      for (int j = 0; j <= r->ny + 1; ++j) {
+        const double x = xleft + i * r->dx - r->dx / 2.;
+        if (x < 0.5) ex7_set(r, i, j, 11., 11. * 6.18, 0., 970., 11.);
+        else ex7_set(r, i, j, 1., 0., 0., 55., 1.);
+      }
+  }
+  ex7_bc(o);
+  o->ranks_stale = 0;
+  ex6_assemble(o);
+}
+
+/* pressure of a sweep vector: `form` 0 is g1*(v4 - 0.5*v2*v2/v1 -
+ * 0.5*v3**2/v1 - q*v5) (the unadjusted v_i and v_p, :1503,1532), 1 the
+ * all-squared g1*(v4 - 0.5*v2**2/v1 - 0.5*v3**2/v1 - q*v5) (nod_lim, the
+ * adjusted vectors and u_bar, :1405-1406,1533-1535) */
+static inline double ex7_psweep(const oracle* o, const double* v, int form) {
+  if (form == 0)
+    return o->gamma1 * (v[3] - 0.5 * v[1] * v[1] / v[0] - 0.5 * (v[2] * v[2]) / v[0] - o->qc * v[4]);
+  return o->gamma1 * (v[3] - 0.5 * (v[1] * v[1]) / v[0] - 0.5 * (v[2] * v[2]) / v[0] - o->qc * v[4]);
+}
+
+/* nod_lim (:1399-1429) */
+static void ex7_nod_lim(oracle* o, const double* v1, const double* v2, const double* vb,
+                        double* out) {
+  const double eps = o->eps;
+  const double p1 = ex7_psweep(o, v1, 1), p2 = ex7_psweep(o, v2, 1);
+  double t;
+  if (p2 > eps) {
+    t = (p1 - eps) / (p1 - p2);
+    o->t_pos_count++;
+  } else {
+    const double pb = ex7_psweep(o, vb, 1);
+    const double t_1 = (p1 - eps) / (p1 - pb);
+    const double d12 = sqrt(sq(v2[4] - v1[4]) + sq(v2[3] - v1[3]) + sq(v2[2] - v1[2]) +
+                            sq(v2[1] - v1[1]) + sq(v2[0] - v1[0]));
+    const double d1b = sqrt(sq(vb[4] - v1[4]) + sq(vb[3] - v1[3]) + sq(vb[2] - v1[2]) +
+                            sq(vb[1] - v1[1]) + sq(vb[0] - v1[0]));
+    t = fmin(t_1 * d1b / d12, 0.25);
+    o->t_neg_count++;
+  }
+  for (int c = 0; c < 5; ++c) out[c] = (1 - t) * v1[c] + t * v2[c];
+}
+
+/* One pass (:1481-1704).  Ordering I (ord 0): every component at sweepI(k).
+ * Ordering II (ord 1) keeps the reference's indexing: components 1-4 at
+ * sweepII(k) and sweepII(k+-1), component 5 at sweepI(k) and, for the
+ * neighbour, sweepI(k-1) in both directions.  The total-pressure check
+ * stops the run in the ordering-I passes only. */
+static int ex7_pass(oracle* o, int ord, int forward, const double* ubar) {
+  const int N = o->nx * o->ny;
+  const double eps = o->eps, w = o->weight;
+  const int *Ii = o->sI_i, *Ij = o->sI_j;
+  const int *Ai = ord ? o->sII_i : o->sI_i, *Aj = ord ? o->sII_j : o->sI_j;
+  const int k0 = forward ? 0 : N - 1, k1 = forward ? N - 1 : 0, dk = forward ? 1 : -1;
+  for (int k = k0; k != k1; k += dk) {
+    double vi[5], vp[5], vit[5], d[5], vpt[5];
+    /* cells of v_i (components 1-4, component 5) and of v_p */
+    const int ai = Ai[k], aj = Aj[k], bi = Ii[k], bj = Ij[k];
+    for (int c = 0; c < 4; ++c) vi[c] = U(o->u, c, ai, aj);
+    vi[4] = U(o->u, 4, bi, bj);
+    const double pres_v_i = ex7_psweep(o, vi, 0);
+    if (pres_v_i <= eps || vi[0] <= eps) {
+      const int kn = k + dk;            /* v_p's components 1-4 */
+      const int k5 = ord ? k - 1 : kn;  /* v_p's component 5 */
+      if (k5 < 0) return SWFD_ERR_UNSUPPORTED; /* the reference reads sweepI(0) */
+      const int ci = Ai[kn], cj = Aj[kn], di = Ii[k5], dj = Ij[k5];
+      for (int c = 0; c < 4; ++c) vp[c] = U(o->u, c, ci, cj);
+      vp[4] = U(o->u, 4, di, dj);
+      ex7_nod_lim(o, vi, vp, ubar, vit);
+      for (int c = 0; c < 5; ++c) d[c] = vi[c] - vit[c];
+      for (int c = 0; c < 5; ++c) vpt[c] = vp[c] + (w / w) * (d[c]);
+      for (int c = 0; c < 4; ++c) U(o->u, c, ai, aj) = vit[c];
+      U(o->u, 4, bi, bj) = vit[4];
+      for (int c = 0; c < 4; ++c) U(o->u, c, ci, cj) = vpt[c];
+      U(o->u, 4, di, dj) = vpt[4];
+      if (ord == 0) {
+        const double pres_v_p = ex7_psweep(o, vp, 0);
+        const double pres_v_i_t = ex7_psweep(o, vit, 1);
+        const double pres_v_p_t = ex7_psweep(o, vpt, 1);
+        if (pres_v_i + pres_v_p > pres_v_i_t + pres_v_p_t + eps) return SWFD_ERR_SWEEP_CHECK;
+      }
+    }
+  }
+  return SWFD_OK;
+}
+
+/* sweep_lim (:1433-1737) on the gathered interior: the density sweep, u_bar
+ * (sequential, j outer), the P(u_bar) stop, alternating I/II pass pairs and
+ * the exit test on g1*(E - 0.5*(m_x^2+m_y^2)/rho) and rho (no q*Y term) */
+static int ex7_sweep_lim(oracle* o) {
+  const int nx = o->nx, ny = o->ny;
+  scalar_sweep2d(o);
+  double ra = 0.0, m1a = 0.0, m2a = 0.0, ea = 0.0, ya = 0.0;
+  const double w = o->weight;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      ra = ra + w * U(o->u, 0, i, j);
+      m1a = m1a + w * U(o->u, 1, i, j);
+      m2a = m2a + w * U(o->u, 2, i, j);
+      ea = ea + w * U(o->u, 3, i, j);
+      ya = ya + w * U(o->u, 4, i, j);
+    }
+  const double ubar[5] = {ra, m1a, m2a, ea, ya};
+  if (o->gamma1 * (ea - 0.5 * (m1a * m1a) / ra - 0.5 * (m2a * m2a) / ra - o->qc * ya) <= 0.)
+    return SWFD_ERR_PUBAR_NONPOS;
+  o->sweep_count++;
+  track_push(o);
+  o->t_pos_count = 0;
+  o->t_neg_count = 0;
+  for (int q = 1; q <= o->cfg.swp_num; ++q) {
+    const int ord = (q % 2 == 1) ? 0 : 1;
+    int st = ex7_pass(o, ord, 1, ubar);
+    if (st == SWFD_OK) st = ex7_pass(o, ord, 0, ubar);
+    if (st != SWFD_OK) return st;
+    double rho_min = 1e20, p_min = 1e20;
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const double u1 = U(o->u, 0, i, j), u2 = U(o->u, 1, i, j), u3 = U(o->u, 2, i, j),
+                     u4 = U(o->u, 3, i, j);
+        p_min = fmin(o->gamma1 * (u4 - 0.5 * (u2 * u2 + u3 * u3) / u1), p_min);
+        rho_min = fmin(u1, rho_min);
+      }
+    o->pre_count++;
+    if (p_min > o->eps && rho_min > o->eps) {
+      o->sweep_track[o->sweep_count - 1] = q;
+      o->neg_track[o->sweep_count - 1] = (int32_t)o->t_neg_count;
+      o->pos_track[o->sweep_count - 1] = (int32_t)o->t_pos_count;
+      break;
+    }
+    if (q == o->cfg.swp_num) {
+      o->fail_count++;
+      return SWFD_ERR_SWEEP_NOCONV;
+    }
+  }
+  return SWFD_OK;
+}
+
+/* wenofd + scheme on every rank; returns the global alphamax */
+static double ex7_flux_divergence(oracle* o) {
+  double am = 0.;
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) am = fmax(am, ex7_findalpha(o->rk[k]));
+  for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
+    ex7_wenofd(o->rk[k]);
+    ex7_scheme(o->rk[k]);
+  }
+  return am;
+}
+
+/* rk (:810-888): dt = min(dx*cfl/alphamax, dy*cfl/alphamax, T - time) */
+static int ex7_step(oracle* o) {
+  if (o->ranks_stale) ex6_distribute(o);
+  const int n = o->cut_x * o->cut_y;
+  for (int stage = 1; stage <= 3; ++stage) {
+    const double am = ex7_flux_divergence(o);
+    o->alphamax = am;
+    if (stage == 1) {
+      const double dtx = o->dx * o->cfg.cfl / am, dty = o->dy * o->cfg.cfl / am;
+      o->dt = fmin(fmin(dtx, dty), o->cfg.time_terminal - o->time);
+      for (int k = 0; k < n; ++k)
+        memcpy(o->rk[k]->u0, o->rk[k]->u, state_len(o->rk[k]) * sizeof(double));
+    }
+    const double dt = o->dt;
+    for (int k = 0; k < n; ++k) {
+      oracle* r = o->rk[k];
+      const size_t len = state_len(r);
+      for (size_t m = 0; m < len; ++m) {
+        const double v = r->u[m] + dt * r->rhs[m];
+        if (stage == 1) r->u[m] = v;
+        else if (stage == 2) r->u[m] = rk2(o, r->u0[m], v);
+        else r->u[m] = rk3(o, r->u0[m], v);
+      }
+    }
+    o->postag = ex7_checkpositivity(o);
+    ex6_gather(o);
+    if (o->cfg.use_limiter == 2 && o->postag == 1) {
+      const int st = ex7_sweep_lim(o);
+      o->postag = 0;
+      if (st != SWFD_OK) {
+        ex6_assemble(o);
+        return o->status = st;
+      }
+    }
+    ex6_scatter(o);
+    ex7_bc(o);
+  }
+  o->time = o->time + o->dt;
+  ex6_assemble(o);
+  return SWFD_OK;
+}
+
 /* rk / rk3 (ex3_vortex_accuracy_2d/main.f90:564-632; ex2_sedov_1d/main.f90:287-328) */
 /* The dt-halving restart RK of ex2 (RK_choice /= 1, ex2_sedov_1d/main.f90:
  * 330-374).  A stage whose result fails checkpositivity sends the step back to
@@ -1853,6 +2426,7 @@ static int step_restart1d(oracle* o) {
 
 int oracle_step(oracle* o) {
   if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) return ex6_step(o);
+  if (o->problem == SWFD_PROBLEM_DETONATION) return ex7_step(o);
   if (o->problem == SWFD_PROBLEM_MATLAB_1D) return ex1_step(o);
   if (o->cfg.rk_choice == 2) return step_restart1d(o);
   const size_t n = state_len(o);
@@ -1978,6 +2552,9 @@ void oracle_init(oracle* o) {
     case SWFD_PROBLEM_SHOCK_DIFFRACTION:
       ex6_init(o);
       break;
+    case SWFD_PROBLEM_DETONATION:
+      ex7_init(o);
+      break;
     case SWFD_PROBLEM_JET_2D: { /* ex5_mach2000_jet/main.f90:744-768 */
       double xleft = 0., xright = 1., yleft = 0., yright = 0.25;
       o->dx = (xright - xleft) / nx;
@@ -2016,7 +2593,16 @@ oracle* oracle_create(const swfd_config* cfg) {
   o->weno_eps = 1e-6;
   o->weno_eps_q = 1e-6f128;
   o->ex4like = (cfg->problem == SWFD_PROBLEM_SEDOV_2D || cfg->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION);
-  if (cfg->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (cfg->problem == SWFD_PROBLEM_DETONATION) {
+    /* u(5,...), q_const = 50, t_const = 50, k_const = 2566.4, step = 2
+     * (ex7_detonation/main.f90:11-19); ex6's WENO epsilon (weno5.f90:104-106) */
+    o->nc = 5;
+    o->qc = 50.;
+    o->tc = 50.;
+    o->kc = 2566.4;
+    o->wall_rows = 2 * cfg->total;
+  }
+  if (cfg->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION || cfg->problem == SWFD_PROBLEM_DETONATION) {
     /* alpha(k)=lin(k)/(1d-12+beta(k))**2 (ex6_shock_diffraction/weno5.f90:104-106,138-140) */
     o->weno_eps = 1e-12;
     o->weno_eps_q = 1e-12f128;
@@ -2047,7 +2633,20 @@ oracle* oracle_create(const swfd_config* cfg) {
     sweeping_order(o);
     /* weights(i,j) = 1./(nSteps_x*nSteps_y) (ex3_vortex_accuracy_2d/main.f90:44) */
     o->weight = 1. / ((double)o->nx * (double)o->ny);
-    if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+    if (o->problem == SWFD_PROBLEM_DETONATION) {
+      /* xleft = 5./cut_x*position_x, dx = (xright - xleft)/nx per rank
+       * (ex7_detonation/main.f90:1224-1231); rank (0,0)'s for the time step */
+      o->dx = (5. / o->cut_x * (0 + 1) - 5. / o->cut_x * 0) / o->nxl;
+      o->dy = (5. / o->cut_y * (0 + 1) - 5. / o->cut_y * 0) / o->nyl;
+      o->rk = calloc((size_t)o->cut_x * o->cut_y, sizeof(oracle*));
+      for (int py = 0; py < o->cut_y; ++py)
+        for (int px = 0; px < o->cut_x; ++px) {
+          oracle* r = ex6_rank_create(o, px, py);
+          r->dx = (5. / o->cut_x * (px + 1) - 5. / o->cut_x * px) / o->nxl;
+          r->dy = (5. / o->cut_y * (py + 1) - 5. / o->cut_y * py) / o->nyl;
+          o->rk[px + o->cut_x * py] = r;
+        }
+    } else if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
       /* xlen = xright - xleft, dx = xlen/nx per rank (:1097-1104); rank (0,0)'s
        * for the time step, every rank's own for its flux differences */
       o->dx = (13. / o->cut_x * (0 + 1) - 13. / o->cut_x * 0) / o->nxl;
@@ -2087,7 +2686,7 @@ int64_t oracle_state_len(const oracle* o) { return (int64_t)state_len(o); }
 void oracle_get_state(const oracle* o, double* out) { memcpy(out, o->u, state_len(o) * sizeof(double)); }
 void oracle_set_state(oracle* o, const double* in) {
   memcpy(o->u, in, state_len(o) * sizeof(double));
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) o->ranks_stale = 1;
+  if (o->rk) o->ranks_stale = 1;
 }
 double oracle_get_time(const oracle* o) { return o->time; }
 void oracle_set_time(oracle* o, double t) { o->time = t; }
@@ -2100,10 +2699,12 @@ int oracle_get_status(const oracle* o) { return o->status; }
 
 /* findalpha of the current state */
 double oracle_find_alpha(oracle* o) {
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (o->rk) {
     if (o->ranks_stale) ex6_distribute(o);
     double am = 0.;
-    for (int k = 0; k < o->cut_x * o->cut_y; ++k) am = fmax(am, ex6_findalpha(o->rk[k]));
+    for (int k = 0; k < o->cut_x * o->cut_y; ++k)
+      am = fmax(am, o->problem == SWFD_PROBLEM_DETONATION ? ex7_findalpha(o->rk[k])
+                                                          : ex6_findalpha(o->rk[k]));
     return o->alphamax = am;
   }
   if (o->ndim == 1) findalpha1d(o); else findalpha2d(o);
@@ -2112,15 +2713,16 @@ double oracle_find_alpha(oracle* o) {
 
 /* wenofd + scheme of the current state; rhs in the state layout */
 void oracle_flux_divergence(oracle* o, double* rhs) {
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (o->rk) {
     if (o->ranks_stale) ex6_distribute(o);
-    o->alphamax = ex6_flux_divergence(o);
+    o->alphamax = o->problem == SWFD_PROBLEM_DETONATION ? ex7_flux_divergence(o)
+                                                        : ex6_flux_divergence(o);
     memset(rhs, 0, state_len(o) * sizeof(double));
     for (int k = 0; k < o->cut_x * o->cut_y; ++k) {
       const oracle* r = o->rk[k];
       for (int j = 1; j <= r->ny; ++j)
         for (int i = 1; i <= r->nx; ++i)
-          for (int c = 0; c < 4; ++c)
+          for (int c = 0; c < o->nc; ++c)
             rhs[IX(o, c, r->px * o->nxl + i, r->py * o->nyl + j)] = r->rhs[IX(r, c, i, j)];
     }
     ex6_assemble(o); /* the wall mirrors change the state, as in the reference */
@@ -2132,19 +2734,20 @@ void oracle_flux_divergence(oracle* o, double* rhs) {
 }
 
 int oracle_check_positivity(oracle* o) {
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (o->rk) {
     if (o->ranks_stale) ex6_distribute(o);
-    return ex6_checkpositivity(o);
+    return o->problem == SWFD_PROBLEM_DETONATION ? ex7_checkpositivity(o)
+                                                 : ex6_checkpositivity(o);
   }
   return check_any(o);
 }
 
 /* sweep_lim on the current state */
 int oracle_sweep(oracle* o) {
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (o->rk) {
     if (o->ranks_stale) ex6_distribute(o);
     ex6_gather(o);
-    int st = sweep_lim2d(o);
+    int st = o->problem == SWFD_PROBLEM_DETONATION ? ex7_sweep_lim(o) : sweep_lim2d(o);
     ex6_scatter(o);
     return st;
   }
@@ -2153,9 +2756,10 @@ int oracle_sweep(oracle* o) {
 
 /* bc on the current state */
 void oracle_bc(oracle* o) {
-  if (o->problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
+  if (o->rk) {
     if (o->ranks_stale) ex6_distribute(o);
-    ex6_bc(o);
+    if (o->problem == SWFD_PROBLEM_DETONATION) ex7_bc(o);
+    else ex6_bc(o);
     ex6_assemble(o);
     return;
   }

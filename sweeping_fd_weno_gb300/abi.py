@@ -35,6 +35,7 @@ VORTEX_2D = 3  # ex3_vortex_accuracy_2d
 SEDOV_2D = 4   # ex4_sedov_2d
 JET_2D = 5     # ex5_mach2000_jet
 SHOCK_DIFFRACTION = 6  # ex6_shock_diffraction
+DETONATION = 7  # ex7_detonation: five components (rho, m_x, m_y, E, rho*Y)
 
 LITERALS_DOUBLE = 0
 LITERALS_QUAD = 1

@@ -32,6 +32,9 @@ def reference_defaults(problem: int) -> dict:
         base.update(nx=800, ny=200, cfl=1.0 / 4.0, time_terminal=0.001, gamma=5.0 / 3.0)
     elif problem == abi.SHOCK_DIFFRACTION:  # ex6_shock_diffraction/main.f90:16-20,695
         base.update(shock_grid(80), cfl=0.9, time_terminal=2.3)
+    elif problem == abi.DETONATION:  # ex7_detonation/main.f90:11-19,43,812
+        base.update(detonation_grid(80), cfl=0.88, time_terminal=0.6, gamma=1.2,
+                    swp_num=20000)
     else:
         raise ValueError(f"unknown problem {problem}")
     return base
@@ -64,11 +67,22 @@ def shock_grid(total: int, cut_x: int = 4, cut_y: int = 8) -> dict:
                 ny=cut_y * (11 * total // cut_y))
 
 
+def detonation_grid(total: int, cut_x: int = 4, cut_y: int = 8) -> dict:
+    """Grid of the detonation example: nx = cut_x*(5*total/cut_x),
+    ny = cut_y*(5*total/cut_y) in integer arithmetic
+    (ex7_detonation/main.f90:11-13)."""
+    return dict(total=total, cut_x=cut_x, cut_y=cut_y, nx=cut_x * (5 * total // cut_x),
+                ny=cut_y * (5 * total // cut_y))
+
+
 def make_config(problem: int, **overrides) -> abi.SwfdConfig:
     d = reference_defaults(problem)
     if problem == abi.SHOCK_DIFFRACTION and "total" in overrides:
         d.update(shock_grid(overrides["total"], overrides.get("cut_x", 4),
                             overrides.get("cut_y", 8)))
+    if problem == abi.DETONATION and "total" in overrides:
+        d.update(detonation_grid(overrides["total"], overrides.get("cut_x", 4),
+                                 overrides.get("cut_y", 8)))
     unknown = set(overrides) - set(d) - {"reserved"}
     if unknown:
         raise KeyError(f"unknown config fields {sorted(unknown)}")
@@ -97,6 +111,11 @@ def workload(name: str, **overrides) -> abi.SwfdConfig:
         # Mach 5.09 shock diffraction around a step; name 'shock<total>'
         # (total 20..80: 260x216 .. 1040x880 cells)
         return make_config(abi.SHOCK_DIFFRACTION, total=int(name[len("shock"):] or 80),
+                           **overrides)
+    if name.startswith("detonation"):
+        # reactive Euler detonation past a step; name 'detonation<total>'
+        # (total 80: 400x400 cells on 4 x 8 ranks)
+        return make_config(abi.DETONATION, total=int(name[len("detonation"):] or 80),
                            **overrides)
     if name.startswith("sedov2d"):
         n = int(name[len("sedov2d"):] or 640)
