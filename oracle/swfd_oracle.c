@@ -1827,8 +1827,10 @@ static void ex6_init(oracle* o) {
  * with k the nearest integer to x*(1/ln2) (binary64), r = x - k*ln2 in
  * binary128, exp(r) by Horner on the Taylor coefficients 1/n! (n <= 24, each
  * the binary128 quotient of the previous by n), times 2^k exactly.  The
- * library evaluates the same sequence of binary128 operations, so the two
- * agree bit for bit. */
+ * library evaluates the same sequence of binary128 operations (qd::exp_rd),
+ * so the two agree bit for bit.  The result is the correctly rounded exp
+ * wherever the binary128 evaluation decides the rounding; the host libm's
+ * exp differs from it by one ulp on a small fraction of arguments. */
 #define EXP7_N 24
 static Q exp7_coef[EXP7_N + 1];
 static int exp7_ready;
@@ -1842,7 +1844,8 @@ double oracle_exp(double x) {
     exp7_ready = 1;
   }
   const double kd = rint(x * 1.4426950408889634);
-  const Q ln2 = 0.693147180559945309417232121458176568f128;
+  /* ln2 as the binary128 sum of a triple-double split (113 bits) */
+  const Q ln2 = ((Q)0x1.62e42fefa39efp-1 + (Q)0x1.abc9e3b39803fp-56) + (Q)0x1.7b57a079a1934p-111;
   const Q r = (Q)x - (Q)kd * ln2;
   Q p = exp7_coef[EXP7_N];
   for (int n = EXP7_N - 1; n >= 0; --n) p = p * r + exp7_coef[n];

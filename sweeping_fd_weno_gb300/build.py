@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 BUILD = PKG / "_build"
 SOURCES = ["swfd_api.cu", "swfd_kernels.cu", "swfd_sweep.cu", "swfd_control.cu", "swfd_probe.cu",
-           "swfd_static.cu", "swfd_batch.cu", "swfd_matlab1d.cu"]
+           "swfd_static.cu", "swfd_batch.cu", "swfd_matlab1d.cu", "swfd_ex7.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",

@@ -12,6 +12,7 @@
 #include "swfd_control.h"
 #include "swfd_graph.h"
 #include "swfd_internal.h"
+#include "swfd_ex7.h"
 
 using namespace swfd;
 
@@ -67,6 +68,7 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
   }
   if (c.rk_choice == 2 && c.problem != SWFD_PROBLEM_SEDOV_1D)
     return bad(SWFD_ERR_INVALID, "rk_choice 2 (the dt-halving restart RK) exists only in ex2");
+  if (c.problem == SWFD_PROBLEM_DETONATION) return ex7_check(c, err);
   if (c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION) {
     // ex6_shock_diffraction/main.f90:16-18: nx = 13*total/cut_x per rank,
     // ny = 11*total/cut_y per rank
@@ -890,6 +892,16 @@ swfd_status swfd_config_default(swfd_config* cfg, int32_t problem) {
       cfg->cfl = 0.9;
       cfg->time_terminal = 2.3;
       break;
+    case SWFD_PROBLEM_DETONATION:  // ex7_detonation/main.f90:11-19,43,812
+      cfg->total = 80;
+      cfg->cut_x = 4;
+      cfg->cut_y = 8;
+      cfg->nx = 4 * (5 * 80 / 4);
+      cfg->ny = 8 * (5 * 80 / 8);
+      cfg->cfl = 0.88;
+      cfg->time_terminal = 0.6;
+      cfg->gamma = 1.2;
+      break;
     default:
       return fail(nullptr, SWFD_ERR_INVALID, "unknown problem");
   }
@@ -902,6 +914,24 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   std::string err;
   swfd_status st = check_config(*cfg, err);
   if (st != SWFD_OK) return fail(nullptr, st, err);
+  if (cfg->problem == SWFD_PROBLEM_DETONATION) {  // its own rank-sliced engine
+    swfd_handle* h = new swfd_handle();
+    h->cfg = *cfg;
+    h->device = cfg->device;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      swfd_destroy(h);
+      return fail(nullptr, SWFD_ERR_CUDA, std::string("swfd_create: ") + cudaGetErrorString(e));
+    }
+    st = ex7_create(h, err);
+    if (st != SWFD_OK) {
+      swfd_destroy(h);
+      return fail(nullptr, st, err);
+    }
+    *out = h;
+    return SWFD_OK;
+  }
   swfd_handle* h = new swfd_handle();
   h->cfg = *cfg;
   st = make_params(*cfg, h->p, err);
@@ -979,6 +1009,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   if (!h) return SWFD_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  ex7_destroy(h->ex7);
   for (int k = 0; k < 3; ++k) cudaFree(h->st[k]);
   cudaFree(h->split);
   cudaFree(h->roe);
@@ -1006,6 +1037,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
 swfd_status swfd_upload_state(swfd_handle* h, const double* u) {
   if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7) return ex7_upload(h, u);
   CU(h, cudaSetDevice(h->device));
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   CU(h, cudaMemcpyAsync(h->d_stage, u, hb, cudaMemcpyHostToDevice, h->stream));
@@ -1017,6 +1049,7 @@ swfd_status swfd_upload_state(swfd_handle* h, const double* u) {
 swfd_status swfd_download_state(swfd_handle* h, double* u) {
   if (!h || !u) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7) return ex7_download(h, u);
   CU(h, cudaSetDevice(h->device));
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   CU(h, launch_soa_to_fortran(h->p, cur_state(h), h->d_stage, h->stream));
@@ -1028,6 +1061,7 @@ swfd_status swfd_download_state(swfd_handle* h, double* u) {
 swfd_status swfd_init_problem(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7) return ex7_init(h);
   std::vector<double> u((size_t)host_len(h->p));
   init_host(h, u.data());
   ST(swfd_upload_state(h, u.data()));
@@ -1049,6 +1083,7 @@ swfd_status swfd_get_time(swfd_handle* h, double* t) {
 swfd_status swfd_set_time(swfd_handle* h, double t) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7) return ex7_set_time(h, t);
   CU(h, cudaSetDevice(h->device));
   h->time = t;
   CU(h, cudaMemcpyAsync(&h->dsc->time, &h->time, sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1075,6 +1110,7 @@ swfd_status matlab1d_steps(swfd_handle* h, long long max_steps, int64_t* steps_o
 swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7) return ex7_step(h, dt_out);
   CU(h, cudaSetDevice(h->device));
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
     swfd_status st = matlab1d_steps(h, 1, nullptr);
@@ -1101,7 +1137,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
 
 swfd_status swfd_step_async(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
-  if (h->eager || h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
+  if (h->eager || h->cfg.problem == SWFD_PROBLEM_MATLAB_1D || h->ex7)
     return swfd_step(h, nullptr);  // eager sections read conditions on the host
   CU(h, cudaSetDevice(h->device));
   ST(build_graph(h, GRAPH_STEP, &h->g_step));
@@ -1119,6 +1155,10 @@ swfd_status swfd_step_async(swfd_handle* h) {
 
 swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
   if (!h || !flux_min_blocks) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  if (h->ex7) {  // one launch shape
+    *flux_min_blocks = 0;
+    return SWFD_OK;
+  }
   SETTLE(h);
   CU(h, cudaSetDevice(h->device));
   *flux_min_blocks = 0;
@@ -1175,6 +1215,21 @@ swfd_status swfd_finish(swfd_handle* h) {
 swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7) {  // DO WHILE (time <= time_terminal - 1d-10) (ex7_detonation/main.f90:97)
+    int64_t done = 0;
+    swfd_status st = SWFD_OK;
+    while (h->time <= h->cfg.time_terminal - 1e-10) {
+      if (max_steps > 0 && done >= max_steps) {
+        st = SWFD_ERR_MAX_STEPS;
+        break;
+      }
+      st = ex7_step(h, nullptr);
+      ++done;
+      if (st != SWFD_OK) break;
+    }
+    if (nsteps_out) *nsteps_out = done;
+    return st;
+  }
   CU(h, cudaSetDevice(h->device));
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
     // while t < tFinal (FD_WENO_Application.m:212), tested on the device
@@ -1232,6 +1287,8 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
 swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
   if (!h || !rhs) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the detonation runs whole steps, find_alpha and state I/O");
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
     return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
@@ -1252,6 +1309,8 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs) {
 swfd_status swfd_sweep(swfd_handle* h) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the detonation runs whole steps, find_alpha and state I/O");
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
     return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
@@ -1267,6 +1326,8 @@ swfd_status swfd_sweep(swfd_handle* h) {
 swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
   if (!h || !postag) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7)
+    return fail(h, SWFD_ERR_UNSUPPORTED, "the detonation runs whole steps, find_alpha and state I/O");
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
     return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
@@ -1279,6 +1340,7 @@ swfd_status swfd_check_positivity(swfd_handle* h, int32_t* postag) {
 swfd_status swfd_find_alpha(swfd_handle* h, double* alphamax) {
   if (!h || !alphamax) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7) return ex7_find_alpha(h, alphamax);
   if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D)
     return fail(h, SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs whole steps only");
   CU(h, cudaSetDevice(h->device));
@@ -1303,6 +1365,10 @@ swfd_status fetch_tracks(swfd_handle* h, std::vector<int32_t>& tr, int64_t& n) {
 swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts) {
   if (!h || !restarts) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7) {
+    *restarts = 0;
+    return SWFD_OK;
+  }
   CU(h, cudaSetDevice(h->device));
   ST(sync_scalars(h));
   *restarts = h->hsc->restart_total;
@@ -1312,6 +1378,7 @@ swfd_status swfd_get_restarts(swfd_handle* h, int64_t* restarts) {
 swfd_status swfd_get_sweep_stats(swfd_handle* h, swfd_sweep_stats* s) {
   if (!h || !s) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
+  if (h->ex7) return ex7_stats(h, s);
   CU(h, cudaSetDevice(h->device));
   std::vector<int32_t> tr;
   int64_t n = 0;
@@ -1337,6 +1404,11 @@ swfd_status swfd_get_sweep_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, 
                                   int64_t cap, int64_t* count) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
+  if (h->ex7) {
+    const int64_t n = ex7_tracks(h, sweep, neg, pos, std::max<int64_t>(cap, 0));
+    if (count) *count = n;
+    return SWFD_OK;
+  }
   CU(h, cudaSetDevice(h->device));
   std::vector<int32_t> tr;
   int64_t n = 0;
@@ -1432,6 +1504,7 @@ swfd_status swfd_get_profile(swfd_handle* h, swfd_profile* prof) {
   if (!h || !prof) return fail(h, SWFD_ERR_INVALID, "NULL argument");
   SETTLE(h);
   *prof = h->prof;
+  if (h->ex7) prof->kernel_launches = ex7_launches(h);
   return SWFD_OK;
 }
 

@@ -319,6 +319,8 @@ swfd_status swfd_batch_admit(swfd_batch* b, const swfd_config* cfg, int64_t requ
     return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine runs the binary64 literals");
   if (c.problem == SWFD_PROBLEM_SEDOV_1D || c.problem == SWFD_PROBLEM_MATLAB_1D)
     return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine holds 2D problems");
+  if (c.problem == SWFD_PROBLEM_DETONATION)
+    return bfail(b, SWFD_ERR_UNSUPPORTED, "the batched engine holds the four-component problems");
   if (c.use_limiter == 1)
     return bfail(b, SWFD_ERR_UNSUPPORTED,
                  "the batched engine runs the sweeping form (use_limiter 0 or 2)");

@@ -229,6 +229,10 @@ struct BatchLaunch {
 
 }  // namespace swfd
 
+namespace swfd {
+struct Ex7;  // the detonation engine (swfd_ex7.h)
+}
+
 struct swfd_handle {
   swfd_config cfg;
   swfd::Params p;
@@ -277,6 +281,8 @@ struct swfd_handle {
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles
+  // the detonation (ex7) keeps its own rank-sliced state; set only for that problem
+  swfd::Ex7* ex7 = nullptr;
 };
 
 namespace swfd {

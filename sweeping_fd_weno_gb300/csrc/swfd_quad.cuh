@@ -378,5 +378,35 @@ SWFD_QD double ru(const q128& a) {
   return nextafter(d, 1.0 / 0.0);
 }
 
+// ---- exp for the detonation's chemistry source -----------------------------
+// exp(x) evaluated in binary128 and rounded once to binary64: x = k*ln2 + r,
+// k the nearest integer to x*(1/ln2) in binary64, r = x - k*ln2 in binary128
+// (ln2 the binary128 sum of a triple-double split, 113 bits), exp(r) by Horner
+// on the Taylor coefficients 1/n!, n <= EXP_N (each the binary128 quotient of
+// the previous by n; exp_coefs), times 2^k exactly.  The truncation and the
+// roundings stay near 2^-105 relative, so the binary64 result is the
+// correctly rounded exp except where exp(x) lies within that of a rounding
+// boundary.
+constexpr int EXP_N = 24;
+SWFD_QD q128 ln2_q() {
+  return add(add(from_double(0x1.62e42fefa39efp-1), from_double(0x1.abc9e3b39803fp-56)),
+             from_double(0x1.7b57a079a1934p-111));
+}
+SWFD_QD_CALL void exp_coefs(q128* c) {
+  c[0] = from_double(1.0);
+  for (int n = 1; n <= EXP_N; ++n) c[n] = div(c[n - 1], from_double((double)n));
+}
+SWFD_QD_CALL double exp_rd(double x, const q128* c) {
+  if (x != x) return x;
+  if (x > 710.) return INFINITY;
+  if (x < -746.) return 0.;
+  const double kd = rint(x * 1.4426950408889634);
+  const q128 r = sub(from_double(x), mul(from_double(kd), ln2_q()));
+  q128 p = c[EXP_N];
+#pragma unroll 1
+  for (int n = EXP_N - 1; n >= 0; --n) p = add(mul(p, r), c[n]);
+  return to_double(scale2(p, (int)kd));
+}
+
 }  // namespace qd
 }  // namespace swfd

@@ -70,6 +70,8 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
   std::string err;
   swfd_status st = check_config(*cfg, err);
   if (st != SWFD_OK) return static_fail(st, err);
+  if (cfg->problem == SWFD_PROBLEM_DETONATION)
+    return static_fail(SWFD_ERR_UNSUPPORTED, "the detonation needs per-rank buffers: use swfd_step");
   Params p;
   st = make_params(*cfg, p, err);
   if (st != SWFD_OK) return static_fail(st, err);

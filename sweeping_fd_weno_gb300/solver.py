@@ -30,10 +30,10 @@ class Solver:
         abi.check(self.lib.swfd_create(C.byref(cfg), C.byref(h)))
         self.h = h
         self.ndim = 1 if cfg.problem in (abi.SEDOV_1D, abi.MATLAB_1D) else 2
-        self.nc = 3 if self.ndim == 1 else 4
+        self.nc = 3 if self.ndim == 1 else (5 if cfg.problem == abi.DETONATION else 4)
         self.nx = cfg.nx
         self.ny = 1 if self.ndim == 1 else cfg.ny
-        self.shape = (1, self.nx + 6, 3) if self.ndim == 1 else (self.ny + 6, self.nx + 6, 4)
+        self.shape = (1, self.nx + 6, 3) if self.ndim == 1 else (self.ny + 6, self.nx + 6, self.nc)
 
     # -- lifetime -----------------------------------------------------------
     def close(self):
@@ -190,6 +190,8 @@ class Solver:
             return 1.3 / self.nx
         if p == abi.SHOCK_DIFFRACTION:  # (13/cut_x - 0)/nxl, the same for every rank
             return (13.0 / self.cfg.cut_x) / (self.nx // self.cfg.cut_x)
+        if p == abi.DETONATION:  # (5/cut_x - 0)/nxl
+            return (5.0 / self.cfg.cut_x) / (self.nx // self.cfg.cut_x)
         return 1.0 / self.nx
 
     def _dy(self):
@@ -200,6 +202,8 @@ class Solver:
             return 1.3 / self.ny
         if p == abi.SHOCK_DIFFRACTION:
             return (11.0 / self.cfg.cut_y) / (self.ny // self.cfg.cut_y)
+        if p == abi.DETONATION:
+            return (5.0 / self.cfg.cut_y) / (self.ny // self.cfg.cut_y)
         return 0.25 / self.ny
 
 

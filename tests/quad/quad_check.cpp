@@ -52,8 +52,9 @@ static bool same_d(double a, double b) {
 
 int main(int argc, char** argv) {
   const long n = argc > 1 ? atol(argv[1]) : 200000;
-  long bad[9] = {0};
-  const char* names[9] = {"from/to", "add", "sub", "mul", "div", "chain", "to_double", "neg0", "div113"};
+  long bad[11] = {0};
+  const char* names[11] = {"from/to", "add", "sub", "mul", "div", "chain", "to_double", "neg0", "div113",
+                           "ln2", "exp"};
   for (long i = 0; i < n; ++i) {
     const int mode = i & 1;
     double x = rdouble(mode), y = rdouble(mode);
@@ -98,8 +99,33 @@ int main(int argc, char** argv) {
   }
   if (!same_d(to_double(add(from_double(-0.0), from_double(-0.0))), -0.0)) bad[7]++;
   if (!same_d(to_double(add(from_double(1.5), from_double(-1.5))), 0.0)) bad[7]++;
+  // exp_rd against the same algorithm in _Float128 (the oracle's oracle_exp)
+  {
+    const F ln2f = ((F)0x1.62e42fefa39efp-1 + (F)0x1.abc9e3b39803fp-56) + (F)0x1.7b57a079a1934p-111;
+    if (!same(toF(ln2_q()), ln2f) || !same(ln2f, (F)0.693147180559945309417232121458176568f128))
+      bad[9]++;
+    q128 qc[EXP_N + 1];
+    F fc[EXP_N + 1];
+    exp_coefs(qc);
+    fc[0] = 1;
+    for (int k = 1; k <= EXP_N; ++k) fc[k] = fc[k - 1] / (F)k;
+    for (int k = 0; k <= EXP_N; ++k)
+      if (!same(toF(qc[k]), fc[k])) bad[10]++;
+    for (long i = 0; i < n / 2; ++i) {
+      const double x = (i % 3 == 0) ? -746. * (double)(rnd() >> 11) / 9007199254740992.0
+                                    : ((double)(rnd() >> 11) / 9007199254740992.0 - 0.5) * 200.;
+      const double kd = rint(x * 1.4426950408889634);
+      const F r = (F)x - (F)kd * ln2f;
+      F p = fc[EXP_N];
+      for (int k = EXP_N - 1; k >= 0; --k) p = p * r + fc[k];
+      uint64_t bits[2] = {0, (uint64_t)((int)kd + 16383) << 48};
+      F two_k;
+      memcpy(&two_k, bits, sizeof(two_k));
+      if (!same_d(exp_rd(x, qc), (double)(p * two_k))) bad[10]++;
+    }
+  }
   long total = 0;
-  for (int k = 0; k < 9; ++k) {
+  for (int k = 0; k < 11; ++k) {
     printf("%s %ld\n", names[k], bad[k]);
     total += bad[k];
   }

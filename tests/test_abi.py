@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol(swfd):
 
 
 @pytest.mark.parametrize("problem", [abi.MATLAB_1D, abi.SEDOV_1D, abi.VORTEX_2D, abi.SEDOV_2D,
-                                     abi.JET_2D, abi.SHOCK_DIFFRACTION])
+                                     abi.JET_2D, abi.SHOCK_DIFFRACTION, abi.DETONATION])
 def test_config_default_matches_reference_parameters(swfd, problem):
     c = abi.config_default(problem).as_dict()
     ref = problems.reference_defaults(problem)
@@ -82,3 +82,22 @@ def test_shock_diffraction_config_checks(swfd):
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
     cfg = problems.workload("shock12", cut_x=3)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
+
+
+def test_detonation_config_checks(swfd):
+    """ex7: grid from total and the rank grid, the wall row inside a rank's
+    local rows, binary64 literals and the sweeping or no limiter."""
+    import ctypes as C
+    from sweeping_fd_weno_gb300 import problems
+    lib = abi.load()
+    h = C.c_void_p()
+    # total 8 on 4 x 8 ranks: the wall row is local row 6 = nyl + 1 of rank row 2
+    cfg = problems.make_config(abi.DETONATION, total=8)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
+    cfg = problems.make_config(abi.DETONATION, total=32)
+    cfg.ny += 8                              # not cut_y*(5*total/cut_y)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
+    for field, value in (("literals", abi.LITERALS_QUAD), ("use_limiter", 1),
+                         ("precision", abi.PRECISION_FP32_BULK)):
+        cfg = problems.make_config(abi.DETONATION, total=32, **{field: value})
+        assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED, field

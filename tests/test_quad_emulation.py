@@ -17,7 +17,7 @@ def test_binary128_matches_float128(tmp_path):
     if not cxx:
         pytest.skip("no g++")
     exe = tmp_path / "quad_check"
-    r = subprocess.run([cxx, "-O2", "-std=gnu++17", "-I", str(CSRC), str(HERE / "quad" / "quad_check.cpp"),
+    r = subprocess.run([cxx, "-O2", "-std=gnu++17", "-ffp-contract=off", "-I", str(CSRC), str(HERE / "quad" / "quad_check.cpp"),
                         "-o", str(exe), "-lm"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe), "300000"], capture_output=True, text=True, timeout=600)
