@@ -1007,12 +1007,8 @@ swfd_status ex7_step(swfd_handle* h, double* dt_out) {
   for (int stage = 1; stage <= 3; ++stage) {
     E7CU(h, cudaMemsetAsync(&v.sc->am_bits, 0, sizeof(unsigned long long), s));
     E7K(h, (k7_alpha<<<e7_grid(cells), E7_BLOCK, 0, s>>>(v)));
-    if (stage == 1) {
-      E7K(h, (k7_dt<<<1, 1, 0, s>>>(v)));
-      E7CU(h, cudaMemcpyAsync(v.u0, v.u, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    } else {
-      E7K(h, (k7_alphamax<<<1, 1, 0, s>>>(v)));
-    }
+    if (stage == 1) E7K(h, (k7_dt<<<1, 1, 0, s>>>(v)));
+    else E7K(h, (k7_alphamax<<<1, 1, 0, s>>>(v)));
     // wenofd: x pass then y pass, each after its wall mirror
     E7K(h, (k7_mirror_x<<<e7_grid((int64_t)v.cut_y * (v.nyl + 2) * 3), E7_BLOCK, 0, s>>>(v)));
     E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LJ * 32), E7_BLOCK, 0, s>>>(v, 0)));
@@ -1022,6 +1018,9 @@ swfd_status ex7_step(swfd_handle* h, double* dt_out) {
     E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LI * 32), E7_BLOCK, 0, s>>>(v, 1)));
     E7K(h, (k7_split<<<e7_grid((int64_t)v.R * (v.nxl + 2) * v.LJ), E7_BLOCK, 0, s>>>(v, 1)));
     E7K(h, (k7_flux<<<e7_grid(faces, 128), 128, 0, s>>>(v, 1)));
+    // u0 = u after wenofd, whose wall mirrors rewrite cells of u (:822)
+    if (stage == 1)
+      E7CU(h, cudaMemcpyAsync(v.u0, v.u, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
     E7CU(h, cudaMemsetAsync(&v.sc->postag, 0, sizeof(int), s));
     E7K(h, (k7_rk<<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
     if (x->use_limiter == 2) {
