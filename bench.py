@@ -407,6 +407,60 @@ def bench_point_energy_1d(args, local):
     return out
 
 
+def bench_detonation(args, local):
+    """The reactive Euler detonation of ex7 at the reference's size (400x400 on
+    its 4 x 8 ranks): GPU steps timed with CUDA events (the host reads the
+    positivity flag after each stage, as the sweep decision needs), and the
+    oracle on one host core for a bounded sample of the same steps, with a
+    value-for-value check of the state after them."""
+    import numpy as np
+    import oracle
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, problems
+    cfg = problems.workload("detonation80", device=local)
+    cells = cfg.nx * cfg.ny
+    s = Solver(cfg)
+    s.init_problem()
+    for _ in range(args.warmup):
+        s.step()
+    s.init_problem()
+    steps = max(args.steps, 10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step()
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    st = s.stats()
+    # the oracle: a bounded sample of the first steps, same result checked
+    sample = max(1, min(steps, args.detonation_sample))
+    g = Solver(cfg)
+    g.init_problem()
+    o = oracle.Oracle(cfg)
+    o.init_problem()
+    t0 = time.perf_counter()
+    for _ in range(sample):
+        o.step()
+    cpu_s = time.perf_counter() - t0
+    for _ in range(sample):
+        g.step()
+    same = bool(np.array_equal(g.state(), o.state()) and g.time == o.time)
+    g.close()
+    s.close()
+    gpu_rate = cells * 3 * steps / gpu_s
+    cpu_rate = cells * 3 * sample / cpu_s
+    return {"workload": "detonation80: ex7 reactive Euler, 400x400 on 4 x 8 ranks, five "
+                        "components, sweeping limiter",
+            "cells": int(cells), "steps": int(steps), "gpu_ms_per_step": gpu_s / steps * 1e3,
+            "value": gpu_rate, "unit": "cell-updates/s",
+            "sweeps": {k: int(v) for k, v in st.items()},
+            "cpu_oracle": {"value": cpu_rate, "cores": 1, "steps": int(sample),
+                           "s": cpu_s, "kind": "port"},
+            "speedup_vs_cpu": gpu_rate / cpu_rate, "same_result_after_sample": same,
+            "timing": "wall clock around the steps with a device synchronize on both sides "
+                      "(each stage reads the positivity flag on the host)"}
+
+
 def bench_serving(args, local):
     """Poisson arrivals (mean 50 req/s) served by continuous batching (an
     FP32-bulk batch and an FP64 batch side by side) and, for comparison, one
@@ -526,6 +580,9 @@ def main():
     ap.add_argument("--no-quad", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-detonation", action="store_true")
+    ap.add_argument("--detonation-sample", type=int, default=2,
+                    help="oracle steps of the detonation leg (about 1.5 s each)")
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--plain-sample", type=int, default=8)
@@ -799,6 +856,8 @@ def main():
         line["batched_to_completion"] = bench_batched_full(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["one_d"] = bench_point_energy_1d(args, local)
+        if not args.no_detonation:
+            line["detonation"] = bench_detonation(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
     if rank == 0:
