@@ -7,7 +7,8 @@
 // nearest, ties to even) -- the same bits as the hardware division -- from
 // integer arithmetic on the significands: the leading quotient bit and five
 // digits of 11 bits, each estimated in binary32 and corrected exactly, then
-// rounded with the remainder as sticky bit.  Operands that are zero,
+// rounded with the remainder as sticky bit (schoolbook division with
+// estimated quotient digits: Knuth, TAOCP vol. 2, 4.3.1, Algorithm D).  Operands that are zero,
 // subnormal, infinite or NaN, and quotients whose exponent is within a
 // binade of the binary64 limits, take the hardware division, so the result
 // equals a / b for every input.  sd::scale<K> (x * 2^K: an addition to the
