@@ -1916,14 +1916,18 @@ static void ex7_interface(const oracle* r, int ydir, const double* L, const doub
                           double* outn) {
   const double g1 = r->gamma1, q = r->qc;
   double evr[5][5], evl[5][5], cu_p[5][5], cu_n[5][5], ur[5], ul[5];
-  double t0 = L[0] / (L[0] + R[0] + 1e-15);
+  /* w/(w+w1+1d-15) and sqrt(..)+1d-15 with the literal in binary128 under
+   * the reference build (:234,240) */
+  double t0 = r->quad ? (double)((Q)L[0] / ((Q)(L[0] + R[0]) + 1e-15f128))
+                      : L[0] / (L[0] + R[0] + 1e-15);
   double t1 = 1. - t0;
   const double vxm = t0 * L[1] + t1 * R[1];
   const double vym = t0 * L[2] + t1 * R[2];
   const double ym = t0 * L[3] + t1 * R[3];
   const double hm = t0 * L[4] + t1 * R[4];
   const double qm = 0.5 * (vxm * vxm + vym * vym);
-  const double cm = sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
+  const double cm = r->quad ? (double)((Q)sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15f128)
+                            : sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
   const double rcm = 1. / cm;
   const double b1 = g1 * rcm * rcm;
   const double b2 = qm * b1;

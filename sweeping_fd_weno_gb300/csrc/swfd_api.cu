@@ -1218,7 +1218,7 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   if (h->ex7) {  // DO WHILE (time <= time_terminal - 1d-10) (ex7_detonation/main.f90:97)
     int64_t done = 0;
     swfd_status st = SWFD_OK;
-    while (h->time <= h->cfg.time_terminal - 1e-10) {
+    while (h->time <= ex7_t_loop(h)) {
       if (max_steps > 0 && done >= max_steps) {
         st = SWFD_ERR_MAX_STEPS;
         break;

@@ -95,8 +95,8 @@ __device__ __forceinline__ void e7_prep(const Ex7View& e, const double* a, doubl
 __device__ __forceinline__ double e7_chem(const Ex7View& e, const double* a) {
   const double rho = a[0], mx = a[1], my = a[2], en = a[3], y = a[4];
   double vx = tdiv(mx, rho), vy = tdiv(my, rho);
-  if (rho < 1e-8) vx = 0.;
-  if (rho < 1e-8) vy = 0.;
+  if (rho < e.lim8_lt) vx = 0.;  // rho < 1d-8
+  if (rho < e.lim8_lt) vy = 0.;
   const double pres = e7_eos(e, rho, vx, vy, en, y);
   return -(e.kc * y * qd::exp_rd(-tdiv(e.tc * rho, pres), e.expc));
 }
@@ -232,14 +232,18 @@ __device__ void e7_interface(const Ex7View& e, int ydir, const double* L, const 
                              const double (*sp)[5], const double (*sn)[5], double* outp,
                              double* outn) {
   const double g1 = e.g1, q = e.q;
-  double t0 = tdiv(L[0], L[0] + Rr[0] + 1e-15);
+  double t0 = e.quad ? qd::to_double(qd::div(qd::from_double(L[0]),
+                                             qd::add(qd::from_double(L[0] + Rr[0]), e.q_1em15)))
+                     : tdiv(L[0], L[0] + Rr[0] + 1e-15);
   double t1 = 1. - t0;
   const double vxm = t0 * L[1] + t1 * Rr[1];
   const double vym = t0 * L[2] + t1 * Rr[2];
   const double ym = t0 * L[3] + t1 * Rr[3];
   const double hm = t0 * L[4] + t1 * Rr[4];
   const double qm = tscale<-1>(vxm * vxm + vym * vym);
-  const double cm = sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
+  const double cm = e.quad ? qd::to_double(qd::add(qd::from_double(sqrt(fabs(g1 * (hm - qm - q * ym)))),
+                                                   e.q_1em15))
+                           : sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
   const double rcm = tdiv(1., cm);
   const double b1 = g1 * rcm * rcm;
   const double b2 = qm * b1;
@@ -296,8 +300,14 @@ __device__ void e7_interface(const Ex7View& e, int ydir, const double* L, const 
       cn[ig] = evl[k][0] * sn[ig][0] + evl[k][1] * sn[ig][1] + evl[k][2] * sn[ig][2] +
                evl[k][3] * sn[ig][3] + evl[k][4] * sn[ig][4];
     }
-    ur[k] = weno_right<double>(cp[0], cp[1], cp[2], cp[3], cp[4], e.weno_eps);
-    ul[k] = weno_left<double>(cn[0], cn[1], cn[2], cn[3], cn[4], e.weno_eps);
+    if (e.quad) {
+      const QuadWeno qw{e.q_c1312, e.q_eps};
+      ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], qw);
+      ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], qw);
+    } else {
+      ur[k] = weno_right<double>(cp[0], cp[1], cp[2], cp[3], cp[4], e.weno_eps);
+      ul[k] = weno_left<double>(cn[0], cn[1], cn[2], cn[3], cn[4], e.weno_eps);
+    }
   }
   for (int k = 0; k < 5; ++k) {
     outp[k] = evr[k][0] * ur[0] + evr[k][1] * ur[1] + evr[k][2] * ur[2] + evr[k][3] * ur[3] +
@@ -362,8 +372,17 @@ __global__ void k7_rk(Ex7View e, int stage) {
       }
       const int64_t o = e7_at(e, r, c, i, j);
       double v = a[c] + dt * rhs;
-      if (stage == 2) v = 0.75 * e.u0[o] + tscale<-2>(v);
-      else if (stage == 3) v = tdiv(e.u0[o] + tscale<1>(v), 3.0);
+      if (e.quad && stage >= 2) {  // 0.75d0*u0 + 0.25d0*(..), (u0 + 2d0*(..))/3d0 in binary128
+        using namespace qd;
+        v = stage == 2 ? to_double(add(mul(from_double(0.75), from_double(e.u0[o])),
+                                       scale2(from_double(v), -2)))
+                       : to_double(div(add(from_double(e.u0[o]), scale2(from_double(v), 1)),
+                                       from_double(3.0)));
+      } else if (stage == 2) {
+        v = 0.75 * e.u0[o] + tscale<-2>(v);
+      } else if (stage == 3) {
+        v = tdiv(e.u0[o] + tscale<1>(v), 3.0);
+      }
       nv[c] = v;
       e.u[o] = v;
     }
@@ -815,9 +834,9 @@ swfd_status ex7_check(const swfd_config& c, std::string& err) {
       return SWFD_ERR_UNSUPPORTED;
     }
   }
-  if (c.literals != SWFD_LITERALS_DOUBLE || c.precision != SWFD_PRECISION_FP64 ||
-      (c.use_limiter != 0 && c.use_limiter != 2) || (c.rk_choice != 0 && c.rk_choice != 1)) {
-    err = "detonation: literals DOUBLE, precision FP64, use_limiter 0 or 2 and rk_choice 1 only";
+  if (c.precision != SWFD_PRECISION_FP64 || (c.use_limiter != 0 && c.use_limiter != 2) ||
+      (c.rk_choice != 0 && c.rk_choice != 1)) {
+    err = "detonation: precision FP64, use_limiter 0 or 2 and rk_choice 1 only";
     return SWFD_ERR_UNSUPPORTED;
   }
   if (c.swp_num <= 0 && c.use_limiter == 2) {
@@ -870,6 +889,18 @@ swfd_status ex7_create(swfd_handle* h, std::string& err) {
   v.q = 50.;
   v.tc = 50.;
   v.kc = 2566.4;
+  v.lim8_lt = 1e-8;
+  x->t_loop = c.time_terminal - 1e-10;
+  if (c.literals == SWFD_LITERALS_QUAD) {  // the constants of the 4-component path
+    using namespace qd;
+    const q128 one = from_double(1.0);
+    v.quad = 1;
+    v.q_c1312 = div(from_double(13.0), from_double(12.0));
+    v.q_eps = div(one, from_double(1e12));
+    v.q_1em15 = div(one, from_double(1e15));
+    v.lim8_lt = ru(div(one, from_double(1e8)));  // rho < 1d-8 <=> rho < ru(1d-8)
+    x->t_loop = rd(sub(from_double(c.time_terminal), div(one, from_double(1e10))));
+  }
   // one device block: 9 rank buffers of 5 planes, alpha, line alphas, the
   // gathered interior, the global view, exp coefficients, scalars, flags
   const int64_t rp = (int64_t)v.R * v.LI * v.LJ, N = (int64_t)v.nx * v.ny;
@@ -1074,5 +1105,6 @@ int64_t ex7_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos, i
 }
 
 int64_t ex7_launches(swfd_handle* h) { return h->ex7->launches; }
+double ex7_t_loop(swfd_handle* h) { return h->ex7->t_loop; }
 
 }  // namespace swfd

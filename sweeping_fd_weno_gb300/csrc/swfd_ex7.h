@@ -37,6 +37,11 @@ struct Ex7View {
   double* ug;     // gathered interior for the sweep: 5 planes of nx*ny, i fastest
   double* gview;  // the global view u(5,-2:nx+3,-2:ny+3) for upload and download
   const qd::q128* expc;  // Taylor coefficients of exp (qd::exp_coefs)
+  // literals QUAD (the reference's -fdefault-real-8 build): 13d0/12d0, 1d-12
+  // and 1d-15 in binary128, and rho < 1d-8 as rho < lim8_lt
+  int quad;
+  double lim8_lt;
+  qd::q128 q_c1312, q_eps, q_1em15;
   Ex7Scalars* sc;
   int* flag;  // sweep: per position, 1 if the step is active on the pass-start state
   int* list;  // sweep: the flagged positions in increasing order
@@ -47,6 +52,7 @@ struct Ex7 {
   Ex7Scalars* hs = nullptr;  // pinned mirror of v.sc
   void* block = nullptr;     // one device allocation holding every buffer
   int use_limiter = 2, swp_num = 0;
+  double t_loop = 0.;  // DO WHILE (time <= time_terminal - 1d-10), literal-exact
   int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;
   std::vector<int32_t> sweep_track, neg_track, pos_track;
   int64_t launches = 0;
@@ -65,5 +71,6 @@ swfd_status ex7_find_alpha(swfd_handle* h, double* alphamax);
 swfd_status ex7_stats(swfd_handle* h, swfd_sweep_stats* s);
 int64_t ex7_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos, int64_t cap);
 int64_t ex7_launches(swfd_handle* h);
+double ex7_t_loop(swfd_handle* h);
 
 }  // namespace swfd

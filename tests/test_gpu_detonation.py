@@ -94,3 +94,21 @@ def test_state_round_trip_and_unsupported_entry_points(swfd, oracle_mod):
     with pytest.raises(RuntimeError):
         g.flux_divergence()
     g.close()
+
+
+@pytest.mark.parametrize("case,steps", [((8, 2, 2), 0), ((32, 4, 8), 6)])
+def test_binary128_literals_match_the_oracle(swfd, oracle_mod, case, steps):
+    """literals QUAD (the reference's -fdefault-real-8 build): the WENO
+    indicators and alphas, the RK combinations, the 1d-15 Roe regularisers,
+    rho < 1d-8 and the time loop with binary128 literals; steps 0 runs to
+    T = 0.6 (with sweeps)."""
+    g, o = pair(oracle_mod, *case, literals=abi.LITERALS_QUAD)
+    if steps == 0:
+        assert g.run() == o.run()
+    else:
+        for k in range(steps):
+            assert g.step() == o.step(), k
+    assert g.time == o.time
+    assert_same(g.state(), o.state(), f"quad {case}")
+    assert g.stats() == o.stats()
+    g.close()
