@@ -1988,6 +1988,44 @@ static void ex7_interface(const oracle* r, int ydir, const double* L, const doub
   }
 }
 
+/* use_limiter = 1: the positivity limiter of one split flux (:336-440), five
+ * components and q*Y in both pressures, theta clamped at 0 */
+static void ex7_zs_limit(oracle* r, const double* ave, double* out) {
+  const double g1 = r->gamma1, q = r->qc;
+  const double d_ave = ave[0], m_ave = ave[1], n_ave = ave[2], e_ave = ave[3], y_ave = ave[4];
+  const double p_ave =
+      g1 * (e_ave - 0.5 * (m_ave * m_ave) / d_ave - 0.5 * (n_ave * n_ave) / d_ave - q * y_ave);
+  double point[2][5];
+  double theta = 1.0;
+  for (int c = 0; c < 5; ++c) {
+    point[0][c] = out[c];
+    point[1][c] = (ave[c] - out[c] / 12.) / (11. / 12.);
+  }
+  for (int ig = 0; ig < 2; ++ig) {
+    const double d_l = point[ig][0];
+    if (d_l < 0.) theta = fmin(theta, fabs(d_ave - 0.) / fabs(d_ave - d_l));
+  }
+  theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    out[0] = theta * out[0] + (1. - theta) * d_ave;
+    r->den_count++;
+  }
+  theta = 1.;
+  point[0][0] = out[0];
+  point[1][0] = (ave[0] - out[0] / 12.) / (11. / 12.);
+  for (int ig = 0; ig < 2; ++ig) {
+    const double d_l = point[ig][0], m_l = point[ig][1], n_l = point[ig][2], e_l = point[ig][3],
+                 y_l = point[ig][4];
+    const double p_l = g1 * (e_l - (m_l * m_l) / d_l / 2. - (n_l * n_l) / d_l / 2. - q * y_l);
+    if (p_l < 0.) theta = fmin(theta, fabs(p_ave - 0.) / fabs(p_ave - p_l));
+  }
+  theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    r->pre_count++;
+    for (int c = 0; c < 5; ++c) out[c] = theta * out[c] + (1. - theta) * ave[c];
+  }
+}
+
 /* findalpha of one rank (:774-808; source_alpha is computed there but never
  * used, so it is left out) */
 static double ex7_findalpha(oracle* r) {
@@ -2059,6 +2097,10 @@ static void ex7_wenofd(oracle* r) {
       const double R[5] = {r->wk_w[i + 1], r->wk_vx[i + 1], r->wk_vy[i + 1], r->wk_ratio[i + 1],
                            r->wk_h[i + 1]};
       ex7_interface(r, 0, L, R, (const double(*)[5])sp, (const double(*)[5])sn, op, on);
+      if (r->cfg.use_limiter == 1) {
+        ex7_zs_limit(r, sp[2], op);
+        ex7_zs_limit(r, sn[2], on);
+      }
       for (int c = 0; c < 5; ++c) {
         UR(r, r->fpf, c, i, j) = al * op[c];
         UR(r, r->fnf, c, i, j) = al * on[c];
@@ -2103,6 +2145,10 @@ static void ex7_wenofd(oracle* r) {
       const double R[5] = {r->wk_w[j + 1], r->wk_vx[j + 1], r->wk_vy[j + 1], r->wk_ratio[j + 1],
                            r->wk_h[j + 1]};
       ex7_interface(r, 1, L, R, (const double(*)[5])sp, (const double(*)[5])sn, op, on);
+      if (r->cfg.use_limiter == 1) {
+        ex7_zs_limit(r, sp[2], op);
+        ex7_zs_limit(r, sn[2], on);
+      }
       for (int c = 0; c < 5; ++c) {
         UR(r, r->gpf, c, i, j) = al * op[c];
         UR(r, r->gnf, c, i, j) = al * on[c];

@@ -317,6 +317,42 @@ __device__ void e7_interface(const Ex7View& e, int ydir, const double* L, const 
   }
 }
 
+// use_limiter = 1: the positivity limiter of one split flux (:336-440), five
+// components and q*Y in both pressures, theta clamped at 0; returns the
+// density (bit 0) and pressure (bit 1) limitings
+__device__ int e7_zs_limit(const Ex7View& e, const double* ave, double* out) {
+  const double g1 = e.g1, q = e.q;
+  const double d_ave = ave[0], m_ave = ave[1], n_ave = ave[2], e_ave = ave[3], y_ave = ave[4];
+  const double p_ave = g1 * (e_ave - tdiv(tscale<-1>(m_ave * m_ave), d_ave) -
+                             tdiv(tscale<-1>(n_ave * n_ave), d_ave) - q * y_ave);
+  double p1[5];
+  for (int c = 0; c < 5; ++c) p1[c] = tdiv(ave[c] - tdiv(out[c], 12.), 11. / 12.);
+  int lim = 0;
+  double theta = 1.0;
+  if (out[0] < 0.) theta = fmin(theta, tdiv(fabs(d_ave - 0.), fabs(d_ave - out[0])));
+  if (p1[0] < 0.) theta = fmin(theta, tdiv(fabs(d_ave - 0.), fabs(d_ave - p1[0])));
+  theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    out[0] = theta * out[0] + (1. - theta) * d_ave;
+    lim |= 1;
+  }
+  theta = 1.;
+  p1[0] = tdiv(ave[0] - tdiv(out[0], 12.), 11. / 12.);
+  for (int ig = 0; ig < 2; ++ig) {
+    const double* pt = ig == 0 ? out : p1;
+    const double d_l = pt[0];
+    const double p_l = g1 * (pt[3] - tscale<-1>(tdiv(pt[1] * pt[1], d_l)) -
+                             tscale<-1>(tdiv(pt[2] * pt[2], d_l)) - q * pt[4]);
+    if (p_l < 0.) theta = fmin(theta, tdiv(fabs(p_ave - 0.), fabs(p_ave - p_l)));
+  }
+  theta = fmax(theta, 0.);
+  if (theta < 1.) {
+    for (int c = 0; c < 5; ++c) out[c] = theta * out[c] + (1. - theta) * ave[c];
+    lim |= 2;
+  }
+  return lim;
+}
+
 // interfaces of every rank (x: i+1/2 for local i = 0..nxl+1 on rows
 // 0..nyl+1; y: j+1/2 for j = 0..nyl+1 on columns 0..nxl+1), scaled by the
 // line's alpha (:444-445, :728-729)
@@ -339,6 +375,12 @@ __global__ void __launch_bounds__(128) k7_flux(Ex7View e, int ydir) {
       sn[ig][c] = e.sn[o];
     }
   e7_interface(e, ydir, L, Rr, sp, sn, op, on);
+  if (e.use_limiter == 1) {
+    const int lp = e7_zs_limit(e, sp[2], op), ln = e7_zs_limit(e, sn[2], on);
+    const int den = (lp & 1) + (ln & 1), pre = (lp >> 1) + (ln >> 1);
+    if (den) atomicAdd((unsigned long long*)&e.sc->lim_den, (unsigned long long)den);
+    if (pre) atomicAdd((unsigned long long*)&e.sc->lim_pre, (unsigned long long)pre);
+  }
   const double al = e.lal[(int64_t)r * e.LL + (ydir ? i : j) + 2];
   double* fp = ydir ? e.gpf : e.fpf;
   double* fn = ydir ? e.gnf : e.fnf;
@@ -834,9 +876,8 @@ swfd_status ex7_check(const swfd_config& c, std::string& err) {
       return SWFD_ERR_UNSUPPORTED;
     }
   }
-  if (c.precision != SWFD_PRECISION_FP64 || (c.use_limiter != 0 && c.use_limiter != 2) ||
-      (c.rk_choice != 0 && c.rk_choice != 1)) {
-    err = "detonation: precision FP64, use_limiter 0 or 2 and rk_choice 1 only";
+  if (c.precision != SWFD_PRECISION_FP64 || (c.rk_choice != 0 && c.rk_choice != 1)) {
+    err = "detonation: precision FP64 and rk_choice 1 only";
     return SWFD_ERR_UNSUPPORTED;
   }
   if (c.swp_num <= 0 && c.use_limiter == 2) {
@@ -889,6 +930,7 @@ swfd_status ex7_create(swfd_handle* h, std::string& err) {
   v.q = 50.;
   v.tc = 50.;
   v.kc = 2566.4;
+  v.use_limiter = c.use_limiter;
   v.lim8_lt = 1e-8;
   x->t_loop = c.time_terminal - 1e-10;
   if (c.literals == SWFD_LITERALS_QUAD) {  // the constants of the 4-component path
@@ -1077,6 +1119,7 @@ swfd_status ex7_step(swfd_handle* h, double* dt_out) {
 
 swfd_status ex7_stats(swfd_handle* h, swfd_sweep_stats* st) {
   const Ex7* x = h->ex7;
+  ST(e7_sync_scalars(h));
   memset(st, 0, sizeof(*st));
   st->sweep_count = x->sweep_count;
   for (size_t k = 0; k < x->sweep_track.size(); ++k) {
@@ -1087,8 +1130,8 @@ swfd_status ex7_stats(swfd_handle* h, swfd_sweep_stats* st) {
     st->total_pos += x->pos_track[k];
     st->max_pos = std::max<int64_t>(st->max_pos, x->pos_track[k]);
   }
-  st->den_count = x->den_count;
-  st->pre_count = x->pre_count;
+  st->den_count = x->den_count + x->hs->lim_den;  // the ranks' limiter counts, summed
+  st->pre_count = x->pre_count + x->hs->lim_pre;
   st->sweep_fail_count = x->fail_count;
   return SWFD_OK;
 }

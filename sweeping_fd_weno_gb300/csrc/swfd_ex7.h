@@ -23,6 +23,7 @@ struct Ex7Scalars {
   long long t_pos, t_neg;                     // nod_lim branch counts of the current sweep
   int nflag, pad;
   double ubar[5];
+  long long lim_den, lim_pre;  // use_limiter = 1: density and pressure limitings
 };
 
 // everything a kernel needs, passed by value
@@ -39,7 +40,7 @@ struct Ex7View {
   const qd::q128* expc;  // Taylor coefficients of exp (qd::exp_coefs)
   // literals QUAD (the reference's -fdefault-real-8 build): 13d0/12d0, 1d-12
   // and 1d-15 in binary128, and rho < 1d-8 as rho < lim8_lt
-  int quad;
+  int quad, use_limiter;
   double lim8_lt;
   qd::q128 q_c1312, q_eps, q_1em15;
   Ex7Scalars* sc;

@@ -86,7 +86,7 @@ def test_shock_diffraction_config_checks(swfd):
 
 def test_detonation_config_checks(swfd):
     """ex7: grid from total and the rank grid, the wall row inside a rank's
-    local rows, FP64 and the sweeping or no limiter."""
+    local rows, FP64 and the SSP-RK3 of its rk."""
     import ctypes as C
     from sweeping_fd_weno_gb300 import problems
     lib = abi.load()
@@ -97,6 +97,7 @@ def test_detonation_config_checks(swfd):
     cfg = problems.make_config(abi.DETONATION, total=32)
     cfg.ny += 8                              # not cut_y*(5*total/cut_y)
     assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID
-    for field, value in (("use_limiter", 1), ("precision", abi.PRECISION_FP32_BULK)):
-        cfg = problems.make_config(abi.DETONATION, total=32, **{field: value})
-        assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED, field
+    cfg = problems.make_config(abi.DETONATION, total=32, precision=abi.PRECISION_FP32_BULK)
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_UNSUPPORTED
+    cfg = problems.make_config(abi.DETONATION, total=32, rk_choice=2)  # ex2's restart RK only
+    assert lib.swfd_create(C.byref(cfg), C.byref(h)) == abi.ERR_INVALID

@@ -112,3 +112,18 @@ def test_binary128_literals_match_the_oracle(swfd, oracle_mod, case, steps):
     assert_same(g.state(), o.state(), f"quad {case}")
     assert g.stats() == o.stats()
     g.close()
+
+
+@pytest.mark.parametrize("literals", [abi.LITERALS_DOUBLE, abi.LITERALS_QUAD])
+def test_flux_limiter_run(swfd, oracle_mod, literals):
+    """use_limiter = 1: the five-component positivity limiter (q*Y in both
+    pressures) on a whole 40 x 40 run; the density and pressure limitings
+    are counted in den_count and pre_count."""
+    g, o = pair(oracle_mod, 8, 2, 2, use_limiter=1, literals=literals)
+    assert g.run() == o.run()
+    assert g.time == o.time
+    assert_same(g.state(), o.state(), f"limiter, literals {literals}")
+    st = g.stats()
+    assert st == o.stats()
+    assert st["den_count"] > 0 and st["pre_count"] > 0
+    g.close()
