@@ -80,7 +80,7 @@ enum {
                                   is u(5,-2:nx+3,-2:ny+3)), the chemistry source
                                   on the fifth; ex6's rank decomposition with
                                   nx = cut_x*(5*total/cut_x), ny = cut_y*(5*total/cut_y),
-                                  the wall's top row 2*total; use_limiter 0 or 2 */
+                                  the wall's top row 2*total */
 };
 
 /* How the reference's double-kind literals (1d-6, 13d0/12d0, 0.75d0, ...)
