@@ -41,6 +41,21 @@ __device__ __forceinline__ double dsq(double a) { return a * a; }
 // Binary32: the hardware division.
 __device__ __forceinline__ double tdiv(double a, double b) { return sd::div(a, b); }
 __device__ __forceinline__ float tdiv(float a, float b) { return a / b; }
+// Division policies of the WENO reconstructions: DivHw is tdiv (the exact
+// quotient, with its out-of-range fallback); DivFlag the same quotient without
+// the fallback branch, raising *bad where the fallback would be needed, so a
+// caller computes many quotients in straight-line code and redoes the work
+// with DivHw in the rare flagged case.
+struct DivHw {
+  template <class T>
+  __device__ __forceinline__ T operator()(T a, T b) const { return tdiv(a, b); }
+};
+struct DivFlag {
+  int* bad;
+  __device__ __forceinline__ double operator()(double a, double b) const {
+    return sd::div_nf(a, b, *bad);
+  }
+};
 // x * 2^K.  Binary64: sd::scale, an addition to the exponent field (the bits
 // of the hardware product).  Binary32: the product.
 template <int K>
@@ -134,45 +149,45 @@ static __device__ __noinline__ double weno_left_qd(double am2, double am1, doubl
 }
 
 // weno_right (weno5.f90:120-146)
-template <class T>
-__device__ __forceinline__ T weno_right(T am2, T am1, T a0, T ap1, T ap2, T eps) {
+template <class T, class D = DivHw>
+__device__ __forceinline__ T weno_right(T am2, T am1, T a0, T ap1, T ap2, T eps, D div = D()) {
   T um1 = T(SWFD_C13) * am2 + T(SWFD_CM76) * am1 + T(SWFD_C116) * a0;
   T um2 = T(SWFD_CM16) * am1 + T(SWFD_C56) * a0 + T(SWFD_C13) * ap1;
   T um3 = T(SWFD_C13) * a0 + T(SWFD_C56) * ap1 + T(SWFD_CM16) * ap2;
   T b1, b2, b3;
   weno_beta(am2, am1, a0, ap1, ap2, b1, b2, b3);
-  T a1 = tdiv(T(0.3), tsq(eps + b1));
-  T a2 = tdiv(T(0.6), tsq(eps + b2));
-  T a3 = tdiv(T(0.1), tsq(eps + b3));
+  T a1 = div(T(0.3), tsq(eps + b1));
+  T a2 = div(T(0.6), tsq(eps + b2));
+  T a3 = div(T(0.1), tsq(eps + b3));
   T s = a1 + a2 + a3;
   T w1, w2, w3;
   if constexpr (sizeof(T) == 4) {  // FP32-bulk: one reciprocal for the three weights
     const T rs = T(1.) / s;
     w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
   } else {  // the reference's three divisions (weno5.f90:134-140)
-    w1 = tdiv(a1, s), w2 = tdiv(a2, s), w3 = tdiv(a3, s);
+    w1 = div(a1, s), w2 = div(a2, s), w3 = div(a3, s);
   }
   return w1 * um3 + w2 * um2 + w3 * um1;
 }
 
 // weno_left (weno5.f90:86-113)
-template <class T>
-__device__ __forceinline__ T weno_left(T am2, T am1, T a0, T ap1, T ap2, T eps) {
+template <class T, class D = DivHw>
+__device__ __forceinline__ T weno_left(T am2, T am1, T a0, T ap1, T ap2, T eps, D div = D()) {
   T up1 = T(SWFD_CM16) * am2 + T(SWFD_C56) * am1 + T(SWFD_C13) * a0;
   T up2 = T(SWFD_C13) * am1 + T(SWFD_C56) * a0 + T(SWFD_CM16) * ap1;
   T up3 = T(SWFD_C116) * a0 + T(SWFD_CM76) * ap1 + T(SWFD_C13) * ap2;
   T b1, b2, b3;
   weno_beta(am2, am1, a0, ap1, ap2, b1, b2, b3);
-  T a1 = tdiv(T(0.1), tsq(eps + b1));
-  T a2 = tdiv(T(0.6), tsq(eps + b2));
-  T a3 = tdiv(T(0.3), tsq(eps + b3));
+  T a1 = div(T(0.1), tsq(eps + b1));
+  T a2 = div(T(0.6), tsq(eps + b2));
+  T a3 = div(T(0.3), tsq(eps + b3));
   T s = a1 + a2 + a3;
   T w1, w2, w3;
   if constexpr (sizeof(T) == 4) {
     const T rs = T(1.) / s;
     w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
   } else {  // weno5.f90:104-110
-    w1 = tdiv(a1, s), w2 = tdiv(a2, s), w3 = tdiv(a3, s);
+    w1 = div(a1, s), w2 = div(a2, s), w3 = div(a3, s);
   }
   return w1 * up3 + w2 * up2 + w3 * up1;
 }

@@ -596,6 +596,54 @@ cudaError_t launch_split(const Params& p, double* u, const DevScalars* dsc, void
 // column i).  sp/sn point at stencil cell -2, component 0 of the positive /
 // negative split flux; components are P apart, stencil cells `step` apart.
 // ---------------------------------------------------------------------------
+// the eight binary64 reconstructions of one interface (four characteristic
+// fields, both split fluxes) under a division policy (DivHw, DivFlag)
+template <int YDIR, class D>
+__device__ __forceinline__ void weno8_fp64(const Eigen2D<double>& E, const double* __restrict__ sp,
+                                           const double* __restrict__ sn, int64_t P, int64_t step,
+                                           double weps, D div, double* ur, double* ul) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double cp[5], cn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double* a = sp + m * step;
+      const double* b = sn + m * step;
+      const double a0 = ldt(a), a1 = ldt(a + P), a2 = ldt(a + 2 * P), a3 = ldt(a + 3 * P);
+      const double b0 = ldt(b), b1 = ldt(b + P), b2 = ldt(b + 2 * P), b3 = ldt(b + 3 * P);
+      if (k == 0) {
+        cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, b0, b1, b2, b3);
+      } else if (k == 1) {
+        cp[m] = proj_row2<YDIR>(E.vt, a0, a1, a2);
+        cn[m] = proj_row2<YDIR>(E.vt, b0, b1, b2);
+      } else if (k == 2) {
+        cp[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, b0, b1, b2, b3);
+      } else {
+        cp[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, a0, a1, a2, a3);
+        cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, b0, b1, b2, b3);
+      }
+    }
+    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps, div);
+    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps, div);
+  }
+}
+struct Weno8 {
+  double ur[4], ul[4];
+};
+// the rare interface whose divisions leave sd::div's own range: the same
+// reconstructions with the exact fallback (out of line: the hot path stays
+// free of the fallback branches)
+template <int YDIR>
+static __device__ __noinline__ Weno8 weno8_hw(Eigen2D<double> E, const double* sp,
+                                              const double* sn, int64_t P, int64_t step,
+                                              double weps) {
+  Weno8 w;
+  weno8_fp64<YDIR>(E, sp, sn, P, step, weps, DivHw(), w.ur, w.ul);
+  return w;
+}
+
 template <int YDIR, class T, bool QD = false>
 __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __restrict__ sp,
                                                const T* __restrict__ sn, int64_t P, int64_t step,
@@ -637,6 +685,18 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
       ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
       ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
     }
+  } else if constexpr (!QD) {
+    // every division without its fallback branch; one check for all eight
+    int bad = 0;
+    weno8_fp64<YDIR>(E, sp, sn, P, step, weps, DivFlag{&bad}, ur, ul);
+    if (bad) {
+      const Weno8 w = weno8_hw<YDIR>(E, sp, sn, P, step, weps);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        ur[k] = w.ur[k];
+        ul[k] = w.ul[k];
+      }
+    }
   } else
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -661,13 +721,8 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
         cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, b0, b1, b2, b3);
       }
     }
-    if constexpr (QD) {
-      ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], *qw);
-      ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], *qw);
-    } else {
-      ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
-      ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
-    }
+    ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], *qw);
+    ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], *qw);
   }
   // evr . ur (main.f90:226-229): row 1 [1,0,1,1]; normal-momentum row
   // [vn-c, 0, vn, vn+c]; tangential row [vt, 1, vt, vt]; energy row

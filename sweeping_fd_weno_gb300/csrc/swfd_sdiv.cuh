@@ -113,6 +113,44 @@ SWFD_SD double div(double a, double b) {
   return dfrom(((ua ^ ub) & 0x8000000000000000ull) | ((uint64_t)e << 52) | (q & frac));
 }
 
+// a / b by the same steps as div, without the fallback: for operands or
+// quotients outside the range div computes itself it sets `bad` and returns an
+// unspecified value.  No branch: a caller that divides many times checks
+// `bad` once and redoes the work with div.
+SWFD_SD double div_nf(double a, double b, int& bad) {
+  const uint64_t ua = dbits(a), ub = dbits(b);
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+  int32_t e = (int32_t)ea - (int32_t)eb + 1023;
+  bad |= (ea - 1u >= 2046u) | (eb - 1u >= 2046u) | (e < 2) | (e > 2045);
+  const uint64_t frac = 0xfffffffffffffull;
+  const uint64_t B = (ub & frac) | (1ull << 52);
+  uint64_t A = (ua & frac) | (1ull << 52);
+  const bool lt = A < B;
+  A = lt ? A << 1 : A;
+  e -= lt ? 1 : 0;
+  A -= B;
+  uint64_t q = 1;
+  const float rcp = 1048576.0f * rcp32((float)(uint32_t)(B >> 21));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    A <<= 11;
+    const float n = ffrom(0x4b000000u | (uint32_t)(A >> 41)) - 8388608.0f;
+    const uint32_t dg = fbits(n * rcp + 8388608.0f) & 0x7fffffu;
+    uint64_t P = B * dg;
+    const bool over = P > A;
+    P -= over ? B : 0;
+    A -= P;
+    q = (q << 11) | (uint64_t)(dg - (over ? 1u : 0u));
+  }
+  const uint32_t low = (uint32_t)q & 7u;
+  q >>= 3;
+  q += (low > 4u || (low == 4u && (A != 0 || (q & 1)))) ? 1 : 0;
+  const bool carry = (q >> 53) != 0;
+  q = carry ? q >> 1 : q;
+  e += carry ? 1 : 0;
+  return dfrom(((ua ^ ub) & 0x8000000000000000ull) | ((uint64_t)(uint32_t)e << 52) | (q & frac));
+}
+
 // x * 2^K: only the exponent field changes while x and the result are normal
 template <int K>
 SWFD_SD double scale(double x) {

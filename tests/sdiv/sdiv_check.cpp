@@ -62,6 +62,13 @@ int main(int argc, char** argv) {
     if (!same(swfd::sd::scale<1>(a), a * 2.0) || !same(swfd::sd::scale<2>(a), a * 4.0) ||
         !same(swfd::sd::scale<-1>(a), a * 0.5) || !same(swfd::sd::scale<-2>(a), a * 0.25))
       bads++;
+    {  // the branch-free form: equal wherever it does not flag
+      int bad_nf = 0;
+      const double r = swfd::sd::div_nf(a, b, bad_nf);
+      if (!bad_nf && !same(r, a / b)) bad++;
+      int bad_q = 0;
+      if (!same(swfd::sd::div_nf(p, c, bad_q), p / c) && !bad_q) bad++;
+    }
     const uint32_t ea = (uint32_t)(swfd::sd::dbits(a) >> 52) & 0x7ff;
     fast += ea != 0 && ea != 0x7ff;
   }
