@@ -228,22 +228,23 @@ __global__ void k7_split(Ex7View e, int ydir) {
 // eigenvectors, projections of the five stencil points, ten WENO5
 // reconstructions, back projection; every product of the eigenvector sums is
 // formed, zeros and ones included, in the reference's order
-__device__ void e7_interface(const Ex7View& e, int ydir, const double* L, const double* Rr,
-                             const double (*sp)[5], const double (*sn)[5], double* outp,
-                             double* outn) {
+template <bool QD>
+__device__ __forceinline__ void e7_interface(const Ex7View& e, int ydir, const double* L,
+                                             const double* Rr, const double (*sp)[5],
+                                             const double (*sn)[5], double* outp, double* outn) {
   const double g1 = e.g1, q = e.q;
-  double t0 = e.quad ? qd::to_double(qd::div(qd::from_double(L[0]),
-                                             qd::add(qd::from_double(L[0] + Rr[0]), e.q_1em15)))
-                     : tdiv(L[0], L[0] + Rr[0] + 1e-15);
+  double t0 = QD ? qd::to_double(qd::div(qd::from_double(L[0]),
+                                         qd::add(qd::from_double(L[0] + Rr[0]), e.q_1em15)))
+                 : tdiv(L[0], L[0] + Rr[0] + 1e-15);
   double t1 = 1. - t0;
   const double vxm = t0 * L[1] + t1 * Rr[1];
   const double vym = t0 * L[2] + t1 * Rr[2];
   const double ym = t0 * L[3] + t1 * Rr[3];
   const double hm = t0 * L[4] + t1 * Rr[4];
   const double qm = tscale<-1>(vxm * vxm + vym * vym);
-  const double cm = e.quad ? qd::to_double(qd::add(qd::from_double(sqrt(fabs(g1 * (hm - qm - q * ym)))),
-                                                   e.q_1em15))
-                           : sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
+  const double cm = QD ? qd::to_double(qd::add(qd::from_double(sqrt(fabs(g1 * (hm - qm - q * ym)))),
+                                               e.q_1em15))
+                       : sqrt(fabs(g1 * (hm - qm - q * ym))) + 1e-15;
   const double rcm = tdiv(1., cm);
   const double b1 = g1 * rcm * rcm;
   const double b2 = qm * b1;
@@ -300,7 +301,7 @@ __device__ void e7_interface(const Ex7View& e, int ydir, const double* L, const 
       cn[ig] = evl[k][0] * sn[ig][0] + evl[k][1] * sn[ig][1] + evl[k][2] * sn[ig][2] +
                evl[k][3] * sn[ig][3] + evl[k][4] * sn[ig][4];
     }
-    if (e.quad) {
+    if constexpr (QD) {
       const QuadWeno qw{e.q_c1312, e.q_eps};
       ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], qw);
       ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], qw);
@@ -356,6 +357,7 @@ __device__ int e7_zs_limit(const Ex7View& e, const double* ave, double* out) {
 // interfaces of every rank (x: i+1/2 for local i = 0..nxl+1 on rows
 // 0..nyl+1; y: j+1/2 for j = 0..nyl+1 on columns 0..nxl+1), scaled by the
 // line's alpha (:444-445, :728-729)
+template <bool QD, bool LIM>
 __global__ void __launch_bounds__(128) k7_flux(Ex7View e, int ydir) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int ni = e.nxl + 2, nj = e.nyl + 2;
@@ -374,8 +376,8 @@ __global__ void __launch_bounds__(128) k7_flux(Ex7View e, int ydir) {
       sp[ig][c] = e.sp[o];
       sn[ig][c] = e.sn[o];
     }
-  e7_interface(e, ydir, L, Rr, sp, sn, op, on);
-  if (e.use_limiter == 1) {
+  e7_interface<QD>(e, ydir, L, Rr, sp, sn, op, on);
+  if constexpr (LIM) {
     const int lp = e7_zs_limit(e, sp[2], op), ln = e7_zs_limit(e, sn[2], on);
     const int den = (lp & 1) + (ln & 1), pre = (lp >> 1) + (ln >> 1);
     if (den) atomicAdd((unsigned long long*)&e.sc->lim_den, (unsigned long long)den);
@@ -392,6 +394,7 @@ __global__ void __launch_bounds__(128) k7_flux(Ex7View e, int ydir) {
 
 // scheme (:738-750) + the RK combination (:824,846,867) over every local cell
 // (the RHS is zero outside the interior) + checkpositivity (:890-913)
+template <bool QD>
 __global__ void k7_rk(Ex7View e, int stage) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int bad = 0;
@@ -414,7 +417,7 @@ __global__ void k7_rk(Ex7View e, int stage) {
       }
       const int64_t o = e7_at(e, r, c, i, j);
       double v = a[c] + dt * rhs;
-      if (e.quad && stage >= 2) {  // 0.75d0*u0 + 0.25d0*(..), (u0 + 2d0*(..))/3d0 in binary128
+      if (QD && stage >= 2) {  // 0.75d0*u0 + 0.25d0*(..), (u0 + 2d0*(..))/3d0 in binary128
         using namespace qd;
         v = stage == 2 ? to_double(add(mul(from_double(0.75), from_double(e.u0[o])),
                                        scale2(from_double(v), -2)))
@@ -776,6 +779,22 @@ swfd_status e7_sync_scalars(swfd_handle* h) {
   return SWFD_OK;
 }
 
+// the interface kernel specialised on the literal form and the limiter
+swfd_status e7_launch_flux(swfd_handle* h, int64_t faces, int ydir) {
+  const Ex7View& v = h->ex7->v;
+  cudaStream_t s = h->stream;
+  const unsigned g = e7_grid(faces, 128);
+  const bool lim = v.use_limiter == 1;
+  if (v.quad) {
+    if (lim) E7K(h, (k7_flux<true, true><<<g, 128, 0, s>>>(v, ydir)));
+    else E7K(h, (k7_flux<true, false><<<g, 128, 0, s>>>(v, ydir)));
+  } else {
+    if (lim) E7K(h, (k7_flux<false, true><<<g, 128, 0, s>>>(v, ydir)));
+    else E7K(h, (k7_flux<false, false><<<g, 128, 0, s>>>(v, ydir)));
+  }
+  return SWFD_OK;
+}
+
 swfd_status e7_bc(swfd_handle* h) {
   const Ex7View& v = h->ex7->v;
   cudaStream_t s = h->stream;
@@ -1086,16 +1105,17 @@ swfd_status ex7_step(swfd_handle* h, double* dt_out) {
     E7K(h, (k7_mirror_x<<<e7_grid((int64_t)v.cut_y * (v.nyl + 2) * 3), E7_BLOCK, 0, s>>>(v)));
     E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LJ * 32), E7_BLOCK, 0, s>>>(v, 0)));
     E7K(h, (k7_split<<<e7_grid((int64_t)v.R * v.LI * (v.nyl + 2)), E7_BLOCK, 0, s>>>(v, 0)));
-    E7K(h, (k7_flux<<<e7_grid(faces, 128), 128, 0, s>>>(v, 0)));
+    ST(e7_launch_flux(h, faces, 0));
     E7K(h, (k7_mirror_y<<<e7_grid((int64_t)v.cut_y * 3 * v.total), E7_BLOCK, 0, s>>>(v)));
     E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LI * 32), E7_BLOCK, 0, s>>>(v, 1)));
     E7K(h, (k7_split<<<e7_grid((int64_t)v.R * (v.nxl + 2) * v.LJ), E7_BLOCK, 0, s>>>(v, 1)));
-    E7K(h, (k7_flux<<<e7_grid(faces, 128), 128, 0, s>>>(v, 1)));
+    ST(e7_launch_flux(h, faces, 1));
     // u0 = u after wenofd, whose wall mirrors rewrite cells of u (:822)
     if (stage == 1)
       E7CU(h, cudaMemcpyAsync(v.u0, v.u, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
     E7CU(h, cudaMemsetAsync(&v.sc->postag, 0, sizeof(int), s));
-    E7K(h, (k7_rk<<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
+    if (v.quad) E7K(h, (k7_rk<true><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
+    else E7K(h, (k7_rk<false><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
     if (x->use_limiter == 2) {
       ST(e7_sync_scalars(h));
       if (x->hs->err & E7_ERR_NONFINITE)
