@@ -20,7 +20,7 @@ namespace swfd {
 
 // Derive the per-example switches (the reference's variant matrix) and the
 // grid spacing exactly as each initdata computes it.
-// Options this build implements; everything else is rejected before any
+// Options the library implements; everything else is rejected before any
 // CUDA call.
 // the MATLAB script's domain and boundary treatment per `problem`
 // (ex1_double_rarefaction_1d/FD_WENO_Application.m:27-150)
