@@ -338,6 +338,11 @@ swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops);
 /* The FP32-bulk form's reciprocal (an FP32 seed refined by two Newton steps
  * in FP64) applied to n host values on the device, for its error test. */
 swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n, double* out);
+/* Test entry point: the FP32-bulk kernels' binary64 -> binary32 conversion
+ * (out_f) and its binary32 -> binary64 widening (out_d), both on the integer
+ * pipes, for n host values; they must equal the hardware conversions. */
+swfd_status swfd_probe_convert(int32_t device, const double* x, int64_t n, float* out_f,
+                               double* out_d);
 
 /* Last error message of the handle (or of the process when h is NULL). */
 swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len);

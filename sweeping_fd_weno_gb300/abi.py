@@ -137,6 +137,7 @@ _SIGS = {
     "swfd_reset_profile": (C.c_int32, [_P]),
     "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
     "swfd_probe_rcp_bulk": (C.c_int32, [C.c_int32, _DP, C.c_int64, _DP]),
+    "swfd_probe_convert": (C.c_int32, [C.c_int32, _DP, C.c_int64, C.POINTER(C.c_float), _DP]),
     "swfd_flux_divergence_static": (C.c_int32, [C.POINTER(SwfdConfig), _P, _P, _P]),
     "swfd_batch_config_default": (C.c_int32, [C.POINTER(SwfdBatchConfig)]),
     "swfd_batch_create": (C.c_int32, [C.POINTER(SwfdBatchConfig), C.POINTER(_P)]),

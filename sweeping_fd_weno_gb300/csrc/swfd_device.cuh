@@ -66,21 +66,38 @@ __device__ __forceinline__ float tscale(float x) {
   return x * f;
 }
 
-// 1/x for the FP32-bulk form, whose results are not bit-exact by design:
-// the FP32 reciprocal as the seed and two Newton-Raphson steps
-// r <- r + r (1 - x r) in FP64.  Each step squares the relative error
-// (2^-23 -> 2^-46 -> below 2^-53), so the result is within an ulp or two of
-// 1/x for fewer FP64 instructions than the IEEE division; magnitudes the
-// FP32 seed cannot hold (decided on the exponent bits) take the division.
-__device__ __forceinline__ double rcp_bulk(double x) {
-  const int ex = (__double2hiint(x) >> 20) & 0x7ff;
-  if (ex < 1023 - 120 || ex > 1023 + 120) return 1.0 / x;
-  double r = (double)__frcp_rn((float)x);
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
+// 1/x for the FP32-bulk form: the correctly rounded reciprocal from sd::div
+// (integer and FP32 pipes; a Newton refinement of an FP32 seed cost four
+// DFMAs and two conversions on the FP64 pipe)
+__device__ __forceinline__ double rcp_bulk(double x) { return sd::div(1.0, x); }
+
+// binary64 <-> binary32 conversions on the integer pipes, the bits of the
+// hardware conversions (round to nearest even): GB300 runs conversions to
+// and from 64-bit types at the FP64 rate.  Zero, subnormal, infinite, NaN
+// and out-of-range values take the hardware conversion (out of line).
+static __device__ __noinline__ float d2f_hw(double x) { return (float)x; }
+static __device__ __noinline__ double f2d_hw(float x) { return (double)x; }
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((u >> 52) & 0x7ff) - 1023 + 127;
+  if ((unsigned)(e - 1) >= 254u) return d2f_hw(x);
+  const unsigned long long m = u & 0xfffffffffffffull;
+  unsigned r = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)m & 0x1fffffffu;
+  r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+  // a rounding carry moves into the exponent (up to infinity, as RNE does)
+  return __uint_as_float(((unsigned)(u >> 32) & 0x80000000u) | (((unsigned)e << 23) + r));
 }
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u >= 254u) return f2d_hw(x);
+  return __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ double tod(double x) { return x; }
+__device__ __forceinline__ double tod(float x) { return f2d(x); }
 
 // beta(1:3) (weno5.f90:100-102); am2..ap2 = average(-2..2)
 template <class T>

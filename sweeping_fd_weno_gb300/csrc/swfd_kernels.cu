@@ -140,9 +140,9 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
         const double vx = u1 >= p.eps2 ? u2 * ri : 0., vy = u1 >= p.eps2 ? u3 * ri : 0.;
         pres = g1 * fma(-0.5 * u1, fma(vx, vx, vy * vy), u4);
       }
-      const float fri = (float)ri;
-      const float sound = sqrtf((float)gamma * (float)pres * fri);
-      a = (double)(fmaxf(fabsf((float)u2 * fri), fabsf((float)u3 * fri)) + sound);
+      const float fri = d2f(ri);
+      const float sound = sqrtf(d2f(gamma) * d2f(pres) * fri);
+      a = f2d(fmaxf(fabsf(d2f(u2) * fri), fabsf(d2f(u3) * fri)) + sound);
     } else {
       double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
              u4 = ld(u + 3 * g.plane + o);
@@ -342,7 +342,7 @@ __device__ __forceinline__ T sqrt_abs(double v);
 template <>
 __device__ __forceinline__ double sqrt_abs<double>(double v) { return sqrt(fabs(v)); }
 template <>
-__device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf((float)v)); }
+__device__ __forceinline__ float sqrt_abs<float>(double v) { return sqrtf(fabsf(d2f(v))); }
 
 // which: 1 = x pass (fp, fn and the x Roe planes), 2 = y pass (gp, gn and,
 // with the ex4 regularisers, the y Roe planes), 3 = both.  With rank
@@ -378,12 +378,12 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
       const bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
       if (guard) vx = vy = 0.;
       const double pres = g1 * fma(-0.5 * rho, fma(vx, vx, vy * vy), e);
-      const float fr = (float)rho, fm = (float)mx, fn = (float)my, fe = (float)e;
-      const float fvx = (float)vx, fvy = (float)vy, fp = (float)pres;
+      const float fr = d2f(rho), fm = d2f(mx), fn = d2f(my), fe = d2f(e);
+      const float fvx = d2f(vx), fvy = d2f(vy), fp = d2f(pres);
       const float fxy = fr * fvx * fvy;
       const float f1 = fmaf(fr * fvx, fvx, fp), f3 = (fe + fp) * fvx;
       const float g2 = fmaf(fr * fvy, fvy, fp), g3 = (fe + fp) * fvy;
-      const float ram = 1.f / (float)amd, hf = 0.5f;
+      const float ram = 1.f / d2f(amd), hf = 0.5f;
       const int64_t S = p.sg.plane;
       float q;
       q = fm * ram;  split[0 * S + o] = hf * (fr + q);  split[4 * S + o] = hf * (fr - q);
@@ -399,18 +399,18 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
         const double vex = guard ? mx * ri : vx, vey = guard ? my * ri : vy;
         const double pre = guard ? g1 * fma(-0.5, fma(mx, vex, my * vey), e) : pres;
         roe[0 * P + o] = sqrtf(fabsf(fr));
-        roe[1 * P + o] = (float)vex;
-        roe[2 * P + o] = (float)vey;
-        roe[3 * P + o] = (float)((pre + e) * ri);
+        roe[1 * P + o] = d2f(vex);
+        roe[2 * P + o] = d2f(vey);
+        roe[3 * P + o] = d2f((pre + e) * ri);
       }
       if (p.roe_reg_ex4 && (which & 2)) {  // ex4_sedov_2d/main.f90:426
         const double t0 = 1. / (rho + 1e-15);
         const double vex = mx * t0, vey = my * t0;
         const double pre = g1 * fma(-0.5, fma(mx, vex, my * vey), e);
         roe[4 * P + o] = sqrtf(fabsf(fr));
-        roe[5 * P + o] = (float)vex;
-        roe[6 * P + o] = (float)vey;
-        roe[7 * P + o] = (float)((pre + e) * t0);
+        roe[5 * P + o] = d2f(vex);
+        roe[6 * P + o] = d2f(vey);
+        roe[7 * P + o] = d2f((pre + e) * t0);
       }
       return;
     }
@@ -1121,7 +1121,7 @@ __device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, 
   if constexpr (sizeof(T) == 4) {  // FP32-bulk: reciprocals of dx, dy
     const T ix = p.fdx_inv, iy = p.fdy_inv;
     if (p.alpha_premul) return -A * ix - B * iy;
-    const T am = T(amd);
+    const T am = d2f(amd);
     return -(am * A) * ix - (am * B) * iy;
   } else {
     const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
@@ -1185,7 +1185,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
     for (int c = 0; c < g.nc; ++c) {
       double r = 0.0;
       if (interior)
-        r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am)
+        r = tod((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am)
                                    : rhs2d_cell<T>(p, flux, c, i, j, am));
       double v;
       if (sizeof(T) == 4) {  // FP32-bulk: the FP64 accumulation with fused multiply-adds
@@ -1266,7 +1266,7 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
   if (in_grid && c < 3) {
     const double dt = dsc->dt;
     double r = 0.0;
-    if (interior) r = (double)rhs1d<T>(p, flux, c, o, dsc->alphamax);
+    if (interior) r = tod(rhs1d<T>(p, flux, c, o, dsc->alphamax));
     if (sizeof(T) == 4) {
       v = fma(dt, r, ld(u + c * P + o));
       if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
@@ -1331,7 +1331,7 @@ __global__ void k_rhs(Params p, const T* __restrict__ flux, const DevScalars* ds
   for (int c = 0; c < g.nc; ++c) {
     double r = 0.0;
     if (interior)
-      r = (double)((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, dsc->alphamax)
+      r = tod((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, dsc->alphamax)
                                  : rhs2d_cell<T>(p, flux, c, i, j, dsc->alphamax));
     rhs[c * P + o] = r;
   }

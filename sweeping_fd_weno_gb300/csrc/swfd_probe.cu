@@ -24,7 +24,37 @@ __global__ void k_rcp_bulk(const double* __restrict__ x, double* __restrict__ ou
     out[k] = swfd::rcp_bulk(x[k]);
 }
 
+__global__ void k_convert(const double* __restrict__ x, float* __restrict__ f,
+                          double* __restrict__ d, int64_t n) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const float v = swfd::d2f(x[k]);
+    f[k] = v;
+    d[k] = swfd::f2d(v);
+  }
+}
 }  // namespace
+
+// the integer-pipe binary64 -> binary32 -> binary64 conversions of the
+// FP32-bulk kernels on host values, for their bit-exactness test
+extern "C" swfd_status swfd_probe_convert(int32_t device, const double* x, int64_t n,
+                                          float* out_f, double* out_d) {
+  if (!x || !out_f || !out_d || n < 0 || n > (int64_t)1 << 26) return SWFD_ERR_INVALID;
+  if (n == 0) return SWFD_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return SWFD_ERR_CUDA;
+  double* d = nullptr;
+  if (cudaMalloc(&d, 2 * n * sizeof(double) + n * sizeof(float)) != cudaSuccess) return SWFD_ERR_OOM;
+  float* f = (float*)(d + 2 * n);
+  cudaError_t e = cudaMemcpy(d, x, n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_convert<<<256, 256>>>(d, f, d + n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out_f, f, n * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(out_d, d + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? SWFD_OK : SWFD_ERR_CUDA;
+}
 
 // the FP32-bulk reciprocal on host values, for its error-bound test
 extern "C" swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n,

@@ -31,3 +31,32 @@ def test_rcp_bulk_within_two_ulp(swfd):
     lg = np.log2(np.abs(x))
     far = (lg < -121) | (lg > 122)
     assert np.array_equal(out[far], ref[far])   # the IEEE division there
+
+
+def test_conversions_match_hardware(swfd):
+    """d2f / f2d (integer pipes) equal numpy's round-to-nearest-even
+    conversions bit for bit, on every class of binary64 value."""
+    rng = np.random.default_rng(11)
+    bits = rng.integers(0, 2**63, size=1 << 18, dtype=np.uint64) | \
+        (rng.integers(0, 2, size=1 << 18, dtype=np.uint64) << np.uint64(63))
+    x = bits.view(np.float64)
+    near = rng.uniform(-1, 1, 1 << 18) * np.exp2(rng.integers(-160, 140, 1 << 18).astype(np.float64))
+    ties = (rng.integers(1, 2**23, 1 << 14).astype(np.float64) + 0.5) * np.exp2(
+        rng.integers(-150, 100, 1 << 14).astype(np.float64))  # binary32 midpoints
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028235677973366e38,
+                        3.4028234663852886e38, 1.1754943508222875e-38, 1.401298464324817e-45,
+                        7.006492321624085e-46, 1e-50, -1e-50, 1e300, -1e300])
+    x = np.ascontiguousarray(np.concatenate([x, near, ties, special]))
+    f = np.empty(x.size, np.float32)
+    d = np.empty(x.size, np.float64)
+    dp = C.POINTER(C.c_double)
+    st = abi.load().swfd_probe_convert(0, x.ctypes.data_as(dp), x.size,
+                                       f.ctypes.data_as(C.POINTER(C.c_float)), d.ctypes.data_as(dp))
+    assert st == 0
+    with np.errstate(over="ignore", invalid="ignore"):
+        ref = x.astype(np.float32)
+    same_f = (f.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(f) & np.isnan(ref))
+    assert same_f.all(), x[~same_f][:5]
+    ref_d = ref.astype(np.float64)
+    same_d = (d.view(np.uint64) == ref_d.view(np.uint64)) | (np.isnan(d) & np.isnan(ref_d))
+    assert same_d.all(), ref[~same_d][:5]
