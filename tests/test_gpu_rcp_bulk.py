@@ -1,6 +1,6 @@
-"""The FP32-bulk form's reciprocal (FP32 seed, two Newton steps in FP64)
-against IEEE division: within two ulp over the magnitudes the form meets,
-and the IEEE division itself outside the seed's range."""
+"""The FP32-bulk form's integer-pipe helpers against the hardware: the
+reciprocal (sd::div(1, x)) equals IEEE division bit for bit, and the
+binary64 <-> binary32 conversions equal the round-to-nearest conversions."""
 import ctypes as C
 
 import numpy as np
@@ -11,12 +11,12 @@ from sweeping_fd_weno_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 
-def test_rcp_bulk_within_two_ulp(swfd):
+def test_rcp_bulk_is_the_ieee_reciprocal(swfd):
     rng = np.random.default_rng(5)
     x = np.concatenate([
         10.0 ** rng.uniform(-30, 30, 200000) * rng.choice([-1.0, 1.0], 200000),
         np.array([1.0, 3.0, 7.0, 0.1, 1e-14, 7.8e-15, 1 - 2.0 ** -53, 1 + 2.0 ** -52, 2.0 ** 100,
-                  2.0 ** -100, 1e-300, 1e300, 5e-324, -1e-310]),
+                  2.0 ** -100, 1e-300, 1e300, 5e-324, -1e-310, 0.0, -0.0, np.inf, 1.7e308]),
     ])
     out = np.empty_like(x)
     dp = C.POINTER(C.c_double)
@@ -24,13 +24,7 @@ def test_rcp_bulk_within_two_ulp(swfd):
     assert st == abi.OK
     with np.errstate(divide="ignore", over="ignore"):
         ref = 1.0 / x
-    fin = np.isfinite(ref)
-    assert np.array_equal(out[~fin], ref[~fin])
-    err = np.abs(out[fin] - ref[fin]) / np.spacing(np.abs(ref[fin]))
-    assert err.max() <= 2.0, (x[fin][err.argmax()], err.max())
-    lg = np.log2(np.abs(x))
-    far = (lg < -121) | (lg > 122)
-    assert np.array_equal(out[far], ref[far])   # the IEEE division there
+    assert np.array_equal(out.view(np.uint64), ref.view(np.uint64))
 
 
 def test_conversions_match_hardware(swfd):
