@@ -48,8 +48,8 @@ FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
 FLUX_FP64_INST_PER_INTERFACE = 739
 FLUX_FP64_INST_PER_INTERFACE_HW_DIV = 1197
 # DRAM bytes of one k_flux_xy<double> launch per interior cell, from an ncu
-# capture of the 1024x1024 vortex (310.6 MB per launch, inputs above L2)
-FLUX_DRAM_BYTES_PER_CELL = 310.6e6 / (1024 * 1024)
+# capture of the 1024x1024 vortex (315.2 MB per launch, inputs above L2)
+FLUX_DRAM_BYTES_PER_CELL = 315.2e6 / (1024 * 1024)
 # the same for k_flux_xy<float> of the FP32-bulk form (134.4 MB per launch)
 FLUX_F32_DRAM_BYTES_PER_CELL = 134.4e6 / (1024 * 1024)
 
@@ -712,7 +712,7 @@ def main():
         roofline.update({
             "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                              "k_flux_xy<double> on the 1024x1024 vortex (310.6 MB), scaled "
+                              "k_flux_xy<double> on the 1024x1024 vortex (315.2 MB), scaled "
                               "per cell to this grid",
             "kernel": "k_flux_xy<double> (characteristic WENO5 interface fluxes, both directions)",
             "compute_bound": "fp64 (the FP64 pipe; divisions and power-of-two products run "
