@@ -267,5 +267,29 @@ def write_output(solver, out_dir: str | Path = ".", new_table: bool | None = Fal
                   (zone,))
             _cols(out / "pre.dat", ((xs[i], ys[j], val(pres[j, i], i, j)) for i, j in cells),
                   (zone,))
+    elif p == abi.DETONATION:
+        # ex7_detonation/main.f90:1264-1394: density, pressure (with the q*Y
+        # term) and the mass fraction Y over 5*total x 5*total cells, the step
+        # region written as 100, 300 and 20
+        total = cfg.total
+        n = 5 * total
+        dx, dy = solver._dx(), solver._dy()
+        q = 50.
+        zone = list_record("zone i=", n, ", j=", n)
+        den, pre, rate = [], [], []
+        for j in range(n):
+            for i in range(n):
+                lrho, lm, ln, le, ly = (float(c) for c in u[j + 3, i + 3, :5])
+                pres = g1 * (le - 0.5 * (lm * lm) / lrho - 0.5 * (ln * ln) / lrho - q * ly)
+                yr = ly / lrho
+                if i + 1 <= total and j + 1 < 2 * total:
+                    lrho, pres, yr = 100., 300., 20.
+                xy = (dx * (i + 1 - 0.5), dy * (j + 1 - 0.5))
+                den.append(xy + (lrho,))
+                pre.append(xy + (pres,))
+                rate.append(xy + (yr,))
+        _cols(out / "den.dat", den, (zone,))
+        _cols(out / "pre.dat", pre, (zone,))
+        _cols(out / "rate.dat", rate, (zone,))
     text += stats_block(solver.stats())
     return text

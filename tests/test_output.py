@@ -93,3 +93,19 @@ def test_point_energy_jet_and_shock_files(oracle_mod, tmp_path):
     assert den[0] == list_record("zone i=", 12 * 13, ", j=", 12 * 11)
     vals = np.array([[float(v) for v in r.split()] for r in den[1:]])
     assert (vals[0, 2] == 0.0) and (vals[:, 2] > 0).any()  # the step region is written as 0
+
+
+def test_detonation_files(oracle_mod, tmp_path):
+    """ex7's output: den.dat, pre.dat (pressure with the q*Y term) and rate.dat
+    (Y = rho*Y/rho) over 5*total x 5*total cells, the step region written as
+    100, 300 and 20."""
+    d = OracleRun(oracle_mod, problems.make_config(abi.DETONATION, total=8, cut_x=2, cut_y=2),
+                  steps=2)
+    text = write_output(d, tmp_path / "ex7")
+    for name, fill in (("den.dat", 100.0), ("pre.dat", 300.0), ("rate.dat", 20.0)):
+        rows = (tmp_path / "ex7" / name).read_text().splitlines()
+        assert rows[0] == list_record("zone i=", 40, ", j=", 40)
+        vals = np.array([[float(v) for v in r.split()] for r in rows[1:]])
+        assert vals.shape == (40 * 40, 3)
+        assert vals[0, 2] == fill and (vals[:, 2] != fill).any()
+    assert " total sweep = " in text
