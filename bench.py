@@ -407,6 +407,64 @@ def bench_point_energy_1d(args, local):
     return out
 
 
+def bench_jet(args, local):
+    """The high-speed jet of ex5 (gamma 5/3, 800x200 half domain with the y=0
+    symmetry plane, u=800 inflow, T=0.001), plain FP64 only: the whole solve
+    to T as one graph (device-side loop over steps, sweeps as conditional
+    nodes), wall clock with a device synchronize on both sides, with the
+    sweep and adjustment counts it printed; the oracle on one host core for a
+    bounded sample of the leading steps, with a value-for-value check."""
+    import numpy as np
+    import oracle
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, problems
+    cfg = problems.workload("jet", device=local)
+    cells = cfg.nx * cfg.ny
+    w = Solver(cfg)                       # warm-up: the same graph shape, a few steps
+    w.init_problem()
+    w.run(max(1, args.warmup))
+    w.close()
+    s = Solver(cfg)
+    s.init_problem()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps = s.run()
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    st, t_end = s.stats(), s.time
+    s.close()
+    sample = max(1, args.jet_sample)
+    g = Solver(cfg)
+    g.init_problem()
+    o = oracle.Oracle(cfg)
+    o.init_problem()
+    t0 = time.perf_counter()
+    for _ in range(sample):
+        o.step()
+    cpu_s = time.perf_counter() - t0
+    for _ in range(sample):
+        g.step()
+    same = bool(np.array_equal(g.state(), o.state()) and g.time == o.time
+                and g.stats() == o.stats())
+    g.close()
+    gpu_rate = cells * 3 * steps / gpu_s
+    cpu_rate = cells * 3 * sample / cpu_s
+    return {"workload": "jet: ex5 high-speed jet, gamma 5/3, 800x200 half domain, u=800 "
+                        "inflow, T=0.001, plain FP64 with the sweeping limiter",
+            "cells": int(cells), "steps": int(steps), "t_end": t_end, "gpu_s": gpu_s,
+            "gpu_ms_per_step": gpu_s / max(steps, 1) * 1e3,
+            "value": gpu_rate, "unit": "cell-updates/s",
+            "sweeps": {k: int(v) for k, v in st.items()},
+            "cpu_oracle": {"value": cpu_rate, "cores": 1, "steps": int(sample),
+                           "s": cpu_s, "kind": "port"},
+            "speedup_vs_cpu": gpu_rate / cpu_rate, "same_result_after_sample": same,
+            "cpu_sample_note": "the oracle's sample is the leading steps, which run no "
+                               "sweep; the solve sweeps in most later stages, so the "
+                               "ratio understates the speed-up over a full CPU solve",
+            "timing": "wall clock around the whole-solve graph launch with a device "
+                      "synchronize on both sides"}
+
+
 def bench_detonation(args, local):
     """The reactive Euler detonation of ex7 at the reference's size (400x400 on
     its 4 x 8 ranks): GPU steps timed with CUDA events (the host reads the
@@ -583,6 +641,9 @@ def main():
     ap.add_argument("--no-detonation", action="store_true")
     ap.add_argument("--detonation-sample", type=int, default=2,
                     help="oracle steps of the detonation leg (about 1.5 s each)")
+    ap.add_argument("--no-jet", action="store_true")
+    ap.add_argument("--jet-sample", type=int, default=3,
+                    help="oracle steps of the jet leg (about 0.3 s each)")
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--plain-sample", type=int, default=8)
@@ -858,6 +919,8 @@ def main():
         line["one_d"] = bench_point_energy_1d(args, local)
         if not args.no_detonation:
             line["detonation"] = bench_detonation(args, local)
+        if not args.no_jet:
+            line["jet"] = bench_jet(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(solver.nx, args.cpu_budget)
     if rank == 0:
