@@ -433,6 +433,26 @@ def bench_jet(args, local):
     gpu_s = time.perf_counter() - t0
     st, t_end = s.stats(), s.time
     s.close()
+    # where a sweeping step's time goes: 20 steps after the first 1000 (the
+    # sweep runs in almost every stage by then), the flux launches bracketed
+    # by the handle's CUDA events; step() adds one host round trip per step
+    q = Solver(cfg)
+    q.init_problem()
+    q.run(1000)
+    q.set_profiling(True)
+    q.reset_profile()
+    sweeps0 = q.stats()["sweep_count"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(20):
+        q.step()
+    torch.cuda.synchronize()
+    prof_s = time.perf_counter() - t0
+    pr = q.profile()
+    split = {"after_steps": 1000, "steps": 20, "wall_ms_per_step": prof_s / 20 * 1e3,
+             "flux_ms_per_step": pr["flux_ms"] / 20,
+             "sweeps": int(q.stats()["sweep_count"] - sweeps0)}
+    q.close()
     sample = max(1, args.jet_sample)
     g = Solver(cfg)
     g.init_problem()
@@ -458,6 +478,7 @@ def bench_jet(args, local):
             "cpu_oracle": {"value": cpu_rate, "cores": 1, "steps": int(sample),
                            "s": cpu_s, "kind": "port"},
             "speedup_vs_cpu": gpu_rate / cpu_rate, "same_result_after_sample": same,
+            "step_split": split,
             "cpu_sample_note": "the oracle's sample is the leading steps, which run no "
                                "sweep; the solve sweeps in most later stages, so the "
                                "ratio understates the speed-up over a full CPU solve",
