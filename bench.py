@@ -770,7 +770,7 @@ def main():
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     import ctypes as C
     fp64 = C.c_double(0.0)
-    abi.load().swfd_probe_fp64_peak(local, C.byref(fp64))
+    abi.load_probe().swfd_probe_fp64_peak(local, C.byref(fp64))
     flux_ms_per_launch = prof["flux_ms"] / max(prof["flux_launches"], 1)
     # per launch (both directions of one stage): read the split fluxes (8
     # doubles) and Roe averages (4 doubles) of every cell once per direction,

@@ -6,7 +6,7 @@
  * example is one Fortran PROGRAM whose internal procedures are called by host
  * association.  Every entry point below replaces one of those procedures (or
  * a group of them) and names it, as path:line inside the reference project.
- * A Fortran host binds them with iso_c_binding.
+ * A Fortran host binds them with iso_c_binding (fortran/swfd_mod.f90).
  *
  * Conventions
  *  - Every call returns swfd_status: 0 on success, a negative value on error.
@@ -328,21 +328,11 @@ swfd_status swfd_reset_profile(swfd_handle* h);
  * All calls share that array and it keeps the last call's contents: calls
  * whose work overlaps on the GPU race and corrupt each other, so order them
  * on one stream.  The first call on a device looks up the array's address
- * with that device current; make it before any stream capture. */
+ * with that device current; make it before any stream capture.  Calls on a
+ * stream that is not capturing look the address up again (a cudaDeviceReset
+ * followed by a new context is followed); calls during capture reuse it. */
 swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const double* u, double* rhs,
                                         void* stream);
-
-/* Measured FP64 FMA throughput of the device in GFLOP/s (2 flops per FMA):
- * the denominator of the FP64-pipe roofline of the FP64 path. */
-swfd_status swfd_probe_fp64_peak(int32_t device, double* gflops);
-/* The FP32-bulk form's reciprocal (an FP32 seed refined by two Newton steps
- * in FP64) applied to n host values on the device, for its error test. */
-swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n, double* out);
-/* Test entry point: the FP32-bulk kernels' binary64 -> binary32 conversion
- * (out_f) and its binary32 -> binary64 widening (out_d), both on the integer
- * pipes, for n host values; they must equal the hardware conversions. */
-swfd_status swfd_probe_convert(int32_t device, const double* x, int64_t n, float* out_f,
-                               double* out_d);
 
 /* Last error message of the handle (or of the process when h is NULL). */
 swfd_status swfd_last_error(swfd_handle* h, char* buf, size_t len);

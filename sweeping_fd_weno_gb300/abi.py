@@ -135,9 +135,6 @@ _SIGS = {
     "swfd_set_profiling": (C.c_int32, [_P, C.c_int32]),
     "swfd_get_profile": (C.c_int32, [_P, C.POINTER(SwfdProfile)]),
     "swfd_reset_profile": (C.c_int32, [_P]),
-    "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
-    "swfd_probe_rcp_bulk": (C.c_int32, [C.c_int32, _DP, C.c_int64, _DP]),
-    "swfd_probe_convert": (C.c_int32, [C.c_int32, _DP, C.c_int64, C.POINTER(C.c_float), _DP]),
     "swfd_flux_divergence_static": (C.c_int32, [C.POINTER(SwfdConfig), _P, _P, _P]),
     "swfd_batch_config_default": (C.c_int32, [C.POINTER(SwfdBatchConfig)]),
     "swfd_batch_create": (C.c_int32, [C.POINTER(SwfdBatchConfig), C.POINTER(_P)]),
@@ -160,7 +157,36 @@ _SIGS = {
     "swfd_status_string": (C.c_char_p, [C.c_int32]),
 }
 
+# libswfd_probe.so (include/swfd_probe.h): measurement and test probes
+PROBE_PATH = LIB_PATH.parent / "libswfd_probe.so"
+_PROBE_SIGS = {
+    "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
+    "swfd_probe_rcp_bulk": (C.c_int32, [C.c_int32, _DP, C.c_int64, _DP]),
+    "swfd_probe_convert": (C.c_int32, [C.c_int32, _DP, C.c_int64, C.POINTER(C.c_float), _DP]),
+}
+
 _lib = None
+_probe = None
+
+
+def load_probe() -> C.CDLL:
+    """Load libswfd_probe.so (once).  Raises if absent."""
+    global _probe
+    if _probe is not None:
+        return _probe
+    if not PROBE_PATH.exists():
+        raise FileNotFoundError(f"{PROBE_PATH} is missing: build it with __graft_entry__.build()")
+    lib = C.CDLL(str(PROBE_PATH))
+    for name, (res, args) in _PROBE_SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _probe = lib
+    return lib
+
+
+def probe_names() -> list[str]:
+    return list(_PROBE_SIGS)
 
 
 def load(path: Path | str | None = None) -> C.CDLL:

@@ -17,8 +17,10 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 BUILD = PKG / "_build"
-SOURCES = ["swfd_api.cu", "swfd_kernels.cu", "swfd_sweep.cu", "swfd_control.cu", "swfd_probe.cu",
+SOURCES = ["swfd_api.cu", "swfd_kernels.cu", "swfd_sweep.cu", "swfd_control.cu",
            "swfd_static.cu", "swfd_batch.cu", "swfd_matlab1d.cu", "swfd_ex7.cu"]
+# measurement and test probes (include/swfd_probe.h): a library of their own
+PROBE_SOURCES = ["swfd_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
@@ -36,7 +38,7 @@ def nvcc() -> str:
 def _stale(obj: Path, src: Path) -> bool:
     if not obj.exists():
         return True
-    deps = [src, *CSRC.glob("*.h"), *CSRC.glob("*.cuh"), PKG.parent / "include" / "swfd.h",
+    deps = [src, *CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(PKG.parent / "include").glob("*.h"),
             Path(__file__)]
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps if d.exists())
 
@@ -48,7 +50,7 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
     cc = nvcc()
     flags = NVCC_FLAGS + list(extra_flags or [])
     jobs = []
-    for name in SOURCES:
+    for name in SOURCES + PROBE_SOURCES:
         src = CSRC / name
         obj = BUILD / (Path(name).stem + ".o")
         if force or _stale(obj, src):
@@ -72,6 +74,16 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
             print(r.stdout, r.stderr)
         if r.returncode != 0:
             raise RuntimeError("nvcc link of libswfd.so failed")
+    probe = OUT / "libswfd_probe.so"
+    pobjs = [str(BUILD / (Path(n).stem + ".o")) for n in PROBE_SOURCES]
+    if force or jobs or not probe.exists():
+        cmd = [cc, *ARCH, "-shared", "-o", str(probe), *pobjs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            print(" ".join(cmd))
+            print(r.stdout, r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc link of libswfd_probe.so failed")
     # the C host request loop over the batch API (host/swfd_serve.c)
     serve, src = OUT / "swfd_serve", PKG / "host" / "swfd_serve.c"
     if force or not serve.exists() or serve.stat().st_mtime < max(src.stat().st_mtime,

@@ -22,7 +22,10 @@
 //    array and corrupt each other's results: order them on one stream;
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//    before any stream capture begins.  Later calls on a stream that is not
+//    capturing look it up again, so a context torn down by cudaDeviceReset
+//    and created anew is followed; a call made while the stream captures
+//    uses the address of the last call outside capture.
 #include <mutex>
 #include <string>
 
@@ -46,10 +49,20 @@ swfd_status static_fail(swfd_status st, const std::string& m) {
   return st;
 }
 
-// device address of g_static_scratch on `dev` (dev must be current)
-cudaError_t static_scratch_addr(int dev, void** out) {
+// device address of g_static_scratch on `dev` (dev must be current).  Outside
+// stream capture the address is looked up every time (a cudaDeviceReset
+// unloads the module, and the next context may place the array elsewhere);
+// during capture the address of the last lookup is used, and a first call on
+// a device made during capture is refused.
+cudaError_t static_scratch_addr(int dev, cudaStream_t s, void** out) {
   std::lock_guard<std::mutex> lk(g_static_mu);
-  if (!g_static_addr[dev]) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const bool capturing = cudaStreamIsCapturing(s, &cs) != cudaSuccess ||
+                         cs != cudaStreamCaptureStatusNone;
+  if (capturing) {
+    cudaGetLastError();  // a refused capture query leaves no sticky error
+    if (!g_static_addr[dev]) return cudaErrorStreamCaptureUnsupported;
+  } else {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess) return e;
@@ -104,8 +117,9 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
     if (s != SWFD_OK) return static_fail(s, std::string(what) + ": " + cudaGetErrorString(ce));
     return SWFD_OK;
   };
+  cudaStream_t s = (cudaStream_t)stream;
   void* base = nullptr;
-  if ((e = static_scratch_addr(cfg->device, &base)) != cudaSuccess)
+  if ((e = static_scratch_addr(cfg->device, s, &base)) != cudaSuccess)
     return done(SWFD_ERR_CUDA, "cudaGetSymbolAddress", e);
   char* c = (char*)base;
   DevScalars* dsc = (DevScalars*)c;
@@ -119,10 +133,12 @@ extern "C" swfd_status swfd_flux_divergence_static(const swfd_config* cfg, const
   double* flux = (double*)c;
   c += 4 * g.nc * plane_b;
   double* rsoa = (double*)c;
-  // the plane pitch used by the kernels must match the carved planes
+  // the plane pitch used by the kernels must match the carved planes; the
+  // split and flux planes (geometry sg) equal the state's here (problems with
+  // rank segments are refused above)
   Params q = p;
   q.g.plane = (int64_t)(plane_b / sizeof(double));
-  cudaStream_t s = (cudaStream_t)stream;
+  q.sg = q.g;
   // the previous call's scalars (alpha accumulator, error word) start at zero
   if ((e = cudaMemsetAsync(dsc, 0, sizeof(DevScalars), s)) != cudaSuccess)
     return done(SWFD_ERR_CUDA, "cudaMemsetAsync", e);

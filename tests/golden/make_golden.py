@@ -1,6 +1,7 @@
-"""Generate the golden fixtures of the CPU oracle (small problems).
+"""Generate the golden fixtures of the CPU oracle.
 
-    python -m tests.golden.make_golden
+    python -m tests.golden.make_golden            # the small runs (seconds)
+    python -m tests.golden.make_golden --jet-full # the 800x200 jet to T (~40 min, one core)
 
 Each fixture stores the final state, the sweep statistics and tracks, the
 time and the last dt of one small run of the oracle.  The reference ships no
@@ -53,10 +54,47 @@ def run_case(oracle_mod, name):
     }
 
 
+def state_digest(u):
+    """SHA-256 of the state's bytes (C order, float64, little endian) and the
+    per-row sums of each component, so that a mismatch can be located."""
+    import hashlib
+    u = np.ascontiguousarray(u, np.float64)
+    return hashlib.sha256(u.astype("<f8").tobytes()).hexdigest(), u.sum(axis=1)
+
+
+def jet_full(oracle_mod):
+    """The jet of ex5_mach2000_jet at its configured size (800x200 half domain,
+    T=0.001) run to T by the oracle: step count, time, last dt, the
+    statistics block, the three tracks and a digest of the final state."""
+    import time as _time
+    o = oracle_mod.Oracle(problems.workload("jet"))
+    o.init_problem()
+    t0 = _time.time()
+    steps = o.run()
+    wall = _time.time() - t0
+    st = o.stats()
+    tr = o.tracks()
+    sha, rows = state_digest(o.state())
+    return {
+        "steps": np.array([steps], np.int64),
+        "stats": np.array([st[k] for k in sorted(st)], np.int64),
+        "sweep_track": tr[0], "neg_track": tr[1], "pos_track": tr[2],
+        "time": np.array([o.time]), "dt": np.array([o.dt]),
+        "state_sha256": np.array(sha), "row_sums": rows,
+        "oracle_wall_s": np.array([wall]),
+    }
+
+
 def main():
     import oracle
     oracle.build()
     out = Path(__file__).resolve().parent
+    if "--jet-full" in sys.argv:
+        d = jet_full(oracle)
+        np.savez_compressed(out / "jet_800x200_to_T.npz", **d)
+        print("jet_800x200_to_T steps", d["steps"][0], "time", d["time"][0],
+              "wall", d["oracle_wall_s"][0], "sha", str(d["state_sha256"]))
+        return
     for name in CASES:
         d = run_case(oracle, name)
         np.savez_compressed(out / f"{name}.npz", **d)

@@ -8,10 +8,11 @@ import pytest
 from sweeping_fd_weno_gb300 import abi, problems
 
 HEADER = abi.LIB_PATH.parents[2] / "include" / "swfd.h"
+PROBE_HEADER = abi.LIB_PATH.parents[2] / "include" / "swfd_probe.h"
 
 
-def declared_functions():
-    text = HEADER.read_text()
+def declared_functions(header=HEADER):
+    text = header.read_text()
     return sorted(set(re.findall(r"^\s*(?:swfd_status|const char\*)\s+(swfd_\w+)\s*\(", text, re.M)))
 
 
@@ -22,6 +23,20 @@ def test_library_exports_every_declared_symbol(swfd):
     for n in names:
         assert hasattr(lib, n), n
     assert sorted(abi.exported_names()) == names
+
+
+def test_probe_library_is_apart_from_the_product(swfd):
+    names = declared_functions(PROBE_HEADER)
+    assert names == sorted(abi.probe_names())
+    probe = abi.load_probe()
+    for n in names:
+        assert hasattr(probe, n), n
+    # the product library exports none of them
+    import subprocess
+    syms = subprocess.run(["nm", "-D", "--defined-only", str(abi.LIB_PATH)], capture_output=True,
+                          text=True).stdout
+    for n in names:
+        assert f" {n}\n" not in syms, n
 
 
 @pytest.mark.parametrize("problem", [abi.MATLAB_1D, abi.SEDOV_1D, abi.VORTEX_2D, abi.SEDOV_2D,

@@ -20,7 +20,7 @@ def test_rcp_bulk_is_the_ieee_reciprocal(swfd):
     ])
     out = np.empty_like(x)
     dp = C.POINTER(C.c_double)
-    st = abi.load().swfd_probe_rcp_bulk(0, x.ctypes.data_as(dp), x.size, out.ctypes.data_as(dp))
+    st = abi.load_probe().swfd_probe_rcp_bulk(0, x.ctypes.data_as(dp), x.size, out.ctypes.data_as(dp))
     assert st == abi.OK
     with np.errstate(divide="ignore", over="ignore"):
         ref = 1.0 / x
@@ -44,7 +44,7 @@ def test_conversions_match_hardware(swfd):
     f = np.empty(x.size, np.float32)
     d = np.empty(x.size, np.float64)
     dp = C.POINTER(C.c_double)
-    st = abi.load().swfd_probe_convert(0, x.ctypes.data_as(dp), x.size,
+    st = abi.load_probe().swfd_probe_convert(0, x.ctypes.data_as(dp), x.size,
                                        f.ctypes.data_as(C.POINTER(C.c_float)), d.ctypes.data_as(dp))
     assert st == 0
     with np.errstate(over="ignore", invalid="ignore"):
