@@ -14,8 +14,10 @@ shard within one grid); the value is the sum of all ranks' work over the
 slowest rank's time.
 
 --impl reference times the reference's algorithm on the host CPU instead: the
-CPU restatement of the reference in its quad-literal mode (the arithmetic of
-the reference's -fdefault-real-8 build), one RK3 step of the vortex per step.
+CPU restatement of the reference (the oracle) on the same 360x360 vortex with
+the same binary64 literals as the GPU line, one solve per host core; beside it
+the binary128-literal pair (the arithmetic of the reference's -fdefault-real-8
+build) on the same grid.
 """
 from __future__ import annotations
 
@@ -340,6 +342,172 @@ def bench_batched_full(args, local):
             "completion_p99_s": float(np.percentile(t, 99)) if len(t) else None}
 
 
+def bench_accuracy(args, local):
+    """The vortex accuracy table: the near-vacuum vortex at 45^2..360^2 to
+    T = 0.01 in plain FP64 and in FP32-bulk on the GPU, with the L1 and Linf
+    density errors against the exact translated solution and the observed
+    orders between successive grids (the methodology of
+    ex3_vortex_accuracy_2d/main.f90:725-777), and the FP32-bulk state's errors
+    against the FP64 state at T."""
+    import math
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, abi, output, problems
+    rows, prev = [], {}
+    for n in args.accuracy_sizes:
+        row, states = {"n": n}, {}
+        for name, prec in (("fp64", abi.PRECISION_FP64), ("fp32_bulk", abi.PRECISION_FP32_BULK)):
+            s = Solver(problems.workload(f"vortex{n}", device=local, precision=prec))
+            s.init_problem()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            steps = s.run()
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            u, t = s.state(), s.time
+            s.close()
+            l1, linf = output.vortex_errors(u, t)
+            r = {"steps": steps, "t": t, "l1": l1, "linf": linf, "gpu_s": wall}
+            if name in prev:
+                pn, pl1, plinf = prev[name]
+                r["order_l1"] = math.log(pl1 / l1) / math.log(n / pn)
+                r["order_linf"] = math.log(plinf / linf) / math.log(n / pn)
+            prev[name] = (n, l1, linf)
+            states[name] = u
+            row[name] = r
+        row["fp32_bulk_vs_fp64"] = precision_errors(states["fp32_bulk"], states["fp64"])
+        rows.append(row)
+    return {"workload": "near-vacuum vortex (eps 10.0828, min density ~7.8e-15), periodic "
+                        "[0,10]^2, mean flow (1,1), T=0.01, dt = dx^(5/3)*0.5/alpha",
+            "errors": "density against the exact translated vortex at the final time: L1 the "
+                      "mean absolute error, Linf the maximum; orders log(e_coarse/e_fine) / "
+                      "log(n_fine/n_coarse)",
+            "table": rows}
+
+
+def bench_sedov_precision(args, local):
+    """The FP32-bulk batch's error at a late time: a seeded sample of the
+    point-energy instances (the 640^2 one included) is run to T = 1 in the
+    FP32-bulk batch to learn each instance's step count; then every instance
+    runs to the common time T_s by which all of them have taken at least a
+    quarter of those steps, in the FP32-bulk batch and in plain FP64 one at a
+    time (the oracle's arithmetic), and the FP32-bulk states are compared with
+    the FP64 ones (L1/Linf density and pressure, mass and energy drift)."""
+    import numpy as np
+    import torch
+    from sweeping_fd_weno_gb300 import Batch, Solver, abi, problems
+    sizes = point_energy_sizes(args.batch_instances)
+    rng = np.random.default_rng(BATCH_SEED + 2)
+    pick = [int(n) for n in rng.choice(sorted(set(sizes) - {640}), size=args.late_sample - 1,
+                                       replace=False)] + [640]
+    cfg_of = lambda n, **kw: problems.make_config(abi.SEDOV_2D, nx=n, ny=n, device=local, **kw)
+    # 1. step counts to T = 1 in the FP32-bulk batch, with (time, steps) samples
+    t0 = time.perf_counter()
+    hist = {k: [(0.0, 0)] for k in range(len(pick))}
+    with Batch(max_slots=len(pick), max_nx=640, max_ny=640, precision=abi.PRECISION_FP32_BULK,
+               ubar_mode=abi.UBAR_TREE, device=local) as b:
+        for k, n in enumerate(pick):
+            assert b.admit(cfg_of(n), k)
+        done = set()
+        while len(done) < len(pick):
+            b.run(args.batch_chunk)
+            for k in range(len(pick)):
+                if k not in done:
+                    hist[k].append(b.progress(k))
+            for rid, st in b.poll():
+                if st != 0:
+                    raise RuntimeError(f"instance {pick[rid]}^2 failed with status {st}")
+                done.add(rid)
+    steps_t1 = [hist[k][-1][1] for k in range(len(pick))]
+    t_quarter = [next(t for t, st in hist[k] if st >= 0.25 * steps_t1[k])
+                 for k in range(len(pick))]
+    ts = float(f"{max(t_quarter):.2g}")
+    if any(next(st for t, st in hist[k] if t >= ts) < 0.25 * steps_t1[k] for k in range(len(pick))):
+        ts = float(f"{max(t_quarter):.3g}")
+    find_s = time.perf_counter() - t0
+    # 2. every instance to T_s: FP32-bulk batch and plain FP64 one at a time
+    t1 = time.perf_counter()
+    u32 = {}
+    with Batch(max_slots=len(pick), max_nx=640, max_ny=640, precision=abi.PRECISION_FP32_BULK,
+               ubar_mode=abi.UBAR_TREE, device=local) as b:
+        for k, n in enumerate(pick):
+            assert b.admit(cfg_of(n, time_terminal=ts), k)
+        left = set(range(len(pick)))
+        while left:
+            b.run(args.batch_chunk)
+            for rid, st in b.poll():
+                if st != 0:
+                    raise RuntimeError(f"instance {pick[rid]}^2 failed with status {st}")
+                u32[rid] = (b.download(rid)[0], b.progress(rid)[1], b.stats(rid))
+                left.discard(rid)
+    fp32_s = time.perf_counter() - t1
+    out = {}
+    t2 = time.perf_counter()
+    for k, n in enumerate(pick):
+        with Solver(cfg_of(n, time_terminal=ts)) as s:
+            s.init_problem()
+            steps64 = s.run()
+            u64, st64 = s.state(), s.stats()
+        ua, steps32, st32 = u32[k]
+        e = precision_errors(ua, u64)
+        e.update({"steps_to_T1_fp32": steps_t1[k], "steps_to_Ts_fp32": steps32,
+                  "steps_to_Ts_fp64": steps64, "quarter_reached_at": t_quarter[k],
+                  "sweeps_fp32": st32["sweep_count"], "sweeps_fp64": st64["sweep_count"]})
+        out[f"{n}^2"] = e
+    fp64_s = time.perf_counter() - t2
+    worst = max(v["rel_l1_density"] for v in out.values())
+    return {"workload": f"{len(pick)} of the point-energy instances (seeded sample, 640^2 "
+                        "included) to a common late time",
+            "T_s": ts, "instances": out, "worst_rel_l1_density": worst,
+            "accepted_at_1e-6": bool(worst < 1e-6),
+            "fp32": "FP32-bulk batch (tree u_bar)", "fp64": "plain FP64, one at a time "
+            "(sequential u_bar: the oracle's arithmetic)",
+            "seconds": {"steps_to_T1": find_s, "fp32_to_Ts": fp32_s, "fp64_to_Ts": fp64_s}}
+
+
+def profile_jet(args, local):
+    """Launch-list mode for the sweep-heavy jet: the 800x200 jet advances
+    --profile-after steps as graphs, its state moves to a solver that runs its
+    sections as plain stream launches (SWFD_LAUNCH=eager: the same kernels and
+    arguments, conditions read on the host; profilers see every kernel), and
+    --profile-steps steps run between cudaProfilerStart and cudaProfilerStop.
+    Under `ncu --profile-from-start off` only those steps' launches are
+    captured.  Prints one JSON line describing the window."""
+    import torch
+    from sweeping_fd_weno_gb300 import Solver, problems
+    torch.cuda.set_device(local)
+    with Solver(problems.workload("jet", device=local)) as g:
+        g.init_problem()
+        g.run(args.profile_after)
+        u, t, n0 = g.state(), g.time, g.stats()
+    prev = os.environ.get("SWFD_LAUNCH")
+    os.environ["SWFD_LAUNCH"] = "eager"
+    try:
+        e = Solver(problems.workload("jet", device=local))
+    finally:
+        if prev is None:
+            del os.environ["SWFD_LAUNCH"]
+        else:
+            os.environ["SWFD_LAUNCH"] = prev
+    with e:
+        e.set_state(u)
+        e.time = t
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        for _ in range(args.profile_steps):
+            e.step()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        torch.cuda.profiler.stop()
+        st = e.stats()
+    print(json.dumps({"mode": "profile_jet", "after_steps": args.profile_after,
+                      "steps": args.profile_steps, "wall_ms_per_step_eager":
+                      wall * 1e3 / args.profile_steps, "sweeps": st["sweep_count"],
+                      "sweep_pairs": st["pre_count"], "max_neg": st["max_neg"],
+                      "time_at_start": t, "stats_before": n0}))
+    return 0
+
+
 def serving_draw(device, plain_fp64=False):
     """Requests of the serving mix, drawn uniformly from three problems: the
     vortex (45^2..360^2, T=0.01), a point-energy instance (128^2..640^2,
@@ -593,11 +761,12 @@ def bench_serving(args, local):
 
 
 def _reference_worker(args):
-    """One serial reference-arithmetic solve (a worker of the reference arm)."""
-    n, warmup, steps = args
+    """One serial solve of the reference's algorithm (a worker of the reference
+    arm): warm-up steps, then the timed steps."""
+    n, warmup, steps, literals = args
     import oracle
     from sweeping_fd_weno_gb300 import problems
-    o = oracle.Oracle(problems.workload(f"vortex{n}", literals=1))
+    o = oracle.Oracle(problems.workload(f"vortex{n}", literals=literals))
     o.init_problem()
     for _ in range(warmup):
         o.step()
@@ -607,35 +776,63 @@ def _reference_worker(args):
     return n * n * 3 * steps, time.perf_counter() - t0
 
 
+# the workload description both arms print (the driver pairs the lines on it)
+L2_NOTE = ("GPU arm: L2 flushed between timed steps (256 MiB write); CPU arm: each core's "
+           "solve resident in its own caches and DRAM")
+
+
+def bench_config(workload, precision, nx, ny, n_gpus):
+    return {"workload": f"{workload}_{precision}", "nx": nx, "ny": ny, "stages_per_step": 3,
+            "precision": "plain FP64 (double literals)" if precision == "fp64"
+            else "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, sweeps)",
+            "l2": L2_NOTE,
+            "parallelism": f"GPU arm: replicas x{n_gpus} (one grid per GPU); CPU arm: one solve "
+                           "per host core"}
+
+
+def reference_pool(n, warmup, steps, literals, cores):
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(cores) as pool:
+        out = pool.map(_reference_worker, [(n, warmup, steps, literals)] * cores)
+    return sum(u for u, _ in out), max(t for _, t in out)
+
+
 def run_reference(args, rank):
-    """The reference's algorithm on the host CPU: the CPU restatement in its
-    quad-literal mode (the arithmetic of the reference's -fdefault-real-8
-    build).  The reference's vortex program is serial, so every host core runs
-    its own solve; the value is all cores' updates over the slowest core's
-    timed steps."""
+    """The reference's algorithm on the host CPU: its CPU restatement (the
+    oracle) on the GPU line's workload -- the 360x360 vortex with binary64
+    literals, the GPU line's arithmetic -- with every host core running its
+    own solve (the reference's vortex program is serial); the value is all
+    cores' updates over the slowest core's timed steps.  Beside it, the
+    binary128-literal pair: the same grid in the arithmetic of the reference's
+    -fdefault-real-8 build, against which the GPU line's quad_literals leg
+    compares."""
     if rank != 0:
         return 0
-    import multiprocessing as mp
     import oracle
     oracle.build()
-    n = args.reference_nx
+    n = args.reference_nx or int(args.workload[len("vortex"):] or 180)
     cores = os.cpu_count() or 1
-    with mp.get_context("spawn").Pool(cores) as pool:
-        out = pool.map(_reference_worker, [(n, args.warmup, args.steps)] * cores)
-    upd = sum(u for u, _ in out)
-    el = max(t for _, t in out)
+    upd, el = reference_pool(n, args.warmup, args.steps, 0, cores)
     v = upd / el
+    qsteps = max(1, args.reference_quad_steps)
+    qupd, qel = reference_pool(n, 0, qsteps, 1, cores)
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex",
-        "config": {"workload": "vortex360_fp64", "sample_nx": n, "ny": n},
+        "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex (no dataset)",
+        "config": bench_config(args.workload, "fp64", n, n, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} SSP-RK3 steps of a {n}x{n} vortex per core "
-                                   f"({cores} independent solves), REAL(16) literals as the "
-                                   "reference's -fdefault-real-8 build; the reference itself is "
-                                   "serial Fortran and no Fortran compiler exists here"},
+                         "sample": f"{args.steps} SSP-RK3 steps (after {args.warmup} untimed) of "
+                                   f"the {n}x{n} vortex per core, {cores} independent solves, "
+                                   "binary64 literals (the GPU line's arithmetic); the reference "
+                                   "itself is serial Fortran and no Fortran compiler exists "
+                                   "here or on the GPU box"},
+        "quad_literals": {"value": qupd / qel, "unit": UNIT, "cores": cores, "kind": "port",
+                          "ms_per_step": qel * 1e3 / qsteps,
+                          "sample": f"{qsteps} SSP-RK3 step(s) of the {n}x{n} vortex per core, "
+                                    "binary128 literals (the reference's -fdefault-real-8 "
+                                    "build); pairs with the GPU line's quad_literals leg"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -652,7 +849,10 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_bulk"],
                     help="arithmetic of the main measurement (the headline is fp64)")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--reference-nx", type=int, default=180)
+    ap.add_argument("--reference-nx", type=int, default=0,
+                    help="grid of the reference arm (default: the workload's own)")
+    ap.add_argument("--reference-quad-steps", type=int, default=1,
+                    help="binary128-literal steps per core of the reference arm (~4 s each)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
@@ -673,6 +873,15 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-chunk", type=int, default=4)
+    ap.add_argument("--profile-jet", action="store_true",
+                    help="launch-list mode: jet steps as plain launches inside a profiler range")
+    ap.add_argument("--profile-after", type=int, default=1000)
+    ap.add_argument("--profile-steps", type=int, default=20)
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-sizes", type=int, nargs="+", default=[45, 90, 180, 360])
+    ap.add_argument("--no-late-precision", action="store_true")
+    ap.add_argument("--late-sample", type=int, default=8,
+                    help="point-energy instances of the late-time FP32-bulk error sample")
     ap.add_argument("--batch-full", action="store_true",
                     help="also run the point-energy batch to T=1 (minutes)")
     ap.add_argument("--batch-chunk", type=int, default=64)
@@ -684,6 +893,8 @@ def main():
     rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.profile_jet:
+        return profile_jet(args, local)
 
     import numpy as np
     import torch
@@ -912,13 +1123,8 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic: ex3 initdata of the near-vacuum isentropic vortex (no dataset)",
-        "config": {"workload": f"{args.workload}_{args.precision}", "nx": solver.nx,
-                   "ny": solver.ny, "stages_per_step": 3,
-                   "precision": "plain FP64 (double literals)" if args.precision == "fp64"
-                   else "FP32-bulk (FP32 fluxes; FP64 pressure, RK accumulation, sweeps)",
-                   "l2": "flushed between timed steps (256 MiB write)",
-                   "flux_min_blocks": flux_min_blocks,
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(args.workload, args.precision, solver.nx, solver.ny, world),
+        "tuning": {"flux_min_blocks": flux_min_blocks},
         "clocks": clk,
         "e2e": e2e,
         "gpu_launches": prof["kernel_launches"],
@@ -934,6 +1140,10 @@ def main():
                 point_energy_sizes(args.batch_instances))
     if not args.no_serving:
         line["serving"] = bench_serving(args, local)
+    if not args.no_accuracy:
+        line["accuracy"] = bench_accuracy(args, local)
+    if not args.no_late_precision:
+        line["late_precision"] = bench_sedov_precision(args, local)
     if args.batch_full:
         line["batched_to_completion"] = bench_batched_full(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -135,7 +135,11 @@ typedef struct swfd_config {
                             from u0 with dt/2; no sweeps).  2 is 1D only. */
   int32_t variant;       /* SWFD_PROBLEM_MATLAB_1D: the script's `problem` (1 linear
                             advection, 2 nonlinear, 3 Sod, 4 Lax, 5 double rarefaction,
-                            6 point energy, 7 jet ambient state); 0 otherwise */
+                            6 point energy, 7 jet ambient state);
+                            SWFD_PROBLEM_JET_2D: 0 the reference's upper half domain
+                            [0,1]x[0,0.25] with its y = 0 symmetry plane, 1 the full
+                            domain [0,1]x[-0.25,0.25] (inflow for |y| <= 0.05, outflow
+                            at the bottom; ny counts the whole height); 0 otherwise */
   int32_t reserved[2];   /* zero */
 } swfd_config;
 

@@ -561,9 +561,13 @@ static void bc2d(oracle* o) {
       for (int i = -2; i <= nx + 3; ++i)
         for (int c = 0; c < 4; ++c) U(u, c, i, ny + ig) = U(u, c, i, ny);
   } else if (o->problem == SWFD_PROBLEM_JET_2D) {
+    /* variant 1: the full domain [0,1]x[-0.25,0.25] of the jet (inflow for
+     * |y| <= 0.05, outflow at the bottom in place of the y = 0 symmetry
+     * plane); the loops and their order are the half domain's */
+    const int full = o->cfg.variant == 1;
     const double ujet = 800.;
     for (int j = -2; j <= ny + 3; ++j) {
-      if (o->y[j + 2] <= 0.05) {
+      if (full ? fabs(o->y[j + 2]) <= 0.05 : o->y[j + 2] <= 0.05) {
         for (int i = 1; i <= 3; ++i) {
           U(u, 0, 1 - i, j) = 5.;
           U(u, 1, 1 - i, j) = 5. * ujet;
@@ -580,11 +584,17 @@ static void bc2d(oracle* o) {
         }
       }
     }
-    for (int j = 1; j <= 3; ++j)
-      for (int i = -2; i <= nx + 3; ++i) {
-        for (int c = 0; c < 4; ++c) U(u, c, i, 1 - j) = U(u, c, i, j);
-        U(u, 2, i, 1 - j) = -U(u, 2, i, j);
-      }
+    if (full) {
+      for (int ig = 1; ig <= 3; ++ig)
+        for (int i = -2; i <= nx + 3; ++i)
+          for (int c = 0; c < 4; ++c) U(u, c, i, 1 - ig) = U(u, c, i, 1);
+    } else {
+      for (int j = 1; j <= 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) {
+          for (int c = 0; c < 4; ++c) U(u, c, i, 1 - j) = U(u, c, i, j);
+          U(u, 2, i, 1 - j) = -U(u, 2, i, j);
+        }
+    }
     for (int ig = 1; ig <= 3; ++ig)
       for (int j = -2; j <= ny + 3; ++j)
         for (int c = 0; c < 4; ++c) U(u, c, nx + ig, j) = U(u, c, nx, j);
@@ -2608,8 +2618,9 @@ void oracle_init(oracle* o) {
     case SWFD_PROBLEM_DETONATION:
       ex7_init(o);
       break;
-    case SWFD_PROBLEM_JET_2D: { /* ex5_mach2000_jet/main.f90:744-768 */
-      double xleft = 0., xright = 1., yleft = 0., yright = 0.25;
+    case SWFD_PROBLEM_JET_2D: { /* ex5_mach2000_jet/main.f90:744-768; variant 1 the full
+                                   domain y in [-0.25, 0.25] */
+      double xleft = 0., xright = 1., yleft = o->cfg.variant == 1 ? -0.25 : 0., yright = 0.25;
       o->dx = (xright - xleft) / nx;
       o->dy = (yright - yleft) / ny;
       for (int i = -2; i <= nx + 3; ++i) o->x[i + 2] = xleft + i * o->dx - o->dx / 2.;

@@ -66,6 +66,8 @@ swfd_status check_config(const swfd_config& c, std::string& err) {
       return bad(SWFD_ERR_UNSUPPORTED, "the MATLAB script's scheme runs in FP64 only");
     if (c.rk_choice == 2) return bad(SWFD_ERR_INVALID, "rk_choice 2 (the restart RK) exists only in ex2");
   }
+  if (c.problem == SWFD_PROBLEM_JET_2D && c.variant != 0 && c.variant != 1)
+    return bad(SWFD_ERR_INVALID, "variant: 0 (the reference's half domain) or 1 (full domain)");
   if (c.rk_choice == 2 && c.problem != SWFD_PROBLEM_SEDOV_1D)
     return bad(SWFD_ERR_INVALID, "rk_choice 2 (the dt-halving restart RK) exists only in ex2");
   if (c.problem == SWFD_PROBLEM_DETONATION) return ex7_check(c, err);
@@ -193,16 +195,28 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
         p.inflow[2] = 0.;
         p.inflow[3] = ple / p.gamma1 + 0.5 * dle * (ule * ule);
       } else {
+        // variant 1: the full domain y in [-0.25, 0.25] (inflow for
+        // |y| <= 0.05, outflow at the bottom) in place of the reference's
+        // upper half with its y = 0 symmetry plane
+        const double yleft = c.variant == 1 ? -0.25 : 0.;
+        p.jet_full = c.variant == 1;
         p.dx = (1. - 0.) / c.nx;  // ex5_mach2000_jet/main.f90:748-754
-        p.dy = (0.25 - 0.) / c.ny;
+        p.dy = (0.25 - yleft) / c.ny;
         p.dt_rule = 4;
         p.alpha_guarded = 1;
         p.pos_strict = 1;
         p.exit_ge = 1;
-        // inflow rows: y(j) = yleft + j*dy - dy/2 <= 0.05 (:703)
+        // inflow rows: y(j) = yleft + j*dy - dy/2 <= 0.05 (:703); full
+        // domain |y(j)| <= 0.05.  Rows jet_jmin..jet_jmax.
+        p.jet_jmin = c.ny + 4;
         p.jet_jmax = -3;
-        for (int j = -2; j <= c.ny + 3; ++j)
-          if (0. + j * p.dy - p.dy / 2. <= 0.05) p.jet_jmax = j;
+        for (int j = -2; j <= c.ny + 3; ++j) {
+          const double y = yleft + j * p.dy - p.dy / 2.;
+          if (p.jet_full ? fabs(y) <= 0.05 : y <= 0.05) {
+            p.jet_jmin = std::min(p.jet_jmin, j);
+            p.jet_jmax = j;
+          }
+        }
         const double ujet = 800.;
         p.jet_in[0] = 5.;
         p.jet_in[1] = 5. * ujet;

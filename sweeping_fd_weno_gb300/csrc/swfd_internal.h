@@ -59,7 +59,9 @@ struct Params {
   double dt_num_y = 0;   // dy*cfl
   double time_terminal = 0;
   // jet inflow (ex5_mach2000_jet/main.f90:702-719)
-  int jet_jmax = 0;      // y(j) <= 0.05  <=>  j <= jet_jmax
+  int jet_jmax = 0;      // y(j) <= 0.05  <=>  j <= jet_jmax (half domain)
+  int jet_jmin = -2;     // full domain: |y(j)| <= 0.05  <=>  jet_jmin <= j <= jet_jmax
+  int jet_full = 0;      // variant 1: full domain, outflow at the bottom
   double jet_in[4] = {0, 0, 0, 0};
   double jet_amb[4] = {0, 0, 0, 0};
   int stop_sweep = 0;    // P(u_bar) <= 0 and swp_num exhaustion stop the run (ex4, ex6)

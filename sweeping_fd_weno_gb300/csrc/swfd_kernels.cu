@@ -61,14 +61,18 @@ __device__ __forceinline__ void bc2d_cell(const Params& p, double* __restrict__ 
     int ii = i, jj = j;
     if (jj > ny) jj = ny;             // top outflow copies row ny
     if (ii > nx) ii = nx;             // right outflow copies column nx
-    if (jj < 1) {                     // bottom reflect of row 1-j
-      jj = 1 - jj;
-      sgn[2] = -1.;
+    if (jj < 1) {
+      if (p.jet_full) {               // full-domain jet: bottom outflow copies row 1
+        jj = 1;
+      } else {                        // bottom reflect of row 1-j
+        jj = 1 - jj;
+        sgn[2] = -1.;
+      }
     }
     if (ii < 1) {
       if (jet) {
         // inflow state of row jj, then (if jj came from the bottom) mirrored
-        const double* s = (jj <= p.jet_jmax) ? p.jet_in : p.jet_amb;
+        const double* s = (jj >= p.jet_jmin && jj <= p.jet_jmax) ? p.jet_in : p.jet_amb;
         for (int c = 0; c < 4; ++c) v[c] = s[c];
         fixed = true;
       } else {

@@ -125,6 +125,26 @@ def vortex_exact(x: float, y: float, t: float, gamma: float = 1.4):
     return e1, e2, e3, e4
 
 
+def vortex_errors(u, t: float, gamma: float = 1.4):
+    """L1 (mean over the interior) and Linf density errors of a vortex state
+    u(-2:ny+3, -2:nx+3, 4) against `exact` at time t, as
+    ex3_vortex_accuracy_2d/main.f90:725-745 computes them (vectorised; the
+    exact density follows vortex_exact's formula)."""
+    import numpy as np
+    ny, nx = u.shape[0] - 6, u.shape[1] - 6
+    dx, dy = 10. / nx, 10. / ny
+    x = np.arange(1, nx + 1) * dx - dx / 2.
+    y = np.arange(1, ny + 1) * dy - dy / 2.
+    X, Y = np.meshgrid(x, y)
+    g1 = gamma - 1.0
+    pi = 3.14159265358979323846264338327950
+    r2 = (X - 5. - t) * (X - 5. - t) + (Y - 5. - t) * (Y - 5. - t)
+    mag = 10.0828
+    e1 = np.power(1 - g1 * (mag * mag) / 8. / gamma / (pi * pi) * np.exp(1. - r2), 1. / g1)
+    d = np.abs(e1 - u[3:ny + 3, 3:nx + 3, 0])
+    return float(d.sum() / nx / ny), float(d.max())
+
+
 def _read_fort7(path: Path):
     """read (7, '(6e13.5)') er1old, eriold"""
     txt = path.read_text() if path.exists() else ""

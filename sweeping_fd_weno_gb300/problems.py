@@ -107,6 +107,10 @@ def workload(name: str, **overrides) -> abi.SwfdConfig:
     if name == "jet":
         # Mach-2000-type jet, 800x200 half domain with the y=0 symmetry plane, T=0.001
         return make_config(abi.JET_2D, **overrides)
+    if name == "jet_full":
+        # the same jet on the full domain [0,1]x[-0.25,0.25] at 800x400 (inflow for
+        # |y| <= 0.05, outflow at the bottom instead of the symmetry plane)
+        return make_config(abi.JET_2D, **dict(dict(ny=400, variant=1), **overrides))
     if name.startswith("shock"):
         # Mach 5.09 shock diffraction around a step; name 'shock<total>'
         # (total 20..80: 260x216 .. 1040x880 cells)

@@ -18,6 +18,8 @@ CASES = {
     "vortex64x48": dict(problem=abi.VORTEX_2D, nx=64, ny=48),
     "sedov2d_40": dict(problem=abi.SEDOV_2D, nx=40, ny=40),
     "jet_96x24": dict(problem=abi.JET_2D, nx=96, ny=24),
+    # the jet's full domain [0,1]x[-0.25,0.25] (variant 1)
+    "jet_full_96x48": dict(problem=abi.JET_2D, nx=96, ny=48, variant=1),
     "sedov1d_200": dict(problem=abi.SEDOV_1D, nx=200, cfl=0.6, swp_num=2, e_background=1e-12),
     "sedov1d_ref": dict(problem=abi.SEDOV_1D, nx=160),
 }
