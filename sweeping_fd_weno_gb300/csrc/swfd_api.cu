@@ -533,7 +533,7 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
       b.k(1);
     } else {
       int n = 0;
-      B_OK(b, launch_density_sweep_par(p, u, h->sweep_scratch, sd, &n));
+      B_OK(b, launch_density_sweep_par(p, u, h->sweep_scratch, h->sweep_cluster, sd, &n));
       b.k(n);
     }
     if (p.g.ndim == 1) {
@@ -566,8 +566,10 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
       b.k(2);
     } else {
       int n = 0;
-      B_OK(b, launch_pressure_pass_par(p, u, -1, 1, h->sweep_scratch, h->dsc, sq, &n));
-      B_OK(b, launch_pressure_pass_par(p, u, -1, 0, h->sweep_scratch, h->dsc, sq, &n));
+      B_OK(b, launch_pressure_pass_par(p, u, -1, 1, h->sweep_scratch, h->sweep_cluster, h->dsc,
+                                       sq, &n));
+      B_OK(b, launch_pressure_pass_par(p, u, -1, 0, h->sweep_scratch, h->sweep_cluster, h->dsc,
+                                       sq, &n));
       b.k(n);
     }
     B_OK(b, launch_exit_count(p, u, h->dsc, sq));
@@ -995,6 +997,9 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if ((e = cudaMalloc(&h->d_stage, hb)) != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaMalloc(&h->sweep_scratch, sweep_scratch_bytes(h->p))) != cudaSuccess)
     return cleanup_fail(e);
+  if (h->p.problem != SWFD_PROBLEM_MATLAB_1D &&
+      (e = cudaMalloc(&h->sweep_cluster, sweep_cluster_bytes(h->p))) != cudaSuccess)
+    return cleanup_fail(e);
   for (int k = 0; k < 8; ++k)
     if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
   for (int k = 0; k < SWFD_CAP_DEPTH; ++k)
@@ -1034,6 +1039,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);
+  cudaFree(h->sweep_cluster);
   if (h->hsc) cudaFreeHost(h->hsc);
   for (int k = 0; k < 8; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);

@@ -250,6 +250,7 @@ struct swfd_handle {
   double* seg_buf = nullptr;  // ex6: per-cell alpha and alpha per rank row / column
   double* rhs_tmp = nullptr;  // nc planes (flux_divergence output)
   void* sweep_scratch = nullptr;  // flag bits, flagged list, chain results
+  void* sweep_cluster = nullptr;  // cluster walks: pass-start values, carries, backup
   swfd::DevScalars* dsc = nullptr;   // device scalars
   swfd::DevScalars* hsc = nullptr;   // pinned host mirror
   // host-side run state
@@ -362,9 +363,11 @@ cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int f
                                  DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 size_t sweep_scratch_bytes(const Params& p);
+size_t sweep_cluster_bytes(const Params& p);  // the cluster-parallel passes' scratch
 cudaError_t launch_pressure_pass_par(const Params& p, double* u, int ordering, int forward,
-                                     void* scratch, DevScalars* dsc, cudaStream_t s, int* nlaunch);
-cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, cudaStream_t s,
-                                     int* nlaunch);
+                                     void* scratch, void* cluster, DevScalars* dsc,
+                                     cudaStream_t s, int* nlaunch);
+cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, void* cluster,
+                                     cudaStream_t s, int* nlaunch);
 
 }  // namespace swfd

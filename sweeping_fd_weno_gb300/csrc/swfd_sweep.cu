@@ -103,59 +103,6 @@ constexpr int SUM_THREADS = 256;
 constexpr int SUM_PER_THREAD = 8;
 constexpr int SUM_WINDOW = SUM_THREADS * SUM_PER_THREAD;
 
-// p / u = ip + rem / 2^d relative to the binade with biased exponent eb of a
-// running sum of sign neg_s (mirrored to a positive sum): floor (fl) and
-// rounded value (r) in units of u; bad = 1 for a tie, an exponent above the
-// binade's or a non-finite p
-__device__ __forceinline__ void sum_classify(double p, int neg_s, int eb, long long& fl,
-                                             long long& r, int& bad) {
-  const unsigned long long pb = (unsigned long long)__double_as_longlong(p);
-  const int ps = (int)(pb >> 63) ^ neg_s;
-  int pe = (int)((pb >> 52) & 0x7ff);
-  unsigned long long mp = pb & 0xfffffffffffffull;
-  fl = 0;
-  r = 0;
-  bad = 0;
-  if (pe == 0x7ff) {
-    bad = 1;
-    return;
-  }
-  if (pe) mp |= 1ull << 52;
-  else pe = 1;
-  if (mp == 0) return;  // +-0
-  const int d = eb - pe;
-  if (d < 0) {  // |p / u| >= 2^53: the sum leaves the binade
-    bad = 1;
-    return;
-  }
-  unsigned long long ip, rem, half;
-  if (d == 0) {
-    ip = mp;
-    rem = 0;
-    half = 1;
-  } else if (d < 64) {
-    ip = mp >> d;
-    rem = mp & ((1ull << d) - 1);
-    half = 1ull << (d - 1);
-    if (rem == half) {
-      bad = 1;
-      return;
-    }
-  } else {  // 0 < |p / u| < 2^-10
-    ip = 0;
-    rem = 1;
-    half = 2;
-  }
-  const long long up = rem > half ? 1 : 0;
-  if (!ps) {
-    fl = (long long)ip;
-    r = (long long)ip + up;
-  } else {
-    fl = -(long long)ip - (rem != 0 ? 1 : 0);
-    r = -((long long)ip + up);
-  }
-}
-
 // s = 0; for m = 0..n-1: s = s + term(m)  (term(m) the FP64 product of the
 // reference), evaluated by one block of SUM_THREADS threads; every thread
 // returns s
@@ -389,8 +336,11 @@ cudaError_t launch_exit_count(const Params& p, const double* u, DevScalars* dsc,
 //
 // Kernels per pass: flag (bitmask of initially-bad step positions),
 // compact (sorted list F), dry run (each F[k] from the original state,
-// stopped at F[k+1]: TERM or MERGE), walker (one warp: true roots, and the
-// MERGE chains run to their end with writes), write (TERM roots in parallel).
+// stopped at F[k+1]: TERM or MERGE), cluster walk (one thread per cluster of
+// MERGE chains ending in a TERM chain, with writes), fix-up (one warp: counts,
+// and the rare cluster walk that reached the next cluster's first position).
+// The batched engine runs the earlier form: dry run, one warp following the
+// MERGE chains in sequence, and the TERM roots written in parallel.
 // ===========================================================================
 
 template <int KIND>
@@ -442,126 +392,230 @@ __global__ void __launch_bounds__(1024) k_compact(int64_t N, SweepScratch sc) {
   }
 }
 
+size_t sweep_scratch_bytes(const Params& p) { return sweep_scratch_bytes_impl(p); }
+size_t sweep_cluster_bytes(const Params& p) { return cluster_scratch_bytes(p); }
+
+// ---------------------------------------------------------------------------
+// Cluster-parallel pass (single-instance path): dry runs as above that also
+// keep each flagged cell's pass-start value, one thread per cluster walking
+// its chains with writes, and one warp that sums the counts and, when a
+// cluster's walk reached the next cluster's first position, undoes the later
+// clusters and finishes the pass sequentially.  Values and counts are those
+// of the sequential walk.
+// ---------------------------------------------------------------------------
 template <int KIND>
-__global__ void k_chain_dry(Params p, double* u, int ordering, int forward, SweepScratch sc,
-                            const DevScalars* dsc) {
+__device__ __forceinline__ int nc_of(const Params& p) { return KIND == 1 ? 1 : p.g.nc; }
+
+template <int KIND>
+__global__ void k_cl_dry(Params p, double* u, int ordering, int forward, SweepScratch sc,
+                         ClusterScratch cs, const DevScalars* dsc) {
   if (ordering < 0) ordering = dsc->ordering;
-  const int64_t N = npos(p.g);
+  const Geom& g = p.g;
+  const int64_t N = npos(g);
   const int m = sc.counters[0];
   double ub[4] = {0, 0, 0, 0};
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const int64_t cell = walk_cell(g, ordering, forward, N, sc.F[k]);
+    for (int c = 0; c < nc_of<KIND>(p); ++c) cs.orig[(int64_t)k * 4 + c] = u[c * g.plane + cell];
     long long a = 0, b = 0;
     int merged = 0;
     int64_t stop = (k + 1 < m) ? sc.F[k + 1] : -1;
-    int64_t e = run_chain<KIND, false>(p, u, ordering, forward, N, sc.F[k], stop, ub, &merged, a,
-                                       b);
-    sc.dry_end[k] = (int)e;
+    run_chain<KIND, false>(p, u, ordering, forward, N, sc.F[k], stop, ub, &merged, a, b);
     sc.dry_merge[k] = (uint8_t)merged;
-    sc.root[k] = 0;
-    if (merged) atomicOr(&sc.counters[1], 1);
   }
 }
 
-// one warp: resolve true roots; run MERGE chains to their end with writes
 template <int KIND>
-__global__ void k_chain_walk(Params p, double* u, int ordering, int forward, SweepScratch sc,
-                             DevScalars* dsc) {
-  if (sc.counters[1] == 0) return;  // no chain reaches the next flagged cell
+__device__ __forceinline__ void bk_save(const Params& p, const double* u, const ClusterScratch& cs,
+                                        int64_t N, int64_t pos, int64_t cell) {
+  for (int c = 0; c < nc_of<KIND>(p); ++c) cs.backup[c * N + pos] = u[c * p.g.plane + cell];
+}
+
+template <int KIND>
+__global__ void k_cl_run(Params p, double* u, int ordering, int forward, SweepScratch sc,
+                         ClusterScratch cs, const DevScalars* dsc) {
   if (ordering < 0) ordering = dsc->ordering;
-  const int64_t N = npos(p.g);
+  const Geom& g = p.g;
+  const int64_t N = npos(g);
   const int m = sc.counters[0];
-  const int lane = threadIdx.x;
   double ub[4] = {0, 0, 0, 0};
   if (KIND == 0)
     for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
-  long long npos_ = 0, nneg = 0;
-  int fail = 0;
-  int64_t covered = -1;
-  int base = 0;
-  while (base < m) {
-    int k = base + lane;
-    bool valid = k < m;
-    int64_t f = valid ? sc.F[k] : INT64_MAX;
-    bool mg = valid && sc.dry_merge[k];
-    bool live = valid && f > covered;
-    unsigned mm = __ballot_sync(0xffffffffu, live && mg);
-    int first = mm ? __ffs(mm) - 1 : 32;
-    if (live && !mg && lane < first) sc.root[k] = 1;
-    if (first == 32) {
-      base += 32;
+  const bool check = KIND == 0 && p.sweep_check && ordering == 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    if (k > 0 && sc.dry_merge[k - 1]) {
+      cs.flag[k] = 0;  // inside a cluster
       continue;
     }
-    int64_t e = 0;
-    if (lane == first) {
-      int merged;
-      e = run_chain<KIND, true>(p, u, ordering, forward, N, f, -1, ub, &merged, npos_, nneg,
-                                &fail);
+    int k1 = k;  // the cluster's last chain
+    while (k1 < m - 1 && sc.dry_merge[k1]) ++k1;
+    const int kn = k1 + 1;
+    const int64_t stop = kn < m ? sc.F[kn] : -1;
+    long long np_ = 0, nn = 0;
+    int fail = 0;
+    uint8_t fl = 1;
+    int64_t covered = -1, bk = sc.F[k];
+    for (int j = k; j <= k1 && fl == 1; ++j) {
+      const int64_t q0 = sc.F[j];
+      if (q0 <= covered) continue;  // absorbed by the previous chain
+      for (; bk <= q0; ++bk) bk_save<KIND>(p, u, cs, N, bk, walk_cell(g, ordering, forward, N, bk));
+      Chain<KIND> cur, nxt;
+      int64_t q = q0, cq = walk_cell(g, ordering, forward, N, q0);
+      cur.load(p, u, cq);
+      for (;;) {
+        if (q >= N - 1) {  // the last position takes no step
+          cur.store(p, u, cq);
+          covered = q;
+          break;
+        }
+        int64_t cn = 0;
+        if (q + 1 == stop) {  // the next cluster's cell, as it was when the pass began
+          for (int c = 0; c < nc_of<KIND>(p); ++c) nxt.s[c] = cs.orig[(int64_t)kn * 4 + c];
+        } else {
+          cn = walk_cell(g, ordering, forward, N, q + 1);
+          for (; bk <= q + 1; ++bk) bk_save<KIND>(p, u, cs, N, bk, walk_cell(g, ordering, forward, N, bk));
+          nxt.load(p, u, cn);
+        }
+        cur.step(p, nxt, ub, np_, nn, check ? &fail : nullptr);
+        cur.store(p, u, cq);
+        ++q;
+        if (q == stop) {  // spill: the carried value of the next cluster's first cell
+          for (int c = 0; c < nc_of<KIND>(p); ++c) cs.carry[(int64_t)k * 4 + c] = nxt.s[c];
+          fl = 2;
+          covered = q - 1;
+          break;
+        }
+        cq = cn;
+        cur = nxt;
+        if (!cur.bad(p)) {
+          cur.store(p, u, cq);
+          covered = q;
+          break;
+        }
+      }
     }
-    covered = __shfl_sync(0xffffffffu, e, first);
-    base += first + 1;
-  }
-  if (KIND == 0 && fail) atomicOr(&dsc->error, ERR_BIT_CHECK);
-  if (KIND == 0 && (npos_ | nneg)) {  // each lane adds the chains it ran
-    atomicAdd((unsigned long long*)&dsc->t_pos, (unsigned long long)npos_);
-    atomicAdd((unsigned long long*)&dsc->t_neg, (unsigned long long)nneg);
+    cs.end[k] = (int)covered;
+    cs.next[k] = kn;
+    cs.cnt[2 * (int64_t)k] = np_;
+    cs.cnt[2 * (int64_t)k + 1] = nn;
+    cs.flag[k] = fl | (fail ? 4 : 0);
   }
 }
 
 template <int KIND>
-__global__ void k_chain_write(Params p, double* u, int ordering, int forward, SweepScratch sc,
-                              DevScalars* dsc) {
+__global__ void k_cl_fix(Params p, double* u, int ordering, int forward, SweepScratch sc,
+                         ClusterScratch cs, DevScalars* dsc) {
   if (ordering < 0) ordering = dsc->ordering;
-  const int64_t N = npos(p.g);
+  const Geom& g = p.g;
+  const int64_t N = npos(g);
   const int m = sc.counters[0];
-  const bool all_roots = sc.counters[1] == 0;
-  double ub[4] = {0, 0, 0, 0};
-  if (KIND == 0)
-    for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
-  long long npos_ = 0, nneg = 0;
+  const int lane = threadIdx.x;
+  // the first cluster whose walk stopped at the next cluster's first position
+  int first = INT_MAX;
+  for (int k = lane; k < m; k += 32)
+    if (cs.flag[k] & 2) {
+      first = k;
+      break;
+    }
+  for (int off = 16; off > 0; off >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, off));
+  long long np_ = 0, nn = 0;
   int fail = 0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
-    if (!(all_roots || sc.root[k])) continue;
-    int merged;
-    run_chain<KIND, true>(p, u, ordering, forward, N, sc.F[k], -1, ub, &merged, npos_, nneg,
-                          &fail);
+  for (int k = lane; k < m && k <= first; k += 32)
+    if (cs.flag[k]) {
+      np_ += cs.cnt[2 * (int64_t)k];
+      nn += cs.cnt[2 * (int64_t)k + 1];
+      fail |= cs.flag[k] & 4;
+    }
+  if (first != INT_MAX) {
+    // undo the clusters after it (disjoint position ranges, one lane each)
+    for (int k = first + 1 + lane; k < m; k += 32) {
+      if (!cs.flag[k]) continue;
+      for (int64_t q = sc.F[k]; q <= cs.end[k]; ++q) {
+        const int64_t cell = walk_cell(g, ordering, forward, N, q);
+        for (int c = 0; c < nc_of<KIND>(p); ++c) u[c * g.plane + cell] = cs.backup[c * N + q];
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double ub[4] = {0, 0, 0, 0};
+      if (KIND == 0)
+        for (int c = 0; c < 4; ++c) ub[c] = dsc->ubar[c];
+      int* chk = (KIND == 0 && p.sweep_check && ordering == 1) ? &fail : nullptr;
+      // the spilled chain from the next cluster's first position with its carried value
+      const int kn = cs.next[first];
+      int64_t q = sc.F[kn], cq = walk_cell(g, ordering, forward, N, q);
+      Chain<KIND> cur, nxt;
+      for (int c = 0; c < nc_of<KIND>(p); ++c) cur.s[c] = cs.carry[(int64_t)first * 4 + c];
+      for (;;) {
+        if (!cur.bad(p) || q >= N - 1) {
+          cur.store(p, u, cq);
+          break;
+        }
+        const int64_t cn = walk_cell(g, ordering, forward, N, q + 1);
+        nxt.load(p, u, cn);
+        cur.step(p, nxt, ub, np_, nn, chk);
+        cur.store(p, u, cq);
+        ++q;
+        cq = cn;
+        cur = nxt;
+      }
+      // then every later flagged position the walk has not reached, in order
+      int64_t covered = q;
+      for (int j = kn + 1; j < m; ++j) {
+        if (sc.F[j] <= covered) continue;
+        int merged;
+        covered = run_chain<KIND, true>(p, u, ordering, forward, N, sc.F[j], -1, ub, &merged, np_,
+                                        nn, chk);
+      }
+    }
   }
-  if (KIND == 0 && fail) atomicOr(&dsc->error, ERR_BIT_CHECK);
-  if (KIND == 0 && (npos_ | nneg)) {
-    atomicAdd((unsigned long long*)&dsc->t_pos, (unsigned long long)npos_);
-    atomicAdd((unsigned long long*)&dsc->t_neg, (unsigned long long)nneg);
+  if constexpr (KIND == 0) {
+    for (int off = 16; off > 0; off >>= 1) {
+      np_ += __shfl_xor_sync(0xffffffffu, np_, off);
+      nn += __shfl_xor_sync(0xffffffffu, nn, off);
+      fail |= __shfl_xor_sync(0xffffffffu, fail, off);
+    }
+    if (lane == 0) {
+      if (fail) atomicOr(&dsc->error, ERR_BIT_CHECK);
+      if (np_ | nn) {
+        atomicAdd((unsigned long long*)&dsc->t_pos, (unsigned long long)np_);
+        atomicAdd((unsigned long long*)&dsc->t_neg, (unsigned long long)nn);
+      }
+    }
   }
 }
-
-size_t sweep_scratch_bytes(const Params& p) { return sweep_scratch_bytes_impl(p); }
 
 template <int KIND>
 static cudaError_t pass_parallel(const Params& p, double* u, int ordering, int forward,
-                                 void* scratch, DevScalars* dsc, cudaStream_t s, int* nlaunch) {
+                                 void* scratch, void* cluster, DevScalars* dsc, cudaStream_t s,
+                                 int* nlaunch) {
   const int64_t N = npos(p.g);
   SweepScratch sc = carve(scratch, p);
+  ClusterScratch cs = carve_cluster(cluster, p);
   const int ord = p.g.ndim == 1 ? 0 : ordering;
   k_flag_bits<KIND><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(p, u, ord, forward, sc, dsc);
   k_compact<<<1, 1024, 0, s>>>(N, sc);
   const int grid = 4 * 152;
-  k_chain_dry<KIND><<<grid, 128, 0, s>>>(p, u, ord, forward, sc, dsc);
-  k_chain_walk<KIND><<<1, 32, 0, s>>>(p, u, ord, forward, sc, dsc);
-  k_chain_write<KIND><<<grid, 128, 0, s>>>(p, u, ord, forward, sc, dsc);
+  k_cl_dry<KIND><<<grid, 128, 0, s>>>(p, u, ord, forward, sc, cs, dsc);
+  k_cl_run<KIND><<<grid, 128, 0, s>>>(p, u, ord, forward, sc, cs, dsc);
+  k_cl_fix<KIND><<<1, 32, 0, s>>>(p, u, ord, forward, sc, cs, dsc);
   *nlaunch += 5;
   return cudaGetLastError();
 }
 
 cudaError_t launch_pressure_pass_par(const Params& p, double* u, int ordering, int forward,
-                                     void* scratch, DevScalars* dsc, cudaStream_t s, int* nlaunch) {
-  return pass_parallel<0>(p, u, ordering, forward, scratch, dsc, s, nlaunch);
+                                     void* scratch, void* cluster, DevScalars* dsc,
+                                     cudaStream_t s, int* nlaunch) {
+  return pass_parallel<0>(p, u, ordering, forward, scratch, cluster, dsc, s, nlaunch);
 }
 
-cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, cudaStream_t s,
-                                     int* nlaunch) {
-  cudaError_t e = pass_parallel<1>(p, u, 1, 1, scratch, nullptr, s, nlaunch);
+cudaError_t launch_density_sweep_par(const Params& p, double* u, void* scratch, void* cluster,
+                                     cudaStream_t s, int* nlaunch) {
+  cudaError_t e = pass_parallel<1>(p, u, 1, 1, scratch, cluster, nullptr, s, nlaunch);
   if (e != cudaSuccess) return e;
-  return pass_parallel<1>(p, u, 1, 0, scratch, nullptr, s, nlaunch);
+  return pass_parallel<1>(p, u, 1, 0, scratch, cluster, nullptr, s, nlaunch);
 }
 
 }  // namespace swfd

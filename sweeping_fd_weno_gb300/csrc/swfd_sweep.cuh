@@ -29,10 +29,14 @@ __host__ __device__ __forceinline__ int64_t npos(const Geom& g) {
 }
 
 // pressure as the sweep computes it
-// (2D ex3_vortex_accuracy_2d/main.f90:946, 1D ex2_sedov_1d/main.f90:603)
+// (2D ex3_vortex_accuracy_2d/main.f90:946, 1D ex2_sedov_1d/main.f90:603).
+// The divisions are sd::div and the products by 0.5 exponent shifts (the
+// same bits as the IEEE operations): a sweep pass is a chain of dependent
+// nodal adjustments, and GB300's FP64 pipe has a long latency, so the
+// integer-pipe division shortens every step of that chain.
 __device__ __forceinline__ double sweep_pres(const Geom& g, double g1, const double* v) {
-  if (g.ndim == 1) return g1 * (v[2] - 0.5 * (v[1] * v[1]) / v[0]);
-  return g1 * (v[3] - 0.5 * (v[1] * v[1] + v[2] * v[2]) / (v[0]));
+  if (g.ndim == 1) return g1 * (v[2] - tdiv(tscale<-1>(v[1] * v[1]), v[0]));
+  return g1 * (v[3] - tdiv(tscale<-1>(v[1] * v[1] + v[2] * v[2]), v[0]));
 }
 
 // nod_lim (ex3_vortex_accuracy_2d/main.f90:846-884; 1D ex2_sedov_1d/main.f90:517-560)
@@ -40,33 +44,33 @@ __device__ inline void nod_lim(const Geom& g, double g1, double eps, const doubl
                         const double* vb, double* out, long long& npos_, long long& nneg) {
   double t;
   if (g.ndim == 1) {
-    double p1 = g1 * (v1[2] - 0.5 * (v1[1] * v1[1] / v1[0]));
-    double p2 = g1 * (v2[2] - 0.5 * (v2[1] * v2[1] / v2[0]));
+    double p1 = g1 * (v1[2] - tscale<-1>(tdiv(v1[1] * v1[1], v1[0])));
+    double p2 = g1 * (v2[2] - tscale<-1>(tdiv(v2[1] * v2[1], v2[0])));
     if (p2 > eps) {
-      t = (p1 - eps) / (p1 - p2);
+      t = tdiv(p1 - eps, p1 - p2);
       ++npos_;
     } else {
-      double pb = g1 * (vb[2] - 0.5 * (vb[1] * vb[1] / vb[0]));
-      double t_1 = (p1 - eps) / (p1 - pb);
+      double pb = g1 * (vb[2] - tscale<-1>(tdiv(vb[1] * vb[1], vb[0])));
+      double t_1 = tdiv(p1 - eps, p1 - pb);
       double d12 = sqrt(dsq(v2[2] - v1[2]) + dsq(v2[1] - v1[1]) + dsq(v2[0] - v1[0]));
       double d1b = sqrt(dsq(vb[2] - v1[2]) + dsq(vb[1] - v1[1]) + dsq(vb[0] - v1[0]));
-      t = fmin(t_1 * d1b / d12, 0.25);
+      t = fmin(tdiv(t_1 * d1b, d12), 0.25);
       ++nneg;
     }
   } else {
-    double p1 = g1 * (v1[3] - 0.5 * (v1[1] * v1[1] + v1[2] * v1[2]) / v1[0]);
-    double p2 = g1 * (v2[3] - 0.5 * (v2[1] * v2[1] + v2[2] * v2[2]) / v2[0]);
+    double p1 = g1 * (v1[3] - tdiv(tscale<-1>(v1[1] * v1[1] + v1[2] * v1[2]), v1[0]));
+    double p2 = g1 * (v2[3] - tdiv(tscale<-1>(v2[1] * v2[1] + v2[2] * v2[2]), v2[0]));
     if (p2 > eps) {
-      t = (p1 - eps) / (p1 - p2);
+      t = tdiv(p1 - eps, p1 - p2);
       ++npos_;
     } else {
-      double pb = g1 * (vb[3] - 0.5 * (vb[1] * vb[1] + vb[2] * vb[2]) / vb[0]);
-      double t_1 = (p1 - eps) / (p1 - pb);
+      double pb = g1 * (vb[3] - tdiv(tscale<-1>(vb[1] * vb[1] + vb[2] * vb[2]), vb[0]));
+      double t_1 = tdiv(p1 - eps, p1 - pb);
       double d12 = sqrt(dsq(v2[3] - v1[3]) + dsq(v2[2] - v1[2]) + dsq(v2[1] - v1[1]) +
                         dsq(v2[0] - v1[0]));
       double d1b = sqrt(dsq(vb[3] - v1[3]) + dsq(vb[2] - v1[2]) + dsq(vb[1] - v1[1]) +
                         dsq(vb[0] - v1[0]));
-      t = fmin(t_1 * d1b / d12, 0.25);
+      t = fmin(tdiv(t_1 * d1b, d12), 0.25);
       ++nneg;
     }
   }
@@ -206,5 +210,103 @@ __host__ __device__ inline SweepScratch carve(void* base, const Params& p) {
   return s;
 }
 
+
+// p / u = ip + rem / 2^d relative to the binade with biased exponent eb of a
+// running sum of sign neg_s (mirrored to a positive sum): floor (fl) and
+// rounded value (r) in units of u; bad = 1 for a tie, an exponent above the
+// binade's or a non-finite p
+__device__ __forceinline__ void sum_classify(double p, int neg_s, int eb, long long& fl,
+                                             long long& r, int& bad) {
+  const unsigned long long pb = (unsigned long long)__double_as_longlong(p);
+  const int ps = (int)(pb >> 63) ^ neg_s;
+  int pe = (int)((pb >> 52) & 0x7ff);
+  unsigned long long mp = pb & 0xfffffffffffffull;
+  fl = 0;
+  r = 0;
+  bad = 0;
+  if (pe == 0x7ff) {
+    bad = 1;
+    return;
+  }
+  if (pe) mp |= 1ull << 52;
+  else pe = 1;
+  if (mp == 0) return;  // +-0
+  const int d = eb - pe;
+  if (d < 0) {  // |p / u| >= 2^53: the sum leaves the binade
+    bad = 1;
+    return;
+  }
+  unsigned long long ip, rem, half;
+  if (d == 0) {
+    ip = mp;
+    rem = 0;
+    half = 1;
+  } else if (d < 64) {
+    ip = mp >> d;
+    rem = mp & ((1ull << d) - 1);
+    half = 1ull << (d - 1);
+    if (rem == half) {
+      bad = 1;
+      return;
+    }
+  } else {  // 0 < |p / u| < 2^-10
+    ip = 0;
+    rem = 1;
+    half = 2;
+  }
+  const long long up = rem > half ? 1 : 0;
+  if (!ps) {
+    fl = (long long)ip;
+    r = (long long)ip + up;
+  } else {
+    fl = -(long long)ip - (rem != 0 ? 1 : 0);
+    r = -((long long)ip + up);
+  }
+}
+
+// Cluster-parallel passes (single-instance path).  A cluster is a maximal
+// run of flagged positions F[k0..k1] whose dry runs each reach the next
+// flagged position (dry_merge[k0..k1-1] = 1, dry_merge[k1] = 0).  One thread
+// walks each cluster in order with writes -- exactly the sequential walk
+// restricted to the cluster's positions -- and stops if its walk reaches the
+// first position of the next cluster, which another thread owns.  The cluster
+// saves the original value of every position it walks over (backup), so that
+// such a spill can be undone: one warp then restores the later clusters and
+// finishes the pass sequentially from the spill.
+struct ClusterScratch {
+  double* orig;      // per k: nc values of cell(F[k]) when the pass starts
+  double* carry;     // per cluster start k: the carried cell state at its stop
+  double* backup;    // per position: nc original values of the positions walked
+  long long* cnt;    // per cluster start k: positive-neighbour and negative-pair counts
+  int* end;          // per cluster start k: last position written
+  int* next;         // per cluster start k: index of the next cluster's start (m: none)
+  uint8_t* flag;     // per k: 0 not a cluster start, 1 done, 2 stopped at the next
+                     // cluster's start, 4 (or'ed) ex6 pressure check failed
+};
+
+inline size_t cluster_scratch_bytes(const Params& p) {
+  const int64_t N = npos(p.g);
+  return (size_t)N * (8 * 4 * 3 + 8 * 2 + 4 * 2 + 1) + 256;
+}
+
+__host__ __device__ inline ClusterScratch carve_cluster(void* base, const Params& p) {
+  const int64_t N = npos(p.g);
+  char* c = (char*)base;
+  ClusterScratch s;
+  s.orig = (double*)c;
+  c += N * 4 * 8;
+  s.carry = (double*)c;
+  c += N * 4 * 8;
+  s.backup = (double*)c;
+  c += N * 4 * 8;
+  s.cnt = (long long*)c;
+  c += N * 2 * 8;
+  s.end = (int*)c;
+  c += N * 4;
+  s.next = (int*)c;
+  c += N * 4;
+  s.flag = (uint8_t*)c;
+  return s;
+}
 
 }  // namespace swfd
