@@ -551,11 +551,11 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
     b.k(2);
     b.cond(s, cudaGraphCondTypeIf, hd, density);
   }
-  B_OK(b, launch_ubar(p, u, h->dsc, s));
+  B_OK(b, launch_ubar(p, u, h->dsc, h->ubar_scratch, s));
   cudaGraphConditionalHandle hw = b.handle();
   B_OK(b, launch_sweep_begin(hw, p, h->dsc, p.stop_sweep, h->cfg.swp_num, s));
   B_OK(b, cudaMemsetAsync(&h->dsc->t_pos, 0, 2 * sizeof(long long), s));
-  b.k(2);
+  b.k(4);  // u_bar's three kernels and sweep_begin
   b.cond(s, cudaGraphCondTypeWhile, hw, [&](cudaStream_t sq) {
     b.count = &h->k_q;
     B_OK(b, launch_q_begin(p, h->dsc, sq));
@@ -581,12 +581,18 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
 
 // one RK stage: findalpha, [dt], LF split, WENO fluxes, RHS + RK combination +
 // checkpositivity, [sweep], bc  (ex3_vortex_accuracy_2d/main.f90:564-632)
+// the bc of stages 1 and 2 carries the next stage's findalpha (2D problems
+// without rank segments); stage 1's findalpha, which also sets dt, stays apart
+bool fused_alpha(const Params& p) { return p.g.ndim == 2 && !p.seg_alpha; }
+
 void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, double* out,
                 bool events) {
   swfd_handle* h = b.h;
   const Params& p = h->p;
-  B_OK(b, launch_alpha(p, in, h->dsc, s, k == 1));
-  b.k(1);
+  if (k == 1 || !fused_alpha(p)) {
+    B_OK(b, launch_alpha(p, in, h->dsc, s, k == 1));
+    b.k(1);
+  }
   {
     int nk = 0;
     B_OK(b, launch_split(p, in, h->dsc, h->split, h->roe, s, &nk));
@@ -615,7 +621,8 @@ void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, doubl
     b.count = saved;
   }
   if (p.g.ndim == 2) {
-    B_OK(b, launch_bc(p, out, s));
+    if (k < 3 && fused_alpha(p)) B_OK(b, launch_bc_alpha(p, out, h->dsc, s));
+    else B_OK(b, launch_bc(p, out, s));
     b.k(1);
   }
 }
@@ -998,7 +1005,8 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if ((e = cudaMalloc(&h->sweep_scratch, sweep_scratch_bytes(h->p))) != cudaSuccess)
     return cleanup_fail(e);
   if (h->p.problem != SWFD_PROBLEM_MATLAB_1D &&
-      (e = cudaMalloc(&h->sweep_cluster, sweep_cluster_bytes(h->p))) != cudaSuccess)
+      ((e = cudaMalloc(&h->sweep_cluster, sweep_cluster_bytes(h->p))) != cudaSuccess ||
+       (e = cudaMalloc(&h->ubar_scratch, ubar_scratch_bytes(h->p))) != cudaSuccess))
     return cleanup_fail(e);
   for (int k = 0; k < 8; ++k)
     if ((e = cudaEventCreate(&h->ev[k])) != cudaSuccess) return cleanup_fail(e);
@@ -1040,6 +1048,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);
   cudaFree(h->sweep_cluster);
+  cudaFree(h->ubar_scratch);
   if (h->hsc) cudaFreeHost(h->hsc);
   for (int k = 0; k < 8; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
@@ -1486,11 +1495,13 @@ swfd_status swfd_sequential_sum(const double* x, int64_t n, double w, int32_t de
     return fail(nullptr, SWFD_ERR_INVALID, "bad arguments");
   CU(nullptr, cudaSetDevice(device));
   double *dx = nullptr, *ds = nullptr;
+  void* scratch = nullptr;
   cudaStream_t s = nullptr;
   auto done = [&](swfd_status st) {
     if (s) cudaStreamSynchronize(s);
     cudaFree(dx);
     cudaFree(ds);
+    cudaFree(scratch);
     if (s) cudaStreamDestroy(s);
     return st;
   };
@@ -1498,9 +1509,10 @@ swfd_status swfd_sequential_sum(const double* x, int64_t n, double w, int32_t de
   if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&dx, (n > 0 ? n : 1) * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&ds, sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&scratch, seq_sum_scratch_bytes(n > 0 ? n : 1))) != cudaSuccess ||
       (n > 0 && (e = cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, s)) !=
                     cudaSuccess) ||
-      (e = launch_seq_sum(dx, (int)n, w, ds, s)) != cudaSuccess ||
+      (e = launch_seq_sum(dx, n, w, ds, scratch, s)) != cudaSuccess ||
       (e = cudaMemcpyAsync(out, ds, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return done(

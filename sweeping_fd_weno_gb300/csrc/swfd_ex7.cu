@@ -826,8 +826,8 @@ swfd_status e7_sweep(swfd_handle* h) {
   // u_bar: five sequential sums, j outer (:1464-1485)
   const double w = 1. / ((double)v.nx * (double)v.ny);
   for (int c = 0; c < 5; ++c) {
-    E7CU(h, launch_seq_sum(v.ug + c * N, (int)N, w, &sc->ubar[c], s));
-    x->launches++;
+    E7CU(h, launch_seq_sum(v.ug + c * N, N, w, &sc->ubar[c], x->sum_scratch, s));
+    x->launches += 3;
   }
   ST(e7_sync_scalars(h));
   const double* ub = x->hs->ubar;
@@ -970,6 +970,7 @@ swfd_status ex7_create(swfd_handle* h, std::string& err) {
   const size_t qbytes = sizeof(qd::q128) * (qd::EXP_N + 1);
   const size_t bytes = ndbl * sizeof(double) + qbytes + sizeof(Ex7Scalars) + 2 * N * sizeof(int) + 256;
   cudaError_t e = cudaMalloc(&x->block, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&x->sum_scratch, seq_sum_scratch_bytes(N));
   if (e != cudaSuccess) {
     err = std::string("detonation: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? SWFD_ERR_OOM : SWFD_ERR_CUDA;
@@ -1014,6 +1015,7 @@ swfd_status ex7_create(swfd_handle* h, std::string& err) {
 void ex7_destroy(Ex7* x) {
   if (!x) return;
   cudaFree(x->block);
+  cudaFree(x->sum_scratch);
   if (x->hs) cudaFreeHost(x->hs);
   delete x;
 }

@@ -52,6 +52,7 @@ struct Ex7 {
   Ex7View v{};
   Ex7Scalars* hs = nullptr;  // pinned mirror of v.sc
   void* block = nullptr;     // one device allocation holding every buffer
+  void* sum_scratch = nullptr;  // the u_bar sums' terms and chunk summaries
   int use_limiter = 2, swp_num = 0;
   double t_loop = 0.;  // DO WHILE (time <= time_terminal - 1d-10), literal-exact
   int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;

@@ -251,6 +251,7 @@ struct swfd_handle {
   double* rhs_tmp = nullptr;  // nc planes (flux_divergence output)
   void* sweep_scratch = nullptr;  // flag bits, flagged list, chain results
   void* sweep_cluster = nullptr;  // cluster walks: pass-start values, carries, backup
+  void* ubar_scratch = nullptr;   // u_bar: the terms and the chunks' summaries
   swfd::DevScalars* dsc = nullptr;   // device scalars
   swfd::DevScalars* hsc = nullptr;   // pinned host mirror
   // host-side run state
@@ -299,6 +300,8 @@ void init_host_state(const Params& p, const swfd_config& cfg, double* u);
 
 // kernels.cu
 cudaError_t launch_bc(const Params& p, double* u, cudaStream_t s);
+// 2D bc fused with the next stage's findalpha (no dt); not for rank segments
+cudaError_t launch_bc_alpha(const Params& p, double* u, DevScalars* dsc, cudaStream_t s);
 // findalpha into dsc->alphamax; with_dt: the dt rule follows (stage 1).
 // dsc's alpha_bits and alpha_done are zero between launches.
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
@@ -340,8 +343,10 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
 cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s);
 // findalpha over the running slots' state `in` (the batch autotuner's probe)
 cudaError_t launch_batch_alpha(const BatchLaunch& b, int in, cudaStream_t s);
-// launch-shape candidates of the flux kernel (resident blocks per SM); returns
-// their number, the default first
+// launch-shape candidates of the flux kernel (resident blocks per SM; FP64
+// values SWFD_FLUX_PAIR + b select the lane-pair kernel with b blocks per SM);
+// returns their number, the default first
+#define SWFD_FLUX_PAIR 10
 int flux_min_blocks_candidates(bool f32, int* out);
 cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
 cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,
@@ -356,8 +361,14 @@ cudaError_t launch_batch_sweep_cond(const BatchLaunch& b, cudaGraphConditionalHa
 // sweep.cu
 cudaError_t launch_rho_min(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_density_sweep(const Params& p, double* u, cudaStream_t s);
-cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
-cudaError_t launch_seq_sum(const double* x, int n, double w, double* out, cudaStream_t s);
+// ubar.cu: u_bar into dsc->ubar (three kernels over the whole GPU, exact)
+size_t ubar_scratch_bytes(const Params& p);
+cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, void* scratch,
+                        cudaStream_t s);
+// s = 0; s = s + w*x(m) for m = 0..n-1 in that order, into *out (device)
+size_t seq_sum_scratch_bytes(int64_t n);
+cudaError_t launch_seq_sum(const double* x, int64_t n, double w, double* out, void* scratch,
+                           cudaStream_t s);
 // ordering < 0: the pass reads its ordering from dsc->ordering
 cudaError_t launch_pressure_pass(const Params& p, double* u, int ordering, int forward,
                                  DevScalars* dsc, cudaStream_t s);

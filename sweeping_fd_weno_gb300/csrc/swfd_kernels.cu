@@ -211,6 +211,29 @@ __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc,
   if (with_dt) dt_body(p, dsc);
 }
 
+// bc followed by the next stage's findalpha, in one pass over the cells: each
+// thread fills its ghost cell (bc2d_cell), then takes the alpha of its cell
+// from the value it just wrote or, for an interior cell, from the state the
+// RK stage and the sweep left; the block maxima and the last block's
+// decisions are k_alpha's.  Problems with rank segments keep their separate
+// findalpha (their per-cell alphas feed the per-row and per-column maxima).
+__global__ void k_bc2d_alpha(Params p, double* __restrict__ u, DevScalars* dsc) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bc2d_cell(p, u, t);
+  double a = alpha_cell(p, u, t);
+  a = block_max(a);
+  if (threadIdx.x != 0) return;
+  atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+  __threadfence();
+  if (atomicAdd(&dsc->alpha_done, 1) != (int)gridDim.x - 1) return;
+  __threadfence();
+  const unsigned long long m = atomicExch(&dsc->alpha_bits, 0ull);
+  dsc->alpha_done = 0;
+  dsc->postag = 0;
+  dsc->alphamax = __longlong_as_double((long long)m);
+  if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
+}
+
 // Threads per block of the per-cell kernels: 256, or fewer (down to one warp)
 // on grids too small to give every SM two blocks, so that the FP64 work of a
 // small grid (2 FP64 instructions per clock per SM) spreads over the SMs.
@@ -226,6 +249,13 @@ static int cell_block(int64_t cells) {
   int b = SWFD_BLOCK;
   while (b > 32 && (cells + b - 1) / b < 2 * sms) b >>= 1;
   return b;
+}
+
+cudaError_t launch_bc_alpha(const Params& p, double* u, DevScalars* dsc, cudaStream_t s) {
+  const int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  const int b = cell_block(n);
+  k_bc2d_alpha<<<(unsigned)((n + b - 1) / b), b, 0, s>>>(p, u, dsc);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
@@ -1000,6 +1030,143 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 interface fluxes with two lanes per interface (no rank segments, no
+// limiter, binary64 literals): lane 0 of a pair reconstructs the positive
+// split flux (four weno_right, its back projection), lane 1 the negative one
+// (four weno_left); both form the interface's Roe eigenvectors.  Each lane
+// holds half the stencil values and chains of one side, so more warps fit an
+// SM and each has shorter dependent chains, at the price of the eigenvectors
+// computed twice.  Every value is the one-lane form's expression.
+// ---------------------------------------------------------------------------
+template <int YDIR, int SIDE, class D>
+__device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const double* __restrict__ s,
+                                           int64_t P, int64_t step, double weps, D div,
+                                           double out[4]) {
+  double w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double c[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double* a = s + m * step;
+      const double a0 = ldt(a), a1 = ldt(a + P), a2 = ldt(a + 2 * P), a3 = ldt(a + 3 * P);
+      if (k == 0) c[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, a0, a1, a2, a3);
+      else if (k == 1) c[m] = proj_row2<YDIR>(E.vt, a0, a1, a2);
+      else if (k == 2) c[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, a0, a1, a2, a3);
+      else c[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, a0, a1, a2, a3);
+    }
+    w[k] = SIDE == 0 ? weno_right(c[0], c[1], c[2], c[3], c[4], weps, div)
+                     : weno_left(c[0], c[1], c[2], c[3], c[4], weps, div);
+  }
+  // evr . w (as interface_flux's back projection)
+  const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
+  out[0] = w[0] + w[2] + w[3];
+  out[n] = E.e_nm * w[0] + E.vn * w[2] + E.e_np * w[3];
+  out[tt] = E.vt * w[0] + w[1] + E.vt * w[2] + E.vt * w[3];
+  out[3] = E.e_hm * w[0] + E.vt * w[1] + E.qm * w[2] + E.e_hp * w[3];
+}
+struct Side4 {
+  double v[4];
+};
+template <int YDIR, int SIDE>
+static __device__ __noinline__ Side4 weno4_side_hw(Eigen2D<double> E, const double* s, int64_t P,
+                                                   int64_t step, double weps) {
+  Side4 r;
+  weno4_side<YDIR, SIDE>(E, s, P, step, weps, DivHw(), r.v);
+  return r;
+}
+template <int YDIR, int SIDE>
+__device__ __forceinline__ void side_flux(const Eigen2D<double>& E, const double* s, int64_t P,
+                                          int64_t step, double weps, double out[4]) {
+  int bad = 0;
+  weno4_side<YDIR, SIDE>(E, s, P, step, weps, DivFlag{&bad}, out);
+  if (bad) {
+    const Side4 r = weno4_side_hw<YDIR, SIDE>(E, s, P, step, weps);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = r.v[k];
+  }
+}
+
+// 16 interfaces of chunk c (x chunks first, then y chunks), two lanes each
+__device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* __restrict__ split,
+                                                const double* __restrict__ roe, double am,
+                                                double* __restrict__ flux, int64_t c,
+                                                int64_t chunks_x, int lane) {
+  const Geom& g = p.g;
+  const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
+  const double g1 = p.gamma1, weps = p.weno_eps;
+  const int side = lane & 1;
+  double o4[4];
+  if (c < chunks_x) {
+    const int64_t t = c * 16 + (lane >> 1);
+    if (t >= flux_faces_x(p)) return;
+    const int lx = p.nxl + 2;  // faces i = 0..nx+1 of rows 1..ny (one segment)
+    const int i = (int)t % lx, j = (int)t / lx + 1;
+    const int64_t o = g.at(i, j);
+    Eigen2D<double> E;
+    roe_eigen2d<double>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
+                        ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
+                        ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
+    if (side == 0) side_flux<0, 0>(E, split + o - 2, S, 1, weps, o4);
+    else side_flux<0, 1>(E, split + 4 * S + o - 2, S, 1, weps, o4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) flux[(4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
+  } else {
+    const int64_t t = (c - chunks_x) * 16 + (lane >> 1);
+    if (t >= flux_faces_y(p)) return;
+    const int i = (int)t % g.nx + 1, j = (int)t / g.nx;
+    const int64_t o = g.at(i, j);
+    const double* rr = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+    Eigen2D<double> E;
+    roe_eigen2d<double>(g1, 1, ldt(rr + o), ldt(rr + o + pit), ldt(rr + P + o),
+                        ldt(rr + P + o + pit), ldt(rr + 2 * P + o), ldt(rr + 2 * P + o + pit),
+                        ldt(rr + 3 * P + o), ldt(rr + 3 * P + o + pit), E);
+    if (side == 0) side_flux<1, 0>(E, split + 8 * S + o - 2 * spit, S, spit, weps, o4);
+    else side_flux<1, 1>(E, split + 12 * S + o - 2 * spit, S, spit, weps, o4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      flux[(8 + 4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
+  }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
+    k_flux_xy_pair(Params p, const double* __restrict__ split, const double* __restrict__ roe,
+                   const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
+  const int64_t chunks_x = (flux_faces_x(p) + 15) / 16;
+  const int64_t chunks = chunks_x + (flux_faces_y(p) + 15) / 16;
+  const int lane = threadIdx.x & 31;
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) break;
+    flux_chunk_pair(p, split, roe, am, flux, c, chunks_x, lane);
+  }
+  if (lane == 0) {  // as k_flux_xy: the last warp out re-arms both counters
+    __threadfence();
+    if (atomicAdd(work + 1, 1) == (int)(gridDim.x * (blockDim.x >> 5)) - 1) {
+      atomicExch(work, 0);
+      atomicExch(work + 1, 0);
+    }
+  }
+}
+
+template <int MINB>
+static int flux_grid_pair() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy_pair<MINB>, SWFD_FLUX_BLOCK, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  return grid;
+}
+
 template <class T, int MINB = SWFD_FLUX_MINB(T)>
 static int flux_grid() {
   static int grid = 0;
@@ -1024,8 +1191,12 @@ int flux_min_blocks_candidates(bool f32, int* out) {
     out[0] = 4, out[1] = 5, out[2] = 6;
     return 3;
   }
+  // FP64: the one-lane kernel (3, 2, 4 blocks per SM) and the lane-pair
+  // kernel (SWFD_FLUX_PAIR + 3..6 blocks per SM)
   out[0] = 3, out[1] = 2, out[2] = 4;
-  return 3;
+  out[3] = SWFD_FLUX_PAIR + 3, out[4] = SWFD_FLUX_PAIR + 4, out[5] = SWFD_FLUX_PAIR + 5;
+  out[6] = SWFD_FLUX_PAIR + 6;
+  return 7;
 }
 
 template <class T, int MINB>
@@ -1061,6 +1232,16 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
     if constexpr (sizeof(T) == 8) {
       if (p.flux_minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
       if (p.flux_minb == 4) return launch_flux_minb<T, 4>(p, sp, rp, dsc, fp, work, s);
+#define SWFD_PAIR_CASE(M)                                                                    \
+  if (p.flux_minb == SWFD_FLUX_PAIR + M) {                                                   \
+    k_flux_xy_pair<M><<<flux_grid_pair<M>(), SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work); \
+    return;                                                                                  \
+  }
+      SWFD_PAIR_CASE(3)
+      SWFD_PAIR_CASE(4)
+      SWFD_PAIR_CASE(5)
+      SWFD_PAIR_CASE(6)
+#undef SWFD_PAIR_CASE
     } else {
       if (p.flux_minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
       if (p.flux_minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);

@@ -103,6 +103,7 @@ constexpr int SUM_THREADS = 256;
 constexpr int SUM_PER_THREAD = 8;
 constexpr int SUM_WINDOW = SUM_THREADS * SUM_PER_THREAD;
 
+// The batched engine's form (the single-instance sweep uses swfd_ubar.cu):
 // s = 0; for m = 0..n-1: s = s + term(m)  (term(m) the FP64 product of the
 // reference), evaluated by one block of SUM_THREADS threads; every thread
 // returns s
@@ -210,28 +211,6 @@ __device__ void ubar_component(const Geom& g, const double* __restrict__ u, int 
     s = seq_sum_block(g.nx * g.ny, [&](int m) { return w * pl[g.at(m % nx + 1, m / nx + 1)]; });
   }
   if (threadIdx.x == 0) out[c] = s;
-}
-
-__global__ void __launch_bounds__(SUM_THREADS) k_ubar_seq(Params p, const double* __restrict__ u,
-                                                          DevScalars* dsc) {
-  if ((int)blockIdx.x < p.g.nc) ubar_component(p.g, u, blockIdx.x, dsc->ubar);
-}
-
-// the same summation over a flat array (test entry point)
-__global__ void __launch_bounds__(SUM_THREADS) k_seq_sum(const double* __restrict__ x, int n,
-                                                         double w, double* out) {
-  const double s = seq_sum_block(n, [&](int m) { return w * x[m]; });
-  if (threadIdx.x == 0) *out = s;
-}
-
-cudaError_t launch_seq_sum(const double* x, int n, double w, double* out, cudaStream_t s) {
-  k_seq_sum<<<1, SUM_THREADS, 0, s>>>(x, n, w, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s) {
-  k_ubar_seq<<<p.g.nc, SUM_THREADS, 0, s>>>(p, u, dsc);
-  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -15,7 +15,7 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
     for s in (a, b):
         s.init_problem()
     minb = b.autotune()
-    assert minb in ((3, 2, 4) if precision == abi.PRECISION_FP64 else (4, 5, 6))
+    assert minb in ((3, 2, 4, 13, 14, 15, 16) if precision == abi.PRECISION_FP64 else (4, 5, 6))
     for _ in range(4):
         assert a.step() == b.step()
     assert np.array_equal(a.state(), b.state())
@@ -23,7 +23,11 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
     b.close()
 
 
+# FP64 13..16: the lane-pair flux kernel (two lanes per interface) with 3..6
+# resident blocks per SM
 @pytest.mark.parametrize("precision,minb", [(abi.PRECISION_FP64, 2), (abi.PRECISION_FP64, 4),
+                                            (abi.PRECISION_FP64, 13), (abi.PRECISION_FP64, 14),
+                                            (abi.PRECISION_FP64, 15), (abi.PRECISION_FP64, 16),
                                             (abi.PRECISION_FP32_BULK, 5),
                                             (abi.PRECISION_FP32_BULK, 6)])
 def test_each_flux_launch_shape_keeps_results(swfd, monkeypatch, precision, minb):
@@ -63,3 +67,25 @@ def test_batch_tile_tuning_keeps_results(swfd, precision):
     for (ua, ta), (ub, tb) in zip(*out):
         assert ta == tb
         assert np.array_equal(ua, ub)
+
+
+@pytest.mark.parametrize("minb", [14, 16])
+@pytest.mark.parametrize("case", [dict(problem=abi.SEDOV_2D, nx=48, ny=40),
+                                  dict(problem=abi.JET_2D, nx=96, ny=24)],
+                         ids=["point_energy", "jet"])
+def test_lane_pair_flux_kernel_matches_the_oracle(swfd, oracle_mod, monkeypatch, minb, case):
+    """The lane-pair FP64 flux kernel on the ex4 form (alpha pre-multiplied,
+    y-pass regulariser planes) and the ex5 form, against the oracle's steps."""
+    monkeypatch.setenv("SWFD_FLUX_MIN_BLOCKS", str(minb))
+    kw = dict(case)
+    prob = kw.pop("problem")
+    g = Solver(problems.make_config(prob, **kw))
+    o = oracle_mod.Oracle(problems.make_config(prob, **kw))
+    g.init_problem()
+    o.init_problem()
+    assert g.autotune() == minb
+    for _ in range(3):
+        assert g.step() == o.step()
+    assert np.array_equal(g.state(), o.state())
+    assert g.stats() == o.stats()
+    g.close()

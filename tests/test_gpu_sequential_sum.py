@@ -67,6 +67,14 @@ def cases():
     nan[20] = -np.inf
     yield "inf - inf", nan, 1.0
     yield "overflow", np.full(5000, 1.7e308), 1.0
+    # lengths at the 2048-term chunks of the summation, a tie on a chunk edge,
+    # and a random walk (a sum that keeps changing binade: many single steps)
+    for n in (2047, 2048, 2049, 6145):
+        yield f"chunk edge {n}", rng.lognormal(0, 2, size=n), 1.0 / n
+    t = np.ones(3 * 2048)
+    t[0] = 2.0 ** 53
+    yield "ties across chunk edges", t, 1.0
+    yield "random walk", rng.normal(size=60_000), 1.0 / 60_000
 
 
 @pytest.mark.parametrize("name,x,w", list(cases()), ids=[c[0] for c in cases()])
