@@ -781,7 +781,8 @@ def bench_serving(args, local):
         r = subprocess.run([str(serve), "--requests", str(args.serve_requests), "--rate",
                             str(args.serve_rate), "--seed", str(SERVE_SEED), "--slots",
                             str(args.serve_slots), "--chunk", str(args.serve_chunk),
-                            "--device", str(local)], capture_output=True, text=True, timeout=900)
+                            "--check", "4", "--device", str(local)],
+                           capture_output=True, text=True, timeout=900)
         if r.returncode == 0:
             c_host = json.loads(r.stdout.strip().splitlines()[-1])
         else:
@@ -796,8 +797,8 @@ def bench_serving(args, local):
                     "20..80 to T=0.05",
         "requests_by_problem": {"vortex": kinds.get(3, 0), "point_energy": kinds.get(4, 0),
                                 "shock_diffraction": kinds.get(6, 0)},
-        "precision": "FP32-bulk batch (vortex, point energy) beside an FP64 batch (shock "
-                     "diffraction: FP32 error 1e-3 fails the 1e-6 bar)",
+        "precision": "FP32-bulk batch (vortex; point energy to T <= 0.05) beside an FP64 "
+                     "batch (shock diffraction: FP32 error 1e-3 fails the 1e-6 bar)",
         "batched": sb, "plain_fp64_one_at_a_time": sp,
         "throughput_ratio": (sb["value"] / sp["value"]) if sp["value"] else None,
         "slots": args.serve_slots, "step_chunk": args.serve_chunk,

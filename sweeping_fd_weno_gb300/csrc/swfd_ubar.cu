@@ -39,21 +39,26 @@ constexpr int UB_THREADS = 256;
 constexpr int UB_PER = 8;
 constexpr int UB_CHUNK = UB_THREADS * UB_PER;  // 2048 terms
 constexpr int UB_EVC = 128;                    // events of a chunk on the fast path
-constexpr int UB_BATCH = 8;                    // chunks the resolver stages at a time
+constexpr int UB_RCAP = 640;                   // run records the resolver stages at a time
+constexpr int UB_ECAP = 640;                   // event records the resolver stages at a time
 
-// one chunk's summary (terms m0 .. m0 + UB_CHUNK - 1 of one sum)
-struct UbChunk {
-  double sum, asum;          // terms: FP64 sum and absolute sum (estimates)
-  unsigned long long qtot;   // speculate: integer increments of the non-event terms
-  int nev;                   // events (> UB_EVC: the chunk is added term by term)
+// one chunk's summary (terms m0 .. m0 + UB_CHUNK - 1 of one sum): its
+// estimates, its event count, and UB_EVC + 1 run and UB_EVC event records, of
+// which the first nev + 1 and nev are used (runs and events alternate: run 0,
+// event 0, run 1, ..., run nev)
+struct UbEst {
+  double sum, asum;  // terms: FP64 sum and absolute sum of the chunk (estimates)
+};
+struct UbRun {
+  long long lo, hi;          // least / largest (prefix since the run's start + floor)
+  unsigned long long rtot;   // sum of the run's integer increments
+  int g;                     // guessed biased exponent | sign << 11
+  int start, count;          // its terms: chunk positions start .. start + count - 1
   int pad;
-  int ev_pos[UB_EVC];        // position in the chunk
-  unsigned long long ev_q[UB_EVC];  // integer prefix of the chunk at the event
-  double ev_t[UB_EVC];       // the term
-  long long run_lo[UB_EVC + 1], run_hi[UB_EVC + 1];  // run k: least / largest
-                             // (prefix since the run's start + floor of the term)
-  int run_g[UB_EVC + 1];     // run k: guessed biased exponent | sign << 11 (-2: empty)
-  int pad2;
+};
+struct UbEv {
+  double t;                  // the term, added in hardware
+  long long pad;
 };
 
 __host__ __device__ inline int64_t ub_terms(const Params& p) {
@@ -61,9 +66,34 @@ __host__ __device__ inline int64_t ub_terms(const Params& p) {
 }
 __host__ __device__ inline int64_t ub_chunks(int64_t n) { return (n + UB_CHUNK - 1) / UB_CHUNK; }
 
+struct UbScratch {
+  double* T;      // nsum x n terms
+  UbEst* est;     // nsum x nch
+  int* nev;       // nsum x nch (> UB_EVC: the chunk is added term by term)
+  UbRun* runs;    // nsum x nch x (UB_EVC + 1)
+  UbEv* evs;      // nsum x nch x UB_EVC
+};
+
+static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 static size_t ub_bytes(int64_t n, int nsum) {
-  const size_t t = ((size_t)nsum * n * sizeof(double) + 255) & ~(size_t)255;
-  return t + (size_t)nsum * ub_chunks(n) * sizeof(UbChunk) + 256;
+  const size_t nc = (size_t)nsum * ub_chunks(n);
+  return a256(nsum * n * sizeof(double)) + a256(nc * sizeof(UbEst)) + a256(nc * sizeof(int)) +
+         a256(nc * (UB_EVC + 1) * sizeof(UbRun)) + a256(nc * UB_EVC * sizeof(UbEv)) + 256;
+}
+static UbScratch ub_carve(void* scratch, int64_t n, int nsum) {
+  const size_t nc = (size_t)nsum * ub_chunks(n);
+  char* c = (char*)scratch;
+  UbScratch u;
+  u.T = (double*)c;
+  c += a256(nsum * n * sizeof(double));
+  u.est = (UbEst*)c;
+  c += a256(nc * sizeof(UbEst));
+  u.nev = (int*)c;
+  c += a256(nc * sizeof(int));
+  u.runs = (UbRun*)c;
+  c += a256(nc * (UB_EVC + 1) * sizeof(UbRun));
+  u.evs = (UbEv*)c;
+  return u;
 }
 size_t ubar_scratch_bytes(const Params& p) { return ub_bytes(ub_terms(p), p.g.nc); }
 
@@ -133,7 +163,7 @@ __device__ __forceinline__ double ub_block_sum(double v) {
 // i-inner order with w = 1/(nx*ny); 1D u*w over -2..n+3 with w = 1/(n+6)
 __global__ void __launch_bounds__(UB_THREADS) k_ub_terms_state(Params p, const double* __restrict__ u,
                                                                double* __restrict__ T,
-                                                               UbChunk* __restrict__ ch) {
+                                                               UbEst* __restrict__ est) {
   const Geom& g = p.g;
   const int c = blockIdx.y;
   const int64_t n = ub_terms(p), nch = ub_chunks(n);
@@ -168,16 +198,13 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_terms_state(Params p, const d
   }
   s = ub_block_sum(s);
   a = ub_block_sum(a);
-  if (threadIdx.x == 0) {
-    ch[c * nch + blockIdx.x].sum = s;
-    ch[c * nch + blockIdx.x].asum = a;
-  }
+  if (threadIdx.x == 0) est[c * nch + blockIdx.x] = UbEst{s, a};
 }
 
 // the same over a flat array: t(m) = w * x(m) (the test entry point)
 __global__ void __launch_bounds__(UB_THREADS) k_ub_terms_flat(const double* __restrict__ x, int64_t n,
                                                               double w, double* __restrict__ T,
-                                                              UbChunk* __restrict__ ch) {
+                                                              UbEst* __restrict__ est) {
   const int64_t m0 = (int64_t)blockIdx.x * UB_CHUNK + threadIdx.x * UB_PER;
   double s = 0.0, a = 0.0;
   for (int e = 0; e < UB_PER && m0 + e < n; ++e) {
@@ -188,10 +215,7 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_terms_flat(const double* __re
   }
   s = ub_block_sum(s);
   a = ub_block_sum(a);
-  if (threadIdx.x == 0) {
-    ch[blockIdx.x].sum = s;
-    ch[blockIdx.x].asum = a;
-  }
+  if (threadIdx.x == 0) est[blockIdx.x] = UbEst{s, a};
 }
 
 // ---------------------------------------------------------------------------
@@ -215,15 +239,16 @@ __device__ __forceinline__ int ub_guess(double x, double margin) {
 // less -- so (m + 64) * 2^-52 of the absolute sum of the terms bounds both.
 // The bound only sets which terms are treated as events: the resolver's
 // checks keep the result exact whatever the guesses.
-__global__ void __launch_bounds__(UB_THREADS) k_ub_spec(const double* __restrict__ T, int64_t n,
-                                                        UbChunk* __restrict__ ch) {
+__global__ void __launch_bounds__(UB_THREADS) k_ub_spec(UbScratch us, int64_t n) {
   const int c = blockIdx.y, tid = threadIdx.x;
-  const int64_t nch = ub_chunks(n);
-  const double* t_c = T + c * n;
-  UbChunk* chc = ch + c * nch;
-  UbChunk& C = chc[blockIdx.x];
+  const int64_t nch = ub_chunks(n), ci = c * nch + blockIdx.x;
+  const double* t_c = us.T + c * n;
+  const UbEst* estc = us.est + c * nch;
+  UbRun* runs = us.runs + ci * (UB_EVC + 1);
+  UbEv* evs = us.evs + ci * UB_EVC;
   __shared__ int s_last[UB_THREADS];
   __shared__ unsigned long long s_evq[UB_EVC];
+  __shared__ int s_evpos[UB_EVC];
   __shared__ long long s_lo[UB_EVC + 1], s_hi[UB_EVC + 1];
   __shared__ int s_g[UB_EVC + 1];
   for (int k = tid; k <= UB_EVC; k += UB_THREADS) {
@@ -234,13 +259,15 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_spec(const double* __restrict
   // the running sum's estimate at the chunk's start
   double ps = 0.0, pa = 0.0;
   for (int64_t k = tid; k < (int64_t)blockIdx.x; k += UB_THREADS) {
-    ps += chc[k].sum;
-    pa += chc[k].asum;
+    ps += estc[k].sum;
+    pa += estc[k].asum;
   }
   ps = ub_block_sum(ps);
   pa = ub_block_sum(pa);
   // this thread's terms
-  const int64_t m0 = (int64_t)blockIdx.x * UB_CHUNK + tid * UB_PER;
+  const int64_t cm0 = (int64_t)blockIdx.x * UB_CHUNK;
+  const int nvalid = (int)min((int64_t)UB_CHUNK, n - cm0);
+  const int64_t m0 = cm0 + tid * UB_PER;
   const int kv = m0 < n ? (int)min((int64_t)UB_PER, n - m0) : 0;
   double t[UB_PER];
   double ls = 0.0, la = 0.0;
@@ -297,10 +324,9 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_spec(const double* __restrict
     if (e >= kv) continue;
     if ((evm >> e) & 1u) {
       if (k < UB_EVC) {
-        C.ev_pos[k] = tid * UB_PER + e;
-        C.ev_q[k] = q;
-        C.ev_t[k] = t[e];
+        evs[k].t = t[e];
         s_evq[k] = q;
+        s_evpos[k] = tid * UB_PER + e;
       }
       ++k;
     } else {
@@ -308,10 +334,7 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_spec(const double* __restrict
       q += (unsigned long long)(fl[e] + ((upm >> e) & 1u));
     }
   }
-  if (tid == 0) {
-    C.qtot = qtot;
-    C.nev = etot;
-  }
+  if (tid == 0) us.nev[ci] = etot;
   __syncthreads();
   // each run's range of (prefix since its start + floor of the term)
   q = qt;
@@ -332,41 +355,41 @@ __global__ void __launch_bounds__(UB_THREADS) k_ub_spec(const double* __restrict
     }
   }
   __syncthreads();
-  for (int r = tid; r <= min(etot, UB_EVC); r += UB_THREADS) {
-    C.run_lo[r] = s_lo[r];
-    C.run_hi[r] = s_hi[r];
-    C.run_g[r] = s_g[r];
+  if (etot > UB_EVC) return;  // added term by term
+  for (int r = tid; r <= etot; r += UB_THREADS) {
+    const int start = r ? s_evpos[r - 1] + 1 : 0;
+    const int stop = r < etot ? s_evpos[r] : nvalid;
+    const unsigned long long qa = r ? s_evq[r - 1] : 0ull, qb = r < etot ? s_evq[r] : qtot;
+    runs[r] = UbRun{s_lo[r], s_hi[r], qb - qa, s_g[r], start, stop - start, 0};
   }
 }
 
 // ---------------------------------------------------------------------------
 // resolve
 // ---------------------------------------------------------------------------
-// one chunk, in thread 0: terms m0 .. m1-1 of the sum (t_c = its terms).
-// Within a run whose first prefix is checked in range, a prefix that leaves
-// the range does so by less than 2^54 (no step exceeds 2^53 + 1 units), so
-// the recorded least and largest prefixes expose it before any wrap-around.
-__device__ double ub_resolve_chunk(const UbChunk& C, const double* __restrict__ t_c, int64_t m0,
-                                   int64_t m1, double s) {
-  const int nev = C.nev;
+// one chunk, in thread 0: terms m0 .. m0+nvalid-1 of the sum (t_c its terms),
+// nev events, its runs and events staged in shared memory.  Within a run
+// whose start is checked in range, a prefix that leaves the range does so by
+// less than 2^54 (no step exceeds 2^53 + 1 units), so the recorded least and
+// largest prefixes expose it before any wrap-around.
+__device__ double ub_resolve_chunk(int nev, const UbRun* runs, const UbEv* evs,
+                                   const double* __restrict__ t_c, int64_t m0, int nvalid,
+                                   double s) {
   if (nev > UB_EVC) {  // too many events for the summary: term by term
-    for (int64_t m = m0; m < m1; ++m) s = s + t_c[m];
+    for (int m = 0; m < nvalid; ++m) s = s + t_c[m0 + m];
     return s;
   }
-  unsigned long long qprev = 0;
-  int start = 0;
   for (int j = 0; j <= nev; ++j) {
-    const unsigned long long qend = j < nev ? C.ev_q[j] : C.qtot;
-    const int stop = j < nev ? C.ev_pos[j] : (int)(m1 - m0);
-    if (stop > start) {  // the run of terms start .. stop-1
+    const UbRun& R = runs[j];
+    if (R.count > 0) {
       bool ok = false;
       const unsigned long long sb = (unsigned long long)__double_as_longlong(s);
       const int eb = (int)((sb >> 52) & 0x7ff), neg = (int)(sb >> 63);
-      if (eb != 0 && eb != 0x7ff && (eb | (neg << 11)) == C.run_g[j]) {
+      if (eb != 0 && eb != 0x7ff && (eb | (neg << 11)) == R.g) {
         const long long M = (long long)((sb & 0xfffffffffffffull) | (1ull << 52));
-        if (C.run_lo[j] >= (1ll << 52) - M && C.run_hi[j] <= (1ll << 53) - 1 - M) {
+        if (R.lo >= (1ll << 52) - M && R.hi <= (1ll << 53) - 1 - M) {
           // every step of the run is its integer step: the sum is M + R in units of u
-          const unsigned long long val = (unsigned long long)(M + (long long)(qend - qprev));
+          const unsigned long long val = (unsigned long long)(M + (long long)R.rtot);
           unsigned long long bits = (val == (1ull << 53))
                                         ? ((unsigned long long)(eb + 1) << 52)
                                         : (((unsigned long long)eb << 52) | (val - (1ull << 52)));
@@ -376,66 +399,72 @@ __device__ double ub_resolve_chunk(const UbChunk& C, const double* __restrict__ 
         }
       }
       if (!ok)
-        for (int m = start; m < stop; ++m) s = s + t_c[m0 + m];
+        for (int m = R.start; m < R.start + R.count; ++m) s = s + t_c[m0 + m];
     }
-    if (j < nev) {
-      s = s + C.ev_t[j];
-      qprev = C.ev_q[j];
-      start = C.ev_pos[j] + 1;
-    }
+    if (j < nev) s = s + evs[j].t;
   }
   return s;
 }
 
-__global__ void __launch_bounds__(UB_THREADS) k_ub_resolve(const double* __restrict__ T, int64_t n,
-                                                           const UbChunk* __restrict__ ch,
+// one block per sum: batches of up to UB_THREADS chunks whose used records fit
+// the staging arrays are copied to shared memory by all threads, then walked
+// by thread 0
+__global__ void __launch_bounds__(UB_THREADS) k_ub_resolve(UbScratch us, int64_t n,
                                                            double* __restrict__ out) {
-  extern __shared__ unsigned long long ub_stage[];
-  UbChunk* sb = (UbChunk*)ub_stage;
-  const int c = blockIdx.x;
+  __shared__ UbRun s_runs[UB_RCAP];
+  __shared__ UbEv s_evs[UB_ECAP];
+  __shared__ int s_nev[UB_THREADS], s_ro[UB_THREADS], s_eo[UB_THREADS];
+  const int c = blockIdx.x, tid = threadIdx.x;
   const int64_t nch = ub_chunks(n);
-  const double* t_c = T + c * n;
-  const UbChunk* chc = ch + c * nch;
+  const double* t_c = us.T + c * n;
   double s = 0.0;
-  constexpr int W = (int)(sizeof(UbChunk) / 8);
-  for (int64_t b0 = 0; b0 < nch; b0 += UB_BATCH) {
-    const int nb = (int)min((int64_t)UB_BATCH, nch - b0);
-    const unsigned long long* src = (const unsigned long long*)(chc + b0);
-    for (int w = threadIdx.x; w < nb * W; w += blockDim.x) ub_stage[w] = src[w];
+  for (int64_t b0 = 0; b0 < nch;) {
+    const int64_t k = b0 + tid;
+    const int nev = k < nch ? us.nev[c * nch + k] : 0;
+    const int rc = (k < nch && nev <= UB_EVC) ? nev + 1 : 0;
+    const int ec = (k < nch && nev <= UB_EVC) ? nev : 0;
+    int ro, eo;
+    ub_block_excl(rc, ec, ro, eo, (int*)nullptr, (int*)nullptr);
+    // the chunks that fit form a prefix of the batch (the offsets only grow)
+    const bool fits = k < nch && ro + rc <= UB_RCAP && eo + ec <= UB_ECAP;
+    const int nb = __syncthreads_count(fits);
+    s_nev[tid] = nev;
+    s_ro[tid] = ro;
+    s_eo[tid] = eo;
+    if (fits) {
+      const UbRun* rs = us.runs + (c * nch + k) * (UB_EVC + 1);
+      const UbEv* es = us.evs + (c * nch + k) * UB_EVC;
+      for (int r = 0; r < rc; ++r) s_runs[ro + r] = rs[r];
+      for (int e = 0; e < ec; ++e) s_evs[eo + e] = es[e];
+    }
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (tid == 0)
       for (int q = 0; q < nb; ++q) {
         const int64_t m0 = (b0 + q) * UB_CHUNK;
-        s = ub_resolve_chunk(sb[q], t_c, m0, min(n, m0 + UB_CHUNK), s);
+        s = ub_resolve_chunk(s_nev[q], s_runs + s_ro[q], s_evs + s_eo[q], t_c, m0,
+                             (int)min((int64_t)UB_CHUNK, n - m0), s);
       }
     __syncthreads();
+    b0 += nb;
   }
-  if (threadIdx.x == 0) out[c] = s;
+  if (tid == 0) out[c] = s;
 }
 
-static cudaError_t ub_finish(const double* T, int64_t n, int nsum, UbChunk* ch, double* out,
+static cudaError_t ub_finish(const UbScratch& us, int64_t n, int nsum, double* out,
                              cudaStream_t s) {
   const dim3 grid((unsigned)ub_chunks(n), nsum);
-  k_ub_spec<<<grid, UB_THREADS, 0, s>>>(T, n, ch);
-  k_ub_resolve<<<nsum, UB_THREADS, UB_BATCH * sizeof(UbChunk), s>>>(T, n, ch, out);
+  k_ub_spec<<<grid, UB_THREADS, 0, s>>>(us, n);
+  k_ub_resolve<<<nsum, UB_THREADS, 0, s>>>(us, n, out);
   return cudaGetLastError();
-}
-
-static void ub_carve(void* scratch, int64_t n, int nsum, double** T, UbChunk** ch) {
-  *T = (double*)scratch;
-  const size_t t = ((size_t)nsum * n * sizeof(double) + 255) & ~(size_t)255;
-  *ch = (UbChunk*)((char*)scratch + t);
 }
 
 // u_bar of the state into dsc->ubar: three kernels
 cudaError_t launch_ubar(const Params& p, const double* u, DevScalars* dsc, void* scratch,
                         cudaStream_t s) {
   const int64_t n = ub_terms(p);
-  double* T;
-  UbChunk* ch;
-  ub_carve(scratch, n, p.g.nc, &T, &ch);
-  k_ub_terms_state<<<dim3((unsigned)ub_chunks(n), p.g.nc), UB_THREADS, 0, s>>>(p, u, T, ch);
-  return ub_finish(T, n, p.g.nc, ch, dsc->ubar, s);
+  const UbScratch us = ub_carve(scratch, n, p.g.nc);
+  k_ub_terms_state<<<dim3((unsigned)ub_chunks(n), p.g.nc), UB_THREADS, 0, s>>>(p, u, us.T, us.est);
+  return ub_finish(us, n, p.g.nc, dsc->ubar, s);
 }
 
 size_t seq_sum_scratch_bytes(int64_t n) { return ub_bytes(n, 1); }
@@ -444,11 +473,9 @@ size_t seq_sum_scratch_bytes(int64_t n) { return ub_bytes(n, 1); }
 cudaError_t launch_seq_sum(const double* x, int64_t n, double w, double* out, void* scratch,
                            cudaStream_t s) {
   if (n <= 0) return cudaMemsetAsync(out, 0, sizeof(double), s);
-  double* T;
-  UbChunk* ch;
-  ub_carve(scratch, n, 1, &T, &ch);
-  k_ub_terms_flat<<<(unsigned)ub_chunks(n), UB_THREADS, 0, s>>>(x, n, w, T, ch);
-  return ub_finish(T, n, 1, ch, out, s);
+  const UbScratch us = ub_carve(scratch, n, 1);
+  k_ub_terms_flat<<<(unsigned)ub_chunks(n), UB_THREADS, 0, s>>>(x, n, w, us.T, us.est);
+  return ub_finish(us, n, 1, out, s);
 }
 
 }  // namespace swfd

@@ -51,11 +51,24 @@ class ServeResult:
                 "launches": self.launches}
 
 
+# Latest final time at which the FP32-bulk point-energy solve stays within
+# 1e-6 relative L1 density error of the FP64 one: measured on eight seeded
+# instances 236^2..640^2, the worst error is 2.0e-7 at T = 0.02, 3.9e-7 at
+# T = 0.05 and 1.8e-6 at T = 0.21 (it grows with the step count).
+POINT_ENERGY_FP32_T_MAX = 0.05
+
+
 def fp32_accepted(cfg) -> bool:
     """The FP32-bulk form is accepted where its relative L1 density error
-    against FP64 stays below 1e-6: the vortex and the point-energy problems.
-    The jet (kinetic-dominated) and the shock diffraction (~1e-3) stay FP64."""
-    return cfg.problem in (abi.VORTEX_2D, abi.SEDOV_2D)
+    against FP64 stays below 1e-6: the vortex (1.8e-8 at T = 0.01 on 360^2),
+    and the point energy up to T = POINT_ENERGY_FP32_T_MAX.  Longer
+    point-energy runs (the batched configuration runs to T = 1), the jet
+    (kinetic-dominated) and the shock diffraction (~1e-3) stay FP64."""
+    if cfg.problem == abi.VORTEX_2D:
+        return True
+    if cfg.problem == abi.SEDOV_2D:
+        return cfg.time_terminal <= POINT_ENERGY_FP32_T_MAX
+    return False
 
 
 def serve_batched(arrivals, batches, step_chunk: int = 4, timeout: float = 600.0,
