@@ -1039,9 +1039,43 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
 // SM and each has shorter dependent chains, at the price of the eigenvectors
 // computed twice.  Every value is the one-lane form's expression.
 // ---------------------------------------------------------------------------
-template <int YDIR, int SIDE, class D>
+// One reconstruction for lane side s as a single instruction stream for both
+// sides: weno_right (s = 0) and weno_left (s = 1) of stencil v0..v4 have the
+// same shape -- three candidates k1*v_a + k2*v_b + k3*v_c over the same
+// positions, the same smoothness indicators, the weights d/(eps+beta)^2
+// normalised by three divisions, and w1*A + w2*B + w3*C -- and differ only in
+// the constants, which each lane selects; so a warp whose lanes take both
+// sides does not diverge, and each side's operations, operands and their
+// order are the reference's (weno5.f90:86-146).
+template <class D>
+__device__ __forceinline__ double weno_side(double v0, double v1, double v2, double v3, double v4,
+                                            int side, double eps, D div) {
+  // weno_right: A = um3 = c13 v2 + c56 v3 + cm16 v4,  B = um2 = cm16 v1 + c56 v2 + c13 v3,
+  //             C = um1 = c13 v0 + cm76 v1 + c116 v2, weights d = 0.3, 0.6, 0.1
+  // weno_left:  A = up3 = c116 v2 + cm76 v3 + c13 v4, B = up2 = c13 v1 + c56 v2 + cm16 v3,
+  //             C = up1 = cm16 v0 + c56 v1 + c13 v2,  weights d = 0.1, 0.6, 0.3
+  const bool l = side != 0;
+  const double a1 = l ? SWFD_C116 : SWFD_C13, a2 = l ? SWFD_CM76 : SWFD_C56,
+               a3 = l ? SWFD_C13 : SWFD_CM16;
+  const double b1 = l ? SWFD_C13 : SWFD_CM16, b3 = l ? SWFD_CM16 : SWFD_C13;
+  const double c1 = l ? SWFD_CM16 : SWFD_C13, c2 = l ? SWFD_C56 : SWFD_CM76,
+               c3 = l ? SWFD_C13 : SWFD_C116;
+  const double d1 = l ? 0.1 : 0.3, d3 = l ? 0.3 : 0.1;
+  const double A = a1 * v2 + a2 * v3 + a3 * v4;
+  const double B = b1 * v1 + SWFD_C56 * v2 + b3 * v3;
+  const double C = c1 * v0 + c2 * v1 + c3 * v2;
+  double be1, be2, be3;
+  weno_beta(v0, v1, v2, v3, v4, be1, be2, be3);
+  const double w1 = div(d1, tsq(eps + be1));
+  const double w2 = div(0.6, tsq(eps + be2));
+  const double w3 = div(d3, tsq(eps + be3));
+  const double sum = w1 + w2 + w3;
+  return div(w1, sum) * A + div(w2, sum) * B + div(w3, sum) * C;
+}
+
+template <int YDIR, class D>
 __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const double* __restrict__ s,
-                                           int64_t P, int64_t step, double weps, D div,
+                                           int64_t P, int64_t step, double weps, int side, D div,
                                            double out[4]) {
   double w[4];
 #pragma unroll
@@ -1056,8 +1090,7 @@ __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const doubl
       else if (k == 2) c[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, a0, a1, a2, a3);
       else c[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, a0, a1, a2, a3);
     }
-    w[k] = SIDE == 0 ? weno_right(c[0], c[1], c[2], c[3], c[4], weps, div)
-                     : weno_left(c[0], c[1], c[2], c[3], c[4], weps, div);
+    w[k] = weno_side(c[0], c[1], c[2], c[3], c[4], side, weps, div);
   }
   // evr . w (as interface_flux's back projection)
   const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
@@ -1069,20 +1102,20 @@ __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const doubl
 struct Side4 {
   double v[4];
 };
-template <int YDIR, int SIDE>
+template <int YDIR>
 static __device__ __noinline__ Side4 weno4_side_hw(Eigen2D<double> E, const double* s, int64_t P,
-                                                   int64_t step, double weps) {
+                                                   int64_t step, double weps, int side) {
   Side4 r;
-  weno4_side<YDIR, SIDE>(E, s, P, step, weps, DivHw(), r.v);
+  weno4_side<YDIR>(E, s, P, step, weps, side, DivHw(), r.v);
   return r;
 }
-template <int YDIR, int SIDE>
+template <int YDIR>
 __device__ __forceinline__ void side_flux(const Eigen2D<double>& E, const double* s, int64_t P,
-                                          int64_t step, double weps, double out[4]) {
+                                          int64_t step, double weps, int side, double out[4]) {
   int bad = 0;
-  weno4_side<YDIR, SIDE>(E, s, P, step, weps, DivFlag{&bad}, out);
+  weno4_side<YDIR>(E, s, P, step, weps, side, DivFlag{&bad}, out);
   if (bad) {
-    const Side4 r = weno4_side_hw<YDIR, SIDE>(E, s, P, step, weps);
+    const Side4 r = weno4_side_hw<YDIR>(E, s, P, step, weps, side);
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = r.v[k];
   }
@@ -1108,8 +1141,7 @@ __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* _
     roe_eigen2d<double>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
                         ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
                         ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
-    if (side == 0) side_flux<0, 0>(E, split + o - 2, S, 1, weps, o4);
-    else side_flux<0, 1>(E, split + 4 * S + o - 2, S, 1, weps, o4);
+    side_flux<0>(E, split + 4 * side * S + o - 2, S, 1, weps, side, o4);
 #pragma unroll
     for (int k = 0; k < 4; ++k) flux[(4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
   } else {
@@ -1122,8 +1154,7 @@ __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* _
     roe_eigen2d<double>(g1, 1, ldt(rr + o), ldt(rr + o + pit), ldt(rr + P + o),
                         ldt(rr + P + o + pit), ldt(rr + 2 * P + o), ldt(rr + 2 * P + o + pit),
                         ldt(rr + 3 * P + o), ldt(rr + 3 * P + o + pit), E);
-    if (side == 0) side_flux<1, 0>(E, split + 8 * S + o - 2 * spit, S, spit, weps, o4);
-    else side_flux<1, 1>(E, split + 12 * S + o - 2 * spit, S, spit, weps, o4);
+    side_flux<1>(E, split + (8 + 4 * side) * S + o - 2 * spit, S, spit, weps, side, o4);
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       flux[(8 + 4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
