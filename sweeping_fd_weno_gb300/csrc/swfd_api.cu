@@ -585,10 +585,45 @@ void emit_sweep(Builder& b, cudaStream_t s, double* u) {
 // without rank segments); stage 1's findalpha, which also sets dt, stays apart
 bool fused_alpha(const Params& p) { return p.g.ndim == 2 && !p.seg_alpha; }
 
+// The FP32-bulk fused stage: findalpha + terms (stage 1, with dt), the
+// stage kernel, [sweep], bc + the next stage's findalpha + terms (stages 1
+// and 2) or the bc alone (stage 3).  The split planes hold the terms.
+void emit_stage32(Builder& b, cudaStream_t s, int k, double* in, double* u0, double* out,
+                  bool events) {
+  swfd_handle* h = b.h;
+  const Params& p = h->p;
+  if (k == 1) {
+    B_OK(b, launch_alpha_terms32(p, in, h->dsc, s, false, true, h->split, h->roe));
+    b.k(1);
+  }
+  if (events)
+    B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1)], s)
+                    : cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
+  const bool sweeps = h->cfg.use_limiter == 2;
+  const cudaGraphConditionalHandle hs = sweeps ? b.handle() : 0;
+  B_OK(b, launch_stage32(p, k, in, u0, h->split, h->roe, h->dsc, out, s, hs, sweeps ? 1 : 0));
+  b.k(1);
+  if (events)
+    B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1) + 1], s)
+                    : cudaEventRecordWithFlags(h->ev[2 * (k - 1) + 1], s,
+                                               cudaEventRecordExternal));
+  if (sweeps) {
+    int* saved = b.count;
+    h->k_sweep_fixed = 0;
+    b.count = &h->k_sweep_fixed;
+    b.cond(s, cudaGraphCondTypeIf, hs, [&](cudaStream_t sw) { emit_sweep(b, sw, out); });
+    b.count = saved;
+  }
+  if (k < 3) B_OK(b, launch_alpha_terms32(p, out, h->dsc, s, true, false, h->split, h->roe));
+  else B_OK(b, launch_bc(p, out, s));
+  b.k(1);
+}
+
 void emit_stage(Builder& b, cudaStream_t s, int k, double* in, double* u0, double* out,
                 bool events) {
   swfd_handle* h = b.h;
   const Params& p = h->p;
+  if (h->stage32) return emit_stage32(b, s, k, in, u0, out, events);
   if (k == 1 || !fused_alpha(p)) {
     B_OK(b, launch_alpha(p, in, h->dsc, s, k == 1));
     b.k(1);
@@ -967,6 +1002,14 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     const char* lm = getenv("SWFD_LAUNCH");
     h->eager = lm && strcmp(lm, "eager") == 0;
   }
+  {  // the fused FP32-bulk stage where it applies (SWFD_FP32_STAGE=split: the
+     // separate splitting, flux and RK kernels, the same bits)
+    const Params& q = h->p;
+    const char* fs = getenv("SWFD_FP32_STAGE");
+    h->stage32 = q.precision == SWFD_PRECISION_FP32_BULK && q.g.ndim == 2 && !q.seg_alpha &&
+                 !q.limiter && !q.quad && cfg->rk_choice != 2 &&
+                 !(fs && strcmp(fs, "split") == 0);
+  }
   const Geom& g = h->p.g;
   auto cleanup_fail = [&](cudaError_t e) {
     std::string m = std::string("swfd_create: ") + cudaGetErrorString(e);
@@ -977,6 +1020,7 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
   if (e != cudaSuccess) return cleanup_fail(e);
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return cleanup_fail(e);
+  if (h->stage32 && (e = stage32_setup()) != cudaSuccess) return cleanup_fail(e);
   const size_t pb = (size_t)g.plane * sizeof(double);
   for (int k = 0; k < 3; ++k)
     if ((e = cudaMalloc(&h->st[k], g.nc * pb)) != cudaSuccess) return cleanup_fail(e);
@@ -1192,7 +1236,8 @@ swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
   CU(h, cudaSetDevice(h->device));
   *flux_min_blocks = 0;
   Params& p = h->p;
-  if (p.g.ndim != 2 || p.seg_alpha || p.limiter) return SWFD_OK;
+  // the fused FP32-bulk stage has one launch shape
+  if (p.g.ndim != 2 || p.seg_alpha || p.limiter || h->stage32) return SWFD_OK;
   // the flux kernel's inputs for the current state (findalpha and the
   // splitting only rewrite per-stage scratch: alphamax, split and Roe planes)
   double* u = cur_state(h);

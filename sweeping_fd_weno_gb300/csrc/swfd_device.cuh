@@ -73,14 +73,16 @@ __device__ __forceinline__ double rcp_bulk(double x) { return sd::div(1.0, x); }
 
 // binary64 <-> binary32 conversions on the integer pipes, the bits of the
 // hardware conversions (round to nearest even): GB300 runs conversions to
-// and from 64-bit types at the FP64 rate.  Zero, subnormal, infinite, NaN
-// and out-of-range values take the hardware conversion (out of line).
+// and from 64-bit types at the FP64 rate.  Zeros keep their sign inline
+// (tested in the out-of-range branch only); subnormal, infinite, NaN and
+// out-of-range values take the hardware conversion (out of line).
 static __device__ __noinline__ float d2f_hw(double x) { return (float)x; }
 static __device__ __noinline__ double f2d_hw(float x) { return (double)x; }
 __device__ __forceinline__ float d2f(double x) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((u >> 52) & 0x7ff) - 1023 + 127;
-  if ((unsigned)(e - 1) >= 254u) return d2f_hw(x);
+  if ((unsigned)(e - 1) >= 254u)  // +-0 inline, the rest out of line
+    return (u << 1) == 0 ? __uint_as_float((unsigned)(u >> 32)) : d2f_hw(x);
   const unsigned long long m = u & 0xfffffffffffffull;
   unsigned r = (unsigned)(m >> 29);
   const unsigned rem = (unsigned)m & 0x1fffffffu;
@@ -91,7 +93,9 @@ __device__ __forceinline__ float d2f(double x) {
 __device__ __forceinline__ double f2d(float x) {
   const unsigned b = __float_as_uint(x);
   const unsigned e = (b >> 23) & 0xffu;
-  if (e - 1u >= 254u) return f2d_hw(x);
+  if (e - 1u >= 254u)  // +-0 inline, the rest out of line
+    return (b << 1) == 0u ? __longlong_as_double((long long)((unsigned long long)b << 32))
+                          : f2d_hw(x);
   return __longlong_as_double((long long)(((unsigned long long)(b & 0x80000000u) << 32) |
                                           ((unsigned long long)(e + 896u) << 52) |
                                           ((unsigned long long)(b & 0x7fffffu) << 29)));

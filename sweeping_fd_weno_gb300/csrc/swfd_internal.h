@@ -282,6 +282,9 @@ struct swfd_handle {
   // profilers that do not look inside graphs with conditional nodes
   int eager = 0;
   long long eager_launches = 0;
+  // FP32-bulk 2D stages as two kernels (k_alpha_terms32, k_stage32); off
+  // with rank segments, the limiter, and SWFD_FP32_STAGE=split
+  int stage32 = 0;
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles
@@ -306,6 +309,19 @@ cudaError_t launch_bc_alpha(const Params& p, double* u, DevScalars* dsc, cudaStr
 // dsc's alpha_bits and alpha_done are zero between launches.
 cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s,
                          bool with_dt = false);
+// FP32-bulk fused stage (2D, no rank segments, no limiter): [bc,] findalpha
+// [and dt] with the nine splitting terms and the Roe planes of every cell
+// (terms: 9 float planes of the state's pitch; roe: the splitting's Roe
+// planes), then one kernel for the split fluxes, interface fluxes, RHS, RK
+// combination and checkpositivity of a stage.  stage32_setup sets the
+// kernel's dynamic shared memory limit (once per process and device).
+cudaError_t launch_alpha_terms32(const Params& p, double* u, DevScalars* dsc, cudaStream_t s,
+                                 bool bc, bool with_dt, void* terms, void* roe);
+cudaError_t launch_stage32(const Params& p, int stage, const double* u, const double* u0,
+                           const void* terms, const void* roe, DevScalars* dsc, double* out,
+                           cudaStream_t s, cudaGraphConditionalHandle hs, int decide);
+cudaError_t stage32_setup();
+size_t stage32_smem_bytes();
 // split, roe and flux planes hold doubles (FP64) or floats (FP32 bulk)
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
                         void* roe, cudaStream_t s, int which = 3);
@@ -347,6 +363,8 @@ cudaError_t launch_batch_alpha(const BatchLaunch& b, int in, cudaStream_t s);
 // values SWFD_FLUX_PAIR + b select the lane-pair kernel with b blocks per SM);
 // returns their number, the default first
 #define SWFD_FLUX_PAIR 10
+// the FP64 flux kernel's default shape: the lane-pair kernel, 4 blocks per SM
+#define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_PAIR + 4)
 int flux_min_blocks_candidates(bool f32, int* out);
 cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
 cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,

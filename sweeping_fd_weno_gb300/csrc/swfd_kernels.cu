@@ -7,6 +7,13 @@ namespace swfd {
 #define SWFD_BLOCK 256
 
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
+// NC: the read-only (non-coherent) path; false for values this kernel may
+// have written itself
+template <bool NC>
+__device__ __forceinline__ double ldc(const double* p) {
+  if constexpr (NC) return __ldg(p);
+  else return *p;
+}
 
 // ---------------------------------------------------------------------------
 // bc: every ghost cell gets its final value directly, resolved through the
@@ -116,6 +123,7 @@ __device__ __forceinline__ double block_max(double v) {
   return v;
 }
 
+template <bool NC = true>
 __device__ __forceinline__ double alpha_cell(const Params& p, const double* __restrict__ u,
                                              int64_t t) {
   const Geom& g = p.g;
@@ -127,15 +135,15 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
     const double g1 = p.gamma1, gamma = p.gamma;
     if (g.ndim == 1) {
       // ex2_sedov_1d/main.f90:278-283
-      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o);
+      double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o);
       double pres = g1 * (u3 - tscale<-1>(tdiv(u2 * u2, u1)));
       double sound = sqrt(tdiv(gamma * pres, u1));
       a = fabs(tdiv(u2, u1)) + sound;
     } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
       // FP32-bulk: the pressure recovered in FP64 (one reciprocal per cell);
       // the CFL quantities (velocities, sound speed, their max) in FP32
-      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
-             u4 = ld(u + 3 * g.plane + o);
+      double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o),
+             u4 = ldc<NC>(u + 3 * g.plane + o);
       const double ri = rcp_bulk(u1);
       double pres;
       if (!p.alpha_guarded) {
@@ -148,8 +156,8 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
       const float sound = sqrtf(d2f(gamma) * d2f(pres) * fri);
       a = f2d(fmaxf(fabsf(d2f(u2) * fri), fabsf(d2f(u3) * fri)) + sound);
     } else {
-      double u1 = ld(u + o), u2 = ld(u + g.plane + o), u3 = ld(u + 2 * g.plane + o),
-             u4 = ld(u + 3 * g.plane + o);
+      double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o),
+             u4 = ldc<NC>(u + 3 * g.plane + o);
       if (!p.alpha_guarded) {
         // ex3_vortex_accuracy_2d/main.f90:556-559
         double pres = g1 * (u4 - tscale<-1>(tdiv(u2 * u2, u1)) - tscale<-1>(tdiv(u3 * u3, u1)));
@@ -193,12 +201,10 @@ __device__ __forceinline__ void dt_body(const Params& p, DevScalars* dsc);
 // re-arms the accumulator and the block counter for the next launch, so a
 // stage needs neither a reset nor a single-thread finishing kernel.  It also
 // clears postag, which the RK kernel of the same stage accumulates.
-__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc, int with_dt) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double a = alpha_cell(p, u, t);
-  alpha_store(p, t, a);
-  a = block_max(a);
-  if (threadIdx.x != 0) return;
+// the block's maximum a folded into alpha_bits by thread 0; the last block
+// finishes the reduction (and, with_dt, the dt rule)
+__device__ __forceinline__ void alpha_last_block(const Params& p, DevScalars* dsc, double a,
+                                                 int with_dt) {
   atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
   __threadfence();
   if (atomicAdd(&dsc->alpha_done, 1) != (int)gridDim.x - 1) return;
@@ -211,27 +217,29 @@ __global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc,
   if (with_dt) dt_body(p, dsc);
 }
 
+__global__ void k_alpha(Params p, const double* __restrict__ u, DevScalars* dsc, int with_dt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double a = alpha_cell(p, u, t);
+  alpha_store(p, t, a);
+  a = block_max(a);
+  if (threadIdx.x != 0) return;
+  alpha_last_block(p, dsc, a, with_dt);
+}
+
 // bc followed by the next stage's findalpha, in one pass over the cells: each
 // thread fills its ghost cell (bc2d_cell), then takes the alpha of its cell
-// from the value it just wrote or, for an interior cell, from the state the
-// RK stage and the sweep left; the block maxima and the last block's
-// decisions are k_alpha's.  Problems with rank segments keep their separate
-// findalpha (their per-cell alphas feed the per-row and per-column maxima).
+// from the value it just wrote (a coherent load) or, for an interior cell,
+// from the state the RK stage and the sweep left; the block maxima and the
+// last block's decisions are k_alpha's.  Problems with rank segments keep
+// their separate findalpha (their per-cell alphas feed the per-row and
+// per-column maxima).
 __global__ void k_bc2d_alpha(Params p, double* __restrict__ u, DevScalars* dsc) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bc2d_cell(p, u, t);
-  double a = alpha_cell(p, u, t);
+  double a = alpha_cell<false>(p, u, t);
   a = block_max(a);
   if (threadIdx.x != 0) return;
-  atomicMax(&dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
-  __threadfence();
-  if (atomicAdd(&dsc->alpha_done, 1) != (int)gridDim.x - 1) return;
-  __threadfence();
-  const unsigned long long m = atomicExch(&dsc->alpha_bits, 0ull);
-  dsc->alpha_done = 0;
-  dsc->postag = 0;
-  dsc->alphamax = __longlong_as_double((long long)m);
-  if (!isfinite(dsc->alphamax) || !(dsc->alphamax > 0.0)) dsc->error |= 1;
+  alpha_last_block(p, dsc, a, 0);
 }
 
 // Threads per block of the per-cell kernels: 256, or fewer (down to one warp)
@@ -390,6 +398,84 @@ __device__ __forceinline__ double reg_recip(const Params& p, double den) {
   return sd::div(1., den + 1e-15);
 }
 
+// FP32-bulk splitting of one cell (no rank segments): the pressure recovered
+// in FP64 (fused multiply-adds, one reciprocal), the conserved values and the
+// x and y fluxes rounded to binary32 and formed there.  The Lax-Friedrichs
+// split fluxes 0.5 (a +- f/alpha) come from these nine terms through
+// split_pm, whether the splitting kernel forms them or the fused stage
+// kernel does in its shared-memory tile: the same operations, the same bits.
+struct Terms32 {
+  float fr, fm, fn, fe;  // rho, m, n, E
+  float f1, fxy, f3;     // x fluxes rho u^2 + p, rho u v, (E + p) u (the first is m)
+  float g2, g3;          // y fluxes rho v^2 + p, (E + p) v (the first is n, the second fxy)
+};
+struct Prim32 {  // FP64 velocities and pressure of the splitting (the Roe planes reuse them)
+  double vx, vy, pres;
+  bool guard;
+};
+__device__ __forceinline__ Terms32 terms32(const Params& p, double rho, double mx, double my,
+                                           double e, double ri, Prim32& q) {
+  double vx = mx * ri, vy = my * ri;
+  q.guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
+  if (q.guard) vx = vy = 0.;
+  q.pres = p.gamma1 * fma(-0.5 * rho, fma(vx, vx, vy * vy), e);
+  q.vx = vx;
+  q.vy = vy;
+  Terms32 t;
+  t.fr = d2f(rho), t.fm = d2f(mx), t.fn = d2f(my), t.fe = d2f(e);
+  const float fvx = d2f(vx), fvy = d2f(vy), fp = d2f(q.pres);
+  t.fxy = t.fr * fvx * fvy;
+  t.f1 = fmaf(t.fr * fvx, fvx, fp);
+  t.f3 = (t.fe + fp) * fvx;
+  t.g2 = fmaf(t.fr * fvy, fvy, fp);
+  t.g3 = (t.fe + fp) * fvy;
+  return t;
+}
+// 0.5 (a + f/alpha) and 0.5 (a - f/alpha) with ram = 1/alpha, each one
+// rounding of a fused multiply-add and an exact halving
+__device__ __forceinline__ void split_pm(float a, float f, float ram, float& sp, float& sn) {
+  sp = 0.5f * fmaf(f, ram, a);
+  sn = 0.5f * fmaf(-f, ram, a);
+}
+// the 16 split values of a cell in the plane order of the split planes:
+// fp (0..3), fn (4..7), gp (8..11), gn (12..15)
+__device__ __forceinline__ void split32(const Terms32& t, float ram, float s[16]) {
+  split_pm(t.fr, t.fm, ram, s[0], s[4]);
+  split_pm(t.fm, t.f1, ram, s[1], s[5]);
+  split_pm(t.fn, t.fxy, ram, s[2], s[6]);
+  split_pm(t.fe, t.f3, ram, s[3], s[7]);
+  split_pm(t.fr, t.fn, ram, s[8], s[12]);
+  split_pm(t.fm, t.fxy, ram, s[9], s[13]);
+  split_pm(t.fn, t.g2, ram, s[10], s[14]);
+  split_pm(t.fe, t.g3, ram, s[11], s[15]);
+}
+// the Roe planes of the FP32-bulk preparation; the enthalpy reuses the
+// recovered pressure (x pass) and, with the ex4 regularisers, the y pass has
+// its own (ex4_sedov_2d/main.f90:426)
+__device__ __forceinline__ void roe32_store(const Params& p, double rho, double mx, double my,
+                                            double e, double ri, const Prim32& q, float fr,
+                                            float* __restrict__ roe, int64_t P, int64_t o,
+                                            int which) {
+  const double g1 = p.gamma1;
+  if (which & 1) {
+    const double vex = q.guard ? mx * ri : q.vx, vey = q.guard ? my * ri : q.vy;
+    const double pre = q.guard ? g1 * fma(-0.5, fma(mx, vex, my * vey), e) : q.pres;
+    roe[0 * P + o] = sqrtf(fabsf(fr));
+    roe[1 * P + o] = d2f(vex);
+    roe[2 * P + o] = d2f(vey);
+    roe[3 * P + o] = d2f((pre + e) * ri);
+  }
+  if (p.roe_reg_ex4 && (which & 2)) {
+    const double t0 = 1. / (rho + 1e-15);
+    const double vex = mx * t0, vey = my * t0;
+    const double pre = g1 * fma(-0.5, fma(mx, vex, my * vey), e);
+    roe[4 * P + o] = sqrtf(fabsf(fr));
+    roe[5 * P + o] = d2f(vex);
+    roe[6 * P + o] = d2f(vey);
+    roe[7 * P + o] = d2f((pre + e) * t0);
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __restrict__ u,
                                             double amd, T* __restrict__ split, T* __restrict__ roe,
@@ -405,47 +491,15 @@ __device__ __forceinline__ void prep2d_cell(const Params& p, const double* __res
   const double ri = F32 ? rcp_bulk(rho) : 0.;
   if constexpr (F32) {
     if (!p.seg_alpha) {
-      // FP32-bulk: the pressure recovered in FP64 (fused multiply-adds, one
-      // reciprocal), the fluxes and the splitting in FP32; the Roe enthalpy
-      // reuses the recovered pressure
-      double vx = mx * ri, vy = my * ri;
-      const bool guard = p.flux_guard_eps2 ? (rho < p.eps2) : (rho < p.lim8_lt);
-      if (guard) vx = vy = 0.;
-      const double pres = g1 * fma(-0.5 * rho, fma(vx, vx, vy * vy), e);
-      const float fr = d2f(rho), fm = d2f(mx), fn = d2f(my), fe = d2f(e);
-      const float fvx = d2f(vx), fvy = d2f(vy), fp = d2f(pres);
-      const float fxy = fr * fvx * fvy;
-      const float f1 = fmaf(fr * fvx, fvx, fp), f3 = (fe + fp) * fvx;
-      const float g2 = fmaf(fr * fvy, fvy, fp), g3 = (fe + fp) * fvy;
-      const float ram = 1.f / d2f(amd), hf = 0.5f;
+      Prim32 q;
+      const Terms32 tm = terms32(p, rho, mx, my, e, ri, q);
+      const float ram = 1.f / d2f(amd);
       const int64_t S = p.sg.plane;
-      float q;
-      q = fm * ram;  split[0 * S + o] = hf * (fr + q);  split[4 * S + o] = hf * (fr - q);
-      q = f1 * ram;  split[1 * S + o] = hf * (fm + q);  split[5 * S + o] = hf * (fm - q);
-      const float qxy = fxy * ram;
-      split[2 * S + o] = hf * (fn + qxy); split[6 * S + o] = hf * (fn - qxy);
-      q = f3 * ram;  split[3 * S + o] = hf * (fe + q);  split[7 * S + o] = hf * (fe - q);
-      q = fn * ram;  split[8 * S + o] = hf * (fr + q);  split[12 * S + o] = hf * (fr - q);
-      split[9 * S + o] = hf * (fm + qxy); split[13 * S + o] = hf * (fm - qxy);
-      q = g2 * ram;  split[10 * S + o] = hf * (fn + q); split[14 * S + o] = hf * (fn - q);
-      q = g3 * ram;  split[11 * S + o] = hf * (fe + q); split[15 * S + o] = hf * (fe - q);
-      if (which & 1) {
-        const double vex = guard ? mx * ri : vx, vey = guard ? my * ri : vy;
-        const double pre = guard ? g1 * fma(-0.5, fma(mx, vex, my * vey), e) : pres;
-        roe[0 * P + o] = sqrtf(fabsf(fr));
-        roe[1 * P + o] = d2f(vex);
-        roe[2 * P + o] = d2f(vey);
-        roe[3 * P + o] = d2f((pre + e) * ri);
-      }
-      if (p.roe_reg_ex4 && (which & 2)) {  // ex4_sedov_2d/main.f90:426
-        const double t0 = 1. / (rho + 1e-15);
-        const double vex = mx * t0, vey = my * t0;
-        const double pre = g1 * fma(-0.5, fma(mx, vex, my * vey), e);
-        roe[4 * P + o] = sqrtf(fabsf(fr));
-        roe[5 * P + o] = d2f(vex);
-        roe[6 * P + o] = d2f(vey);
-        roe[7 * P + o] = d2f((pre + e) * t0);
-      }
+      float sp[16];
+      split32(tm, ram, sp);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) split[k * S + o] = sp[k];
+      roe32_store(p, rho, mx, my, e, ri, q, tm.fr, roe, P, o, which);
       return;
     }
   }
@@ -678,6 +732,56 @@ static __device__ __noinline__ Weno8 weno8_hw(Eigen2D<double> E, const double* s
   return w;
 }
 
+// the eight binary32 reconstructions of one interface from its stencil
+// values, [stencil cell][component] of the positive (a) and negative (b)
+// split fluxes: each is projected onto the four characteristic fields and
+// reconstructed (weno_right for a, weno_left for b)
+template <int YDIR>
+__device__ __forceinline__ void weno8_f32(const Eigen2D<float>& E, const float (&a)[5][4],
+                                          const float (&b)[5][4], float weps, float ur[4],
+                                          float ul[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float cp[5], cn[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const float *x = a[m], *y = b[m];
+      if (k == 0) {
+        cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, x[0], x[1], x[2], x[3]);
+        cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, y[0], y[1], y[2], y[3]);
+      } else if (k == 1) {
+        cp[m] = proj_row2<YDIR>(E.vt, x[0], x[1], x[2]);
+        cn[m] = proj_row2<YDIR>(E.vt, y[0], y[1], y[2]);
+      } else if (k == 2) {
+        cp[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, x[0], x[1], x[2], x[3]);
+        cn[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, y[0], y[1], y[2], y[3]);
+      } else {
+        cp[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, x[0], x[1], x[2], x[3]);
+        cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, y[0], y[1], y[2], y[3]);
+      }
+    }
+    ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
+    ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
+  }
+}
+
+// evr . ur (main.f90:226-229): row 1 [1,0,1,1]; normal-momentum row
+// [vn-c, 0, vn, vn+c]; tangential row [vt, 1, vt, vt]; energy row
+// [H-vn c, vt, q, H+vn c]
+template <int YDIR, class T>
+__device__ __forceinline__ void back_project(const Eigen2D<T>& E, const T ur[4], const T ul[4],
+                                             T outp[4], T outn[4]) {
+  const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
+  outp[0] = ur[0] + ur[2] + ur[3];
+  outn[0] = ul[0] + ul[2] + ul[3];
+  outp[n] = E.e_nm * ur[0] + E.vn * ur[2] + E.e_np * ur[3];
+  outn[n] = E.e_nm * ul[0] + E.vn * ul[2] + E.e_np * ul[3];
+  outp[tt] = E.vt * ur[0] + ur[1] + E.vt * ur[2] + E.vt * ur[3];
+  outn[tt] = E.vt * ul[0] + ul[1] + E.vt * ul[2] + E.vt * ul[3];
+  outp[3] = E.e_hm * ur[0] + E.vt * ur[1] + E.qm * ur[2] + E.e_hp * ur[3];
+  outn[3] = E.e_hm * ul[0] + E.vt * ul[1] + E.qm * ul[2] + E.e_hp * ul[3];
+}
+
 template <int YDIR, class T, bool QD = false>
 __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __restrict__ sp,
                                                const T* __restrict__ sn, int64_t P, int64_t step,
@@ -696,29 +800,7 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
         a[m][c] = ldt(sp + m * step + c * P);
         b[m][c] = ldt(sn + m * step + c * P);
       }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      T cp[5], cn[5];
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const T *x = a[m], *y = b[m];
-        if (k == 0) {
-          cp[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, x[0], x[1], x[2], x[3]);
-          cn[m] = proj_row<YDIR>(E.l1_0, E.l1_n, E.l1_t, E.l1_3, y[0], y[1], y[2], y[3]);
-        } else if (k == 1) {
-          cp[m] = proj_row2<YDIR>(E.vt, x[0], x[1], x[2]);
-          cn[m] = proj_row2<YDIR>(E.vt, y[0], y[1], y[2]);
-        } else if (k == 2) {
-          cp[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, x[0], x[1], x[2], x[3]);
-          cn[m] = proj_row<YDIR>(E.l3_0, E.l3_n, E.l3_t, E.l3_3, y[0], y[1], y[2], y[3]);
-        } else {
-          cp[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, x[0], x[1], x[2], x[3]);
-          cn[m] = proj_row<YDIR>(E.l4_0, E.l4_n, E.l4_t, E.l4_3, y[0], y[1], y[2], y[3]);
-        }
-      }
-      ur[k] = weno_right(cp[0], cp[1], cp[2], cp[3], cp[4], weps);
-      ul[k] = weno_left(cn[0], cn[1], cn[2], cn[3], cn[4], weps);
-    }
+    weno8_f32<YDIR>(E, a, b, weps, ur, ul);
   } else if constexpr (!QD) {
     // every division without its fallback branch; one check for all eight
     int bad = 0;
@@ -758,18 +840,7 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
     ur[k] = weno_right_qd(cp[0], cp[1], cp[2], cp[3], cp[4], *qw);
     ul[k] = weno_left_qd(cn[0], cn[1], cn[2], cn[3], cn[4], *qw);
   }
-  // evr . ur (main.f90:226-229): row 1 [1,0,1,1]; normal-momentum row
-  // [vn-c, 0, vn, vn+c]; tangential row [vt, 1, vt, vt]; energy row
-  // [H-vn c, vt, q, H+vn c]
-  const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
-  outp[0] = ur[0] + ur[2] + ur[3];
-  outn[0] = ul[0] + ul[2] + ul[3];
-  outp[n] = E.e_nm * ur[0] + E.vn * ur[2] + E.e_np * ur[3];
-  outn[n] = E.e_nm * ul[0] + E.vn * ul[2] + E.e_np * ul[3];
-  outp[tt] = E.vt * ur[0] + ur[1] + E.vt * ur[2] + E.vt * ur[3];
-  outn[tt] = E.vt * ul[0] + ul[1] + E.vt * ul[2] + E.vt * ul[3];
-  outp[3] = E.e_hm * ur[0] + E.vt * ur[1] + E.qm * ur[2] + E.e_hp * ur[3];
-  outn[3] = E.e_hm * ul[0] + E.vt * ul[1] + E.qm * ul[2] + E.e_hp * ul[3];
+  back_project<YDIR, T>(E, ur, ul, outp, outn);
 }
 
 // 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157); vxm and hm come
@@ -1222,11 +1293,10 @@ int flux_min_blocks_candidates(bool f32, int* out) {
     out[0] = 4, out[1] = 5, out[2] = 6;
     return 3;
   }
-  // FP64: the one-lane kernel (3, 2, 4 blocks per SM) and the lane-pair
-  // kernel (SWFD_FLUX_PAIR + 3..6 blocks per SM)
-  out[0] = 3, out[1] = 2, out[2] = 4;
-  out[3] = SWFD_FLUX_PAIR + 3, out[4] = SWFD_FLUX_PAIR + 4, out[5] = SWFD_FLUX_PAIR + 5;
-  out[6] = SWFD_FLUX_PAIR + 6;
+  // FP64: the lane-pair kernel (SWFD_FLUX_PAIR + 3..6 blocks per SM; the
+  // default 4 first) and the one-lane kernel (3, 2, 4 blocks per SM)
+  out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_PAIR + 3, out[2] = SWFD_FLUX_PAIR + 5;
+  out[3] = SWFD_FLUX_PAIR + 6, out[4] = 3, out[5] = 2, out[6] = 4;
   return 7;
 }
 
@@ -1259,12 +1329,17 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       return;
     }
   }
-  if (!p.seg_alpha && !p.limiter && p.flux_minb && p.flux_minb != SWFD_FLUX_MINB(T)) {
+  // the FP64 default shape is the lane-pair kernel with 4 blocks per SM
+  // (SWFD_FLUX_DEFAULT64); flux_minb 3 selects the one-lane kernel's default
+  int minb = p.flux_minb;
+  if constexpr (sizeof(T) == 8)
+    if (!minb) minb = SWFD_FLUX_DEFAULT64;
+  if (!p.seg_alpha && !p.limiter && minb && minb != SWFD_FLUX_MINB(T)) {
     if constexpr (sizeof(T) == 8) {
-      if (p.flux_minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
-      if (p.flux_minb == 4) return launch_flux_minb<T, 4>(p, sp, rp, dsc, fp, work, s);
+      if (minb == 2) return launch_flux_minb<T, 2>(p, sp, rp, dsc, fp, work, s);
+      if (minb == 4) return launch_flux_minb<T, 4>(p, sp, rp, dsc, fp, work, s);
 #define SWFD_PAIR_CASE(M)                                                                    \
-  if (p.flux_minb == SWFD_FLUX_PAIR + M) {                                                   \
+  if (minb == SWFD_FLUX_PAIR + M) {                                                          \
     k_flux_xy_pair<M><<<flux_grid_pair<M>(), SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work); \
     return;                                                                                  \
   }
@@ -1274,8 +1349,8 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       SWFD_PAIR_CASE(6)
 #undef SWFD_PAIR_CASE
     } else {
-      if (p.flux_minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
-      if (p.flux_minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
+      if (minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
+      if (minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
     }
   }
   if (p.seg_alpha && p.limiter)
@@ -1324,6 +1399,31 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
 // ---------------------------------------------------------------------------
 // ox, oy: the cell's offsets in the x and y flux planes (its own rank
 // segment's copy; the cell offset itself without segments)
+// FP32-bulk RHS of a cell from its flux differences A (x) and B (y)
+__device__ __forceinline__ float rhs32(const Params& p, float A, float B, double amd) {
+  const float ix = p.fdx_inv, iy = p.fdy_inv;
+  if (p.alpha_premul) return -A * ix - B * iy;
+  const float am = d2f(amd);
+  return -(am * A) * ix - (am * B) * iy;
+}
+// FP32-bulk RK stage value: the FP64 accumulation with fused multiply-adds
+// (u + dt L; 0.75 u0 + 0.25 v; (u0 + 2 v)/3)
+__device__ __forceinline__ double rk32_value(int stage, double dt, double r, double u,
+                                             const double* u0) {
+  double v = fma(dt, r, u);
+  if (stage == 2) v = fma(0.75, *u0, 0.25 * v);
+  else if (stage == 3) v = fma(2.0, v, *u0) * (1.0 / 3.0);
+  return v;
+}
+// FP32-bulk checkpositivity of a 2D cell: the pressure in FP64 with one
+// reciprocal
+__device__ __forceinline__ int pos32_bad(const Params& p, const double nv[4]) {
+  const double ri = -0.5 * rcp_bulk(nv[0]);
+  const double pe = fma(fma(nv[2], nv[2], nv[1] * nv[1]), ri, nv[3]);
+  if (p.pos_strict) return (nv[0] < p.eps) || (pe < p.eps);
+  return (nv[0] <= p.eps) || (pe <= p.eps);
+}
+
 template <class T>
 __device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, int c, int64_t ox,
                                    int64_t oy, double amd) {
@@ -1335,10 +1435,7 @@ __device__ __forceinline__ T rhs2d(const Params& p, const T* __restrict__ flux, 
   T A = (ldt(fpf + ox) - ldt(fnf + ox + 1)) - (ldt(fpf + ox - 1) - ldt(fnf + ox));
   T B = (ldt(gpf + oy) - ldt(gnf + oy + pit)) - (ldt(gpf + oy - pit) - ldt(gnf + oy));
   if constexpr (sizeof(T) == 4) {  // FP32-bulk: reciprocals of dx, dy
-    const T ix = p.fdx_inv, iy = p.fdy_inv;
-    if (p.alpha_premul) return -A * ix - B * iy;
-    const T am = d2f(amd);
-    return -(am * A) * ix - (am * B) * iy;
+    return rhs32(p, A, B, amd);
   } else {
     const T dx = T(p.dx), dy = T(p.dy), am = T(amd);
     // (-x)/d == -(x/d): the divisions on the integer pipes (tdiv)
@@ -1405,9 +1502,7 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
                                    : rhs2d_cell<T>(p, flux, c, i, j, am));
       double v;
       if (sizeof(T) == 4) {  // FP32-bulk: the FP64 accumulation with fused multiply-adds
-        v = fma(dt, r, ld(u + c * P + o));
-        if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
-        else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
+        v = rk32_value(stage, dt, r, ld(u + c * P + o), u0 + c * P + o);
       } else {
         v = ld(u + c * P + o) + dt * r;
         if (stage >= 2) v = rk_combine(p, stage, u0[c * P + o], v);
@@ -1419,10 +1514,10 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       // checkpositivity (ex3_vortex_accuracy_2d/main.f90:640-647,
       // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
       double pe;
+      if (sizeof(T) == 4 && g.ndim == 2) return pos32_bad(p, nv);
       if (sizeof(T) == 4) {  // FP32-bulk: FP64 with one reciprocal
         const double ri = -0.5 * rcp_bulk(nv[0]);
-        if (g.ndim == 1) pe = fma(nv[1] * nv[1], ri, nv[2]);
-        else pe = fma(fma(nv[2], nv[2], nv[1] * nv[1]), ri, nv[3]);
+        pe = fma(nv[1] * nv[1], ri, nv[2]);
       } else if (g.ndim == 1) {
         pe = nv[2] - tscale<-1>(tdiv(nv[1] * nv[1], nv[0]));
       } else {
@@ -1531,6 +1626,270 @@ cudaError_t launch_rk(const Params& p, int stage, const double* u, const double*
   else
     k_rk<double><<<gb, b, 0, s>>>(p, stage, u, u0, (const double*)flux,
                                   const_cast<DevScalars*>(dsc), out, hs, decide);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP32-bulk fused stage (2D, no rank segments, no limiter): two kernels per RK
+// stage instead of four.
+//   k_alpha_terms32: [bc,] findalpha [and dt], and per cell the nine
+//     splitting terms (Terms32) and the Roe planes -- the FP64 work of the
+//     splitting, once per cell.
+//   k_stage32: per tile of 32 x 8 interior cells, the split fluxes of the tile
+//     and its stencil halo formed in shared memory from the terms and this
+//     stage's alpha, the interface fluxes of every face the tile's cells
+//     difference, then the RHS, the RK combination and checkpositivity of the
+//     tile's cells; the split, Roe and flux planes of the separate kernels
+//     never go through memory.  Every value is formed by the same functions as
+//     the separate kernels' (split32/split_pm, roe_eigen2d, weno8_f32,
+//     back_project, rhs32, rk32_value, pos32_bad), so both give the same bits.
+// Terms planes (floats, plane pitch of the state): fr fm fn fe f1 fxy f3 g2 g3.
+// ---------------------------------------------------------------------------
+template <bool NC>
+__device__ __forceinline__ void terms32_cell(const Params& p, const double* __restrict__ u,
+                                             float* __restrict__ terms, float* __restrict__ roe,
+                                             int64_t t) {
+  const Geom& g = p.g;
+  if (t >= (int64_t)g.LI * g.LJ) return;
+  const int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
+  const int64_t o = g.at(i, j), P = g.plane;
+  const double rho = ldc<NC>(u + o), mx = ldc<NC>(u + P + o), my = ldc<NC>(u + 2 * P + o),
+               e = ldc<NC>(u + 3 * P + o);
+  const double ri = rcp_bulk(rho);
+  Prim32 q;
+  const Terms32 tm = terms32(p, rho, mx, my, e, ri, q);
+  terms[0 * P + o] = tm.fr;
+  terms[1 * P + o] = tm.fm;
+  terms[2 * P + o] = tm.fn;
+  terms[3 * P + o] = tm.fe;
+  terms[4 * P + o] = tm.f1;
+  terms[5 * P + o] = tm.fxy;
+  terms[6 * P + o] = tm.f3;
+  terms[7 * P + o] = tm.g2;
+  terms[8 * P + o] = tm.g3;
+  roe32_store(p, rho, mx, my, e, ri, q, tm.fr, roe, P, o, 3);
+}
+
+// BC: the stage-2/3 form (bc of the previous stage's output first; a ghost
+// cell's values are then read back with coherent loads)
+template <bool BC>
+__global__ void k_alpha_terms32(Params p, double* __restrict__ u, DevScalars* dsc, int with_dt,
+                                float* __restrict__ terms, float* __restrict__ roe) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (BC) bc2d_cell(p, u, t);
+  double a = alpha_cell<!BC>(p, u, t);
+  terms32_cell<!BC>(p, u, terms, roe, t);
+  a = block_max(a);
+  if (threadIdx.x != 0) return;
+  alpha_last_block(p, dsc, a, with_dt);
+}
+
+cudaError_t launch_alpha_terms32(const Params& p, double* u, DevScalars* dsc, cudaStream_t s,
+                                 bool bc, bool with_dt, void* terms, void* roe) {
+  const int64_t n = (int64_t)p.g.LI * p.g.LJ;
+  const int b = cell_block(n);
+  const unsigned gb = (unsigned)((n + b - 1) / b);
+  if (bc)
+    k_alpha_terms32<true><<<gb, b, 0, s>>>(p, u, dsc, with_dt, (float*)terms, (float*)roe);
+  else
+    k_alpha_terms32<false><<<gb, b, 0, s>>>(p, u, dsc, with_dt, (float*)terms, (float*)roe);
+  return cudaGetLastError();
+}
+
+#define S32_TX 32
+#define S32_TY 8
+#define S32_THREADS 256
+struct Stage32Tile {
+  float xs[8][S32_TY][S32_TX + 6];  // fp (0..3), fn (4..7) of columns i0-3 .. i0+TX+2
+  float ys[8][S32_TY + 6][S32_TX];  // gp, gn of rows j0-3 .. j0+TY+2
+  float rx[4][S32_TY][S32_TX + 3];  // x-pass Roe planes of columns i0-1 .. i0+TX+1
+  float ry[4][S32_TY + 3][S32_TX];  // y-pass Roe planes of rows j0-1 .. j0+TY+1
+  float fx[8][S32_TY][S32_TX + 2];  // x faces i0-1 .. i0+TX: op (0..3), on (4..7)
+  float fy[8][S32_TY + 2][S32_TX];  // y faces j0-1 .. j0+TY
+};
+
+__host__ __device__ __forceinline__ int stage32_tiles(const Geom& g) {
+  return ((g.nx + S32_TX - 1) / S32_TX) * ((g.ny + S32_TY - 1) / S32_TY);
+}
+// ghost cells (three layers around the interior): rows -2..0 and ny+1..ny+3
+// over the full width, then columns -2..0 and nx+1..nx+3 of rows 1..ny
+__host__ __device__ __forceinline__ int64_t stage32_ghosts(const Geom& g) {
+  return 6 * (int64_t)g.LI + 6 * (int64_t)g.ny;
+}
+
+__global__ void __launch_bounds__(S32_THREADS, 2)
+    k_stage32(Params p, int stage, const double* __restrict__ u, const double* u0,
+              const float* __restrict__ terms, const float* __restrict__ roe, DevScalars* dsc,
+              double* out, cudaGraphConditionalHandle hs, int decide) {
+  extern __shared__ __align__(16) unsigned char s32_raw[];
+  Stage32Tile& sm = *reinterpret_cast<Stage32Tile*>(s32_raw);
+  const Geom& g = p.g;
+  const int64_t P = g.plane;
+  const int tid = threadIdx.x;
+  const double dt = dsc->dt, amd = dsc->alphamax;
+  const int tiles_x = (g.nx + S32_TX - 1) / S32_TX, tiles = stage32_tiles(g);
+  int bad = 0;
+  if ((int)blockIdx.x >= tiles) {
+    // ghost cells: the RK combination with a zero RHS (rk_cell's)
+    const int64_t k = (int64_t)(blockIdx.x - tiles) * S32_THREADS + tid;
+    if (k < stage32_ghosts(g)) {
+      int i, j;
+      const int64_t band = 3 * (int64_t)g.LI;
+      if (k < 2 * band) {
+        const int64_t r = k < band ? k : k - band;
+        j = (int)(r / g.LI) + (k < band ? -2 : g.ny + 1);
+        i = (int)(r % g.LI) - 2;
+      } else {
+        const int64_t r = k - 2 * band;
+        const int c = (int)(r % 6);
+        j = (int)(r / 6) + 1;
+        i = c < 3 ? c - 2 : g.nx + c - 2;
+      }
+      const int64_t o = g.at(i, j);
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        out[c * P + o] = rk32_value(stage, dt, 0.0, ld(u + c * P + o), u0 + c * P + o);
+    }
+    rk_block_done(dsc, 0, stage, hs, decide);
+    return;
+  }
+  const int i0 = 1 + (blockIdx.x % tiles_x) * S32_TX, j0 = 1 + (blockIdx.x / tiles_x) * S32_TY;
+  const int nxv = min(S32_TX, g.nx - i0 + 1), nyv = min(S32_TY, g.ny - j0 + 1);
+  // phase 1: split fluxes and Roe planes of the tile and its halo
+  {
+    const float ram = 1.f / d2f(amd);
+    const int wxs = nxv + 6, wrx = nxv + 3;
+    const int n1 = nyv * wxs, n2 = n1 + (nyv + 6) * nxv, n3 = n2 + nyv * wrx,
+              n4 = n3 + (nyv + 3) * nxv;
+    const float* ry_src = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+    for (int k = tid; k < n4; k += S32_THREADS) {
+      if (k < n1) {
+        const int r = k / wxs, c = k - r * wxs;
+        const int64_t o = g.at(i0 - 3 + c, j0 + r);
+        const float fr = terms[o], fm = terms[P + o], fn = terms[2 * P + o],
+                    fe = terms[3 * P + o], f1 = terms[4 * P + o], fxy = terms[5 * P + o],
+                    f3 = terms[6 * P + o];
+        split_pm(fr, fm, ram, sm.xs[0][r][c], sm.xs[4][r][c]);
+        split_pm(fm, f1, ram, sm.xs[1][r][c], sm.xs[5][r][c]);
+        split_pm(fn, fxy, ram, sm.xs[2][r][c], sm.xs[6][r][c]);
+        split_pm(fe, f3, ram, sm.xs[3][r][c], sm.xs[7][r][c]);
+      } else if (k < n2) {
+        const int kk = k - n1, r = kk / nxv, c = kk - r * nxv;
+        const int64_t o = g.at(i0 + c, j0 - 3 + r);
+        const float fr = terms[o], fm = terms[P + o], fn = terms[2 * P + o],
+                    fe = terms[3 * P + o], fxy = terms[5 * P + o], g2 = terms[7 * P + o],
+                    g3 = terms[8 * P + o];
+        split_pm(fr, fn, ram, sm.ys[0][r][c], sm.ys[4][r][c]);
+        split_pm(fm, fxy, ram, sm.ys[1][r][c], sm.ys[5][r][c]);
+        split_pm(fn, g2, ram, sm.ys[2][r][c], sm.ys[6][r][c]);
+        split_pm(fe, g3, ram, sm.ys[3][r][c], sm.ys[7][r][c]);
+      } else if (k < n3) {
+        const int kk = k - n2, r = kk / wrx, c = kk - r * wrx;
+        const int64_t o = g.at(i0 - 1 + c, j0 + r);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sm.rx[q][r][c] = roe[q * P + o];
+      } else {
+        const int kk = k - n3, r = kk / nxv, c = kk - r * nxv;
+        const int64_t o = g.at(i0 + c, j0 - 1 + r);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sm.ry[q][r][c] = ry_src[q * P + o];
+      }
+    }
+  }
+  __syncthreads();
+  // phase 2: the faces.  x faces first, their count rounded up to whole warps
+  // so that no warp mixes the two directions.
+  {
+    const float g1 = (float)p.gamma1, weps = (float)p.weno_eps;
+    const float am = p.alpha_premul ? (float)amd : 1.f;
+    const int wfx = nxv + 2, nfx = nyv * wfx, nfx_pad = (nfx + 31) & ~31;
+    const int nf = nfx_pad + (nyv + 2) * nxv;
+    for (int k = tid; k < nf; k += S32_THREADS) {
+      float a[5][4], b[5][4], op[4], on[4];
+      if (k < nfx_pad) {
+        if (k >= nfx) continue;
+        const int r = k / wfx, f = k - r * wfx;
+        Eigen2D<float> E;
+        roe_eigen2d<float>(g1, 0, sm.rx[0][r][f], sm.rx[0][r][f + 1], sm.rx[1][r][f],
+                           sm.rx[1][r][f + 1], sm.rx[2][r][f], sm.rx[2][r][f + 1],
+                           sm.rx[3][r][f], sm.rx[3][r][f + 1], E);
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            a[m][c] = sm.xs[c][r][f + m];
+            b[m][c] = sm.xs[4 + c][r][f + m];
+          }
+        float ur[4], ul[4];
+        weno8_f32<0>(E, a, b, weps, ur, ul);
+        back_project<0, float>(E, ur, ul, op, on);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          sm.fx[c][r][f] = p.alpha_premul ? am * op[c] : op[c];
+          sm.fx[4 + c][r][f] = p.alpha_premul ? am * on[c] : on[c];
+        }
+      } else {
+        const int kk = k - nfx_pad, f = kk / nxv, c0 = kk - f * nxv;
+        Eigen2D<float> E;
+        roe_eigen2d<float>(g1, 1, sm.ry[0][f][c0], sm.ry[0][f + 1][c0], sm.ry[1][f][c0],
+                           sm.ry[1][f + 1][c0], sm.ry[2][f][c0], sm.ry[2][f + 1][c0],
+                           sm.ry[3][f][c0], sm.ry[3][f + 1][c0], E);
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            a[m][c] = sm.ys[c][f + m][c0];
+            b[m][c] = sm.ys[4 + c][f + m][c0];
+          }
+        float ur[4], ul[4];
+        weno8_f32<1>(E, a, b, weps, ur, ul);
+        back_project<1, float>(E, ur, ul, op, on);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          sm.fy[c][f][c0] = p.alpha_premul ? am * op[c] : op[c];
+          sm.fy[4 + c][f][c0] = p.alpha_premul ? am * on[c] : on[c];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // phase 3: RHS, RK combination and checkpositivity of the tile's cells
+  {
+    const int r = tid / S32_TX, c = tid % S32_TX;
+    if (r < nyv && c < nxv) {
+      const int64_t o = g.at(i0 + c, j0 + r);
+      double nv[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float A = (sm.fx[k][r][c + 1] - sm.fx[4 + k][r][c + 2]) -
+                        (sm.fx[k][r][c] - sm.fx[4 + k][r][c + 1]);
+        const float B = (sm.fy[k][r + 1][c] - sm.fy[4 + k][r + 2][c]) -
+                        (sm.fy[k][r][c] - sm.fy[4 + k][r + 1][c]);
+        const double v =
+            rk32_value(stage, dt, tod(rhs32(p, A, B, amd)), ld(u + k * P + o), u0 + k * P + o);
+        nv[k] = v;
+        out[k * P + o] = v;
+      }
+      bad = pos32_bad(p, nv);
+    }
+  }
+  rk_block_done(dsc, bad, stage, hs, decide);
+}
+
+size_t stage32_smem_bytes() { return sizeof(Stage32Tile); }
+
+cudaError_t stage32_setup() {
+  return cudaFuncSetAttribute(k_stage32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(Stage32Tile));
+}
+
+cudaError_t launch_stage32(const Params& p, int stage, const double* u, const double* u0,
+                           const void* terms, const void* roe, DevScalars* dsc, double* out,
+                           cudaStream_t s, cudaGraphConditionalHandle hs, int decide) {
+  const int64_t blocks =
+      stage32_tiles(p.g) + (stage32_ghosts(p.g) + S32_THREADS - 1) / S32_THREADS;
+  k_stage32<<<(unsigned)blocks, S32_THREADS, sizeof(Stage32Tile), s>>>(
+      p, stage, u, u0, (const float*)terms, (const float*)roe, dsc, out, hs, decide);
   return cudaGetLastError();
 }
 

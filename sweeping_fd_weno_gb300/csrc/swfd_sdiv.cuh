@@ -72,7 +72,14 @@ SWFD_SD double div(double a, double b) {
   // biased exponent of the quotient when ma >= mb; the result's is e or e - 1
   // before rounding and at most one more after it
   int32_t e = (int32_t)ea - (int32_t)eb + 1023;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 2 || e > 2045) return div_hw(a, b);
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 2 || e > 2045) {
+    // a zero dividend over a normal divisor: a zero with the sign of the
+    // quotient (IEEE 754), without the fallback call -- flux differences of
+    // a uniform state at rest are exact zeros.  Tested inside the range
+    // branch, so the normal operands' path has no extra instruction.
+    if ((ua << 1) == 0 && eb - 1u < 2046u) return dfrom((ua ^ ub) & 0x8000000000000000ull);
+    return div_hw(a, b);
+  }
   const uint64_t frac = 0xfffffffffffffull;
   const uint64_t B = (ub & frac) | (1ull << 52);
   uint64_t A = (ua & frac) | (1ull << 52);
@@ -158,7 +165,7 @@ SWFD_SD double scale(double x) {
   constexpr double f = K >= 0 ? (double)(1ull << (K >= 0 ? K : 0)) : 1.0 / (double)(1ull << (K < 0 ? -K : 0));
   const uint64_t u = dbits(x);
   const uint32_t e = (uint32_t)(u >> 52) & 0x7ffu;
-  if (e - lo > hi - lo) return mul_hw(x, f);
+  if (e - lo > hi - lo) return (u << 1) == 0 ? x : mul_hw(x, f);  // +-0 * 2^K = +-0
   return dfrom(u + ((uint64_t)(int64_t)K << 52));
 }
 

@@ -25,7 +25,8 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
 
 # FP64 13..16: the lane-pair flux kernel (two lanes per interface) with 3..6
 # resident blocks per SM
-@pytest.mark.parametrize("precision,minb", [(abi.PRECISION_FP64, 2), (abi.PRECISION_FP64, 4),
+@pytest.mark.parametrize("precision,minb", [(abi.PRECISION_FP64, 2), (abi.PRECISION_FP64, 3),
+                                            (abi.PRECISION_FP64, 4),
                                             (abi.PRECISION_FP64, 13), (abi.PRECISION_FP64, 14),
                                             (abi.PRECISION_FP64, 15), (abi.PRECISION_FP64, 16),
                                             (abi.PRECISION_FP32_BULK, 5),
@@ -69,13 +70,14 @@ def test_batch_tile_tuning_keeps_results(swfd, precision):
         assert np.array_equal(ua, ub)
 
 
-@pytest.mark.parametrize("minb", [14, 16])
+@pytest.mark.parametrize("minb", [3, 14, 16])
 @pytest.mark.parametrize("case", [dict(problem=abi.SEDOV_2D, nx=48, ny=40),
                                   dict(problem=abi.JET_2D, nx=96, ny=24)],
                          ids=["point_energy", "jet"])
 def test_lane_pair_flux_kernel_matches_the_oracle(swfd, oracle_mod, monkeypatch, minb, case):
-    """The lane-pair FP64 flux kernel on the ex4 form (alpha pre-multiplied,
-    y-pass regulariser planes) and the ex5 form, against the oracle's steps."""
+    """The FP64 flux kernels (3: one lane per interface; 14, 16: the lane-pair
+    kernel, the default 14) on the ex4 form (alpha pre-multiplied, y-pass
+    regulariser planes) and the ex5 form, against the oracle's steps."""
     monkeypatch.setenv("SWFD_FLUX_MIN_BLOCKS", str(minb))
     kw = dict(case)
     prob = kw.pop("problem")
