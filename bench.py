@@ -1119,6 +1119,11 @@ def main():
                 "ms_per_step": ms32 / args.steps,
                 "speedup_vs_fp64": total_ms / ms32 if ms32 else None,
                 "flux_min_blocks": minb32,
+                "stage_kernels": ("split: findalpha, splitting, fluxes, RK + positivity, bc"
+                                  if os.environ.get("SWFD_FP32_STAGE") == "split" else
+                                  "fused: [bc +] findalpha + splitting terms, then one tile "
+                                  "kernel for split fluxes, interface fluxes, RHS, RK and "
+                                  "positivity"),
                 "rel_l1_density_err_vs_fp64": float(np.abs(r32 - r64).sum() / np.abs(r64).sum()),
                 "errors_vs_fp64": precision_errors(u32f, u64f),
                 "arithmetic": "FP32 LF splitting, WENO5 fluxes and flux differences; FP64 pressure "

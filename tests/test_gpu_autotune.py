@@ -8,8 +8,11 @@ from sweeping_fd_weno_gb300 import Batch, Solver, abi, problems
 pytestmark = pytest.mark.gpu
 
 
+# FP32-bulk: the separate splitting, flux and RK kernels (SWFD_FP32_STAGE=
+# split, the batch engine's kernels); the fused stage has one launch shape
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_FP32_BULK])
-def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
+def test_flux_launch_shape_tuning_keeps_results(swfd, monkeypatch, precision):
+    monkeypatch.setenv("SWFD_FP32_STAGE", "split")
     cfg = problems.make_config(abi.VORTEX_2D, nx=64, ny=64, precision=precision)
     a, b = Solver(cfg), Solver(cfg)
     for s in (a, b):
@@ -34,6 +37,7 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, precision):
 def test_each_flux_launch_shape_keeps_results(swfd, monkeypatch, precision, minb):
     # SWFD_FLUX_MIN_BLOCKS pins a candidate: every shape runs, not only the fastest
     monkeypatch.setenv("SWFD_FLUX_MIN_BLOCKS", str(minb))
+    monkeypatch.setenv("SWFD_FP32_STAGE", "split")
     cfg = problems.make_config(abi.VORTEX_2D, nx=72, ny=56, precision=precision)
     a, b = Solver(cfg), Solver(cfg)
     for s in (a, b):
@@ -48,6 +52,15 @@ def test_each_flux_launch_shape_keeps_results(swfd, monkeypatch, precision, minb
 
 def test_flux_tuning_skips_segmented_and_limited_problems(swfd):
     s = Solver(problems.make_config(abi.VORTEX_2D, nx=48, ny=48, use_limiter=1))
+    s.init_problem()
+    assert s.autotune() == 0
+    s.close()
+
+
+def test_flux_tuning_skips_the_fused_fp32_stage(swfd, monkeypatch):
+    monkeypatch.delenv("SWFD_FP32_STAGE", raising=False)
+    s = Solver(problems.make_config(abi.VORTEX_2D, nx=48, ny=48,
+                                    precision=abi.PRECISION_FP32_BULK))
     s.init_problem()
     assert s.autotune() == 0
     s.close()

@@ -49,21 +49,22 @@ def test_fused_stage_equals_separate_kernels(swfd, monkeypatch, name, case, step
     assert a["stats"] == b["stats"]
     for x, y in zip(a["tracks"], b["tracks"]):
         assert np.array_equal(x, y)
-    bad = ~(a["u"] == b["u"])
-    assert not bad.any(), f"{int(bad.sum())} state values differ"
+    # bit patterns: the sign of a zero and a NaN's payload count too
+    bad = a["u"].view(np.uint64) != b["u"].view(np.uint64)
+    assert not bad.any(), f"{int(bad.sum())} state values differ, first at {np.argwhere(bad)[:4]}"
     # two kernels per stage instead of four (sweeps aside)
     assert b["launches"] < a["launches"], (a["launches"], b["launches"])
-    if name.startswith("jet"):
+    if name == "jet_96x24":
         assert b["stats"]["sweep_count"] > 0  # the sweeps ran in both
 
 
 def test_fused_stage_kernel_count_per_step(swfd, monkeypatch):
-    """vortex 64x64 without sweeps: findalpha+terms, then per stage the stage
-    kernel and bc+findalpha+terms (the bc alone after stage 3), and the time
-    advance -- 8 kernels per step (14 with the separate kernels)."""
+    """vortex 64x64: findalpha+terms, then per stage the stage kernel and
+    bc+findalpha+terms (the bc alone after stage 3), and the time advance --
+    8 kernels per step against 14 with the separate kernels (the sweeps'
+    kernels are the same in both)."""
     case = dict(problem=abi.VORTEX_2D, nx=64, ny=64)
     a = run(monkeypatch, "split", case, 4)
     b = run(monkeypatch, "fused", case, 4)
-    assert a["stats"]["sweep_count"] == 0
-    assert b["launches"] == 8 * 4, b["launches"]
-    assert a["launches"] == 14 * 4, a["launches"]
+    assert a["stats"] == b["stats"]
+    assert a["launches"] - b["launches"] == (14 - 8) * 4, (a["launches"], b["launches"])
