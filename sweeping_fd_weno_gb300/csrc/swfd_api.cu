@@ -601,7 +601,8 @@ void emit_stage32(Builder& b, cudaStream_t s, int k, double* in, double* u0, dou
                     : cudaEventRecordWithFlags(h->ev[2 * (k - 1)], s, cudaEventRecordExternal));
   const bool sweeps = h->cfg.use_limiter == 2;
   const cudaGraphConditionalHandle hs = sweeps ? b.handle() : 0;
-  B_OK(b, launch_stage32(p, k, in, u0, h->split, h->roe, h->dsc, out, s, hs, sweeps ? 1 : 0));
+  B_OK(b, launch_stage32(p, h->stage32, k, in, u0, h->split, h->roe, h->dsc, out, s, hs,
+                         sweeps ? 1 : 0));
   b.k(1);
   if (events)
     B_OK(b, b.eager ? cudaEventRecord(h->ev[2 * (k - 1) + 1], s)
@@ -1006,9 +1007,13 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
      // separate splitting, flux and RK kernels, the same bits)
     const Params& q = h->p;
     const char* fs = getenv("SWFD_FP32_STAGE");
-    h->stage32 = q.precision == SWFD_PRECISION_FP32_BULK && q.g.ndim == 2 && !q.seg_alpha &&
-                 !q.limiter && !q.quad && cfg->rk_choice != 2 &&
-                 !(fs && strcmp(fs, "split") == 0);
+    const bool on = q.precision == SWFD_PRECISION_FP32_BULK && q.g.ndim == 2 && !q.seg_alpha &&
+                    !q.limiter && !q.quad && cfg->rk_choice != 2 &&
+                    !(fs && strcmp(fs, "split") == 0);
+    // SWFD_STAGE32_SHAPE pins the stage kernel's launch shape (1..5)
+    const char* sh = getenv("SWFD_STAGE32_SHAPE");
+    const int shape = sh ? atoi(sh) : 0;
+    h->stage32 = on ? ((shape >= 1 && shape <= 5) ? shape : 4) : 0;
   }
   const Geom& g = h->p.g;
   auto cleanup_fail = [&](cudaError_t e) {

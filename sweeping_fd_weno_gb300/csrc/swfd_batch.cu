@@ -52,10 +52,14 @@ struct swfd_batch {
   std::vector<long long> prefix;
   long long* d_tprefix = nullptr;  // cell-tile prefix of the per-cell kernels
   std::vector<long long> tprefix;
+  long long* d_s32prefix = nullptr;  // the fused FP32-bulk stage's tile + ghost-chunk prefix
+  std::vector<long long> s32prefix;
+  bool fused32 = false;            // this run's running slots all take the fused FP32 stage
   int tile_cells = 2048;           // cells per tile (swfd_batch_autotune picks it)
   DevScalars* d_dsc = nullptr;  // one DevScalars per slot, contiguous: one read-back per run
   DevScalars* h_dsc = nullptr;  // pinned mirror
   cudaGraphExec_t g_run = nullptr;
+  cudaGraphExec_t g_run32 = nullptr;  // the same loop with the fused FP32-bulk stage
   double* d_stage = nullptr;
   size_t stage_bytes = 0;
   int64_t pool_bytes = 0, used_bytes = 0;
@@ -106,6 +110,7 @@ BatchLaunch launch_desc(swfd_batch* b) {
   L.ctl = b->d_ctl;
   L.prefix = b->d_prefix;
   L.tprefix = b->d_tprefix;
+  L.s32prefix = b->d_s32prefix;
   L.n_slots = b->cfg.max_slots;
   L.max_cell = b->max_cell;
   L.fp32 = b->cfg.precision == SWFD_PRECISION_FP32_BULK;
@@ -115,8 +120,8 @@ BatchLaunch launch_desc(swfd_batch* b) {
 }
 
 // WHILE (some slot runs and steps < limit) { stage 1..3 with conditional
-// sweeps and bc; per-slot time advance }
-swfd_status build_run_graph(swfd_batch* b) {
+// sweeps and bc; per-slot time advance }; fused: the FP32-bulk fused stage
+swfd_status build_run_graph(swfd_batch* b, bool fused) {
   Builder bd;
   bd.cap = b->cap;
   bd.max_depth = 3;
@@ -133,7 +138,8 @@ swfd_status build_run_graph(swfd_batch* b) {
     for (int k = 1; k <= 3; ++k) {
       const int in = in_of[k - 1], out = out_of[k - 1];
       cudaGraphConditionalHandle hs = bd.handle();
-      B_OK(bd, launch_batch_stage(L, k, in, out, hs, sb));
+      if (fused) B_OK(bd, launch_batch_stage32(L, k, in, out, hs, sb));
+      else B_OK(bd, launch_batch_stage(L, k, in, out, hs, sb));
       bd.cond(sb, cudaGraphCondTypeIf, hs, [&](cudaStream_t sw) {
         B_OK(bd, launch_batch_sweep_head(L, out, sw));
         cudaGraphConditionalHandle hq = bd.handle();
@@ -154,7 +160,7 @@ swfd_status build_run_graph(swfd_batch* b) {
     return bfail(b, SWFD_ERR_CUDA, std::string("batch graph capture: ") +
                                        cudaGetErrorString(bd.err != cudaSuccess ? bd.err : e2));
   }
-  cudaError_t e3 = cudaGraphInstantiate(&b->g_run, g, 0);
+  cudaError_t e3 = cudaGraphInstantiate(fused ? &b->g_run32 : &b->g_run, g, 0);
   cudaGraphDestroy(g);
   if (e3 != cudaSuccess)
     return bfail(b, SWFD_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e3));
@@ -253,6 +259,7 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   b->tab.assign(n, BatchSlot{});
   b->prefix.assign(n + 1, 0);
   b->tprefix.assign(n + 1, 0);
+  b->s32prefix.assign(n + 1, 0);
   b->max_cell = (long long)(cfg->max_nx + 6) * (cfg->max_ny + 6);
   b->stage_bytes = (size_t)4 * b->max_cell * sizeof(double);
   if ((e = cudaMalloc(&b->d_tab, n * sizeof(BatchSlot))) != cudaSuccess) return bad(e);
@@ -260,6 +267,7 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   if ((e = cudaMallocHost(&b->h_ctl, sizeof(BatchCtl))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_prefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_tprefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
+  if ((e = cudaMalloc(&b->d_s32prefix, (n + 1) * sizeof(long long))) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess) return bad(e);
   if ((e = cudaMalloc(&b->d_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
   if ((e = cudaMallocHost(&b->h_dsc, n * sizeof(DevScalars))) != cudaSuccess) return bad(e);
@@ -273,7 +281,9 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   b->pool_bytes = cfg->pool_bytes > 0 ? cfg->pool_bytes : (int64_t)(0.8 * (double)fr);
-  if (build_run_graph(b) != SWFD_OK) {
+  const bool f32 = cfg->precision == SWFD_PRECISION_FP32_BULK;
+  if (f32 && (e = stage32_setup()) != cudaSuccess) return bad(e);
+  if (build_run_graph(b, false) != SWFD_OK || (f32 && build_run_graph(b, true) != SWFD_OK)) {
     std::string m = b->last_error;
     swfd_batch_destroy(b);
     return bfail(nullptr, SWFD_ERR_CUDA, m);
@@ -291,10 +301,12 @@ swfd_status swfd_batch_destroy(swfd_batch* b) {
     cudaFree(sh.tracks);
   }
   if (b->g_run) cudaGraphExecDestroy(b->g_run);
+  if (b->g_run32) cudaGraphExecDestroy(b->g_run32);
   cudaFree(b->d_tab);
   cudaFree(b->d_ctl);
   cudaFree(b->d_prefix);
   cudaFree(b->d_tprefix);
+  cudaFree(b->d_s32prefix);
   cudaFree(b->d_stage);
   cudaFree(b->d_dsc);
   if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -417,18 +429,30 @@ namespace {
 swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
   const int n = b->cfg.max_slots;
   int running = 0;
-  long long chunks = 0, tiles = 0;
+  long long chunks = 0, tiles = 0, items = 0;
+  // the fused FP32-bulk stage when every running slot takes it (2D, no rank
+  // segments, no limiter) and SWFD_FP32_STAGE is not "split"
+  const char* fs = getenv("SWFD_FP32_STAGE");
+  bool fused = b->g_run32 != nullptr && !(fs && strcmp(fs, "split") == 0);
   for (int k = 0; k < n; ++k) {
     b->prefix[k] = chunks;
     b->tprefix[k] = tiles;
+    b->s32prefix[k] = items;
     if (b->slots[k].state == 1) {
       ++running;
       chunks += b->tab[k].chunks;
       tiles += (b->tab[k].ncell + b->tile_cells - 1) / b->tile_cells;
+      const Params& q = b->tab[k].p;
+      if (q.g.ndim != 2 || q.seg_alpha || q.limiter || q.quad) fused = false;
+      else items += stage32_items(q);
     }
   }
   b->prefix[n] = chunks;
   b->tprefix[n] = tiles;
+  b->s32prefix[n] = items;
+  b->fused32 = fused;
+  BCU(b, cudaMemcpyAsync(b->d_s32prefix, b->s32prefix.data(), (n + 1) * sizeof(long long),
+                         cudaMemcpyHostToDevice, b->stream));
   BCU(b, cudaMemcpyAsync(b->d_prefix, b->prefix.data(), (n + 1) * sizeof(long long),
                          cudaMemcpyHostToDevice, b->stream));
   BCU(b, cudaMemcpyAsync(b->d_tprefix, b->tprefix.data(), (n + 1) * sizeof(long long),
@@ -440,6 +464,7 @@ swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
   c.total_tiles = tiles;
   c.tile_cells = b->tile_cells;
   c.steps_limit = max_steps;
+  c.total_s32 = items;
   BCU(b, cudaMemcpyAsync(b->d_ctl, &c, sizeof(BatchCtl), cudaMemcpyHostToDevice, b->stream));
   return SWFD_OK;
 }
@@ -505,7 +530,7 @@ swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out)
     swfd_status st = upload_plan(b, max_steps);
     if (st != SWFD_OK) return st;
   }
-  BCU(b, cudaGraphLaunch(b->g_run, b->stream));
+  BCU(b, cudaGraphLaunch(b->fused32 ? b->g_run32 : b->g_run, b->stream));
   BCU(b, cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, b->stream));
   BCU(b, cudaMemcpyAsync(b->tab.data(), b->d_tab, n * sizeof(BatchSlot), cudaMemcpyDeviceToHost,
                          b->stream));

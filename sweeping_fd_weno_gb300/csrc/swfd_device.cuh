@@ -285,16 +285,68 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   E.l4_3 = t2;
 }
 
+// FP32-bulk reconstructions: weno5's expressions (weno5.f90:86-146) in
+// binary32 with fused multiply-adds and reciprocal-estimate weights
+// (__fdividef: the MUFU reciprocal and a product, within 2 ulp).  The
+// FP32-bulk form is judged by its error against the FP64 form, not bit for
+// bit; every FP32 path (one instance, fused stage, batch) calls these, so
+// they agree with each other bit for bit.
+__device__ __forceinline__ void weno_beta_f32(float am2, float am1, float a0, float ap1, float ap2,
+                                              float& b1, float& b2, float& b3) {
+  const float c1312 = 13.f / 12.f;
+  const float s1 = fmaf(-2.f, ap1, a0) + ap2, t1 = fmaf(3.f, a0, fmaf(-4.f, ap1, ap2));
+  const float s2 = fmaf(-2.f, a0, am1) + ap1, t2 = am1 - ap1;
+  const float s3 = fmaf(-2.f, am1, am2) + a0, t3 = fmaf(3.f, a0, fmaf(-4.f, am1, am2));
+  b1 = fmaf(c1312, s1 * s1, 0.25f * (t1 * t1));
+  b2 = fmaf(c1312, s2 * s2, 0.25f * (t2 * t2));
+  b3 = fmaf(c1312, s3 * s3, 0.25f * (t3 * t3));
+}
+// the three nonlinear weights of linear weights d1, d2, d3 applied to the
+// candidates c1, c2, c3
+__device__ __forceinline__ float weno_combine_f32(float b1, float b2, float b3, float d1, float d2,
+                                                  float d3, float c1, float c2, float c3,
+                                                  float eps) {
+  const float e1 = eps + b1, e2 = eps + b2, e3 = eps + b3;
+  const float a1 = __fdividef(d1, e1 * e1), a2 = __fdividef(d2, e2 * e2),
+              a3 = __fdividef(d3, e3 * e3);
+  const float rs = __fdividef(1.f, a1 + a2 + a3);
+  return fmaf(a1 * rs, c1, fmaf(a2 * rs, c2, (a3 * rs) * c3));
+}
+__device__ __forceinline__ float weno_right(float am2, float am1, float a0, float ap1, float ap2,
+                                            float eps) {
+  const float um1 = fmaf(float(SWFD_C116), a0, fmaf(float(SWFD_CM76), am1, float(SWFD_C13) * am2));
+  const float um2 = fmaf(float(SWFD_C13), ap1, fmaf(float(SWFD_C56), a0, float(SWFD_CM16) * am1));
+  const float um3 = fmaf(float(SWFD_CM16), ap2, fmaf(float(SWFD_C56), ap1, float(SWFD_C13) * a0));
+  float b1, b2, b3;
+  weno_beta_f32(am2, am1, a0, ap1, ap2, b1, b2, b3);
+  return weno_combine_f32(b1, b2, b3, 0.3f, 0.6f, 0.1f, um3, um2, um1, eps);
+}
+__device__ __forceinline__ float weno_left(float am2, float am1, float a0, float ap1, float ap2,
+                                           float eps) {
+  const float up1 = fmaf(float(SWFD_C13), a0, fmaf(float(SWFD_C56), am1, float(SWFD_CM16) * am2));
+  const float up2 = fmaf(float(SWFD_CM16), ap1, fmaf(float(SWFD_C56), a0, float(SWFD_C13) * am1));
+  const float up3 = fmaf(float(SWFD_C13), ap2, fmaf(float(SWFD_CM76), ap1, float(SWFD_C116) * a0));
+  float b1, b2, b3;
+  weno_beta_f32(am2, am1, a0, ap1, ap2, b1, b2, b3);
+  return weno_combine_f32(b1, b2, b3, 0.1f, 0.6f, 0.3f, up3, up2, up1, eps);
+}
+
 // evl(k,:) . f with f in component order (rho, m_x, m_y, E), summed left to
 // right over the component index as the reference does (main.f90:212-213).
+// FP32-bulk: the same sums with fused multiply-adds.
 template <int YDIR, class T>
 __device__ __forceinline__ T proj_row(T l0, T ln, T lt, T l3, T f0, T f1, T f2, T f3) {
+  if constexpr (sizeof(T) == 4) {
+    if (!YDIR) return fmaf(l3, f3, fmaf(lt, f2, fmaf(ln, f1, l0 * f0)));
+    return fmaf(l3, f3, fmaf(ln, f2, fmaf(lt, f1, l0 * f0)));
+  }
   if (!YDIR) return l0 * f0 + ln * f1 + lt * f2 + l3 * f3;
   return l0 * f0 + lt * f1 + ln * f2 + l3 * f3;
 }
 // evl row 2: x pass [-vym, 0, 1, 0] -> f2 - vym*f0; y pass [-vxm, 1, 0, 0] -> f1 - vxm*f0
 template <int YDIR, class T>
 __device__ __forceinline__ T proj_row2(T vt, T f0, T f1, T f2) {
+  if constexpr (sizeof(T) == 4) return fmaf(-vt, f0, YDIR ? f1 : f2);
   if (!YDIR) return -vt * f0 + f2;
   return -vt * f0 + f1;
 }

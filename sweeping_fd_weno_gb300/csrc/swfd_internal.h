@@ -213,6 +213,7 @@ struct BatchCtl {
   int tile_cells;         // cells per tile of the per-cell batched kernels
   long long steps;        // steps taken by the current launch
   long long steps_limit;
+  long long total_s32;    // fused FP32-bulk stage: tiles and ghost chunks of the running slots
   int cond;               // eager launch mode: value of the last conditional decision
 };
 
@@ -222,6 +223,7 @@ struct BatchLaunch {
   BatchCtl* ctl;            // device batch scalars
   const long long* prefix;  // device flux-chunk prefix (n_slots + 1)
   const long long* tprefix; // device cell-tile prefix (n_slots + 1)
+  const long long* s32prefix; // device prefix of the fused stage's tiles and ghost chunks
   int n_slots;
   long long max_cell;       // largest slot (LI*LJ)
   int fp32;
@@ -282,8 +284,9 @@ struct swfd_handle {
   // profilers that do not look inside graphs with conditional nodes
   int eager = 0;
   long long eager_launches = 0;
-  // FP32-bulk 2D stages as two kernels (k_alpha_terms32, k_stage32); off
-  // with rank segments, the limiter, and SWFD_FP32_STAGE=split
+  // FP32-bulk 2D stages as two kernels (k_alpha_terms32, k_stage32): the
+  // stage kernel's launch shape (launch_stage32), 0 = the separate kernels
+  // (rank segments, the limiter, SWFD_FP32_STAGE=split)
   int stage32 = 0;
   // host staging for layout conversion
   double* h_stage = nullptr;  // pinned, nc * LI * LJ doubles
@@ -317,9 +320,12 @@ cudaError_t launch_alpha(const Params& p, const double* u, DevScalars* dsc, cuda
 // kernel's dynamic shared memory limit (once per process and device).
 cudaError_t launch_alpha_terms32(const Params& p, double* u, DevScalars* dsc, cudaStream_t s,
                                  bool bc, bool with_dt, void* terms, void* roe);
-cudaError_t launch_stage32(const Params& p, int stage, const double* u, const double* u0,
-                           const void* terms, const void* roe, DevScalars* dsc, double* out,
-                           cudaStream_t s, cudaGraphConditionalHandle hs, int decide);
+// shape: 1 = 256 threads per tile, 2 tiles per SM; 2 = 320 x 2; 3 = 256 x 3;
+// 4 = 256 x 4 (default); 5 = 320 x 3
+cudaError_t launch_stage32(const Params& p, int shape, int stage, const double* u,
+                           const double* u0, const void* terms, const void* roe, DevScalars* dsc,
+                           double* out, cudaStream_t s, cudaGraphConditionalHandle hs,
+                           int decide);
 cudaError_t stage32_setup();
 size_t stage32_smem_bytes();
 // split, roe and flux planes hold doubles (FP64) or floats (FP32 bulk)
@@ -359,6 +365,13 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
 cudaError_t launch_batch_bc(const BatchLaunch& b, int out, cudaStream_t s);
 // findalpha over the running slots' state `in` (the batch autotuner's probe)
 cudaError_t launch_batch_alpha(const BatchLaunch& b, int in, cudaStream_t s);
+// the FP32-bulk fused stage over the batch (every running slot 2D without
+// rank segments or limiter): stage reset, findalpha with the splitting terms,
+// the per-slot alphamax [and dt], the stage kernel over all slots' tiles and
+// ghost chunks (stage32_items each, s32prefix), the sweep condition
+cudaError_t launch_batch_stage32(const BatchLaunch& b, int stage, int in, int out,
+                                 cudaGraphConditionalHandle h_sweep, cudaStream_t s);
+long long stage32_items(const Params& p);
 // launch-shape candidates of the flux kernel (resident blocks per SM; FP64
 // values SWFD_FLUX_PAIR + b select the lane-pair kernel with b blocks per SM);
 // returns their number, the default first

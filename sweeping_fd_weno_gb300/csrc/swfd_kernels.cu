@@ -772,6 +772,17 @@ template <int YDIR, class T>
 __device__ __forceinline__ void back_project(const Eigen2D<T>& E, const T ur[4], const T ul[4],
                                              T outp[4], T outn[4]) {
   const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
+  if constexpr (sizeof(T) == 4) {  // FP32-bulk: fused multiply-adds
+    outp[0] = ur[0] + ur[2] + ur[3];
+    outn[0] = ul[0] + ul[2] + ul[3];
+    outp[n] = fmaf(E.e_np, ur[3], fmaf(E.vn, ur[2], E.e_nm * ur[0]));
+    outn[n] = fmaf(E.e_np, ul[3], fmaf(E.vn, ul[2], E.e_nm * ul[0]));
+    outp[tt] = fmaf(E.vt, ur[3], fmaf(E.vt, ur[2], fmaf(E.vt, ur[0], ur[1])));
+    outn[tt] = fmaf(E.vt, ul[3], fmaf(E.vt, ul[2], fmaf(E.vt, ul[0], ul[1])));
+    outp[3] = fmaf(E.e_hp, ur[3], fmaf(E.qm, ur[2], fmaf(E.vt, ur[1], E.e_hm * ur[0])));
+    outn[3] = fmaf(E.e_hp, ul[3], fmaf(E.qm, ul[2], fmaf(E.vt, ul[1], E.e_hm * ul[0])));
+    return;
+  }
   outp[0] = ur[0] + ur[2] + ur[3];
   outn[0] = ul[0] + ul[2] + ul[3];
   outp[n] = E.e_nm * ur[0] + E.vn * ur[2] + E.e_np * ur[3];
@@ -1698,7 +1709,6 @@ cudaError_t launch_alpha_terms32(const Params& p, double* u, DevScalars* dsc, cu
 
 #define S32_TX 32
 #define S32_TY 8
-#define S32_THREADS 256
 struct Stage32Tile {
   float xs[8][S32_TY][S32_TX + 6];  // fp (0..3), fn (4..7) of columns i0-3 .. i0+TX+2
   float ys[8][S32_TY + 6][S32_TX];  // gp, gn of rows j0-3 .. j0+TY+2
@@ -1717,43 +1727,49 @@ __host__ __device__ __forceinline__ int64_t stage32_ghosts(const Geom& g) {
   return 6 * (int64_t)g.LI + 6 * (int64_t)g.ny;
 }
 
-__global__ void __launch_bounds__(S32_THREADS, 2)
-    k_stage32(Params p, int stage, const double* __restrict__ u, const double* u0,
-              const float* __restrict__ terms, const float* __restrict__ roe, DevScalars* dsc,
-              double* out, cudaGraphConditionalHandle hs, int decide) {
-  extern __shared__ __align__(16) unsigned char s32_raw[];
-  Stage32Tile& sm = *reinterpret_cast<Stage32Tile*>(s32_raw);
+// the RK combination of ghost chunk kk (NT consecutive ghost cells) with a
+// zero RHS, as rk_cell does for the ghost cells
+template <int NT>
+__device__ __forceinline__ void stage32_ghosts_chunk(const Params& p, int stage,
+                                                     const double* __restrict__ u,
+                                                     const double* u0, double dt, double* out,
+                                                     int64_t kk) {
+  const Geom& g = p.g;
+  const int64_t P = g.plane;
+  const int64_t k = kk * NT + threadIdx.x;
+  if (k >= stage32_ghosts(g)) return;
+  int i, j;
+  const int64_t band = 3 * (int64_t)g.LI;
+  if (k < 2 * band) {
+    const int64_t r = k < band ? k : k - band;
+    j = (int)(r / g.LI) + (k < band ? -2 : g.ny + 1);
+    i = (int)(r % g.LI) - 2;
+  } else {
+    const int64_t r = k - 2 * band;
+    const int c = (int)(r % 6);
+    j = (int)(r / 6) + 1;
+    i = c < 3 ? c - 2 : g.nx + c - 2;
+  }
+  const int64_t o = g.at(i, j);
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    out[c * P + o] = rk32_value(stage, dt, 0.0, ld(u + c * P + o), u0 + c * P + o);
+}
+
+// one 32 x 8 tile of the fused stage; returns this thread's positivity flag.
+// Every thread of the block calls it (it synchronises the block).
+template <int NT>
+__device__ __forceinline__ int stage32_tile(const Params& p, int stage,
+                                            const double* __restrict__ u, const double* u0,
+                                            const float* __restrict__ terms,
+                                            const float* __restrict__ roe, double dt, double amd,
+                                            double* out, int tile, Stage32Tile& sm) {
   const Geom& g = p.g;
   const int64_t P = g.plane;
   const int tid = threadIdx.x;
-  const double dt = dsc->dt, amd = dsc->alphamax;
-  const int tiles_x = (g.nx + S32_TX - 1) / S32_TX, tiles = stage32_tiles(g);
+  const int tiles_x = (g.nx + S32_TX - 1) / S32_TX;
   int bad = 0;
-  if ((int)blockIdx.x >= tiles) {
-    // ghost cells: the RK combination with a zero RHS (rk_cell's)
-    const int64_t k = (int64_t)(blockIdx.x - tiles) * S32_THREADS + tid;
-    if (k < stage32_ghosts(g)) {
-      int i, j;
-      const int64_t band = 3 * (int64_t)g.LI;
-      if (k < 2 * band) {
-        const int64_t r = k < band ? k : k - band;
-        j = (int)(r / g.LI) + (k < band ? -2 : g.ny + 1);
-        i = (int)(r % g.LI) - 2;
-      } else {
-        const int64_t r = k - 2 * band;
-        const int c = (int)(r % 6);
-        j = (int)(r / 6) + 1;
-        i = c < 3 ? c - 2 : g.nx + c - 2;
-      }
-      const int64_t o = g.at(i, j);
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        out[c * P + o] = rk32_value(stage, dt, 0.0, ld(u + c * P + o), u0 + c * P + o);
-    }
-    rk_block_done(dsc, 0, stage, hs, decide);
-    return;
-  }
-  const int i0 = 1 + (blockIdx.x % tiles_x) * S32_TX, j0 = 1 + (blockIdx.x / tiles_x) * S32_TY;
+  const int i0 = 1 + (tile % tiles_x) * S32_TX, j0 = 1 + (tile / tiles_x) * S32_TY;
   const int nxv = min(S32_TX, g.nx - i0 + 1), nyv = min(S32_TY, g.ny - j0 + 1);
   // phase 1: split fluxes and Roe planes of the tile and its halo
   {
@@ -1762,7 +1778,7 @@ __global__ void __launch_bounds__(S32_THREADS, 2)
     const int n1 = nyv * wxs, n2 = n1 + (nyv + 6) * nxv, n3 = n2 + nyv * wrx,
               n4 = n3 + (nyv + 3) * nxv;
     const float* ry_src = roe + (p.roe_reg_ex4 ? 4 * P : 0);
-    for (int k = tid; k < n4; k += S32_THREADS) {
+    for (int k = tid; k < n4; k += NT) {
       if (k < n1) {
         const int r = k / wxs, c = k - r * wxs;
         const int64_t o = g.at(i0 - 3 + c, j0 + r);
@@ -1804,7 +1820,7 @@ __global__ void __launch_bounds__(S32_THREADS, 2)
     const float am = p.alpha_premul ? (float)amd : 1.f;
     const int wfx = nxv + 2, nfx = nyv * wfx, nfx_pad = (nfx + 31) & ~31;
     const int nf = nfx_pad + (nyv + 2) * nxv;
-    for (int k = tid; k < nf; k += S32_THREADS) {
+    for (int k = tid; k < nf; k += NT) {
       float a[5][4], b[5][4], op[4], on[4];
       if (k < nfx_pad) {
         if (k >= nfx) continue;
@@ -1873,23 +1889,68 @@ __global__ void __launch_bounds__(S32_THREADS, 2)
       bad = pos32_bad(p, nv);
     }
   }
+  return bad;
+}
+
+// NT threads per tile (256: three rounds of faces; 320: two), MINB resident
+// tiles per SM.  Blocks past the tiles run the ghost cells' RK combination.
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_stage32(Params p, int stage, const double* __restrict__ u, const double* u0,
+              const float* __restrict__ terms, const float* __restrict__ roe, DevScalars* dsc,
+              double* out, cudaGraphConditionalHandle hs, int decide) {
+  extern __shared__ __align__(16) unsigned char s32_raw[];
+  Stage32Tile& sm = *reinterpret_cast<Stage32Tile*>(s32_raw);
+  const double dt = dsc->dt, amd = dsc->alphamax;
+  const int tiles = stage32_tiles(p.g);
+  int bad = 0;
+  if ((int)blockIdx.x >= tiles)
+    stage32_ghosts_chunk<NT>(p, stage, u, u0, dt, out, (int64_t)blockIdx.x - tiles);
+  else
+    bad = stage32_tile<NT>(p, stage, u, u0, terms, roe, dt, amd, out, (int)blockIdx.x, sm);
   rk_block_done(dsc, bad, stage, hs, decide);
 }
 
 size_t stage32_smem_bytes() { return sizeof(Stage32Tile); }
 
+cudaError_t batch_stage32_setup();
+// the launch shapes (threads per tile, tiles per SM): 1 = 256 x 2,
+// 2 = 320 x 2, 3 = 256 x 3, 4 = 256 x 4 (the default: 64 registers, the
+// fastest on the 360^2 and 1024^2 vortex), 5 = 320 x 3
 cudaError_t stage32_setup() {
-  return cudaFuncSetAttribute(k_stage32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(Stage32Tile));
+  const int b = (int)sizeof(Stage32Tile);
+  cudaError_t e = cudaFuncSetAttribute(k_stage32<256, 2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stage32<320, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stage32<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stage32<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stage32<320, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = batch_stage32_setup();
+  return e;
 }
 
-cudaError_t launch_stage32(const Params& p, int stage, const double* u, const double* u0,
-                           const void* terms, const void* roe, DevScalars* dsc, double* out,
-                           cudaStream_t s, cudaGraphConditionalHandle hs, int decide) {
-  const int64_t blocks =
-      stage32_tiles(p.g) + (stage32_ghosts(p.g) + S32_THREADS - 1) / S32_THREADS;
-  k_stage32<<<(unsigned)blocks, S32_THREADS, sizeof(Stage32Tile), s>>>(
+template <int NT, int MINB>
+static void stage32_go(const Params& p, int stage, const double* u, const double* u0,
+                       const void* terms, const void* roe, DevScalars* dsc, double* out,
+                       cudaStream_t s, cudaGraphConditionalHandle hs, int decide) {
+  const int64_t blocks = stage32_tiles(p.g) + (stage32_ghosts(p.g) + NT - 1) / NT;
+  k_stage32<NT, MINB><<<(unsigned)blocks, NT, sizeof(Stage32Tile), s>>>(
       p, stage, u, u0, (const float*)terms, (const float*)roe, dsc, out, hs, decide);
+}
+
+cudaError_t launch_stage32(const Params& p, int shape, int stage, const double* u,
+                           const double* u0, const void* terms, const void* roe, DevScalars* dsc,
+                           double* out, cudaStream_t s, cudaGraphConditionalHandle hs,
+                           int decide) {
+  if (shape == 1) stage32_go<256, 2>(p, stage, u, u0, terms, roe, dsc, out, s, hs, decide);
+  else if (shape == 2) stage32_go<320, 2>(p, stage, u, u0, terms, roe, dsc, out, s, hs, decide);
+  else if (shape == 3) stage32_go<256, 3>(p, stage, u, u0, terms, roe, dsc, out, s, hs, decide);
+  else if (shape == 5) stage32_go<320, 3>(p, stage, u, u0, terms, roe, dsc, out, s, hs, decide);
+  else stage32_go<256, 4>(p, stage, u, u0, terms, roe, dsc, out, s, hs, decide);
   return cudaGetLastError();
 }
 
@@ -2252,6 +2313,95 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
     kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
     kb_rk<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, stage, in, out);
   }
+  if (h_sweep) kb_cond_any_postag<<<1, 1, 0, s>>>(h_sweep, b.ctl);
+  return cudaGetLastError();
+}
+
+// The fused FP32-bulk stage over the batch: findalpha with each cell's
+// splitting terms (kb_alpha's tiles), then k_stage32's tiles and ghost chunks
+// of all running slots taken round robin by a persistent grid (the slot of
+// item k: s32prefix[s] <= k < s32prefix[s+1]); each slot's positivity flag as
+// kb_rk sets it.
+__global__ void kb_alpha_terms32(const BatchSlot* __restrict__ tab,
+                                 const long long* __restrict__ tp, int n,
+                                 const BatchCtl* __restrict__ ctl, int in) {
+  const long long total = ctl->total_tiles;
+  const int tc = ctl->tile_cells;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(tp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;  // uniform over the block
+    const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
+    double a = 0.0;
+    for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+      a = fmax(a, alpha_cell(sl.p, sl.st[in], t));
+      terms32_cell<true>(sl.p, sl.st[in], (float*)sl.split, (float*)sl.roe, t);
+    }
+    a = block_max(a);
+    if (threadIdx.x == 0)
+      atomicMax(&sl.dsc->alpha_bits, (unsigned long long)__double_as_longlong(a));
+    __syncthreads();  // block_max's shared words are reused by the next tile
+  }
+}
+
+long long stage32_items(const Params& p) {
+  return stage32_tiles(p.g) + (stage32_ghosts(p.g) + 255) / 256;
+}
+
+__global__ void __launch_bounds__(256, 4)
+    kb_stage32(const BatchSlot* __restrict__ tab, const long long* __restrict__ sp, int n,
+               BatchCtl* ctl, int stage, int in, int out) {
+  extern __shared__ __align__(16) unsigned char s32_raw[];
+  Stage32Tile& sm = *reinterpret_cast<Stage32Tile*>(s32_raw);
+  const long long total = ctl->total_s32;
+  for (long long k = blockIdx.x; k < total; k += gridDim.x) {
+    const int s = tile_slot(sp, n, k);
+    const BatchSlot& sl = tab[s];
+    if (!sl.active) continue;  // uniform over the block
+    DevScalars* d = sl.dsc;
+    const double dt = d->dt, am = d->alphamax;
+    const long long local = k - sp[s];
+    const int tiles = stage32_tiles(sl.p.g);
+    if (local < tiles) {
+      const int bad = stage32_tile<256>(sl.p, stage, sl.st[in], sl.st[0], (const float*)sl.split,
+                                        (const float*)sl.roe, dt, am, sl.st[out], (int)local, sm);
+      if (block_or(bad) && threadIdx.x == 0) {
+        atomicOr(&d->postag, 1);
+        if (sl.use_limiter == 2) atomicOr(&ctl->any_postag, 1);
+      }
+    } else {
+      stage32_ghosts_chunk<256>(sl.p, stage, sl.st[in], sl.st[0], dt, sl.st[out], local - tiles);
+    }
+    __syncthreads();  // the next item rewrites the tile's shared memory
+  }
+}
+
+cudaError_t batch_stage32_setup() {
+  return cudaFuncSetAttribute(kb_stage32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(Stage32Tile));
+}
+
+static int batch_stage32_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_stage32, 256, sizeof(Stage32Tile));
+    grid = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+  }
+  return grid;
+}
+
+cudaError_t launch_batch_stage32(const BatchLaunch& b, int stage, int in, int out,
+                                 cudaGraphConditionalHandle h_sweep, cudaStream_t s) {
+  const int n = b.n_slots;
+  const int gs = (n + 127) / 128;
+  kb_stage_reset<<<gs, 128, 0, s>>>(b.tab, b.ctl, n);
+  kb_alpha_terms32<<<batch_tile_grid(), SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in);
+  kb_alpha_final<<<gs, 128, 0, s>>>(b.tab, n, stage);
+  kb_stage32<<<batch_stage32_grid(), 256, sizeof(Stage32Tile), s>>>(b.tab, b.s32prefix, n,
+                                                                     b.ctl, stage, in, out);
   if (h_sweep) kb_cond_any_postag<<<1, 1, 0, s>>>(h_sweep, b.ctl);
   return cudaGetLastError();
 }

@@ -68,3 +68,39 @@ def test_fused_stage_kernel_count_per_step(swfd, monkeypatch):
     b = run(monkeypatch, "fused", case, 4)
     assert a["stats"] == b["stats"]
     assert a["launches"] - b["launches"] == (14 - 8) * 4, (a["launches"], b["launches"])
+
+
+@pytest.mark.parametrize("shape", [1, 2, 3, 4, 5])
+def test_every_stage_kernel_shape_gives_the_same_bits(swfd, monkeypatch, shape):
+    """SWFD_STAGE32_SHAPE pins the stage kernel's launch shape (threads per
+    tile x tiles per SM: 256x2, 320x2, 256x3, 256x4, 320x3); each gives the
+    separate kernels' bits (ex4 switches, partial tiles, 12 steps)."""
+    case = dict(problem=abi.SEDOV_2D, nx=70, ny=50)
+    a = run(monkeypatch, "split", case, 12)
+    monkeypatch.setenv("SWFD_STAGE32_SHAPE", str(shape))
+    b = run(monkeypatch, "fused", case, 12)
+    monkeypatch.delenv("SWFD_STAGE32_SHAPE")
+    assert a["t"] == b["t"] and a["stats"] == b["stats"]
+    assert np.array_equal(a["u"].view(np.uint64), b["u"].view(np.uint64))
+
+
+def test_batched_fused_stage_equals_separate_kernels(swfd, monkeypatch):
+    """The batch engine takes the fused FP32 stage when every running slot is
+    2D without rank segments or limiter (kb_alpha_terms32, kb_stage32 over
+    all slots' tiles); against its separate kernels each instance keeps its
+    bits, time and statistics."""
+    from sweeping_fd_weno_gb300 import Batch
+    mix = [dict(problem=abi.VORTEX_2D, nx=45, ny=45), dict(problem=abi.SEDOV_2D, nx=70, ny=50),
+           dict(problem=abi.JET_2D, nx=96, ny=24), dict(problem=abi.VORTEX_2D, nx=64, ny=48)]
+    out = {}
+    for mode in ("split", "fused"):
+        monkeypatch.setenv("SWFD_FP32_STAGE", mode)
+        with Batch(max_slots=4, max_nx=128, max_ny=128, precision=F32) as b:
+            for k, m in enumerate(mix):
+                kw = dict(m)
+                assert b.admit(problems.make_config(kw.pop("problem"), precision=F32, **kw), k)
+            assert b.run(8) >= 1
+            out[mode] = [(b.download(k), b.stats(k)) for k in range(len(mix))]
+    for k, (((ua, ta), sa), ((ub, tb), sb)) in enumerate(zip(out["split"], out["fused"])):
+        assert ta == tb and sa == sb, k
+        assert np.array_equal(ua.view(np.uint64), ub.view(np.uint64)), k
