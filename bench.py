@@ -701,10 +701,10 @@ def bench_jet(args, local):
 
 def bench_detonation(args, local):
     """The reactive Euler detonation of ex7 at the reference's size (400x400 on
-    its 4 x 8 ranks): GPU steps timed with CUDA events (the host reads the
-    positivity flag after each stage, as the sweep decision needs), and the
-    oracle on one host core for a bounded sample of the same steps, with a
-    value-for-value check of the state after them."""
+    its 4 x 8 ranks): each GPU step one graph launch (the sweep decisions and
+    its pass loop are conditional nodes) and one read-back of the scalars,
+    and the oracle on one host core for a bounded sample of the same steps,
+    with a value-for-value check of the state after them."""
     import numpy as np
     import oracle
     import torch
@@ -750,7 +750,8 @@ def bench_detonation(args, local):
                            "s": cpu_s, "kind": "port"},
             "speedup_vs_cpu": gpu_rate / cpu_rate, "same_result_after_sample": same,
             "timing": "wall clock around the steps with a device synchronize on both sides "
-                      "(each stage reads the positivity flag on the host)"}
+                      "(each step one graph launch with device-side sweep control and one "
+                      "read-back of the scalars)"}
 
 
 def bench_serving(args, local):

@@ -977,8 +977,12 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     swfd_handle* h = new swfd_handle();
     h->cfg = *cfg;
     h->device = cfg->device;
+    const char* lm = getenv("SWFD_LAUNCH");  // eager: plain launches (for profilers)
+    h->eager = lm && strcmp(lm, "eager") == 0;
     cudaError_t e = cudaSetDevice(h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < SWFD_CAP_DEPTH && e == cudaSuccess; ++k)  // graph capture streams
+      e = cudaStreamCreateWithFlags(&h->cap[k], cudaStreamNonBlocking);
     if (e != cudaSuccess) {
       swfd_destroy(h);
       return fail(nullptr, SWFD_ERR_CUDA, std::string("swfd_create: ") + cudaGetErrorString(e));

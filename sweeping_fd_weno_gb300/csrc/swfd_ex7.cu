@@ -23,6 +23,7 @@
 
 #include "swfd_device.cuh"
 #include "swfd_ex7.h"
+#include "swfd_graph.h"
 
 namespace swfd {
 
@@ -613,6 +614,7 @@ __global__ void k7_density(Ex7View e) {
       rho[a] = delta;
     }
   }
+  e.sc->den_count++;
 }
 
 // v_i of step k: components 1-4 at ordering `ord`, component 5 at ordering I
@@ -626,7 +628,14 @@ __device__ __forceinline__ bool e7_bad(const Ex7View& e, const double* v) {
   return e7_psweep(e, v, 0) <= e.eps || v[0] <= e.eps;
 }
 
+// ordering of pass pair q: I for odd q, II for even (:1490-1493); ord < 0
+// takes it from the device's q
+__device__ __forceinline__ int e7_ord(const Ex7View& e, int ord) {
+  return ord >= 0 ? ord : ((e.sc->q % 2 == 1) ? 0 : 1);
+}
+
 __global__ void k7_flag(Ex7View e, int ord, int fwd) {
+  ord = e7_ord(e, ord);
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int N = e.nx * e.ny;
   if (k >= N) return;
@@ -725,6 +734,7 @@ __device__ bool e7_step(const Ex7View& e, int ord, int fwd, int k) {
 }
 
 __global__ void k7_walk(Ex7View e, int ord, int fwd) {
+  ord = e7_ord(e, ord);
   const int N = e.nx * e.ny, nf = e.sc->nflag;
   const int dk = fwd ? 1 : -1, kend = fwd ? N - 1 : 0;
   int li = fwd ? 0 : nf - 1;
@@ -738,6 +748,71 @@ __global__ void k7_walk(Ex7View e, int ord, int fwd) {
     else k = (fwd ? li < nf : li >= 0) ? e.list[li] : -1;
   }
 }
+
+// ---------------------------------------------------------------------------
+// the sweep's and the stages' decisions on the device (graph conditions; in
+// the eager launch mode the condition word sc->cond)
+// ---------------------------------------------------------------------------
+// the sweep after checkpositivity (:858-863), unless alpha or dt went bad
+__global__ void k7_cond_postag(cudaGraphConditionalHandle h, Ex7View e) {
+  set_cond(h, &e.sc->cond, (e.sc->postag && !(e.sc->err & E7_ERR_NONFINITE)) ? 1u : 0u);
+}
+// scalar_sweep only when min rho < 1d-12 (:1748-1755)
+__global__ void k7_cond_density(cudaGraphConditionalHandle h, Ex7View e) {
+  set_cond(h, &e.sc->cond, e7_unkey(e.sc->rho_min_key) < 1e-12 ? 1u : 0u);
+}
+// after u_bar: the stop on P(u_bar) <= 0 (:1495-1499), the sweep's count and
+// track entries, then the pass pairs from q = 1
+__global__ void k7_sweep_begin(cudaGraphConditionalHandle h, Ex7View e, int swp_num) {
+  Ex7Scalars* sc = e.sc;
+  const double* ub = sc->ubar;
+  if (e.g1 * (ub[3] - 0.5 * (ub[1] * ub[1]) / ub[0] - 0.5 * (ub[2] * ub[2]) / ub[0] -
+              e.q * ub[4]) <= 0.) {
+    sc->err |= E7_ERR_PUBAR;
+    set_cond(h, &sc->cond, 0u);
+    return;
+  }
+  const long long n = sc->sweep_count++;
+  if (n < sc->track_cap)
+    sc->tracks[n] = sc->tracks[sc->track_cap + n] = sc->tracks[2 * sc->track_cap + n] = 0;
+  sc->t_pos = sc->t_neg = 0;
+  sc->q = 1;
+  if (swp_num < 1) {
+    sc->fail_count++;
+    sc->err |= E7_ERR_NOCONV;
+  }
+  set_cond(h, &sc->cond, swp_num >= 1 ? 1u : 0u);
+}
+// after a pass pair and the minima: the stops (total pressure increased,
+// sweepI(0)), the exit test p_min > eps and rho_min > eps with its track
+// entries (:1660-1672), or the next q up to swp_num
+__global__ void k7_q_end(cudaGraphConditionalHandle h, Ex7View e, int swp_num) {
+  Ex7Scalars* sc = e.sc;
+  if (sc->err & (E7_ERR_SWEEP_CHECK | E7_ERR_SWEEP_INDEX)) {
+    set_cond(h, &sc->cond, 0u);
+    return;
+  }
+  sc->pre_count++;
+  if (e7_unkey(sc->p_min_key) > e.eps && e7_unkey(sc->rho_min_key) > e.eps) {
+    const long long n = sc->sweep_count - 1, c = sc->track_cap;
+    if (n < c) {
+      sc->tracks[n] = sc->q;
+      sc->tracks[c + n] = (int)sc->t_neg;
+      sc->tracks[2 * c + n] = (int)sc->t_pos;
+    }
+    set_cond(h, &sc->cond, 0u);
+    return;
+  }
+  if (++sc->q > swp_num) {
+    sc->fail_count++;
+    sc->err |= E7_ERR_NOCONV;
+    set_cond(h, &sc->cond, 0u);
+    return;
+  }
+  set_cond(h, &sc->cond, 1u);
+}
+// time = time + dt (:97-99)
+__global__ void k7_time_advance(Ex7View e) { e.sc->time = e.sc->time + e.sc->dt; }
 
 }  // namespace
 
@@ -779,93 +854,190 @@ swfd_status e7_sync_scalars(swfd_handle* h) {
   return SWFD_OK;
 }
 
+// a launch recorded into the builder (a capture, or eager on the stream)
+#define E7B(b, launch)          \
+  do {                          \
+    launch;                     \
+    (b).ok(cudaGetLastError()); \
+    (b).k(1);                   \
+  } while (0)
+
 // the interface kernel specialised on the literal form and the limiter
-swfd_status e7_launch_flux(swfd_handle* h, int64_t faces, int ydir) {
-  const Ex7View& v = h->ex7->v;
-  cudaStream_t s = h->stream;
+void e7_emit_flux(Builder& b, const Ex7View& v, int64_t faces, int ydir, cudaStream_t s) {
   const unsigned g = e7_grid(faces, 128);
   const bool lim = v.use_limiter == 1;
   if (v.quad) {
-    if (lim) E7K(h, (k7_flux<true, true><<<g, 128, 0, s>>>(v, ydir)));
-    else E7K(h, (k7_flux<true, false><<<g, 128, 0, s>>>(v, ydir)));
+    if (lim) E7B(b, (k7_flux<true, true><<<g, 128, 0, s>>>(v, ydir)));
+    else E7B(b, (k7_flux<true, false><<<g, 128, 0, s>>>(v, ydir)));
   } else {
-    if (lim) E7K(h, (k7_flux<false, true><<<g, 128, 0, s>>>(v, ydir)));
-    else E7K(h, (k7_flux<false, false><<<g, 128, 0, s>>>(v, ydir)));
+    if (lim) E7B(b, (k7_flux<false, true><<<g, 128, 0, s>>>(v, ydir)));
+    else E7B(b, (k7_flux<false, false><<<g, 128, 0, s>>>(v, ydir)));
   }
-  return SWFD_OK;
 }
 
-swfd_status e7_bc(swfd_handle* h) {
-  const Ex7View& v = h->ex7->v;
-  cudaStream_t s = h->stream;
+void e7_emit_bc(Builder& b, const Ex7View& v, cudaStream_t s) {
   for (int rep = 0; rep < 2; ++rep) {  // twice, for the corners (:943-959)
-    E7K(h, (k7_exchange_x<<<e7_grid((int64_t)v.R * v.LJ * 3), E7_BLOCK, 0, s>>>(v)));
-    E7K(h, (k7_exchange_y<<<e7_grid((int64_t)v.R * v.LI * 3), E7_BLOCK, 0, s>>>(v)));
+    E7B(b, (k7_exchange_x<<<e7_grid((int64_t)v.R * v.LJ * 3), E7_BLOCK, 0, s>>>(v)));
+    E7B(b, (k7_exchange_y<<<e7_grid((int64_t)v.R * v.LI * 3), E7_BLOCK, 0, s>>>(v)));
   }
   const unsigned g = e7_grid((int64_t)v.R * v.LI * v.LJ);
-  for (int which = 0; which < 4; ++which) E7K(h, (k7_bc_rule<<<g, E7_BLOCK, 0, s>>>(v, which)));
+  for (int which = 0; which < 4; ++which) E7B(b, (k7_bc_rule<<<g, E7_BLOCK, 0, s>>>(v, which)));
+}
+
+// plain stream launches (initdata's bc)
+swfd_status e7_bc(swfd_handle* h) {
+  Builder b;
+  b.h = h;
+  b.eager = true;
+  b.launched = &h->ex7->launches;
+  e7_emit_bc(b, h->ex7->v, h->stream);
+  if (b.err != cudaSuccess)
+    return e7_fail(h, SWFD_ERR_CUDA, std::string("detonation: ") + cudaGetErrorString(b.err));
   return SWFD_OK;
 }
 
-// sweep_lim on the gathered interior; the ranks are gathered before and
-// scattered after by the caller
-swfd_status e7_sweep(swfd_handle* h) {
-  Ex7* x = h->ex7;
+// sweep_lim on the gathered interior (:1435-1680): gather, [scalar_sweep],
+// u_bar, then WHILE the pass pairs run { ordering I or II forward and
+// backward, the minima, the exit test }, scatter.  Every decision is a
+// device kernel's (k7_cond_density, k7_sweep_begin, k7_q_end).
+void e7_emit_sweep(Builder& b, Ex7* x, cudaStream_t s) {
   const Ex7View& v = x->v;
-  cudaStream_t s = h->stream;
   const int64_t N = (int64_t)v.nx * v.ny;
   Ex7Scalars* sc = v.sc;
-  // scalar_sweep: only when min rho < 1d-12 (:1748-1755)
-  E7CU(h, cudaMemsetAsync(&sc->rho_min_key, 0xff, 2 * sizeof(unsigned long long), s));
-  E7K(h, (k7_min<<<e7_grid(N), E7_BLOCK, 0, s>>>(v)));
-  ST(e7_sync_scalars(h));
-  if (e7_unkey(x->hs->rho_min_key) < 1e-12) {
-    E7K(h, (k7_density<<<1, 1, 0, s>>>(v)));
-    x->den_count++;
-  }
+  int* saved = b.count;
+  x->k_sweep = x->k_q = 0;  // every stage emits the same sweep: count it once
+  b.count = &x->k_sweep;
+  E7B(b, (k7_gather<<<e7_grid(N), E7_BLOCK, 0, s>>>(v, 1)));
+  B_OK(b, cudaMemsetAsync(&sc->rho_min_key, 0xff, 2 * sizeof(unsigned long long), s));
+  E7B(b, (k7_min<<<e7_grid(N), E7_BLOCK, 0, s>>>(v)));
+  const cudaGraphConditionalHandle hd = b.handle();
+  E7B(b, (k7_cond_density<<<1, 1, 0, s>>>(hd, v)));
+  b.cond(s, cudaGraphCondTypeIf, hd, [&](cudaStream_t sd) {
+    b.count = nullptr;  // counted through den_count
+    E7B(b, (k7_density<<<1, 1, 0, sd>>>(v)));
+    b.count = &x->k_sweep;
+  });
   // u_bar: five sequential sums, j outer (:1464-1485)
   const double w = 1. / ((double)v.nx * (double)v.ny);
   for (int c = 0; c < 5; ++c) {
-    E7CU(h, launch_seq_sum(v.ug + c * N, N, w, &sc->ubar[c], x->sum_scratch, s));
-    x->launches += 3;
+    B_OK(b, launch_seq_sum(v.ug + c * N, N, w, &sc->ubar[c], x->sum_scratch, s));
+    b.k(3);
   }
-  ST(e7_sync_scalars(h));
-  const double* ub = x->hs->ubar;
-  // stop on P(u_bar) <= 0 (:1495-1499)
-  if (v.g1 * (ub[3] - 0.5 * (ub[1] * ub[1]) / ub[0] - 0.5 * (ub[2] * ub[2]) / ub[0] - v.q * ub[4]) <= 0.)
-    return e7_fail(h, SWFD_ERR_PUBAR_NONPOS, "detonation sweep: P(u_bar) <= 0");
-  x->sweep_count++;
-  x->sweep_track.push_back(0);
-  x->neg_track.push_back(0);
-  x->pos_track.push_back(0);
-  E7CU(h, cudaMemsetAsync(&sc->t_pos, 0, 2 * sizeof(long long), s));
-  for (int q = 1; q <= x->swp_num; ++q) {
-    const int ord = (q % 2 == 1) ? 0 : 1;
+  const cudaGraphConditionalHandle hw = b.handle();
+  E7B(b, (k7_sweep_begin<<<1, 1, 0, s>>>(hw, v, x->swp_num)));
+  b.cond(s, cudaGraphCondTypeWhile, hw, [&](cudaStream_t sq) {
+    b.count = &x->k_q;
     for (int fwd = 1; fwd >= 0; --fwd) {
-      E7K(h, (k7_flag<<<e7_grid(N), E7_BLOCK, 0, s>>>(v, ord, fwd)));
-      E7K(h, (k7_compact<<<1, 1024, 0, s>>>(v)));
-      E7K(h, (k7_walk<<<1, 1, 0, s>>>(v, ord, fwd)));
+      E7B(b, (k7_flag<<<e7_grid(N), E7_BLOCK, 0, sq>>>(v, -1, fwd)));
+      E7B(b, (k7_compact<<<1, 1024, 0, sq>>>(v)));
+      E7B(b, (k7_walk<<<1, 1, 0, sq>>>(v, -1, fwd)));
     }
-    E7CU(h, cudaMemsetAsync(&sc->rho_min_key, 0xff, 2 * sizeof(unsigned long long), s));
-    E7K(h, (k7_min<<<e7_grid(N), E7_BLOCK, 0, s>>>(v)));
-    ST(e7_sync_scalars(h));
-    if (x->hs->err & E7_ERR_SWEEP_CHECK)
-      return e7_fail(h, SWFD_ERR_SWEEP_CHECK, "detonation sweep: total pressure increased");
-    if (x->hs->err & E7_ERR_SWEEP_INDEX)
-      return e7_fail(h, SWFD_ERR_UNSUPPORTED,
-                     "detonation sweep: the first ordering-II step adjusts, where the "
-                     "reference reads sweepI(0)");
-    x->pre_count++;
-    const double p_min = e7_unkey(x->hs->p_min_key), rho_min = e7_unkey(x->hs->rho_min_key);
-    if (p_min > v.eps && rho_min > v.eps) {
-      x->sweep_track.back() = q;
-      x->neg_track.back() = (int32_t)x->hs->t_neg;
-      x->pos_track.back() = (int32_t)x->hs->t_pos;
-      return SWFD_OK;
+    B_OK(b, cudaMemsetAsync(&sc->rho_min_key, 0xff, 2 * sizeof(unsigned long long), sq));
+    E7B(b, (k7_min<<<e7_grid(N), E7_BLOCK, 0, sq>>>(v)));
+    E7B(b, (k7_q_end<<<1, 1, 0, sq>>>(hw, v, x->swp_num)));
+    b.count = &x->k_sweep;
+  });
+  E7B(b, (k7_gather<<<e7_grid(N), E7_BLOCK, 0, s>>>(v, 0)));
+  b.count = saved;
+}
+
+// rk (:810-888): three stages of wenofd, scheme, the RK combination,
+// checkpositivity, IF (postag) the sweep, bc; then the time advance
+void e7_emit_step(Builder& b, Ex7* x, cudaStream_t s) {
+  const Ex7View& v = x->v;
+  const int64_t cells = (int64_t)v.R * v.LI * v.LJ;
+  const int64_t faces = (int64_t)v.R * (v.nxl + 2) * (v.nyl + 2);
+  x->k_step = 0;
+  b.count = &x->k_step;
+  for (int stage = 1; stage <= 3; ++stage) {
+    B_OK(b, cudaMemsetAsync(&v.sc->am_bits, 0, sizeof(unsigned long long), s));
+    E7B(b, (k7_alpha<<<e7_grid(cells), E7_BLOCK, 0, s>>>(v)));
+    if (stage == 1) E7B(b, (k7_dt<<<1, 1, 0, s>>>(v)));
+    else E7B(b, (k7_alphamax<<<1, 1, 0, s>>>(v)));
+    // wenofd: x pass then y pass, each after its wall mirror
+    E7B(b, (k7_mirror_x<<<e7_grid((int64_t)v.cut_y * (v.nyl + 2) * 3), E7_BLOCK, 0, s>>>(v)));
+    E7B(b, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LJ * 32), E7_BLOCK, 0, s>>>(v, 0)));
+    E7B(b, (k7_split<<<e7_grid((int64_t)v.R * v.LI * (v.nyl + 2)), E7_BLOCK, 0, s>>>(v, 0)));
+    e7_emit_flux(b, v, faces, 0, s);
+    E7B(b, (k7_mirror_y<<<e7_grid((int64_t)v.cut_y * 3 * v.total), E7_BLOCK, 0, s>>>(v)));
+    E7B(b, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LI * 32), E7_BLOCK, 0, s>>>(v, 1)));
+    E7B(b, (k7_split<<<e7_grid((int64_t)v.R * (v.nxl + 2) * v.LJ), E7_BLOCK, 0, s>>>(v, 1)));
+    e7_emit_flux(b, v, faces, 1, s);
+    // u0 = u after wenofd, whose wall mirrors rewrite cells of u (:822)
+    if (stage == 1)
+      B_OK(b, cudaMemcpyAsync(v.u0, v.u, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    B_OK(b, cudaMemsetAsync(&v.sc->postag, 0, sizeof(int), s));
+    if (v.quad) E7B(b, (k7_rk<true><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
+    else E7B(b, (k7_rk<false><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
+    if (x->use_limiter == 2) {
+      const cudaGraphConditionalHandle hs = b.handle();
+      E7B(b, (k7_cond_postag<<<1, 1, 0, s>>>(hs, v)));
+      b.cond(s, cudaGraphCondTypeIf, hs, [&](cudaStream_t sw) { e7_emit_sweep(b, x, sw); });
+      b.count = &x->k_step;
     }
+    e7_emit_bc(b, v, s);
   }
-  x->fail_count++;
-  return e7_fail(h, SWFD_ERR_SWEEP_NOCONV, "detonation sweep: swp_num reached");
+  E7B(b, (k7_time_advance<<<1, 1, 0, s>>>(v)));
+}
+
+// the step graph, captured once
+swfd_status e7_build_step(swfd_handle* h) {
+  Ex7* x = h->ex7;
+  if (x->g_step || h->eager) return SWFD_OK;
+  Builder b;
+  b.h = h;
+  b.cap = h->cap;
+  b.max_depth = SWFD_CAP_DEPTH - 1;
+  cudaStream_t s = h->cap[0];
+  E7CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  cudaStreamCaptureStatus cs;
+  b.ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &b.root, nullptr, nullptr, nullptr));
+  e7_emit_step(b, x, s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s, &g);
+  if (b.err != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return e7_fail(h, SWFD_ERR_CUDA, std::string("detonation graph capture: ") +
+                                         cudaGetErrorString(b.err != cudaSuccess ? b.err : e2));
+  }
+  cudaError_t e3 = cudaGraphInstantiate(&x->g_step, g, 0);
+  cudaGraphDestroy(g);
+  if (e3 != cudaSuccess)
+    return e7_fail(h, SWFD_ERR_CUDA,
+                   std::string("detonation graph instantiate: ") + cudaGetErrorString(e3));
+  return SWFD_OK;
+}
+
+// the device's view of the track buffer (after a reset of the scalars too)
+swfd_status e7_publish_tracks(swfd_handle* h) {
+  Ex7* x = h->ex7;
+  const long long lc = x->track_cap;
+  E7CU(h, cudaMemcpyAsync(&x->v.sc->tracks, &x->tracks, sizeof(int*), cudaMemcpyHostToDevice,
+                          h->stream));
+  E7CU(h, cudaMemcpyAsync(&x->v.sc->track_cap, &lc, sizeof(long long), cudaMemcpyHostToDevice,
+                          h->stream));
+  E7CU(h, cudaStreamSynchronize(h->stream));
+  return SWFD_OK;
+}
+
+// room on the device for `extra` more sweeps' track entries (the host
+// mirror holds the count after the last step)
+swfd_status e7_ensure_tracks(swfd_handle* h, int64_t extra) {
+  Ex7* x = h->ex7;
+  const int64_t need = x->hs->sweep_count + extra;
+  if (need <= x->track_cap) return SWFD_OK;
+  const int64_t cap = std::max<int64_t>(need, 2 * x->track_cap + 1024);
+  int* nt = nullptr;
+  E7CU(h, cudaMalloc(&nt, 3 * cap * sizeof(int)));
+  E7CU(h, cudaMemsetAsync(nt, 0, 3 * cap * sizeof(int), h->stream));
+  for (int c = 0; c < 3 && x->tracks; ++c)
+    E7CU(h, cudaMemcpyAsync(nt + c * cap, x->tracks + c * x->track_cap,
+                            x->track_cap * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+  E7CU(h, cudaStreamSynchronize(h->stream));
+  cudaFree(x->tracks);
+  x->tracks = nt;
+  x->track_cap = cap;
+  return e7_publish_tracks(h);
 }
 
 }  // namespace
@@ -1014,6 +1186,8 @@ swfd_status ex7_create(swfd_handle* h, std::string& err) {
 
 void ex7_destroy(Ex7* x) {
   if (!x) return;
+  if (x->g_step) cudaGraphExecDestroy(x->g_step);
+  cudaFree(x->tracks);
   cudaFree(x->block);
   cudaFree(x->sum_scratch);
   if (x->hs) cudaFreeHost(x->hs);
@@ -1043,13 +1217,9 @@ swfd_status ex7_init(swfd_handle* h) {
                           h->stream));
   ST(e7_bc(h));
   E7CU(h, cudaMemsetAsync(v.sc, 0, sizeof(Ex7Scalars), h->stream));
-  E7CU(h, cudaStreamSynchronize(h->stream));
   h->time = 0.;
-  x->sweep_count = x->den_count = x->pre_count = x->fail_count = 0;
-  x->sweep_track.clear();
-  x->neg_track.clear();
-  x->pos_track.clear();
-  return SWFD_OK;
+  ST(e7_publish_tracks(h));  // the reset cleared the scalars' track buffer
+  return e7_sync_scalars(h);
 }
 
 swfd_status ex7_upload(swfd_handle* h, const double* u) {
@@ -1089,84 +1259,93 @@ swfd_status ex7_find_alpha(swfd_handle* h, double* alphamax) {
   return SWFD_OK;
 }
 
-// rk (:810-888): three stages of wenofd, scheme, the RK combination,
-// checkpositivity, the sweep on the gathered interior and bc
+// One step (:810-888) as one graph launch (SWFD_LAUNCH=eager: the same
+// kernels on the stream, the conditions read back), then one read-back of
+// the scalars: the device's errors become the step's status, its time the
+// host's.
 swfd_status ex7_step(swfd_handle* h, double* dt_out) {
   Ex7* x = h->ex7;
-  const Ex7View& v = x->v;
-  cudaStream_t s = h->stream;
-  const int64_t cells = (int64_t)v.R * v.LI * v.LJ;
-  const int64_t faces = (int64_t)v.R * (v.nxl + 2) * (v.nyl + 2);
-  const int64_t N = (int64_t)v.nx * v.ny;
-  for (int stage = 1; stage <= 3; ++stage) {
-    E7CU(h, cudaMemsetAsync(&v.sc->am_bits, 0, sizeof(unsigned long long), s));
-    E7K(h, (k7_alpha<<<e7_grid(cells), E7_BLOCK, 0, s>>>(v)));
-    if (stage == 1) E7K(h, (k7_dt<<<1, 1, 0, s>>>(v)));
-    else E7K(h, (k7_alphamax<<<1, 1, 0, s>>>(v)));
-    // wenofd: x pass then y pass, each after its wall mirror
-    E7K(h, (k7_mirror_x<<<e7_grid((int64_t)v.cut_y * (v.nyl + 2) * 3), E7_BLOCK, 0, s>>>(v)));
-    E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LJ * 32), E7_BLOCK, 0, s>>>(v, 0)));
-    E7K(h, (k7_split<<<e7_grid((int64_t)v.R * v.LI * (v.nyl + 2)), E7_BLOCK, 0, s>>>(v, 0)));
-    ST(e7_launch_flux(h, faces, 0));
-    E7K(h, (k7_mirror_y<<<e7_grid((int64_t)v.cut_y * 3 * v.total), E7_BLOCK, 0, s>>>(v)));
-    E7K(h, (k7_line_alpha<<<e7_grid((int64_t)v.R * v.LI * 32), E7_BLOCK, 0, s>>>(v, 1)));
-    E7K(h, (k7_split<<<e7_grid((int64_t)v.R * (v.nxl + 2) * v.LJ), E7_BLOCK, 0, s>>>(v, 1)));
-    ST(e7_launch_flux(h, faces, 1));
-    // u0 = u after wenofd, whose wall mirrors rewrite cells of u (:822)
-    if (stage == 1)
-      E7CU(h, cudaMemcpyAsync(v.u0, v.u, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    E7CU(h, cudaMemsetAsync(&v.sc->postag, 0, sizeof(int), s));
-    if (v.quad) E7K(h, (k7_rk<true><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
-    else E7K(h, (k7_rk<false><<<e7_grid(cells), E7_BLOCK, 0, s>>>(v, stage)));
-    if (x->use_limiter == 2) {
-      ST(e7_sync_scalars(h));
-      if (x->hs->err & E7_ERR_NONFINITE)
-        return e7_fail(h, SWFD_ERR_NONFINITE, "detonation: non-finite alpha or dt");
-      if (x->hs->postag) {
-        E7K(h, (k7_gather<<<e7_grid(N), E7_BLOCK, 0, s>>>(v, 1)));
-        ST(e7_sweep(h));
-        E7K(h, (k7_gather<<<e7_grid(N), E7_BLOCK, 0, s>>>(v, 0)));
-      }
-    }
-    ST(e7_bc(h));
+  ST(e7_ensure_tracks(h, 3));
+  const Ex7Scalars before = *x->hs;
+  if (h->eager) {
+    Builder b;
+    b.h = h;
+    b.eager = true;
+    b.cond_word = &x->v.sc->cond;
+    b.launched = &x->launches;
+    e7_emit_step(b, x, h->stream);
+    if (b.err != cudaSuccess)
+      return e7_fail(h, SWFD_ERR_CUDA, std::string("detonation: ") + cudaGetErrorString(b.err));
+  } else {
+    ST(e7_build_step(h));
+    E7CU(h, cudaGraphLaunch(x->g_step, h->stream));
   }
   ST(e7_sync_scalars(h));
-  if (x->hs->err & E7_ERR_NONFINITE)
+  const Ex7Scalars& a = *x->hs;
+  if (!h->eager)  // kernels run: the step's, each sweep's fixed part, densities, pass pairs
+    x->launches += x->k_step + (a.sweep_count - before.sweep_count) * x->k_sweep +
+                   (a.den_count - before.den_count) + (a.pre_count - before.pre_count) * x->k_q;
+  if (a.err & E7_ERR_NONFINITE)
     return e7_fail(h, SWFD_ERR_NONFINITE, "detonation: non-finite alpha or dt");
-  h->time = h->time + x->hs->dt;
-  E7CU(h, cudaMemcpyAsync(&v.sc->time, &h->time, sizeof(double), cudaMemcpyHostToDevice, s));
-  if (dt_out) *dt_out = x->hs->dt;
+  if (a.err & E7_ERR_PUBAR)
+    return e7_fail(h, SWFD_ERR_PUBAR_NONPOS, "detonation sweep: P(u_bar) <= 0");
+  if (a.err & E7_ERR_SWEEP_CHECK)
+    return e7_fail(h, SWFD_ERR_SWEEP_CHECK, "detonation sweep: total pressure increased");
+  if (a.err & E7_ERR_SWEEP_INDEX)
+    return e7_fail(h, SWFD_ERR_UNSUPPORTED,
+                   "detonation sweep: the first ordering-II step adjusts, where the "
+                   "reference reads sweepI(0)");
+  if (a.err & E7_ERR_NOCONV)
+    return e7_fail(h, SWFD_ERR_SWEEP_NOCONV, "detonation sweep: swp_num reached");
+  h->time = a.time;
+  if (dt_out) *dt_out = a.dt;
+  return SWFD_OK;
+}
+
+// the device's tracks of the sweeps so far (n entries each)
+swfd_status e7_read_tracks(swfd_handle* h, std::vector<int32_t>& t, int64_t& n) {
+  Ex7* x = h->ex7;
+  ST(e7_sync_scalars(h));
+  n = std::min<int64_t>(x->hs->sweep_count, x->track_cap);
+  t.assign(3 * (size_t)n, 0);
+  for (int c = 0; c < 3 && n > 0; ++c)
+    E7CU(h, cudaMemcpy(t.data() + c * n, x->tracks + c * x->track_cap, n * sizeof(int32_t),
+                       cudaMemcpyDeviceToHost));
   return SWFD_OK;
 }
 
 swfd_status ex7_stats(swfd_handle* h, swfd_sweep_stats* st) {
   const Ex7* x = h->ex7;
-  ST(e7_sync_scalars(h));
+  std::vector<int32_t> t;
+  int64_t n = 0;
+  ST(e7_read_tracks(h, t, n));
   memset(st, 0, sizeof(*st));
-  st->sweep_count = x->sweep_count;
-  for (size_t k = 0; k < x->sweep_track.size(); ++k) {
-    st->total_sweep += x->sweep_track[k];
-    st->max_sweep = std::max<int64_t>(st->max_sweep, x->sweep_track[k]);
-    st->total_neg += x->neg_track[k];
-    st->max_neg = std::max<int64_t>(st->max_neg, x->neg_track[k]);
-    st->total_pos += x->pos_track[k];
-    st->max_pos = std::max<int64_t>(st->max_pos, x->pos_track[k]);
+  st->sweep_count = x->hs->sweep_count;
+  for (int64_t k = 0; k < n; ++k) {
+    st->total_sweep += t[k];
+    st->max_sweep = std::max<int64_t>(st->max_sweep, t[k]);
+    st->total_neg += t[n + k];
+    st->max_neg = std::max<int64_t>(st->max_neg, t[n + k]);
+    st->total_pos += t[2 * n + k];
+    st->max_pos = std::max<int64_t>(st->max_pos, t[2 * n + k]);
   }
-  st->den_count = x->den_count + x->hs->lim_den;  // the ranks' limiter counts, summed
-  st->pre_count = x->pre_count + x->hs->lim_pre;
-  st->sweep_fail_count = x->fail_count;
+  st->den_count = x->hs->den_count + x->hs->lim_den;  // the ranks' limiter counts, summed
+  st->pre_count = x->hs->pre_count + x->hs->lim_pre;
+  st->sweep_fail_count = x->hs->fail_count;
   return SWFD_OK;
 }
 
 int64_t ex7_tracks(swfd_handle* h, int32_t* sweep, int32_t* neg, int32_t* pos, int64_t cap) {
-  const Ex7* x = h->ex7;
-  const int64_t n = std::min<int64_t>((int64_t)x->sweep_track.size(), cap);
-  for (int64_t k = 0; k < n; ++k) {
-    if (sweep) sweep[k] = x->sweep_track[k];
-    if (neg) neg[k] = x->neg_track[k];
-    if (pos) pos[k] = x->pos_track[k];
+  std::vector<int32_t> t;
+  int64_t n = 0;
+  if (e7_read_tracks(h, t, n) != SWFD_OK) return -1;
+  const int64_t m = std::min<int64_t>(n, cap);
+  for (int64_t k = 0; k < m; ++k) {
+    if (sweep) sweep[k] = t[k];
+    if (neg) neg[k] = t[n + k];
+    if (pos) pos[k] = t[2 * n + k];
   }
-  return (int64_t)x->sweep_track.size();
+  return n;
 }
 
 int64_t ex7_launches(swfd_handle* h) { return h->ex7->launches; }

@@ -14,6 +14,8 @@ namespace swfd {
 constexpr int E7_ERR_NONFINITE = 1;     // alpha or dt not finite
 constexpr int E7_ERR_SWEEP_CHECK = 2;   // a nodal adjustment raised the pair's total pressure
 constexpr int E7_ERR_SWEEP_INDEX = 4;   // the ordering-II pass needed sweepI(0)
+constexpr int E7_ERR_PUBAR = 8;         // the sweep's P(u_bar) <= 0
+constexpr int E7_ERR_NOCONV = 16;       // the sweep reached swp_num
 
 struct Ex7Scalars {
   unsigned long long am_bits;  // alphamax as bits (non-negative values)
@@ -24,6 +26,13 @@ struct Ex7Scalars {
   int nflag, pad;
   double ubar[5];
   long long lim_den, lim_pre;  // use_limiter = 1: density and pressure limitings
+  // the sweep's control on the device: its pass pair q, the condition word of
+  // the eager launch mode, the statistics and the tracks (sweep, neg, pos;
+  // 3 x track_cap, grown by the host between steps)
+  int q, cond;
+  long long sweep_count, den_count, pre_count, fail_count;
+  int* tracks;
+  long long track_cap;
 };
 
 // everything a kernel needs, passed by value
@@ -55,9 +64,15 @@ struct Ex7 {
   void* sum_scratch = nullptr;  // the u_bar sums' terms and chunk summaries
   int use_limiter = 2, swp_num = 0;
   double t_loop = 0.;  // DO WHILE (time <= time_terminal - 1d-10), literal-exact
-  int64_t sweep_count = 0, den_count = 0, pre_count = 0, fail_count = 0;
-  std::vector<int32_t> sweep_track, neg_track, pos_track;
-  int64_t launches = 0;
+  int* tracks = nullptr;  // device sweep tracks (3 x track_cap)
+  int64_t track_cap = 0;
+  // one step as a CUDA graph: three stages, each with an IF around the sweep
+  // (whose pass pairs are a WHILE) -- no host synchronisation inside a step
+  cudaGraphExec_t g_step = nullptr;
+  // kernels per graph section (launch accounting): the step without sweeps,
+  // a sweep's fixed part, one pass pair
+  int k_step = 0, k_sweep = 0, k_q = 0;
+  long long launches = 0;
 };
 
 // configuration check (total, rank grid, wall mirrors inside the local arrays)
