@@ -45,15 +45,25 @@ STAGE_BYTES_PER_CELL = (64 + 96 + 96) / 3.0
 # FP64 pipe instructions (379 DADD, 465 DMUL, 353 DFMA -- the DFMAs are the
 # divisions and the square root); with the divisions and the products by
 # 2, 4, 0.25 and 0.5 on the integer pipes (the same bits), 739 (355 DADD,
-# 379 DMUL, 5 DFMA).  Both counted by ncu on k_flux_xy<double>.
+# 379 DMUL, 5 DFMA).  Both counted by ncu on the one-lane k_flux_xy<double>;
+# the default lane-pair kernel executes 774 (both lanes of a pair form the
+# interface's eigenvectors), and 739 stays the work the roofline counts.
 FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
 FLUX_FP64_INST_PER_INTERFACE = 739
+FLUX_FP64_INST_PER_INTERFACE_EXECUTED = 774
 FLUX_FP64_INST_PER_INTERFACE_HW_DIV = 1197
-# DRAM bytes of one k_flux_xy<double> launch per interior cell, from an ncu
-# capture of the 1024x1024 vortex (315.2 MB per launch, inputs above L2)
-FLUX_DRAM_BYTES_PER_CELL = 315.2e6 / (1024 * 1024)
-# the same for k_flux_xy<float> of the FP32-bulk form (134.4 MB per launch)
+# DRAM bytes of one k_flux_xy_pair<4> launch per interior cell, from an ncu
+# capture of the 1024x1024 vortex (313.3 MB per launch, inputs above L2)
+FLUX_DRAM_BYTES_PER_CELL = 313.3e6 / (1024 * 1024)
+# the same for k_flux_xy<float> of the FP32-bulk form's separate kernels
+# (134.4 MB per launch) and for its fused stage kernel k_stage32<256, 4>
+# (107.9 MB per launch)
 FLUX_F32_DRAM_BYTES_PER_CELL = 134.4e6 / (1024 * 1024)
+STAGE32_DRAM_BYTES_PER_CELL = 107.9e6 / (1024 * 1024)
+# algorithmic bytes of one fused FP32-bulk stage per interior cell: the nine
+# splitting terms and four Roe planes (FP32) read once, u and u0 read and u
+# written (FP64)
+STAGE32_BYTES_PER_CELL = 9 * 4 + 4 * 4 + 3 * 32
 
 
 def precision_errors(u32, u64, gamma=1.4):
@@ -1034,7 +1044,9 @@ def main():
     # doubles) and Roe averages (4 doubles) of every cell once per direction,
     # write 8 doubles per interface
     f32 = args.precision != "fp64"
-    launch_bytes = 2 * cells * (12 + 8) * (4.0 if f32 else 8.0)
+    fused32 = f32 and os.environ.get("SWFD_FP32_STAGE") != "split"
+    launch_bytes = (cells * STAGE32_BYTES_PER_CELL if fused32
+                    else 2 * cells * (12 + 8) * (4.0 if f32 else 8.0))
     achieved = launch_bytes / (flux_ms_per_launch * 1e-3) / 1e9
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -1052,9 +1064,10 @@ def main():
         roofline.update({
             "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                              "k_flux_xy<double> on the 1024x1024 vortex (315.2 MB), scaled "
+                              "k_flux_xy_pair<4> on the 1024x1024 vortex (313.3 MB), scaled "
                               "per cell to this grid",
-            "kernel": "k_flux_xy<double> (characteristic WENO5 interface fluxes, both directions)",
+            "kernel": "k_flux_xy_pair<4> (characteristic WENO5 interface fluxes, both "
+                      "directions, two lanes per interface; the default FP64 shape)",
             "compute_bound": "fp64 (the FP64 pipe; divisions and power-of-two products run "
                              "on the integer pipes)",
             "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,
@@ -1062,6 +1075,7 @@ def main():
                      "peak_source": "measured by swfd_probe_fp64_peak (DFMA chains; 2 flops "
                                     "each)",
                      "inst_per_interface": FLUX_FP64_INST_PER_INTERFACE,
+                     "inst_per_interface_executed": FLUX_FP64_INST_PER_INTERFACE_EXECUTED,
                      # the all-hardware instruction stream of the same arithmetic
                      # (hardware divisions) over the measured time: above 1.0 means
                      # faster than that stream could run at the FP64 peak
@@ -1073,6 +1087,16 @@ def main():
                      "achieved_gflops_source_count": 2 * cells * FLUX_FLOPS_PER_INTERFACE
                      / (flux_ms_per_launch * 1e-3) / 1e9,
                      "flops_per_interface": FLUX_FLOPS_PER_INTERFACE}})
+    elif fused32:
+        roofline.update({
+            "traffic": STAGE32_DRAM_BYTES_PER_CELL * cells,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                              "k_stage32<256, 4> on the 1024x1024 vortex (107.9 MB), scaled "
+                              "per cell to this grid",
+            "kernel": "k_stage32<256, 4> (the fused FP32-bulk stage: split fluxes in shared "
+                      "memory, interface fluxes, RHS, RK combination, positivity)",
+            "compute_bound": "issue (ncu on the 1024x1024 vortex: 68 % issue active, FMA "
+                             "pipe 36 %, FP64 pipe 33 %, DRAM 10 %)"})
     else:
         roofline.update({
             "traffic": FLUX_F32_DRAM_BYTES_PER_CELL * cells,

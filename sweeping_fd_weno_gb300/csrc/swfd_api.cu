@@ -1253,7 +1253,7 @@ swfd_status swfd_autotune(swfd_handle* h, int32_t* flux_min_blocks) {
   CU(h, launch_alpha(p, u, h->dsc, h->stream));
   int nk = 0;
   CU(h, launch_split(p, u, h->dsc, h->split, h->roe, h->stream, &nk));
-  int cand[8];
+  int cand[16];
   const int nc = flux_min_blocks_candidates(p.precision == SWFD_PRECISION_FP32_BULK, cand);
   const int saved = p.flux_minb;
   float best = 0.f;
