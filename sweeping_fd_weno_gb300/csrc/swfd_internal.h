@@ -376,9 +376,6 @@ long long stage32_items(const Params& p);
 // values SWFD_FLUX_PAIR + b select the lane-pair kernel with b blocks per SM);
 // returns their number, the default first
 #define SWFD_FLUX_PAIR 10
-// SWFD_FLUX_PAIR_LOOP + b: the lane-pair kernel with its four characteristic
-// fields in a loop (a quarter of the code), b blocks per SM
-#define SWFD_FLUX_PAIR_LOOP 20
 // the FP64 flux kernel's default shape: the lane-pair kernel, 4 blocks per SM
 #define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_PAIR + 4)
 int flux_min_blocks_candidates(bool f32, int* out);

@@ -1155,65 +1155,11 @@ __device__ __forceinline__ double weno_side(double v0, double v1, double v2, dou
   return div(w1, sum) * A + div(w2, sum) * B + div(w3, sum) * C;
 }
 
-// LOOP: the four characteristic fields in a loop that is not unrolled (one
-// field's projection and reconstruction in the instruction stream, a quarter
-// of the code: a smaller instruction footprint for the warps of an SM), the
-// stencil values held in registers across it and the back projection
-// accumulated field by field in the reference's order of the sums; the
-// same operations and operands either way.
-template <int YDIR, bool LOOP, class D>
+template <int YDIR, class D>
 __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const double* __restrict__ s,
                                            int64_t P, int64_t step, double weps, int side, D div,
                                            double out[4]) {
   const int n = YDIR ? 2 : 1, tt = YDIR ? 1 : 2;
-  if constexpr (LOOP) {
-    double a[5][4];
-#pragma unroll
-    for (int m = 0; m < 5; ++m)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) a[m][c] = ldt(s + m * step + c * P);
-    double acc0 = 0., accn = 0., acct = 0., acc3 = 0.;
-#pragma unroll 1
-    for (int k = 0; k < 4; ++k) {
-      double c[5];
-      if (k == 1) {
-#pragma unroll
-        for (int m = 0; m < 5; ++m) c[m] = proj_row2<YDIR>(E.vt, a[m][0], a[m][1], a[m][2]);
-      } else {
-        const double l0 = k == 0 ? E.l1_0 : (k == 2 ? E.l3_0 : E.l4_0);
-        const double ln = k == 0 ? E.l1_n : (k == 2 ? E.l3_n : E.l4_n);
-        const double lt = k == 0 ? E.l1_t : (k == 2 ? E.l3_t : E.l4_t);
-        const double l3 = k == 0 ? E.l1_3 : (k == 2 ? E.l3_3 : E.l4_3);
-#pragma unroll
-        for (int m = 0; m < 5; ++m)
-          c[m] = proj_row<YDIR>(l0, ln, lt, l3, a[m][0], a[m][1], a[m][2], a[m][3]);
-      }
-      const double w = weno_side(c[0], c[1], c[2], c[3], c[4], side, weps, div);
-      // evr . w, one field at a time: row 1 w0 + w2 + w3; normal row
-      // e_nm w0 + vn w2 + e_np w3; tangential vt w0 + w1 + vt w2 + vt w3;
-      // energy e_hm w0 + vt w1 + qm w2 + e_hp w3 (left to right)
-      if (k == 0) {
-        acc0 = w;
-        accn = E.e_nm * w;
-        acct = E.vt * w;
-        acc3 = E.e_hm * w;
-      } else if (k == 1) {
-        acct = acct + w;
-        acc3 = acc3 + E.vt * w;
-      } else {
-        const double cn = k == 2 ? E.vn : E.e_np, c3 = k == 2 ? E.qm : E.e_hp;
-        acc0 = acc0 + w;
-        accn = accn + cn * w;
-        acct = acct + E.vt * w;
-        acc3 = acc3 + c3 * w;
-      }
-    }
-    out[0] = acc0;
-    out[n] = accn;
-    out[tt] = acct;
-    out[3] = acc3;
-    return;
-  }
   double w[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -1238,27 +1184,26 @@ __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const doubl
 struct Side4 {
   double v[4];
 };
-template <int YDIR, bool LOOP>
+template <int YDIR>
 static __device__ __noinline__ Side4 weno4_side_hw(Eigen2D<double> E, const double* s, int64_t P,
                                                    int64_t step, double weps, int side) {
   Side4 r;
-  weno4_side<YDIR, LOOP>(E, s, P, step, weps, side, DivHw(), r.v);
+  weno4_side<YDIR>(E, s, P, step, weps, side, DivHw(), r.v);
   return r;
 }
-template <int YDIR, bool LOOP>
+template <int YDIR>
 __device__ __forceinline__ void side_flux(const Eigen2D<double>& E, const double* s, int64_t P,
                                           int64_t step, double weps, int side, double out[4]) {
   int bad = 0;
-  weno4_side<YDIR, LOOP>(E, s, P, step, weps, side, DivFlag{&bad}, out);
+  weno4_side<YDIR>(E, s, P, step, weps, side, DivFlag{&bad}, out);
   if (bad) {
-    const Side4 r = weno4_side_hw<YDIR, LOOP>(E, s, P, step, weps, side);
+    const Side4 r = weno4_side_hw<YDIR>(E, s, P, step, weps, side);
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = r.v[k];
   }
 }
 
 // 16 interfaces of chunk c (x chunks first, then y chunks), two lanes each
-template <bool LOOP>
 __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* __restrict__ split,
                                                 const double* __restrict__ roe, double am,
                                                 double* __restrict__ flux, int64_t c,
@@ -1278,7 +1223,7 @@ __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* _
     roe_eigen2d<double>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
                         ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
                         ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
-    side_flux<0, LOOP>(E, split + 4 * side * S + o - 2, S, 1, weps, side, o4);
+    side_flux<0>(E, split + 4 * side * S + o - 2, S, 1, weps, side, o4);
 #pragma unroll
     for (int k = 0; k < 4; ++k) flux[(4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
   } else {
@@ -1291,14 +1236,14 @@ __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* _
     roe_eigen2d<double>(g1, 1, ldt(rr + o), ldt(rr + o + pit), ldt(rr + P + o),
                         ldt(rr + P + o + pit), ldt(rr + 2 * P + o), ldt(rr + 2 * P + o + pit),
                         ldt(rr + 3 * P + o), ldt(rr + 3 * P + o + pit), E);
-    side_flux<1, LOOP>(E, split + (8 + 4 * side) * S + o - 2 * spit, S, spit, weps, side, o4);
+    side_flux<1>(E, split + (8 + 4 * side) * S + o - 2 * spit, S, spit, weps, side, o4);
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       flux[(8 + 4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
   }
 }
 
-template <int MINB, bool LOOP = false>
+template <int MINB>
 __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
     k_flux_xy_pair(Params p, const double* __restrict__ split, const double* __restrict__ roe,
                    const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
@@ -1311,7 +1256,7 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
     if (lane == 0) c = atomicAdd(work, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= chunks) break;
-    flux_chunk_pair<LOOP>(p, split, roe, am, flux, c, chunks_x, lane);
+    flux_chunk_pair(p, split, roe, am, flux, c, chunks_x, lane);
   }
   if (lane == 0) {  // as k_flux_xy: the last warp out re-arms both counters
     __threadfence();
@@ -1322,15 +1267,14 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
   }
 }
 
-template <int MINB, bool LOOP = false>
+template <int MINB>
 static int flux_grid_pair() {
   static int grid = 0;
   if (!grid) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy_pair<MINB, LOOP>,
-                                                  SWFD_FLUX_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy_pair<MINB>, SWFD_FLUX_BLOCK, 0);
     grid = sms * (per > 0 ? per : 1);
   }
   return grid;
@@ -1364,9 +1308,7 @@ int flux_min_blocks_candidates(bool f32, int* out) {
   // default 4 first) and the one-lane kernel (3, 2, 4 blocks per SM)
   out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_PAIR + 3, out[2] = SWFD_FLUX_PAIR + 5;
   out[3] = SWFD_FLUX_PAIR + 6, out[4] = 3, out[5] = 2, out[6] = 4;
-  out[7] = SWFD_FLUX_PAIR_LOOP + 4, out[8] = SWFD_FLUX_PAIR_LOOP + 5;
-  out[9] = SWFD_FLUX_PAIR_LOOP + 6;
-  return 10;
+  return 7;
 }
 
 template <class T, int MINB>
@@ -1417,16 +1359,6 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       SWFD_PAIR_CASE(5)
       SWFD_PAIR_CASE(6)
 #undef SWFD_PAIR_CASE
-#define SWFD_PAIR_LOOP_CASE(M)                                                           \
-  if (minb == SWFD_FLUX_PAIR_LOOP + M) {                                                 \
-    k_flux_xy_pair<M, true><<<flux_grid_pair<M, true>(), SWFD_FLUX_BLOCK, 0, s>>>(       \
-        p, sp, rp, dsc, fp, work);                                                       \
-    return;                                                                              \
-  }
-      SWFD_PAIR_LOOP_CASE(4)
-      SWFD_PAIR_LOOP_CASE(5)
-      SWFD_PAIR_LOOP_CASE(6)
-#undef SWFD_PAIR_LOOP_CASE
     } else {
       if (minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
       if (minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
