@@ -619,10 +619,9 @@ __global__ void k_prep2d(Params p, const double* __restrict__ u, const DevScalar
 }
 
 template <class T>
-__global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalars* dsc,
-                         T* __restrict__ split) {
+__device__ __forceinline__ void prep1d_cell(const Params& p, const double* __restrict__ u,
+                                            double amd, T* __restrict__ split, int t) {
   const Geom& g = p.g;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.LI) return;
   const int64_t o = t, P = g.plane;
   const double g1 = p.gamma1;
@@ -634,12 +633,18 @@ __global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalar
   double pres = g1 * (e - 0.5 * rho * (vx * vx));
   double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
   double a[3] = {rho, mx, e};
-  const T am = T(dsc->alphamax);
+  const T am = T(amd);
   for (int c = 0; c < 3; ++c) {
     T q = T(f[c]) / am;
     split[c * P + o] = T(0.5) * (T(a[c]) + q);
     split[(3 + c) * P + o] = T(0.5) * (T(a[c]) - q);
   }
+}
+
+template <class T>
+__global__ void k_prep1d(Params p, const double* __restrict__ u, const DevScalars* dsc,
+                         T* __restrict__ split) {
+  prep1d_cell<T>(p, u, dsc->alphamax, split, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc, void* split,
@@ -857,8 +862,9 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
 // 1D: eigenvectors at cell m (ex2_sedov_1d/main.f90:89-157); vxm and hm come
 // from the FP64 state (pressure recovery), the rest is in T
 template <class T, bool QD = false>
-__global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
-                         T* __restrict__ flux) {
+__device__ __forceinline__ void flux1d_lane(const Params& p, const double* __restrict__ u,
+                                            const T* __restrict__ split, T* __restrict__ flux,
+                                            int t) {
   // eight lanes per cell: lanes 0..5 of a group each reconstruct one
   // characteristic field (k = lane / 2) of one side (lane % 2: the positive
   // flux at the right face, the negative one), so that the six WENO chains of
@@ -867,8 +873,9 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
   // these dependent chains); the group then exchanges the six values and
   // lanes 0..5 form the six output components.  Every value is computed by
   // the same expression as in a one-thread-per-cell form.
+  // t: the lane's index; lanes 8m..8m+7 are lanes of one warp (the group's
+  // shuffles), and every lane of the warp takes part
   const Geom& g = p.g;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = t >> 3, sub = t & 7;  // cell 0..n+1, lane in its group
   const bool active = m <= g.nx + 1;
   const int mm = active ? m : g.nx + 1;  // inactive lanes repeat the last cell
@@ -923,6 +930,12 @@ __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __rest
     case 5: flux[5 * P + o] = r20 * ul0 + qm * ul1 + r22 * ul2; break;
     default: break;
   }
+}
+
+template <class T, bool QD = false>
+__global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
+                         T* __restrict__ flux) {
+  flux1d_lane<T, QD>(p, u, split, flux, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Both directions in one persistent launch: a grid of exactly the resident
@@ -1573,12 +1586,13 @@ __global__ void k_rk(Params p, int stage, const double* __restrict__ u, const do
 // 1D: four lanes per cell, lane c < 3 forming component c (its RHS and RK
 // combination are a chain of their own), lane 0 testing the cell's
 // positivity from the three new values; the expressions are rk_cell's.
+// lane t (every lane of its warp takes part: the group's shuffles); returns
+// the positivity flag of lane 0 of an interior cell's group
 template <class T>
-__global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const double* u0,
-                       const T* __restrict__ flux, DevScalars* dsc, double* out,
-                       cudaGraphConditionalHandle hs, int decide) {
+__device__ __forceinline__ int rk1d_lane(const Params& p, int stage, const double* __restrict__ u,
+                                         const double* u0, const T* __restrict__ flux, double dt,
+                                         double amd, double* out, int64_t t) {
   const Geom& g = p.g;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int cell = (int)(t >> 2), c = (int)(t & 3);
   const bool in_grid = cell < g.LI;
   const int i = cell - 2;
@@ -1586,9 +1600,8 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
   const int64_t P = g.plane, o = in_grid ? g.at(i, -2) : 0;
   double v = 0.0;
   if (in_grid && c < 3) {
-    const double dt = dsc->dt;
     double r = 0.0;
-    if (interior) r = tod(rhs1d<T>(p, flux, c, o, dsc->alphamax));
+    if (interior) r = tod(rhs1d<T>(p, flux, c, o, amd));
     if (sizeof(T) == 4) {
       v = fma(dt, r, ld(u + c * P + o));
       if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
@@ -1610,6 +1623,15 @@ __global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const 
     if (p.pos_strict) bad = (n0 < p.eps) || (pe < p.eps);
     else bad = (n0 <= p.eps) || (pe <= p.eps);
   }
+  return bad;
+}
+
+template <class T>
+__global__ void k_rk1d(Params p, int stage, const double* __restrict__ u, const double* u0,
+                       const T* __restrict__ flux, DevScalars* dsc, double* out,
+                       cudaGraphConditionalHandle hs, int decide) {
+  const int bad = rk1d_lane<T>(p, stage, u, u0, flux, dsc->dt, dsc->alphamax, out,
+                               (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   rk_block_done(dsc, bad, stage, hs, decide);
 }
 
