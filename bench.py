@@ -1018,15 +1018,13 @@ def main():
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        solver.set_state(hu)
-        solver.step()
-        solver.state(out=hu)
+        solver.step_host(hu)  # upload, step, download: one synchronisation
     e2e_s = time.perf_counter() - t0
     _, e2e_s, e2e_value = aggregate(cells * 3 * args.e2e_steps, e2e_s)
     state_bytes = int(np.prod(solver.shape)) * 8
     e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
-           "steps": args.e2e_steps}
+           "steps": args.e2e_steps, "call": "swfd_step_host (pinned host state in and out)"}
 
     # dominant kernel: the WENO flux kernel (one launch per stage, both directions)
     peaks = {}

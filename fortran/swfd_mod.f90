@@ -167,6 +167,16 @@ module swfd_mod
       real(c_double) :: dt
     end function
 
+    ! CALL rk on the host's own u, in and out, with one synchronisation
+    integer(c_int32_t) function swfd_step_host(h, u_in, u_out, dt) &
+        bind(C, name="swfd_step_host")
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double) :: u_in(*)
+      real(c_double) :: u_out(*)
+      real(c_double) :: dt
+    end function
+
     ! DO WHILE (time <= time_terminal - 1d-10)
     integer(c_int32_t) function swfd_run(h, max_steps, nsteps) bind(C, name="swfd_run")
       import :: c_int32_t, c_int64_t, c_ptr

@@ -188,6 +188,13 @@ swfd_status swfd_flux_divergence(swfd_handle* h, double* rhs);
  * `time = time + dt` (:53).  dt_out may be NULL. */
 swfd_status swfd_step(swfd_handle* h, double* dt_out);
 
+/* One step from a host state to a host state (a host that keeps its state
+ * u(ncomp,-2:nx+3,-2:ny+3) between steps, as the reference's time loop
+ * does, ex3_vortex_accuracy_2d/main.f90:51-56): upload u_in, swfd_step,
+ * download into u_out, with one synchronisation at the end.  u_in may equal
+ * u_out.  dt_out may be NULL. */
+swfd_status swfd_step_host(swfd_handle* h, const double* u_in, double* u_out, double* dt_out);
+
 /* The time loop DO WHILE (time <= time_terminal - 1d-10)
  * (ex3_vortex_accuracy_2d/main.f90:51-56), bounded by max_steps (<= 0: none).
  * nsteps_out may be NULL. */

@@ -115,6 +115,7 @@ _SIGS = {
     "swfd_download_state": (C.c_int32, [_P, _DP]),
     "swfd_flux_divergence": (C.c_int32, [_P, _DP]),
     "swfd_step": (C.c_int32, [_P, _DP]),
+    "swfd_step_host": (C.c_int32, [_P, _DP, _DP, _DP]),
     "swfd_run": (C.c_int32, [_P, C.c_int64, C.POINTER(C.c_int64)]),
     "swfd_sweep": (C.c_int32, [_P]),
     "swfd_check_positivity": (C.c_int32, [_P, C.POINTER(C.c_int32)]),

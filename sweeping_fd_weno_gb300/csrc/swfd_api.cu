@@ -1189,20 +1189,9 @@ swfd_status matlab1d_steps(swfd_handle* h, long long max_steps, int64_t* steps_o
   return st;
 }
 
-swfd_status swfd_step(swfd_handle* h, double* dt_out) {
-  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
-  SETTLE(h);
-  if (h->ex7) return ex7_step(h, dt_out);
-  CU(h, cudaSetDevice(h->device));
-  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
-    swfd_status st = matlab1d_steps(h, 1, nullptr);
-    if (dt_out) *dt_out = h->hsc->dt;
-    return st;
-  }
-  ST(build_graph(h, GRAPH_STEP, &h->g_step));
-  ST(ensure_tracks(h, 3));
-  DevScalars before = *h->hsc;
-  ST(launch_kind(h, GRAPH_STEP, h->g_step));
+// after a step's graph: the one synchronisation (scalars and device
+// errors), launch accounting, the flux timings with profiling on, dt
+swfd_status step_done(swfd_handle* h, const DevScalars& before, double* dt_out) {
   swfd_status st = check_device_error(h);
   account(h, before, *h->hsc, 1, 0);
   if (h->prof_on && h->cfg.rk_choice != 2) {  // the restart RK records no flux events
@@ -1215,6 +1204,50 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   }
   if (dt_out) *dt_out = h->hsc->dt;
   return st;
+}
+
+swfd_status swfd_step(swfd_handle* h, double* dt_out) {
+  if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);
+  if (h->ex7) return ex7_step(h, dt_out);
+  CU(h, cudaSetDevice(h->device));
+  if (h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
+    swfd_status st = matlab1d_steps(h, 1, nullptr);
+    if (dt_out) *dt_out = h->hsc->dt;
+    return st;
+  }
+  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  // the host mirror holds the scalars of the last step (no step is pending):
+  // the track arrays grow, with a synchronisation, only when a step's three
+  // sweeps could overflow them
+  if (h->hsc->sweep_count + 3 > h->track_cap) ST(ensure_tracks(h, 3));
+  DevScalars before = *h->hsc;
+  ST(launch_kind(h, GRAPH_STEP, h->g_step));
+  return step_done(h, before, dt_out);
+}
+
+/* One step from a host state to a host state: the upload, the step graph and
+ * the download on the handle's stream with one synchronisation at the end
+ * (what swfd_upload_state, swfd_step and swfd_download_state do with three). */
+swfd_status swfd_step_host(swfd_handle* h, const double* u_in, double* u_out, double* dt_out) {
+  if (!h || !u_in || !u_out) return fail(h, SWFD_ERR_INVALID, "NULL argument");
+  SETTLE(h);
+  if (h->ex7 || h->eager || h->cfg.problem == SWFD_PROBLEM_MATLAB_1D) {
+    ST(swfd_upload_state(h, u_in));
+    ST(swfd_step(h, dt_out));
+    return swfd_download_state(h, u_out);
+  }
+  CU(h, cudaSetDevice(h->device));
+  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  if (h->hsc->sweep_count + 3 > h->track_cap) ST(ensure_tracks(h, 3));
+  const size_t hb = (size_t)host_len(h->p) * sizeof(double);
+  CU(h, cudaMemcpyAsync(h->d_stage, u_in, hb, cudaMemcpyHostToDevice, h->stream));
+  CU(h, launch_fortran_to_soa(h->p, h->d_stage, cur_state(h), h->stream));
+  DevScalars before = *h->hsc;
+  CU(h, cudaGraphLaunch(h->g_step, h->stream));
+  CU(h, launch_soa_to_fortran(h->p, cur_state(h), h->d_stage, h->stream));
+  CU(h, cudaMemcpyAsync(u_out, h->d_stage, hb, cudaMemcpyDeviceToHost, h->stream));
+  return step_done(h, before, dt_out);
 }
 
 swfd_status swfd_step_async(swfd_handle* h) {

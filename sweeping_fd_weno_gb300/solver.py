@@ -88,6 +88,18 @@ class Solver:
         self._chk(self.lib.swfd_step(self.h, C.byref(dt)))
         return dt.value
 
+    def step_host(self, u_in: np.ndarray, u_out: np.ndarray | None = None) -> float:
+        """One step from a host state to a host state (upload, step, download,
+        one synchronisation); u_out may be u_in.  Returns dt."""
+        assert u_in.shape == self.shape and u_in.dtype == np.float64 and u_in.flags["C_CONTIGUOUS"]
+        if u_out is None:
+            u_out = u_in
+        assert u_out.shape == self.shape and u_out.dtype == np.float64 and \
+            u_out.flags["C_CONTIGUOUS"]
+        dt = C.c_double()
+        self._chk(self.lib.swfd_step_host(self.h, abi.dptr(u_in), abi.dptr(u_out), C.byref(dt)))
+        return dt.value
+
     def step_async(self):
         """Enqueue one step on the solver's stream without waiting; finish()
         (or any other call) waits for it and reports its status."""

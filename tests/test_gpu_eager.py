@@ -11,6 +11,9 @@ CASES = [
     ("sedov2d", dict(problem=abi.SEDOV_2D, nx=64, ny=64), 6),
     ("sedov1d", dict(problem=abi.SEDOV_1D, nx=800, cfl=0.6, swp_num=2, e_background=1e-12), 8),
     ("jet", dict(problem=abi.JET_2D, nx=96, ny=24), 4),
+    ("vortex_fp32_fused", dict(problem=abi.VORTEX_2D, nx=64, ny=48,
+                               precision=abi.PRECISION_FP32_BULK), 6),
+    ("detonation", dict(problem=abi.DETONATION, total=8, cut_x=2, cut_y=2), 6),
 ]
 
 
