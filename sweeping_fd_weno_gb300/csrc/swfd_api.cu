@@ -1007,6 +1007,10 @@ swfd_status swfd_create(const swfd_config* cfg, swfd_handle** out) {
     const char* lm = getenv("SWFD_LAUNCH");
     h->eager = lm && strcmp(lm, "eager") == 0;
   }
+  if (const char* hb = getenv("SWFD_HEAVY_BLOCK")) {  // 32..1024: the splitting's and RK's block
+    const int v = atoi(hb);
+    if (v >= 32 && v <= 1024 && (v & (v - 1)) == 0) h->p.heavy_block = v;
+  }
   {  // the fused FP32-bulk stage where it applies (SWFD_FP32_STAGE=split: the
      // separate splitting, flux and RK kernels, the same bits)
     const Params& q = h->p;

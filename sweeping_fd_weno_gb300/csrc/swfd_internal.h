@@ -68,6 +68,9 @@ struct Params {
   int limiter = 0;       // use_limiter = 1: the positivity flux limiter in wenofd
   int limiter_clamp = 0; // ex6 clamps its theta at 0 (theta = max(theta, 0.))
   int flux_minb = 0;     // flux kernel launch shape chosen by swfd_autotune (0: default)
+  // largest block of the splitting and RK kernels (~70 registers a thread):
+  // 128 puts a 360^2 grid's cells in one wave of resident blocks
+  int heavy_block = 128;
   // Shock diffraction (ex6_shock_diffraction/main.f90).  The reference's
   // rank grid cut_x x cut_y (ranks of nxl x nyl cells) is part of its
   // arithmetic: the x pass of row j uses the max alpha over the cells of

@@ -246,7 +246,7 @@ __global__ void k_bc2d_alpha(Params p, double* __restrict__ u, DevScalars* dsc) 
 // on grids too small to give every SM two blocks, so that the FP64 work of a
 // small grid (2 FP64 instructions per clock per SM) spreads over the SMs.
 // The per-cell results do not depend on it.
-static int cell_block(int64_t cells) {
+static int cell_block(int64_t cells, int bmax = SWFD_BLOCK) {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -254,7 +254,7 @@ static int cell_block(int64_t cells) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  int b = SWFD_BLOCK;
+  int b = bmax > 0 ? bmax : SWFD_BLOCK;
   while (b > 32 && (cells + b - 1) / b < 2 * sms) b >>= 1;
   return b;
 }
@@ -656,7 +656,7 @@ cudaError_t launch_prep(const Params& p, const double* u, const DevScalars* dsc,
     else k_prep1d<double><<<gb, b, 0, s>>>(p, u, dsc, (double*)split);
   } else {
     int64_t n = (int64_t)p.g.LI * p.g.LJ;
-    const int b = cell_block(n);
+    const int b = cell_block(n, p.heavy_block);
     const unsigned gb = (unsigned)((n + b - 1) / b);
     if (f32) k_prep2d<float><<<gb, b, 0, s>>>(p, u, dsc, (float*)split, (float*)roe, which);
     else k_prep2d<double><<<gb, b, 0, s>>>(p, u, dsc, (double*)split, (double*)roe, which);
@@ -1507,7 +1507,9 @@ __device__ __forceinline__ double rk_combine(const Params& p, int stage, double 
   return tdiv(u0 + tscale<1>(v), 3.0);
 }
 
-template <class T>
+// NC: the components as a compile-time count (4 in 2D, 3 in 1D), so that
+// the components' chains are unrolled side by side and nv stays in registers
+template <class T, int NC = 4>
 __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double* __restrict__ u,
                                        const double* u0, const T* __restrict__ flux, double dt,
                                        double am, double* out, int64_t t) {
@@ -1517,13 +1519,13 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
   if (t < ncell) {
     int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
     const int64_t o = g.at(i, j), P = g.plane;
-    bool interior = (i >= 1 && i <= g.nx) && (g.ndim == 1 || (j >= 1 && j <= g.ny));
+    bool interior = (i >= 1 && i <= g.nx) && (NC == 3 || (j >= 1 && j <= g.ny));
     double nv[4];
-    for (int c = 0; c < g.nc; ++c) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
       double r = 0.0;
       if (interior)
-        r = tod((g.ndim == 1) ? rhs1d<T>(p, flux, c, o, am)
-                                   : rhs2d_cell<T>(p, flux, c, i, j, am));
+        r = tod((NC == 3) ? rhs1d<T>(p, flux, c, o, am) : rhs2d_cell<T>(p, flux, c, i, j, am));
       double v;
       if (sizeof(T) == 4) {  // FP32-bulk: the FP64 accumulation with fused multiply-adds
         v = rk32_value(stage, dt, r, ld(u + c * P + o), u0 + c * P + o);
@@ -1538,11 +1540,11 @@ __device__ __forceinline__ int rk_cell(const Params& p, int stage, const double*
       // checkpositivity (ex3_vortex_accuracy_2d/main.f90:640-647,
       // ex2_sedov_1d/main.f90:381-387; `<` in ex4/ex5)
       double pe;
-      if (sizeof(T) == 4 && g.ndim == 2) return pos32_bad(p, nv);
+      if (sizeof(T) == 4 && NC == 4) return pos32_bad(p, nv);
       if (sizeof(T) == 4) {  // FP32-bulk: FP64 with one reciprocal
         const double ri = -0.5 * rcp_bulk(nv[0]);
         pe = fma(nv[1] * nv[1], ri, nv[2]);
-      } else if (g.ndim == 1) {
+      } else if (NC == 3) {
         pe = nv[2] - tscale<-1>(tdiv(nv[1] * nv[1], nv[0]));
       } else {
         pe = nv[3] - tscale<-1>(tdiv(nv[2] * nv[2], nv[0])) - tscale<-1>(tdiv(nv[1] * nv[1], nv[0]));
@@ -1651,7 +1653,7 @@ cudaError_t launch_rk(const Params& p, int stage, const double* u, const double*
                                       const_cast<DevScalars*>(dsc), out, hs, decide);
     return cudaGetLastError();
   }
-  const int b = cell_block(n);
+  const int b = cell_block(n, p.heavy_block);
   const unsigned gb = (unsigned)((n + b - 1) / b);
   if (p.precision == SWFD_PRECISION_FP32_BULK)
     k_rk<float><<<gb, b, 0, s>>>(p, stage, u, u0, (const float*)flux,
@@ -2241,8 +2243,10 @@ __global__ void kb_rk(const BatchSlot* __restrict__ tab, const long long* __rest
     const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
     int bad = 0;
     for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x)
-      bad |= rk_cell<T>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux, dt, am, sl.st[out],
-                        t);
+      bad |= sl.p.g.ndim == 1 ? rk_cell<T, 3>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux,
+                                             dt, am, sl.st[out], t)
+                              : rk_cell<T, 4>(sl.p, stage, sl.st[in], sl.st[0], (const T*)sl.flux,
+                                             dt, am, sl.st[out], t);
     if (block_or(bad) && threadIdx.x == 0) {
       atomicOr(&d->postag, 1);
       if (sl.use_limiter == 2) atomicOr(&ctl->any_postag, 1);
