@@ -54,12 +54,15 @@ struct swfd_batch {
   std::vector<long long> tprefix;
   long long* d_s32prefix = nullptr;  // the fused FP32-bulk stage's tile + ghost-chunk prefix
   std::vector<long long> s32prefix;
-  bool fused32 = false;            // this run's running slots all take the fused FP32 stage
+  // this run's running slots are all 2D without rank segments, limiter or
+  // binary128 literals: the fast graph (FP32-bulk: the fused stage; FP64: the
+  // lane-pair flux kernel)
+  bool fast = false;
   int tile_cells = 2048;           // cells per tile (swfd_batch_autotune picks it)
   DevScalars* d_dsc = nullptr;  // one DevScalars per slot, contiguous: one read-back per run
   DevScalars* h_dsc = nullptr;  // pinned mirror
   cudaGraphExec_t g_run = nullptr;
-  cudaGraphExec_t g_run32 = nullptr;  // the same loop with the fused FP32-bulk stage
+  cudaGraphExec_t g_fast = nullptr;  // the same loop for such slots only
   double* d_stage = nullptr;
   size_t stage_bytes = 0;
   int64_t pool_bytes = 0, used_bytes = 0;
@@ -116,16 +119,21 @@ BatchLaunch launch_desc(swfd_batch* b) {
   L.fp32 = b->cfg.precision == SWFD_PRECISION_FP32_BULK;
   L.ubar_tree = b->cfg.ubar_mode == SWFD_UBAR_TREE;
   L.segmented = 1;
+  L.pair64 = 0;
   return L;
 }
 
 // WHILE (some slot runs and steps < limit) { stage 1..3 with conditional
-// sweeps and bc; per-slot time advance }; fused: the FP32-bulk fused stage
-swfd_status build_run_graph(swfd_batch* b, bool fused) {
+// sweeps and bc; per-slot time advance }; fast: the graph for slots that are
+// all 2D without rank segments, limiter or binary128 literals (FP32-bulk:
+// the fused stage; FP64: the lane-pair flux kernel)
+swfd_status build_run_graph(swfd_batch* b, bool fast) {
   Builder bd;
   bd.cap = b->cap;
   bd.max_depth = 3;
-  const BatchLaunch L = launch_desc(b);
+  BatchLaunch L = launch_desc(b);
+  const bool fused = fast && L.fp32;
+  L.pair64 = fast && !L.fp32;
   cudaStream_t s = b->cap[0];
   BCU(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   cudaStreamCaptureStatus cs;
@@ -160,7 +168,7 @@ swfd_status build_run_graph(swfd_batch* b, bool fused) {
     return bfail(b, SWFD_ERR_CUDA, std::string("batch graph capture: ") +
                                        cudaGetErrorString(bd.err != cudaSuccess ? bd.err : e2));
   }
-  cudaError_t e3 = cudaGraphInstantiate(fused ? &b->g_run32 : &b->g_run, g, 0);
+  cudaError_t e3 = cudaGraphInstantiate(fast ? &b->g_fast : &b->g_run, g, 0);
   cudaGraphDestroy(g);
   if (e3 != cudaSuccess)
     return bfail(b, SWFD_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e3));
@@ -283,7 +291,7 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   b->pool_bytes = cfg->pool_bytes > 0 ? cfg->pool_bytes : (int64_t)(0.8 * (double)fr);
   const bool f32 = cfg->precision == SWFD_PRECISION_FP32_BULK;
   if (f32 && (e = stage32_setup()) != cudaSuccess) return bad(e);
-  if (build_run_graph(b, false) != SWFD_OK || (f32 && build_run_graph(b, true) != SWFD_OK)) {
+  if (build_run_graph(b, false) != SWFD_OK || build_run_graph(b, true) != SWFD_OK) {
     std::string m = b->last_error;
     swfd_batch_destroy(b);
     return bfail(nullptr, SWFD_ERR_CUDA, m);
@@ -301,7 +309,7 @@ swfd_status swfd_batch_destroy(swfd_batch* b) {
     cudaFree(sh.tracks);
   }
   if (b->g_run) cudaGraphExecDestroy(b->g_run);
-  if (b->g_run32) cudaGraphExecDestroy(b->g_run32);
+  if (b->g_fast) cudaGraphExecDestroy(b->g_fast);
   cudaFree(b->d_tab);
   cudaFree(b->d_ctl);
   cudaFree(b->d_prefix);
@@ -430,10 +438,12 @@ swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
   const int n = b->cfg.max_slots;
   int running = 0;
   long long chunks = 0, tiles = 0, items = 0;
-  // the fused FP32-bulk stage when every running slot takes it (2D, no rank
-  // segments, no limiter) and SWFD_FP32_STAGE is not "split"
+  // the fast graph when every running slot takes it (2D, no rank segments,
+  // no limiter, binary64 literals); SWFD_FP32_STAGE=split keeps an FP32-bulk
+  // batch on the separate kernels
   const char* fs = getenv("SWFD_FP32_STAGE");
-  bool fused = b->g_run32 != nullptr && !(fs && strcmp(fs, "split") == 0);
+  bool fused = b->g_fast != nullptr &&
+               !(b->cfg.precision == SWFD_PRECISION_FP32_BULK && fs && strcmp(fs, "split") == 0);
   for (int k = 0; k < n; ++k) {
     b->prefix[k] = chunks;
     b->tprefix[k] = tiles;
@@ -450,7 +460,7 @@ swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
   b->prefix[n] = chunks;
   b->tprefix[n] = tiles;
   b->s32prefix[n] = items;
-  b->fused32 = fused;
+  b->fast = fused;
   BCU(b, cudaMemcpyAsync(b->d_s32prefix, b->s32prefix.data(), (n + 1) * sizeof(long long),
                          cudaMemcpyHostToDevice, b->stream));
   BCU(b, cudaMemcpyAsync(b->d_prefix, b->prefix.data(), (n + 1) * sizeof(long long),
@@ -530,7 +540,7 @@ swfd_status swfd_batch_run(swfd_batch* b, int64_t max_steps, int64_t* steps_out)
     swfd_status st = upload_plan(b, max_steps);
     if (st != SWFD_OK) return st;
   }
-  BCU(b, cudaGraphLaunch(b->fused32 ? b->g_run32 : b->g_run, b->stream));
+  BCU(b, cudaGraphLaunch(b->fast ? b->g_fast : b->g_run, b->stream));
   BCU(b, cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, b->stream));
   BCU(b, cudaMemcpyAsync(b->tab.data(), b->d_tab, n * sizeof(BatchSlot), cudaMemcpyDeviceToHost,
                          b->stream));
