@@ -54,15 +54,14 @@ struct swfd_batch {
   std::vector<long long> tprefix;
   long long* d_s32prefix = nullptr;  // the fused FP32-bulk stage's tile + ghost-chunk prefix
   std::vector<long long> s32prefix;
-  // this run's running slots are all 2D without rank segments, limiter or
-  // binary128 literals: the fast graph (FP32-bulk: the fused stage; FP64: the
-  // lane-pair flux kernel)
+  // FP32-bulk: this run's running slots are all 2D without rank segments,
+  // limiter or binary128 literals: the graph with the fused stage
   bool fast = false;
   int tile_cells = 2048;           // cells per tile (swfd_batch_autotune picks it)
   DevScalars* d_dsc = nullptr;  // one DevScalars per slot, contiguous: one read-back per run
   DevScalars* h_dsc = nullptr;  // pinned mirror
   cudaGraphExec_t g_run = nullptr;
-  cudaGraphExec_t g_fast = nullptr;  // the same loop for such slots only
+  cudaGraphExec_t g_fast = nullptr;  // the same loop with the fused FP32-bulk stage
   double* d_stage = nullptr;
   size_t stage_bytes = 0;
   int64_t pool_bytes = 0, used_bytes = 0;
@@ -119,21 +118,21 @@ BatchLaunch launch_desc(swfd_batch* b) {
   L.fp32 = b->cfg.precision == SWFD_PRECISION_FP32_BULK;
   L.ubar_tree = b->cfg.ubar_mode == SWFD_UBAR_TREE;
   L.segmented = 1;
-  L.pair64 = 0;
   return L;
 }
 
 // WHILE (some slot runs and steps < limit) { stage 1..3 with conditional
-// sweeps and bc; per-slot time advance }; fast: the graph for slots that are
-// all 2D without rank segments, limiter or binary128 literals (FP32-bulk:
-// the fused stage; FP64: the lane-pair flux kernel)
+// sweeps and bc; per-slot time advance }; fast: the FP32-bulk fused stage
+// (for slots that are all 2D without rank segments, limiter or binary128
+// literals).  An FP64 form of the fast graph with the lane-pair flux kernel
+// was measured slower than kb_flux<double> here (2.21e8 against 2.52e8
+// cell-updates/s on the 256-instance mix) and is not built.
 swfd_status build_run_graph(swfd_batch* b, bool fast) {
   Builder bd;
   bd.cap = b->cap;
   bd.max_depth = 3;
-  BatchLaunch L = launch_desc(b);
-  const bool fused = fast && L.fp32;
-  L.pair64 = fast && !L.fp32;
+  const BatchLaunch L = launch_desc(b);
+  const bool fused = fast;
   cudaStream_t s = b->cap[0];
   BCU(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   cudaStreamCaptureStatus cs;
@@ -291,7 +290,7 @@ swfd_status swfd_batch_create(const swfd_batch_config* cfg, swfd_batch** out) {
   b->pool_bytes = cfg->pool_bytes > 0 ? cfg->pool_bytes : (int64_t)(0.8 * (double)fr);
   const bool f32 = cfg->precision == SWFD_PRECISION_FP32_BULK;
   if (f32 && (e = stage32_setup()) != cudaSuccess) return bad(e);
-  if (build_run_graph(b, false) != SWFD_OK || build_run_graph(b, true) != SWFD_OK) {
+  if (build_run_graph(b, false) != SWFD_OK || (f32 && build_run_graph(b, true) != SWFD_OK)) {
     std::string m = b->last_error;
     swfd_batch_destroy(b);
     return bfail(nullptr, SWFD_ERR_CUDA, m);
@@ -438,12 +437,11 @@ swfd_status upload_plan(swfd_batch* b, int64_t max_steps) {
   const int n = b->cfg.max_slots;
   int running = 0;
   long long chunks = 0, tiles = 0, items = 0;
-  // the fast graph when every running slot takes it (2D, no rank segments,
-  // no limiter, binary64 literals); SWFD_FP32_STAGE=split keeps an FP32-bulk
-  // batch on the separate kernels
+  // the fused FP32-bulk stage when every running slot takes it (2D, no rank
+  // segments, no limiter, binary64 literals) and SWFD_FP32_STAGE is not
+  // "split"
   const char* fs = getenv("SWFD_FP32_STAGE");
-  bool fused = b->g_fast != nullptr &&
-               !(b->cfg.precision == SWFD_PRECISION_FP32_BULK && fs && strcmp(fs, "split") == 0);
+  bool fused = b->g_fast != nullptr && !(fs && strcmp(fs, "split") == 0);
   for (int k = 0; k < n; ++k) {
     b->prefix[k] = chunks;
     b->tprefix[k] = tiles;

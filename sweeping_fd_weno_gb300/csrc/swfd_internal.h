@@ -232,7 +232,6 @@ struct BatchLaunch {
   int fp32;
   int ubar_tree;
   int segmented;            // slots may hold rank-segmented problems (ex6)
-  int pair64;               // FP64: every running slot takes the lane-pair flux kernel
 };
 
 }  // namespace swfd

@@ -1216,44 +1216,7 @@ __device__ __forceinline__ void side_flux(const Eigen2D<double>& E, const double
   }
 }
 
-// interface t of direction ydir (x: faces i = 0..nx+1 of rows 1..ny; y: faces
-// j = 0..ny+1 of columns 1..nx), side `side` (lane & 1 of its pair)
-__device__ __forceinline__ void flux_pair_face(const Params& p, const double* __restrict__ split,
-                                               const double* __restrict__ roe, double am,
-                                               double* __restrict__ flux, int ydir, int64_t t,
-                                               int side) {
-  const Geom& g = p.g;
-  const int64_t P = g.plane, pit = g.pitch, S = p.sg.plane, spit = p.sg.pitch;
-  const double g1 = p.gamma1, weps = p.weno_eps;
-  double o4[4];
-  if (!ydir) {
-    const int lx = p.nxl + 2;  // faces i = 0..nx+1 of rows 1..ny (one segment)
-    const int i = (int)t % lx, j = (int)t / lx + 1;
-    const int64_t o = g.at(i, j);
-    Eigen2D<double> E;
-    roe_eigen2d<double>(g1, 0, ldt(roe + o), ldt(roe + o + 1), ldt(roe + P + o),
-                        ldt(roe + P + o + 1), ldt(roe + 2 * P + o), ldt(roe + 2 * P + o + 1),
-                        ldt(roe + 3 * P + o), ldt(roe + 3 * P + o + 1), E);
-    side_flux<0>(E, split + 4 * side * S + o - 2, S, 1, weps, side, o4);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) flux[(4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
-  } else {
-    const int i = (int)t % g.nx + 1, j = (int)t / g.nx;
-    const int64_t o = g.at(i, j);
-    const double* rr = roe + (p.roe_reg_ex4 ? 4 * P : 0);
-    Eigen2D<double> E;
-    roe_eigen2d<double>(g1, 1, ldt(rr + o), ldt(rr + o + pit), ldt(rr + P + o),
-                        ldt(rr + P + o + pit), ldt(rr + 2 * P + o), ldt(rr + 2 * P + o + pit),
-                        ldt(rr + 3 * P + o), ldt(rr + 3 * P + o + pit), E);
-    side_flux<1>(E, split + (8 + 4 * side) * S + o - 2 * spit, S, spit, weps, side, o4);
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      flux[(8 + 4 * side + k) * S + o] = p.alpha_premul ? am * o4[k] : o4[k];
-  }
-}
-
 // 16 interfaces of chunk c (x chunks first, then y chunks), two lanes each
-// (flux_pair_face's work, with each direction's index setup in its branch)
 __device__ __forceinline__ void flux_chunk_pair(const Params& p, const double* __restrict__ split,
                                                 const double* __restrict__ roe, double am,
                                                 double* __restrict__ flux, int64_t c,
@@ -2266,54 +2229,6 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, SWFD_FLUX_MINB(T))
   }
 }
 
-// FP64 batches whose running slots all take the lane-pair kernel (2D, no
-// rank segments, no limiter, binary64 literals): kb_flux's 32-interface
-// chunks, each as two halves of 16 interfaces with two lanes per interface
-__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, 4)
-    kb_flux_pair(const BatchSlot* __restrict__ tab, const long long* __restrict__ prefix, int n,
-                 BatchCtl* ctl) {
-  const int lane = threadIdx.x & 31;
-  const long long total = ctl->total_chunks;
-  for (;;) {
-    int c = 0;
-    if (lane == 0) c = atomicAdd(&ctl->flux_work, 1);
-    c = __shfl_sync(0xffffffffu, c, 0);
-    if (c >= total) break;
-    int lo = 0, hi = n - 1;  // last slot with prefix[s] <= c
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (prefix[mid] <= c) lo = mid;
-      else hi = mid - 1;
-    }
-    const BatchSlot& sl = tab[lo];
-    if (!sl.active) continue;
-    const double am = sl.p.alpha_premul ? sl.dsc->alphamax : 1.0;
-    const long long cc = c - prefix[lo];
-    const int ydir = cc < sl.chunks_x ? 0 : 1;
-    const long long base = (ydir ? cc - sl.chunks_x : cc) * 32;
-    const long long faces = ydir ? flux_faces_y(sl.p) : flux_faces_x(sl.p);
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-      const long long t = base + h * 16 + (lane >> 1);
-      if (t < faces)
-        flux_pair_face(sl.p, (const double*)sl.split, (const double*)sl.roe, am,
-                       (double*)sl.flux, ydir, t, lane & 1);
-    }
-  }
-}
-
-static int kb_flux_pair_grid() {
-  static int grid = 0;
-  if (!grid) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_flux_pair, SWFD_FLUX_BLOCK, 0);
-    grid = sms * (per > 0 ? per : 1);
-  }
-  return grid;
-}
-
 template <class T>
 __global__ void kb_rk(const BatchSlot* __restrict__ tab, const long long* __restrict__ tp, int n,
                       BatchCtl* ctl, int stage, int in, int out) {
@@ -2421,10 +2336,7 @@ cudaError_t launch_batch_stage(const BatchLaunch& b, int stage, int in, int out,
       kb_walls<<<dim3(1, n), 256, 0, s>>>(b.tab, in, 1);
       kb_prep<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, in, 2);
     }
-    if (b.pair64)
-      kb_flux_pair<<<kb_flux_pair_grid(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
-    else
-      kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
+    kb_flux<double><<<flux_grid<double>(), SWFD_FLUX_BLOCK, 0, s>>>(b.tab, b.prefix, n, b.ctl);
     kb_rk<double><<<tg, SWFD_BLOCK, 0, s>>>(b.tab, b.tprefix, n, b.ctl, stage, in, out);
   }
   if (h_sweep) kb_cond_any_postag<<<1, 1, 0, s>>>(h_sweep, b.ctl);

@@ -8,7 +8,9 @@
 // The grids are small (the script's problems run 20..801 cells) and a step is
 // a chain of short dependent phases, so one thread block runs whole steps:
 // the cell- and interface-parallel phases are spread over its threads and
-// separated by block barriers, and the sequential sweeps run in thread 0.  A
+// separated by block barriers; the sweeps flag each pass's bad positions over
+// the block and walk the chains from them in thread 0, which also forms the
+// weighted means (left-to-right sums).  A
 // launch advances up to max_steps steps (the time loop `while t < tFinal`,
 // :212, is tested on the device).
 //
@@ -192,6 +194,18 @@ __device__ __forceinline__ double P14(const double* x) {  // the sweep files' ga
   return (1.4 - 1) * (x[2] - 1. / 2. * ((x[1] * x[1]) / x[0]));
 }
 
+// shared memory of the block-cooperative sweep: the flagged positions of a
+// pass (n - 1 <= SW_CAP; larger grids take the thread-0 sweep)
+constexpr int SW_CAP = 4096;
+struct SweepShared {
+  int list[SW_CAP];
+  int cnt;
+  int wcnt[MT / 32];
+  double red[MT / 32];
+  double red_out, pu;
+  double ub[3];
+};
+
 struct Sweep {
   double* uh;
   int n;
@@ -297,6 +311,158 @@ struct Sweep {
       d->tracks[2 * d->track_cap + k] = (int)d->t_pos;
     }
   }
+  // ---- block-cooperative forms (every thread of the block calls them): the
+  // minima and the pass-start flags over the block's threads, the
+  // sequential parts (the weighted sums, the adjustments) in thread 0; the
+  // same values and counts as the thread-0 forms above ----
+  // fmin over the block (NaN is fmin's identity, as in the thread-0 fold)
+  __device__ double block_min(double v, SweepShared& S) const {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) S.red[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = S.red[0];
+      for (int k = 1; k < MT / 32; ++k) m = fmin(m, S.red[k]);
+      S.red_out = m;
+    }
+    __syncthreads();
+    const double r = S.red_out;
+    __syncthreads();
+    return r;
+  }
+  __device__ double rho_min_par(SweepShared& S) const {
+    double v = __longlong_as_double(0x7ff8000000000000ll);
+    for (int i = 1 + threadIdx.x; i <= n; i += MT) v = fmin(v, uh[i - 1]);
+    return block_min(v, S);
+  }
+  __device__ void pressure_data_par(double& pmin, double& pu, SweepShared& S) const {
+    double v = __longlong_as_double(0x7ff8000000000000ll);
+    for (int i = 1 + threadIdx.x; i <= n; i += MT) {
+      double x[3];
+      get(i, x);
+      v = fmin(v, x[2] - 1. / 2. * ((x[1] * x[1]) / x[0]));
+    }
+    if (threadIdx.x == 0) {  // the weighted means, left to right
+      double ra = 0, ma = 0, ea = 0;
+      for (int i = 1; i <= n; ++i) {
+        double x[3];
+        get(i, x);
+        ra = ra + x[0] * w, ma = ma + x[1] * w, ea = ea + x[2] * w;
+      }
+      S.pu = ea - 1. / 2. * ((ma * ma) / ra);
+    }
+    pmin = block_min(v, S);  // its barriers publish S.pu
+    pu = S.pu;
+  }
+  __device__ static bool sweep_bad(const double* v) { return P14(v) <= 1e-12 || v[0] < 0; }
+  // the positions s = 1..n-1 of pass `pass` whose cell is bad on the
+  // pass-start state, in pass order, into S.list[0..S.cnt)
+  __device__ void flag_list(int pass, SweepShared& S) const {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) S.cnt = 0;
+    __syncthreads();
+    for (int base = 1; base <= n - 1; base += MT) {
+      const int s = base + threadIdx.x;
+      bool f = false;
+      if (s <= n - 1) {
+        double v[3];
+        get(pass == 0 ? s : n - s + 1, v);
+        f = sweep_bad(v);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (lane == 0) S.wcnt[wid] = __popc(m);
+      __syncthreads();
+      int off = S.cnt;
+      for (int k = 0; k < wid; ++k) off += S.wcnt[k];
+      if (f) S.list[off + __popc(m & ((1u << lane) - 1u))] = s;
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int k = 0; k < MT / 32; ++k) S.cnt += S.wcnt[k];
+      __syncthreads();
+    }
+  }
+  // one pass from its flagged positions: at a flagged position the cell is
+  // unchanged since the pass start, so it adjusts; each adjustment changes the
+  // next position's cell, which is checked afresh (the chain goes on while it
+  // is bad); a position a chain passed is not visited again -- the visits and
+  // adjustments of the sequential pass
+  __device__ void walk(int pass, const double* ub, const SweepShared& S) {
+    int s_next = 1;
+    for (int k = 0; k < S.cnt; ++k) {
+      int s = S.list[k];
+      if (s < s_next) continue;
+      for (;;) {
+        const int j = pass == 0 ? s : n - s + 1, jp = pass == 0 ? j + 1 : j - 1;
+        double vj[3], vp[3], vjt[3], nv[3];
+        get(j, vj);
+        get(jp, vp);
+        node_adj(vj, vp, ub, vjt);
+        for (int c = 0; c < 3; ++c) nv[c] = vp[c] + (w / w) * (vj[c] - vjt[c]);
+        put(j, vjt);
+        put(jp, nv);
+        if (++s > n - 1) break;
+        double v2[3];
+        get(pass == 0 ? s : n - s + 1, v2);
+        if (!sweep_bad(v2)) break;
+      }
+      s_next = s + 1;
+    }
+  }
+  __device__ void swp_alg_par(int swp_num, SweepShared& S) {
+    const double epsi = 1e-12;
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 3; ++c) {
+        double ub = 0;
+        for (int i = 1; i <= n; ++i) ub = ub + uh[c * n + i - 1] * w;
+        S.ub[c] = ub;
+      }
+      d->sweep_count++;
+      d->t_pos = d->t_neg = 0;
+    }
+    __syncthreads();
+    int q;
+    for (q = 1; q <= swp_num; ++q) {
+      for (int pass = 0; pass < 2; ++pass) {
+        flag_list(pass, S);
+        if (threadIdx.x == 0) walk(pass, S.ub, S);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) d->pre_count++;
+      double pmin, pu;
+      pressure_data_par(pmin, pu, S);
+      const double rmin = rho_min_par(S);
+      if (pmin > epsi && rmin > epsi) break;
+    }
+    if (threadIdx.x == 0) {
+      const long long k = d->sweep_count - 1;
+      if (q > swp_num) {
+        q = swp_num;
+        d->fail_count++;
+      }
+      if (k < d->track_cap) {
+        d->tracks[k] = q;
+        d->tracks[d->track_cap + k] = (int)d->t_neg;
+        d->tracks[2 * d->track_cap + k] = (int)d->t_pos;
+      }
+    }
+    __syncthreads();
+  }
+  // apply_sweep.m, block-cooperative
+  __device__ void apply_par(int swp_num, SweepShared& S) {
+    if (rho_min_par(S) <= 1e-13) {
+      if (threadIdx.x == 0) scalar_pos();
+      __syncthreads();
+    }
+    double pmin, pu;
+    pressure_data_par(pmin, pu, S);
+    if (pmin <= 1e-13 && pu > 0) {
+      if (threadIdx.x == 0) scalar_pos();
+      __syncthreads();
+      pressure_data_par(pmin, pu, S);
+      if (pu > 1e-13) swp_alg_par(swp_num, S);
+    }
+  }
   // apply_sweep.m
   __device__ void apply(int swp_num) {
     if (rho_min() <= 1e-13) scalar_pos();
@@ -316,6 +482,7 @@ __global__ void __launch_bounds__(MT, 1)
   __shared__ double sh[32];
   __shared__ double s_l;
   __shared__ int s_go;
+  __shared__ SweepShared ssw;
   const int n = p.g.nx;
   const int64_t P = p.g.plane;
   const Ctx c{n, per, p.gamma - 1};
@@ -365,9 +532,13 @@ __global__ void __launch_bounds__(MT, 1)
           else o = 1. / 3. * ui + 2. / 3. * (o - dd);
         }
       __syncthreads();
-      if (sweeping && threadIdx.x == 0) {
-        Sweep s{w.uh, n, 1. * 1. / n, d};
-        s.apply(swp_num);
+      if (sweeping) {
+        Sweep sw{w.uh, n, 1. * 1. / n, d};
+        if (n - 1 <= SW_CAP) {
+          sw.apply_par(swp_num, ssw);
+        } else if (threadIdx.x == 0) {
+          sw.apply(swp_num);
+        }
       }
       __syncthreads();
     }
