@@ -19,6 +19,8 @@
 // qd::exp_rd (binary128, rounded once), which the oracle evaluates with the
 // same binary128 operations.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "swfd_device.cuh"
@@ -230,9 +232,8 @@ __global__ void k7_split(Ex7View e, int ydir) {
 // reconstructions, back projection; every product of the eigenvector sums is
 // formed, zeros and ones included, in the reference's order
 template <bool QD>
-__device__ __forceinline__ void e7_interface(const Ex7View& e, int ydir, const double* L,
-                                             const double* Rr, const double (*sp)[5],
-                                             const double (*sn)[5], double* outp, double* outn) {
+__device__ __forceinline__ void e7_eigen(const Ex7View& e, int ydir, const double* L,
+                                         const double* Rr, double (*evl)[5], double (*evr)[5]) {
   const double g1 = e.g1, q = e.q;
   double t0 = QD ? qd::to_double(qd::div(qd::from_double(L[0]),
                                          qd::add(qd::from_double(L[0] + Rr[0]), e.q_1em15)))
@@ -249,7 +250,6 @@ __device__ __forceinline__ void e7_interface(const Ex7View& e, int ydir, const d
   const double rcm = tdiv(1., cm);
   const double b1 = g1 * rcm * rcm;
   const double b2 = qm * b1;
-  double evr[5][5], evl[5][5];
   if (!ydir) {
     t0 = vxm * cm;
     const double er[5][5] = {{1.0, 1.0, 0.0, 0.0, 1.0},
@@ -293,6 +293,14 @@ __device__ __forceinline__ void e7_interface(const Ex7View& e, int ydir, const d
         evl[k][m] = el[k][m];
       }
   }
+}
+
+template <bool QD>
+__device__ __forceinline__ void e7_interface(const Ex7View& e, int ydir, const double* L,
+                                             const double* Rr, const double (*sp)[5],
+                                             const double (*sn)[5], double* outp, double* outn) {
+  double evr[5][5], evl[5][5];
+  e7_eigen<QD>(e, ydir, L, Rr, evl, evr);
   double ur[5], ul[5];
   for (int k = 0; k < 5; ++k) {
     double cp[5], cn[5];

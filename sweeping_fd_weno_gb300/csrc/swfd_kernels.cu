@@ -1134,40 +1134,6 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
 // SM and each has shorter dependent chains, at the price of the eigenvectors
 // computed twice.  Every value is the one-lane form's expression.
 // ---------------------------------------------------------------------------
-// One reconstruction for lane side s as a single instruction stream for both
-// sides: weno_right (s = 0) and weno_left (s = 1) of stencil v0..v4 have the
-// same shape -- three candidates k1*v_a + k2*v_b + k3*v_c over the same
-// positions, the same smoothness indicators, the weights d/(eps+beta)^2
-// normalised by three divisions, and w1*A + w2*B + w3*C -- and differ only in
-// the constants, which each lane selects; so a warp whose lanes take both
-// sides does not diverge, and each side's operations, operands and their
-// order are the reference's (weno5.f90:86-146).
-template <class D>
-__device__ __forceinline__ double weno_side(double v0, double v1, double v2, double v3, double v4,
-                                            int side, double eps, D div) {
-  // weno_right: A = um3 = c13 v2 + c56 v3 + cm16 v4,  B = um2 = cm16 v1 + c56 v2 + c13 v3,
-  //             C = um1 = c13 v0 + cm76 v1 + c116 v2, weights d = 0.3, 0.6, 0.1
-  // weno_left:  A = up3 = c116 v2 + cm76 v3 + c13 v4, B = up2 = c13 v1 + c56 v2 + cm16 v3,
-  //             C = up1 = cm16 v0 + c56 v1 + c13 v2,  weights d = 0.1, 0.6, 0.3
-  const bool l = side != 0;
-  const double a1 = l ? SWFD_C116 : SWFD_C13, a2 = l ? SWFD_CM76 : SWFD_C56,
-               a3 = l ? SWFD_C13 : SWFD_CM16;
-  const double b1 = l ? SWFD_C13 : SWFD_CM16, b3 = l ? SWFD_CM16 : SWFD_C13;
-  const double c1 = l ? SWFD_CM16 : SWFD_C13, c2 = l ? SWFD_C56 : SWFD_CM76,
-               c3 = l ? SWFD_C13 : SWFD_C116;
-  const double d1 = l ? 0.1 : 0.3, d3 = l ? 0.3 : 0.1;
-  const double A = a1 * v2 + a2 * v3 + a3 * v4;
-  const double B = b1 * v1 + SWFD_C56 * v2 + b3 * v3;
-  const double C = c1 * v0 + c2 * v1 + c3 * v2;
-  double be1, be2, be3;
-  weno_beta(v0, v1, v2, v3, v4, be1, be2, be3);
-  const double w1 = div(d1, tsq(eps + be1));
-  const double w2 = div(0.6, tsq(eps + be2));
-  const double w3 = div(d3, tsq(eps + be3));
-  const double sum = w1 + w2 + w3;
-  return div(w1, sum) * A + div(w2, sum) * B + div(w3, sum) * C;
-}
-
 template <int YDIR, class D>
 __device__ __forceinline__ void weno4_side(const Eigen2D<double>& E, const double* __restrict__ s,
                                            int64_t P, int64_t step, double weps, int side, D div,

@@ -104,3 +104,22 @@ def test_lane_pair_flux_kernel_matches_the_oracle(swfd, oracle_mod, monkeypatch,
     assert np.array_equal(g.state(), o.state())
     assert g.stats() == o.stats()
     g.close()
+
+
+@pytest.mark.parametrize("block", [32, 256, 1024])
+def test_heavy_kernel_block_size_keeps_results(swfd, monkeypatch, block):
+    """SWFD_HEAVY_BLOCK sets the largest block of the splitting and RK kernels
+    (default 128): launch shape only, the same bits (ex4 form, 6 steps)."""
+    cfg = problems.make_config(abi.SEDOV_2D, nx=70, ny=50)
+    monkeypatch.delenv("SWFD_HEAVY_BLOCK", raising=False)
+    a = Solver(cfg)
+    monkeypatch.setenv("SWFD_HEAVY_BLOCK", str(block))
+    b = Solver(cfg)
+    for s in (a, b):
+        s.init_problem()
+    for _ in range(6):
+        assert a.step() == b.step()
+    assert np.array_equal(a.state(), b.state())
+    assert a.stats() == b.stats()
+    a.close()
+    b.close()
