@@ -750,7 +750,7 @@ enum { GRAPH_STEP = 0, GRAPH_SOLVE = 1, GRAPH_SWEEP = 2 };
 void emit_kind(Builder& b, cudaStream_t s, int kind) {
   swfd_handle* h = b.h;
   if (kind == GRAPH_STEP) {
-    emit_step(b, s, true);
+    emit_step(b, s, h->prof_on != 0);  // the flux events only when profiling
     B_OK(b, launch_time_advance(h->dsc, s));
     b.k(1);
   } else if (kind == GRAPH_SOLVE) {
@@ -1210,6 +1210,18 @@ swfd_status step_done(swfd_handle* h, const DevScalars& before, double* dt_out) 
   return st;
 }
 
+// the step graph, with the flux event nodes exactly when profiling is on
+// (each node is a dependency hop inside the step)
+swfd_status step_graph(swfd_handle* h) {
+  if (h->g_step && h->g_step_events != h->prof_on) {
+    cudaGraphExecDestroy(h->g_step);
+    h->g_step = nullptr;
+  }
+  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  h->g_step_events = h->prof_on;
+  return SWFD_OK;
+}
+
 swfd_status swfd_step(swfd_handle* h, double* dt_out) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
   SETTLE(h);
@@ -1220,7 +1232,7 @@ swfd_status swfd_step(swfd_handle* h, double* dt_out) {
     if (dt_out) *dt_out = h->hsc->dt;
     return st;
   }
-  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  ST(step_graph(h));
   // the host mirror holds the scalars of the last step (no step is pending):
   // the track arrays grow, with a synchronisation, only when a step's three
   // sweeps could overflow them
@@ -1242,7 +1254,7 @@ swfd_status swfd_step_host(swfd_handle* h, const double* u_in, double* u_out, do
     return swfd_download_state(h, u_out);
   }
   CU(h, cudaSetDevice(h->device));
-  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  ST(step_graph(h));
   if (h->hsc->sweep_count + 3 > h->track_cap) ST(ensure_tracks(h, 3));
   const size_t hb = (size_t)host_len(h->p) * sizeof(double);
   CU(h, cudaMemcpyAsync(h->d_stage, u_in, hb, cudaMemcpyHostToDevice, h->stream));
@@ -1259,7 +1271,7 @@ swfd_status swfd_step_async(swfd_handle* h) {
   if (h->eager || h->cfg.problem == SWFD_PROBLEM_MATLAB_1D || h->ex7)
     return swfd_step(h, nullptr);  // eager sections read conditions on the host
   CU(h, cudaSetDevice(h->device));
-  ST(build_graph(h, GRAPH_STEP, &h->g_step));
+  ST(step_graph(h));
   // a step records at most three sweeps: grow the track arrays (after
   // finishing what is enqueued) before the pending steps could overflow them
   if (h->hsc->sweep_count + 3 * (h->pending + 1) > h->track_cap) {
@@ -1619,6 +1631,7 @@ swfd_status swfd_get_stream(swfd_handle* h, void** stream) {
 
 swfd_status swfd_set_profiling(swfd_handle* h, int32_t on) {
   if (!h) return fail(h, SWFD_ERR_INVALID, "NULL handle");
+  SETTLE(h);  // enqueued steps report with the setting they ran under
   h->prof_on = on ? 1 : 0;
   return SWFD_OK;
 }

@@ -269,6 +269,7 @@ struct swfd_handle {
   // CUDA graphs, built on first use: one SSP-RK3 step (with flux events),
   // a solve (WHILE time <= T - 1d-10 over the step), and sweep_lim alone
   cudaGraphExec_t g_step = nullptr, g_solve = nullptr, g_sweep = nullptr;
+  int g_step_events = 0;  // g_step records the flux events (built with profiling on)
   cudaStream_t cap[SWFD_CAP_DEPTH] = {};  // capture streams, one per conditional nesting depth
   int* d_tracks = nullptr;   // device sweep tracks (3 x track_cap)
   int64_t track_cap = 0;
