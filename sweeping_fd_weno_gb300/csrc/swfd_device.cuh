@@ -321,8 +321,8 @@ __device__ __forceinline__ double weno_side(double v0, double v1, double v2, dou
 
 // FP32-bulk reconstructions: weno5's expressions (weno5.f90:86-146) in
 // binary32 with fused multiply-adds and reciprocal-estimate weights
-// (__fdividef: the MUFU reciprocal and a product, within 2 ulp).  The
-// FP32-bulk form is judged by its error against the FP64 form, not bit for
+// (__fdividef: CUDA's fast approximate division, within 2 ulp).  The
+// FP32-bulk form is accepted by its error against the FP64 form, not bit for
 // bit; every FP32 path (one instance, fused stage, batch) calls these, so
 // they agree with each other bit for bit.
 __device__ __forceinline__ void weno_beta_f32(float am2, float am1, float a0, float ap1, float ap2,
