@@ -818,6 +818,42 @@ static void findalpha1d(oracle* o) {
   o->alphamax = am;
 }
 
+/* use_limiter = 1 in ex2 (ex2_sedov_1d/main.f90:159-245): the positivity
+ * limiter of one split flux of cell m, with three components.  ave: the split
+ * flux at cell m (hp(:, m) or hn(:, m)); out: its reconstructed flux
+ * (hp_flux(:, m) or hn_flux(:, m)), limited in place. */
+static void zs_limit1d(oracle* o, const double* ave, double* out) {
+  const double g1 = o->gamma1;
+  const double d_ave = ave[0], m_ave = ave[1], e_ave = ave[2];
+  const double p_ave = g1 * (e_ave - 0.5 * (m_ave * m_ave) / d_ave);
+  double point[2][3];
+  double theta = 1.0;
+  for (int c = 0; c < 3; ++c) {
+    point[0][c] = out[c];
+    point[1][c] = (ave[c] - out[c] / 12.) / (11. / 12.);
+  }
+  for (int ig = 0; ig < 2; ++ig) {
+    double d_l = point[ig][0];
+    if (d_l < 0.) theta = fmin(theta, fabs(d_ave - 0.) / fabs(d_ave - d_l));
+  }
+  if (theta < 1.) {
+    out[0] = theta * out[0] + (1. - theta) * d_ave;
+    o->den_count++;
+  }
+  theta = 1.;
+  point[0][0] = out[0];
+  point[1][0] = (ave[0] - out[0] / 12.) / (11. / 12.);
+  for (int ig = 0; ig < 2; ++ig) {
+    double d_l = point[ig][0], m_l = point[ig][1], e_l = point[ig][2];
+    double p_l = g1 * (e_l - (m_l * m_l) / d_l / 2.);
+    if (p_l < 0.) theta = fmin(theta, fabs(p_ave - 0.) / fabs(p_ave - p_l));
+  }
+  if (theta < 1.) {
+    o->pre_count++;
+    for (int c = 0; c < 3; ++c) out[c] = theta * out[c] + (1. - theta) * ave[c];
+  }
+}
+
 /* wenofd (ex2_sedov_1d/main.f90:75-250): eigenvectors at cell m */
 static void wenofd1d(oracle* o) {
   const int n = o->nx;
@@ -866,6 +902,21 @@ static void wenofd1d(oracle* o) {
     for (int k = 0; k < 3; ++k) {
       U1(o->fpf, k, m) = evr[k][0] * ur[0] + evr[k][1] * ur[1] + evr[k][2] * ur[2];
       U1(o->fnf, k, m) = evr[k][0] * ul[0] + evr[k][1] * ul[1] + evr[k][2] * ul[2];
+    }
+    if (o->cfg.use_limiter == 1) { /* :159-245, hp_flux then hn_flux */
+      double a[3], b[3], op[3], on[3];
+      for (int c = 0; c < 3; ++c) {
+        a[c] = U1(o->fp, c, m);
+        b[c] = U1(o->fn, c, m);
+        op[c] = U1(o->fpf, c, m);
+        on[c] = U1(o->fnf, c, m);
+      }
+      zs_limit1d(o, a, op);
+      zs_limit1d(o, b, on);
+      for (int c = 0; c < 3; ++c) {
+        U1(o->fpf, c, m) = op[c];
+        U1(o->fnf, c, m) = on[c];
+      }
     }
   }
 }

@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 BUILD = PKG / "_build"
 SOURCES = ["swfd_api.cu", "swfd_kernels.cu", "swfd_sweep.cu", "swfd_ubar.cu", "swfd_control.cu",
-           "swfd_static.cu", "swfd_batch.cu", "swfd_matlab1d.cu", "swfd_ex7.cu"]
+           "swfd_static.cu", "swfd_batch.cu", "swfd_matlab1d.cu", "swfd_ex7.cu", "swfd_solve1d.cu"]
 # measurement and test probes (include/swfd_probe.h): a library of their own
 PROBE_SOURCES = ["swfd_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

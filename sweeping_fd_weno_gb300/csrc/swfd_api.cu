@@ -247,9 +247,9 @@ swfd_status make_params(const swfd_config& c, Params& p, std::string& err) {
   p.fdx_inv = (float)(1.0 / p.dx);
   p.fdy_inv = g.ndim == 2 ? (float)(1.0 / p.dy) : 0.f;
   p.stop_sweep = c.problem == SWFD_PROBLEM_SEDOV_2D || c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
-  // the positivity limiter exists in the 2D examples only (ex2 has no
-  // use_limiter == 1 branch)
-  p.limiter = c.use_limiter == 1 && g.ndim == 2;
+  // the positivity limiter of the split fluxes (use_limiter 1; 1D:
+  // ex2_sedov_1d/main.f90:159-245)
+  p.limiter = c.use_limiter == 1;
   p.limiter_clamp = c.problem == SWFD_PROBLEM_SHOCK_DIFFRACTION;
   if (!p.seg_alpha) {
     p.cut_x = p.cut_y = 1;
@@ -472,6 +472,8 @@ swfd_status check_device_error(swfd_handle* h) {
   CU(h, cudaMemsetAsync(&h->dsc->error, 0, sizeof(int), h->stream));
   CU(h, cudaStreamSynchronize(h->stream));
   h->hsc->error = 0;
+  if (e & ERR_BIT_TIMEOUT)
+    return fail(h, SWFD_ERR_TIMEOUT, "device-side wait timed out (persistent 1D solve barrier)");
   if (e & ERR_BIT_RESTART)
     return fail(h, SWFD_ERR_RESTART_LIMIT, "restart RK: no positive state within "
                                            "SWFD_RESTART_LIMIT dt halvings");
@@ -867,6 +869,81 @@ swfd_status finish_pending(swfd_handle* h) {
   return st;
 }
 
+// The 1D solve as persistent launches (swfd_solve1d.cu): one cooperative
+// launch runs the time loop on the device; a stage whose checkpositivity
+// fails ends it, sweep_lim runs on that stage's output as plain launches
+// (the conditions read on the host) and the next launch resumes at the
+// following stage.  SWFD_SOLVE1D=graph keeps the graph kernels.
+bool use_solve1d(swfd_handle* h, Solve1dShape* sh) {
+  if (h->cfg.rk_choice == 2) return false;
+  const char* env = getenv("SWFD_SOLVE1D");
+  if (env && strcmp(env, "graph") == 0) return false;
+  return solve1d_shape(h->p, sh);
+}
+
+swfd_status run_solve1d(swfd_handle* h, const Solve1dShape& sh, int64_t max_steps,
+                        int64_t* nsteps_out) {
+  if (h->s1_grid < sh.grid) {
+    cudaFree(h->s1_parts);
+    h->s1_parts = nullptr;
+    h->s1_grid = 0;
+    CU(h, cudaMalloc(&h->s1_parts, 2 * (size_t)sh.grid * sizeof(Solve1dPart)));
+    h->s1_grid = sh.grid;
+  }
+  if (!h->s1_bar) CU(h, cudaMalloc(&h->s1_bar, sizeof(unsigned)));
+  Solve1dArgs a;
+  for (int k = 0; k < 3; ++k) a.st[k] = h->st[(h->cur + k) % 3];
+  a.parts = h->s1_parts;
+  a.bar = h->s1_bar;
+  a.cells = sh.cells;
+  a.sweeps = h->cfg.use_limiter == 2;
+  int64_t done = 0;
+  const int64_t chunk = 4096;  // steps per launch sequence (bounds the track growth)
+  swfd_status st = SWFD_OK;
+  while (h->time <= h->p.t_loop) {
+    if (max_steps > 0 && done >= max_steps) {
+      st = SWFD_ERR_MAX_STEPS;
+      break;
+    }
+    long long lim = (long long)(max_steps > 0 ? std::min<int64_t>(chunk, max_steps - done) : chunk);
+    ST(ensure_tracks(h, 3 * lim));
+    const DevScalars before = *h->hsc;
+    CU(h, cudaMemcpyAsync(&h->dsc->steps_limit, &lim, sizeof(long long), cudaMemcpyHostToDevice,
+                          h->stream));
+    CU(h, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), h->stream));
+    a.resume = 1;
+    for (;;) {
+      CU(h, launch_solve1d(h->p, sh, a, h->dsc, h->stream));
+      h->prof.kernel_launches += 1;
+      st = check_device_error(h);
+      const int pause = h->hsc->solve_pause;
+      if (st != SWFD_OK || !pause) break;
+      // sweep_lim on the output of stage `pause`
+      Builder b;
+      b.h = h;
+      b.eager = true;
+      b.cond_word = &h->dsc->cond;
+      b.launched = &h->eager_launches;
+      emit_sweep(b, h->stream, a.st[pause % 3]);
+      if (b.err != cudaSuccess)
+        return fail(h, SWFD_ERR_CUDA, std::string("1D sweep: ") + cudaGetErrorString(b.err));
+      h->prof.kernel_launches += h->eager_launches;
+      h->eager_launches = 0;
+      st = check_device_error(h);
+      if (st != SWFD_OK) break;
+      a.resume = pause + 1;
+    }
+    const int64_t steps = h->hsc->steps;
+    h->prof.stages += 3 * steps;
+    h->prof.sweep_invocations += h->hsc->sweep_count - before.sweep_count;
+    done += steps;
+    if (st != SWFD_OK) break;
+    if (steps < lim) break;  // the time test ended the loop
+  }
+  if (nsteps_out) *nsteps_out = done;
+  return st;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1101,6 +1178,8 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->seg_buf);
   cudaFree(h->rhs_tmp);
   cudaFree(h->m1_wk);
+  cudaFree(h->s1_parts);
+  cudaFree(h->s1_bar);
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);
@@ -1387,6 +1466,10 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
     }
     if (nsteps_out) *nsteps_out = done;
     return st;
+  }
+  {
+    Solve1dShape sh;
+    if (use_solve1d(h, &sh)) return run_solve1d(h, sh, max_steps, nsteps_out);
   }
   ST(build_graph(h, GRAPH_SOLVE, &h->g_solve));
   int64_t done = 0;

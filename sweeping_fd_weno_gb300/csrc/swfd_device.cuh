@@ -34,6 +34,13 @@ __device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double tabs(double a) { return fabs(a); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
+// -a (IEEE negation: the sign bit flipped).  Binary64 on the integer pipe, so
+// a negated value that is selected at run time, not folded into its
+// product, costs no FP64 instruction.
+__device__ __forceinline__ double tneg(double a) {
+  return __hiloint2double(__double2hiint(a) ^ (int)0x80000000, __double2loint(a));
+}
+__device__ __forceinline__ float tneg(float a) { return -a; }
 __device__ __forceinline__ double dsq(double a) { return a * a; }
 // a / b.  Binary64: sd::div, the correctly rounded quotient (the bits of the
 // hardware division) from integer and FP32 arithmetic, which leaves the FP64
@@ -272,15 +279,15 @@ __device__ __forceinline__ void roe_eigen2d(T g1, int ydir, T wl, T wr, T vxl, T
   T t2 = tscale<-1>(b1);
   T t3 = b1 * vt;
   E.l1_0 = tscale<-1>(b2 + t0);
-  E.l1_n = -tscale<-1>(t1 + rcm);  // (-0.5)*x == -(0.5*x)
-  E.l1_t = -tscale<-1>(t3);
+  E.l1_n = tneg(tscale<-1>(t1 + rcm));  // (-0.5)*x == -(0.5*x)
+  E.l1_t = tneg(tscale<-1>(t3));
   E.l1_3 = t2;
   E.l3_0 = T(1.) - b2;
   E.l3_n = t1;
   E.l3_t = t3;
-  E.l3_3 = -b1;
+  E.l3_3 = tneg(b1);
   E.l4_0 = tscale<-1>(b2 - t0);
-  E.l4_n = -tscale<-1>(t1 - rcm);
+  E.l4_n = tneg(tscale<-1>(t1 - rcm));
   E.l4_t = E.l1_t;
   E.l4_3 = t2;
 }

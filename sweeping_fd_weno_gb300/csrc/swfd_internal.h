@@ -140,7 +140,8 @@ enum : int {
   ERR_BIT_PUBAR = 4,     // P(u_bar) <= 0 (ex4 stop)
   ERR_BIT_NOCONV = 8,    // sweep reached swp_num (ex4 stop)
   ERR_BIT_CHECK = 16,    // nodal adjustment raised the total pressure (ex6 stop)
-  ERR_BIT_RESTART = 32   // restart RK: SWFD_RESTART_LIMIT dt halvings without a positive state
+  ERR_BIT_RESTART = 32,  // restart RK: SWFD_RESTART_LIMIT dt halvings without a positive state
+  ERR_BIT_TIMEOUT = 64   // a bounded device-side wait (a grid barrier) ran out
 };
 
 // conditional nesting depth of the graphs: solve WHILE > restart WHILE > IF > IF
@@ -177,6 +178,7 @@ struct DevScalars {
   double alphatemp;       // restart RK: alphamax of the step's first findalpha
   long long restart_total;  // restart RK: dt halvings of all steps
   long long rk_runs[4];   // RK stages run, by stage (1..3)
+  int solve_pause;        // persistent 1D solve: the stage whose sweep is pending (0: none)
 };
 
 // The value of a conditional node: set on the graph's handle, or written to
@@ -240,6 +242,32 @@ namespace swfd {
 struct Ex7;  // the detonation engine (swfd_ex7.h)
 }
 
+namespace swfd {
+// The persistent 1D solve (swfd_solve1d.cu): one block per SM, each owning
+// `cells` consecutive cells, the whole time loop in one cooperative launch.
+#define SWFD_SOLVE1D_MAX_BLOCK 512
+#define SWFD_SOLVE1D_MIN_CELLS 6
+#define SWFD_SOLVE1D_MAX_CELLS 62
+struct Solve1dPart {  // one block's contribution to a stage's grid reduction
+  double a;           // maximum findalpha term of its cells
+  int bad;            // a cell failed checkpositivity
+  int pad;
+};
+struct Solve1dArgs {
+  double* st[3];       // X (the step's start and u0), Y, Z
+  Solve1dPart* parts;  // 2 x grid
+  unsigned* bar;       // grid-barrier counter (zeroed by the launcher)
+  int cells;           // cells per block
+  int resume;          // 1: stage 1; 2, 3: that stage after the previous stage's
+                       // sweep; 4: the time advance after a stage-3 sweep
+  int sweeps;          // use_limiter == 2: a failed checkpositivity pauses for sweep_lim
+};
+struct Solve1dShape {
+  int grid, block, cells;
+  size_t smem;
+};
+}  // namespace swfd
+
 struct swfd_handle {
   swfd_config cfg;
   swfd::Params p;
@@ -297,6 +325,11 @@ struct swfd_handle {
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles
   // the detonation (ex7) keeps its own rank-sliced state; set only for that problem
   swfd::Ex7* ex7 = nullptr;
+  // the persistent 1D solve: the blocks' alpha and positivity parts (2 x
+  // grid) and its grid-barrier counter, allocated on its first run
+  swfd::Solve1dPart* s1_parts = nullptr;
+  unsigned* s1_bar = nullptr;
+  int s1_grid = 0;
 };
 
 namespace swfd {
@@ -356,6 +389,16 @@ cudaError_t launch_rhs(const Params& p, const void* flux, const DevScalars* dsc,
                        cudaStream_t s);
 cudaError_t launch_positivity(const Params& p, const double* u, DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_time_advance(DevScalars* dsc, cudaStream_t s);
+
+// solve1d.cu: the launch shape of the persistent 1D solve (FP64, binary64
+// literals); false when the problem or the device does not take it (the
+// solve then runs as graph kernels)
+bool solve1d_shape(const Params& p, Solve1dShape* sh);
+// one cooperative launch: stages from a.resume while time <= t_loop and
+// dsc->steps < dsc->steps_limit; it stops early at a stage whose
+// checkpositivity failed (dsc->solve_pause = the stage) when a.sweeps
+cudaError_t launch_solve1d(const Params& p, const Solve1dShape& sh, const Solve1dArgs& a,
+                           DevScalars* dsc, cudaStream_t s);
 cudaError_t launch_fortran_to_soa(const Params& p, const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_soa_to_fortran(const Params& p, const double* src, double* dst, cudaStream_t s);
 // quad: the reference build's binary128 smoothness indicators and alphas
@@ -377,11 +420,14 @@ cudaError_t launch_batch_stage32(const BatchLaunch& b, int stage, int in, int ou
                                  cudaGraphConditionalHandle h_sweep, cudaStream_t s);
 long long stage32_items(const Params& p);
 // launch-shape candidates of the flux kernel (resident blocks per SM; FP64
-// values SWFD_FLUX_PAIR + b select the lane-pair kernel with b blocks per SM);
-// returns their number, the default first
+// values SWFD_FLUX_PAIR + b and SWFD_FLUX_LOOP + b select the lane-pair
+// kernels with b blocks per SM); returns their number, the default first
 #define SWFD_FLUX_PAIR 10
-// the FP64 flux kernel's default shape: the lane-pair kernel, 4 blocks per SM
-#define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_PAIR + 4)
+// SWFD_FLUX_LOOP + b: the lane-pair kernel's short form (one code path for both
+// directions, the characteristic fields in a loop)
+#define SWFD_FLUX_LOOP 20
+// the FP64 flux kernel's default shape: the short lane-pair kernel, 5 blocks per SM
+#define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_LOOP + 5)
 int flux_min_blocks_candidates(bool f32, int* out);
 cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
 cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,

@@ -1,6 +1,6 @@
 // swfd_kernels.cu -- boundary conditions, CFL reduction, LF splitting, the
 // characteristic WENO5 interface fluxes and the fused RHS + SSP-RK3 update.
-#include "swfd_device.cuh"
+#include "swfd_1d.cuh"
 
 namespace swfd {
 
@@ -135,10 +135,7 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
     const double g1 = p.gamma1, gamma = p.gamma;
     if (g.ndim == 1) {
       // ex2_sedov_1d/main.f90:278-283
-      double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o);
-      double pres = g1 * (u3 - tscale<-1>(tdiv(u2 * u2, u1)));
-      double sound = sqrt(tdiv(gamma * pres, u1));
-      a = fabs(tdiv(u2, u1)) + sound;
+      a = alpha1d(p, ldc<NC>(u + o), ldc<NC>(u + g.plane + o), ldc<NC>(u + 2 * g.plane + o));
     } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
       // FP32-bulk: the pressure recovered in FP64 (one reciprocal per cell);
       // the CFL quantities (velocities, sound speed, their max) in FP32
@@ -624,20 +621,11 @@ __device__ __forceinline__ void prep1d_cell(const Params& p, const double* __res
   const Geom& g = p.g;
   if (t >= g.LI) return;
   const int64_t o = t, P = g.plane;
-  const double g1 = p.gamma1;
-  double rho = ld(u + o), mx = ld(u + P + o), e = ld(u + 2 * P + o);
-  // fflux (ex2_sedov_1d/main.f90:57-73)
-  double vx = 0.;
-  if (rho > p.lim8_gt) vx = mx / rho;
-  if (rho <= p.lim8_le) vx = 0.;
-  double pres = g1 * (e - 0.5 * rho * (vx * vx));
-  double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
-  double a[3] = {rho, mx, e};
-  const T am = T(amd);
+  T sp[3], sn[3];
+  split1d<T>(p, ld(u + o), ld(u + P + o), ld(u + 2 * P + o), amd, sp, sn);
   for (int c = 0; c < 3; ++c) {
-    T q = T(f[c]) / am;
-    split[c * P + o] = T(0.5) * (T(a[c]) + q);
-    split[(3 + c) * P + o] = T(0.5) * (T(a[c]) - q);
+    split[c * P + o] = sp[c];
+    split[(3 + c) * P + o] = sn[c];
   }
 }
 
@@ -864,7 +852,7 @@ __device__ __forceinline__ void interface_flux(const Eigen2D<T>& E, const T* __r
 template <class T, bool QD = false>
 __device__ __forceinline__ void flux1d_lane(const Params& p, const double* __restrict__ u,
                                             const T* __restrict__ split, T* __restrict__ flux,
-                                            int t) {
+                                            int t, unsigned long long* cnt) {
   // eight lanes per cell: lanes 0..5 of a group each reconstruct one
   // characteristic field (k = lane / 2) of one side (lane % 2: the positive
   // flux at the right face, the negative one), so that the six WENO chains of
@@ -880,62 +868,33 @@ __device__ __forceinline__ void flux1d_lane(const Params& p, const double* __res
   const bool active = m <= g.nx + 1;
   const int mm = active ? m : g.nx + 1;  // inactive lanes repeat the last cell
   const int64_t P = g.plane, o = g.at(mm, -2);
-  const double g1d = p.gamma1;
-  double u1 = ld(u + o), u2 = ld(u + P + o), u3 = ld(u + 2 * P + o);
-  double vxd = tdiv(u2, u1);
-  double hmd = tdiv(g1d * (u3 - tdiv(tscale<-1>(u2 * u2), u1)) + u3, u1);
-  const T g1 = T(g1d), vxm = T(vxd), hm = T(hmd);
-  T qm = tscale<-1>(vxm) * vxm;
-  T cm = sqrt(g1 * (hm - qm));
-  T t0 = vxm * cm;
-  T r10 = vxm - cm, r12 = vxm + cm, r20 = hm - t0, r22 = hm + t0;
-  T rcm = tdiv(T(1.), cm);
-  T b1 = g1 * rcm * rcm;
-  T b2 = qm * b1;
-  t0 = vxm * rcm;
-  T t1 = b1 * vxm;
-  T t2 = tscale<-1>(b1);
-  T L[3][3] = {{tscale<-1>(b2 + t0), -tscale<-1>(t1 + rcm), t2},
-               {T(1.) - b2, t1, -b1},
-               {tscale<-1>(b2 - t0), -tscale<-1>(t1 - rcm), t2}};
-  const T weps = T(p.weno_eps);
-  const int k = sub < 6 ? sub >> 1 : 0, side = sub & 1;
-  const T* sp = split + (side ? 3 * P : 0);
-  T cs[5];
+  Eigen1D<T> E;
+  eigen1d<T>(p.gamma1, ld(u + o), ld(u + P + o), ld(u + 2 * P + o), E);
+  const T v = recon1d<T, QD>(p, E, sub, [&](int side, int c, int jj) {
+    return ldt(split + (side ? 3 * P : 0) + c * P + o + jj - 2);
+  });
+  const T r = back1d<T>(E, v, sub);
+  if (!p.limiter) {
+    if (active && sub < 6) flux[sub * P + o] = r;
+    return;
+  }
+  // use_limiter 1: lanes 0 and 3 limit and store their side's components
+  T w[3];
+  int nd = 0, np = 0;
+  const bool lim = limit1d_group<T>(
+      p, r, sub, [&](int side, int c) { return ldt(split + (side ? 3 * P : 0) + c * P + o); }, w,
+      nd, np);
+  if (active && lim) {
 #pragma unroll
-  for (int jj = 0; jj < 5; ++jj) {
-    const int64_t s = o + jj - 2;
-    cs[jj] = L[k][0] * ldt(sp + s) + L[k][1] * ldt(sp + P + s) + L[k][2] * ldt(sp + 2 * P + s);
-  }
-  T v;
-  if constexpr (QD) {
-    const QuadWeno qw{p.q_c1312, p.q_weno_eps};
-    v = side ? weno_left_qd(cs[0], cs[1], cs[2], cs[3], cs[4], qw)
-             : weno_right_qd(cs[0], cs[1], cs[2], cs[3], cs[4], qw);
-  } else {
-    v = side ? weno_left(cs[0], cs[1], cs[2], cs[3], cs[4], weps)
-             : weno_right(cs[0], cs[1], cs[2], cs[3], cs[4], weps);
-  }
-  const int base = threadIdx.x & ~7 & 31;
-  const T ur0 = __shfl_sync(0xffffffffu, v, base + 0), ul0 = __shfl_sync(0xffffffffu, v, base + 1);
-  const T ur1 = __shfl_sync(0xffffffffu, v, base + 2), ul1 = __shfl_sync(0xffffffffu, v, base + 3);
-  const T ur2 = __shfl_sync(0xffffffffu, v, base + 4), ul2 = __shfl_sync(0xffffffffu, v, base + 5);
-  if (!active) return;
-  switch (sub) {
-    case 0: flux[o] = ur0 + ur1 + ur2; break;
-    case 1: flux[P + o] = r10 * ur0 + vxm * ur1 + r12 * ur2; break;
-    case 2: flux[2 * P + o] = r20 * ur0 + qm * ur1 + r22 * ur2; break;
-    case 3: flux[3 * P + o] = ul0 + ul1 + ul2; break;
-    case 4: flux[4 * P + o] = r10 * ul0 + vxm * ul1 + r12 * ul2; break;
-    case 5: flux[5 * P + o] = r20 * ul0 + qm * ul1 + r22 * ul2; break;
-    default: break;
+    for (int c = 0; c < 3; ++c) flux[(sub + c) * P + o] = w[c];
+    count_limited(cnt, nd, np);
   }
 }
 
 template <class T, bool QD = false>
 __global__ void k_flux1d(Params p, const double* __restrict__ u, const T* __restrict__ split,
-                         T* __restrict__ flux) {
-  flux1d_lane<T, QD>(p, u, split, flux, blockIdx.x * blockDim.x + threadIdx.x);
+                         T* __restrict__ flux, unsigned long long* cnt) {
+  flux1d_lane<T, QD>(p, u, split, flux, blockIdx.x * blockDim.x + threadIdx.x, cnt);
 }
 
 // Both directions in one persistent launch: a grid of exactly the resident
@@ -989,10 +948,6 @@ __device__ __forceinline__ void zs_limit(const Params& p, const T* __restrict__ 
   }
 }
 
-__device__ __forceinline__ void count_limited(unsigned long long* cnt, int nd, int np) {
-  if (nd) atomicAdd(cnt, (unsigned long long)nd);
-  if (np) atomicAdd(cnt + 1, (unsigned long long)np);
-}
 
 // the 32 interfaces of chunk c (x chunks first, then y chunks).  SEG: the
 // problem may have rank segments (ex6); without them the face index maps
@@ -1259,6 +1214,149 @@ static int flux_grid_pair() {
   return grid;
 }
 
+// ---------------------------------------------------------------------------
+// The lane-pair interface fluxes as one short instruction stream: the x and y
+// interfaces share one code path (the direction is warp-uniform: a chunk holds
+// interfaces of one direction; it selects the addresses, the projection
+// coefficients' order and the output planes), and one reconstruction runs in
+// a loop over the four characteristic fields, the back projection accumulated
+// field by field in the order of its sums.  Every value is the lane-pair
+// kernel's expression; the code a warp executes per interface is about an
+// eighth of the unrolled form's, which the instruction cache holds while 16
+// warps per SM are at different points of it.
+// ---------------------------------------------------------------------------
+template <class D>
+__device__ __forceinline__ void weno4_side_loop(const Eigen2D<double>& E, int ydir,
+                                                const double* __restrict__ s, int64_t P,
+                                                int64_t step, double weps, int side, D div,
+                                                double& o0, double& on, double& ot, double& o3) {
+  const double nvt = tneg(E.vt);
+#pragma unroll 1
+  for (int k = 0; k < 4; ++k) {
+    double c[5];
+    if (k == 1) {  // evl row 2: x pass -vt*f0 + f2, y pass -vt*f0 + f1
+      const int64_t pg = ydir ? P : 2 * P;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const double* a = s + m * step;
+        c[m] = nvt * ldt(a) + ldt(a + pg);
+      }
+    } else {
+      // rows 1, 3, 4: l0*f0 + ln*f1 + lt*f2 + l3*f3 (x), l0*f0 + lt*f1 + ln*f2 + l3*f3 (y)
+      const double l0 = k == 0 ? E.l1_0 : k == 2 ? E.l3_0 : E.l4_0;
+      const double ln = k == 0 ? E.l1_n : k == 2 ? E.l3_n : E.l4_n;
+      const double lt = k == 0 ? E.l1_t : k == 2 ? E.l3_t : E.l4_t;
+      const double l3 = k == 0 ? E.l1_3 : k == 2 ? E.l3_3 : E.l4_3;
+      const double k1 = ydir ? lt : ln, k2 = ydir ? ln : lt;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const double* a = s + m * step;
+        c[m] = l0 * ldt(a) + k1 * ldt(a + P) + k2 * ldt(a + 2 * P) + l3 * ldt(a + 3 * P);
+      }
+    }
+    const double w = weno_side(c[0], c[1], c[2], c[3], c[4], side, weps, div);
+    // evr . w, each sum in its order:
+    //   o0 = w0 + w2 + w3,  on = e_nm w0 + vn w2 + e_np w3,
+    //   ot = vt w0 + w1 + vt w2 + vt w3,  o3 = e_hm w0 + vt w1 + qm w2 + e_hp w3
+    if (k == 0) {
+      o0 = w;
+      on = E.e_nm * w;
+      ot = E.vt * w;
+      o3 = E.e_hm * w;
+    } else if (k == 1) {
+      ot = ot + w;
+      o3 = o3 + E.vt * w;
+    } else {
+      const double cn = k == 2 ? E.vn : E.e_np, c3 = k == 2 ? E.qm : E.e_hp;
+      o0 = o0 + w;
+      on = on + cn * w;
+      ot = ot + E.vt * w;
+      o3 = o3 + c3 * w;
+    }
+  }
+}
+static __device__ __noinline__ Side4 weno4_side_loop_hw(Eigen2D<double> E, int ydir,
+                                                        const double* s, int64_t P, int64_t step,
+                                                        double weps, int side) {
+  Side4 r;
+  weno4_side_loop(E, ydir, s, P, step, weps, side, DivHw(), r.v[0], r.v[1], r.v[2], r.v[3]);
+  return r;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
+    k_flux_xy_loop(Params p, const double* __restrict__ split, const double* __restrict__ roe,
+                   const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
+  const Geom& g = p.g;
+  const int64_t chunks_x = (flux_faces_x(p) + 15) / 16;
+  const int64_t chunks = chunks_x + (flux_faces_y(p) + 15) / 16;
+  const int lane = threadIdx.x & 31, side = lane & 1;
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+  const int64_t P = g.plane, S = p.sg.plane, spit = p.sg.pitch;
+  const double g1 = p.gamma1, weps = p.weno_eps;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) break;
+    // the interface: its direction, offset, Roe neighbour, stencil start and step
+    int ydir;
+    int64_t o, rnb, step;
+    const double* rb;
+    if (c < chunks_x) {
+      const int64_t t = (int64_t)c * 16 + (lane >> 1);
+      if (t >= flux_faces_x(p)) continue;
+      const int lx = p.nxl + 2;  // faces i = 0..nx+1 of rows 1..ny (one segment)
+      o = g.at((int)t % lx, (int)t / lx + 1);
+      ydir = 0, rnb = 1, step = 1, rb = roe;
+    } else {
+      const int64_t t = ((int64_t)c - chunks_x) * 16 + (lane >> 1);
+      if (t >= flux_faces_y(p)) continue;
+      o = g.at((int)t % g.nx + 1, (int)t / g.nx);
+      ydir = 1, rnb = g.pitch, step = spit, rb = roe + (p.roe_reg_ex4 ? 4 * P : 0);
+    }
+    Eigen2D<double> E;
+    roe_eigen2d<double>(g1, ydir, ldt(rb + o), ldt(rb + o + rnb), ldt(rb + P + o),
+                        ldt(rb + P + o + rnb), ldt(rb + 2 * P + o), ldt(rb + 2 * P + o + rnb),
+                        ldt(rb + 3 * P + o), ldt(rb + 3 * P + o + rnb), E);
+    const int64_t pl = 8 * ydir + 4 * side;  // the side's first split and flux plane
+    const double* s = split + pl * S + o - 2 * step;
+    double o0, on, ot, o3;
+    int bad = 0;
+    weno4_side_loop(E, ydir, s, S, step, weps, side, DivFlag{&bad}, o0, on, ot, o3);
+    if (bad) {
+      const Side4 r = weno4_side_loop_hw(E, ydir, s, S, step, weps, side);
+      o0 = r.v[0], on = r.v[1], ot = r.v[2], o3 = r.v[3];
+    }
+    double* f = flux + pl * S + o;
+    const int64_t fn = ydir ? 2 * S : S, ft = ydir ? S : 2 * S;
+    f[0] = p.alpha_premul ? am * o0 : o0;
+    f[fn] = p.alpha_premul ? am * on : on;
+    f[ft] = p.alpha_premul ? am * ot : ot;
+    f[3 * S] = p.alpha_premul ? am * o3 : o3;
+  }
+  if (lane == 0) {  // as k_flux_xy: the last warp out re-arms both counters
+    __threadfence();
+    if (atomicAdd(work + 1, 1) == (int)(gridDim.x * (blockDim.x >> 5)) - 1) {
+      atomicExch(work, 0);
+      atomicExch(work + 1, 0);
+    }
+  }
+}
+
+template <int MINB>
+static int flux_grid_loop() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy_loop<MINB>, SWFD_FLUX_BLOCK, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  return grid;
+}
+
 template <class T, int MINB = SWFD_FLUX_MINB(T)>
 static int flux_grid() {
   static int grid = 0;
@@ -1275,19 +1373,21 @@ static int flux_grid() {
 
 // Launch-shape variants of the common flux kernel (no rank segments, no
 // limiter) that swfd_autotune times: resident blocks per SM, traded against
-// registers per thread (FP64: 3 = 168 registers, 2 = 236, 4 = 128 with about
-// 200 bytes of spills; FP32: 4 = 128, 5 = 102, 6 = 85).  The first entry is
-// the default.
+// registers per thread (FP64 one-lane kernel: 3 = 168 registers, 2 = 236, 4 =
+// 128 with spills; FP32: 4 = 128, 5 = 102, 6 = 85), and for FP64 the
+// lane-pair kernels.  The first entry is the default.
 int flux_min_blocks_candidates(bool f32, int* out) {
   if (f32) {
     out[0] = 4, out[1] = 5, out[2] = 6;
     return 3;
   }
-  // FP64: the lane-pair kernel (SWFD_FLUX_PAIR + 3..6 blocks per SM; the
-  // default 4 first) and the one-lane kernel (3, 2, 4 blocks per SM)
-  out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_PAIR + 3, out[2] = SWFD_FLUX_PAIR + 5;
-  out[3] = SWFD_FLUX_PAIR + 6, out[4] = 3, out[5] = 2, out[6] = 4;
-  return 7;
+  // FP64: the short lane-pair kernel (SWFD_FLUX_LOOP + 5 blocks per SM, the
+  // default; + 4), the unrolled lane-pair kernel (SWFD_FLUX_PAIR + 3..6) and
+  // the one-lane kernel (3, 2, 4 blocks per SM)
+  out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_LOOP + 4, out[2] = SWFD_FLUX_PAIR + 4;
+  out[3] = SWFD_FLUX_PAIR + 3, out[4] = SWFD_FLUX_PAIR + 5, out[5] = SWFD_FLUX_PAIR + 6;
+  out[6] = 3, out[7] = 2, out[8] = 4;
+  return 9;
 }
 
 template <class T, int MINB>
@@ -1319,8 +1419,8 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       return;
     }
   }
-  // the FP64 default shape is the lane-pair kernel with 4 blocks per SM
-  // (SWFD_FLUX_DEFAULT64); flux_minb 3 selects the one-lane kernel's default
+  // the FP64 default shape is the short lane-pair kernel with 5 blocks per
+  // SM (SWFD_FLUX_DEFAULT64); flux_minb 3 selects the one-lane kernel's default
   int minb = p.flux_minb;
   if constexpr (sizeof(T) == 8)
     if (!minb) minb = SWFD_FLUX_DEFAULT64;
@@ -1338,6 +1438,14 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       SWFD_PAIR_CASE(5)
       SWFD_PAIR_CASE(6)
 #undef SWFD_PAIR_CASE
+#define SWFD_LOOP_CASE(M)                                                                    \
+  if (minb == SWFD_FLUX_LOOP + M) {                                                          \
+    k_flux_xy_loop<M><<<flux_grid_loop<M>(), SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work); \
+    return;                                                                                  \
+  }
+      SWFD_LOOP_CASE(4)
+      SWFD_LOOP_CASE(5)
+#undef SWFD_LOOP_CASE
     } else {
       if (minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
       if (minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);
@@ -1361,14 +1469,17 @@ cudaError_t launch_flux(const Params& p, const void* split, const void* roe,
     // the 1D eigenvectors come from the state, which the caller passes as roe
     const int64_t lanes = 8 * (int64_t)(g.nx + 2);  // eight lanes per cell
     const int b = cell_block(lanes), gb = (int)((lanes + b - 1) / b);
+    // the limiter's counts: den_count and pre_count, adjacent in DevScalars
+    unsigned long long* cnt = (unsigned long long*)&const_cast<DevScalars*>(dsc)->den_count;
     if (f32)
-      k_flux1d<float><<<gb, b, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux);
+      k_flux1d<float><<<gb, b, 0, s>>>(p, (const double*)roe, (const float*)split, (float*)flux,
+                                       cnt);
     else if (p.quad)
       k_flux1d<double, true><<<gb, b, 0, s>>>(p, (const double*)roe, (const double*)split,
-                                               (double*)flux);
+                                               (double*)flux, cnt);
     else
       k_flux1d<double><<<gb, b, 0, s>>>(p, (const double*)roe, (const double*)split,
-                                         (double*)flux);
+                                         (double*)flux, cnt);
     return cudaGetLastError();
   }
   if (f32)
@@ -1441,10 +1552,7 @@ __device__ __forceinline__ T rhs1d(const Params& p, const T* __restrict__ flux, 
   const int64_t P = p.g.plane;
   const T* hp = flux + c * P;
   const T* hn = flux + (3 + c) * P;
-  const T am = T(amd);
-  T fl_i = am * (ldt(hp + o - 1) - ldt(hn + o));
-  T fl_ip1 = am * (ldt(hp + o) - ldt(hn + o + 1));
-  return -tdiv(fl_ip1 - fl_i, T(p.dx));
+  return rhs1d_value<T>(p, amd, ldt(hp + o - 1), ldt(hn + o), ldt(hp + o), ldt(hn + o + 1));
 }
 
 __device__ __forceinline__ int block_or(int v) { return __syncthreads_or(v); }
@@ -1457,21 +1565,6 @@ __device__ __forceinline__ T rhs2d_cell(const Params& p, const T* __restrict__ f
   return rhs2d<T>(p, flux, c, seg_x_off(p, i, j, sx), seg_y_off(p, i, j, sy), amd);
 }
 
-// u0 may alias out (stage 3 writes the step-start buffer); each element of
-// u0 is read only by the thread that then writes it.
-// u = 0.75d0*u0 + 0.25d0*v and u = (u0 + 2d0*v)/3d0
-// (ex3_vortex_accuracy_2d/main.f90:604,621); in binary128 for the QUAD build
-// (0.75*u0 and 0.25*v are exact there)
-__device__ __forceinline__ double rk_combine(const Params& p, int stage, double u0, double v) {
-  if (p.quad) {
-    using namespace qd;
-    if (stage == 2)
-      return to_double(add(mul(from_double(0.75), from_double(u0)), scale2(from_double(v), -2)));
-    return to_double(div(add(from_double(u0), scale2(from_double(v), 1)), from_double(3.0)));
-  }
-  if (stage == 2) return 0.75 * u0 + tscale<-2>(v);
-  return tdiv(u0 + tscale<1>(v), 3.0);
-}
 
 // NC: the components as a compile-time count (4 in 2D, 3 in 1D), so that
 // the components' chains are unrolled side by side and nv stays in registers
@@ -1570,27 +1663,14 @@ __device__ __forceinline__ int rk1d_lane(const Params& p, int stage, const doubl
   if (in_grid && c < 3) {
     double r = 0.0;
     if (interior) r = tod(rhs1d<T>(p, flux, c, o, amd));
-    if (sizeof(T) == 4) {
-      v = fma(dt, r, ld(u + c * P + o));
-      if (stage == 2) v = fma(0.75, u0[c * P + o], 0.25 * v);
-      else if (stage == 3) v = fma(2.0, v, u0[c * P + o]) * (1.0 / 3.0);
-    } else {
-      v = ld(u + c * P + o) + dt * r;
-      if (stage >= 2) v = rk_combine(p, stage, u0[c * P + o], v);
-    }
+    v = rk1d_value<T>(p, stage, dt, r, ld(u + c * P + o), u0 + c * P + o);
     out[c * P + o] = v;
   }
   const int base = threadIdx.x & ~3 & 31;
   const double n0 = __shfl_sync(0xffffffffu, v, base), n1 = __shfl_sync(0xffffffffu, v, base + 1),
                n2 = __shfl_sync(0xffffffffu, v, base + 2);
   int bad = 0;
-  if (interior && c == 0) {
-    double pe;
-    if (sizeof(T) == 4) pe = fma(n1 * n1, -0.5 * rcp_bulk(n0), n2);
-    else pe = n2 - tscale<-1>(tdiv(n1 * n1, n0));
-    if (p.pos_strict) bad = (n0 < p.eps) || (pe < p.eps);
-    else bad = (n0 <= p.eps) || (pe <= p.eps);
-  }
+  if (interior && c == 0) bad = pos1d_bad<T>(p, n0, n1, n2);
   return bad;
 }
 
