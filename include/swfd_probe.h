@@ -3,8 +3,9 @@
  *
  * Not part of the product ABI (include/swfd.h) and with no counterpart in the
  * reference: the benchmark uses the FP64 throughput probe as the denominator
- * of the FP64-pipe roofline, and the tests use the other two to check the
- * FP32-bulk form's reciprocal and conversions against IEEE arithmetic.  The
+ * of the FP64-pipe roofline, and the tests use the others to check the
+ * FP32-bulk form's reciprocal and conversions against IEEE arithmetic and
+ * the persistent kernels' grid barrier's bounded wait.  The
  * kernels run the same device functions as libswfd.so (swfd_device.cuh).
  */
 #ifndef SWFD_PROBE_H
@@ -28,6 +29,12 @@ swfd_status swfd_probe_rcp_bulk(int32_t device, const double* x, int64_t n, doub
  * pipes, for n host values; they must equal the hardware conversions. */
 swfd_status swfd_probe_convert(int32_t device, const double* x, int64_t n, float* out_f,
                                double* out_d);
+/* Test entry point: two blocks of a cooperative launch at the persistent
+ * kernels' grid barrier, the second absent when `absent` is set.  The wait
+ * must end after wait_ms (0 < wait_ms <= 2000) with the timeout bit (64) in
+ * *err_bits, without a fault; *passed counts the blocks that passed it. */
+swfd_status swfd_probe_barrier_timeout(int32_t device, int32_t absent, double wait_ms,
+                                       int32_t* err_bits, int32_t* passed);
 
 #ifdef __cplusplus
 }

@@ -164,6 +164,8 @@ _PROBE_SIGS = {
     "swfd_probe_fp64_peak": (C.c_int32, [C.c_int32, _DP]),
     "swfd_probe_rcp_bulk": (C.c_int32, [C.c_int32, _DP, C.c_int64, _DP]),
     "swfd_probe_convert": (C.c_int32, [C.c_int32, _DP, C.c_int64, C.POINTER(C.c_float), _DP]),
+    "swfd_probe_barrier_timeout": (C.c_int32, [C.c_int32, C.c_int32, C.c_double,
+                                              C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -1,8 +1,11 @@
 // swfd_probe.cu -- FP64 pipe throughput probe.  The FP64 path of this library
 // is bounded by the FP64 pipe, whose peak is not a published constant of
 // this part; this kernel measures it (independent DFMA chains, 8 per thread).
+// Also test entry points: the FP32-bulk reciprocal and conversions, and the
+// persistent kernels' bounded grid barrier.
 #include "swfd_internal.h"
 #include "swfd_device.cuh"
+#include "swfd_gridsync.cuh"
 
 namespace {
 
@@ -33,7 +36,47 @@ __global__ void k_convert(const double* __restrict__ x, float* __restrict__ f,
     d[k] = swfd::f2d(v);
   }
 }
+// two blocks at one grid barrier; with `absent` the second block returns
+// without arriving, so the first one's wait runs out
+__global__ void k_barrier_probe(unsigned* cnt, int* err, int* passed, int absent,
+                                unsigned long long wait_ns) {
+  if (absent && blockIdx.x == 1) return;
+  const bool ok = swfd::grid_barrier(cnt, 1, err, wait_ns);
+  if (threadIdx.x == 0 && ok) atomicAdd(passed, 1);
+}
 }  // namespace
+
+// The persistent kernels' grid barrier with one block absent (or, absent =
+// 0, all present): the wait of the other block must end after wait_ms with
+// ERR_BIT_TIMEOUT in *err_bits and the context stay usable; *passed counts
+// the blocks that passed the barrier.
+extern "C" swfd_status swfd_probe_barrier_timeout(int32_t device, int32_t absent, double wait_ms,
+                                                  int32_t* err_bits, int32_t* passed) {
+  if (!err_bits || !passed || !(wait_ms > 0.0) || wait_ms > 2000.0) return SWFD_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return SWFD_ERR_CUDA;
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) return SWFD_ERR_UNSUPPORTED;
+  int* d = nullptr;
+  if (cudaMalloc(&d, 4 * sizeof(int)) != cudaSuccess) return SWFD_ERR_OOM;
+  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(int));
+  unsigned* cnt = (unsigned*)d;
+  int* err = d + 1;
+  int* pass = d + 2;
+  int ab = absent ? 1 : 0;
+  unsigned long long ns = (unsigned long long)(wait_ms * 1e6);
+  void* args[] = {&cnt, &err, &pass, &ab, &ns};
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(2), dim3(32), args, 0,
+                                    nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, 4 * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  *err_bits = h[1];
+  *passed = h[2];
+  return e == cudaSuccess ? SWFD_OK : SWFD_ERR_CUDA;
+}
 
 // the integer-pipe binary64 -> binary32 -> binary64 conversions of the
 // FP32-bulk kernels on host values, for their bit-exactness test

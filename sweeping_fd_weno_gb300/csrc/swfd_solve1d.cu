@@ -15,57 +15,14 @@
 //
 // Every value is computed by the separate kernels' code (swfd_1d.cuh).
 #include "swfd_1d.cuh"
+#include "swfd_gridsync.cuh"
 
 namespace swfd {
 namespace {
 
 // a grid barrier gives up after 2 s of waiting (the slowest legitimate wait
-// is one stage of the other blocks, microseconds) or 2^24 polls
+// is one stage of the other blocks, microseconds)
 constexpr unsigned long long S1_WAIT_NS = 2000000000ull;
-constexpr long long S1_MAX_POLLS = 1ll << 24;
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
-  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Grid barrier number k (1, 2, ...): every block adds one to *cnt (zero at
-// launch) and waits until it holds k * gridDim.x.  A block whose wait runs
-// out, or that sees another block's timeout, sets ERR_BIT_TIMEOUT and every
-// thread of the block gets false.
-__device__ bool s1_barrier(unsigned* cnt, unsigned k, int* err) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    red_release_add_u32(cnt, 1u);
-    const unsigned target = k * gridDim.x;
-    const unsigned long long t0 = global_ns();
-    int good = 1;
-    for (long long it = 0; (int)(ld_acquire_u32(cnt) - target) < 0; ++it) {
-      if ((it & 63) == 63 &&
-          (global_ns() - t0 > S1_WAIT_NS || it > S1_MAX_POLLS ||
-           (*(volatile int*)err & ERR_BIT_TIMEOUT))) {
-        atomicOr(err, ERR_BIT_TIMEOUT);
-        good = 0;
-        break;
-      }
-    }
-    __threadfence();
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
 
 // maximum over the block (values >= 0) and the OR of the flags, in every thread
 __device__ __forceinline__ void s1_block_reduce(double& v, int& f) {
@@ -170,7 +127,7 @@ __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
         v = fmax(v, fmax(0.0, alpha1d(p, in[q], in[P + q], in[2 * P + q])));
       s1_block_reduce(v, f);
       if (tid == 0) a.parts[par * G + b] = Solve1dPart{v, 0, 0};
-      if (!s1_barrier(a.bar, ++nbar, &dsc->error)) return;
+      if (!grid_barrier(a.bar, ++nbar, &dsc->error, S1_WAIT_NS)) return;
       int unused;
       s1_grid_reduce(a.parts + par * G, am, unused);
       par ^= 1;
@@ -257,7 +214,7 @@ __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
       a.parts[par * G + b] = Solve1dPart{av, bad, 0};
       if (b == 0) dsc->rk_runs[stage]++;
     }
-    if (!s1_barrier(a.bar, ++nbar, &dsc->error)) return;
+    if (!grid_barrier(a.bar, ++nbar, &dsc->error, S1_WAIT_NS)) return;
     int postag;
     s1_grid_reduce(a.parts + par * G, am_next, postag);
     par ^= 1;
