@@ -38,19 +38,25 @@ __device__ __forceinline__ double alpha1d(const Params& p, double u1, double u2,
   return fabs(v) + sound;
 }
 
-// fflux (ex2_sedov_1d/main.f90:57-73) and the split of one cell
-// fp = 0.5 (u + f/alphamax), fn = 0.5 (u - f/alphamax)  (:82-85); the
-// divisions are tdiv's correctly rounded quotients (the hardware's bits)
-template <class T>
-__device__ __forceinline__ void split1d(const Params& p, double rho, double mx, double e,
-                                        double amd, T sp[3], T sn[3]) {
+// fflux (ex2_sedov_1d/main.f90:57-73) of one cell
+__device__ __forceinline__ void fflux1d(const Params& p, double rho, double mx, double e,
+                                        double f[3]) {
   const double g1 = p.gamma1;
   double vx = 0.;
   if (rho > p.lim8_gt) vx = tdiv(mx, rho);
   if (rho <= p.lim8_le) vx = 0.;
   double pres = g1 * (e - 0.5 * rho * (vx * vx));
-  double f[3] = {mx, rho * (vx * vx) + pres, (e + pres) * vx};
-  double a[3] = {rho, mx, e};
+  f[0] = mx;
+  f[1] = rho * (vx * vx) + pres;
+  f[2] = (e + pres) * vx;
+}
+
+// the split of one cell from its state a and fflux f:
+// fp = 0.5 (u + f/alphamax), fn = 0.5 (u - f/alphamax)  (:82-85); the
+// divisions are tdiv's correctly rounded quotients (the hardware's bits)
+template <class T>
+__device__ __forceinline__ void split1d_f(const double a[3], const double f[3], double amd,
+                                          T sp[3], T sn[3]) {
   const T am = T(amd);
   T q[3];
   if constexpr (sizeof(T) == 8) {
@@ -65,6 +71,15 @@ __device__ __forceinline__ void split1d(const Params& p, double rho, double mx, 
     sp[c] = T(0.5) * (T(a[c]) + q[c]);
     sn[c] = T(0.5) * (T(a[c]) - q[c]);
   }
+}
+
+template <class T>
+__device__ __forceinline__ void split1d(const Params& p, double rho, double mx, double e,
+                                        double amd, T sp[3], T sn[3]) {
+  const double a[3] = {rho, mx, e};
+  double f[3];
+  fflux1d(p, rho, mx, e, f);
+  split1d_f<T>(a, f, amd, sp, sn);
 }
 
 // eigenvectors at cell m (ex2_sedov_1d/main.f90:103-133): vxm and hm come
@@ -140,19 +155,20 @@ __device__ __forceinline__ T recon1d(const Params& p, const Eigen1D<T>& E, int s
 
 // output component sub (0..5) of a cell's interface fluxes from its six
 // reconstructions: 0..2 the positive flux evr . ur, 3..5 the negative one
-// evr . ul (:152-157)
+// evr . ul (:152-157); lanes 6 and 7 get a value nobody stores
 template <class T>
 __device__ __forceinline__ T back1d_combine(const Eigen1D<T>& E, T ur0, T ul0, T ur1, T ul1, T ur2,
                                             T ul2, int sub) {
-  switch (sub) {
-    case 0: return ur0 + ur1 + ur2;
-    case 1: return E.r10 * ur0 + E.vxm * ur1 + E.r12 * ur2;
-    case 2: return E.r20 * ur0 + E.qm * ur1 + E.r22 * ur2;
-    case 3: return ul0 + ul1 + ul2;
-    case 4: return E.r10 * ul0 + E.vxm * ul1 + E.r12 * ul2;
-    case 5: return E.r20 * ul0 + E.qm * ul1 + E.r22 * ul2;
-    default: return T(0);
-  }
+  // one instruction stream for the six lanes (a warp pays for every FP64
+  // instruction of every branch its lanes take): the lane's row of evr and
+  // side selected in registers; row 1 is ones, and 1*x is x exactly
+  const int row = sub % 3;
+  const bool neg = sub >= 3;
+  const T a0 = neg ? ul0 : ur0, a1 = neg ? ul1 : ur1, a2 = neg ? ul2 : ur2;
+  const T e0 = row == 0 ? T(1) : row == 1 ? E.r10 : E.r20;
+  const T e1 = row == 0 ? T(1) : row == 1 ? E.vxm : E.qm;
+  const T e2 = row == 0 ? T(1) : row == 1 ? E.r12 : E.r22;
+  return e0 * a0 + e1 * a1 + e2 * a2;
 }
 
 // The group of eight exchanges its six reconstructions by warp shuffles

@@ -883,18 +883,17 @@ bool use_solve1d(swfd_handle* h, Solve1dShape* sh) {
 
 swfd_status run_solve1d(swfd_handle* h, const Solve1dShape& sh, int64_t max_steps,
                         int64_t* nsteps_out) {
-  if (h->s1_grid < sh.grid) {
-    cudaFree(h->s1_parts);
-    h->s1_parts = nullptr;
-    h->s1_grid = 0;
-    CU(h, cudaMalloc(&h->s1_parts, 2 * (size_t)sh.grid * sizeof(Solve1dPart)));
-    h->s1_grid = sh.grid;
-  }
-  if (!h->s1_bar) CU(h, cudaMalloc(&h->s1_bar, sizeof(unsigned)));
+  const size_t pre_bytes = 2 * (size_t)h->p.g.LI * SWFD_SOLVE1D_PRE * sizeof(double);
+  // the ready flags: one per block, at most one block per cell
+  if (!h->s1_scratch)
+    CU(h, cudaMalloc(&h->s1_scratch, pre_bytes + 4 * sizeof(Solve1dSlot) +
+                                         (size_t)h->p.g.LI * sizeof(unsigned)));
   Solve1dArgs a;
   for (int k = 0; k < 3; ++k) a.st[k] = h->st[(h->cur + k) % 3];
-  a.parts = h->s1_parts;
-  a.bar = h->s1_bar;
+  a.pre = (double*)h->s1_scratch;
+  a.slots = (Solve1dSlot*)((char*)h->s1_scratch + pre_bytes);
+  a.bar = (unsigned*)(a.slots + 3);
+  a.ready = (unsigned*)(a.slots + 4);
   a.cells = sh.cells;
   a.sweeps = h->cfg.use_limiter == 2;
   int64_t done = 0;
@@ -1178,8 +1177,7 @@ swfd_status swfd_destroy(swfd_handle* h) {
   cudaFree(h->seg_buf);
   cudaFree(h->rhs_tmp);
   cudaFree(h->m1_wk);
-  cudaFree(h->s1_parts);
-  cudaFree(h->s1_bar);
+  cudaFree(h->s1_scratch);
   cudaFree(h->dsc);
   cudaFree(h->d_stage);
   cudaFree(h->sweep_scratch);

@@ -23,6 +23,31 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// barrier `id` (1..15) of the block's first `nthreads` threads (a multiple of 32)
+__device__ __forceinline__ void bar_named(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Wait (thread 0 of a warp group) until *flag >= v; false when the wait ran
+// out (wait_ns or GRID_BARRIER_MAX_POLLS polls) or another block timed out,
+// with ERR_BIT_TIMEOUT set in *err.
+__device__ __forceinline__ bool wait_flag(const unsigned* flag, unsigned v, int* err,
+                                          unsigned long long wait_ns) {
+  const unsigned long long t0 = global_ns();
+  for (long long it = 0; (int)(ld_acquire_u32(flag) - v) < 0; ++it) {
+    if ((it & 63) == 63 &&
+        (global_ns() - t0 > wait_ns || it > GRID_BARRIER_MAX_POLLS ||
+         (*(volatile int*)err & ERR_BIT_TIMEOUT))) {
+      atomicOr(err, ERR_BIT_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
 // Grid barrier number k (1, 2, ...): every block adds one to *cnt (zero at
 // launch) and waits until it holds k * gridDim.x.  A block whose wait runs
 // out (wait_ns, or GRID_BARRIER_MAX_POLLS polls), or that sees another
@@ -35,22 +60,30 @@ __device__ __forceinline__ bool grid_barrier(unsigned* cnt, unsigned k, int* err
   if (threadIdx.x == 0) {
     __threadfence();
     red_release_add_u32(cnt, 1u);
-    const unsigned target = k * gridDim.x;
-    const unsigned long long t0 = global_ns();
-    int good = 1;
-    for (long long it = 0; (int)(ld_acquire_u32(cnt) - target) < 0; ++it) {
-      if ((it & 63) == 63 &&
-          (global_ns() - t0 > wait_ns || it > GRID_BARRIER_MAX_POLLS ||
-           (*(volatile int*)err & ERR_BIT_TIMEOUT))) {
-        atomicOr(err, ERR_BIT_TIMEOUT);
-        good = 0;
-        break;
-      }
-    }
+    const int good = wait_flag(cnt, k * gridDim.x, err, wait_ns) ? 1 : 0;
     __threadfence();
     ok = good;
   }
   __syncthreads();
+  return ok != 0;
+}
+
+// The same barrier for the block's first `nthreads` threads only (named
+// barrier `id`): the block's other warps go on with work no other block
+// waits for at this barrier.
+__device__ __forceinline__ bool grid_barrier_part(unsigned* cnt, unsigned k, int* err,
+                                                  unsigned long long wait_ns, int id,
+                                                  int nthreads) {
+  __shared__ int ok;
+  bar_named(id, nthreads);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    red_release_add_u32(cnt, 1u);
+    const int good = wait_flag(cnt, k * gridDim.x, err, wait_ns) ? 1 : 0;
+    __threadfence();
+    ok = good;
+  }
+  bar_named(id, nthreads);
   return ok != 0;
 }
 

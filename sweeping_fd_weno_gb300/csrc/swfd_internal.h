@@ -248,15 +248,19 @@ namespace swfd {
 #define SWFD_SOLVE1D_MAX_BLOCK 512
 #define SWFD_SOLVE1D_MIN_CELLS 6
 #define SWFD_SOLVE1D_MAX_CELLS 62
-struct Solve1dPart {  // one block's contribution to a stage's grid reduction
-  double a;           // maximum findalpha term of its cells
-  int bad;            // a cell failed checkpositivity
+struct Solve1dSlot {         // a stage's grid reduction (three rotate)
+  unsigned long long abits;  // maximum findalpha term (bits of a value >= 0)
+  int bad;                   // some cell failed checkpositivity
   int pad;
 };
+// per cell and stage parity: fflux (3 doubles) and the eigenvectors (15)
+#define SWFD_SOLVE1D_PRE 18
 struct Solve1dArgs {
   double* st[3];       // X (the step's start and u0), Y, Z
-  Solve1dPart* parts;  // 2 x grid
+  double* pre;         // 2 x LI x SWFD_SOLVE1D_PRE
+  Solve1dSlot* slots;  // 3, zeroed by the launcher
   unsigned* bar;       // grid-barrier counter (zeroed by the launcher)
+  unsigned* ready;     // per block: the epoch of its published terms (zeroed by the launcher)
   int cells;           // cells per block
   int resume;          // 1: stage 1; 2, 3: that stage after the previous stage's
                        // sweep; 4: the time advance after a stage-3 sweep
@@ -325,11 +329,10 @@ struct swfd_handle {
   double* d_stage = nullptr;  // device, nc * LI * LJ doubles
   // the detonation (ex7) keeps its own rank-sliced state; set only for that problem
   swfd::Ex7* ex7 = nullptr;
-  // the persistent 1D solve: the blocks' alpha and positivity parts (2 x
-  // grid) and its grid-barrier counter, allocated on its first run
-  swfd::Solve1dPart* s1_parts = nullptr;
-  unsigned* s1_bar = nullptr;
-  int s1_grid = 0;
+  // the persistent 1D solve's scratch, allocated on its first run: the
+  // cells' precomputed terms, then the three reduction slots and the
+  // grid-barrier counter
+  void* s1_scratch = nullptr;
 };
 
 namespace swfd {
