@@ -46,16 +46,16 @@ STAGE_BYTES_PER_CELL = (64 + 96 + 96) / 3.0
 # divisions and the square root); with the divisions and the products by
 # 2, 4, 0.25 and 0.5 on the integer pipes (the same bits), 739 (355 DADD,
 # 379 DMUL, 5 DFMA).  Both counted by ncu on the one-lane k_flux_xy<double>;
-# the default kernel, k_flux_xy_loop<5> (two lanes per interface, both form
-# the interface's eigenvectors), executes 780 (374 DADD, 396 DMUL, 10 DFMA;
-# ncu on the 1024x1024 vortex), and 739 stays the work the roofline counts.
+# the default kernel, k_flux_xy_share<5> (two lanes per interface, the
+# eigenvectors formed once per interface and shared), executes 737 (ncu on
+# the 1024x1024 vortex), and 739 stays the work the roofline counts.
 FLUX_FLOPS_PER_INTERFACE = 800 + 50 + 1
 FLUX_FP64_INST_PER_INTERFACE = 739
-FLUX_FP64_INST_PER_INTERFACE_EXECUTED = 780
+FLUX_FP64_INST_PER_INTERFACE_EXECUTED = 737
 FLUX_FP64_INST_PER_INTERFACE_HW_DIV = 1197
-# DRAM bytes of one k_flux_xy_loop<5> launch per interior cell, from an ncu
-# capture of the 1024x1024 vortex (312.0 MB per launch, inputs above L2)
-FLUX_DRAM_BYTES_PER_CELL = 312.0e6 / (1024 * 1024)
+# DRAM bytes of one k_flux_xy_share<5> launch per interior cell, from an ncu
+# capture of the 1024x1024 vortex (313.9 MB per launch, inputs above L2)
+FLUX_DRAM_BYTES_PER_CELL = 313.9e6 / (1024 * 1024)
 # the same for k_flux_xy<float> of the FP32-bulk form's separate kernels
 # (134.4 MB per launch) and for its fused stage kernel k_stage32<256, 4>
 # (107.9 MB per launch)
@@ -1067,11 +1067,12 @@ def main():
         roofline.update({
             "traffic": FLUX_DRAM_BYTES_PER_CELL * cells,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                              "k_flux_xy_loop<5> on the 1024x1024 vortex (312.0 MB), scaled "
+                              "k_flux_xy_share<5> on the 1024x1024 vortex (313.9 MB), scaled "
                               "per cell to this grid",
-            "kernel": "k_flux_xy_loop<5> (characteristic WENO5 interface fluxes, both "
+            "kernel": "k_flux_xy_share<5> (characteristic WENO5 interface fluxes, both "
                       "directions in one code path, two lanes per interface, the fields "
-                      "in a loop; the default FP64 shape)",
+                      "in a loop, each interface's eigenvectors formed once; the default "
+                      "FP64 shape)",
             "compute_bound": "fp64 (the FP64 pipe; divisions and power-of-two products run "
                              "on the integer pipes)",
             "fp64": {"achieved_ginst_per_s": fp64_inst_rate, "peak_ginst_per_s": fp64_peak_inst,

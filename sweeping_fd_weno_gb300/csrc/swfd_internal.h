@@ -429,8 +429,12 @@ long long stage32_items(const Params& p);
 // SWFD_FLUX_LOOP + b: the lane-pair kernel's short form (one code path for both
 // directions, the characteristic fields in a loop)
 #define SWFD_FLUX_LOOP 20
-// the FP64 flux kernel's default shape: the short lane-pair kernel, 5 blocks per SM
-#define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_LOOP + 5)
+// SWFD_FLUX_SHARE + b: the short form with each interface's eigenvectors
+// formed once, by one lane, and shared through shared memory
+#define SWFD_FLUX_SHARE 40
+// the FP64 flux kernel's default shape: the short lane-pair kernel with
+// shared eigenvectors, 5 blocks per SM
+#define SWFD_FLUX_DEFAULT64 (SWFD_FLUX_SHARE + 5)
 int flux_min_blocks_candidates(bool f32, int* out);
 cudaError_t launch_batch_time_advance(const BatchLaunch& b, cudaStream_t s);
 cudaError_t launch_batch_run_cond(cudaGraphConditionalHandle h, const BatchLaunch& b, int advance,

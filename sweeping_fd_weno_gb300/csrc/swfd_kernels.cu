@@ -1344,6 +1344,123 @@ __global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
   }
 }
 
+// The short lane-pair kernel with each interface's eigenvectors formed once:
+// a warp takes 32 interfaces of one direction, each lane forms one
+// interface's Roe eigenvectors into shared memory, then the lane pairs
+// reconstruct the interfaces in two rounds of 16 (lane 0 of a pair the
+// positive split flux, lane 1 the negative one), reading the eigenvectors
+// back.  About 40 FP64 instructions fewer per interface than forming them
+// in both lanes; every value is k_flux_xy_loop's.
+constexpr int EIG2D_N = 19;  // the Eigen2D entries the reconstruction uses
+__device__ __forceinline__ void eig2d_store(const Eigen2D<double>& E, double* s) {
+  const double v[EIG2D_N] = {E.vn,   E.vt,   E.qm,   E.e_nm, E.e_np, E.e_hm, E.e_hp,
+                             E.l1_0, E.l1_n, E.l1_t, E.l1_3, E.l3_0, E.l3_n, E.l3_t,
+                             E.l3_3, E.l4_0, E.l4_n, E.l4_t, E.l4_3};
+#pragma unroll
+  for (int k = 0; k < EIG2D_N; ++k) s[32 * k] = v[k];
+}
+__device__ __forceinline__ void eig2d_load(Eigen2D<double>& E, const double* s) {
+  double v[EIG2D_N];
+#pragma unroll
+  for (int k = 0; k < EIG2D_N; ++k) v[k] = s[32 * k];
+  E.vn = v[0], E.vt = v[1], E.qm = v[2], E.e_nm = v[3], E.e_np = v[4], E.e_hm = v[5];
+  E.e_hp = v[6], E.l1_0 = v[7], E.l1_n = v[8], E.l1_t = v[9], E.l1_3 = v[10];
+  E.l3_0 = v[11], E.l3_n = v[12], E.l3_t = v[13], E.l3_3 = v[14], E.l4_0 = v[15];
+  E.l4_n = v[16], E.l4_t = v[17], E.l4_3 = v[18];
+  E.cm = 0.0;  // not used by the reconstruction
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(SWFD_FLUX_BLOCK, MINB)
+    k_flux_xy_share(Params p, const double* __restrict__ split, const double* __restrict__ roe,
+                    const DevScalars* dsc, double* __restrict__ flux, int* __restrict__ work) {
+  __shared__ double sE[SWFD_FLUX_BLOCK / 32][EIG2D_N * 32];
+  const Geom& g = p.g;
+  const int64_t fx = flux_faces_x(p), fy = flux_faces_y(p);
+  const int64_t chunks_x = (fx + 31) / 32;
+  const int64_t chunks = chunks_x + (fy + 31) / 32;
+  const int lane = threadIdx.x & 31, side = lane & 1;
+  double* se = sE[threadIdx.x >> 5];
+  const double am = p.alpha_premul ? dsc->alphamax : 1.0;
+  const int64_t P = g.plane, S = p.sg.plane, spit = p.sg.pitch;
+  const double g1 = p.gamma1, weps = p.weno_eps;
+  const int lx = p.nxl + 2;  // x faces i = 0..nx+1 of rows 1..ny (one segment)
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(work, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= chunks) break;
+    // 32 interfaces of one direction: t0 .. t0 + 31
+    const int ydir = c < chunks_x ? 0 : 1;
+    const int64_t t0 = ydir ? ((int64_t)c - chunks_x) * 32 : (int64_t)c * 32;
+    const int64_t nfaces = ydir ? fy : fx;
+    const int64_t rnb = ydir ? g.pitch : 1, step = ydir ? spit : 1;
+    const double* rb = ydir ? roe + (p.roe_reg_ex4 ? 4 * P : 0) : roe;
+    auto offset = [&](int64_t t) {
+      return ydir ? g.at((int)t % g.nx + 1, (int)t / g.nx) : g.at((int)t % lx, (int)t / lx + 1);
+    };
+    {  // the eigenvectors of interface t0 + lane
+      const int64_t t = t0 + lane;
+      if (t < nfaces) {
+        const int64_t o = offset(t);
+        Eigen2D<double> E;
+        roe_eigen2d<double>(g1, ydir, ldt(rb + o), ldt(rb + o + rnb), ldt(rb + P + o),
+                            ldt(rb + P + o + rnb), ldt(rb + 2 * P + o),
+                            ldt(rb + 2 * P + o + rnb), ldt(rb + 3 * P + o),
+                            ldt(rb + 3 * P + o + rnb), E);
+        eig2d_store(E, se + lane);
+      }
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {  // interfaces t0 + 16 h + lane / 2, two lanes each
+      const int j = 16 * h + (lane >> 1);
+      const int64_t t = t0 + j;
+      if (t < nfaces) {
+        const int64_t o = offset(t);
+        Eigen2D<double> E;
+        eig2d_load(E, se + j);
+        const int64_t pl = 8 * ydir + 4 * side;  // the side's first split and flux plane
+        const double* s = split + pl * S + o - 2 * step;
+        double o0, on, ot, o3;
+        int bad = 0;
+        weno4_side_loop(E, ydir, s, S, step, weps, side, DivFlag{&bad}, o0, on, ot, o3);
+        if (bad) {
+          const Side4 r = weno4_side_loop_hw(E, ydir, s, S, step, weps, side);
+          o0 = r.v[0], on = r.v[1], ot = r.v[2], o3 = r.v[3];
+        }
+        double* f = flux + pl * S + o;
+        const int64_t fn = ydir ? 2 * S : S, ft = ydir ? S : 2 * S;
+        f[0] = p.alpha_premul ? am * o0 : o0;
+        f[fn] = p.alpha_premul ? am * on : on;
+        f[ft] = p.alpha_premul ? am * ot : ot;
+        f[3 * S] = p.alpha_premul ? am * o3 : o3;
+      }
+    }
+    __syncwarp();  // the next chunk rewrites se
+  }
+  if (lane == 0) {  // as k_flux_xy: the last warp out re-arms both counters
+    __threadfence();
+    if (atomicAdd(work + 1, 1) == (int)(gridDim.x * (blockDim.x >> 5)) - 1) {
+      atomicExch(work, 0);
+      atomicExch(work + 1, 0);
+    }
+  }
+}
+
+template <int MINB>
+static int flux_grid_share() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flux_xy_share<MINB>, SWFD_FLUX_BLOCK, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  return grid;
+}
+
 template <int MINB>
 static int flux_grid_loop() {
   static int grid = 0;
@@ -1381,13 +1498,15 @@ int flux_min_blocks_candidates(bool f32, int* out) {
     out[0] = 4, out[1] = 5, out[2] = 6;
     return 3;
   }
-  // FP64: the short lane-pair kernel (SWFD_FLUX_LOOP + 5 blocks per SM, the
-  // default; + 4), the unrolled lane-pair kernel (SWFD_FLUX_PAIR + 3..6) and
-  // the one-lane kernel (3, 2, 4 blocks per SM)
-  out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_LOOP + 4, out[2] = SWFD_FLUX_PAIR + 4;
-  out[3] = SWFD_FLUX_PAIR + 3, out[4] = SWFD_FLUX_PAIR + 5, out[5] = SWFD_FLUX_PAIR + 6;
-  out[6] = 3, out[7] = 2, out[8] = 4;
-  return 9;
+  // FP64: the short lane-pair kernel with shared eigenvectors
+  // (SWFD_FLUX_SHARE + 5 blocks per SM, the default; + 4), without
+  // (SWFD_FLUX_LOOP + 5, + 4), the unrolled lane-pair kernel
+  // (SWFD_FLUX_PAIR + 3..6) and the one-lane kernel (3, 2, 4 blocks per SM)
+  out[0] = SWFD_FLUX_DEFAULT64, out[1] = SWFD_FLUX_SHARE + 4, out[2] = SWFD_FLUX_LOOP + 5;
+  out[3] = SWFD_FLUX_LOOP + 4, out[4] = SWFD_FLUX_PAIR + 4, out[5] = SWFD_FLUX_PAIR + 3;
+  out[6] = SWFD_FLUX_PAIR + 5, out[7] = SWFD_FLUX_PAIR + 6, out[8] = 3, out[9] = 2;
+  out[10] = 4;
+  return 11;
 }
 
 template <class T, int MINB>
@@ -1419,8 +1538,9 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       return;
     }
   }
-  // the FP64 default shape is the short lane-pair kernel with 5 blocks per
-  // SM (SWFD_FLUX_DEFAULT64); flux_minb 3 selects the one-lane kernel's default
+  // the FP64 default shape is the short lane-pair kernel with shared
+  // eigenvectors, 5 blocks per SM (SWFD_FLUX_DEFAULT64); flux_minb 3 selects
+  // the one-lane kernel's default
   int minb = p.flux_minb;
   if constexpr (sizeof(T) == 8)
     if (!minb) minb = SWFD_FLUX_DEFAULT64;
@@ -1446,6 +1566,14 @@ static void launch_flux_xy(const Params& p, const void* split, const void* roe,
       SWFD_LOOP_CASE(4)
       SWFD_LOOP_CASE(5)
 #undef SWFD_LOOP_CASE
+#define SWFD_SHARE_CASE(M)                                                                     \
+  if (minb == SWFD_FLUX_SHARE + M) {                                                           \
+    k_flux_xy_share<M><<<flux_grid_share<M>(), SWFD_FLUX_BLOCK, 0, s>>>(p, sp, rp, dsc, fp, work); \
+    return;                                                                                    \
+  }
+      SWFD_SHARE_CASE(4)
+      SWFD_SHARE_CASE(5)
+#undef SWFD_SHARE_CASE
     } else {
       if (minb == 5) return launch_flux_minb<T, 5>(p, sp, rp, dsc, fp, work, s);
       if (minb == 6) return launch_flux_minb<T, 6>(p, sp, rp, dsc, fp, work, s);

@@ -18,8 +18,8 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, monkeypatch, precision):
     for s in (a, b):
         s.init_problem()
     minb = b.autotune()
-    assert minb in ((3, 2, 4, 13, 14, 15, 16, 24, 25) if precision == abi.PRECISION_FP64
-                    else (4, 5, 6))
+    assert minb in ((3, 2, 4, 13, 14, 15, 16, 24, 25, 44, 45)
+                    if precision == abi.PRECISION_FP64 else (4, 5, 6))
     for _ in range(4):
         assert a.step() == b.step()
     assert np.array_equal(a.state(), b.state())
@@ -29,12 +29,14 @@ def test_flux_launch_shape_tuning_keeps_results(swfd, monkeypatch, precision):
 
 # FP64 13..16: the lane-pair flux kernel (two lanes per interface) with 3..6
 # resident blocks per SM; 24, 25: its short form (one code path for both
-# directions, the fields in a loop) with 4, 5
+# directions, the fields in a loop) with 4, 5; 44, 45: the short form with
+# each interface's eigenvectors formed once and shared
 @pytest.mark.parametrize("precision,minb", [(abi.PRECISION_FP64, 2), (abi.PRECISION_FP64, 3),
                                             (abi.PRECISION_FP64, 4),
                                             (abi.PRECISION_FP64, 13), (abi.PRECISION_FP64, 14),
                                             (abi.PRECISION_FP64, 15), (abi.PRECISION_FP64, 16),
                                             (abi.PRECISION_FP64, 24), (abi.PRECISION_FP64, 25),
+                                            (abi.PRECISION_FP64, 44), (abi.PRECISION_FP64, 45),
                                             (abi.PRECISION_FP32_BULK, 5),
                                             (abi.PRECISION_FP32_BULK, 6)])
 def test_each_flux_launch_shape_keeps_results(swfd, monkeypatch, precision, minb):
@@ -86,13 +88,14 @@ def test_batch_tile_tuning_keeps_results(swfd, precision):
         assert np.array_equal(ua, ub)
 
 
-@pytest.mark.parametrize("minb", [3, 14, 16, 24, 25])
+@pytest.mark.parametrize("minb", [3, 14, 16, 24, 25, 44, 45])
 @pytest.mark.parametrize("case", [dict(problem=abi.SEDOV_2D, nx=48, ny=40),
                                   dict(problem=abi.JET_2D, nx=96, ny=24)],
                          ids=["point_energy", "jet"])
 def test_lane_pair_flux_kernel_matches_the_oracle(swfd, oracle_mod, monkeypatch, minb, case):
     """The FP64 flux kernels (3: one lane per interface; 14, 16: the lane-pair
-    kernel; 24, 25: its short form, the default 25) on the ex4 form (alpha
+    kernel; 24, 25: its short form; 44, 45: the short form with shared
+    eigenvectors, the default 45) on the ex4 form (alpha
     pre-multiplied, y-pass regulariser planes) and the ex5 form, against the
     oracle's steps."""
     monkeypatch.setenv("SWFD_FLUX_MIN_BLOCKS", str(minb))
