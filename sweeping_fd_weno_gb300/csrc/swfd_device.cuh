@@ -63,6 +63,21 @@ struct DivFlag {
     return sd::div_nf(a, b, *bad);
   }
 };
+// a / b with tdiv's bits and no branch for the common operands: a zero
+// dividend over a normal divisor gives the signed zero inline (the state at
+// rest has zero momenta); other operands or quotients outside sd::div_nf's
+// range set bad, and the caller redoes its divisions with tdiv.  Independent
+// divisions in straight-line code interleave, where tdiv's fallback branch
+// would run them one after another.
+__device__ __forceinline__ double div_nfz(double a, double b, int& bad) {
+  int out = 0;
+  const double q = sd::div_nf(a, b, out);
+  const uint64_t ua = sd::dbits(a), ub = sd::dbits(b);
+  const bool z = (ua << 1) == 0 && ((uint32_t)(ub >> 52) & 0x7ffu) - 1u < 2046u;
+  bad |= z ? 0 : out;
+  return z ? sd::dfrom((ua ^ ub) & 0x8000000000000000ull) : q;
+}
+
 // x * 2^K.  Binary64: sd::scale, an addition to the exponent field (the bits
 // of the hardware product).  Binary32: the product.
 template <int K>

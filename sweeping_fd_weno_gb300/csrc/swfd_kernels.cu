@@ -155,22 +155,32 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
     } else {
       double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o),
              u4 = ldc<NC>(u + 3 * g.plane + o);
+      // the first quotients straight-line (they interleave), tdiv's fallback
+      // for the rare operand
+      int bad = 0;
+      double q2 = div_nfz(u2, u1, bad), q3 = div_nfz(u3, u1, bad);
       if (!p.alpha_guarded) {
         // ex3_vortex_accuracy_2d/main.f90:556-559
-        double pres = g1 * (u4 - tscale<-1>(tdiv(u2 * u2, u1)) - tscale<-1>(tdiv(u3 * u3, u1)));
+        double k2 = div_nfz(u2 * u2, u1, bad), k3 = div_nfz(u3 * u3, u1, bad);
+        if (bad) {
+          q2 = tdiv(u2, u1), q3 = tdiv(u3, u1);
+          k2 = tdiv(u2 * u2, u1), k3 = tdiv(u3 * u3, u1);
+        }
+        double pres = g1 * (u4 - tscale<-1>(k2) - tscale<-1>(k3));
         double sound = sqrt(tdiv(gamma * pres, u1));
-        a = fmax(fabs(tdiv(u2, u1)) + sound, fabs(tdiv(u3, u1)) + sound);
+        a = fmax(fabs(q2) + sound, fabs(q3) + sound);
       } else {
         // ex5_mach2000_jet/main.f90:571-584
+        if (bad) q2 = tdiv(u2, u1), q3 = tdiv(u3, u1);
         double vx = 0., vy = 0.;
         if (u1 >= p.eps2) {
-          vx = tdiv(u2, u1);
-          vy = tdiv(u3, u1);
+          vx = q2;
+          vy = q3;
         }
         const double hu1 = tscale<-1>(u1);
         double pres = g1 * (u4 - hu1 * (vx * vx) - hu1 * (vy * vy));
         double sound = sqrt(tdiv(gamma * pres, u1));
-        a = fmax(fabs(tdiv(u2, u1)) + sound, fabs(tdiv(u3, u1)) + sound);
+        a = fmax(fabs(q2) + sound, fabs(q3) + sound);
       }
     }
     a = fmax(0.0, a);
