@@ -5,13 +5,16 @@
 // graph kernels per stage (findalpha, splitting, fluxes, RK stage) its time
 // is the kernels' launch and drain latencies.  Here a cooperative grid of
 // one block per SM runs the whole time loop.  Each block owns a contiguous
-// range of cells and, per stage, computes in shared memory the split fluxes
-// of its range plus a three-cell halo, the interface fluxes of its range
-// plus one, the RK stage of its own cells, their positivity and their
-// findalpha term for the next stage; one grid barrier per stage then makes
-// the stage's state, the maximum alpha and the positivity flag visible to
-// every block.  A stage whose state fails checkpositivity ends the launch:
-// the host runs sweep_lim on it and launches again at the next stage.
+// range of cells.  Per stage it splits its range plus a three-cell halo in
+// shared memory (dividing the stored fflux of each cell by the new
+// alphamax), forms the interface fluxes of its range plus one on each side
+// (reading the stored eigenvectors), and the RK stage of its own cells;
+// then, on four warps side by side, checkpositivity and the next findalpha
+// term (folded into the grid reduction, then the grid barrier) and the
+// eigenvectors and fflux of its cells' new state (stored for the next stage,
+// published to the neighbours by the block's ready flag).  A stage whose
+// state fails checkpositivity ends the launch: the host runs sweep_lim on
+// it and launches again at the next stage.
 //
 // Every value is computed by the separate kernels' code (swfd_1d.cuh).
 #include "swfd_1d.cuh"
