@@ -123,7 +123,9 @@ __device__ __forceinline__ double block_max(double v) {
   return v;
 }
 
-template <bool NC = true>
+// F32: the FP32-bulk 2D form only (the fused FP32 kernels), so that the
+// other forms' code -- and its registers -- stay out of those kernels
+template <bool NC = true, bool F32 = false>
 __device__ __forceinline__ double alpha_cell(const Params& p, const double* __restrict__ u,
                                              int64_t t) {
   const Geom& g = p.g;
@@ -133,10 +135,10 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
     int i = ((int)t % g.LI) - 2, j = ((int)t / g.LI) - 2;
     int64_t o = g.at(i, j);
     const double g1 = p.gamma1, gamma = p.gamma;
-    if (g.ndim == 1) {
+    if (!F32 && g.ndim == 1) {
       // ex2_sedov_1d/main.f90:278-283
       a = alpha1d(p, ldc<NC>(u + o), ldc<NC>(u + g.plane + o), ldc<NC>(u + 2 * g.plane + o));
-    } else if (p.precision == SWFD_PRECISION_FP32_BULK) {
+    } else if (F32 || p.precision == SWFD_PRECISION_FP32_BULK) {
       // FP32-bulk: the pressure recovered in FP64 (one reciprocal per cell);
       // the CFL quantities (velocities, sound speed, their max) in FP32
       double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o),
@@ -152,7 +154,7 @@ __device__ __forceinline__ double alpha_cell(const Params& p, const double* __re
       const float fri = d2f(ri);
       const float sound = sqrtf(d2f(gamma) * d2f(pres) * fri);
       a = f2d(fmaxf(fabsf(d2f(u2) * fri), fabsf(d2f(u3) * fri)) + sound);
-    } else {
+    } else if constexpr (!F32) {
       double u1 = ldc<NC>(u + o), u2 = ldc<NC>(u + g.plane + o), u3 = ldc<NC>(u + 2 * g.plane + o),
              u4 = ldc<NC>(u + 3 * g.plane + o);
       // the first quotients straight-line (they interleave), tdiv's fallback
@@ -1896,7 +1898,7 @@ __global__ void k_alpha_terms32(Params p, double* __restrict__ u, DevScalars* ds
                                 float* __restrict__ terms, float* __restrict__ roe) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (BC) bc2d_cell(p, u, t);
-  double a = alpha_cell<!BC>(p, u, t);
+  double a = alpha_cell<!BC, true>(p, u, t);
   terms32_cell<!BC>(p, u, terms, roe, t);
   a = block_max(a);
   if (threadIdx.x != 0) return;
@@ -2544,7 +2546,7 @@ __global__ void kb_alpha_terms32(const BatchSlot* __restrict__ tab,
     const long long c0 = (k - tp[s]) * tc, c1 = min(c0 + tc, sl.ncell);
     double a = 0.0;
     for (long long t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
-      a = fmax(a, alpha_cell(sl.p, sl.st[in], t));
+      a = fmax(a, alpha_cell<true, true>(sl.p, sl.st[in], t));
       terms32_cell<true>(sl.p, sl.st[in], (float*)sl.split, (float*)sl.roe, t);
     }
     a = block_max(a);
