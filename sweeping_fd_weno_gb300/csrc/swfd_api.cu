@@ -875,7 +875,7 @@ swfd_status finish_pending(swfd_handle* h) {
 // (the conditions read on the host) and the next launch resumes at the
 // following stage.  SWFD_SOLVE1D=graph keeps the graph kernels.
 bool use_solve1d(swfd_handle* h, Solve1dShape* sh) {
-  if (h->cfg.rk_choice == 2) return false;
+  if (h->cfg.rk_choice == 2 || h->s1_refused) return false;
   const char* env = getenv("SWFD_SOLVE1D");
   if (env && strcmp(env, "graph") == 0) return false;
   return solve1d_shape(h->p, sh);
@@ -912,7 +912,16 @@ swfd_status run_solve1d(swfd_handle* h, const Solve1dShape& sh, int64_t max_step
     CU(h, cudaMemsetAsync(&h->dsc->steps, 0, sizeof(long long), h->stream));
     a.resume = 1;
     for (;;) {
-      CU(h, launch_solve1d(h->p, sh, a, h->dsc, h->stream));
+      const cudaError_t le = launch_solve1d(h->p, sh, a, h->dsc, h->stream);
+      if (le == cudaErrorCooperativeLaunchTooLarge && done == 0 && a.resume == 1) {
+        // the grid cannot be resident at once here (another context holds
+        // SMs): nothing ran; the caller takes the graph kernels
+        cudaGetLastError();
+        h->s1_refused = 1;
+        if (nsteps_out) *nsteps_out = 0;
+        return SWFD_OK;
+      }
+      CU(h, le);
       h->prof.kernel_launches += 1;
       st = check_device_error(h);
       const int pause = h->hsc->solve_pause;
@@ -1467,7 +1476,10 @@ swfd_status swfd_run(swfd_handle* h, int64_t max_steps, int64_t* nsteps_out) {
   }
   {
     Solve1dShape sh;
-    if (use_solve1d(h, &sh)) return run_solve1d(h, sh, max_steps, nsteps_out);
+    if (use_solve1d(h, &sh)) {
+      const swfd_status s1 = run_solve1d(h, sh, max_steps, nsteps_out);
+      if (!h->s1_refused) return s1;
+    }
   }
   ST(build_graph(h, GRAPH_SOLVE, &h->g_solve));
   int64_t done = 0;

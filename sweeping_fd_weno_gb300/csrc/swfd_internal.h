@@ -333,6 +333,7 @@ struct swfd_handle {
   // cells' precomputed terms, then the three reduction slots and the
   // grid-barrier counter
   void* s1_scratch = nullptr;
+  int s1_refused = 0;  // the device refused the cooperative grid: graph kernels from then on
 };
 
 namespace swfd {
