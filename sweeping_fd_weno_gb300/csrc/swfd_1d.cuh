@@ -53,10 +53,20 @@ __device__ __forceinline__ void split1d_f(const double a[3], const double f[3], 
   } else {
     for (int c = 0; c < 3; ++c) q[c] = tdiv(T(f[c]), am);
   }
-  for (int c = 0; c < 3; ++c) {
-    sp[c] = T(0.5) * (T(a[c]) + q[c]);
-    sn[c] = T(0.5) * (T(a[c]) - q[c]);
+  for (int c = 0; c < 3; ++c) {  // 0.5d0* as an exponent shift (tscale): the same values
+    sp[c] = tscale<-1>(T(a[c]) + q[c]);
+    sn[c] = tscale<-1>(T(a[c]) - q[c]);
   }
+}
+
+// one component of split1d_f (binary64): the same values, one division
+__device__ __forceinline__ void split1d_one(double u, double f, double amd, double& sp,
+                                            double& sn) {
+  int bad = 0;
+  double q = div_nfz(f, amd, bad);
+  if (bad) q = tdiv(f, amd);
+  sp = tscale<-1>(u + q);
+  sn = tscale<-1>(u - q);
 }
 
 template <class T>
@@ -95,9 +105,10 @@ __device__ __forceinline__ void eigen1d(double g1d, double u1, double u2, double
   t0 = vxm * rcm;
   T t1 = b1 * vxm;
   T t2 = tscale<-1>(b1);
-  E.L[0][0] = tscale<-1>(b2 + t0), E.L[0][1] = -tscale<-1>(t1 + rcm), E.L[0][2] = t2;
-  E.L[1][0] = T(1.) - b2, E.L[1][1] = t1, E.L[1][2] = -b1;
-  E.L[2][0] = tscale<-1>(b2 - t0), E.L[2][1] = -tscale<-1>(t1 - rcm), E.L[2][2] = t2;
+  // (-0.5)*x == -(0.5*x); the negations as sign flips (tneg)
+  E.L[0][0] = tscale<-1>(b2 + t0), E.L[0][1] = tneg(tscale<-1>(t1 + rcm)), E.L[0][2] = t2;
+  E.L[1][0] = T(1.) - b2, E.L[1][1] = t1, E.L[1][2] = tneg(b1);
+  E.L[2][0] = tscale<-1>(b2 - t0), E.L[2][1] = tneg(tscale<-1>(t1 - rcm)), E.L[2][2] = t2;
 }
 
 static __device__ __noinline__ double weno_side_hw(double v0, double v1, double v2, double v3,
@@ -157,16 +168,90 @@ __device__ __forceinline__ T back1d_combine(const Eigen1D<T>& E, T ur0, T ul0, T
   return e0 * a0 + e1 * a1 + e2 * a2;
 }
 
-// The group of eight exchanges its six reconstructions by warp shuffles
-// (every lane of the warp takes part; groups are eight aligned lanes) and
-// lane sub 0..5 returns output component sub
-template <class T>
+// The group of G (8 or 16) aligned lanes exchanges its six reconstructions
+// by warp shuffles (every lane of the warp takes part): reconstruction m
+// (field m/2, side m%2) is on lane m * G/8 of the group, and lane sub 0..5
+// returns output component sub
+template <class T, int G = 8>
 __device__ __forceinline__ T back1d(const Eigen1D<T>& E, T v, int sub) {
-  const int base = threadIdx.x & ~7 & 31;
-  const T ur0 = __shfl_sync(0xffffffffu, v, base + 0), ul0 = __shfl_sync(0xffffffffu, v, base + 1);
-  const T ur1 = __shfl_sync(0xffffffffu, v, base + 2), ul1 = __shfl_sync(0xffffffffu, v, base + 3);
-  const T ur2 = __shfl_sync(0xffffffffu, v, base + 4), ul2 = __shfl_sync(0xffffffffu, v, base + 5);
+  static_assert(G == 8 || G == 16, "groups of eight or sixteen lanes");
+  constexpr int S = G / 8;
+  const int base = threadIdx.x & ~(G - 1) & 31;
+  const T ur0 = __shfl_sync(0xffffffffu, v, base + 0 * S);
+  const T ul0 = __shfl_sync(0xffffffffu, v, base + 1 * S);
+  const T ur1 = __shfl_sync(0xffffffffu, v, base + 2 * S);
+  const T ul1 = __shfl_sync(0xffffffffu, v, base + 3 * S);
+  const T ur2 = __shfl_sync(0xffffffffu, v, base + 4 * S);
+  const T ul2 = __shfl_sync(0xffffffffu, v, base + 5 * S);
   return back1d_combine(E, ur0, ul0, ur1, ul1, ur2, ul2, sub);
+}
+
+// The persistent solve's reconstruction: sixteen lanes per flux cell, two
+// per reconstruction.  The pair u = sub/2 (u < 6) reconstructs field u/2 of
+// side u%2 as recon1d's lane u does (pairs 6 and 7 repeat pairs 0 and 1);
+// each lane of the pair takes part of weno_side's operations, so the warp
+// issues ~50 FP64 instructions for a reconstruction instead of ~80.  Lane 0
+// of the pair projects the stencil values v2..v4 and forms the candidate of
+// v2..v4 with its smoothness indicator and weight; lane 1 projects v0..v2
+// and does the same for the candidate of v0..v2; both form the middle
+// candidate and weight from v1..v3 (one value from the partner), the sum of
+// the weights and the normalised terms; lane 0 adds the partner's term and
+// returns the reconstruction.  Every operation, operand and order is
+// weno_side's (weno5.f90:86-146), so the value equals recon1d's.
+template <class SP>
+__device__ __forceinline__ double recon1d_pair(const Params& p, const Eigen1D<double>& E, int sub,
+                                               SP sp) {
+  const double eps = p.weno_eps;
+  const int u = sub >> 1, h = sub & 1;
+  const int k = u < 6 ? u >> 1 : 0, side = u & 1;
+  const double l0 = k == 0 ? E.L[0][0] : k == 1 ? E.L[1][0] : E.L[2][0];
+  const double l1 = k == 0 ? E.L[0][1] : k == 1 ? E.L[1][1] : E.L[2][1];
+  const double l2 = k == 0 ? E.L[0][2] : k == 1 ? E.L[1][2] : E.L[2][2];
+  const int j0 = h ? 0 : 2;
+  double c[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    c[i] = l0 * sp(side, 0, j0 + i) + l1 * sp(side, 1, j0 + i) + l2 * sp(side, 2, j0 + i);
+  // the partner's middle value: v1 on lane 0, v3 on lane 1
+  const double o = __shfl_xor_sync(0xffffffffu, c[1], 1);
+  const double v1 = h ? c[1] : o, v2 = h ? c[2] : c[0], v3 = h ? o : c[1];
+  const bool l = side != 0;
+  // the lane's own candidate: A = a1 v2 + a2 v3 + a3 v4 (lane 0) or
+  // C = c1 v0 + c2 v1 + c3 v2 (lane 1), weno_side's constants
+  const double k1 = h ? (l ? SWFD_CM16 : SWFD_C13) : (l ? SWFD_C116 : SWFD_C13);
+  const double k2 = h ? (l ? SWFD_C56 : SWFD_CM76) : (l ? SWFD_CM76 : SWFD_C56);
+  const double k3 = h ? (l ? SWFD_C13 : SWFD_C116) : (l ? SWFD_C13 : SWFD_CM16);
+  const double P = k1 * c[0] + k2 * c[1] + k3 * c[2];
+  // its smoothness indicator (weno_beta): beta1 of v2..v4 on lane 0, beta3
+  // of v0..v2 on lane 1; s is the same form, t1 = 3 v2 - 4 v3 + v4 and
+  // t3 = v0 - 4 v1 + 3 v2
+  const double c1312 = 13.0 / 12.0;
+  const double s = c[0] - tscale<1>(c[1]) + c[2];
+  const double m3 = 3.0 * (h ? c[2] : c[0]);
+  const double t = (h ? c[0] : m3) - tscale<2>(c[1]) + (h ? m3 : c[2]);
+  const double bP = c1312 * tsq(s) + tscale<-2>(tsq(t));
+  // the middle candidate B and beta2 of v1..v3, on both lanes
+  const double b1 = l ? SWFD_C13 : SWFD_CM16, b3 = l ? SWFD_CM16 : SWFD_C13;
+  const double B = b1 * v1 + SWFD_C56 * v2 + b3 * v3;
+  const double s2 = v1 - tscale<1>(v2) + v3, t2 = v1 - v3;
+  const double bB = c1312 * tsq(s2) + tscale<-2>(tsq(t2));
+  int bad = 0;
+  const DivFlag dv{&bad};
+  const double dP = h ? (l ? 0.3 : 0.1) : (l ? 0.1 : 0.3);
+  const double wP = dv(dP, tsq(eps + bP));
+  const double w2 = dv(0.6, tsq(eps + bB));
+  const double ow = __shfl_xor_sync(0xffffffffu, wP, 1);
+  const double w1 = h ? ow : wP, w3 = h ? wP : ow;
+  const double sum = w1 + w2 + w3;
+  const double tP = dv(wP, sum) * P;
+  const double s12 = tP + dv(w2, sum) * B;  // lane 0: w1/sum * A + w2/sum * B
+  const double oP = __shfl_xor_sync(0xffffffffu, tP, 1);
+  double v = s12 + oP;  // lane 0: + w3/sum * C
+  if (__any_sync(0xffffffffu, bad)) {  // a quotient outside sd::div's range: hardware division
+    const double y0 = __shfl_xor_sync(0xffffffffu, c[0], 1);
+    if (h == 0) v = weno_side_hw(y0, v1, c[0], c[1], c[2], side, eps);
+  }
+  return v;
 }
 
 // use_limiter = 1 (ex2_sedov_1d/main.f90:159-245): the positivity limiter
@@ -213,15 +298,15 @@ __device__ __forceinline__ void count_limited(unsigned long long* cnt, int nd, i
   if (np) atomicAdd(cnt + 1, (unsigned long long)np);
 }
 
-// The limiter on a cell's two reconstructed split fluxes, after back1d:
-// lane 0 of the group limits hp_flux (its three components from lanes 0..2),
+// The limiter on a cell's two reconstructed split fluxes, after back1d (a
+// group of G lanes): lane 0 of the group limits hp_flux (its three components from lanes 0..2),
 // lane 3 hn_flux (lanes 3..5); ave(side, c) is the split value at cell m.
 // Every lane of the warp takes part; lanes 0 and 3 return true with w, the
 // side's limited components, and add their limitings to nd, np.
-template <class T, class AV>
+template <class T, int G = 8, class AV>
 __device__ __forceinline__ bool limit1d_group(const Params& p, T r, int sub, AV ave, T w[3],
                                               int& nd, int& np) {
-  const int base = (threadIdx.x & ~7 & 31) + (sub >= 3 ? 3 : 0);
+  const int base = (threadIdx.x & ~(G - 1) & 31) + (sub >= 3 ? 3 : 0);
 #pragma unroll
   for (int c = 0; c < 3; ++c) w[c] = __shfl_sync(0xffffffffu, r, base + c);
   if (sub != 0 && sub != 3) return false;

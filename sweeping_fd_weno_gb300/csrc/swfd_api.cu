@@ -884,16 +884,18 @@ bool use_solve1d(swfd_handle* h, Solve1dShape* sh) {
 swfd_status run_solve1d(swfd_handle* h, const Solve1dShape& sh, int64_t max_steps,
                         int64_t* nsteps_out) {
   const size_t pre_bytes = 2 * (size_t)h->p.g.LI * SWFD_SOLVE1D_PRE * sizeof(double);
-  // the ready flags: one per block, at most one block per cell
+  // the reduction words (three per block) and the ready flags (one per
+  // block), at most one block per cell
+  const size_t LI = (size_t)h->p.g.LI;
   if (!h->s1_scratch)
-    CU(h, cudaMalloc(&h->s1_scratch, pre_bytes + 4 * sizeof(Solve1dSlot) +
-                                         (size_t)h->p.g.LI * sizeof(unsigned)));
+    CU(h, cudaMalloc(&h->s1_scratch,
+                     pre_bytes + 3 * LI * SWFD_SOLVE1D_WSTRIDE * sizeof(unsigned long long) +
+                         LI * sizeof(unsigned)));
   Solve1dArgs a;
   for (int k = 0; k < 3; ++k) a.st[k] = h->st[(h->cur + k) % 3];
   a.pre = (double*)h->s1_scratch;
-  a.slots = (Solve1dSlot*)((char*)h->s1_scratch + pre_bytes);
-  a.bar = (unsigned*)(a.slots + 3);
-  a.ready = (unsigned*)(a.slots + 4);
+  a.red = (unsigned long long*)((char*)h->s1_scratch + pre_bytes);
+  a.ready = (unsigned*)(a.red + 3 * LI * SWFD_SOLVE1D_WSTRIDE);
   a.cells = sh.cells;
   a.sweeps = h->cfg.use_limiter == 2;
   int64_t done = 0;

@@ -26,6 +26,18 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+// after relaxed loads that observed release stores: acquire what they published
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
 // barrier `id` (1..15) of the block's first `nthreads` threads (a multiple of 32)
 __device__ __forceinline__ void bar_named(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
@@ -65,25 +77,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* cnt, unsigned k, int* err
     ok = good;
   }
   __syncthreads();
-  return ok != 0;
-}
-
-// The same barrier for the block's first `nthreads` threads only (named
-// barrier `id`): the block's other warps go on with work no other block
-// waits for at this barrier.
-__device__ __forceinline__ bool grid_barrier_part(unsigned* cnt, unsigned k, int* err,
-                                                  unsigned long long wait_ns, int id,
-                                                  int nthreads) {
-  __shared__ int ok;
-  bar_named(id, nthreads);
-  if (threadIdx.x == 0) {
-    __threadfence();
-    red_release_add_u32(cnt, 1u);
-    const int good = wait_flag(cnt, k * gridDim.x, err, wait_ns) ? 1 : 0;
-    __threadfence();
-    ok = good;
-  }
-  bar_named(id, nthreads);
   return ok != 0;
 }
 

@@ -248,23 +248,23 @@ namespace swfd {
 #define SWFD_SOLVE1D_MAX_BLOCK 512
 #define SWFD_SOLVE1D_MIN_CELLS 6
 #define SWFD_SOLVE1D_MAX_CELLS 62
-struct Solve1dSlot {         // a stage's grid reduction (three rotate)
-  unsigned long long abits;  // maximum findalpha term (bits of a value >= 0)
-  int bad;                   // some cell failed checkpositivity
-  int pad;
-};
 // per cell and stage parity: fflux (3 doubles) and the eigenvectors (15)
 #define SWFD_SOLVE1D_PRE 18
+// grid reductions: three sets of one word per block, each word on a
+// 128-byte line of its own (the launcher fills them with ones); a block
+// polls at most SWFD_SOLVE1D_POLL words per thread
+#define SWFD_SOLVE1D_POLL 4
+#define SWFD_SOLVE1D_WSTRIDE 16
 struct Solve1dArgs {
-  double* st[3];       // X (the step's start and u0), Y, Z
-  double* pre;         // 2 x LI x SWFD_SOLVE1D_PRE
-  Solve1dSlot* slots;  // 3, zeroed by the launcher
-  unsigned* bar;       // grid-barrier counter (zeroed by the launcher)
-  unsigned* ready;     // per block: the epoch of its published terms (zeroed by the launcher)
-  int cells;           // cells per block
-  int resume;          // 1: stage 1; 2, 3: that stage after the previous stage's
-                       // sweep; 4: the time advance after a stage-3 sweep
-  int sweeps;          // use_limiter == 2: a failed checkpositivity pauses for sweep_lim
+  double* st[3];            // X (the step's start and u0), Y, Z
+  double* pre;              // 2 x LI x SWFD_SOLVE1D_PRE
+  unsigned long long* red;  // 3 x grid x SWFD_SOLVE1D_WSTRIDE: a block's maximum alpha bits
+                            // and positivity flag
+  unsigned* ready;          // per block: the epoch of its published terms (zeroed by the launcher)
+  int cells;                // cells per block
+  int resume;               // 1: stage 1; 2, 3: that stage after the previous stage's
+                            // sweep; 4: the time advance after a stage-3 sweep
+  int sweeps;               // use_limiter == 2: a failed checkpositivity pauses for sweep_lim
 };
 struct Solve1dShape {
   int grid, block, cells;

@@ -5,16 +5,18 @@
 // graph kernels per stage (findalpha, splitting, fluxes, RK stage) its time
 // is the kernels' launch and drain latencies.  Here a cooperative grid of
 // one block per SM runs the whole time loop.  Each block owns a contiguous
-// range of cells.  Per stage it splits its range plus a three-cell halo in
-// shared memory (dividing the stored fflux of each cell by the new
-// alphamax), forms the interface fluxes of its range plus one on each side
-// (reading the stored eigenvectors), and the RK stage of its own cells;
-// then, on four warps side by side, checkpositivity and the next findalpha
-// term (folded into the grid reduction, then the grid barrier) and the
-// eigenvectors and fflux of its cells' new state (stored for the next stage,
-// published to the neighbours by the block's ready flag).  A stage whose
-// state fails checkpositivity ends the launch: the host runs sweep_lim on
-// it and launches again at the next stage.
+// range of cells and keeps everything a stage reads in shared memory: the
+// state and fflux of its range plus a three-cell halo, and the eigenvectors
+// of its flux cells.  Per stage it splits (dividing the fflux by the new
+// alphamax), forms the interface fluxes of its range plus one on each side,
+// and the RK stage of its own cells; then, on four warps side by side,
+// checkpositivity and the next findalpha term (posted to the grid reduction)
+// beside the eigenvectors and fflux of its cells' new state (kept for the
+// block itself and stored in global memory for its neighbours, who are told
+// by the block's ready flag); those two warps then wait for the neighbours'
+// flags and copy the next stage's halo into shared memory.  A stage whose
+// state fails checkpositivity ends the launch: the host runs sweep_lim on it
+// and launches again at the next stage.
 //
 // Every value is computed by the separate kernels' code (swfd_1d.cuh).
 #include "swfd_1d.cuh"
@@ -23,8 +25,8 @@
 namespace swfd {
 namespace {
 
-// a grid barrier gives up after 2 s of waiting (the slowest legitimate wait
-// is one stage of the other blocks, microseconds)
+// a wait gives up after 2 s (the slowest legitimate wait is one stage of
+// the other blocks, microseconds)
 constexpr unsigned long long S1_WAIT_NS = 2000000000ull;
 
 // an interface's eigenvectors (S1_EIG values, `stride` apart)
@@ -45,105 +47,110 @@ __device__ __forceinline__ void s1_eig_load(Eigen1D<double>& E, const double* s,
   for (int k = 0; k < 9; ++k) E.L[k / 3][k % 3] = s[(6 + k) * stride + j];
 }
 
-// maximum over the block (values >= 0) and the OR of the flags, in every thread
-__device__ __forceinline__ void s1_block_reduce(double& v, int& f) {
-  __shared__ double wm[32];
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) wm[w] = v;
-  f = __syncthreads_or(f);
-  v = 0.0;
-  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v = fmax(v, wm[k]);
-  __syncthreads();  // wm is rewritten by the next call
-}
-
-// Grid barrier k with the grid's maximum alpha and positivity flag: every
-// block folds its maximum (alpha >= 0, so the bit patterns order as the
-// values do) and flag into slot k % 3 before it arrives; after the barrier
-// every block reads the slot.  Block 0 clears slot (k + 2) % 3 -- read by
-// every block before it arrived at barrier k, next filled after barrier
-// k + 1.  Returns false when the barrier's wait ran out.
-__device__ __forceinline__ bool s1_sync_reduce(const Solve1dArgs& a, unsigned k, int* err,
-                                               double v, int f, double& am, int& bad) {
-  __shared__ double sa;
-  __shared__ int sb;
-  Solve1dSlot* sl = a.slots + k % 3;
-  if (threadIdx.x == 0) {
-    atomicMax(&sl->abits, (unsigned long long)__double_as_longlong(v));
-    if (f) atomicOr(&sl->bad, 1);
-  }
-  if (!grid_barrier(a.bar, k, err, S1_WAIT_NS)) return false;
-  if (threadIdx.x == 0) {
-    sa = __longlong_as_double((long long)*(volatile unsigned long long*)&sl->abits);
-    sb = *(volatile int*)&sl->bad;
-    if (blockIdx.x == 0) {
-      Solve1dSlot* old = a.slots + (k + 2) % 3;
-      old->abits = 0;
-      old->bad = 0;
-    }
-  }
-  __syncthreads();
-  am = sa;
-  bad = sb;
-  __syncthreads();  // sa, sb are rewritten by the next call
-  return true;
-}
-
-// The same on the block's first two warps only (named barrier 1): their
-// maximum v and flag f go to slot k % 3, the grid barrier passes, and
-// *am, *bad (shared) receive the grid's values.  Returns false when the
-// barrier's wait ran out.
-__device__ __forceinline__ bool s1_sync_reduce_2w(const Solve1dArgs& a, unsigned k, int* err,
-                                                  double v, int f, double* am, int* bad) {
-  __shared__ double wv[2];
-  __shared__ int wf[2];
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  f = __any_sync(0xffffffffu, f);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) wv[w] = v, wf[w] = f;
-  bar_named(1, 64);
-  Solve1dSlot* sl = a.slots + k % 3;
-  if (threadIdx.x == 0) {
-    atomicMax(&sl->abits, (unsigned long long)__double_as_longlong(fmax(wv[0], wv[1])));
-    if (wf[0] | wf[1]) atomicOr(&sl->bad, 1);
-  }
-  if (!grid_barrier_part(a.bar, k, err, S1_WAIT_NS, 1, 64)) return false;
-  if (threadIdx.x == 0) {
-    *am = __longlong_as_double((long long)*(volatile unsigned long long*)&sl->abits);
-    *bad = *(volatile int*)&sl->bad;
-    if (blockIdx.x == 0) {
-      Solve1dSlot* old = a.slots + (k + 2) % 3;
-      old->abits = 0;
-      old->bad = 0;
-    }
-  }
-  return true;
-}
-
-// the block's neighbours have published the terms of epoch e (thread 0)
-__device__ __forceinline__ bool s1_wait_neighbours(const Solve1dArgs& a, unsigned e, int* err) {
-  const int b = blockIdx.x;
-  if (b > 0 && !wait_flag(a.ready + b - 1, e, err, S1_WAIT_NS)) return false;
-  if (b + 1 < (int)gridDim.x && !wait_flag(a.ready + b + 1, e, err, S1_WAIT_NS)) return false;
-  return true;
-}
-
 // a cell's precomputed terms: fflux (3 doubles) and the eigenvectors
 constexpr int S1_PRE = 3 + S1_EIG;
 static_assert(S1_PRE == SWFD_SOLVE1D_PRE, "the scratch's per-cell terms");
 
+// A reduction word: the bits of the block's maximum findalpha term (a value
+// >= 0, so the bit patterns order as the values do and the sign bit is free)
+// with the sign bit set when one of its cells failed checkpositivity.
+// S1_EMPTY (all ones, a negative NaN) is never a word.
+constexpr unsigned long long S1_BAD = 1ull << 63;
+constexpr unsigned long long S1_EMPTY = ~0ull;
+
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+
+// Grid reduction k (1, 2, ...) on the block's first two warps: the maximum
+// alpha bits `ab` and flag `f` of the lanes fold into the block's word,
+// which thread 0 posts in set k % 3 (a relaxed store; the caller's thread 0
+// issued a gpu-scope fence after its last store -- the emptying of its word
+// at reduction k - 1 -- while warp 1 computed findalpha, so fence and store
+// form a release); then the 64 threads poll the
+// grid's words of set k % 3 until none is empty, and *am, *bad (shared)
+// receive the grid's maximum and flag.  The words are the only values read
+// from other blocks, so the polls need no acquire fence (a gpu-scope fence
+// here measured ~3 us).  Thread 0 then empties its word of set (k + 2) % 3
+// for reduction k + 2: every block has posted reduction k, after reading
+// every word of reduction k - 1 (set (k + 2) % 3), and the emptying store
+// follows the polls that saw those posts; a block polls that set again only
+// after it has seen this block's word of reduction k + 1, released after
+// the emptying.  Returns false when the wait ran out (ERR_BIT_TIMEOUT in
+// *err).
+__device__ __forceinline__ bool s1_reduce_2w(const Solve1dArgs& a, unsigned k, int* err,
+                                             unsigned long long ab, int f, double* am,
+                                             int* bad) {
+  __shared__ unsigned long long wv[2];
+  __shared__ int wf[2], wok[2];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int G = gridDim.x;
+  for (int o = 16; o > 0; o >>= 1) ab = umax64(ab, __shfl_xor_sync(0xffffffffu, ab, o));
+  f = __any_sync(0xffffffffu, f);
+  if (lane == 0) wv[w] = ab, wf[w] = f;
+  bar_named(1, 64);
+  // word j of set k % 3 at set + j * W, a 128-byte line of its own: the
+  // grid's polls of one word go to one line, not the whole set's to a few
+  constexpr int W = SWFD_SOLVE1D_WSTRIDE;
+  unsigned long long* set = a.red + (size_t)(k % 3) * G * W;
+  if (tid == 0)
+    st_relaxed_u64(set + (size_t)blockIdx.x * W,
+                   umax64(wv[0], wv[1]) | ((wf[0] | wf[1]) ? S1_BAD : 0ull));
+  // thread tid polls words tid, tid + 64, ... (at most SWFD_SOLVE1D_POLL),
+  // all of them in each round
+  unsigned long long m = 0;
+  int fl = 0, pend = 0, ok = 1;
+#pragma unroll
+  for (int s = 0; s < SWFD_SOLVE1D_POLL; ++s)
+    if (tid + 64 * s < G) pend |= 1 << s;
+  const unsigned long long t0 = global_ns();
+  for (long long it = 0; pend; ++it) {
+    unsigned long long v[SWFD_SOLVE1D_POLL];
+#pragma unroll
+    for (int s = 0; s < SWFD_SOLVE1D_POLL; ++s)
+      v[s] = (pend >> s) & 1 ? ld_relaxed_u64(set + (size_t)(tid + 64 * s) * W) : S1_EMPTY;
+#pragma unroll
+    for (int s = 0; s < SWFD_SOLVE1D_POLL; ++s)
+      if (v[s] != S1_EMPTY) {
+        m = umax64(m, v[s] & ~S1_BAD);
+        fl |= (int)(v[s] >> 63);
+        pend &= ~(1 << s);
+      }
+    if (pend && (it & 63) == 63 &&
+        (global_ns() - t0 > S1_WAIT_NS || it > GRID_BARRIER_MAX_POLLS ||
+         (*(volatile int*)err & ERR_BIT_TIMEOUT))) {
+      atomicOr(err, ERR_BIT_TIMEOUT);
+      ok = 0;
+      break;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = umax64(m, __shfl_xor_sync(0xffffffffu, m, o));
+  fl = __any_sync(0xffffffffu, fl);
+  ok = __all_sync(0xffffffffu, ok);
+  bar_named(1, 64);  // thread 0 has read wv, wf
+  if (lane == 0) wv[w] = m, wf[w] = fl, wok[w] = ok;
+  bar_named(1, 64);
+  const bool good = wok[0] && wok[1];
+  if (tid == 0) {
+    *am = __longlong_as_double((long long)umax64(wv[0], wv[1]));
+    *bad = wf[0] | wf[1];
+    if (good)
+      st_relaxed_u64(a.red + ((size_t)((k + 2) % 3) * G + blockIdx.x) * W, S1_EMPTY);
+  }
+  return good;
+}
+
 // The state buffers: st[0] = X (the step's start, u0, written back by stage
 // 3), st[1] = Y, st[2] = Z; stage k reads st[k-1] and writes st[k % 3]
-// (the rotation of the separate kernels' step).  The buffers change during
-// the launch, so they are read with coherent loads.
+// (the rotation of the separate kernels' step).
 //
 // A GB300 SM sub-partition retires one warp-wide FP64 instruction per ~64
 // cycles whatever the warp's active lanes, so a stage's time is the FP64
-// instruction count of the warps on its critical path.  Each stage ends with
-// the block's four warps side by side: checkpositivity, the next findalpha
-// term, the eigenvectors and fflux of its cells' new state (stored for the
-// next stage's split and fluxes, its own and its neighbours'); after the
-// barrier only the division by the new alphamax is left of the splitting.
+// instruction count of the warps on its critical path plus the latency of
+// its memory round trips.  Between two grid reductions a block reads global
+// memory only for the halo (after the neighbours' flags, beside the grid
+// reduction) and for u0 after a resume; the interface fluxes run on all
+// four sub-partitions (two lanes per reconstruction).
 __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
     k_solve1d(Params p, Solve1dArgs a, DevScalars* dsc, double t_loop) {
   extern __shared__ double sm[];
@@ -151,116 +158,188 @@ __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
   const int n = g.nx, LI = g.LI;
   const int64_t P = g.plane;
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int G = gridDim.x;
   // owned cells [a0, a1) (offsets: cell i at i + 2), interface-flux cells
   // [f0, f1] within 2..n+3 (the reference's m = 0..n+1), split cells
-  // [f0 - 2, f1 + 2]
+  // [s0, f1 + 2] = [f0 - 2, f1 + 2], of which [s0, a0) and [a1, f1 + 2]
+  // are the halo
   const int a0 = b * a.cells, a1 = min(LI, a0 + a.cells), nown = a1 - a0;
   const int f0 = max(a0 - 1, 2), f1 = min(a1, n + 3);
   const int nf = f1 - f0 + 1, s0 = f0 - 2, ns = nf + 4;
+  const int nhl = a0 - s0, nhr = max(0, f1 + 3 - a1);
   const int SW = a.cells + 6, FW = a.cells + 2;
-  double* ssp = sm;            // split: fp 0..2, fn 3..5, 6 x SW
-  double* sfl = ssp + 6 * SW;  // interface fluxes: hp 0..2, hn 3..5, 6 x FW
-  double* sev = sfl + 6 * FW;  // eigenvectors of the flux cells, S1_EIG x FW
-  double* snew = sev + S1_EIG * FW;  // the stage's new state of the owned cells, 3 x cells
-  // the split runs on threads [0, ns), the eigenvector copies on the warps
-  // after them, threads [ev0, ev0 + nf)
-  const int ev0 = (ns + 31) & ~31;
-  const double* u0 = a.st[0];
+  double* sst = sm;                 // state of the split cells, 3 x SW
+  double* sff = sst + 3 * SW;       // their fflux, 3 x SW (right after sst)
+  double* ssp = sff + 3 * SW;       // split: fp 0..2, fn 3..5, 6 x SW
+  double* sfl = ssp + 6 * SW;       // interface fluxes: hp 0..2, hn 3..5, 6 x FW
+  double* sev = sfl + 6 * FW;       // eigenvectors of the flux cells, S1_EIG x FW
+  double* su0 = sev + S1_EIG * FW;  // u0 of the owned cells, 3 x cells
+  __shared__ double s_am;
+  __shared__ int s_tag, s_ok, s_nok[2];
   const bool sweeps = a.sweeps != 0;
 
-  double time = dsc->time, dt = dsc->dt, am = 0.0, am_next = 0.0;
+  double time = dsc->time, dt = dsc->dt, am = 0.0;
   long long steps = dsc->steps;
   const long long lim = dsc->steps_limit;
-  int err = 0, pause = 0, pb = 0;
-  unsigned nbar = 0, epoch = 0;  // grid barriers passed; terms published
-  bool have_pre = false;
+  int err = 0, pause = 0, pw = 0;
+  unsigned nred = 0, epoch = 0;  // grid reductions passed; terms published
+  bool after = false;            // the terms follow a stage (else the launch's start)
+  bool u0_ok = false;            // su0 holds u0 (a stage 1 ran in this launch)
   int stage = a.resume;
   if (stage == 4) {  // the step whose stage-3 sweep the host ran: time = time + dt (:44)
     time = time + dt;
     ++steps;
     stage = 1;
   }
+  // the launch starts from the state stage `stage` reads: its owned cells
+  const double* src = a.st[stage - 1];
+  for (int w = tid; w < 3 * nown; w += blockDim.x) {
+    const int c = w / nown, t = w - c * nown;
+    sst[c * SW + a0 + t - s0] = src[c * P + a0 + t];
+  }
+  __syncthreads();
   for (;;) {
-    // DO WHILE (time <= time_terminal - 1d-10), within the launch's step bound
-    if (stage == 1 && !(time <= t_loop && steps < lim && err == 0)) break;
-    const double* in = a.st[stage - 1];
-    double* out = a.st[stage % 3];
-    if (!have_pre) {
-      // findalpha (:273-285), eigenvectors and fflux of the owned cells of
-      // the stage's input, on three warps
-      double v = 0.0;
+    // ---- the terms of the state in sst (owned cells; src in global memory)
+    // for the next stage: warps 0 and 1 checkpositivity (:376-392, after a
+    // stage) and findalpha (:273-285), then the grid reduction; warps 2 and
+    // 3 the eigenvectors (:103-133) and fflux (:57-73), kept and published
+    // to the neighbours (ready flag), then the neighbours' halo
+    ++epoch;
+    ++nred;
+    if (warp < 2) {
+      unsigned long long ab = 0;
+      int bad = 0;
       for (int t = lane; t < nown; t += 32) {
-        const int q = a0 + t;
-        const double u1 = in[q], u2 = in[P + q], u3 = in[2 * P + q];
+        const int q = a0 + t, tt = q - s0;
+        const double n0 = sst[tt], n1 = sst[SW + tt], n2 = sst[2 * SW + tt];
         if (warp == 0) {
-          v = fmax(v, fmax(0.0, alpha1d(p, u1, u2, u3)));
-        } else if (warp == 1 || warp == 2) {
-          double* pre = a.pre + ((int64_t)pb * LI + q) * S1_PRE;
-          if (warp == 1) {
-            Eigen1D<double> E;
-            eigen1d<double>(p.gamma1, u1, u2, u3, E);
-            s1_eig_store(E, pre + 3, 1, 0);
-          } else {
-            double f[3];
-            fflux1d(p, u1, u2, u3, f);
-            for (int c = 0; c < 3; ++c) pre[c] = f[c];
-          }
+          if (after && q - 2 >= 1 && q - 2 <= n) bad |= pos1d_bad<double>(p, n0, n1, n2);
+        } else {
+          const double al = fmax(0.0, alpha1d(p, n0, n1, n2));
+          ab = umax64(ab, (unsigned long long)__double_as_longlong(al) & ~S1_BAD);
         }
       }
-      int unused = 0;
-      s1_block_reduce(v, unused);  // (a block barrier: the terms are stored)
-      ++epoch;
-      if (tid == 0) {
-        __threadfence();
-        st_release_u32(a.ready + b, epoch);
+      // the release half of thread 0's post (see s1_reduce_2w), beside warp 1's findalpha
+      if (tid == 0) fence_acq_rel_gpu();
+      const bool ok = s1_reduce_2w(a, nred, &dsc->error, ab, bad, &s_am, &s_tag);
+      if (tid == 0) s_ok = ok ? 1 : 0;
+    } else if (warp < 4) {
+      double* prew = a.pre + (int64_t)pw * LI * S1_PRE;
+      for (int t = lane; t < nown; t += 32) {
+        const int q = a0 + t, tt = q - s0;
+        const double n0 = sst[tt], n1 = sst[SW + tt], n2 = sst[2 * SW + tt];
+        double* pq = prew + (int64_t)q * S1_PRE;
+        if (warp == 2) {
+          Eigen1D<double> E;
+          eigen1d<double>(p.gamma1, n0, n1, n2, E);
+          s1_eig_store(E, pq + 3, 1, 0);
+          if (q >= f0 && q <= f1) s1_eig_store(E, sev, FW, q - f0);
+        } else {
+          double f[3];
+          fflux1d(p, n0, n1, n2, f);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) pq[c] = f[c], sff[c * SW + tt] = f[c];
+        }
       }
-      if (!s1_sync_reduce(a, ++nbar, &dsc->error, v, 0, am, unused)) return;
-    } else {
-      am = am_next;
+      bar_named(2, 64);
+      // the release store orders the block's stores of the state (before
+      // the block barrier after the RK stage) and of the terms (before the
+      // named barrier) before the flag
+      if (tid == 64) st_release_u32(a.ready + b, epoch);
+      if (tid == 64 || tid == 96) {  // the left and the right neighbour, side by side
+        const int nb = tid == 64 ? b - 1 : b + 1;
+        int okn = 1;
+        if (nb >= 0 && nb < G) okn = wait_flag(a.ready + nb, epoch, &dsc->error, S1_WAIT_NS);
+        s_nok[tid == 96] = okn;
+      }
+      bar_named(2, 64);
+      if (s_nok[0] && s_nok[1]) {
+        // the halo, all loads first: thread 64 + t2 takes value t2 of the
+        // halo cells' state (from src) and fflux (six per cell), and value
+        // 63 - t2 of the eigenvectors of the flux cells next to the range
+        // (f0 below a0: 0..14, f1 at a1: 15..29)
+        const int t2 = tid - 64;
+        const bool hasA = t2 < 6 * (nhl + nhr);
+        const int eB = 63 - t2;
+        const bool right = eB >= S1_EIG;
+        const int qB = right ? f1 : f0, kB = eB - (right ? S1_EIG : 0);
+        const bool hasB = eB < 2 * S1_EIG && (right ? f1 >= a1 : f0 < a0);
+        double vA = 0.0, vB = 0.0;
+        int dA = 0;
+        if (hasA) {
+          const int ci = t2 / 6, comp = t2 - 6 * ci;
+          const int q = ci < nhl ? s0 + ci : a1 + (ci - nhl);
+          dA = comp * SW + q - s0;  // comp 3..5 land in sff
+          vA = comp < 3 ? __ldcg(src + comp * P + q)
+                        : __ldcg(prew + (int64_t)q * S1_PRE + (comp - 3));
+        }
+        if (hasB) vB = __ldcg(prew + (int64_t)qB * S1_PRE + 3 + kB);
+        if (hasA) sst[dA] = vA;
+        if (hasB) sev[kB * FW + qB - f0] = vB;
+      }
     }
-    {  // the neighbours' terms of this stage (their ready flags)
-      __shared__ int nok;
-      if (tid == 0) nok = s1_wait_neighbours(a, epoch, &dsc->error) ? 1 : 0;
-      __syncthreads();
-      if (!nok) return;
+    __syncthreads();
+    if (!s_ok || !s_nok[0] || !s_nok[1]) return;
+    const double am_next = s_am;
+    const int postag = s_tag;
+    pw ^= 1;
+    if (after) {
+      if (tid == 0 && b == 0) dsc->rk_runs[stage]++;
+      if (postag && sweeps) {  // sweep_lim runs on the host's launches
+        pause = stage;
+        break;
+      }
+      if (stage == 3) {  // time = time + dt (:44)
+        time = time + dt;
+        ++steps;
+        stage = 1;
+      } else {
+        ++stage;
+      }
     }
+    // ---- stage `stage`: DO WHILE (time <= time_terminal - 1d-10), within
+    // the launch's step bound
+    if (stage == 1 && !(time <= t_loop && steps < lim && err == 0)) break;
+    am = am_next;
+    double* out = a.st[stage % 3];
     if (!isfinite(am) || !(am > 0.0)) err |= ERR_BIT_ALPHA;
     if (stage == 1) {  // dt = dx*cfl/alphamax (:293)
       dt = p.dt_num_x / am;
       if (!isfinite(dt)) err |= ERR_BIT_DT;
     }
-    const double* pre = a.pre + (int64_t)pb * LI * S1_PRE;
-    if (tid < ns) {  // the split (:82-85) of cells s0 .. s0 + ns - 1 from their fflux
-      const int q = s0 + tid;
-      const double u[3] = {in[q], in[P + q], in[2 * P + q]};
-      const double* pq = pre + (int64_t)q * S1_PRE;
-      const double f[3] = {pq[0], pq[1], pq[2]};
-      double sp[3], sn[3];
-      split1d_f<double>(u, f, am, sp, sn);
-      for (int c = 0; c < 3; ++c) ssp[c * SW + tid] = sp[c], ssp[(3 + c) * SW + tid] = sn[c];
-    } else if (tid >= ev0 && tid < ev0 + nf) {  // the flux cells' eigenvectors (:103-133)
-      const int j = tid - ev0;
-      const double* pq = pre + (int64_t)(f0 + j) * S1_PRE + 3;
-      for (int k = 0; k < S1_EIG; ++k) sev[k * FW + j] = pq[k];
+    {  // the split (:82-85) of cells s0 .. s0 + ns - 1 from their fflux, one
+       // component per warp (ns <= 32) or group of warps
+      const int nsr = (ns + 31) & ~31;
+      for (int w = tid; w < 3 * nsr; w += blockDim.x) {
+        const int c = w / nsr, t = w - c * nsr;
+        if (t < ns) {
+          double sp, sn;
+          split1d_one(sst[c * SW + t], sff[c * SW + t], am, sp, sn);
+          ssp[c * SW + t] = sp;
+          ssp[(3 + c) * SW + t] = sn;
+        }
+      }
     }
     __syncthreads();
-    {  // interface fluxes (:88-157), eight lanes per flux cell f0 + j
-      const int j = tid >> 3, sub = tid & 7;
+    // interface fluxes (:88-157), sixteen lanes per flux cell f0 + j
+    for (int jb = 0; jb < nf; jb += (int)(blockDim.x >> 4)) {
+      const int j = jb + (tid >> 4), sub = tid & 15;
       const int jc = j < nf ? j : max(nf - 1, 0);  // lanes past the range repeat the last cell
       Eigen1D<double> E;
       s1_eig_load(E, sev, FW, jc);
-      const double v = recon1d<double, false>(
+      const double v = recon1d_pair(
           p, E, sub, [&](int side, int c, int jj) { return ssp[(3 * side + c) * SW + jc + jj]; });
-      const double r = back1d<double>(E, v, sub);
+      const double r = back1d<double, 16>(E, v, sub);
       if (!p.limiter) {
         if (j < nf && sub < 6) sfl[sub * FW + j] = r;
       } else {  // use_limiter 1 (:159-245): lanes 0 and 3 limit their side
         double w[3];
         int nd = 0, np = 0;
-        const bool lim = limit1d_group<double>(
+        const bool lim1 = limit1d_group<double, 16>(
             p, r, sub, [&](int side, int c) { return ssp[(3 * side + c) * SW + jc + 2]; }, w, nd,
             np);
-        if (j < nf && lim) {
+        if (j < nf && lim1) {
+#pragma unroll
           for (int c = 0; c < 3; ++c) sfl[(sub + c) * FW + j] = w[c];
           // a flux cell next to the range is also the neighbour block's:
           // the block that owns the cell counts its limitings
@@ -271,86 +350,31 @@ __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
     }
     __syncthreads();
     {  // scheme (:252-271) and the RK stage of the owned cells, four lanes per
-       // cell (lane c < 3: component c)
+       // cell (lane c < 3: component c); the new state replaces the stage's
+       // input in sst (each value read and written by one thread)
       const int cell = tid >> 2, c = tid & 3, q = a0 + cell;
       const int i = q - 2;
       if (cell < nown && c < 3) {
+        const int tt = q - s0;
+        const double uin = sst[c * SW + tt];
         double r = 0.0;
         if (i >= 1 && i <= n) {
           const int k = q - f0;
           r = rhs1d_value<double>(p, am, sfl[c * FW + k - 1], sfl[(3 + c) * FW + k],
                                   sfl[c * FW + k], sfl[(3 + c) * FW + k + 1]);
         }
-        const double v = rk1d_value<double>(p, stage, dt, r, in[c * P + q], u0 + c * P + q);
+        const double u0v =
+            stage == 1 ? uin : u0_ok ? su0[c * a.cells + cell] : a.st[0][c * P + q];
+        const double v = rk1d_value<double>(p, stage, dt, r, uin, &u0v);
         out[c * P + q] = v;
-        snew[c * a.cells + cell] = v;
+        sst[c * SW + tt] = v;
+        if (stage == 1) su0[c * a.cells + cell] = uin;
       }
     }
+    if (stage == 1) u0_ok = true;
     __syncthreads();
-    // the new state of the owned cells: warps 0 and 1 checkpositivity
-    // (:376-392) and the next findalpha term, then the grid barrier that
-    // reduces them; warps 2 and 3 meanwhile the eigenvectors and fflux the
-    // next stage splits and reconstructs from, published to the neighbours
-    // by the block's ready flag (epoch)
-    __shared__ double s_am;
-    __shared__ int s_tag, s_ok;
-    ++epoch;
-    if (warp < 2) {
-      double av = 0.0;
-      int bad = 0;
-      for (int t = lane; t < nown; t += 32) {
-        const double n0 = snew[t], n1 = snew[a.cells + t], n2 = snew[2 * a.cells + t];
-        const int q = a0 + t;
-        if (warp == 0) {
-          if (q - 2 >= 1 && q - 2 <= n) bad |= pos1d_bad<double>(p, n0, n1, n2);
-        } else {
-          av = fmax(av, fmax(0.0, alpha1d(p, n0, n1, n2)));
-        }
-      }
-      const bool ok = s1_sync_reduce_2w(a, ++nbar, &dsc->error, av, bad, &s_am, &s_tag);
-      if (tid == 0) s_ok = ok ? 1 : 0;
-    } else {
-      ++nbar;  // the block's grid-barrier count, as warps 0 and 1 keep it
-      if (warp < 4) {
-        for (int t = lane; t < nown; t += 32) {
-          const double n0 = snew[t], n1 = snew[a.cells + t], n2 = snew[2 * a.cells + t];
-          double* pq = a.pre + ((int64_t)(pb ^ 1) * LI + a0 + t) * S1_PRE;
-          if (warp == 2) {
-            Eigen1D<double> E;
-            eigen1d<double>(p.gamma1, n0, n1, n2, E);
-            s1_eig_store(E, pq + 3, 1, 0);
-          } else {
-            double f[3];
-            fflux1d(p, n0, n1, n2, f);
-            for (int c = 0; c < 3; ++c) pq[c] = f[c];
-          }
-        }
-        bar_named(2, 64);
-        if (tid == 64) {
-          __threadfence();
-          st_release_u32(a.ready + b, epoch);
-        }
-      }
-    }
-    if (tid == 0 && b == 0) dsc->rk_runs[stage]++;
-    __syncthreads();
-    if (!s_ok) return;
-    am_next = s_am;
-    const int postag = s_tag;
-    __syncthreads();  // s_am, s_tag, s_ok are rewritten by the next stage
-    pb ^= 1;
-    have_pre = true;
-    if (postag && sweeps) {  // sweep_lim runs on the host's launches
-      pause = stage;
-      break;
-    }
-    if (stage == 3) {  // time = time + dt (:44)
-      time = time + dt;
-      ++steps;
-      stage = 1;
-    } else {
-      ++stage;
-    }
+    src = out;
+    after = true;
   }
   if (b == 0 && tid == 0) {
     dsc->time = time;
@@ -375,13 +399,16 @@ bool solve1d_shape(const Params& p, Solve1dShape* sh) {
   int cells = std::max(SWFD_SOLVE1D_MIN_CELLS, (LI + sms - 1) / sms);
   if (const char* env = getenv("SWFD_SOLVE1D_CELLS")) cells = std::max(cells, atoi(env));
   if (cells > SWFD_SOLVE1D_MAX_CELLS) return false;
-  // eight lanes per flux cell (cells + 2 of them), and at least the four
-  // warps of a stage's last phase
-  const int block = std::max(128, (8 * (cells + 2) + 31) / 32 * 32);
+  // sixteen lanes per flux cell (cells + 2 of them; more take turns), four
+  // per owned cell in the RK stage, and at least the four warps of the
+  // terms of a stage
+  const int block =
+      std::min(SWFD_SOLVE1D_MAX_BLOCK, std::max(128, (16 * (cells + 2) + 31) / 32 * 32));
   sh->cells = cells;
   sh->block = block;
   sh->grid = (LI + cells - 1) / cells;
-  sh->smem = (size_t)(6 * (cells + 6) + (6 + S1_EIG) * (cells + 2) + 3 * cells) * sizeof(double);
+  if (sh->grid > 64 * SWFD_SOLVE1D_POLL || 4 * cells > block) return false;
+  sh->smem = (size_t)(12 * (cells + 6) + (6 + S1_EIG) * (cells + 2) + 3 * cells) * sizeof(double);
   int per = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve1d, block, sh->smem) !=
           cudaSuccess ||
@@ -392,8 +419,9 @@ bool solve1d_shape(const Params& p, Solve1dShape* sh) {
 
 cudaError_t launch_solve1d(const Params& p, const Solve1dShape& sh, const Solve1dArgs& a,
                            DevScalars* dsc, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(a.slots, 0, 3 * sizeof(Solve1dSlot), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(a.bar, 0, sizeof(unsigned), s);
+  // the reduction words empty (all ones), the ready flags zero
+  cudaError_t e = cudaMemsetAsync(
+      a.red, 0xff, 3 * (size_t)sh.grid * SWFD_SOLVE1D_WSTRIDE * sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.ready, 0, sh.grid * sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   Params pp = p;
