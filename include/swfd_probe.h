@@ -36,6 +36,17 @@ swfd_status swfd_probe_convert(int32_t device, const double* x, int64_t n, float
 swfd_status swfd_probe_barrier_timeout(int32_t device, int32_t absent, double wait_ms,
                                        int32_t* err_bits, int32_t* passed);
 
+/* Two blocks of a cooperative launch at one grid reduction of the
+ * persistent 1D solve (per-block words polled by every block; block b posts
+ * the value b + 1, block 0 a failed-positivity flag), the second absent
+ * when `absent` is set.  The polls must end after wait_ms (0 < wait_ms <=
+ * 2000) with the timeout bit (64) in *err_bits, without a fault; *passed
+ * counts the blocks whose reduction completed and am_max[b], bad_flag[b]
+ * (two entries each) hold what block b received. */
+swfd_status swfd_probe_reduce_timeout(int32_t device, int32_t absent, double wait_ms,
+                                      int32_t* err_bits, int32_t* passed, double* am_max,
+                                      int32_t* bad_flag);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,7 +2,9 @@
 // is bounded by the FP64 pipe, whose peak is not a published constant of
 // this part; this kernel measures it (independent DFMA chains, 8 per thread).
 // Also test entry points: the FP32-bulk reciprocal and conversions, and the
-// persistent kernels' bounded grid barrier.
+// persistent kernels' bounded grid barrier and grid reduction.
+#include <string.h>
+
 #include "swfd_internal.h"
 #include "swfd_device.cuh"
 #include "swfd_gridsync.cuh"
@@ -44,7 +46,75 @@ __global__ void k_barrier_probe(unsigned* cnt, int* err, int* passed, int absent
   const bool ok = swfd::grid_barrier(cnt, 1, err, wait_ns);
   if (threadIdx.x == 0 && ok) atomicAdd(passed, 1);
 }
+// two blocks at one reduction of the persistent 1D solve (block b posts the
+// value b + 1, block 0 the flag); with `absent` the second block returns
+// without posting, so the first one's polls run out
+__global__ void k_reduce_probe(unsigned long long* red, int* err, int* passed, double* am_out,
+                               int* bad_out, int absent, unsigned long long wait_ns) {
+  __shared__ double am;
+  __shared__ int bad;
+  if (absent && blockIdx.x == 1) return;
+  const double v = threadIdx.x == 0 ? (double)(blockIdx.x + 1) : 0.0;
+  const int f = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool ok = swfd::grid_reduce_2w(red, 1, err, wait_ns,
+                                       (unsigned long long)__double_as_longlong(v), f, &am, &bad);
+  if (threadIdx.x == 0 && ok) {
+    atomicAdd(passed, 1);
+    am_out[blockIdx.x] = am;
+    bad_out[blockIdx.x] = bad;
+  }
+}
 }  // namespace
+
+// The persistent 1D solve's grid reduction with one block absent (or,
+// absent = 0, both present): the polls of the other block must end after
+// wait_ms with ERR_BIT_TIMEOUT in *err_bits and the context stay usable;
+// *passed counts the blocks whose reduction completed, am_max[b] and
+// bad_flag[b] (two each) what block b received.
+extern "C" swfd_status swfd_probe_reduce_timeout(int32_t device, int32_t absent, double wait_ms,
+                                                 int32_t* err_bits, int32_t* passed,
+                                                 double* am_max, int32_t* bad_flag) {
+  if (!err_bits || !passed || !am_max || !bad_flag || !(wait_ms > 0.0) || wait_ms > 2000.0)
+    return SWFD_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return SWFD_ERR_CUDA;
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) return SWFD_ERR_UNSUPPORTED;
+  // three sets of two words, SWFD_SOLVE1D_WSTRIDE apart; then err, passed,
+  // the two blocks' results
+  const size_t nred = 3 * 2 * SWFD_SOLVE1D_WSTRIDE;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, (nred + 8) * sizeof(unsigned long long)) != cudaSuccess) return SWFD_ERR_OOM;
+  cudaError_t e = cudaMemset(d, 0xff, nred * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(d + nred, 0, 8 * sizeof(unsigned long long));
+  unsigned long long* red = d;
+  int* err = (int*)(d + nred);
+  int* pass = err + 1;
+  double* am = (double*)(d + nred + 2);
+  int* bad = (int*)(d + nred + 4);
+  int ab = absent ? 1 : 0;
+  unsigned long long ns = (unsigned long long)(wait_ms * 1e6);
+  void* args[] = {&red, &err, &pass, &am, &bad, &ab, &ns};
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((const void*)k_reduce_probe, dim3(2), dim3(64), args, 0,
+                                    nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h, d + nred, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  int hi[4];
+  double hd[2];
+  memcpy(hi, h, sizeof(hi));
+  memcpy(hd, h + 2, sizeof(hd));
+  int hb[2];
+  memcpy(hb, h + 4, sizeof(hb));
+  *err_bits = hi[0];
+  *passed = hi[1];
+  am_max[0] = hd[0], am_max[1] = hd[1];
+  bad_flag[0] = hb[0], bad_flag[1] = hb[1];
+  return e == cudaSuccess ? SWFD_OK : SWFD_ERR_CUDA;
+}
 
 // The persistent kernels' grid barrier with one block absent (or, absent =
 // 0, all present): the wait of the other block must end after wait_ms with
