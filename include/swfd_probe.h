@@ -43,6 +43,13 @@ swfd_status swfd_probe_barrier_timeout(int32_t device, int32_t absent, double wa
  * 2000) with the timeout bit (64) in *err_bits, without a fault; *passed
  * counts the blocks whose reduction completed and am_max[b], bad_flag[b]
  * (two entries each) hold what block b received. */
+/* Host only (no device): the ranges of block b of the persistent 1D solve
+ * for nx cells and `cells` cells per block, from the kernel's own layout
+ * function: out[0..9] = a0, a1, nown (owned cells [a0, a1)), f0, f1, nf
+ * (interface-flux cells [f0, f1]), s0, ns (split cells [s0, s0 + ns)), nhl,
+ * nhr (halo cells below a0 and from a1 up); offsets 0..nx+5, cell i at
+ * i + 2. */
+swfd_status swfd_probe_solve1d_layout(int32_t nx, int32_t cells, int32_t b, int32_t* out);
 swfd_status swfd_probe_reduce_timeout(int32_t device, int32_t absent, double wait_ms,
                                       int32_t* err_bits, int32_t* passed, double* am_max,
                                       int32_t* bad_flag);

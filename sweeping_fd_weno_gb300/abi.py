@@ -166,6 +166,8 @@ _PROBE_SIGS = {
     "swfd_probe_convert": (C.c_int32, [C.c_int32, _DP, C.c_int64, C.POINTER(C.c_float), _DP]),
     "swfd_probe_barrier_timeout": (C.c_int32, [C.c_int32, C.c_int32, C.c_double,
                                               C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "swfd_probe_solve1d_layout": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32,
+                                             C.POINTER(C.c_int32)]),
     "swfd_probe_reduce_timeout": (C.c_int32, [C.c_int32, C.c_int32, C.c_double,
                                              C.POINTER(C.c_int32), C.POINTER(C.c_int32), _DP,
                                              C.POINTER(C.c_int32)]),

@@ -266,6 +266,29 @@ struct Solve1dArgs {
                             // sweep; 4: the time advance after a stage-3 sweep
   int sweeps;               // use_limiter == 2: a failed checkpositivity pauses for sweep_lim
 };
+// A block's ranges in the persistent 1D solve (cells at offsets 0..LI-1,
+// cell i at i + 2): owned cells [a0, a1), interface-flux cells [f0, f1]
+// within 2..nx+3 (the reference's m = 0..nx+1), split cells [s0, s0 + ns) =
+// [f0 - 2, f1 + 2], of which nhl cells below a0 and nhr from a1 up are the
+// halo.  The kernel and its layout probe both call this.
+struct Solve1dLayout {
+  int a0, a1, nown, f0, f1, nf, s0, ns, nhl, nhr;
+};
+__host__ __device__ __forceinline__ Solve1dLayout solve1d_layout(int b, int cells, int LI,
+                                                                 int nx) {
+  Solve1dLayout L;
+  L.a0 = b * cells;
+  L.a1 = min(LI, L.a0 + cells);
+  L.nown = L.a1 - L.a0;
+  L.f0 = max(L.a0 - 1, 2);
+  L.f1 = min(L.a1, nx + 3);
+  L.nf = L.f1 - L.f0 + 1;
+  L.s0 = L.f0 - 2;
+  L.ns = L.nf + 4;
+  L.nhl = L.a0 - L.s0;
+  L.nhr = max(0, L.f1 + 3 - L.a1);
+  return L;
+}
 struct Solve1dShape {
   int grid, block, cells;
   size_t smem;

@@ -116,6 +116,19 @@ extern "C" swfd_status swfd_probe_reduce_timeout(int32_t device, int32_t absent,
   return e == cudaSuccess ? SWFD_OK : SWFD_ERR_CUDA;
 }
 
+// The ranges of block b of the persistent 1D solve for nx cells (LI = nx + 6
+// with the ghosts) and `cells` per block, on the host: the kernel's own
+// layout function, for the in-bounds test of every shape
+extern "C" swfd_status swfd_probe_solve1d_layout(int32_t nx, int32_t cells, int32_t b,
+                                                 int32_t* out) {
+  if (!out || nx < 1 || cells < 1 || b < 0 || b * (int64_t)cells >= (int64_t)nx + 6)
+    return SWFD_ERR_INVALID;
+  const swfd::Solve1dLayout L = swfd::solve1d_layout(b, cells, nx + 6, nx);
+  const int32_t v[10] = {L.a0, L.a1, L.nown, L.f0, L.f1, L.nf, L.s0, L.ns, L.nhl, L.nhr};
+  memcpy(out, v, sizeof(v));
+  return SWFD_OK;
+}
+
 // The persistent kernels' grid barrier with one block absent (or, absent =
 // 0, all present): the wait of the other block must end after wait_ms with
 // ERR_BIT_TIMEOUT in *err_bits and the context stay usable; *passed counts

@@ -70,14 +70,11 @@ __global__ void __launch_bounds__(SWFD_SOLVE1D_MAX_BLOCK)
   const int64_t P = g.plane;
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = gridDim.x;
-  // owned cells [a0, a1) (offsets: cell i at i + 2), interface-flux cells
-  // [f0, f1] within 2..n+3 (the reference's m = 0..n+1), split cells
-  // [s0, f1 + 2] = [f0 - 2, f1 + 2], of which [s0, a0) and [a1, f1 + 2]
-  // are the halo
-  const int a0 = b * a.cells, a1 = min(LI, a0 + a.cells), nown = a1 - a0;
-  const int f0 = max(a0 - 1, 2), f1 = min(a1, n + 3);
-  const int nf = f1 - f0 + 1, s0 = f0 - 2, ns = nf + 4;
-  const int nhl = a0 - s0, nhr = max(0, f1 + 3 - a1);
+  // owned cells [a0, a1), flux cells [f0, f1], split cells [s0, f1 + 2],
+  // of which [s0, a0) and [a1, f1 + 2] are the halo (solve1d_layout)
+  const Solve1dLayout L = solve1d_layout(b, a.cells, LI, n);
+  const int a0 = L.a0, a1 = L.a1, nown = L.nown, f0 = L.f0, f1 = L.f1;
+  const int nf = L.nf, s0 = L.s0, ns = L.ns, nhl = L.nhl, nhr = L.nhr;
   const int SW = a.cells + 6, FW = a.cells + 2;
   double* sst = sm;                 // state of the split cells, 3 x SW
   double* sff = sst + 3 * SW;       // their fflux, 3 x SW (right after sst)
